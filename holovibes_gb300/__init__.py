@@ -1,0 +1,341 @@
+"""holovibes_gb300: GB300-native Holovibes hologram pipeline (sm_103a CUDA behind a C ABI).
+
+Python mirror of the reference's Pipe / compute-step interface over ctypes. The compute runs
+in ``lib/libholovibes_gb300.so``; there is no CPU fallback: every entry point raises when the
+library is missing or a CUDA call fails.
+
+    fd = FrameDescriptor(width=512, height=512, depth=2)
+    s = Settings.defaults(); s.space_transformation = SPACE_ANGULARSP; ...
+    pipe = Pipe(fd, s)
+    pipe.enqueue(frames_uint16)        # BatchInputQueue::enqueue
+    img = pipe.pull()                  # output Queue dequeue (uint16 H x W)
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import _build
+
+# ---------------------------------------------------------------------------------- constants
+HV_OK = 0
+HV_NO_CHANGE = 1
+HV_INVALID_VALUE = 2
+HV_NO_IN_DATA = 3
+HV_NOT_STARTED = 4
+HV_WRONG_COMP_MODE = 5
+HV_WRONG_IMG_TYPE = 6
+HV_FAILURE = 7
+HV_ERR_CUDA = 8
+HV_ERR_OOM = 9
+HV_ERR_TIMEOUT = 10
+HV_ERR_ADMISSION = 11
+HV_ERR_UNSUPPORTED = 12
+STATUS_NAMES = {
+    0: "OK", 1: "NO_CHANGE", 2: "INVALID_VALUE", 3: "NO_IN_DATA", 4: "NOT_STARTED", 5: "WRONG_COMP_MODE",
+    6: "WRONG_IMG_TYPE", 7: "FAILURE", 8: "ERR_CUDA", 9: "ERR_OOM", 10: "ERR_TIMEOUT", 11: "ERR_ADMISSION",
+    12: "ERR_UNSUPPORTED",
+}
+
+SPACE_NONE, SPACE_FRESNELTR, SPACE_ANGULARSP = 0, 1, 2
+TIME_NONE, TIME_STFT, TIME_PCA, TIME_SSA_STFT = 0, 1, 2, 3
+IMG_MODULUS, IMG_SQUARED_MODULUS, IMG_ARGUMENT = 0, 1, 2
+LENS_FP64, LENS_REF32 = 0, 1
+MEM_HOST, MEM_DEVICE = 0, 1
+
+SPACE_NAMES = {"NONE": 0, "None": 0, "FRESNELTR": 1, "FFT1": 1, "1FFT": 1, "Fresnel Tr.": 1,
+               "ANGULARSP": 2, "FFT2": 2, "2FFT": 2, "Angular SP.": 2}
+TIME_NAMES = {"NONE": 0, "None": 0, "STFT": 1, "PCA": 2, "SSA_STFT": 3}
+IMG_NAMES = {"MODULUS": 0, "SQUARED_MODULUS": 1, "ARGUMENT": 2}
+
+
+class HoloError(RuntimeError):
+    """A non-OK hv_status from the library (the reference's ApiCode / CUDA failures)."""
+
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)}: {last_error()}")
+
+
+# ---------------------------------------------------------------------------------- structs
+class FrameDescriptor(C.Structure):
+    """camera::FrameDescriptor (Camera/include/frame_desc.hh:13-48)."""
+
+    _fields_ = [("width", C.c_uint16), ("height", C.c_uint16), ("depth", C.c_uint32), ("byte_endian", C.c_uint32)]
+
+    def __init__(self, width=0, height=0, depth=2, byte_endian=0):
+        super().__init__(width, height, depth, byte_endian)
+
+    @property
+    def frame_res(self) -> int:
+        return int(self.width) * int(self.height)
+
+    @property
+    def frame_size(self) -> int:
+        return self.frame_res * int(self.depth)
+
+
+class Settings(C.Structure):
+    """Flat record of the compute settings this path reads (include/holovibes_gb300.h hv_settings)."""
+
+    _fields_ = [
+        ("space_transformation", C.c_int32), ("time_transformation", C.c_int32),
+        ("time_transformation_size", C.c_int32), ("time_stride", C.c_int32), ("batch_size", C.c_int32),
+        ("lambda_", C.c_float), ("z_distance", C.c_float), ("pixel_size", C.c_float), ("image_type", C.c_int32),
+        ("p_start", C.c_int32), ("p_width", C.c_int32), ("fft_shift", C.c_int32), ("renorm", C.c_int32),
+        ("renorm_constant", C.c_int32), ("accumulation", C.c_int32), ("log_enabled", C.c_int32),
+        ("contrast_enabled", C.c_int32), ("contrast_auto_refresh", C.c_int32), ("contrast_invert", C.c_int32),
+        ("contrast_min", C.c_float), ("contrast_max", C.c_float), ("contrast_lower", C.c_float),
+        ("contrast_upper", C.c_float), ("reticle_display", C.c_int32), ("reticle_scale", C.c_float),
+        ("unwrap_2d", C.c_int32), ("lens_mode", C.c_int32), ("output_buffer_size", C.c_int32),
+        ("input_buffer_size", C.c_int32),
+    ]
+
+    @classmethod
+    def defaults(cls) -> "Settings":
+        s = cls()
+        lib().hv_settings_default(C.byref(s))
+        return s
+
+    @classmethod
+    def from_json(cls, text: str, base: "Settings | None" = None) -> "Settings":
+        """ComputeSettingsApi::load_compute_settings (compute_settings.cc:66-99): partial merge."""
+        s = cls() if base is None else base.copy()
+        if base is None:
+            lib().hv_settings_default(C.byref(s))
+        check(lib().hv_settings_from_json(text.encode(), C.byref(s)), "hv_settings_from_json")
+        return s
+
+    def copy(self) -> "Settings":
+        s = Settings()
+        C.memmove(C.byref(s), C.byref(self), C.sizeof(Settings))
+        return s
+
+    def validate(self, fd: FrameDescriptor | None = None) -> "Settings":
+        s = self.copy()
+        check(lib().hv_settings_validate(C.byref(s), C.byref(fd) if fd is not None else None), "hv_settings_validate")
+        return s
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+    def update(self, **kw) -> "Settings":
+        for k, v in kw.items():
+            if k == "lambda":
+                k = "lambda_"
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+        return self
+
+
+# ---------------------------------------------------------------------------------- library
+_LIB = None
+
+
+def lib_path() -> Path:
+    return _build.lib_path()
+
+
+def lib() -> C.CDLL:
+    """Loads the in-tree shared library (building it first if it is absent)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not path.exists():
+        if os.environ.get("HV_NO_BUILD"):
+            raise RuntimeError(f"{path} is missing; run __graft_entry__.build()")
+        _build.build_library()
+    L = C.CDLL(str(path))
+    _declare(L)
+    _LIB = L
+    return L
+
+
+def _declare(L: C.CDLL) -> None:
+    vp, sz, i32, f32, i64, u64 = C.c_void_p, C.c_size_t, C.c_int, C.c_float, C.c_int64, C.c_uint64
+    st = C.c_int
+    sig = {
+        "hv_version": (C.c_char_p, []),
+        "hv_last_error": (C.c_char_p, []),
+        "hv_kernel_launches": (u64, []),
+        "hv_settings_default": (None, [C.POINTER(Settings)]),
+        "hv_settings_from_json": (st, [C.c_char_p, C.POINTER(Settings)]),
+        "hv_settings_validate": (st, [C.POINTER(Settings), C.POINTER(FrameDescriptor)]),
+        "hv_pipe_create": (vp, [C.POINTER(FrameDescriptor), C.POINTER(Settings), vp, C.POINTER(C.c_int)]),
+        "hv_pipe_destroy": (None, [vp]),
+        "hv_pipe_footprint": (sz, [C.POINTER(FrameDescriptor), C.POINTER(Settings)]),
+        "hv_pipe_push_frames": (st, [vp, vp, sz, i32]),
+        "hv_pipe_output_count": (sz, [vp]),
+        "hv_pipe_pull_output": (st, [vp, vp, i32, i64]),
+        "hv_pipe_update_settings": (st, [vp, C.POINTER(Settings)]),
+        "hv_pipe_request_autocontrast": (st, [vp]),
+        "hv_pipe_sync": (st, [vp]),
+        "hv_pipe_get_contrast_range": (st, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+        "hv_pipe_get_float_frame": (st, [vp, vp]),
+        "hv_pipe_get_ring": (st, [vp, vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+        "hv_pipe_kernel_launches": (u64, [vp]),
+        "hv_pipe_stream": (vp, [vp]),
+        "hv_fft_size_supported": (i32, [i32]),
+        "hv_fresnel_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
+        "hv_angular_spectrum_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
+        "hv_spatial_transform": (st, [vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, i32, i32, vp]),
+        "hv_fft2d": (st, [vp, vp, i32, i32, i32, i32, f32, vp]),
+        "hv_time_view": (st, [vp, i32, i32, i32, vp, i32, i32, f32, i32, vp, vp, vp]),
+        "hv_time_view_partials": (i32, [i32, i32]),
+        "hv_stft_weights": (st, [vp, i32, i32, i32, vp]),
+        "hv_pca_covariance": (st, [vp, i32, sz, vp, vp, vp]),
+        "hv_pca_cov_workspace": (sz, [i32, sz]),
+        "hv_pca_eigh": (st, [vp, i32, vp, vp, i32, i32, vp, vp, vp]),
+        "hv_pca_eigh_workspace": (sz, [i32]),
+        "hv_unwrap_2d": (st, [vp, vp, i32, i32, vp, vp]),
+        "hv_unwrap_workspace": (sz, [i32, i32]),
+        "hv_renormalize": (st, [vp, sz, i32, vp, i32, vp, vp]),
+        "hv_reduce_workspace": (sz, [sz]),
+        "hv_shift_corners": (st, [vp, i32, i32, vp]),
+        "hv_accumulate": (st, [vp, vp, i32, i32, i32, i32, vp, sz, vp]),
+        "hv_log10": (st, [vp, sz, vp]),
+        "hv_percentile": (st, [vp, i32, i32, f32, f32, f32, vp, vp, vp]),
+        "hv_percentile_workspace": (sz, [sz]),
+        "hv_contrast_to_ushort": (st, [vp, vp, i32, i32, vp, sz, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def last_error() -> str:
+    if _LIB is None:
+        return ""
+    msg = _LIB.hv_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(status: int, what: str) -> int:
+    if status not in (HV_OK, HV_NO_CHANGE):
+        raise HoloError(status, what)
+    return status
+
+
+def version() -> str:
+    return lib().hv_version().decode()
+
+
+def kernel_launches() -> int:
+    return int(lib().hv_kernel_launches())
+
+
+def fft_size_supported(n: int) -> bool:
+    return bool(lib().hv_fft_size_supported(n))
+
+
+# ---------------------------------------------------------------------------------- Pipe
+class Pipe:
+    """Drop-in for the reference's Pipe (Backend/includes/core/pipe.hh:70-125): raw frames in,
+    uint16 holograms out, settings applied at cycle boundaries."""
+
+    def __init__(self, fd: FrameDescriptor, settings: Settings, stream: int | None = None):
+        self.fd = fd
+        self.settings = settings.copy()
+        status = C.c_int(0)
+        self._p = lib().hv_pipe_create(C.byref(fd), C.byref(self.settings), stream, C.byref(status))
+        if not self._p:
+            raise HoloError(status.value, "hv_pipe_create")
+
+    def close(self) -> None:
+        if getattr(self, "_p", None):
+            lib().hv_pipe_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def footprint(fd: FrameDescriptor, settings: Settings) -> int:
+        return int(lib().hv_pipe_footprint(C.byref(fd), C.byref(settings)))
+
+    @property
+    def stream(self) -> int:
+        return lib().hv_pipe_stream(self._p)
+
+    def enqueue(self, frames) -> None:
+        """BatchInputQueue::enqueue: numpy array (host) of n frames, or an object with
+        ``data_ptr()`` and ``is_cuda`` (device memory, consumed in place)."""
+        if hasattr(frames, "data_ptr") and getattr(frames, "is_cuda", False):
+            n = frames.numel() * frames.element_size() // self.fd.frame_size
+            check(lib().hv_pipe_push_frames(self._p, frames.data_ptr(), n, MEM_DEVICE), "hv_pipe_push_frames")
+            return
+        arr = np.ascontiguousarray(frames)
+        n = arr.nbytes // self.fd.frame_size
+        check(lib().hv_pipe_push_frames(self._p, arr.ctypes.data, n, MEM_HOST), "hv_pipe_push_frames")
+
+    def enqueue_ptr(self, ptr: int, n: int, mem: int) -> None:
+        check(lib().hv_pipe_push_frames(self._p, ptr, n, mem), "hv_pipe_push_frames")
+
+    def output_count(self) -> int:
+        return int(lib().hv_pipe_output_count(self._p))
+
+    def pull(self, timeout_us: int = 10_000_000) -> np.ndarray:
+        out = np.empty((self.fd.height, self.fd.width), dtype=np.uint16)
+        check(lib().hv_pipe_pull_output(self._p, out.ctypes.data, MEM_HOST, timeout_us), "hv_pipe_pull_output")
+        return out
+
+    def pull_into(self, ptr: int, mem: int, timeout_us: int = 10_000_000) -> None:
+        check(lib().hv_pipe_pull_output(self._p, ptr, mem, timeout_us), "hv_pipe_pull_output")
+
+    def pull_all(self) -> list[np.ndarray]:
+        out = []
+        while self.output_count() > 0:
+            out.append(self.pull())
+        return out
+
+    def update_settings(self, settings: Settings) -> int:
+        st = lib().hv_pipe_update_settings(self._p, C.byref(settings))
+        check(st, "hv_pipe_update_settings")
+        if st == HV_OK:
+            self.settings = settings.copy()
+        return st
+
+    def request_autocontrast(self) -> None:
+        check(lib().hv_pipe_request_autocontrast(self._p), "hv_pipe_request_autocontrast")
+
+    def sync(self) -> None:
+        check(lib().hv_pipe_sync(self._p), "hv_pipe_sync")
+
+    def contrast_range(self) -> tuple[float, float]:
+        lo, hi = C.c_float(), C.c_float()
+        check(lib().hv_pipe_get_contrast_range(self._p, C.byref(lo), C.byref(hi)), "hv_pipe_get_contrast_range")
+        return lo.value, hi.value
+
+    def float_frame(self) -> np.ndarray:
+        out = np.empty((self.fd.height, self.fd.width), dtype=np.float32)
+        check(lib().hv_pipe_get_float_frame(self._p, out.ctypes.data), "hv_pipe_get_float_frame")
+        return out
+
+    def ring(self) -> tuple[np.ndarray, int, int]:
+        T = self.settings.time_transformation_size
+        out = np.empty((T, self.fd.height, self.fd.width), dtype=np.complex64)
+        a, b = C.c_int32(), C.c_int32()
+        check(lib().hv_pipe_get_ring(self._p, out.ctypes.data, C.byref(a), C.byref(b)), "hv_pipe_get_ring")
+        return out, a.value, b.value
+
+    def kernel_launches(self) -> int:
+        return int(lib().hv_pipe_kernel_launches(self._p))
+
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,202 @@
+// C ABI entry points for the compute steps, settings and library state.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "hv_internal.h"
+
+namespace hv {
+
+static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches{0};
+
+void set_last_error(const char* msg, const char* file, int line)
+{
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s (%s:%d)", msg ? msg : "error", file, line);
+    g_last_error = buf;
+}
+
+void set_last_error_msg(const char* msg) { g_last_error = msg ? msg : ""; }
+
+void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+void settings_default(hv_settings* s);
+hv_status settings_from_json(const char* text, hv_settings* s);
+hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd);
+
+}  // namespace hv
+
+using namespace hv;
+
+static inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
+
+extern "C" {
+
+const char* hv_version(void) { return "holovibes_gb300 0.1.0 (sm_103a)"; }
+
+const char* hv_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t hv_kernel_launches(void) { return launch_count(); }
+
+void hv_settings_default(hv_settings* s)
+{
+    if (s)
+        settings_default(s);
+}
+
+hv_status hv_settings_from_json(const char* json, hv_settings* s) { return settings_from_json(json, s); }
+
+hv_status hv_settings_validate(hv_settings* s, const hv_frame_desc* fd) { return settings_validate(s, fd); }
+
+int hv_fft_size_supported(int n) { return fft_size_supported(n) ? 1 : 0; }
+
+hv_status hv_fresnel_lens(void* lens_c64, int width, int height, float lambda, float z, float pixel_size_um,
+                          int lens_mode, void* stream)
+{
+    if (!lens_c64 || width <= 0 || height <= 0)
+        return HV_INVALID_VALUE;
+    return make_fresnel_lens(static_cast<float2*>(lens_c64), width, height, lambda, z, pixel_size_um, lens_mode,
+                             S(stream));
+}
+
+hv_status hv_angular_spectrum_lens(void* lens_c64, int width, int height, float lambda, float z,
+                                   float pixel_size_um, int lens_mode, void* stream)
+{
+    if (!lens_c64 || width <= 0 || height <= 0 || (width & 1) || (height & 1))
+        return HV_INVALID_VALUE;
+    return make_spectral_lens(static_cast<float2*>(lens_c64), width, height, lambda, z, pixel_size_um, lens_mode,
+                              S(stream));
+}
+
+hv_status hv_spatial_transform(const void* raw, int raw_bytes, int big_endian, int width, int height, int batch,
+                               int space, const void* lens_c64, void* work_c64, void* ring_c64, int slot0,
+                               int nslots, void* stream)
+{
+    const int kind = raw_kind(raw_bytes, big_endian);
+    if (!raw || !ring_c64 || kind < 0 || width <= 0 || height <= 0 || batch < 0 || nslots <= 0 || slot0 < 0 ||
+        slot0 >= nslots || batch > nslots)
+        return HV_INVALID_VALUE;
+    if (space != HV_SPACE_NONE && (!lens_c64 || !work_c64))
+        return HV_INVALID_VALUE;
+    return spatial_transform(raw, kind, width, height, batch, space, static_cast<const float2*>(lens_c64),
+                             static_cast<float2*>(work_c64), static_cast<float2*>(ring_c64), slot0, nslots, S(stream));
+}
+
+hv_status hv_fft2d(const void* in_c64, void* out_c64, int n0, int n1, int batch, int inverse, float scale,
+                   void* stream)
+{
+    if (!in_c64 || !out_c64 || batch <= 0)
+        return HV_INVALID_VALUE;
+    return fft2d(static_cast<const float2*>(in_c64), static_cast<float2*>(out_c64), n0, n1, batch, inverse, scale,
+                 S(stream));
+}
+
+hv_status hv_time_view(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
+                       int img_type, float scale, int shift, float* out_f32, double* partials_f64, void* stream)
+{
+    if (!ring_c64 || !weights_c64 || !out_f32 || img_type < 0 || img_type > HV_IMG_ARGUMENT)
+        return HV_INVALID_VALUE;
+    return time_view(static_cast<const float2*>(ring_c64), T, width, height, static_cast<const float2*>(weights_c64), K,
+                     img_type, scale, shift, out_f32, partials_f64, S(stream));
+}
+
+int hv_time_view_partials(int width, int height) { return time_view_partials(width, height); }
+
+hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* stream)
+{
+    if (!weights_c64 || pmin < 0 || pmax < pmin || pmax >= T)
+        return HV_INVALID_VALUE;
+    return stft_weights(static_cast<float2*>(weights_c64), T, pmin, pmax, S(stream));
+}
+
+hv_status hv_pca_covariance(const void* ring_c64, int T, size_t npix, void* cov_c128, void* work, void* stream)
+{
+    if (!ring_c64 || !cov_c128 || !work)
+        return HV_INVALID_VALUE;
+    return pca_covariance(static_cast<const float2*>(ring_c64), T, npix, static_cast<double2*>(cov_c128), work,
+                          S(stream));
+}
+
+size_t hv_pca_cov_workspace(int T, size_t npix) { return pca_cov_workspace(T, npix); }
+
+hv_status hv_pca_eigh(void* cov_c128, int T, double* eigenvalues, void* eigenvectors_c128, int pmin, int pmax,
+                      void* weights_c64, void* work, void* stream)
+{
+    if (!cov_c128 || !eigenvalues || !eigenvectors_c128 || !work || T <= 0)
+        return HV_INVALID_VALUE;
+    if (weights_c64 && (pmin < 0 || pmax < pmin || pmax >= T))
+        return HV_INVALID_VALUE;
+    return pca_eigh(static_cast<double2*>(cov_c128), T, eigenvalues, static_cast<double2*>(eigenvectors_c128), pmin,
+                    pmax, static_cast<float2*>(weights_c64), work, S(stream));
+}
+
+size_t hv_pca_eigh_workspace(int T) { return pca_eigh_workspace(T); }
+
+hv_status hv_unwrap_2d(const float* in, float* out, int width, int height, void* work, void* stream)
+{
+    if (!in || !out || !work)
+        return HV_INVALID_VALUE;
+    return unwrap_2d(in, out, width, height, work, S(stream));
+}
+
+size_t hv_unwrap_workspace(int width, int height) { return unwrap_workspace(width, height); }
+
+hv_status hv_renormalize(float* frame, size_t n, int renorm_constant, const double* partials_f64, int npartials,
+                         void* work, void* stream)
+{
+    if (!frame || !work || n == 0)
+        return HV_INVALID_VALUE;
+    float* factors = reinterpret_cast<float*>(static_cast<char*>(work) + reduce_workspace(n));
+    hv_status r = renorm_factors(frame, n, renorm_constant, partials_f64, npartials, factors, work, S(stream));
+    if (r != HV_OK)
+        return r;
+    // one-row frame: renormalise in place, no shift, no accumulation
+    return renorm_shift_accumulate(frame, frame, static_cast<int>(n), 1, factors, 0, nullptr, 0, 0, 0, 0, 0, S(stream));
+}
+
+size_t hv_reduce_workspace(size_t n) { return reduce_workspace(n) + 64; }
+
+hv_status hv_shift_corners(float* frame, int width, int height, void* stream)
+{
+    if (!frame)
+        return HV_INVALID_VALUE;
+    return shift_corners(frame, width, height, S(stream));
+}
+
+hv_status hv_accumulate(const float* frame, float* acc_ring, int A, int slot, int start, int count, float* out,
+                        size_t n, void* stream)
+{
+    if (!frame || !acc_ring || !out)
+        return HV_INVALID_VALUE;
+    return accumulate(frame, acc_ring, A, slot, start, count, out, n, S(stream));
+}
+
+hv_status hv_log10(float* frame, size_t n, void* stream)
+{
+    if (!frame)
+        return HV_INVALID_VALUE;
+    return log10_map(frame, n, S(stream));
+}
+
+hv_status hv_percentile(const float* frame, int width, int height, float lower, float upper, float reticle_scale,
+                        float* range_f32, void* work, void* stream)
+{
+    if (!frame || !range_f32 || !work || width <= 0 || height <= 0)
+        return HV_INVALID_VALUE;
+    return percentile(frame, width, height, lower, upper, reticle_scale, range_f32, work, S(stream));
+}
+
+size_t hv_percentile_workspace(size_t n) { return percentile_workspace(n); }
+
+hv_status hv_contrast_to_ushort(const float* frame, const float* range_f32, int invert, int apply_contrast,
+                                uint16_t* out, size_t n, void* stream)
+{
+    if (!frame || !out || (apply_contrast && !range_f32))
+        return HV_INVALID_VALUE;
+    return contrast_to_ushort(frame, range_f32, invert, apply_contrast, out, n, S(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+// Internal declarations shared by the translation units of the library (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "holovibes_gb300.h"
+
+namespace hv {
+
+void set_last_error(const char* msg, const char* file, int line);
+void set_last_error_msg(const char* msg);
+void count_launch(uint64_t n = 1);
+uint64_t launch_count();
+
+// spatial.cu
+bool fft_size_supported(int n);
+int raw_kind(int raw_bytes, int big_endian);
+hv_status make_fresnel_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st);
+hv_status make_spectral_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st);
+hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
+                            float2* work, float2* ring, int slot0, int nslots, cudaStream_t st);
+hv_status fft2d(const float2* in, float2* out, int n0, int n1, int batch, int inverse, float scale, cudaStream_t st);
+
+// time_transform.cu
+int time_view_partials(int W, int H);
+hv_status time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type, float scale,
+                    int shift, float* out, double* partials, cudaStream_t st);
+hv_status stft_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
+hv_status delta_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
+size_t pca_cov_workspace(int T, size_t npix);
+hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st);
+size_t pca_eigh_workspace(int T);
+hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
+                   cudaStream_t st);
+
+// render.cu
+size_t unwrap_workspace(int W, int H);
+hv_status unwrap_2d(const float* in, float* out, int W, int H, void* work, cudaStream_t st);
+size_t reduce_workspace(size_t n);
+hv_status renorm_factors(const float* frame, size_t n, int renorm_constant, const double* partials, int npartials,
+                         float* factors, void* work, cudaStream_t st);
+hv_status renorm_shift_accumulate(const float* in, float* out, int W, int H, const float* factors, int shift,
+                                  float* acc_ring, int A, int slot, int start, int count, int log_enabled,
+                                  cudaStream_t st, float prescale = 1.0f);
+hv_status shift_corners(float* frame, int W, int H, cudaStream_t st);
+hv_status accumulate(const float* frame, float* acc_ring, int A, int slot, int start, int count, float* out, size_t n,
+                     cudaStream_t st);
+hv_status log10_map(float* frame, size_t n, cudaStream_t st);
+size_t percentile_workspace(size_t n);
+hv_status percentile(const float* frame, int W, int H, float lower, float upper, float reticle_scale, float* range,
+                     void* work, cudaStream_t st);
+hv_status contrast_to_ushort(const float* frame, const float* range, int invert, int apply, uint16_t* out, size_t n,
+                             cudaStream_t st);
+
+}  // namespace hv
+
+#define HV_CUDA_TRY(expr)                                                                                              \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        cudaError_t hv_err__ = (expr);                                                                                 \
+        if (hv_err__ != cudaSuccess)                                                                                   \
+        {                                                                                                              \
+            hv::set_last_error(cudaGetErrorString(hv_err__), __FILE__, __LINE__);                                      \
+            return (hv_err__ == cudaErrorMemoryAllocation) ? HV_ERR_OOM : HV_ERR_CUDA;                                \
+        }                                                                                                              \
+    } while (0)
+
+#define HV_LAUNCH_CHECK() HV_CUDA_TRY(cudaGetLastError())

@@ -1,0 +1,676 @@
+// The Pipe: a GB300-native drop-in for the reference's Pipe / ICompute engine.
+//
+// Reference behaviour (Holovibes):
+//   buffers / ctor       Backend/includes/core/icompute.hh:123-171, Backend/sources/core/icompute.cc:71-175
+//   step list (refresh)  Backend/sources/core/pipe.cc:255-387
+//   cycle (exec)         Backend/sources/core/pipe.cc:650-676
+//   stride gate          Backend/sources/core/pipe.cc:400-416 (process the batch at which the batch
+//                        counter reaches time_stride, drop the others)
+//   wait T               Backend/sources/core/pipe.cc:418-427 (no output until the ring is full)
+//   ring enqueue         Backend/sources/data_struct/queue.cc:332-380
+//   accumulation queue   Backend/sources/data_struct/queue.cc:149-189, image_accumulation.cc:136-157
+//   autocontrast gating  Backend/sources/compute/rendering.cc:239-299, rendering.hh:168-181
+//   input queue          Backend/sources/data_struct/batch_input_queue.cc:124-235
+//   output queue         Backend/sources/core/pipe.cc:491-524
+//
+// GB300 design: the host bookkeeping of a cycle (stride gate, ring indices, accumulation
+// indices, autocontrast flags) is deterministic, so it runs at enqueue time on the caller's
+// thread and every cycle is a stream of kernel launches with no host round trip (the reference
+// synchronises the stream inside Queue::enqueue_multiple, on percentile D2H copies and at the
+// end of each cycle). Raw frames arrive in a device ring of batch slots through a copy stream;
+// outputs leave through a device ring of uint16 frames with one event each.
+#include <chrono>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "hv_internal.h"
+
+namespace hv {
+void settings_default(hv_settings* s);
+hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd);
+}  // namespace hv
+
+using namespace hv;
+
+struct hv_pipe
+{
+    hv_frame_desc fd{};
+    hv_settings s{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    bool own_stream = false;
+
+    int W = 0, H = 0;
+    size_t HW = 0;
+    int depth = 2, kind = 0;
+    int B = 1, T = 1, S = 1, K = 1, pmin = 0, pmax = 0, A = 0;
+
+    // device buffers
+    std::vector<void*> allocs;
+    float2* lens = nullptr;
+    float2* spatial = nullptr;
+    float2* ring = nullptr;
+    float2* weights = nullptr;
+    double2* cov = nullptr;
+    double* evals = nullptr;
+    double2* evecs = nullptr;
+    void* cov_work = nullptr;
+    void* eig_work = nullptr;
+    float* view = nullptr;
+    float* unwrapped = nullptr;
+    void* unwrap_work = nullptr;
+    double* partials = nullptr;
+    int npartials = 0;
+    void* reduce_work = nullptr;
+    float* factors = nullptr;
+    float* post = nullptr;
+    float* acc_ring = nullptr;
+    float* range = nullptr;
+    void* pct_work = nullptr;
+
+    // input ring of batch slots
+    uint8_t* in_ring = nullptr;
+    int in_slots = 0;
+    size_t batch_bytes = 0;
+    std::vector<cudaEvent_t> in_filled, in_consumed;
+    int in_slot = 0;
+    int in_fill = 0;  // frames already in the current slot
+
+    // output ring
+    uint16_t* out_ring = nullptr;
+    int out_cap = 0;
+    std::vector<cudaEvent_t> out_ready, out_freed;
+    int out_head = 0, out_count = 0;
+    uint64_t out_overwritten = 0;
+
+    // cycle state
+    int ring_start = 0, ring_size = 0;
+    int batch_index = 0;
+    int acc_start = 0, acc_size = 0;
+    bool autocontrast_pending = false;
+    bool last_frame_valid = false;
+    uint64_t launches0 = 0;
+
+    std::mutex mu;
+};
+
+namespace {
+
+template <class T>
+hv_status dalloc(hv_pipe* p, T*& ptr, size_t bytes)
+{
+    void* v = nullptr;
+    if (bytes == 0)
+        bytes = 16;
+    cudaError_t e = cudaMalloc(&v, bytes);
+    if (e != cudaSuccess)
+    {
+        set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+        return e == cudaErrorMemoryAllocation ? HV_ERR_OOM : HV_ERR_CUDA;
+    }
+    p->allocs.push_back(v);
+    ptr = static_cast<T*>(v);
+    return HV_OK;
+}
+
+void free_buffers(hv_pipe* p)
+{
+    for (void* v : p->allocs)
+        cudaFree(v);
+    p->allocs.clear();
+    for (auto* vec : {&p->in_filled, &p->in_consumed, &p->out_ready, &p->out_freed})
+    {
+        for (cudaEvent_t e : *vec)
+            cudaEventDestroy(e);
+        vec->clear();
+    }
+}
+
+bool uses_pca(const hv_settings& s) { return s.time_transformation == HV_TIME_PCA; }
+bool uses_unwrap(const hv_settings& s) { return s.image_type == HV_IMG_ARGUMENT && s.unwrap_2d; }
+
+struct Sizes
+{
+    size_t total = 0;
+    void add(size_t b) { total += (b + 255) / 256 * 256; }
+};
+
+size_t footprint(const hv_frame_desc& fd, const hv_settings& s)
+{
+    const size_t HW = static_cast<size_t>(fd.width) * fd.height;
+    const int B = s.batch_size, T = s.time_transformation_size;
+    const int K = (s.p_width != 0 ? std::min(s.p_start + s.p_width, T) : s.p_start) - s.p_start + 1;
+    Sizes z;
+    z.add(HW * 8);                                                      // lens
+    z.add(s.space_transformation != HV_SPACE_NONE ? HW * 8 * B : 16);  // spatial
+    z.add(HW * 8 * T);                                                  // ring
+    z.add(static_cast<size_t>(K > 0 ? K : 1) * T * 8);                 // weights
+    if (uses_pca(s))
+    {
+        z.add(static_cast<size_t>(T) * T * 16 * 2 + T * 8);
+        z.add(pca_cov_workspace(T, HW));
+        z.add(pca_eigh_workspace(T));
+    }
+    z.add(HW * 4 * 2);  // view + post
+    if (uses_unwrap(s))
+    {
+        z.add(HW * 4);
+        z.add(unwrap_workspace(fd.width, fd.height));
+    }
+    z.add(static_cast<size_t>(time_view_partials(fd.width, fd.height)) * 8);
+    z.add(reduce_workspace(HW));
+    z.add(64);
+    if (s.accumulation > 1)
+        z.add(HW * 4 * s.accumulation);
+    z.add(64);
+    z.add(percentile_workspace(HW));
+    const int in_slots = std::max(2, s.input_buffer_size / std::max(1, B));
+    z.add(HW * fd.depth * B * static_cast<size_t>(in_slots));
+    z.add(HW * 2 * static_cast<size_t>(std::max(1, s.output_buffer_size)));
+    return z.total;
+}
+
+hv_status build(hv_pipe* p)
+{
+    free_buffers(p);
+    const hv_settings& s = p->s;
+    p->W = p->fd.width;
+    p->H = p->fd.height;
+    p->HW = static_cast<size_t>(p->W) * p->H;
+    p->depth = static_cast<int>(p->fd.depth);
+    p->kind = raw_kind(p->depth, p->fd.byte_endian != 0);
+    p->B = s.batch_size;
+    p->T = s.time_transformation_size;
+    p->S = s.time_stride;
+    // Converts::insert_compute_p_accu (converts.cc:76-92)
+    p->pmin = s.p_start;
+    p->pmax = s.p_width != 0 ? std::max(0, std::min(p->pmin + s.p_width, p->T)) : p->pmin;
+    if (p->pmax > p->T - 1)
+        p->pmax = p->T - 1;  // the reference reads past the buffer there; validation keeps p + width < T
+    p->K = p->pmax - p->pmin + 1;
+    p->A = s.accumulation > 1 ? s.accumulation : 0;
+    const size_t HW = p->HW;
+    hv_status st;
+#define HV_ALLOC(ptr, bytes)                                                                                           \
+    if ((st = dalloc(p, ptr, bytes)) != HV_OK)                                                                         \
+        return st;
+    HV_ALLOC(p->lens, HW * sizeof(float2));
+    HV_ALLOC(p->spatial, (s.space_transformation != HV_SPACE_NONE ? HW * p->B : 1) * sizeof(float2));
+    HV_ALLOC(p->ring, HW * p->T * sizeof(float2));
+    HV_ALLOC(p->weights, static_cast<size_t>(p->K) * p->T * sizeof(float2));
+    if (uses_pca(s))
+    {
+        HV_ALLOC(p->cov, static_cast<size_t>(p->T) * p->T * sizeof(double2));
+        HV_ALLOC(p->evecs, static_cast<size_t>(p->T) * p->T * sizeof(double2));
+        HV_ALLOC(p->evals, static_cast<size_t>(p->T) * sizeof(double));
+        HV_ALLOC(p->cov_work, pca_cov_workspace(p->T, HW));
+        HV_ALLOC(p->eig_work, pca_eigh_workspace(p->T));
+    }
+    HV_ALLOC(p->view, HW * sizeof(float));
+    HV_ALLOC(p->post, HW * sizeof(float));
+    if (uses_unwrap(s))
+    {
+        HV_ALLOC(p->unwrapped, HW * sizeof(float));
+        HV_ALLOC(p->unwrap_work, unwrap_workspace(p->W, p->H));
+    }
+    p->npartials = time_view_partials(p->W, p->H);
+    HV_ALLOC(p->partials, static_cast<size_t>(p->npartials) * sizeof(double));
+    HV_ALLOC(p->reduce_work, reduce_workspace(HW));
+    HV_ALLOC(p->factors, 4 * sizeof(float));
+    if (p->A > 0)
+    {
+        HV_ALLOC(p->acc_ring, HW * p->A * sizeof(float));
+    }
+    HV_ALLOC(p->range, 4 * sizeof(float));
+    HV_ALLOC(p->pct_work, percentile_workspace(HW));
+    p->in_slots = std::max(2, s.input_buffer_size / std::max(1, p->B));
+    p->batch_bytes = HW * p->depth * p->B;
+    HV_ALLOC(p->in_ring, p->batch_bytes * p->in_slots);
+    p->out_cap = std::max(1, s.output_buffer_size);
+    HV_ALLOC(p->out_ring, HW * sizeof(uint16_t) * p->out_cap);
+#undef HV_ALLOC
+    auto mk_events = [&](std::vector<cudaEvent_t>& v, int n) -> hv_status {
+        v.resize(n);
+        for (int i = 0; i < n; ++i)
+            HV_CUDA_TRY(cudaEventCreateWithFlags(&v[i], cudaEventDisableTiming));
+        return HV_OK;
+    };
+    if ((st = mk_events(p->in_filled, p->in_slots)) != HV_OK || (st = mk_events(p->in_consumed, p->in_slots)) != HV_OK ||
+        (st = mk_events(p->out_ready, p->out_cap)) != HV_OK || (st = mk_events(p->out_freed, p->out_cap)) != HV_OK)
+        return st;
+
+    // ring starts zeroed like Queue::resize (queue.cc:131-134)
+    HV_CUDA_TRY(cudaMemsetAsync(p->ring, 0, HW * p->T * sizeof(float2), p->stream));
+    // lens (computed once per refresh, fourier_transform.cc:93-137)
+    if (s.space_transformation == HV_SPACE_FRESNELTR)
+        st = make_fresnel_lens(p->lens, p->W, p->H, s.lambda, s.z_distance, s.pixel_size, s.lens_mode, p->stream);
+    else if (s.space_transformation == HV_SPACE_ANGULARSP)
+        st = make_spectral_lens(p->lens, p->W, p->H, s.lambda, s.z_distance, s.pixel_size, s.lens_mode, p->stream);
+    if (st != HV_OK)
+        return st;
+    if (s.time_transformation == HV_TIME_STFT)
+        st = stft_weights(p->weights, p->T, p->pmin, p->pmax, p->stream);
+    else if (s.time_transformation == HV_TIME_NONE)
+        st = delta_weights(p->weights, p->T, p->pmin, p->pmax, p->stream);
+    if (st != HV_OK)
+        return st;
+    float r0[4] = {s.contrast_min, s.contrast_max, 0.f, 0.f};
+    HV_CUDA_TRY(cudaMemcpyAsync(p->range, r0, sizeof(r0), cudaMemcpyHostToDevice, p->stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+
+    p->ring_start = p->ring_size = 0;
+    p->batch_index = 0;
+    p->acc_start = p->acc_size = 0;
+    p->autocontrast_pending = s.contrast_enabled && s.contrast_auto_refresh;
+    p->in_slot = 0;
+    p->in_fill = 0;
+    p->out_head = p->out_count = 0;
+    p->last_frame_valid = false;
+    return HV_OK;
+}
+
+// Rendering of one output from a full ring (pipe.cc:334-374).
+hv_status render(hv_pipe* p)
+{
+    const hv_settings& s = p->s;
+    cudaStream_t st = p->stream;
+    hv_status r;
+    const bool pca = uses_pca(s);
+    const bool unwrap = uses_unwrap(s);
+    if (pca)
+    {
+        if ((r = pca_covariance(p->ring, p->T, p->HW, p->cov, p->cov_work, st)) != HV_OK)
+            return r;
+        if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, p->weights, p->eig_work, st)) != HV_OK)
+            return r;
+    }
+    // converts.cc:50-62: PCA views are scaled by (2 << 16) - 1
+    const float scale = pca ? static_cast<float>((2 << 16) - 1) : 1.0f;
+    const bool shift_in_view = s.fft_shift && !unwrap;
+    const bool renorm = s.renorm != 0;
+    const float* frame = p->view;
+    if (!unwrap)
+    {
+        if ((r = time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale, shift_in_view ? 1 : 0,
+                           p->view, renorm ? p->partials : nullptr, st)) != HV_OK)
+            return r;
+        if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
+                                          p->reduce_work, st)) != HV_OK)
+            return r;
+    }
+    else
+    {
+        if ((r = time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, 1.0f, 0, p->view, nullptr, st)) !=
+            HV_OK)
+            return r;
+        if ((r = unwrap_2d(p->view, p->unwrapped, p->W, p->H, p->unwrap_work, st)) != HV_OK)
+            return r;
+        if (pca && (r = renorm_shift_accumulate(p->unwrapped, p->unwrapped, p->W, p->H, nullptr, 0, nullptr, 0, 0, 0, 0,
+                                                0, st, scale)) != HV_OK)
+            return r;
+        frame = p->unwrapped;
+        if (renorm && (r = renorm_factors(frame, p->HW, s.renorm_constant, nullptr, 0, p->factors, p->reduce_work, st)) !=
+                          HV_OK)
+            return r;
+    }
+    // accumulation queue bookkeeping (Queue::enqueue, queue.cc:149-189)
+    int slot = 0, start = 0, count = 0;
+    if (p->A > 0)
+    {
+        slot = (p->acc_start + p->acc_size) % p->A;
+        if (p->acc_size < p->A)
+            ++p->acc_size;
+        else
+            p->acc_start = (p->acc_start + 1) % p->A;
+        start = p->acc_start;
+        count = p->acc_size;
+    }
+    const int shift_after = (s.fft_shift && unwrap) ? 1 : 0;
+    if ((r = renorm_shift_accumulate(frame, p->post, p->W, p->H, renorm ? p->factors : nullptr, shift_after,
+                                     p->A > 0 ? p->acc_ring : nullptr, p->A, slot, start, count, s.log_enabled, st,
+                                     1.0f)) != HV_OK)
+        return r;
+    // autocontrast (rendering.cc:239-299): first frame without accumulation, or at accumulation
+    // size 1 and when the accumulation queue is full
+    if (s.contrast_enabled && p->autocontrast_pending)
+    {
+        const bool apply = p->A == 0 || p->acc_size == p->A || p->acc_size == 1;
+        if (apply)
+        {
+            if ((r = percentile(p->post, p->W, p->H, s.contrast_lower, s.contrast_upper,
+                                s.reticle_display ? s.reticle_scale : 0.0f, p->range, p->pct_work, st)) != HV_OK)
+                return r;
+            if (p->A == 0 || p->acc_size == p->A)
+                p->autocontrast_pending = false;
+        }
+    }
+    // output slot (overwrite the oldest when the queue is full, like Queue::enqueue)
+    int slot_out;
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        if (p->out_count == p->out_cap)
+        {
+            p->out_head = (p->out_head + 1) % p->out_cap;
+            --p->out_count;
+            ++p->out_overwritten;
+        }
+        slot_out = (p->out_head + p->out_count) % p->out_cap;
+    }
+    HV_CUDA_TRY(cudaStreamWaitEvent(st, p->out_freed[slot_out], 0));
+    if ((r = contrast_to_ushort(p->post, p->range, s.contrast_invert, s.contrast_enabled, p->out_ring + slot_out * p->HW,
+                                p->HW, st)) != HV_OK)
+        return r;
+    HV_CUDA_TRY(cudaEventRecord(p->out_ready[slot_out], st));
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        ++p->out_count;
+    }
+    p->last_frame_valid = true;
+    return HV_OK;
+}
+
+// One batch of B raw frames at device address `raw` (pipe.cc:295-334).
+hv_status process_batch(hv_pipe* p, const uint8_t* raw)
+{
+    // insert_wait_time_stride (pipe.cc:400-416)
+    p->batch_index += p->B;
+    if (p->batch_index != p->S)
+        return HV_OK;
+    p->batch_index = 0;
+    // Queue::enqueue_multiple (queue.cc:332-380)
+    int nb = p->B;
+    const int T = p->T;
+    const size_t frame_bytes = p->HW * p->depth;
+    if (nb > T)
+    {
+        raw += static_cast<size_t>(nb - T) * frame_bytes;
+        p->ring_start = (p->ring_start + nb - T) % T;
+        nb = T;
+    }
+    const int begin = (p->ring_start + p->ring_size) % T;
+    hv_status r = spatial_transform(raw, p->kind, p->W, p->H, nb, p->s.space_transformation, p->lens, p->spatial,
+                                    p->ring, begin, T, p->stream);
+    if (r != HV_OK)
+        return r;
+    p->ring_size += nb;
+    if (p->ring_size > T)
+    {
+        p->ring_start = (p->ring_start + p->ring_size - T) % T;
+        p->ring_size = T;
+    }
+    // insert_wait_time_transformation_size (pipe.cc:418-427)
+    if (p->ring_size < T)
+        return HV_OK;
+    return render(p);
+}
+
+}  // namespace
+
+// ==================================================================================== C ABI
+
+extern "C" {
+
+size_t hv_pipe_footprint(const hv_frame_desc* fd, const hv_settings* settings)
+{
+    if (!fd || !settings)
+        return 0;
+    hv_settings s = *settings;
+    if (settings_validate(&s, fd) != HV_OK)
+        return 0;
+    return footprint(*fd, s);
+}
+
+hv_pipe* hv_pipe_create(const hv_frame_desc* fd, const hv_settings* settings, void* stream, hv_status* status)
+{
+    hv_status dummy;
+    hv_status& out = status ? *status : dummy;
+    if (!fd || !settings)
+    {
+        out = HV_INVALID_VALUE;
+        return nullptr;
+    }
+    hv_pipe* p = new (std::nothrow) hv_pipe();
+    if (!p)
+    {
+        out = HV_FAILURE;
+        return nullptr;
+    }
+    p->fd = *fd;
+    p->s = *settings;
+    if ((out = settings_validate(&p->s, fd)) != HV_OK)
+    {
+        delete p;
+        return nullptr;
+    }
+    if (cudaGetDevice(&p->device) != cudaSuccess)
+    {
+        set_last_error_msg("no CUDA device");
+        out = HV_ERR_CUDA;
+        delete p;
+        return nullptr;
+    }
+    if (stream)
+        p->stream = static_cast<cudaStream_t>(stream);
+    else
+    {
+        if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+        {
+            out = HV_ERR_CUDA;
+            delete p;
+            return nullptr;
+        }
+        p->own_stream = true;
+    }
+    if (cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        out = HV_ERR_CUDA;
+        hv_pipe_destroy(p);
+        return nullptr;
+    }
+    p->launches0 = launch_count();
+    if ((out = build(p)) != HV_OK)
+    {
+        hv_pipe_destroy(p);
+        return nullptr;
+    }
+    return p;
+}
+
+void hv_pipe_destroy(hv_pipe* p)
+{
+    if (!p)
+        return;
+    if (p->stream)
+        cudaStreamSynchronize(p->stream);
+    if (p->copy_stream)
+        cudaStreamSynchronize(p->copy_stream);
+    free_buffers(p);
+    if (p->copy_stream)
+        cudaStreamDestroy(p->copy_stream);
+    if (p->own_stream && p->stream)
+        cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+hv_status hv_pipe_push_frames(hv_pipe* p, const void* frames, size_t n, int mem)
+{
+    if (!p || (!frames && n))
+        return HV_INVALID_VALUE;
+    const size_t frame_bytes = p->HW * p->depth;
+    const uint8_t* src = static_cast<const uint8_t*>(frames);
+    const cudaMemcpyKind kind = mem == HV_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    hv_status r;
+    while (n > 0)
+    {
+        if (mem == HV_MEM_DEVICE && p->in_fill == 0 && n >= static_cast<size_t>(p->B))
+        {
+            // zero-copy: the batch is consumed in place, stream-ordered on the pipe's stream
+            if ((r = process_batch(p, src)) != HV_OK)
+                return r;
+            src += frame_bytes * p->B;
+            n -= p->B;
+            continue;
+        }
+        const int slot = p->in_slot;
+        const size_t take = std::min(n, static_cast<size_t>(p->B - p->in_fill));
+        uint8_t* dst = p->in_ring + slot * p->batch_bytes + static_cast<size_t>(p->in_fill) * frame_bytes;
+        if (p->in_fill == 0)
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->in_consumed[slot], 0));
+        HV_CUDA_TRY(cudaMemcpyAsync(dst, src, take * frame_bytes, kind, p->copy_stream));
+        p->in_fill += static_cast<int>(take);
+        src += take * frame_bytes;
+        n -= take;
+        if (p->in_fill == p->B)
+        {
+            HV_CUDA_TRY(cudaEventRecord(p->in_filled[slot], p->copy_stream));
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->in_filled[slot], 0));
+            if ((r = process_batch(p, p->in_ring + slot * p->batch_bytes)) != HV_OK)
+                return r;
+            HV_CUDA_TRY(cudaEventRecord(p->in_consumed[slot], p->stream));
+            p->in_fill = 0;
+            p->in_slot = (slot + 1) % p->in_slots;
+        }
+    }
+    // the caller may reuse host memory on return: wait for its copies only
+    if (mem == HV_MEM_HOST)
+        HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
+    return HV_OK;
+}
+
+size_t hv_pipe_output_count(hv_pipe* p)
+{
+    if (!p)
+        return 0;
+    std::lock_guard<std::mutex> g(p->mu);
+    return static_cast<size_t>(p->out_count);
+}
+
+hv_status hv_pipe_pull_output(hv_pipe* p, uint16_t* dst, int mem, int64_t timeout_us)
+{
+    if (!p || !dst)
+        return HV_INVALID_VALUE;
+    int slot;
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        if (p->out_count == 0)
+            return timeout_us > 0 ? HV_ERR_TIMEOUT : HV_NO_IN_DATA;
+        slot = p->out_head;
+    }
+    // bounded wait for the frame's kernels
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;)
+    {
+        const cudaError_t e = cudaEventQuery(p->out_ready[slot]);
+        if (e == cudaSuccess)
+            break;
+        if (e != cudaErrorNotReady)
+        {
+            set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+            return HV_ERR_CUDA;
+        }
+        const auto us =
+            std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_us >= 0 && us > timeout_us)
+            return HV_ERR_TIMEOUT;
+        std::this_thread::yield();
+    }
+    HV_CUDA_TRY(cudaMemcpyAsync(dst, p->out_ring + slot * p->HW, p->HW * sizeof(uint16_t),
+                                mem == HV_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                p->copy_stream));
+    HV_CUDA_TRY(cudaEventRecord(p->out_freed[slot], p->copy_stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        if (p->out_head == slot && p->out_count > 0)
+        {
+            p->out_head = (p->out_head + 1) % p->out_cap;
+            --p->out_count;
+        }
+    }
+    return HV_OK;
+}
+
+hv_status hv_pipe_update_settings(hv_pipe* p, const hv_settings* settings)
+{
+    if (!p || !settings)
+        return HV_INVALID_VALUE;
+    hv_settings ns = *settings;
+    hv_status r = settings_validate(&ns, &p->fd);
+    if (r != HV_OK)
+        return r;
+    if (std::memcmp(&ns, &p->s, sizeof(ns)) == 0)
+        return HV_NO_CHANGE;
+    HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
+    p->s = ns;
+    return build(p);
+}
+
+hv_status hv_pipe_request_autocontrast(hv_pipe* p)
+{
+    if (!p)
+        return HV_INVALID_VALUE;
+    p->autocontrast_pending = p->s.contrast_enabled != 0;
+    return HV_OK;
+}
+
+hv_status hv_pipe_sync(hv_pipe* p)
+{
+    if (!p)
+        return HV_INVALID_VALUE;
+    HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return HV_OK;
+}
+
+hv_status hv_pipe_get_contrast_range(hv_pipe* p, float* min_out, float* max_out)
+{
+    if (!p)
+        return HV_INVALID_VALUE;
+    float r[2];
+    HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    HV_CUDA_TRY(cudaMemcpy(r, p->range, sizeof(r), cudaMemcpyDeviceToHost));
+    if (min_out)
+        *min_out = r[0];
+    if (max_out)
+        *max_out = r[1];
+    return HV_OK;
+}
+
+hv_status hv_pipe_get_float_frame(hv_pipe* p, float* dst)
+{
+    if (!p || !dst)
+        return HV_INVALID_VALUE;
+    if (!p->last_frame_valid)
+        return HV_NO_IN_DATA;
+    HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    HV_CUDA_TRY(cudaMemcpy(dst, p->post, p->HW * sizeof(float), cudaMemcpyDeviceToHost));
+    return HV_OK;
+}
+
+hv_status hv_pipe_get_ring(hv_pipe* p, void* dst_host, int32_t* start, int32_t* size)
+{
+    if (!p)
+        return HV_INVALID_VALUE;
+    HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    if (dst_host)
+        HV_CUDA_TRY(cudaMemcpy(dst_host, p->ring, p->HW * p->T * sizeof(float2), cudaMemcpyDeviceToHost));
+    if (start)
+        *start = p->ring_start;
+    if (size)
+        *size = p->ring_size;
+    return HV_OK;
+}
+
+uint64_t hv_pipe_kernel_launches(hv_pipe* p)
+{
+    return p ? launch_count() - p->launches0 : 0;
+}
+
+void* hv_pipe_stream(hv_pipe* p) { return p ? static_cast<void*>(p->stream) : nullptr; }
+
+}  // extern "C"

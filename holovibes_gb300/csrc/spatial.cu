@@ -1,0 +1,437 @@
+// Spatial stage: lenses, fused convert + 2-D FFT passes, Fresnel / angular-spectrum propagation.
+//
+// Reference behaviour (Holovibes):
+//   convert        Backend/cuda_sources/tools_conversion.cu:107-171
+//   Fresnel lens   Backend/cuda_sources/masks.cu:7-29, fresnel_transform.cu:14-63
+//   AS lens        Backend/cuda_sources/masks.cu:31-59, angular_spectrum.cu:14-31, fourier_transform.cc:121-137
+//   Fresnel        Backend/cuda_sources/fresnel_transform.cu:65-83   (x*L then forward FFT2, no 1/N)
+//   angular spec.  Backend/cuda_sources/angular_spectrum.cu:33-63     (FFT2, *G, inverse FFT2, /(H*W))
+//   ring enqueue   Backend/sources/data_struct/queue.cc:332-380
+//
+// GB300 design: no cuFFT. A batch of B frames goes through two or three shared-memory passes:
+//   row pass   : raw u8/u16/f32 -> complex (+ Fresnel lens) -> forward row FFT
+//   column pass: forward column FFT (+ transfer function G, inverse column FFT for AS)
+//   row pass   : inverse row FFT * 1/(H*W) (AS only)
+// and the last pass writes straight into the time-ring slots, so the reference's separate
+// mask, divide and ring-copy passes disappear.
+#include <math.h>
+
+#include "fft_smem.cuh"
+#include "hv_internal.h"
+
+namespace hv {
+
+// ====================================================================================== lenses
+
+__global__ void k_fresnel_lens(float2* out, int W, int H, double lam, double z, double pixel_size_um, int mode)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= W || y >= H)
+        return;
+    const int S = W > H ? W : H;
+    // centre crop of the S x S lens (fresnel_transform.cu:37-62)
+    const int si = (H > W) ? x + (S - W) / 2 : x;
+    const int sj = (W > H) ? y + (S - H) / 2 : y;
+    float2 v;
+    if (mode == HV_LENS_REF32)
+    {
+        const float lam32 = static_cast<float>(lam), z32 = static_cast<float>(z);
+        const float c = static_cast<float>(M_PI / static_cast<double>(__fmul_rn(lam32, z32)));
+        const float dx = __fmul_rn(static_cast<float>(pixel_size_um), 1.0e-6f);
+        const float xf = __fmul_rn(__fsub_rn(static_cast<float>(si), static_cast<float>(S >> 1)), dx);
+        const float yf = __fmul_rn(__fsub_rn(static_cast<float>(sj), static_cast<float>(S >> 1)), dx);
+        const float cs = __fmul_rn(c, __fadd_rn(__fmul_rn(xf, xf), __fmul_rn(yf, yf)));
+        v = make_float2(cosf(cs), sinf(cs));
+    }
+    else
+    {
+        const double dx = pixel_size_um * 1e-6;
+        const double xd = (si - (S >> 1)) * dx;
+        const double yd = (sj - (S >> 1)) * dx;
+        double ph = M_PI / (lam * z) * (xd * xd + yd * yd);
+        ph = fmod(ph, 2.0 * M_PI);
+        double s, c;
+        sincos(ph, &s, &c);
+        v = make_float2(static_cast<float>(c), static_cast<float>(s));
+    }
+    out[static_cast<size_t>(y) * W + x] = v;
+}
+
+__global__ void k_spectral_lens(float2* out, int W, int H, double lam, double z, double pixel_size_um, int mode)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= W || y >= H)
+        return;
+    float2 v;
+    if (mode == HV_LENS_REF32)
+    {
+        const float lam32 = static_cast<float>(lam), z32 = static_cast<float>(z);
+        const float step = __fmul_rn(static_cast<float>(pixel_size_um), 1e-6f);
+        const float u_step = __fdiv_rn(1.0f, __fmul_rn(static_cast<float>(W), step));
+        const float v_step = __fdiv_rn(1.0f, __fmul_rn(static_cast<float>(H), step));
+        const float u = __fmul_rn(static_cast<float>(x - (W >> 1)), u_step);
+        const float vv = __fmul_rn(static_cast<float>(y - (H >> 1)), v_step);
+        float tmp = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(lam32, lam32), __fadd_rn(__fmul_rn(u, u), __fmul_rn(vv, vv))));
+        if (tmp < 0.0f)
+            tmp = 0.0f;
+        const double ph_d = __dmul_rn(__ddiv_rn(__dmul_rn(2.0 * M_PI, static_cast<double>(z32)), static_cast<double>(lam32)),
+                                      static_cast<double>(__fsqrt_rn(tmp)));
+        const float ph = static_cast<float>(ph_d);
+        v = make_float2(cosf(ph), sinf(ph));
+    }
+    else
+    {
+        const double step = pixel_size_um * 1e-6;
+        const double u = (x - (W >> 1)) / (W * step);
+        const double vv = (y - (H >> 1)) / (H * step);
+        double tmp = 1.0 - lam * lam * (u * u + vv * vv);
+        if (tmp < 0.0)
+            tmp = 0.0;
+        double ph = 2.0 * M_PI * z / lam * sqrt(tmp);
+        ph = fmod(ph, 2.0 * M_PI);
+        double s, c;
+        sincos(ph, &s, &c);
+        v = make_float2(static_cast<float>(c), static_cast<float>(s));
+    }
+    // quadrant swap into FFT layout (shift_corners on the lens, fourier_transform.cc:134)
+    const int xs = (x + W / 2) % W;
+    const int ys = (y + H / 2) % H;
+    out[static_cast<size_t>(ys) * W + xs] = v;
+}
+
+// ====================================================================================== FFT passes
+
+struct RowPass
+{
+    const void* in;        // batch of frames, row-major rows x N
+    int in_kind;           // InKind
+    size_t in_frame;       // elements between input frames
+    float2* out;
+    FrameMap out_map;      // output frame slots
+    const float2* premul;  // rows x N multiplier applied before the transform (or null)
+    int rows;              // rows per frame
+    int inverse;           // 1: conj in / conj out (unnormalised inverse)
+    float scale;
+};
+
+template <int N, int F>
+__global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass p)
+{
+    using Tl = fft::Tile<N, F, false>;
+    extern __shared__ float2 smem[];
+    float2* tw = smem;
+    float2* sm = smem + N;
+    fft::fill_twiddles<N>(tw, Tl::NT);
+    __syncthreads();
+
+    const int b = blockIdx.y;
+    const int row0 = blockIdx.x * F;
+    const size_t in_base = static_cast<size_t>(b) * p.in_frame;
+    const int rows = p.rows;
+    const int kind = p.in_kind;
+    const bool inv = p.inverse != 0;
+    auto src = [&](int f, int n) -> float2 {
+        const int y = row0 + f;
+        if (y >= rows)
+            return make_float2(0.f, 0.f);
+        const size_t e = static_cast<size_t>(y) * N + n;
+        float2 v = load_pixel(p.in, in_base + e, kind);
+        if (p.premul)
+            v = cmul(v, __ldg(p.premul + e));
+        return inv ? cconj(v) : v;
+    };
+    float2* out = p.out + p.out_map.offset(b);
+    const float sc = p.scale;
+    auto dst = [&](int f, int n, float2 v) {
+        const int y = row0 + f;
+        if (y >= rows)
+            return;
+        if (inv)
+            v = cconj(v);
+        out[static_cast<size_t>(y) * N + n] = cscale(v, sc);
+    };
+    Tl::run(sm, tw, src, dst);
+}
+
+struct ColPass
+{
+    const float2* in;
+    size_t in_frame;
+    float2* out;
+    FrameMap out_map;
+    const float2* postmul;  // rows x width multiplier applied between forward and inverse (AS), or null
+    int width;              // row length (number of columns)
+    int mode;               // 0 forward, 1 inverse, 2 forward * postmul then inverse
+    float scale;
+};
+
+template <int N, int F>
+__global__ void __launch_bounds__(fft::Tile<N, F, true>::NT) k_fft_cols(ColPass p)
+{
+    using Tl = fft::Tile<N, F, true>;
+    extern __shared__ float2 smem[];
+    float2* tw = smem;
+    float2* sm = smem + N;
+    fft::fill_twiddles<N>(tw, Tl::NT);
+    __syncthreads();
+
+    const int b = blockIdx.y;
+    const int c0 = blockIdx.x * F;
+    const int W = p.width;
+    const float2* in = p.in + static_cast<size_t>(b) * p.in_frame;
+    float2* out = p.out + p.out_map.offset(b);
+    const float sc = p.scale;
+    if (p.mode == 2)
+    {
+        auto src = [&](int f, int n) -> float2 {
+            const int c = c0 + f;
+            return (c < W) ? in[static_cast<size_t>(n) * W + c] : make_float2(0.f, 0.f);
+        };
+        const float2* G = p.postmul;
+        // forward result * G, conjugated for the inverse transform, parked in shared memory
+        auto mid = [&](int f, int n, float2 v) {
+            const int c = c0 + f;
+            const float2 g = (c < W) ? __ldg(G + static_cast<size_t>(n) * W + c) : make_float2(0.f, 0.f);
+            sm[Tl::addr(f, n)] = cconj(cmul(v, g));
+        };
+        Tl::run(sm, tw, src, mid);
+        __syncthreads();
+        auto src2 = [&](int f, int n) -> float2 { return sm[Tl::addr(f, n)]; };
+        auto dst2 = [&](int f, int n, float2 v) {
+            const int c = c0 + f;
+            if (c < W)
+                out[static_cast<size_t>(n) * W + c] = cscale(cconj(v), sc);
+        };
+        Tl::run(sm, tw, src2, dst2);
+    }
+    else
+    {
+        const bool inv = p.mode == 1;
+        auto src = [&](int f, int n) -> float2 {
+            const int c = c0 + f;
+            if (c >= W)
+                return make_float2(0.f, 0.f);
+            const float2 v = in[static_cast<size_t>(n) * W + c];
+            return inv ? cconj(v) : v;
+        };
+        auto dst = [&](int f, int n, float2 v) {
+            const int c = c0 + f;
+            if (c >= W)
+                return;
+            if (inv)
+                v = cconj(v);
+            out[static_cast<size_t>(n) * W + c] = cscale(v, sc);
+        };
+        Tl::run(sm, tw, src, dst);
+    }
+}
+
+// Raw -> complex into ring slots (space transformation NONE).
+__global__ void k_convert(const void* in, int kind, size_t frame_px, int batch, float2* ring, FrameMap map)
+{
+    const size_t total = frame_px * batch;
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        const int b = static_cast<int>(e / frame_px);
+        const size_t px = e - static_cast<size_t>(b) * frame_px;
+        ring[map.offset(b) + px] = load_pixel(in, e, kind);
+    }
+}
+
+// ====================================================================================== dispatch
+
+namespace {
+
+// Rows per CTA for the row pass (about 256 threads) and columns per CTA for the column pass.
+template <int N>
+constexpr int row_lanes()
+{
+    constexpr int per_row = N / fft::Plan<N>::E;
+    return per_row >= 256 ? 1 : 256 / per_row;
+}
+template <int N>
+constexpr int col_lanes()
+{
+    constexpr int E = fft::Plan<N>::E;
+    // at most 512 threads and 128 KB of tile per CTA
+    int f = 16;
+    while (f > 1 && (f * N / E > 512 || f * N * 8 > 128 * 1024))
+        f /= 2;
+    return f;
+}
+
+template <int N>
+hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
+{
+    constexpr int F = row_lanes<N>();
+    using Tl = fft::Tile<N, F, false>;
+    const size_t smem = (static_cast<size_t>(N) + static_cast<size_t>(F) * N) * sizeof(float2);
+    if (smem > 48 * 1024)
+        HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_rows<N, F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+    dim3 grid((p.rows + F - 1) / F, nframes);
+    k_fft_rows<N, F><<<grid, Tl::NT, smem, st>>>(p);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+template <int N>
+hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
+{
+    constexpr int F = col_lanes<N>();
+    using Tl = fft::Tile<N, F, true>;
+    const size_t smem = (static_cast<size_t>(N) + static_cast<size_t>(F) * N) * sizeof(float2);
+    if (smem > 48 * 1024)
+        HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_cols<N, F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+    dim3 grid((p.width + F - 1) / F, nframes);
+    k_fft_cols<N, F><<<grid, Tl::NT, smem, st>>>(p);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+#define HV_FFT_SIZES(X)                                                                                                \
+    X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(48) X(96) X(192) X(384) X(768) X(1536)
+
+}  // namespace
+
+bool fft_size_supported(int n)
+{
+    switch (n)
+    {
+#define HV_CASE(N)                                                                                                     \
+    case N: return true;
+        HV_FFT_SIZES(HV_CASE)
+#undef HV_CASE
+    default: return false;
+    }
+}
+
+hv_status fft_rows(const RowPass& p, int N, int nframes, cudaStream_t st)
+{
+    switch (N)
+    {
+#define HV_CASE(NN)                                                                                                    \
+    case NN: return launch_rows<NN>(p, nframes, st);
+        HV_FFT_SIZES(HV_CASE)
+#undef HV_CASE
+    default: set_last_error_msg("unsupported FFT length"); return HV_ERR_UNSUPPORTED;
+    }
+}
+
+hv_status fft_cols(const ColPass& p, int N, int nframes, cudaStream_t st)
+{
+    switch (N)
+    {
+#define HV_CASE(NN)                                                                                                    \
+    case NN: return launch_cols<NN>(p, nframes, st);
+        HV_FFT_SIZES(HV_CASE)
+#undef HV_CASE
+    default: set_last_error_msg("unsupported FFT length"); return HV_ERR_UNSUPPORTED;
+    }
+}
+
+hv_status make_fresnel_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st)
+{
+    dim3 block(128), grid((W + 127) / 128, H);
+    k_fresnel_lens<<<grid, block, 0, st>>>(lens, W, H, lam, z, ps, mode);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+hv_status make_spectral_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st)
+{
+    dim3 block(128), grid((W + 127) / 128, H);
+    k_spectral_lens<<<grid, block, 0, st>>>(lens, W, H, lam, z, ps, mode);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+int raw_kind(int raw_bytes, int big_endian)
+{
+    switch (raw_bytes)
+    {
+    case 1: return IN_U8;
+    case 2: return big_endian ? IN_U16_BE : IN_U16;
+    case 4: return IN_F32;
+    case 8: return IN_C64;
+    default: return -1;
+    }
+}
+
+hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
+                            float2* work, float2* ring, int slot0, int nslots, cudaStream_t st)
+{
+    const size_t HW = static_cast<size_t>(W) * H;
+    const FrameMap ring_map{HW, slot0, nslots};
+    const FrameMap work_map{HW, 0, batch > 0 ? batch : 1};
+    if (batch <= 0)
+        return HV_OK;
+    if (space == HV_SPACE_NONE)
+    {
+        const size_t total = HW * batch;
+        const int block = 256;
+        const int grid = static_cast<int>((total + block - 1) / block < 152 * 16 ? (total + block - 1) / block : 152 * 16);
+        k_convert<<<grid, block, 0, st>>>(raw, kind, HW, batch, ring, ring_map);
+        HV_LAUNCH_CHECK();
+        count_launch();
+        return HV_OK;
+    }
+    if (!fft_size_supported(W) || !fft_size_supported(H))
+    {
+        set_last_error_msg("frame width/height not supported by the shared-memory FFT");
+        return HV_ERR_UNSUPPORTED;
+    }
+    if (space == HV_SPACE_FRESNELTR)
+    {
+        // x*L, forward rows -> work; forward columns -> ring slots
+        RowPass r{raw, kind, HW, work, work_map, lens, H, 0, 1.0f};
+        hv_status s = fft_rows(r, W, batch, st);
+        if (s != HV_OK)
+            return s;
+        ColPass c{work, HW, ring, ring_map, nullptr, W, 0, 1.0f};
+        return fft_cols(c, H, batch, st);
+    }
+    if (space == HV_SPACE_ANGULARSP)
+    {
+        // forward rows -> work; columns: forward, *G, inverse (in place); inverse rows /(H*W) -> ring
+        RowPass r{raw, kind, HW, work, work_map, nullptr, H, 0, 1.0f};
+        hv_status s = fft_rows(r, W, batch, st);
+        if (s != HV_OK)
+            return s;
+        ColPass c{work, HW, work, work_map, lens, W, 2, 1.0f};
+        s = fft_cols(c, H, batch, st);
+        if (s != HV_OK)
+            return s;
+        RowPass r2{work, IN_C64, HW, ring, ring_map, nullptr, H, 1, 1.0f / static_cast<float>(HW)};
+        return fft_rows(r2, W, batch, st);
+    }
+    set_last_error_msg("unknown space transformation");
+    return HV_INVALID_VALUE;
+}
+
+hv_status fft2d(const float2* in, float2* out, int n0, int n1, int batch, int inverse, float scale, cudaStream_t st)
+{
+    if (!fft_size_supported(n0) || !fft_size_supported(n1))
+    {
+        set_last_error_msg("FFT length not supported");
+        return HV_ERR_UNSUPPORTED;
+    }
+    const size_t HW = static_cast<size_t>(n0) * n1;
+    const FrameMap map{HW, 0, batch};
+    RowPass r{in, IN_C64, HW, out, map, nullptr, n0, inverse, 1.0f};
+    hv_status s = fft_rows(r, n1, batch, st);
+    if (s != HV_OK)
+        return s;
+    ColPass c{out, HW, out, map, nullptr, n1, inverse ? 1 : 0, scale};
+    return fft_cols(c, n0, batch, st);
+}
+
+}  // namespace hv

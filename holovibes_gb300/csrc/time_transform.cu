@@ -1,0 +1,579 @@
+// Time transforms over the ring of T complex frames, fused with the view.
+//
+// Reference behaviour (Holovibes):
+//   STFT           Backend/cuda_sources/stft.cu:9-15 with the plan of Backend/sources/core/icompute.cc:109-115:
+//                  a forward T-point DFT along time over the ring STORAGE order, all T bins.
+//   PCA            Backend/sources/compute/matrix_operations.cc:9-103, fourier_transform.cc:340-377:
+//                  cov = H^H H (Cgemm3m), cusolverDnCheevd (ascending), p_acc = H V (Cgemm3m).
+//   p range        Backend/sources/compute/converts.cc:76-92
+//   views          Backend/cuda_sources/tools_conversion.cu:11-103,199-232 (mean over [pmin, pmax]
+//                  of hypotf, hypotf^2 or atan2)
+//   PCA x131071    Backend/sources/compute/converts.cc:50-62
+//
+// GB300 design: only the K = pmax - pmin + 1 bins the view reads are computed, as a dense
+// contraction X[k][pix] = sum_t W[k][t] ring[t][pix] with W = DFT twiddles (STFT) or the selected
+// eigenvector columns (PCA); the view, the bin average, the PCA scale, the fftshift permutation
+// and the renormalisation partial sums are fused into the same kernel, so the T x HW p_acc
+// buffer of the reference never exists.
+#include <math.h>
+
+#include "hv_common.cuh"
+#include "hv_internal.h"
+
+namespace hv {
+
+constexpr int TV_THREADS = 256;
+constexpr int TV_KC = 16;  // bins per register chunk
+
+__device__ __forceinline__ float view_value(float2 X, int img_type)
+{
+    if (img_type == HV_IMG_MODULUS)
+        return hypotf(X.x, X.y);
+    if (img_type == HV_IMG_SQUARED_MODULUS)
+    {
+        const float t = hypotf(X.x, X.y);
+        return t * t;
+    }
+    return atan2f(X.y, X.x);
+}
+
+// ring: [T][HW] complex; weights: [K][T] complex. One pixel per thread.
+__global__ void __launch_bounds__(TV_THREADS) k_time_view(const float2* __restrict__ ring, int T, int W, int H,
+                                                           const float2* __restrict__ weights, int K, int img_type,
+                                                           float scale, int shift, float* __restrict__ out,
+                                                           double* __restrict__ partials)
+{
+    extern __shared__ __align__(16) float2 wsm[];  // [T][TV_KC], read as float4 pairs
+    __shared__ double red[TV_THREADS / 32];
+    const size_t HW = static_cast<size_t>(W) * H;
+    const size_t pix = blockIdx.x * static_cast<size_t>(TV_THREADS) + threadIdx.x;
+    const bool valid = pix < HW;
+    float acc_view = 0.f;
+    for (int k0 = 0; k0 < K; k0 += TV_KC)
+    {
+        __syncthreads();
+        for (int e = threadIdx.x; e < T * TV_KC; e += TV_THREADS)
+        {
+            const int t = e / TV_KC, kk = e - t * TV_KC;
+            const int k = k0 + kk;
+            wsm[e] = (k < K) ? weights[static_cast<size_t>(k) * T + t] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        float2 acc[TV_KC];
+#pragma unroll
+        for (int kk = 0; kk < TV_KC; ++kk)
+            acc[kk] = make_float2(0.f, 0.f);
+        const int kn = (K - k0) < TV_KC ? (K - k0) : TV_KC;
+        if (valid)
+        {
+            const float2* src = ring + pix;
+            if (kn == 1)
+            {
+#pragma unroll 8
+                for (int t = 0; t < T; ++t)
+                {
+                    const float2 x = __ldg(src + static_cast<size_t>(t) * HW);
+                    const float2 w = wsm[t * TV_KC];
+                    acc[0].x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc[0].x));
+                    acc[0].y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc[0].y));
+                }
+            }
+            else
+            {
+#pragma unroll 2
+                for (int t = 0; t < T; ++t)
+                {
+                    const float2 x = __ldg(src + static_cast<size_t>(t) * HW);
+                    const float4* w4 = reinterpret_cast<const float4*>(wsm + t * TV_KC);
+#pragma unroll
+                    for (int kk = 0; kk < TV_KC; kk += 2)
+                    {
+                        const float4 w = w4[kk / 2];
+                        acc[kk].x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc[kk].x));
+                        acc[kk].y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc[kk].y));
+                        acc[kk + 1].x = fmaf(x.x, w.z, fmaf(-x.y, w.w, acc[kk + 1].x));
+                        acc[kk + 1].y = fmaf(x.x, w.w, fmaf(x.y, w.z, acc[kk + 1].y));
+                    }
+                }
+            }
+#pragma unroll
+            for (int kk = 0; kk < TV_KC; ++kk)
+                if (kk < kn)
+                    acc_view += view_value(acc[kk], img_type);
+        }
+    }
+    float v = 0.f;
+    if (valid)
+    {
+        v = acc_view / static_cast<float>(K);
+        if (scale != 1.0f)
+            v = v * scale;
+        const int x = static_cast<int>(pix % W);
+        const int y = static_cast<int>(pix / W);
+        size_t dst = pix;
+        if (shift)
+            dst = static_cast<size_t>((y + H / 2) % H) * W + (x + W / 2) % W;
+        out[dst] = v;
+    }
+    if (partials)
+    {
+        double d = valid ? static_cast<double>(v) : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            d += __shfl_down_sync(0xffffffffu, d, o);
+        if ((threadIdx.x & 31) == 0)
+            red[threadIdx.x >> 5] = d;
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            double s = 0.0;
+            for (int i = 0; i < TV_THREADS / 32; ++i)
+                s += red[i];
+            partials[blockIdx.x] = s;
+        }
+    }
+}
+
+int time_view_partials(int W, int H)
+{
+    const size_t HW = static_cast<size_t>(W) * H;
+    return static_cast<int>((HW + TV_THREADS - 1) / TV_THREADS);
+}
+
+hv_status time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type, float scale,
+                    int shift, float* out, double* partials, cudaStream_t st)
+{
+    if (T <= 0 || K <= 0 || W <= 0 || H <= 0)
+    {
+        set_last_error_msg("time_view: bad sizes");
+        return HV_INVALID_VALUE;
+    }
+    if (shift && ((W & 1) || (H & 1)))
+    {
+        set_last_error_msg("fftshift needs even width and height");
+        return HV_INVALID_VALUE;
+    }
+    const size_t smem = static_cast<size_t>(T) * TV_KC * sizeof(float2);
+    if (smem > 200 * 1024)
+    {
+        set_last_error_msg("time window too large for the time-view kernel");
+        return HV_ERR_UNSUPPORTED;
+    }
+    if (smem > 48 * 1024)
+        HV_CUDA_TRY(cudaFuncSetAttribute(k_time_view, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+    const int grid = time_view_partials(W, H);
+    k_time_view<<<grid, TV_THREADS, smem, st>>>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+// ------------------------------------------------------------------------------ weights
+
+__global__ void k_stft_weights(float2* w, int T, int pmin, int K)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= K * T)
+        return;
+    const int k = e / T, t = e - k * T;
+    const long long m = (static_cast<long long>(pmin + k) * t) % T;
+    double s, c;
+    sincospi(-2.0 * static_cast<double>(m) / static_cast<double>(T), &s, &c);
+    w[e] = make_float2(static_cast<float>(c), static_cast<float>(s));
+}
+
+__global__ void k_delta_weights(float2* w, int T, int pmin, int K)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= K * T)
+        return;
+    const int k = e / T, t = e - k * T;
+    w[e] = make_float2(t == pmin + k ? 1.f : 0.f, 0.f);
+}
+
+hv_status stft_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st)
+{
+    const int K = pmax - pmin + 1;
+    if (K <= 0 || T <= 0)
+        return HV_INVALID_VALUE;
+    k_stft_weights<<<(K * T + 255) / 256, 256, 0, st>>>(weights, T, pmin, K);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+hv_status delta_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st)
+{
+    const int K = pmax - pmin + 1;
+    if (K <= 0 || T <= 0)
+        return HV_INVALID_VALUE;
+    k_delta_weights<<<(K * T + 255) / 256, 256, 0, st>>>(weights, T, pmin, K);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+// ------------------------------------------------------------------------------ PCA covariance
+// C[i][j] = sum_pix conj(H[pix][i]) H[pix][j], H[pix][t] = ring[t][pix]. Split-K over pixel
+// chunks: CTA (tile, chunk) accumulates a 32 x 32 complex tile in FP32 registers, partial tiles
+// are summed in FP64 by k_cov_reduce, which also mirrors the Hermitian triangle.
+
+constexpr int COV_TILE = 32;
+constexpr int COV_THREADS = 256;
+constexpr int COV_PX = 32;  // pixels per shared-memory stage
+
+struct CovPlan
+{
+    int tiles1d, ntiles, chunks;
+    size_t chunk_px;
+};
+
+static CovPlan cov_plan(int T, size_t npix)
+{
+    CovPlan p;
+    p.tiles1d = (T + COV_TILE - 1) / COV_TILE;
+    p.ntiles = p.tiles1d * (p.tiles1d + 1) / 2;
+    int chunks = (152 * 8 + p.ntiles - 1) / p.ntiles;
+    const size_t max_chunks = (npix + COV_PX - 1) / COV_PX;
+    if (static_cast<size_t>(chunks) > max_chunks)
+        chunks = static_cast<int>(max_chunks);
+    if (chunks < 1)
+        chunks = 1;
+    p.chunks = chunks;
+    p.chunk_px = ((npix + chunks - 1) / chunks + COV_PX - 1) / COV_PX * COV_PX;
+    return p;
+}
+
+__global__ void __launch_bounds__(COV_THREADS) k_cov_partial(const float2* __restrict__ ring, int T, size_t npix,
+                                                              int tiles1d, size_t chunk_px, float2* __restrict__ part)
+{
+    __shared__ float2 A[COV_PX][COV_TILE + 1];
+    __shared__ float2 B[COV_PX][COV_TILE + 1];
+    // tile index -> (ti, tj) with ti <= tj
+    int t = blockIdx.x, ti = 0;
+    while (t >= tiles1d - ti)
+    {
+        t -= tiles1d - ti;
+        ++ti;
+    }
+    const int tj = ti + t;
+    const int chunk = blockIdx.y;
+    const size_t p0 = chunk * chunk_px;
+    const size_t p1 = (p0 + chunk_px < npix) ? p0 + chunk_px : npix;
+    // thread -> 2 x 2 outputs: rows ri*2 + {0,1}, cols cj*2 + {0,1}
+    const int ri = threadIdx.x / 16, cj = threadIdx.x % 16;
+    float2 acc[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+            acc[a][b] = make_float2(0.f, 0.f);
+    for (size_t px0 = p0; px0 < p1; px0 += COV_PX)
+    {
+        __syncthreads();
+        for (int e = threadIdx.x; e < COV_PX * COV_TILE; e += COV_THREADS)
+        {
+            const int c = e / COV_PX, pp = e % COV_PX;  // pixel fastest: coalesced ring reads
+            const size_t px = px0 + pp;
+            const int ia = ti * COV_TILE + c, ib = tj * COV_TILE + c;
+            A[pp][c] = (px < p1 && ia < T) ? __ldg(ring + static_cast<size_t>(ia) * npix + px) : make_float2(0.f, 0.f);
+            B[pp][c] = (px < p1 && ib < T) ? __ldg(ring + static_cast<size_t>(ib) * npix + px) : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int pp = 0; pp < COV_PX; ++pp)
+        {
+            const float2 a0 = A[pp][ri * 2], a1 = A[pp][ri * 2 + 1];
+            const float2 b0 = B[pp][cj * 2], b1 = B[pp][cj * 2 + 1];
+            // conj(a) * b
+            acc[0][0].x = fmaf(a0.x, b0.x, fmaf(a0.y, b0.y, acc[0][0].x));
+            acc[0][0].y = fmaf(a0.x, b0.y, fmaf(-a0.y, b0.x, acc[0][0].y));
+            acc[0][1].x = fmaf(a0.x, b1.x, fmaf(a0.y, b1.y, acc[0][1].x));
+            acc[0][1].y = fmaf(a0.x, b1.y, fmaf(-a0.y, b1.x, acc[0][1].y));
+            acc[1][0].x = fmaf(a1.x, b0.x, fmaf(a1.y, b0.y, acc[1][0].x));
+            acc[1][0].y = fmaf(a1.x, b0.y, fmaf(-a1.y, b0.x, acc[1][0].y));
+            acc[1][1].x = fmaf(a1.x, b1.x, fmaf(a1.y, b1.y, acc[1][1].x));
+            acc[1][1].y = fmaf(a1.x, b1.y, fmaf(-a1.y, b1.x, acc[1][1].y));
+        }
+    }
+    // part layout: [chunk][tile][32][32]
+    float2* dst = part + (static_cast<size_t>(chunk) * gridDim.x + blockIdx.x) * COV_TILE * COV_TILE;
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+            dst[(ri * 2 + a) * COV_TILE + cj * 2 + b] = acc[a][b];
+}
+
+__global__ void k_cov_reduce(const float2* __restrict__ part, int T, int tiles1d, int ntiles, int chunks,
+                             double2* __restrict__ cov)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;  // over T*T
+    if (e >= T * T)
+        return;
+    int i = e / T, j = e % T;
+    const bool mirror = i > j;  // lower triangle: conj of (j, i)
+    if (mirror)
+    {
+        const int s = i;
+        i = j;
+        j = s;
+    }
+    const int ti = i / COV_TILE, tj = j / COV_TILE;
+    // tile index of (ti, tj), ti <= tj
+    const int tile = ti * tiles1d - ti * (ti - 1) / 2 + (tj - ti);
+    const int li = i % COV_TILE, lj = j % COV_TILE;
+    double re = 0.0, im = 0.0;
+    for (int c = 0; c < chunks; ++c)
+    {
+        const float2 v = part[(static_cast<size_t>(c) * ntiles + tile) * COV_TILE * COV_TILE + li * COV_TILE + lj];
+        re += v.x;
+        im += v.y;
+    }
+    // cov[i][j] stored row-major at e; both triangles
+    cov[e] = mirror ? make_double2(re, -im) : make_double2(re, im);
+}
+
+size_t pca_cov_workspace(int T, size_t npix)
+{
+    const CovPlan p = cov_plan(T, npix);
+    return static_cast<size_t>(p.chunks) * p.ntiles * COV_TILE * COV_TILE * sizeof(float2);
+}
+
+hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st)
+{
+    if (T <= 0 || npix == 0)
+        return HV_INVALID_VALUE;
+    const CovPlan p = cov_plan(T, npix);
+    float2* part = static_cast<float2*>(work);
+    dim3 grid(p.ntiles, p.chunks);
+    k_cov_partial<<<grid, COV_THREADS, 0, st>>>(ring, T, npix, p.tiles1d, p.chunk_px, part);
+    HV_LAUNCH_CHECK();
+    k_cov_reduce<<<(T * T + 255) / 256, 256, 0, st>>>(part, T, p.tiles1d, p.ntiles, p.chunks, cov);
+    HV_LAUNCH_CHECK();
+    count_launch(2);
+    return HV_OK;
+}
+
+// ------------------------------------------------------------------------------ FP64 Jacobi
+// Cyclic two-sided Jacobi with the round-robin (tournament) ordering: each step rotates T/2
+// disjoint (p, q) pairs in parallel. A rotation first turns A[p][q] real with a phase on index q
+// and then applies the real symmetric Schur rotation (Golub & Van Loan, Alg. 8.4.1), i.e.
+// J = diag(1, e^{-i phi}) R(c, s). Matrix in global memory (row-major, complex128), one CTA.
+// The sweep count is bounded; convergence is tested on the off-diagonal Frobenius norm.
+
+constexpr int JAC_THREADS = 512;
+constexpr int JAC_MAX_SWEEPS = 40;
+
+__device__ __forceinline__ double2 zmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void __launch_bounds__(JAC_THREADS) k_jacobi(double2* A, double2* V, int T, int Tp, double* evals,
+                                                         int* pair_buf, double* rot_buf)
+{
+    // pair_buf: 2*(Tp/2) ints; rot_buf: 4*(Tp/2) doubles (c, s, cos phi, sin phi)
+    __shared__ double red[JAC_THREADS / 32];
+    __shared__ double s_off, s_norm;
+    const int tid = threadIdx.x;
+    // V = I
+    for (int e = tid; e < T * T; e += JAC_THREADS)
+        V[e] = make_double2((e / T) == (e % T) ? 1.0 : 0.0, 0.0);
+    __syncthreads();
+    const int npairs = Tp / 2;
+    for (int sweep = 0; sweep < JAC_MAX_SWEEPS; ++sweep)
+    {
+        // off-diagonal norm and total norm
+        double off = 0.0, nrm = 0.0;
+        for (int e = tid; e < T * T; e += JAC_THREADS)
+        {
+            const double2 a = A[e];
+            const double m = a.x * a.x + a.y * a.y;
+            nrm += m;
+            if ((e / T) != (e % T))
+                off += m;
+        }
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            off += __shfl_down_sync(0xffffffffu, off, o);
+            nrm += __shfl_down_sync(0xffffffffu, nrm, o);
+        }
+        if ((tid & 31) == 0)
+            red[tid >> 5] = off;
+        __syncthreads();
+        if (tid == 0)
+        {
+            double s = 0.0;
+            for (int i = 0; i < JAC_THREADS / 32; ++i)
+                s += red[i];
+            s_off = s;
+        }
+        __syncthreads();
+        if ((tid & 31) == 0)
+            red[tid >> 5] = nrm;
+        __syncthreads();
+        if (tid == 0)
+        {
+            double s = 0.0;
+            for (int i = 0; i < JAC_THREADS / 32; ++i)
+                s += red[i];
+            s_norm = s;
+        }
+        __syncthreads();
+        if (s_off <= 1e-30 * s_norm || s_norm == 0.0)
+            break;
+        for (int step = 0; step < Tp - 1; ++step)
+        {
+            // round-robin pairing: player Tp-1 fixed, others rotate
+            for (int k = tid; k < npairs; k += JAC_THREADS)
+            {
+                int a, b;
+                if (k == 0)
+                {
+                    a = Tp - 1;
+                    b = step % (Tp - 1);
+                }
+                else
+                {
+                    a = (step + k) % (Tp - 1);
+                    b = (step - k + (Tp - 1)) % (Tp - 1);
+                }
+                const int p = a < b ? a : b, q = a < b ? b : a;
+                pair_buf[2 * k] = p;
+                pair_buf[2 * k + 1] = q;
+                double c = 1.0, s = 0.0, cph = 1.0, sph = 0.0;
+                if (q < T)
+                {
+                    const double2 apq = A[p * T + q];
+                    const double mag = hypot(apq.x, apq.y);
+                    const double app = A[p * T + p].x, aqq = A[q * T + q].x;
+                    if (mag > 1e-300 && mag > 1e-18 * sqrt(fabs(app * aqq)))
+                    {
+                        cph = apq.x / mag;
+                        sph = apq.y / mag;
+                        const double tau = (aqq - app) / (2.0 * mag);
+                        const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                        c = 1.0 / sqrt(1.0 + t * t);
+                        s = t * c;
+                    }
+                }
+                rot_buf[4 * k] = c;
+                rot_buf[4 * k + 1] = s;
+                rot_buf[4 * k + 2] = cph;
+                rot_buf[4 * k + 3] = sph;
+            }
+            __syncthreads();
+            // column update A <- A J and V <- V J; J = [[c, s], [-s e^{-i phi}, c e^{-i phi}]]
+            for (int e = tid; e < npairs * T; e += JAC_THREADS)
+            {
+                const int k = e / T, r = e % T;
+                const int p = pair_buf[2 * k], q = pair_buf[2 * k + 1];
+                if (q >= T)
+                    continue;
+                const double c = rot_buf[4 * k], s = rot_buf[4 * k + 1];
+                const double2 em = make_double2(rot_buf[4 * k + 2], -rot_buf[4 * k + 3]);  // e^{-i phi}
+                {
+                    const double2 ap = A[r * T + p], aq = A[r * T + q];
+                    const double2 aqe = zmul(aq, em);
+                    A[r * T + p] = make_double2(c * ap.x - s * aqe.x, c * ap.y - s * aqe.y);
+                    A[r * T + q] = make_double2(s * ap.x + c * aqe.x, s * ap.y + c * aqe.y);
+                }
+                {
+                    const double2 vp = V[r * T + p], vq = V[r * T + q];
+                    const double2 vqe = zmul(vq, em);
+                    V[r * T + p] = make_double2(c * vp.x - s * vqe.x, c * vp.y - s * vqe.y);
+                    V[r * T + q] = make_double2(s * vp.x + c * vqe.x, s * vp.y + c * vqe.y);
+                }
+            }
+            __syncthreads();
+            // row update A <- J^H A: row p <- c A_p - s e^{i phi} A_q, row q <- s A_p + c e^{i phi} A_q
+            for (int e = tid; e < npairs * T; e += JAC_THREADS)
+            {
+                const int k = e / T, col = e % T;
+                const int p = pair_buf[2 * k], q = pair_buf[2 * k + 1];
+                if (q >= T)
+                    continue;
+                const double c = rot_buf[4 * k], s = rot_buf[4 * k + 1];
+                const double2 ep = make_double2(rot_buf[4 * k + 2], rot_buf[4 * k + 3]);  // e^{i phi}
+                const double2 ap = A[p * T + col], aq = A[q * T + col];
+                const double2 aqe = zmul(aq, ep);
+                A[p * T + col] = make_double2(c * ap.x - s * aqe.x, c * ap.y - s * aqe.y);
+                A[q * T + col] = make_double2(s * ap.x + c * aqe.x, s * ap.y + c * aqe.y);
+            }
+            __syncthreads();
+            // exact zeros / real diagonal for the rotated pairs
+            for (int k = tid; k < npairs; k += JAC_THREADS)
+            {
+                const int p = pair_buf[2 * k], q = pair_buf[2 * k + 1];
+                if (q >= T || rot_buf[4 * k + 1] == 0.0)
+                    continue;
+                A[p * T + q] = make_double2(0.0, 0.0);
+                A[q * T + p] = make_double2(0.0, 0.0);
+                A[p * T + p].y = 0.0;
+                A[q * T + q].y = 0.0;
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = tid; i < T; i += JAC_THREADS)
+        evals[i] = A[i * T + i].x;
+}
+
+// Sort eigenpairs ascending (rank = number of smaller values, ties by index), write the
+// eigenvectors column-major like cusolverDnCheevd (evec[t + j*T]) and the PCA weights.
+__global__ void k_eig_sort(const double* evals_in, const double2* V, int T, double* evals, double2* evecs, int pmin,
+                           int pmax, float2* weights)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < T; i += gridDim.x * blockDim.x)
+    {
+        const double ei = evals_in[i];
+        int rank = 0;
+        for (int j = 0; j < T; ++j)
+        {
+            const double ej = evals_in[j];
+            rank += (ej < ei) || (ej == ei && j < i);
+        }
+        evals[rank] = ei;
+        for (int t = 0; t < T; ++t)
+        {
+            const double2 v = V[t * T + i];  // column i of V (row-major)
+            evecs[static_cast<size_t>(rank) * T + t] = v;
+            if (weights && rank >= pmin && rank <= pmax)
+                weights[static_cast<size_t>(rank - pmin) * T + t] =
+                    make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+        }
+    }
+}
+
+size_t pca_eigh_workspace(int T)
+{
+    const int Tp = (T % 2) ? T + 1 : T;
+    return static_cast<size_t>(T) * T * sizeof(double2) + static_cast<size_t>(2 * Tp) * sizeof(double) +
+           static_cast<size_t>(T) * sizeof(double) + static_cast<size_t>(Tp) * sizeof(int) + 256;
+}
+
+hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
+                   cudaStream_t st)
+{
+    if (T <= 0 || !work)
+        return HV_INVALID_VALUE;
+    const int Tp = (T % 2) ? T + 1 : T;
+    char* base = static_cast<char*>(work);
+    double2* V = reinterpret_cast<double2*>(base);
+    size_t off = static_cast<size_t>(T) * T * sizeof(double2);
+    double* rot = reinterpret_cast<double*>(base + off);
+    off += static_cast<size_t>(2 * Tp) * sizeof(double);
+    double* ev_unsorted = reinterpret_cast<double*>(base + off);
+    off += static_cast<size_t>(T) * sizeof(double);
+    int* pairs = reinterpret_cast<int*>(base + off);
+    k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);
+    HV_LAUNCH_CHECK();
+    k_eig_sort<<<(T + 127) / 128, 128, 0, st>>>(ev_unsorted, V, T, evals, evecs, pmin, pmax, weights);
+    HV_LAUNCH_CHECK();
+    count_launch(2);
+    return HV_OK;
+}
+
+}  // namespace hv

@@ -1,0 +1,263 @@
+/* holovibes_gb300 C ABI.
+ *
+ * A GB300-native (sm_103a) implementation of the Holovibes hologram path:
+ * raw camera frames -> complex -> Fresnel / angular-spectrum propagation -> time ring ->
+ * STFT bins / PCA -> modulus / squared modulus / argument (+ 2-D unwrap) -> renormalisation ->
+ * fftshift -> image accumulation -> percentile contrast -> uint16.
+ *
+ * Two levels are exported:
+ *   1. The Pipe (hv_pipe_*): the drop-in for the reference's Pipe/ICompute engine
+ *      (Backend/includes/core/pipe.hh:70-125, Backend/sources/core/pipe.cc:255-387,650-676),
+ *      fed like its BatchInputQueue and drained like its output Queue.
+ *   2. Compute steps (hv_*): stream-ordered calls on caller-owned device buffers, one per
+ *      reference CUDA-layer function they replace (cited per function).
+ *
+ * Conventions: plain pointers and sizes, no exceptions across the ABI, every call returns an
+ * hv_status. Device pointers are CUDA device addresses; `stream` is a cudaStream_t passed as
+ * void* (NULL = legacy default stream). All compute steps are asynchronous on `stream`.
+ */
+#ifndef HOLOVIBES_GB300_H
+#define HOLOVIBES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The first eight values are the reference's ApiCode
+ * (Backend/includes/enum/enum_api_code.hh:13-23); the rest are device-side failures that the
+ * reference turns into exit() / exceptions (Backend/cuda_includes/common.cuh:52-64). */
+typedef enum hv_status
+{
+    HV_OK = 0,
+    HV_NO_CHANGE = 1,
+    HV_INVALID_VALUE = 2,
+    HV_NO_IN_DATA = 3,
+    HV_NOT_STARTED = 4,
+    HV_WRONG_COMP_MODE = 5,
+    HV_WRONG_IMG_TYPE = 6,
+    HV_FAILURE = 7,
+    HV_ERR_CUDA = 8,
+    HV_ERR_OOM = 9,
+    HV_ERR_TIMEOUT = 10,
+    HV_ERR_ADMISSION = 11,
+    HV_ERR_UNSUPPORTED = 12
+} hv_status;
+
+/* camera::FrameDescriptor (Camera/include/frame_desc.hh:13-48): depth in bytes per pixel
+ * (1 = uint8, 2 = uint16, 4 = float32), byte_endian 0 = little, 1 = big. */
+typedef struct hv_frame_desc
+{
+    uint16_t width;
+    uint16_t height;
+    uint32_t depth;
+    uint32_t byte_endian;
+} hv_frame_desc;
+
+/* SpaceTransformation (Backend/includes/enum/enum_space_transformation.hh:17-22). */
+enum { HV_SPACE_NONE = 0, HV_SPACE_FRESNELTR = 1, HV_SPACE_ANGULARSP = 2 };
+/* TimeTransformation (Backend/includes/enum/enum_time_transformation.hh:16-22). */
+enum { HV_TIME_NONE = 0, HV_TIME_STFT = 1, HV_TIME_PCA = 2, HV_TIME_SSA_STFT = 3 };
+/* ImgType (Backend/includes/enum/enum_img_type.hh:16-26); only the first three are on this path. */
+enum { HV_IMG_MODULUS = 0, HV_IMG_SQUARED_MODULUS = 1, HV_IMG_ARGUMENT = 2 };
+/* Lens phase precision: FP64 (exact phase, reduced mod 2*pi) or the reference's float32 expression. */
+enum { HV_LENS_FP64 = 0, HV_LENS_REF32 = 1 };
+/* Memory kinds for hv_pipe_push_frames / hv_pipe_pull_output. */
+enum { HV_MEM_HOST = 0, HV_MEM_DEVICE = 1 };
+
+/* Flat settings record: the subset of the reference's typed settings that this path reads
+ * (Backend/includes/core/holovibes.hh:370-450 defaults; compute-settings JSON keys in
+ * Backend/includes/struct/*.hh). hv_settings_default() fills the reference defaults. */
+typedef struct hv_settings
+{
+    int32_t space_transformation;    /* image_rendering.space_transformation */
+    int32_t time_transformation;     /* image_rendering.time_transformation */
+    int32_t time_transformation_size; /* image_rendering.time_transformation_size (T) */
+    int32_t time_stride;             /* image_rendering.time_transformation_stride (S) */
+    int32_t batch_size;              /* image_rendering.batch_size (B) */
+    float lambda;                    /* image_rendering.lambda [m] */
+    float z_distance;                /* image_rendering.propagation_distance [m] */
+    float pixel_size;                /* input info pixel pitch [um] */
+    int32_t image_type;              /* view.image_type */
+    int32_t p_start;                 /* view.z.start */
+    int32_t p_width;                 /* view.z.width */
+    int32_t fft_shift;               /* view.fft_shift */
+    int32_t renorm;                  /* view.renorm */
+    int32_t renorm_constant;         /* advanced.renorm_constant */
+    int32_t accumulation;            /* view.window.xy.output_image_accumulation */
+    int32_t log_enabled;             /* view.window.xy.log_enabled */
+    int32_t contrast_enabled;        /* view.window.xy.contrast.enabled */
+    int32_t contrast_auto_refresh;   /* view.window.xy.contrast.auto_refresh */
+    int32_t contrast_invert;         /* view.window.xy.contrast.invert */
+    float contrast_min;              /* view.window.xy.contrast.min */
+    float contrast_max;              /* view.window.xy.contrast.max */
+    float contrast_lower;            /* advanced.contrast.lower [%] */
+    float contrast_upper;            /* advanced.contrast.upper [%] */
+    int32_t reticle_display;         /* view.reticle.display_enabled */
+    float reticle_scale;             /* view.reticle.scale */
+    int32_t unwrap_2d;               /* Unwrap2d setting */
+    int32_t lens_mode;               /* HV_LENS_FP64 (default) or HV_LENS_REF32 */
+    int32_t output_buffer_size;      /* advanced.buffer_size.output: output frames kept */
+    int32_t input_buffer_size;       /* advanced.buffer_size.input: raw frames kept */
+} hv_settings;
+
+/* ------------------------------------------------------------------------------------------
+ * Library
+ * ---------------------------------------------------------------------------------------- */
+const char* hv_version(void);
+/* Last error message of the calling thread (empty string when none). */
+const char* hv_last_error(void);
+/* Kernels launched by this library in this process (all threads). */
+uint64_t hv_kernel_launches(void);
+void hv_settings_default(hv_settings* s);
+/* Parses a compute-settings JSON document (the reference's ComputeSettings layout,
+ * Backend/sources/core/compute_settings.cc:66-99) and merges it into *s. Unknown keys fail
+ * with HV_FAILURE like merge_json (compute_settings.cc:24-36). */
+hv_status hv_settings_from_json(const char* json, hv_settings* s);
+/* Validates and adjusts settings like the reference's TransformApi setters
+ * (Backend/sources/api/transform_api.cc:16-206): stride >= batch and a multiple of it,
+ * z != 0, p range inside the time window. Returns HV_INVALID_VALUE for unsupported values. */
+hv_status hv_settings_validate(hv_settings* s, const hv_frame_desc* fd);
+
+/* ------------------------------------------------------------------------------------------
+ * Pipe (drop-in for Pipe / ICompute; Backend/includes/core/pipe.hh:70-125)
+ * ---------------------------------------------------------------------------------------- */
+typedef struct hv_pipe hv_pipe;
+
+/* Creates a pipe on the current CUDA device: allocates the spatial buffer, the time ring,
+ * the view / accumulation / output buffers (ICompute ctor, Backend/includes/core/icompute.hh:123-171).
+ * `stream` may be NULL, in which case the pipe creates and owns a non-blocking stream. */
+hv_pipe* hv_pipe_create(const hv_frame_desc* fd, const hv_settings* settings, void* stream, hv_status* status);
+void hv_pipe_destroy(hv_pipe* p);
+/* Device bytes held by a pipe with these settings (admission by HBM footprint). */
+size_t hv_pipe_footprint(const hv_frame_desc* fd, const hv_settings* settings);
+/* Replaces BatchInputQueue::enqueue (Backend/sources/data_struct/batch_input_queue.cc:124-202)
+ * followed by the compute cycles it unblocks (Pipe::exec, pipe.cc:650-676). `n` frames of
+ * fd->depth bytes each; `mem` is HV_MEM_HOST or HV_MEM_DEVICE. Work is enqueued on the pipe's
+ * stream; host memory is copied before the call returns only if it is pageable. */
+hv_status hv_pipe_push_frames(hv_pipe* p, const void* frames, size_t n, int mem);
+/* Number of uint16 output frames produced and not yet pulled. */
+size_t hv_pipe_output_count(hv_pipe* p);
+/* Replaces the output Queue dequeue: copies the oldest output frame (W*H uint16) into dst,
+ * waiting at most timeout_us microseconds for it (HV_ERR_TIMEOUT otherwise). */
+hv_status hv_pipe_pull_output(hv_pipe* p, uint16_t* dst, int mem, int64_t timeout_us);
+/* Applies new settings at the next cycle boundary (pipe_refresh / pipe_cycle updates,
+ * Backend/includes/core/pipe.hh:192-213). Returns HV_NO_CHANGE when nothing changed. */
+hv_status hv_pipe_update_settings(hv_pipe* p, const hv_settings* settings);
+/* Requests an autocontrast on the next output (Rendering::request_autocontrast,
+ * Backend/sources/compute/rendering.cc:87-99). */
+hv_status hv_pipe_request_autocontrast(hv_pipe* p);
+/* Blocks until all work enqueued on the pipe's stream finished. */
+hv_status hv_pipe_sync(hv_pipe* p);
+/* Current XY contrast range (XYContrastRange setting) after the last autocontrast. */
+hv_status hv_pipe_get_contrast_range(hv_pipe* p, float* min_out, float* max_out);
+/* Copies the last float frame fed to the contrast stage (gpu_postprocess_frame) into dst (host). */
+hv_status hv_pipe_get_float_frame(hv_pipe* p, float* dst);
+/* Copies the time ring storage (T frames of complex64, slot order) and its start/size. */
+hv_status hv_pipe_get_ring(hv_pipe* p, void* dst_host, int32_t* start, int32_t* size);
+/* Number of kernels this pipe launched since creation. */
+uint64_t hv_pipe_kernel_launches(hv_pipe* p);
+void* hv_pipe_stream(hv_pipe* p);
+
+/* ------------------------------------------------------------------------------------------
+ * Compute steps (device buffers, stream-ordered)
+ * ---------------------------------------------------------------------------------------- */
+
+/* Supported transform lengths for the shared-memory FFT (each of width and height). */
+int hv_fft_size_supported(int n);
+
+/* Fresnel quadratic lens, H x W complex64, centre-cropped from the max(W,H) square.
+ * Replaces fresnel_transform_lens + kernel_quadratic_lens (Backend/cuda_sources/fresnel_transform.cu:14-63,
+ * masks.cu:7-29). */
+hv_status hv_fresnel_lens(void* lens_c64, int width, int height, float lambda, float z, float pixel_size_um,
+                          int lens_mode, void* stream);
+/* Angular-spectrum transfer function in FFT layout (already quadrant-swapped).
+ * Replaces angular_spectrum_lens + kernel_spectral_lens + shift_corners
+ * (Backend/cuda_sources/angular_spectrum.cu:14-31, masks.cu:31-59, fourier_transform.cc:121-137). */
+hv_status hv_angular_spectrum_lens(void* lens_c64, int width, int height, float lambda, float z,
+                                   float pixel_size_um, int lens_mode, void* stream);
+
+/* Fused raw->complex convert + spatial propagation of `batch` frames, written into slots
+ * (slot0 + b) % nslots of a ring of complex64 frames. Replaces input_queue_to_input_buffer
+ * (tools_conversion.cu:120-171) + fresnel_transform (fresnel_transform.cu:65-83) /
+ * angular_spectrum (angular_spectrum.cu:33-63) + Queue::enqueue_multiple (queue.cc:332-380).
+ * `raw_kind`: bytes per pixel (1, 2, 4) or 8 for complex64 input; `big_endian` swaps 16-bit.
+ * `work_c64` must hold batch*W*H complex64 (unused for space NONE). */
+hv_status hv_spatial_transform(const void* raw, int raw_bytes, int big_endian, int width, int height, int batch,
+                               int space, const void* lens_c64, void* work_c64, void* ring_c64, int slot0,
+                               int nslots, void* stream);
+
+/* Batched 2-D complex FFT over `batch` row-major n0 x n1 arrays (n0 rows of n1 samples),
+ * forward (sign -1) or inverse (sign +1, unnormalised), multiplied by `scale`. */
+hv_status hv_fft2d(const void* in_c64, void* out_c64, int n0, int n1, int batch, int inverse, float scale,
+                   void* stream);
+
+/* Fused time transform + view: for every pixel, X_k = sum_t ring[t] * W[k][t] for k < K,
+ * then out = scale * mean_k f(X_k) with f = |.|, |.|^2 or atan2 (img_type), written at the
+ * fftshift-ed position when `shift` is set. `weights_c64` is K x T complex64. Per-CTA partial
+ * sums of the written values go to `partials_f64` (hv_time_view_partials entries) when not NULL.
+ * Replaces stft (stft.cu:9-15) / matrix_multiply_complex (matrix_operations.cc:77-103) +
+ * complex_to_modulus / _squared_modulus / _argument (tools_conversion.cu:11-103,199-232). */
+hv_status hv_time_view(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
+                       int img_type, float scale, int shift, float* out_f32, double* partials_f64, void* stream);
+int hv_time_view_partials(int width, int height);
+/* STFT weights W[k][t] = exp(-2*pi*i*(pmin+k)*t/T), k <= pmax-pmin, computed in FP64. */
+hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* stream);
+
+/* PCA: covariance C = H^H H of the ring (H = HW x T column-major view), FP32 accumulation,
+ * written as complex128 T x T (both triangles). Replaces cov_matrix (matrix_operations.cc:9-26).
+ * `work` must hold hv_pca_cov_workspace(T, W*H) bytes. */
+hv_status hv_pca_covariance(const void* ring_c64, int T, size_t npix, void* cov_c128, void* work, void* stream);
+size_t hv_pca_cov_workspace(int T, size_t npix);
+/* FP64 cyclic Jacobi eigensolve of the Hermitian T x T complex128 matrix (lower triangle
+ * read): ascending eigenvalues, orthonormal eigenvectors as columns. Replaces cusolverDnCheevd
+ * (matrix_operations.cc:44-65). Writes the columns pmin..pmax as PCA weights W[k][t] = V[t][pmin+k]
+ * (complex64) when weights_c64 != NULL. `cov_c128` is overwritten. `work` needs hv_pca_eigh_workspace(T) bytes. */
+hv_status hv_pca_eigh(void* cov_c128, int T, double* eigenvalues, void* eigenvectors_c128, int pmin, int pmax,
+                      void* weights_c64, void* work, void* stream);
+size_t hv_pca_eigh_workspace(int T);
+
+/* 2-D phase unwrap of a float phase image, then rescale to [0, 65535]. Replaces unwrap_2d +
+ * rescale_float_unwrap2d (tools_unwrap.cu:269-369, tools_conversion.cu:315-335). `work` must hold
+ * hv_unwrap_workspace(W, H) bytes. */
+hv_status hv_unwrap_2d(const float* in, float* out, int width, int height, void* work, void* stream);
+size_t hv_unwrap_workspace(int width, int height);
+
+/* Renormalisation x <- x * 2^c * N / sum(x), the sum being taken from `partials_f64`
+ * (npartials entries) or computed here when partials_f64 is NULL. Replaces gpu_normalize
+ * (tools_compute.cu:99-123). `work` needs hv_reduce_workspace(n) bytes. */
+hv_status hv_renormalize(float* frame, size_t n, int renorm_constant, const double* partials_f64, int npartials,
+                         void* work, void* stream);
+size_t hv_reduce_workspace(size_t n);
+/* In-place quadrant swap (fftshift for even sizes). Replaces shift_corners (shift_corners.cu:8-70). */
+hv_status hv_shift_corners(float* frame, int width, int height, void* stream);
+/* Writes `frame` into slot `slot` of an A-frame float ring and stores into `out` the mean of
+ * `count` frames starting at slot `start` (circular). Replaces Queue::enqueue +
+ * accumulate_images (tools_conversion.cu:418-458, image_accumulation.cc:136-157). */
+hv_status hv_accumulate(const float* frame, float* acc_ring, int A, int slot, int start, int count, float* out,
+                        size_t n, void* stream);
+/* In-place log10 (map_log10, rendering.cc:127-138). */
+hv_status hv_log10(float* frame, size_t n, void* stream);
+
+/* Autocontrast: the values at percentiles `lower` and `upper` of the frame (or of the reticle
+ * disc when reticle_scale > 0), clamped to >= 1, written to range_f32[0..1] on the device.
+ * Exact selection (radix select), identical to sorting. Replaces compute_percentile_xy_view
+ * + ContrastApi::update_contrast (percentile.cu:75-94,139-222; contrast_api.cc:137-146).
+ * `work` needs hv_percentile_workspace(width*height) bytes. */
+hv_status hv_percentile(const float* frame, int width, int height, float lower, float upper, float reticle_scale,
+                        float* range_f32, void* work, void* stream);
+size_t hv_percentile_workspace(size_t n);
+/* Contrast map x <- 65535/(max-min+FLT_EPSILON)*(x-min) (min/max from range_f32 on the device,
+ * swapped when invert) then float->ushort (clamp <=0 -> 0, >65535 -> 65535, truncation).
+ * apply_contrast = 0 skips the map. Replaces apply_contrast_correction + float_to_ushort
+ * (contrast_correction.cu:5-17, tools_conversion.cu:350-387). */
+hv_status hv_contrast_to_ushort(const float* frame, const float* range_f32, int invert, int apply_contrast,
+                                uint16_t* out, size_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HOLOVIBES_GB300_H */

@@ -1,0 +1,580 @@
+"""FP64 CPU oracle of the Holovibes hologram path. TEST INFRASTRUCTURE ONLY.
+
+This module is the checker: only ``tests/``, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` import it. The product
+(``holovibes_gb300``) never imports it and has no CPU fallback.
+
+It restates, in numpy complex128 / float64, the equations of the reference's hot path
+(raw frames -> complex -> spatial propagation -> time ring -> STFT bins / PCA -> view ->
+unwrap -> renorm -> fftshift -> accumulation -> percentile contrast -> uint16). Every
+function cites the reference file:line it follows (paths relative to the Holovibes tree).
+
+Parity status: UNPINNED by reference golden vectors. The reference's own test data are
+Git-LFS pointers with no committed ``R_ref.holo`` outputs, and its numeric kernels call
+cuFFT / cuBLAS / cuSOLVER / thrust, so no reference output exists to pin against. The
+oracle is anchored on the reference's call sites (cited below) and, on the GPU, the
+library-anchor tests run the same library calls (cuFFT, cuSOLVER via torch) in the
+reference's order and compare them with this module.
+
+Stages that the reference computes in float32 on the host/GPU with integer or float
+truncation (percentile index, contrast factor, float->ushort) are restated here in
+float32 with the same operation order, so that uint16 output can be compared bit for
+bit when the float input frame is identical.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+F32 = np.float32
+
+# ----------------------------------------------------------------------------------------
+# a1: raw -> complex  (Backend/cuda_sources/tools_conversion.cu:107-171)
+# ----------------------------------------------------------------------------------------
+
+
+def convert_frames(raw: np.ndarray) -> np.ndarray:
+    """u8 -> x*257, u16 -> x, f32 -> x; imaginary part 0 (tools_conversion.cu:134-145)."""
+    if raw.dtype == np.uint8:
+        return raw.astype(np.float64) * 257.0 + 0j
+    if raw.dtype == np.uint16:
+        return raw.astype(np.float64) + 0j
+    if raw.dtype == np.float32:
+        return raw.astype(np.float64) + 0j
+    raise TypeError(f"unsupported raw dtype {raw.dtype}")
+
+
+def byteswap16(raw: np.ndarray) -> np.ndarray:
+    """Big-endian 16-bit input (Backend/sources/data_struct/queue.cc:191-202, tools_conversion.cu endianness_conversion)."""
+    return ((raw.astype(np.uint16) << 8) | (raw.astype(np.uint16) >> 8)).astype(np.uint16)
+
+
+# ----------------------------------------------------------------------------------------
+# a2: Fresnel quadratic lens (Backend/cuda_sources/masks.cu:7-29, fresnel_transform.cu:14-63)
+# ----------------------------------------------------------------------------------------
+
+
+def _crop_square(square: np.ndarray, W: int, H: int) -> np.ndarray:
+    """Centre crop of the max(W,H) square lens (fresnel_transform.cu:37-62)."""
+    S = square.shape[0]
+    if W == H:
+        return square
+    if W > H:  # contiguous rows starting at row (S-H)/2
+        r0 = (S - H) // 2
+        return square[r0:r0 + H, :W]
+    c0 = (S - W) // 2  # H > W: row-by-row copy with a column offset
+    return square[:H, c0:c0 + W]
+
+
+def fresnel_lens(W: int, H: int, lam: float, z: float, pixel_size_um: float, mode: str = "fp64") -> np.ndarray:
+    """L[j,i] = exp(i*pi/(lam*z)*(x^2+y^2)), x=(i-S/2)*dx, dx = pixel_size*1e-6 on the S=max(W,H) square.
+
+    mode "fp64": the exact phase in float64. mode "ref32": the reference's float32 expression
+    (masks.cu:10-27: c = (float)(M_PI/(lam*z)), x = (i - (float)(S>>1))*dx, csquare = c*(x*x+y*y)).
+    """
+    S = max(W, H)
+    idx = np.arange(S)
+    # the reference holds lambda, z and the pixel pitch as float32 settings
+    lam, z, pixel_size_um = float(F32(lam)), float(F32(z)), float(F32(pixel_size_um))
+    if mode == "fp64":
+        dx = pixel_size_um * 1e-6
+        x = (idx - (S >> 1)) * dx
+        c = math.pi / (lam * z)
+        ph = c * (x[None, :] ** 2 + x[:, None] ** 2)
+        lens = np.exp(1j * ph)
+    elif mode == "ref32":
+        lam32, z32, ps32 = F32(lam), F32(z), F32(pixel_size_um)
+        c = F32(math.pi / float(F32(lam32 * z32)))
+        dx = F32(ps32 * F32(1.0e-6))
+        x = (idx.astype(F32) - F32(S >> 1)) * dx
+        xx = (x * x).astype(F32)
+        cs = (c * (xx[None, :] + xx[:, None]).astype(F32)).astype(F32)
+        lens = np.cos(cs.astype(np.float64)) + 1j * np.sin(cs.astype(np.float64))
+    else:
+        raise ValueError(mode)
+    return _crop_square(lens, W, H)
+
+
+# ----------------------------------------------------------------------------------------
+# a4: angular-spectrum transfer function (masks.cu:31-59, angular_spectrum.cu:14-31,
+#     fourier_transform.cc:121-137 (+ shift_corners))
+# ----------------------------------------------------------------------------------------
+
+
+def shift_corners(img: np.ndarray) -> np.ndarray:
+    """Quadrant swap of shift_corners.cu:8-44 for even W,H (= fftshift = ifftshift)."""
+    H, W = img.shape[-2:]
+    if H % 2 or W % 2:
+        raise ValueError("shift_corners is a quadrant swap only for even dimensions")
+    return np.roll(np.roll(img, H // 2, axis=-2), W // 2, axis=-1)
+
+
+def angular_spectrum_lens(W: int, H: int, lam: float, z: float, pixel_size_um: float, mode: str = "fp64") -> np.ndarray:
+    """G[y,x] = exp(i*2*pi*z/lam*sqrt(max(0, 1-lam^2(u^2+v^2)))), u=(x-W/2)/(W*dx), v=(y-H/2)/(H*dy),
+    then quadrant-swapped into FFT layout (fourier_transform.cc:134).
+
+    mode "ref32" follows the float32 expression of masks.cu:43-55: u_step = 1.0f/(Nx*x_step),
+    u = (x-(Nx>>1))*u_step, tmp = 1.0f - lam*lam*(u*u+v*v) in float32, and the phase
+    2.0f*M_PI*z/lam*sqrtf(tmp) evaluated in double then rounded to float32.
+    """
+    xs = np.arange(W)
+    ys = np.arange(H)
+    lam, z, pixel_size_um = float(F32(lam)), float(F32(z)), float(F32(pixel_size_um))
+    if mode == "fp64":
+        step = pixel_size_um * 1e-6
+        u = (xs - (W >> 1)) / (W * step)
+        v = (ys - (H >> 1)) / (H * step)
+        tmp = 1.0 - lam * lam * (u[None, :] ** 2 + v[:, None] ** 2)
+        tmp = np.maximum(tmp, 0.0)
+        ph = 2.0 * math.pi * z / lam * np.sqrt(tmp)
+        # reduce the large phase modulo 2*pi before exponentiation (pure float64 identity)
+        G = np.exp(1j * np.mod(ph, 2.0 * math.pi))
+    elif mode == "ref32":
+        lam32, z32 = F32(lam), F32(z)
+        step = F32(F32(pixel_size_um) * F32(1e-6))
+        u_step = F32(F32(1.0) / F32(F32(W) * step))
+        v_step = F32(F32(1.0) / F32(F32(H) * step))
+        u = (xs - (W >> 1)).astype(F32) * u_step
+        v = (ys - (H >> 1)).astype(F32) * v_step
+        uu = (u * u).astype(F32)
+        vv = (v * v).astype(F32)
+        s = (uu[None, :] + vv[:, None]).astype(F32)
+        ll = F32(lam32 * lam32)
+        tmp = (F32(1.0) - (ll * s).astype(F32)).astype(F32)
+        tmp = np.maximum(tmp, F32(0.0))
+        sq = np.sqrt(tmp).astype(F32).astype(np.float64)
+        ph = ((2.0 * math.pi * float(z32)) / float(lam32)) * sq
+        ph32 = ph.astype(F32).astype(np.float64)
+        G = np.cos(ph32) + 1j * np.sin(ph32)
+    else:
+        raise ValueError(mode)
+    return shift_corners(G)
+
+
+# ----------------------------------------------------------------------------------------
+# a3/a5/a6: spatial transforms (fresnel_transform.cu:65-83, angular_spectrum.cu:33-63,
+#            apply_mask.cu:7-34)
+# ----------------------------------------------------------------------------------------
+
+
+def fresnel_transform(frames: np.ndarray, lens: np.ndarray) -> np.ndarray:
+    """x <- FFT2(x * L), forward, unnormalised, no shift (fresnel_transform.cu:74-79)."""
+    return np.fft.fft2(frames * lens[None], axes=(-2, -1))
+
+
+def angular_spectrum(frames: np.ndarray, lens: np.ndarray) -> np.ndarray:
+    """x <- IFFT2(FFT2(x) * G) / (H*W): cuFFT's unnormalised inverse then kernel_complex_divide
+    (angular_spectrum.cu:47-61). numpy's ifft2 carries the same 1/(H*W)."""
+    return np.fft.ifft2(np.fft.fft2(frames, axes=(-2, -1)) * lens[None], axes=(-2, -1))
+
+
+def spatial_transform(frames: np.ndarray, kind: str, lens: np.ndarray | None) -> np.ndarray:
+    """Dispatch of FourierTransform::insert_fft (fourier_transform.cc:30-72)."""
+    if kind == "NONE":
+        return frames
+    if kind == "FRESNELTR":
+        return fresnel_transform(frames, lens)
+    if kind == "ANGULARSP":
+        return angular_spectrum(frames, lens)
+    raise ValueError(kind)
+
+
+# ----------------------------------------------------------------------------------------
+# a7: time-transformation ring (Backend/sources/data_struct/queue.cc:332-380)
+# ----------------------------------------------------------------------------------------
+
+
+class Ring:
+    """Circular queue of T frames with the reference's start/size bookkeeping.
+
+    enqueue_multiple follows queue.cc:332-380: frames land at (start+size) % T with wrap;
+    a batch larger than T keeps only its last T frames; when the queue overflows, start
+    advances. ``data`` is the raw STORAGE (slot order), which is what the time transforms
+    read (fourier_transform.cc:238-240, get_data()).
+    """
+
+    def __init__(self, T: int, shape: tuple, dtype=np.complex128):
+        self.T = T
+        self.data = np.zeros((T,) + tuple(shape), dtype=dtype)
+        self.start = 0
+        self.size = 0
+
+    def enqueue_multiple(self, elts: np.ndarray) -> None:
+        nb = elts.shape[0]
+        T = self.T
+        if nb > T:
+            elts = elts[nb - T:]
+            self.start = (self.start + nb - T) % T
+            nb = T
+        begin = (self.start + self.size) % T
+        for j in range(nb):
+            self.data[(begin + j) % T] = elts[j]
+        self.size += nb
+        if self.size > T:
+            self.start = (self.start + self.size - T) % T
+            self.size = T
+
+    def enqueue(self, elt: np.ndarray) -> None:
+        """Single enqueue (queue.cc:149-189)."""
+        end = (self.start + self.size) % self.T
+        self.data[end] = elt
+        if self.size < self.T:
+            self.size += 1
+        else:
+            self.start = (self.start + 1) % self.T
+
+    def is_full(self) -> bool:
+        return self.size == self.T
+
+    def clear(self) -> None:
+        self.start = 0
+        self.size = 0
+
+
+# ----------------------------------------------------------------------------------------
+# a8: STFT over ring storage order (stft.cu:9-15, icompute.cc:109-115)
+# a12: p range (converts.cc:76-92)
+# ----------------------------------------------------------------------------------------
+
+
+def p_range(p_start: int, p_width: int, T: int) -> tuple[int, int]:
+    """pmin = p.start; pmax = max(0, min(pmin + width, T)) if width else pmin (converts.cc:81-88)."""
+    pmin = p_start
+    pmax = max(0, min(pmin + p_width, T)) if p_width != 0 else pmin
+    return pmin, pmax
+
+
+def stft_bins(storage: np.ndarray, pmin: int, pmax: int) -> np.ndarray:
+    """X[k] = sum_t storage[t] * exp(-2*pi*i*k*t/T) for k in [pmin, pmax]: cuFFT forward along time
+    (planMany batch=HW, stride=HW) restricted to the bins the view reads."""
+    T = storage.shape[0]
+    t = np.arange(T)
+    ks = np.arange(pmin, pmax + 1)
+    W = np.exp(-2j * np.pi * np.outer(ks, t) / T)  # [K, T]
+    flat = storage.reshape(T, -1)
+    return (W @ flat).reshape((len(ks),) + storage.shape[1:])
+
+
+# ----------------------------------------------------------------------------------------
+# a9-a11: PCA (matrix_operations.cc:9-103, fourier_transform.cc:340-377)
+# ----------------------------------------------------------------------------------------
+
+
+def pca_covariance(storage: np.ndarray) -> np.ndarray:
+    """cov = H^H H with H the column-major HW x T view of the ring storage (matrix_operations.cc:9-26).
+    cov[i, j] = sum_pix conj(H[pix, i]) * H[pix, j]."""
+    T = storage.shape[0]
+    Hm = storage.reshape(T, -1).T  # [HW, T]
+    return Hm.conj().T @ Hm
+
+
+def pca_eigh(cov: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Ascending eigenvalues, eigenvectors as columns, from the LOWER triangle (cusolverDnCheevd,
+    matrix_operations.cc:44-65). numpy.linalg.eigh(UPLO='L') has the same contract."""
+    w, V = np.linalg.eigh(cov, UPLO="L")
+    return w, V
+
+
+def pca_project(storage: np.ndarray, V: np.ndarray, pmin: int, pmax: int) -> np.ndarray:
+    """p_acc[:, j] = H @ V[:, j] (matrix_multiply_complex, matrix_operations.cc:77-103), for j in [pmin, pmax]."""
+    T = storage.shape[0]
+    Hm = storage.reshape(T, -1).T
+    P = Hm @ V[:, pmin:pmax + 1]  # [HW, K]
+    return P.T.reshape((pmax - pmin + 1,) + storage.shape[1:])
+
+
+# ----------------------------------------------------------------------------------------
+# a13-a16: views (tools_conversion.cu:11-103,199-218; converts.cc:50-62)
+# ----------------------------------------------------------------------------------------
+
+PCA_SCALE = float((2 << 16) - 1)  # 131071, converts.cc:58
+
+
+def view(planes: np.ndarray, img_type: str) -> np.ndarray:
+    """Mean over the selected planes of |X|, |X|^2 or atan2(Im, Re)."""
+    if img_type == "MODULUS":
+        v = np.abs(planes)
+    elif img_type == "SQUARED_MODULUS":
+        v = np.abs(planes) ** 2
+    elif img_type == "ARGUMENT":
+        v = np.arctan2(planes.imag, planes.real)
+    else:
+        raise ValueError(img_type)
+    return v.mean(axis=0)
+
+
+# ----------------------------------------------------------------------------------------
+# a17: 2-D phase unwrap (tools_unwrap.cu:79-95,269-369; tools.cu:50-68) + rescale
+#      (tools_conversion.cu:315-335)
+# ----------------------------------------------------------------------------------------
+
+M_2PI_F = float(F32(6.28318530717959))  # common.cuh:29
+
+
+def unwrap_2d(phase: np.ndarray) -> np.ndarray:
+    """Fourier-domain unwrap of an H x W phase image.
+
+    The reference plans its unwrap FFT as plan(width, height) (icompute.hh:140), i.e. it
+    transforms the row-major buffer as ``width`` rows of ``height`` samples; this restatement
+    does the same by viewing the buffer as a (W, H) array. Frequency indices come from the
+    circ-shifted fx/fy grids (tools_unwrap.cu:79-95, 269-296). cuFFT transforms are unnormalised.
+    """
+    H, W = phase.shape
+    flat = phase.reshape(-1)
+    j, i = np.divmod(np.arange(H * W), W)
+    fx = (i - (W >> 1)).astype(np.float64)
+    fy = (j - (H >> 1)).astype(np.float64)
+    # circ_shift(out, in, W, H, -W/2, -H/2): out[(y-H/2)%H][(x-W/2)%W] = in[y][x]
+    def circ(a):
+        a2 = a.reshape(H, W)
+        return np.roll(np.roll(a2, -(H >> 1), axis=0), -(W >> 1), axis=1).reshape(-1)
+    sfx, sfy = circ(fx), circ(fy)
+    z = np.exp(1j * flat)
+    n0, n1 = W, H  # plan(width, height): slowest dimension = width
+
+    def fft(a):
+        return np.fft.fft2(a.reshape(n0, n1)).reshape(-1)
+
+    def ifft(a):  # unnormalised inverse
+        return np.fft.ifft2(a.reshape(n0, n1)).reshape(-1) * (n0 * n1)
+
+    Z = fft(z)
+    gx = ifft(Z * sfx) * (1j * M_2PI_F)
+    gy = ifft(Z * sfy) * (1j * M_2PI_F)
+    zc = np.conj(z * 1j)
+    gx = fft(gx * zc)
+    gy = fft(gy * zc)
+    norm = sfx * sfx + sfy * sfy
+    with np.errstate(divide="ignore", invalid="ignore"):
+        cx = np.where(norm != 0, sfx / np.where(norm != 0, norm, 1), 0.0)
+        cy = np.where(norm != 0, sfy / np.where(norm != 0, norm, 1), 0.0)
+    acc = ifft(gx * cx + gy * cy)
+    return (acc.imag / -M_2PI_F).reshape(H, W)
+
+
+def rescale_unwrap2d(img: np.ndarray) -> np.ndarray:
+    """(in+|min|)/(|min|+max)*65535 if min<0 else (in-min)/(max-min)*65535 (tools_conversion.cu:315-335)."""
+    mn, mx = img.min(), img.max()
+    if mn < 0:
+        return (img + abs(mn)) / (abs(mn) + mx) * 65535.0
+    return (img - mn) / (mx - mn) * 65535.0
+
+
+# ----------------------------------------------------------------------------------------
+# a18: renormalisation (tools_compute.cu:99-123, postprocessing.cc:135-155)
+# ----------------------------------------------------------------------------------------
+
+
+def renormalize(img: np.ndarray, renorm_constant: int) -> np.ndarray:
+    """x <- x * 2^c * N / sum(x)."""
+    return img * float(1 << renorm_constant) * (img.size / img.sum(dtype=np.float64))
+
+
+# ----------------------------------------------------------------------------------------
+# a20: image accumulation (tools_conversion.cu:418-441, image_accumulation.cc:136-157)
+# ----------------------------------------------------------------------------------------
+
+
+class Accumulator:
+    """Rolling mean over the last A frames; a frame is enqueued, then the mean of the current size."""
+
+    def __init__(self, A: int, shape: tuple):
+        self.ring = Ring(A, shape, dtype=np.float64)
+
+    def push(self, img: np.ndarray) -> np.ndarray:
+        self.ring.enqueue(img)
+        r = self.ring
+        idx = [(r.start + i) % r.T for i in range(r.size)]
+        return r.data[idx].mean(axis=0)
+
+
+# ----------------------------------------------------------------------------------------
+# a21-a23: percentile contrast and uint16 (percentile.cu:75-94,139-222; contrast_api.cc:137-146;
+#          contrast_correction.cu:5-17; tools_conversion.cu:350-359,382-387). float32 math.
+# ----------------------------------------------------------------------------------------
+
+
+def percentile_index(pct: float, n: int) -> int:
+    """(uint)(h_percent / 100 * frame_res) evaluated in float32 (percentile.cu:85), clamped to n-1."""
+    idx = int(np.floor(F32(F32(pct) / F32(100)) * F32(n)))
+    return min(max(idx, 0), n - 1)
+
+
+def reticle_values(img32: np.ndarray, scale: float) -> np.ndarray:
+    """Pixels inside the contrast reticle circle (percentile.cu:15-43,159-181)."""
+    H, W = img32.shape
+    radius = int(F32(scale) * F32(min(W, H)) / F32(2))
+    cx, cy = W // 2, H // 2
+    y, x = np.mgrid[0:H, 0:W]
+    m = (x - cx) ** 2 + (y - cy) ** 2 <= radius * radius
+    return img32[m]
+
+
+def autocontrast(img32: np.ndarray, lower: float, upper: float, reticle_scale: float | None = None) -> tuple[float, float]:
+    """Sorted-copy percentiles, then update_contrast's clamp of both ends to >= 1.0."""
+    vals = img32.reshape(-1) if reticle_scale is None else reticle_values(img32, reticle_scale)
+    s = np.sort(vals.astype(F32))
+    n = s.size
+    lo = F32(s[percentile_index(lower, n)])
+    hi = F32(s[percentile_index(upper, n)])
+    lo = lo if lo > F32(1.0) else F32(1.0)
+    hi = hi if hi > F32(1.0) else F32(1.0)
+    return float(lo), float(hi)
+
+
+def apply_contrast(img32: np.ndarray, cmin: float, cmax: float, invert: bool = False) -> np.ndarray:
+    """factor = 65535 / (max - min + FLT_EPSILON); x <- factor * (x - min), in float32."""
+    mn, mx = (F32(cmax), F32(cmin)) if invert else (F32(cmin), F32(cmax))
+    eps = F32(np.finfo(np.float32).eps)
+    factor = F32(F32(65535.0) / F32(F32(mx - mn) + eps))
+    return (factor * (img32.astype(F32) - mn).astype(F32)).astype(F32)
+
+
+def float_to_ushort(img32: np.ndarray) -> np.ndarray:
+    """x<=0 -> 0; (uint)x > 65535 -> 65535; else truncation (tools_conversion.cu:350-359). NaN -> 0."""
+    x = img32.astype(F32)
+    out = np.zeros(x.shape, dtype=np.uint16)
+    with np.errstate(invalid="ignore"):
+        pos = x > 0
+        big = x >= F32(65536.0)
+        mid = pos & ~big
+    out[big & pos] = 65535
+    out[mid] = np.trunc(x[mid]).astype(np.uint16)
+    return out
+
+
+def log10_view(img: np.ndarray) -> np.ndarray:
+    """map_log10 (rendering.cc:127-138)."""
+    return np.log10(img)
+
+
+# ----------------------------------------------------------------------------------------
+# Pipe model (Backend/sources/core/pipe.cc:255-387, 389-467; rendering.cc:239-299)
+# ----------------------------------------------------------------------------------------
+
+
+@dataclass
+class OracleSettings:
+    width: int
+    height: int
+    depth: int = 2  # bytes per pixel: 1, 2 or 4 (float)
+    space_transformation: str = "NONE"  # NONE / FRESNELTR / ANGULARSP
+    time_transformation: str = "NONE"  # NONE / STFT / PCA
+    time_transformation_size: int = 1
+    time_stride: int = 1
+    batch_size: int = 1
+    lam: float = 852e-9
+    z: float = 0.0
+    pixel_size: float = 12.0
+    image_type: str = "MODULUS"
+    p_start: int = 0
+    p_width: int = 0
+    fft_shift: bool = False
+    renorm: bool = True
+    renorm_constant: int = 5
+    accumulation: int = 0
+    log_enabled: bool = False
+    contrast_enabled: bool = True
+    contrast_auto_refresh: bool = True
+    contrast_invert: bool = False
+    contrast_min: float = 1.0
+    contrast_max: float = 65535.0
+    contrast_lower: float = 0.02
+    contrast_upper: float = 99.98
+    reticle_display: bool = False
+    reticle_scale: float = 0.5
+    unwrap_2d: bool = False
+    lens_mode: str = "fp64"
+
+
+@dataclass
+class OracleOutput:
+    float_frame: np.ndarray  # the frame fed to the contrast stage (float64)
+    contrast: tuple
+    ushort: np.ndarray
+    autocontrast_applied: bool = False
+
+
+class OraclePipe:
+    """Cycle-level model of Pipe::exec/refresh: stride gate, ring, wait-T, time transform,
+    view, unwrap, renorm, fftshift, accumulation, autocontrast and uint16."""
+
+    def __init__(self, s: OracleSettings):
+        self.s = s
+        H, W = s.height, s.width
+        self.ring = Ring(s.time_transformation_size, (H, W))
+        self.batch_index = 0
+        self.lens = None
+        if s.space_transformation == "FRESNELTR":
+            self.lens = fresnel_lens(W, H, s.lam, s.z, s.pixel_size, s.lens_mode)
+        elif s.space_transformation == "ANGULARSP":
+            self.lens = angular_spectrum_lens(W, H, s.lam, s.z, s.pixel_size, s.lens_mode)
+        self.acc = Accumulator(s.accumulation, (H, W)) if s.accumulation > 1 else None
+        self.autocontrast_pending = s.contrast_enabled and s.contrast_auto_refresh
+        self.crange = (s.contrast_min, s.contrast_max)
+        self.last_V = None
+
+    def process_batch(self, raw: np.ndarray, convert_f32=True) -> OracleOutput | None:
+        s = self.s
+        # wait_time_stride (pipe.cc:400-416)
+        self.batch_index += s.batch_size
+        if self.batch_index != s.time_stride:
+            return None
+        self.batch_index = 0
+        frames = convert_frames(raw)
+        frames = spatial_transform(frames, s.space_transformation, self.lens)
+        self.ring.enqueue_multiple(frames)
+        if self.ring.size < s.time_transformation_size:
+            return None
+        return self._render()
+
+    def _render(self) -> OracleOutput:
+        s = self.s
+        T = s.time_transformation_size
+        pmin, pmax = p_range(s.p_start, s.p_width, T)
+        if s.time_transformation == "STFT":
+            planes = stft_bins(self.ring.data, pmin, pmax)
+        elif s.time_transformation == "PCA":
+            cov = pca_covariance(self.ring.data)
+            _, V = pca_eigh(cov)
+            self.last_V = V
+            planes = pca_project(self.ring.data, V, pmin, pmax)
+        else:
+            planes = self.ring.data[pmin:pmax + 1]
+        img = view(planes, s.image_type)
+        if s.image_type == "ARGUMENT" and s.unwrap_2d:
+            img = rescale_unwrap2d(unwrap_2d(img))
+        if s.time_transformation == "PCA":
+            img = img * PCA_SCALE
+        if s.renorm:
+            img = renormalize(img, s.renorm_constant)
+        if s.fft_shift:
+            img = shift_corners(img)
+        if self.acc is not None:
+            img = self.acc.push(img)
+        if s.log_enabled:
+            img = log10_view(img)
+        img32 = img.astype(F32)
+        applied = False
+        if s.contrast_enabled:
+            if self.autocontrast_pending and self._should_autocontrast():
+                applied = True
+                self.crange = autocontrast(img32, s.contrast_lower, s.contrast_upper,
+                                           s.reticle_scale if s.reticle_display else None)
+                if self.acc is None or self.acc.ring.is_full():
+                    self.autocontrast_pending = False
+            c = apply_contrast(img32, self.crange[0], self.crange[1], s.contrast_invert)
+        else:
+            c = img32
+        return OracleOutput(float_frame=img, contrast=self.crange, ushort=float_to_ushort(c),
+                            autocontrast_applied=applied)
+
+    def _should_autocontrast(self) -> bool:
+        """should_apply_contrast (rendering.hh:168-181)."""
+        if self.acc is None:
+            return True
+        r = self.acc.ring
+        return r.is_full() or r.size == 1

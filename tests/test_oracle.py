@@ -1,0 +1,117 @@
+"""CPU checks of the oracle itself: ring semantics of Queue::enqueue_multiple, STFT over storage
+order, the float32 restatements of the percentile index / contrast / uint16 conversion, lens
+symmetries and the unwrap's recovery of a smooth phase. No GPU."""
+
+import numpy as np
+import pytest
+
+import holovibes_oracle as O
+
+
+def test_ring_enqueue_multiple_wraps_and_overflows():
+    r = O.Ring(4, (1,))
+    r.enqueue_multiple(np.arange(3, dtype=np.complex128).reshape(3, 1))
+    assert (r.start, r.size) == (0, 3)
+    r.enqueue_multiple(np.arange(3, 5, dtype=np.complex128).reshape(2, 1))
+    # frames 0..4: slot0 overwritten by frame 4, start advances to 1
+    assert (r.start, r.size) == (1, 4)
+    assert list(r.data[:, 0].real) == [4, 1, 2, 3]
+    # a batch larger than the ring keeps its last T frames
+    r2 = O.Ring(3, (1,))
+    r2.enqueue_multiple(np.arange(7, dtype=np.complex128).reshape(7, 1))
+    assert r2.size == 3
+    order = [(r2.start + i) % 3 for i in range(3)]
+    assert list(r2.data[order, 0].real) == [4, 5, 6]
+
+
+def test_stft_bins_match_fft_over_storage():
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((16, 3, 5)) + 1j * rng.standard_normal((16, 3, 5))
+    full = np.fft.fft(x, axis=0)
+    assert np.allclose(O.stft_bins(x, 2, 6), full[2:7])
+
+
+def test_p_range():
+    assert O.p_range(1, 0, 16) == (1, 1)
+    assert O.p_range(28, 3, 32) == (28, 31)
+    assert O.p_range(30, 5, 32) == (30, 32)  # clamped to T like converts.cc:84-86
+
+
+def test_percentile_index_float32():
+    # 99.5 / 100 * 262144 in float32 -> 260833.28 -> 260833
+    assert O.percentile_index(99.5, 262144) == 260833
+    assert O.percentile_index(0.5, 262144) == 1310
+    assert O.percentile_index(100.0, 10) == 9  # clamped (the reference reads past the end)
+
+
+def test_float_to_ushort_edges():
+    x = np.array([-1.0, 0.0, 0.5, 1.9, 65534.9, 65535.0, 65535.99, 65536.0, 1e20, np.inf, np.nan], np.float32)
+    assert list(O.float_to_ushort(x)) == [0, 0, 0, 1, 65534, 65535, 65535, 65535, 65535, 65535, 0]
+
+
+def test_autocontrast_clamps_to_one():
+    f = np.full((4, 4), 0.25, np.float32)
+    assert O.autocontrast(f, 1, 99) == (1.0, 1.0)
+
+
+def test_contrast_factor_float32():
+    f = np.array([[100.0, 200.0]], np.float32)
+    c = O.apply_contrast(f, 100.0, 200.0)
+    assert c.dtype == np.float32 and c[0, 0] == 0.0 and abs(c[0, 1] - 65535.0) < 0.1
+
+
+def test_lens_modes_agree_for_small_phase():
+    # with a small phase range the float32 restatement is within float rounding of the exact lens
+    a = O.fresnel_lens(64, 48, 852e-9, 10.0, 5.0, "fp64")
+    b = O.fresnel_lens(64, 48, 852e-9, 10.0, 5.0, "ref32")
+    assert np.abs(a - b).max() < 1e-5
+    g = O.angular_spectrum_lens(64, 64, 852e-9, 1e-4, 20.0, "fp64")
+    g32 = O.angular_spectrum_lens(64, 64, 852e-9, 1e-4, 20.0, "ref32")
+    assert np.abs(g - g32).max() < 1e-3
+    # lens crops: vertical and horizontal frames are centre crops of the square lens
+    sq = O.fresnel_lens(64, 64, 852e-9, 0.3, 20.0)
+    assert np.allclose(O.fresnel_lens(64, 32, 852e-9, 0.3, 20.0), sq[16:48, :])
+    assert np.allclose(O.fresnel_lens(32, 64, 852e-9, 0.3, 20.0), sq[:, 16:48])
+
+
+def test_angular_spectrum_identity_at_tiny_z():
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((1, 32, 32)) + 0j
+    G = O.angular_spectrum_lens(32, 32, 852e-9, 1e-12, 20.0)
+    y = O.angular_spectrum(x, G)
+    assert np.allclose(np.abs(y), np.abs(x), atol=1e-6)
+
+
+def test_unwrap_recovers_smooth_phase():
+    H = W = 64
+    y, x = np.mgrid[0:H, 0:W]
+    phase = 4.0 * np.sin(2 * np.pi * x / W) * np.cos(2 * np.pi * y / H)
+    wrapped = np.angle(np.exp(1j * phase))
+    u = O.unwrap_2d(wrapped)
+    # the Fourier unwrap recovers the phase up to scale, offset and sign (the reference's
+    # Im(.)/-2pi convention returns -phase for exp(+i phase)); the images correlate
+    a, b = O.rescale_unwrap2d(u), O.rescale_unwrap2d(phase)
+    assert abs(np.corrcoef(a.ravel(), b.ravel())[0, 1]) > 0.99
+
+
+def test_oracle_pipe_stride_and_wait():
+    s = O.OracleSettings(width=16, height=16, time_transformation="STFT", time_transformation_size=4, time_stride=4,
+                         batch_size=2, p_start=1, contrast_enabled=False)
+    p = O.OraclePipe(s)
+    raw = np.random.default_rng(0).integers(0, 4096, (2, 16, 16)).astype(np.uint16)
+    outs = [p.process_batch(raw) for _ in range(6)]
+    # batches 1,3,5 are dropped by the stride gate; batch 2 fills half the ring; outputs from batch 4 on
+    assert [o is not None for o in outs] == [False, False, False, True, False, True]
+
+
+def test_pca_pipeline_dominant_components():
+    rng = np.random.default_rng(3)
+    T = 8
+    fields = [rng.standard_normal((6, 6)) + 1j * rng.standard_normal((6, 6)) for _ in range(2)]
+    t = np.arange(T)
+    ring = np.exp(2j * np.pi * 0.1 * t)[:, None, None] * fields[0] * 3 + np.exp(2j * np.pi * 0.3 * t)[:, None, None] * fields[1]
+    w, V = O.pca_eigh(O.pca_covariance(ring))
+    assert np.all(np.diff(w) >= -1e-9)
+    P = O.pca_project(ring, V, T - 2, T - 1)
+    # the two dominant components carry the whole signal
+    assert np.isclose((np.abs(P) ** 2).sum(), (np.abs(ring) ** 2).sum(), rtol=1e-9)

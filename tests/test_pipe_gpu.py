@@ -1,0 +1,176 @@
+"""End-to-end Pipe (hv_pipe_*) against the oracle's cycle model (OraclePipe): stride gate, ring
+order, time transform, view, unwrap, renorm, fftshift, accumulation, autocontrast and uint16.
+
+Bars: the float frame fed to the contrast stage within rel-L2 <= 1e-4 of the FP64 oracle
+(argument views: wrapped-angle comparison); uint16 output identical to the oracle's contrast
+stage applied to the GPU's own float frame (bit-exact), and ring storage identical in slot order."""
+
+import numpy as np
+import pytest
+
+import holovibes_oracle as O
+from gpu_util import rel_l2, wrapped_diff
+
+import holovibes_gb300 as hv
+from holovibes_gb300.synthetic import Interferogram
+
+IMG = {0: "MODULUS", 1: "SQUARED_MODULUS", 2: "ARGUMENT"}
+SPACE = {0: "NONE", 1: "FRESNELTR", 2: "ANGULARSP"}
+TIME = {0: "NONE", 1: "STFT", 2: "PCA"}
+
+
+def _oracle_settings(fd, s):
+    return O.OracleSettings(
+        width=fd.width, height=fd.height, depth=fd.depth, space_transformation=SPACE[s.space_transformation],
+        time_transformation=TIME[s.time_transformation], time_transformation_size=s.time_transformation_size,
+        time_stride=s.time_stride, batch_size=s.batch_size, lam=s.lambda_, z=s.z_distance, pixel_size=s.pixel_size,
+        image_type=IMG[s.image_type], p_start=s.p_start, p_width=s.p_width, fft_shift=bool(s.fft_shift),
+        renorm=bool(s.renorm), renorm_constant=s.renorm_constant, accumulation=s.accumulation,
+        log_enabled=bool(s.log_enabled), contrast_enabled=bool(s.contrast_enabled),
+        contrast_auto_refresh=bool(s.contrast_auto_refresh), contrast_invert=bool(s.contrast_invert),
+        contrast_min=s.contrast_min, contrast_max=s.contrast_max, contrast_lower=s.contrast_lower,
+        contrast_upper=s.contrast_upper, reticle_display=bool(s.reticle_display), reticle_scale=s.reticle_scale,
+        unwrap_2d=bool(s.unwrap_2d), lens_mode="fp64" if s.lens_mode == 0 else "ref32")
+
+
+CASES = {
+    # name: (W, H, depth, settings overrides, batches)
+    "as_stft_mod_shift": (64, 64, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=8,
+                                           time_stride=4, batch_size=4, z_distance=0.3, pixel_size=20.0, p_start=1,
+                                           fft_shift=1, renorm=0, contrast_enabled=1, contrast_lower=0.5,
+                                           contrast_upper=99.5), 5),
+    "fresnel_pca_sqmod": (64, 64, 1, dict(space_transformation=1, time_transformation=2, time_transformation_size=16,
+                                           time_stride=8, batch_size=8, lambda_=785e-9, z_distance=0.45,
+                                           pixel_size=12.0, image_type=1, p_start=12, p_width=3, renorm=1,
+                                           contrast_enabled=1, contrast_lower=0.5, contrast_upper=99.5), 4),
+    "as_stft_arg_acc": (96, 64, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=16,
+                                         time_stride=4, batch_size=4, z_distance=0.3, pixel_size=20.0, image_type=2,
+                                         p_start=3, p_width=4, fft_shift=1, renorm=0, accumulation=3,
+                                         contrast_enabled=1, contrast_lower=0.5, contrast_upper=99.5), 9),
+    "as_stft_arg_unwrap": (64, 64, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=8,
+                                            time_stride=8, batch_size=8, z_distance=0.3, pixel_size=20.0,
+                                            image_type=2, p_start=1, p_width=0, unwrap_2d=1, renorm=1,
+                                            contrast_enabled=1, contrast_lower=0.5, contrast_upper=99.5), 3),
+    "stride_drop": (32, 32, 2, dict(space_transformation=0, time_transformation=1, time_transformation_size=4,
+                                     time_stride=6, batch_size=2, p_start=1, renorm=1, contrast_enabled=0), 12),
+    "batch_gt_T": (32, 48, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=3,
+                                    time_stride=5, batch_size=5, z_distance=0.2, pixel_size=12.0, p_start=1,
+                                    p_width=1, renorm=1, contrast_enabled=1, contrast_auto_refresh=0,
+                                    contrast_min=10.0, contrast_max=5000.0), 4),
+    "none_none_log_reticle": (64, 32, 4, dict(space_transformation=0, time_transformation=0,
+                                               time_transformation_size=2, time_stride=2, batch_size=2, p_start=1,
+                                               renorm=1, log_enabled=1, contrast_enabled=1, reticle_display=1,
+                                               reticle_scale=0.5, contrast_lower=1.0, contrast_upper=99.0), 3),
+    "fresnel_stft_ref32_big_endian": (128, 64, 2, dict(space_transformation=1, time_transformation=1,
+                                                        time_transformation_size=4, time_stride=4, batch_size=4,
+                                                        z_distance=0.3, pixel_size=20.0, p_start=2, p_width=1,
+                                                        lens_mode=1, renorm=1, fft_shift=1, contrast_enabled=1,
+                                                        contrast_invert=1), 2),
+}
+
+
+def _raw(W, H, depth, n, seed):
+    if depth == 4:
+        g = Interferogram(width=W, height=H, seed=seed, dtype=np.float32, max_value=4095)
+    elif depth == 1:
+        g = Interferogram(width=W, height=H, seed=seed, dtype=np.uint8, max_value=255)
+    else:
+        g = Interferogram(width=W, height=H, seed=seed)
+    return g.frames(0, n)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_pipe_matches_oracle(cuda, case):
+    W, H, depth, over, nbatches = CASES[case]
+    big_endian = case.endswith("big_endian")
+    fd = hv.FrameDescriptor(W, H, depth, 1 if big_endian else 0)
+    s = hv.Settings.defaults().update(**over)
+    s = s.validate(fd)
+    B = s.batch_size
+    raw = _raw(W, H, depth, B * nbatches, seed=len(case))
+    oracle = O.OraclePipe(_oracle_settings(fd, s))
+    pipe = hv.Pipe(fd, s)
+    outputs = 0
+    expected = None
+    for b in range(nbatches):
+        batch = raw[b * B:(b + 1) * B]
+        ref = oracle.process_batch(batch)
+        pipe.enqueue(O.byteswap16(batch) if big_endian else batch)
+        if ref is None:
+            assert pipe.output_count() == 0
+            continue
+        outputs += 1
+        assert pipe.output_count() == 1
+        got_u16 = pipe.pull()
+        got_f = pipe.float_frame()
+        # float frame vs FP64 oracle
+        if s.image_type == hv.IMG_ARGUMENT and not s.unwrap_2d:
+            d = np.abs(wrapped_diff(got_f, ref.float_frame))
+            assert np.mean(d > 1e-3) < 5e-3, case
+        else:
+            assert rel_l2(got_f, ref.float_frame) <= 1e-4, case
+        # contrast stage bit-exact on the GPU's own float frame
+        if s.contrast_enabled:
+            if ref.autocontrast_applied:
+                expected = O.autocontrast(got_f, s.contrast_lower, s.contrast_upper,
+                                          s.reticle_scale if s.reticle_display else None)
+            elif not s.contrast_auto_refresh:
+                expected = (s.contrast_min, s.contrast_max)
+            crange = pipe.contrast_range()
+            assert np.float32(crange[0]) == np.float32(expected[0]), case
+            assert np.float32(crange[1]) == np.float32(expected[1]), case
+            ref_u16 = O.float_to_ushort(O.apply_contrast(got_f, expected[0], expected[1], bool(s.contrast_invert)))
+        else:
+            ref_u16 = O.float_to_ushort(got_f)
+        assert np.array_equal(got_u16, ref_u16), case
+    assert outputs > 0
+    ring, start, size = pipe.ring()
+    assert start == oracle.ring.start and size == oracle.ring.size
+    assert rel_l2(ring, oracle.ring.data) <= 1e-4
+    pipe.close()
+
+
+@pytest.mark.gpu
+def test_pipe_device_push_and_partial_batches(cuda):
+    """Device frames are consumed in place; host pushes may split batches arbitrarily."""
+    import torch
+
+    W, H = 64, 64
+    fd = hv.FrameDescriptor(W, H, 2)
+    s = hv.Settings.defaults().update(space_transformation=2, time_transformation=1, time_transformation_size=8,
+                                      time_stride=4, batch_size=4, z_distance=0.3, pixel_size=20.0, p_start=1,
+                                      renorm=0, contrast_enabled=1, contrast_lower=0.5, contrast_upper=99.5)
+    raw = _raw(W, H, 2, 24, 2)
+    a, b = hv.Pipe(fd, s), hv.Pipe(fd, s)
+    cuts = [0, 3, 9, 10, 17, 24]
+    for lo, hi in zip(cuts[:-1], cuts[1:]):
+        a.enqueue(raw[lo:hi])
+    t = torch.from_numpy(raw.view(np.int16)).cuda()
+    b.enqueue(t)
+    b.sync()
+    oa, ob = a.pull_all(), b.pull_all()
+    assert len(oa) == len(ob) == 5
+    for x, y in zip(oa, ob):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.gpu
+def test_pipe_update_settings_and_errors(cuda):
+    fd = hv.FrameDescriptor(64, 64, 2)
+    s = hv.Settings.defaults().update(space_transformation=2, time_transformation=1, time_transformation_size=4,
+                                      time_stride=4, batch_size=4, z_distance=0.3, pixel_size=20.0, p_start=1)
+    p = hv.Pipe(fd, s)
+    assert p.update_settings(s) == hv.HV_NO_CHANGE
+    s2 = s.copy().update(image_type=hv.IMG_SQUARED_MODULUS)
+    assert p.update_settings(s2) == hv.HV_OK
+    with pytest.raises(hv.HoloError) as e:
+        p.pull(timeout_us=1000)
+    assert e.value.status in (hv.HV_ERR_TIMEOUT, hv.HV_NO_IN_DATA)
+    with pytest.raises(hv.HoloError):
+        hv.Pipe(hv.FrameDescriptor(1000, 64, 2), s)  # 1000 is not a supported FFT length
+    bad = s.copy().update(image_type=4)
+    with pytest.raises(hv.HoloError) as e:
+        hv.Pipe(fd, bad)
+    assert e.value.status == hv.HV_WRONG_IMG_TYPE
+    p.close()
