@@ -186,6 +186,8 @@ def _declare(L: C.CDLL) -> None:
         "hv_angular_spectrum_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
         "hv_spatial_transform": (st, [vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, i32, i32, vp]),
         "hv_fft2d": (st, [vp, vp, i32, i32, i32, i32, f32, vp]),
+        "hv_fft_rows": (st, [vp, i32, i32, vp, i32, i32, i32, vp, i32, f32, i32, i32, vp]),
+        "hv_fft_cols": (st, [vp, vp, i32, i32, i32, vp, i32, f32, i32, i32, vp]),
         "hv_time_view": (st, [vp, i32, i32, i32, vp, i32, i32, f32, i32, vp, vp, vp]),
         "hv_time_view_partials": (i32, [i32, i32]),
         "hv_stft_weights": (st, [vp, i32, i32, i32, vp]),

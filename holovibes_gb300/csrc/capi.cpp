@@ -94,6 +94,26 @@ hv_status hv_fft2d(const void* in_c64, void* out_c64, int n0, int n1, int batch,
                  S(stream));
 }
 
+hv_status hv_fft_rows(const void* in, int in_bytes, int big_endian, void* out_c64, int width, int height, int batch,
+                      const void* premul_c64, int inverse, float scale, int slot0, int nslots, void* stream)
+{
+    const int kind = raw_kind(in_bytes, big_endian);
+    if (!in || !out_c64 || kind < 0 || batch <= 0 || nslots <= 0 || slot0 < 0 || slot0 >= nslots || batch > nslots)
+        return HV_INVALID_VALUE;
+    return fft_rows_pass(in, kind, static_cast<float2*>(out_c64), width, height, batch,
+                         static_cast<const float2*>(premul_c64), inverse, scale, slot0, nslots, S(stream));
+}
+
+hv_status hv_fft_cols(const void* in_c64, void* out_c64, int width, int height, int batch, const void* postmul_c64,
+                      int mode, float scale, int slot0, int nslots, void* stream)
+{
+    if (!in_c64 || !out_c64 || batch <= 0 || mode < 0 || mode > 2 || (mode == 2 && !postmul_c64) || nslots <= 0 ||
+        slot0 < 0 || slot0 >= nslots || batch > nslots)
+        return HV_INVALID_VALUE;
+    return fft_cols_pass(static_cast<const float2*>(in_c64), static_cast<float2*>(out_c64), width, height, batch,
+                         static_cast<const float2*>(postmul_c64), mode, scale, slot0, nslots, S(stream));
+}
+
 hv_status hv_time_view(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
                        int img_type, float scale, int shift, float* out_f32, double* partials_f64, void* stream)
 {

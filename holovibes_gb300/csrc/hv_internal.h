@@ -22,6 +22,10 @@ hv_status make_spectral_lens(float2* lens, int W, int H, float lam, float z, flo
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
                             float2* work, float2* ring, int slot0, int nslots, cudaStream_t st);
 hv_status fft2d(const float2* in, float2* out, int n0, int n1, int batch, int inverse, float scale, cudaStream_t st);
+hv_status fft_rows_pass(const void* in, int kind, float2* out, int W, int H, int batch, const float2* premul,
+                        int inverse, float scale, int slot0, int nslots, cudaStream_t st);
+hv_status fft_cols_pass(const float2* in, float2* out, int W, int H, int batch, const float2* postmul, int mode,
+                        float scale, int slot0, int nslots, cudaStream_t st);
 
 // time_transform.cu
 int time_view_partials(int W, int H);

@@ -417,6 +417,22 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
     return HV_INVALID_VALUE;
 }
 
+hv_status fft_rows_pass(const void* in, int kind, float2* out, int W, int H, int batch, const float2* premul,
+                        int inverse, float scale, int slot0, int nslots, cudaStream_t st)
+{
+    const size_t HW = static_cast<size_t>(W) * H;
+    RowPass r{in, kind, HW, out, FrameMap{HW, slot0, nslots}, premul, H, inverse, scale};
+    return fft_rows(r, W, batch, st);
+}
+
+hv_status fft_cols_pass(const float2* in, float2* out, int W, int H, int batch, const float2* postmul, int mode,
+                        float scale, int slot0, int nslots, cudaStream_t st)
+{
+    const size_t HW = static_cast<size_t>(W) * H;
+    ColPass c{in, HW, out, FrameMap{HW, slot0, nslots}, postmul, W, mode, scale};
+    return fft_cols(c, H, batch, st);
+}
+
 hv_status fft2d(const float2* in, float2* out, int n0, int n1, int batch, int inverse, float scale, cudaStream_t st)
 {
     if (!fft_size_supported(n0) || !fft_size_supported(n1))

@@ -194,6 +194,18 @@ hv_status hv_spatial_transform(const void* raw, int raw_bytes, int big_endian, i
 hv_status hv_fft2d(const void* in_c64, void* out_c64, int n0, int n1, int batch, int inverse, float scale,
                    void* stream);
 
+/* The two passes of the spatial stage, exposed separately (timing, custom pipelines).
+ * Row pass: raw/complex input (in_bytes 1, 2, 4 or 8) converted, multiplied by premul (H x W, or
+ * NULL), FFT along each row of `width` samples (inverse: conj in / conj out), times `scale`,
+ * written to slots (slot0 + b) % nslots of out. Column pass: FFT along each column of `height`
+ * samples; mode 0 forward, 1 inverse, 2 forward * postmul (H x W) then inverse (the angular
+ * spectrum's middle pass). Together they replace cufftXtExec with the 2-D plan of
+ * Backend/sources/core/icompute.cc:151-175 and the apply_mask / kernel_complex_divide passes. */
+hv_status hv_fft_rows(const void* in, int in_bytes, int big_endian, void* out_c64, int width, int height, int batch,
+                      const void* premul_c64, int inverse, float scale, int slot0, int nslots, void* stream);
+hv_status hv_fft_cols(const void* in_c64, void* out_c64, int width, int height, int batch, const void* postmul_c64,
+                      int mode, float scale, int slot0, int nslots, void* stream);
+
 /* Fused time transform + view: for every pixel, X_k = sum_t ring[t] * W[k][t] for k < K,
  * then out = scale * mean_k f(X_k) with f = |.|, |.|^2 or atan2 (img_type), written at the
  * fftshift-ed position when `shift` is set. `weights_c64` is K x T complex64. Per-CTA partial

@@ -25,11 +25,31 @@ bit when the float input frame is identical.
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
 
+try:  # multi-threaded pocketfft when scipy is present (FFTW is not available on these hosts)
+    import scipy.fft as _sfft
+except ImportError:  # pragma: no cover
+    _sfft = None
+
 F32 = np.float32
+FFT_WORKERS = int(os.environ.get("HV_ORACLE_FFT_WORKERS", "0")) or (os.cpu_count() or 1)
+
+
+def fft2(a: np.ndarray, axes=(-2, -1)) -> np.ndarray:
+    if _sfft is not None:
+        return _sfft.fft2(a, axes=axes, workers=FFT_WORKERS)
+    return np.fft.fft2(a, axes=axes)
+
+
+def ifft2(a: np.ndarray, axes=(-2, -1)) -> np.ndarray:
+    """Normalised inverse (1/N), like numpy.fft.ifft2."""
+    if _sfft is not None:
+        return _sfft.ifft2(a, axes=axes, workers=FFT_WORKERS)
+    return np.fft.ifft2(a, axes=axes)
 
 # ----------------------------------------------------------------------------------------
 # a1: raw -> complex  (Backend/cuda_sources/tools_conversion.cu:107-171)
@@ -162,13 +182,13 @@ def angular_spectrum_lens(W: int, H: int, lam: float, z: float, pixel_size_um: f
 
 def fresnel_transform(frames: np.ndarray, lens: np.ndarray) -> np.ndarray:
     """x <- FFT2(x * L), forward, unnormalised, no shift (fresnel_transform.cu:74-79)."""
-    return np.fft.fft2(frames * lens[None], axes=(-2, -1))
+    return fft2(frames * lens[None], axes=(-2, -1))
 
 
 def angular_spectrum(frames: np.ndarray, lens: np.ndarray) -> np.ndarray:
     """x <- IFFT2(FFT2(x) * G) / (H*W): cuFFT's unnormalised inverse then kernel_complex_divide
     (angular_spectrum.cu:47-61). numpy's ifft2 carries the same 1/(H*W)."""
-    return np.fft.ifft2(np.fft.fft2(frames, axes=(-2, -1)) * lens[None], axes=(-2, -1))
+    return ifft2(fft2(frames, axes=(-2, -1)) * lens[None], axes=(-2, -1))
 
 
 def spatial_transform(frames: np.ndarray, kind: str, lens: np.ndarray | None) -> np.ndarray:
@@ -336,10 +356,10 @@ def unwrap_2d(phase: np.ndarray) -> np.ndarray:
     n0, n1 = W, H  # plan(width, height): slowest dimension = width
 
     def fft(a):
-        return np.fft.fft2(a.reshape(n0, n1)).reshape(-1)
+        return fft2(a.reshape(n0, n1)).reshape(-1)
 
     def ifft(a):  # unnormalised inverse
-        return np.fft.ifft2(a.reshape(n0, n1)).reshape(-1) * (n0 * n1)
+        return ifft2(a.reshape(n0, n1)).reshape(-1) * (n0 * n1)
 
     Z = fft(z)
     gx = ifft(Z * sfx) * (1j * M_2PI_F)

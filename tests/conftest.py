@@ -31,3 +31,11 @@ def cuda():
 
     hv.lib()
     return torch
+
+
+@pytest.fixture(autouse=True)
+def _release_device_copies():
+    yield
+    mod = sys.modules.get("gpu_util")
+    if mod is not None:
+        mod.release()

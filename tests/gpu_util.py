@@ -8,7 +8,22 @@ import torch
 import holovibes_gb300 as hv
 
 
+_KEEP: list = []  # device copies stay alive until the end of the test (pointers outlive temporaries)
+
+
+def release() -> None:
+    if _KEEP:
+        torch.cuda.synchronize()
+        _KEEP.clear()
+
+
 def dev(a: np.ndarray) -> torch.Tensor:
+    t = _dev(a)
+    _KEEP.append(t)
+    return t
+
+
+def _dev(a: np.ndarray) -> torch.Tensor:
     a = np.ascontiguousarray(a)
     if a.dtype == np.complex64:
         t = torch.from_numpy(a.view(np.float32).copy())
