@@ -193,6 +193,8 @@ def _declare(L: C.CDLL) -> None:
         "hv_stft_weights": (st, [vp, i32, i32, i32, vp]),
         "hv_pca_covariance": (st, [vp, i32, sz, vp, vp, vp]),
         "hv_pca_cov_workspace": (sz, [i32, sz]),
+        "hv_pca_covariance_mode": (None, [i32]),
+        "hv_pca_covariance_status": (st, [vp]),
         "hv_pca_eigh": (st, [vp, i32, vp, vp, i32, i32, vp, vp, vp]),
         "hv_pca_eigh_workspace": (sz, [i32]),
         "hv_unwrap_2d": (st, [vp, vp, i32, i32, vp, vp]),

@@ -142,6 +142,15 @@ hv_status hv_pca_covariance(const void* ring_c64, int T, size_t npix, void* cov_
 
 size_t hv_pca_cov_workspace(int T, size_t npix) { return pca_cov_workspace(T, npix); }
 
+void hv_pca_covariance_mode(int mode) { set_cov_mode(mode); }
+
+hv_status hv_pca_covariance_status(const void* work)
+{
+    if (!work)
+        return HV_INVALID_VALUE;
+    return pca_cov_status(work);
+}
+
 hv_status hv_pca_eigh(void* cov_c128, int T, double* eigenvalues, void* eigenvectors_c128, int pmin, int pmax,
                       void* weights_c64, void* work, void* stream)
 {

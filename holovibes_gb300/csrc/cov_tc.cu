@@ -1,0 +1,398 @@
+// PCA covariance on the 5th-generation tensor cores (tcgen05, TMEM accumulator), split-BF16.
+//
+// Reference: cov = H^H H with cublasCgemm3m (Backend/sources/compute/matrix_operations.cc:9-26),
+// H the HW x T column-major view of the time ring.
+//
+// Formulation: Y is the 2T x HW real matrix with rows 2t = Re(ring[t]) and 2t+1 = Im(ring[t]);
+// G = Y Y^T (2T x 2T) gives C_re[i][j] = G[2i][2j] + G[2i+1][2j+1] and
+// C_im[i][j] = G[2i][2j+1] - G[2i+1][2j]. Each FP32 sample is split y = yh + yl with yh, yl in
+// BF16, and G ~= Yh Yh^T + Yh Yl^T + Yl Yh^T (the Yl Yl^T term is below FP32 resolution), so
+// three BF16 MMAs with FP32 accumulation per K step recover ~16-bit-mantissa accuracy.
+//
+// Kernel: one CTA per SM-slot walks a contiguous range of 64-pixel chunks. All warps load a chunk
+// (coalesced float2), split it and write Yh / Yl into shared memory in the no-swizzle K-major
+// canonical layout (8-row x 16-byte core matrices); one thread issues the MMAs
+// (M = 128 rows of Y, rows >= 2T are zero; N = 2T rounded to 16; K = 16) into a TMEM
+// accumulator; tcgen05.commit signals an mbarrier per buffer so loads of chunk c+2 wait only
+// for the MMAs of chunk c (two buffers). Every wait is bounded and reports through an error flag.
+// Per-CTA partial G tiles are summed in FP64 by k_cov_tc_reduce.
+#include <cuda_bf16.h>
+
+#include "hv_common.cuh"
+#include "hv_internal.h"
+
+namespace hv {
+
+namespace {
+
+constexpr int TC_THREADS = 256;
+constexpr int TC_KC = 64;           // pixels (K elements) per chunk
+constexpr int TC_ROWS = 128;        // M rows of the operand tile (2T <= 128, zero padded)
+constexpr int TILE_BYTES = TC_ROWS * TC_KC * 2;  // one BF16 tile: 16 KB
+constexpr uint32_t kSpinLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Canonical no-swizzle K-major layout: element (r, k) of a 128 x 64 BF16 tile.
+// Core matrix = 8 rows x 8 k (16 B per row, 128 B); k-groups adjacent (LBO = 128 B),
+// row groups 8 k-groups apart (SBO = 1024 B).
+__device__ __forceinline__ uint32_t tile_offset(int r, int kgroup)
+{
+    return static_cast<uint32_t>((r >> 3) * 1024 + kgroup * 128 + (r & 7) * 16);
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
+{
+    const uint64_t lbo = 128 >> 4, sbo = 1024 >> 4;
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((addr & 0x3FFFF) >> 4);
+    d |= lbo << 16;
+    d |= sbo << 32;
+    d |= 1ull << 46;  // descriptor version for tcgen05
+    // base offset 0, LBO mode 0, swizzle none (bits 61-63 = 0)
+    return d;
+}
+
+// kind::f16 instruction descriptor: D F32, A/B BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+           (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Bounded wait for phase `parity` of the barrier; returns false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+    const uint32_t addr = smem_u32(bar);
+    for (uint32_t i = 0; i < kSpinLimit; ++i)
+    {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+        v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b)
+{
+    return static_cast<uint32_t>(__bfloat16_as_ushort(a)) | (static_cast<uint32_t>(__bfloat16_as_ushort(b)) << 16);
+}
+
+// part: [gridDim.x][2T][2T] FP32 partial G; err: set to 1 when a bounded wait gave up.
+__global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict__ ring, int T, size_t npix,
+                                                       size_t chunks_per_cta, int N, uint32_t tmem_cols,
+                                                       float* __restrict__ part, int* __restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    // [buf][hi/lo] tiles
+    uint8_t* tiles = smem;
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int rows = 2 * T;
+    const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
+    const size_t c_begin = blockIdx.x * chunks_per_cta;
+    size_t c_end = c_begin + chunks_per_cta;
+    if (c_end > nchunks)
+        c_end = nchunks;
+
+    // zero all tiles once (rows >= 2T stay zero)
+    for (int i = tid; i < 4 * TILE_BYTES / 16; i += TC_THREADS)
+        reinterpret_cast<uint4*>(tiles)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0)
+    {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        s_fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = instr_desc(TC_ROWS, N);
+
+    // work items per chunk: T rows x 8 k-groups (8 pixels each)
+    const int items = T * (TC_KC / 8);
+    size_t it = 0;
+    bool fail = false;
+    for (size_t c = c_begin; c < c_end; ++c, ++it)
+    {
+        const int buf = static_cast<int>(it & 1);
+        if (it >= 2)
+        {
+            // MMAs of chunk it-2 read this buffer; their commit is use number (it-2)/2 of bars[buf]
+            if (!mbar_wait(&bars[buf], static_cast<uint32_t>(((it - 2) >> 1) & 1)))
+                fail = true;
+        }
+        uint8_t* th = tiles + buf * 2 * TILE_BYTES;
+        uint8_t* tl = th + TILE_BYTES;
+        const size_t p0 = c * TC_KC;
+        for (int w = tid; w < items; w += TC_THREADS)
+        {
+            const int t = w % T, g = w / T;
+            const size_t p = p0 + static_cast<size_t>(g) * 8;
+            const float2* src = ring + static_cast<size_t>(t) * npix + p;
+            float2 v[8];
+            if (p + 8 <= npix)
+            {
+                const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                {
+                    const float4 f = __ldg(s4 + q);
+                    v[2 * q] = make_float2(f.x, f.y);
+                    v[2 * q + 1] = make_float2(f.z, f.w);
+                }
+            }
+            else
+            {
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    v[q] = (p + q < npix) ? __ldg(src + q) : make_float2(0.f, 0.f);
+            }
+            uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+            {
+                const __nv_bfloat16 a0 = __float2bfloat16_rn(v[2 * q].x), a1 = __float2bfloat16_rn(v[2 * q + 1].x);
+                const __nv_bfloat16 b0 = __float2bfloat16_rn(v[2 * q].y), b1 = __float2bfloat16_rn(v[2 * q + 1].y);
+                rh[q] = pack_bf16(a0, a1);
+                ih[q] = pack_bf16(b0, b1);
+                rl[q] = pack_bf16(__float2bfloat16_rn(v[2 * q].x - __bfloat162float(a0)),
+                                  __float2bfloat16_rn(v[2 * q + 1].x - __bfloat162float(a1)));
+                il[q] = pack_bf16(__float2bfloat16_rn(v[2 * q].y - __bfloat162float(b0)),
+                                  __float2bfloat16_rn(v[2 * q + 1].y - __bfloat162float(b1)));
+            }
+            const uint32_t ore = tile_offset(2 * t, g), oim = tile_offset(2 * t + 1, g);
+            *reinterpret_cast<uint4*>(th + ore) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+            *reinterpret_cast<uint4*>(th + oim) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+            *reinterpret_cast<uint4*>(tl + ore) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+            *reinterpret_cast<uint4*>(tl + oim) = make_uint4(il[0], il[1], il[2], il[3]);
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0)
+        {
+            tc_fence_after();
+            const uint32_t ah = smem_u32(th), al = smem_u32(tl);
+#pragma unroll
+            for (int s = 0; s < TC_KC / 16; ++s)
+            {
+                const uint64_t dh = smem_desc(ah + s * 256), dl = smem_desc(al + s * 256);
+                const uint32_t acc0 = (it > 0 || s > 0) ? 1u : 0u;
+                mma_bf16(tmem, dh, dh, idesc, acc0);  // Yh Yh^T
+                mma_bf16(tmem, dh, dl, idesc, 1u);    // Yh Yl^T
+                mma_bf16(tmem, dl, dh, idesc, 1u);    // Yl Yh^T
+            }
+            mma_commit(&bars[buf]);
+        }
+    }
+    // drain: the last commit on each used buffer
+    const size_t used = it;
+    if (used >= 1)
+    {
+        const size_t last = used - 1;
+        if (!mbar_wait(&bars[last & 1], static_cast<uint32_t>((last >> 1) & 1)))
+            fail = true;
+    }
+    if (used >= 2)
+    {
+        const size_t prev = used - 2;
+        if (!mbar_wait(&bars[prev & 1], static_cast<uint32_t>((prev >> 1) & 1)))
+            fail = true;
+    }
+    if (fail)
+        s_fail = 1;
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // epilogue: warps 0-3 read TMEM lanes 32w..32w+31 (row r of G), columns 0..N-1
+    if (warp < 4)
+    {
+        const int r = warp * 32 + lane;
+        float* dst = part + static_cast<size_t>(blockIdx.x) * rows * rows;
+        for (int c0 = 0; c0 < N; c0 += 16)
+        {
+            float v[16];
+            const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
+            tmem_ld16(taddr, v);
+            if (r < rows && used > 0)
+            {
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (c0 + i < rows)
+                        dst[static_cast<size_t>(r) * rows + c0 + i] = v[i];
+            }
+            else if (r < rows)
+            {
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (c0 + i < rows)
+                        dst[static_cast<size_t>(r) * rows + c0 + i] = 0.f;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+    {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols) : "memory");
+    }
+    if (tid == 0 && s_fail)
+        atomicExch(err, 1);
+}
+
+// cov[i][j] (complex128, row-major, both triangles, zeroed before) += a slice of the FP32
+// partial G tiles, summed in FP64.
+__global__ void k_cov_tc_reduce(const float* __restrict__ part, int T, int nparts, int per_slice,
+                                double2* __restrict__ cov)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= T * T)
+        return;
+    const int i = e / T, j = e % T;
+    const int R = 2 * T;
+    double g00 = 0, g11 = 0, g01 = 0, g10 = 0;
+    const int c0 = blockIdx.y * per_slice;
+    const int c1 = min(nparts, c0 + per_slice);
+#pragma unroll 4
+    for (int c = c0; c < c1; ++c)
+    {
+        const float* G = part + static_cast<size_t>(c) * R * R;
+        g00 += G[(2 * i) * R + 2 * j];
+        g11 += G[(2 * i + 1) * R + 2 * j + 1];
+        g01 += G[(2 * i) * R + 2 * j + 1];
+        g10 += G[(2 * i + 1) * R + 2 * j];
+    }
+    atomicAdd(&cov[e].x, g00 + g11);
+    atomicAdd(&cov[e].y, g01 - g10);
+}
+
+struct TcPlan
+{
+    int ctas;
+    size_t chunks_per_cta;
+    int N;
+    uint32_t cols;
+};
+
+TcPlan tc_plan(int T, size_t npix)
+{
+    TcPlan p;
+    const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
+    int ctas = 152 * 2;
+    if (static_cast<size_t>(ctas) > nchunks)
+        ctas = static_cast<int>(nchunks);
+    if (ctas < 1)
+        ctas = 1;
+    p.chunks_per_cta = (nchunks + ctas - 1) / ctas;
+    p.ctas = static_cast<int>((nchunks + p.chunks_per_cta - 1) / p.chunks_per_cta);
+    p.N = (2 * T + 15) / 16 * 16;
+    uint32_t cols = 32;
+    while (cols < static_cast<uint32_t>(p.N))
+        cols <<= 1;
+    p.cols = cols;
+    return p;
+}
+
+}  // namespace
+
+bool cov_tc_supported(int T) { return T >= 1 && 2 * T <= TC_ROWS; }
+
+size_t cov_tc_workspace(int T, size_t npix)
+{
+    const TcPlan p = tc_plan(T, npix);
+    return static_cast<size_t>(p.ctas) * 4 * T * T * sizeof(float) + 256;
+}
+
+hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, cudaStream_t st)
+{
+    if (!cov_tc_supported(T) || npix == 0)
+        return HV_ERR_UNSUPPORTED;
+    if (npix % 8 != 0 || (reinterpret_cast<uintptr_t>(ring) & 15) != 0)
+    {
+        set_last_error_msg("tensor-core covariance needs 16-byte aligned frames of a multiple of 8 pixels");
+        return HV_ERR_UNSUPPORTED;
+    }
+    const TcPlan p = tc_plan(T, npix);
+    const size_t smem = 4 * static_cast<size_t>(TILE_BYTES) + 1024;
+    HV_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    float* part = static_cast<float*>(work);
+    k_cov_tc<<<p.ctas, TC_THREADS, smem, st>>>(ring, T, npix, p.chunks_per_cta, p.N, p.cols, part, err);
+    HV_LAUNCH_CHECK();
+    const int slices = p.ctas < 16 ? p.ctas : 16;
+    const int per = (p.ctas + slices - 1) / slices;
+    k_cov_tc_reduce<<<dim3((T * T + 255) / 256, (p.ctas + per - 1) / per), 256, 0, st>>>(part, T, p.ctas, per, cov);
+    HV_LAUNCH_CHECK();
+    count_launch(2);
+    return HV_OK;
+}
+
+}  // namespace hv

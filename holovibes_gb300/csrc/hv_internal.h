@@ -34,6 +34,12 @@ hv_status time_view(const float2* ring, int T, int W, int H, const float2* weigh
 hv_status stft_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
 hv_status delta_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
 size_t pca_cov_workspace(int T, size_t npix);
+void set_cov_mode(int mode);
+hv_status pca_cov_status(const void* work);
+// cov_tc.cu
+bool cov_tc_supported(int T);
+size_t cov_tc_workspace(int T, size_t npix);
+hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, cudaStream_t st);
 hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st);
 size_t pca_eigh_workspace(int T);
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,

@@ -306,8 +306,10 @@ __global__ void __launch_bounds__(COV_THREADS) k_cov_partial(const float2* __res
             dst[(ri * 2 + a) * COV_TILE + cj * 2 + b] = acc[a][b];
 }
 
+// Sums the partial tiles of a slice of chunks in FP64 and adds them atomically into cov
+// (zeroed before); grid.y splits the chunks so the reduction is not latency bound.
 __global__ void k_cov_reduce(const float2* __restrict__ part, int T, int tiles1d, int ntiles, int chunks,
-                             double2* __restrict__ cov)
+                             int chunks_per_slice, double2* __restrict__ cov)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;  // over T*T
     if (e >= T * T)
@@ -321,38 +323,77 @@ __global__ void k_cov_reduce(const float2* __restrict__ part, int T, int tiles1d
         j = s;
     }
     const int ti = i / COV_TILE, tj = j / COV_TILE;
-    // tile index of (ti, tj), ti <= tj
     const int tile = ti * tiles1d - ti * (ti - 1) / 2 + (tj - ti);
     const int li = i % COV_TILE, lj = j % COV_TILE;
+    const int c0 = blockIdx.y * chunks_per_slice;
+    const int c1 = min(chunks, c0 + chunks_per_slice);
     double re = 0.0, im = 0.0;
-    for (int c = 0; c < chunks; ++c)
+#pragma unroll 4
+    for (int c = c0; c < c1; ++c)
     {
         const float2 v = part[(static_cast<size_t>(c) * ntiles + tile) * COV_TILE * COV_TILE + li * COV_TILE + lj];
         re += v.x;
         im += v.y;
     }
-    // cov[i][j] stored row-major at e; both triangles
-    cov[e] = mirror ? make_double2(re, -im) : make_double2(re, im);
+    atomicAdd(&cov[e].x, re);
+    atomicAdd(&cov[e].y, mirror ? -im : im);
 }
+
+static int g_cov_mode = 0;  // 0 auto (tensor cores when supported), 1 SIMT, 2 tensor cores
+
+constexpr size_t COV_FLAGS = 256;
 
 size_t pca_cov_workspace(int T, size_t npix)
 {
     const CovPlan p = cov_plan(T, npix);
-    return static_cast<size_t>(p.chunks) * p.ntiles * COV_TILE * COV_TILE * sizeof(float2);
+    size_t simt = static_cast<size_t>(p.chunks) * p.ntiles * COV_TILE * COV_TILE * sizeof(float2);
+    size_t tc = cov_tc_supported(T) ? cov_tc_workspace(T, npix) : 0;
+    return COV_FLAGS + (simt > tc ? simt : tc);
 }
+
+void set_cov_mode(int mode) { g_cov_mode = mode; }
 
 hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st)
 {
     if (T <= 0 || npix == 0)
         return HV_INVALID_VALUE;
+    int* err = static_cast<int*>(work);
+    char* ws = static_cast<char*>(work) + COV_FLAGS;
+    HV_CUDA_TRY(cudaMemsetAsync(cov, 0, static_cast<size_t>(T) * T * sizeof(double2), st));
+    const bool tc_ok = cov_tc_supported(T) && npix % 8 == 0 && (reinterpret_cast<uintptr_t>(ring) & 15) == 0;
+    if ((g_cov_mode == 0 && tc_ok) || g_cov_mode == 2)
+    {
+        if (!tc_ok)
+        {
+            set_last_error_msg("tensor-core covariance unsupported for this shape");
+            return HV_ERR_UNSUPPORTED;
+        }
+        HV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+        return cov_tc(ring, T, npix, cov, ws, err, st);
+    }
     const CovPlan p = cov_plan(T, npix);
-    float2* part = static_cast<float2*>(work);
+    float2* part = reinterpret_cast<float2*>(ws);
     dim3 grid(p.ntiles, p.chunks);
     k_cov_partial<<<grid, COV_THREADS, 0, st>>>(ring, T, npix, p.tiles1d, p.chunk_px, part);
     HV_LAUNCH_CHECK();
-    k_cov_reduce<<<(T * T + 255) / 256, 256, 0, st>>>(part, T, p.tiles1d, p.ntiles, p.chunks, cov);
+    const int slices = p.chunks < 32 ? p.chunks : 32;
+    const int per = (p.chunks + slices - 1) / slices;
+    dim3 rgrid((T * T + 255) / 256, (p.chunks + per - 1) / per);
+    k_cov_reduce<<<rgrid, 256, 0, st>>>(part, T, p.tiles1d, p.ntiles, p.chunks, per, cov);
     HV_LAUNCH_CHECK();
     count_launch(2);
+    return HV_OK;
+}
+
+hv_status pca_cov_status(const void* work)
+{
+    int flag = 0;
+    HV_CUDA_TRY(cudaMemcpy(&flag, work, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag)
+    {
+        set_last_error_msg("tensor-core covariance: a bounded wait gave up");
+        return HV_ERR_TIMEOUT;
+    }
     return HV_OK;
 }
 
@@ -521,6 +562,205 @@ __global__ void __launch_bounds__(JAC_THREADS) k_jacobi(double2* A, double2* V, 
         evals[i] = A[i * T + i].x;
 }
 
+// Shared-memory variant for T <= 64 (A and V resident in shared memory, one CTA). The step
+// update works on 2 x 2 blocks: for row pair k1 and column pair k2, the block of A becomes
+// J1^H B J2 and the mirrored block its conjugate transpose (A stays Hermitian), so each step is
+// one barrier-separated phase; steps whose rotations are all identities are skipped.
+constexpr int JS_THREADS = 256;
+constexpr int JS_MAX_T = 64;
+
+__global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __restrict__ Ain, double2* __restrict__ Vout,
+                                                            int T, int Tp, double* __restrict__ evals)
+{
+    extern __shared__ double2 js[];
+    const int LD = T + 1;
+    double2* A = js;
+    double2* V = js + T * LD;
+    __shared__ int pp[JS_MAX_T / 2], pq[JS_MAX_T / 2], act[JS_MAX_T / 2];
+    __shared__ double rc[JS_MAX_T / 2], rs[JS_MAX_T / 2], rcp[JS_MAX_T / 2], rsp[JS_MAX_T / 2];
+    __shared__ double red[JS_THREADS / 32][2];
+    __shared__ int s_done;
+    const int tid = threadIdx.x;
+    const int npairs = Tp / 2;
+    for (int e = tid; e < T * T; e += JS_THREADS)
+    {
+        const int i = e / T, j = e % T;
+        A[i * LD + j] = Ain[e];
+        V[i * LD + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    }
+    __syncthreads();
+    const int nblocks = npairs * (npairs + 1) / 2;
+    for (int sweep = 0; sweep < JAC_MAX_SWEEPS; ++sweep)
+    {
+        double off = 0.0, nrm = 0.0;
+        for (int e = tid; e < T * T; e += JS_THREADS)
+        {
+            const int i = e / T, j = e % T;
+            const double2 a = A[i * LD + j];
+            const double m = a.x * a.x + a.y * a.y;
+            nrm += m;
+            if (i != j)
+                off += m;
+        }
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            off += __shfl_down_sync(0xffffffffu, off, o);
+            nrm += __shfl_down_sync(0xffffffffu, nrm, o);
+        }
+        if ((tid & 31) == 0)
+        {
+            red[tid >> 5][0] = off;
+            red[tid >> 5][1] = nrm;
+        }
+        __syncthreads();
+        if (tid == 0)
+        {
+            double so = 0.0, sn = 0.0;
+            for (int i = 0; i < JS_THREADS / 32; ++i)
+            {
+                so += red[i][0];
+                sn += red[i][1];
+            }
+            s_done = (so <= 1e-30 * sn || sn == 0.0) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_done)
+            break;
+        for (int step = 0; step < Tp - 1; ++step)
+        {
+            int active = 0;
+            if (tid < npairs)
+            {
+                const int k = tid;
+                int a, b;
+                if (k == 0)
+                {
+                    a = Tp - 1;
+                    b = step % (Tp - 1);
+                }
+                else
+                {
+                    a = (step + k) % (Tp - 1);
+                    b = (step - k + (Tp - 1)) % (Tp - 1);
+                }
+                const int p = a < b ? a : b, q = a < b ? b : a;
+                pp[k] = p;
+                pq[k] = q;
+                double c = 1.0, s = 0.0, cph = 1.0, sph = 0.0;
+                if (q < T)
+                {
+                    const double2 apq = A[p * LD + q];
+                    const double mag = hypot(apq.x, apq.y);
+                    const double app = A[p * LD + p].x, aqq = A[q * LD + q].x;
+                    if (mag > 1e-300 && mag > 1e-18 * sqrt(fabs(app * aqq)))
+                    {
+                        cph = apq.x / mag;
+                        sph = apq.y / mag;
+                        const double tau = (aqq - app) / (2.0 * mag);
+                        const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                        c = 1.0 / sqrt(1.0 + t * t);
+                        s = t * c;
+                        active = 1;
+                    }
+                }
+                rc[k] = c;
+                rs[k] = s;
+                rcp[k] = cph;
+                rsp[k] = sph;
+                act[k] = active;
+            }
+            if (!__syncthreads_or(active))
+                continue;
+            // A <- J^H A J, block by block (k1 >= k2) with the mirror block
+            for (int e = tid; e < nblocks; e += JS_THREADS)
+            {
+                int k1 = static_cast<int>((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+                while (k1 * (k1 + 1) / 2 > e)
+                    --k1;
+                while ((k1 + 1) * (k1 + 2) / 2 <= e)
+                    ++k1;
+                const int k2 = e - k1 * (k1 + 1) / 2;
+                if (!act[k1] && !act[k2])
+                    continue;
+                const int r0 = pp[k1], r1 = pq[k1], c0 = pp[k2], c1 = pq[k2];
+                const bool hr1 = r1 < T, hc1 = c1 < T;
+                double2 B[2][2];
+                B[0][0] = A[r0 * LD + c0];
+                B[0][1] = hc1 ? A[r0 * LD + c1] : make_double2(0, 0);
+                B[1][0] = hr1 ? A[r1 * LD + c0] : make_double2(0, 0);
+                B[1][1] = (hr1 && hc1) ? A[r1 * LD + c1] : make_double2(0, 0);
+                // X = B J2, J2 = [[c, s], [-s e^{-i phi}, c e^{-i phi}]]
+                const double c2 = rc[k2], s2 = rs[k2];
+                const double2 em2 = make_double2(rcp[k2], -rsp[k2]);
+                double2 X[2][2];
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+                {
+                    const double2 b1 = zmul(B[r][1], em2);
+                    X[r][0] = make_double2(c2 * B[r][0].x - s2 * b1.x, c2 * B[r][0].y - s2 * b1.y);
+                    X[r][1] = make_double2(s2 * B[r][0].x + c2 * b1.x, s2 * B[r][0].y + c2 * b1.y);
+                }
+                // Y = J1^H X: row0 = c X0 - s e^{i phi} X1, row1 = s X0 + c e^{i phi} X1
+                const double c1r = rc[k1], s1r = rs[k1];
+                const double2 ep1 = make_double2(rcp[k1], rsp[k1]);
+                double2 Y[2][2];
+#pragma unroll
+                for (int cc = 0; cc < 2; ++cc)
+                {
+                    const double2 x1 = zmul(X[1][cc], ep1);
+                    Y[0][cc] = make_double2(c1r * X[0][cc].x - s1r * x1.x, c1r * X[0][cc].y - s1r * x1.y);
+                    Y[1][cc] = make_double2(s1r * X[0][cc].x + c1r * x1.x, s1r * X[0][cc].y + c1r * x1.y);
+                }
+                if (k1 == k2 && act[k1])
+                {
+                    Y[0][1] = make_double2(0, 0);
+                    Y[1][0] = make_double2(0, 0);
+                    Y[0][0].y = 0.0;
+                    Y[1][1].y = 0.0;
+                }
+                A[r0 * LD + c0] = Y[0][0];
+                if (hc1)
+                    A[r0 * LD + c1] = Y[0][1];
+                if (hr1)
+                    A[r1 * LD + c0] = Y[1][0];
+                if (hr1 && hc1)
+                    A[r1 * LD + c1] = Y[1][1];
+                if (k1 != k2)
+                {
+                    A[c0 * LD + r0] = make_double2(Y[0][0].x, -Y[0][0].y);
+                    if (hc1)
+                        A[c1 * LD + r0] = make_double2(Y[0][1].x, -Y[0][1].y);
+                    if (hr1)
+                        A[c0 * LD + r1] = make_double2(Y[1][0].x, -Y[1][0].y);
+                    if (hr1 && hc1)
+                        A[c1 * LD + r1] = make_double2(Y[1][1].x, -Y[1][1].y);
+                }
+            }
+            // V <- V J for the active pairs
+            for (int e = tid; e < npairs * T; e += JS_THREADS)
+            {
+                const int k = e / T, r = e % T;
+                if (!act[k])
+                    continue;
+                const int p = pp[k], q = pq[k];
+                const double c = rc[k], s = rs[k];
+                const double2 em = make_double2(rcp[k], -rsp[k]);
+                const double2 vp = V[r * LD + p], vq = zmul(V[r * LD + q], em);
+                V[r * LD + p] = make_double2(c * vp.x - s * vq.x, c * vp.y - s * vq.y);
+                V[r * LD + q] = make_double2(s * vp.x + c * vq.x, s * vp.y + c * vq.y);
+            }
+            __syncthreads();
+        }
+    }
+    for (int e = tid; e < T * T; e += JS_THREADS)
+    {
+        const int i = e / T, j = e % T;
+        Vout[e] = V[i * LD + j];
+    }
+    for (int i = tid; i < T; i += JS_THREADS)
+        evals[i] = A[i * LD + i].x;
+}
+
 // Sort eigenpairs ascending (rank = number of smaller values, ties by index), write the
 // eigenvectors column-major like cusolverDnCheevd (evec[t + j*T]) and the PCA weights.
 __global__ void k_eig_sort(const double* evals_in, const double2* V, int T, double* evals, double2* evecs, int pmin,
@@ -568,7 +808,16 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     double* ev_unsorted = reinterpret_cast<double*>(base + off);
     off += static_cast<size_t>(T) * sizeof(double);
     int* pairs = reinterpret_cast<int*>(base + off);
-    k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);
+    if (T <= JS_MAX_T)
+    {
+        const size_t smem = 2 * static_cast<size_t>(T) * (T + 1) * sizeof(double2);
+        if (smem > 48 * 1024)
+            HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem)));
+        k_jacobi_smem<<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted);
+    }
+    else
+        k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);
     HV_LAUNCH_CHECK();
     k_eig_sort<<<(T + 127) / 128, 128, 0, st>>>(ev_unsorted, V, T, evals, evecs, pmin, pmax, weights);
     HV_LAUNCH_CHECK();

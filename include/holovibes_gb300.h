@@ -223,6 +223,12 @@ hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* st
  * `work` must hold hv_pca_cov_workspace(T, W*H) bytes. */
 hv_status hv_pca_covariance(const void* ring_c64, int T, size_t npix, void* cov_c128, void* work, void* stream);
 size_t hv_pca_cov_workspace(int T, size_t npix);
+/* Covariance engine: 0 = automatic (tcgen05 split-BF16 tensor cores for T <= 64 and frames of a
+ * multiple of 8 pixels, else FP32 SIMT), 1 = FP32 SIMT, 2 = tensor cores only. Process-wide. */
+void hv_pca_covariance_mode(int mode);
+/* After the covariance's stream work finished: HV_ERR_TIMEOUT when a bounded device wait in the
+ * tensor-core kernel gave up (results invalid), HV_OK otherwise. Synchronous read of `work`. */
+hv_status hv_pca_covariance_status(const void* work);
 /* FP64 cyclic Jacobi eigensolve of the Hermitian T x T complex128 matrix (lower triangle
  * read): ascending eigenvalues, orthonormal eigenvectors as columns. Replaces cusolverDnCheevd
  * (matrix_operations.cc:44-65). Writes the columns pmin..pmax as PCA weights W[k][t] = V[t][pmin+k]

@@ -1,0 +1,63 @@
+"""The two covariance engines (FP32 SIMT and tcgen05 split-BF16 tensor cores) and the two Jacobi
+paths (shared-memory for T <= 64, global-memory beyond) against the FP64 oracle.
+Tolerances: SIMT covariance rel-L2 <= 1e-6, tensor-core (BF16x3, FP32 accumulation) <= 2e-5;
+eigenvalues within 1e-6 of the largest (FP64 Jacobi on the FP64-summed covariance)."""
+
+import numpy as np
+import pytest
+
+import holovibes_oracle as O
+from gpu_util import call, dev, empty, host, ptr, rel_l2
+
+import holovibes_gb300 as hv
+
+
+def _ring(T, npix, seed):
+    rng = np.random.default_rng(seed)
+    t = np.arange(T)
+    ring = np.zeros((T, npix), np.complex128)
+    for m in range(min(T, 8)):
+        f = rng.uniform(0.02, 0.48)
+        ring += np.exp(2j * np.pi * f * t)[:, None] * ((rng.standard_normal(npix) + 1j * rng.standard_normal(npix)) / (m + 1))[None]
+    ring += 0.05 * (rng.standard_normal((T, npix)) + 1j * rng.standard_normal((T, npix)))
+    return (ring * 1000).astype(np.complex64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,tol", [(1, 1e-6), (2, 2e-5)])
+@pytest.mark.parametrize("T,npix", [(32, 65536), (64, 4096), (17, 1000), (1, 64), (32, 64 * 1024 + 8)])
+def test_covariance_engine(cuda, mode, tol, T, npix):
+    ring = _ring(T, npix, T * 3 + mode)
+    rd = dev(ring)
+    cov = empty(T * T * 16)
+    work = empty(hv.lib().hv_pca_cov_workspace(T, npix))
+    hv.lib().hv_pca_covariance_mode(mode)
+    try:
+        call("hv_pca_covariance", ptr(rd), T, npix, ptr(cov), ptr(work), None)
+        cuda.cuda.synchronize()
+        assert hv.lib().hv_pca_covariance_status(ptr(work)) == hv.HV_OK
+    finally:
+        hv.lib().hv_pca_covariance_mode(0)
+    got = host(cov, np.complex128, (T, T))
+    ref = O.pca_covariance(ring.astype(np.complex128).reshape(T, npix, 1))
+    assert rel_l2(got, ref) <= tol
+    assert np.abs(got - got.conj().T).max() <= 1e-12 * np.abs(got).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("T", [2, 31, 64, 96])
+def test_jacobi_paths(cuda, T):
+    rng = np.random.default_rng(T)
+    X = rng.standard_normal((T, T)) + 1j * rng.standard_normal((T, T))
+    A = X @ X.conj().T + np.diag(np.arange(T) * 3.0)
+    covd = dev(A.astype(np.complex128))
+    evals = empty(T * 8)
+    evecs = empty(T * T * 16)
+    work = empty(hv.lib().hv_pca_eigh_workspace(T))
+    call("hv_pca_eigh", ptr(covd), T, ptr(evals), ptr(evecs), 0, 0, None, ptr(work), None)
+    ev = host(evals, np.float64, (T,))
+    V = host(evecs, np.complex128, (T, T)).T
+    w = np.linalg.eigvalsh(A)
+    assert np.abs(ev - w).max() <= 1e-9 * np.abs(w).max()
+    assert np.abs(V.conj().T @ V - np.eye(T)).max() < 1e-10
+    assert np.abs(A @ V - V * ev[None, :]).max() <= 1e-9 * np.abs(w).max()
