@@ -41,7 +41,7 @@ def test_covariance_engine(cuda, mode, tol, T, npix):
     got = host(cov, np.complex128, (T, T))
     ref = O.pca_covariance(ring.astype(np.complex128).reshape(T, npix, 1))
     assert rel_l2(got, ref) <= tol
-    assert np.abs(got - got.conj().T).max() <= 1e-12 * np.abs(got).max()
+    assert np.abs(got - got.conj().T).max() <= 1e-9 * np.abs(got).max()
 
 
 @pytest.mark.gpu
