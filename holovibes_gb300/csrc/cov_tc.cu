@@ -317,7 +317,10 @@ __global__ void k_cov_tc_reduce(const float* __restrict__ part, int T, int npart
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= T * T)
         return;
-    const int i = e / T, j = e % T;
+    // the upper triangle is summed and mirrored, so the result is exactly Hermitian
+    const int ei = e / T, ej = e % T;
+    const bool mirror = ei > ej;
+    const int i = mirror ? ej : ei, j = mirror ? ei : ej;
     const int R = 2 * T;
     double g00 = 0, g11 = 0, g01 = 0, g10 = 0;
     const int c0 = blockIdx.y * per_slice;
@@ -332,7 +335,8 @@ __global__ void k_cov_tc_reduce(const float* __restrict__ part, int T, int npart
         g10 += G[(2 * i + 1) * R + 2 * j];
     }
     atomicAdd(&cov[e].x, g00 + g11);
-    atomicAdd(&cov[e].y, g01 - g10);
+    if (i != j)
+        atomicAdd(&cov[e].y, mirror ? -(g01 - g10) : (g01 - g10));
 }
 
 struct TcPlan

@@ -336,7 +336,8 @@ __global__ void k_cov_reduce(const float2* __restrict__ part, int T, int tiles1d
         im += v.y;
     }
     atomicAdd(&cov[e].x, re);
-    atomicAdd(&cov[e].y, mirror ? -im : im);
+    if (i != j)  // Hermitian: the diagonal is real
+        atomicAdd(&cov[e].y, mirror ? -im : im);
 }
 
 static int g_cov_mode = 0;  // 0 auto (tensor cores when supported), 1 SIMT, 2 tensor cores
@@ -360,6 +361,7 @@ hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, v
     int* err = static_cast<int*>(work);
     char* ws = static_cast<char*>(work) + COV_FLAGS;
     HV_CUDA_TRY(cudaMemsetAsync(cov, 0, static_cast<size_t>(T) * T * sizeof(double2), st));
+    HV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
     const bool tc_ok = cov_tc_supported(T) && npix % 8 == 0 && (reinterpret_cast<uintptr_t>(ring) & 15) == 0;
     if ((g_cov_mode == 0 && tc_ok) || g_cov_mode == 2)
     {
@@ -368,7 +370,6 @@ hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, v
             set_last_error_msg("tensor-core covariance unsupported for this shape");
             return HV_ERR_UNSUPPORTED;
         }
-        HV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
         return cov_tc(ring, T, npix, cov, ws, err, st);
     }
     const CovPlan p = cov_plan(T, npix);
