@@ -199,6 +199,7 @@ def _declare(L: C.CDLL) -> None:
         "hv_pca_eigh_workspace": (sz, [i32]),
         "hv_unwrap_2d": (st, [vp, vp, i32, i32, vp, vp]),
         "hv_unwrap_workspace": (sz, [i32, i32]),
+        "hv_unwrap_2d_noalloc": (st, [vp, vp, i32, i32, vp]),
         "hv_renormalize": (st, [vp, sz, i32, vp, i32, vp, vp]),
         "hv_reduce_workspace": (sz, [sz]),
         "hv_shift_corners": (st, [vp, i32, i32, vp]),

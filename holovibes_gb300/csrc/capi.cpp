@@ -229,3 +229,14 @@ hv_status hv_contrast_to_ushort(const float* frame, const float* range_f32, int 
 }
 
 }  // extern "C"
+
+namespace hv {
+hv_status unwrap_2d_noalloc(const float* in, float* out, int W, int H, cudaStream_t st);
+}
+
+extern "C" hv_status hv_unwrap_2d_noalloc(const float* in, float* out, int width, int height, void* stream)
+{
+    if (!in || !out)
+        return HV_INVALID_VALUE;
+    return hv::unwrap_2d_noalloc(in, out, width, height, static_cast<cudaStream_t>(stream));
+}

@@ -17,6 +17,8 @@
 #include <float.h>
 #include <math.h>
 
+#include <mutex>
+
 #include "hv_common.cuh"
 #include "hv_internal.h"
 
@@ -211,6 +213,53 @@ hv_status unwrap_2d(const float* in, float* out, int W, int H, void* work, cudaS
     HV_LAUNCH_CHECK();
     count_launch(7);
     return HV_OK;
+}
+
+// ---------------------------------------------------------------------- unwrap without allocation
+// Some callers cannot allocate device memory at all: a frame-grabber or acquisition callback that
+// runs on a driver thread with a real-time budget, or a host application whose memory policy
+// forbids cudaMalloc once streaming has started. hv_unwrap_2d_noalloc serves them: its scratch
+// (four complex frames and the min/max keys, the same layout hv_unwrap_2d takes from `work`) is
+// this file-scope device array, sized for frames of at most HV_UNWRAP_NOALLOC_MAX_PIXELS pixels.
+// Every GPU that loads the library keeps the array (8 MiB) until the process exits.
+
+constexpr size_t kUnwrapNoallocMaxPixels = HV_UNWRAP_NOALLOC_MAX_PIXELS;
+static __device__ __align__(256) float2 g_unwrap_scratch[4 * kUnwrapNoallocMaxPixels + 32];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[kMaxDevices] = {};
+}  // namespace
+
+hv_status unwrap_2d_noalloc(const float* in, float* out, int W, int H, cudaStream_t st)
+{
+    const size_t n = static_cast<size_t>(W) * H;
+    if (W <= 0 || H <= 0 || n > kUnwrapNoallocMaxPixels)
+    {
+        set_last_error_msg("hv_unwrap_2d_noalloc: frame larger than the 262144-pixel static scratch");
+        return HV_INVALID_VALUE;
+    }
+    int dev = 0;
+    HV_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        return HV_INVALID_VALUE;
+    void* ptr = nullptr;
+    {
+        // set-up on the first call on each device (with that device current): the host-side name
+        // of the array is not a device address, so fetch the address once and keep it
+        std::lock_guard<std::mutex> g(g_scratch_mu);
+        if (!g_scratch_ptr[dev])
+        {
+            void* p = nullptr;
+            HV_CUDA_TRY(cudaGetSymbolAddress(&p, g_unwrap_scratch));
+            g_scratch_ptr[dev] = p;
+        }
+        ptr = g_scratch_ptr[dev];
+    }
+    // every buffer of the scratch is fully written before it is read, and the min/max keys are
+    // re-initialised by unwrap_2d itself, so the previous call's contents never leak into this one
+    return unwrap_2d(in, out, W, H, ptr, st);
 }
 
 // ====================================================================================== renorm

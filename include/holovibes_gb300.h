@@ -243,6 +243,19 @@ size_t hv_pca_eigh_workspace(int T);
 hv_status hv_unwrap_2d(const float* in, float* out, int width, int height, void* work, void* stream);
 size_t hv_unwrap_workspace(int width, int height);
 
+/* hv_unwrap_2d for callers that cannot allocate device memory (no counterpart in the reference).
+ * Acquisition callbacks on a driver thread, or applications that forbid cudaMalloc once frames are
+ * streaming, cannot provide `work`: this entry point takes none and calls no cudaMalloc, cudaFree or
+ * allocating library routine. Its scratch is a static device array inside the library, sized for
+ * frames of at most HV_UNWRAP_NOALLOC_MAX_PIXELS pixels; larger frames fail with HV_INVALID_VALUE.
+ * Every GPU that loads the library keeps that array (8 MiB) until the process exits.
+ * The first call on each device looks up the array's device address (with that device current);
+ * make that first call before any stream capture. All calls share the one array: calls whose GPU
+ * work overlaps (different streams, or different host threads) race and corrupt each other's
+ * results, so serialise them on one stream. Results match hv_unwrap_2d. */
+#define HV_UNWRAP_NOALLOC_MAX_PIXELS 262144
+hv_status hv_unwrap_2d_noalloc(const float* in, float* out, int width, int height, void* stream);
+
 /* Renormalisation x <- x * 2^c * N / sum(x), the sum being taken from `partials_f64`
  * (npartials entries) or computed here when partials_f64 is NULL. Replaces gpu_normalize
  * (tools_compute.cu:99-123). `work` needs hv_reduce_workspace(n) bytes. */
