@@ -45,6 +45,7 @@ SPACE_NONE, SPACE_FRESNELTR, SPACE_ANGULARSP = 0, 1, 2
 TIME_NONE, TIME_STFT, TIME_PCA, TIME_SSA_STFT = 0, 1, 2, 3
 IMG_MODULUS, IMG_SQUARED_MODULUS, IMG_ARGUMENT = 0, 1, 2
 LENS_FP64, LENS_REF32 = 0, 1
+EIG_FP32, EIG_FP64 = 0, 1
 MEM_HOST, MEM_DEVICE = 0, 1
 
 SPACE_NAMES = {"NONE": 0, "None": 0, "FRESNELTR": 1, "FFT1": 1, "1FFT": 1, "Fresnel Tr.": 1,
@@ -197,6 +198,7 @@ def _declare(L: C.CDLL) -> None:
         "hv_pca_covariance_status": (st, [vp]),
         "hv_pca_eigh": (st, [vp, i32, vp, vp, i32, i32, vp, vp, vp]),
         "hv_pca_eigh_workspace": (sz, [i32]),
+        "hv_pca_eig_precision": (None, [i32]),
         "hv_unwrap_2d": (st, [vp, vp, i32, i32, vp, vp]),
         "hv_unwrap_workspace": (sz, [i32, i32]),
         "hv_unwrap_2d_noalloc": (st, [vp, vp, i32, i32, vp]),

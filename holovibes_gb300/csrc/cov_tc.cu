@@ -177,13 +177,56 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
     const uint32_t tmem = tmem_base;
     const uint32_t idesc = instr_desc(TC_ROWS, N);
 
-    // work items per chunk: T rows x 8 k-groups (8 pixels each)
+    // work items per chunk: T rows x 8 k-groups (8 pixels each); at most 2 per thread (T <= 64).
+    // The loads of chunk c+1 are issued into registers before chunk c is split and stored, so
+    // global loads stay in flight while this CTA converts and the tensor cores run.
     const int items = T * (TC_KC / 8);
+    float2 nxt[2][8];
+    auto load_chunk = [&](size_t c) {
+        const size_t p0 = c * TC_KC;
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+        {
+            const int w = tid + q * TC_THREADS;
+            if (w >= items)
+                continue;
+            const int t = w % T, g = w / T;
+            const size_t p = p0 + static_cast<size_t>(g) * 8;
+            const float2* src = ring + static_cast<size_t>(t) * npix + p;
+            if (p + 8 <= npix)
+            {
+                const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+                for (int h = 0; h < 4; ++h)
+                {
+                    const float4 f = __ldcs(s4 + h);
+                    nxt[q][2 * h] = make_float2(f.x, f.y);
+                    nxt[q][2 * h + 1] = make_float2(f.z, f.w);
+                }
+            }
+            else
+            {
+#pragma unroll
+                for (int h = 0; h < 8; ++h)
+                    nxt[q][h] = (p + h < npix) ? __ldg(src + h) : make_float2(0.f, 0.f);
+            }
+        }
+    };
+    if (c_begin < c_end)
+        load_chunk(c_begin);
     size_t it = 0;
     bool fail = false;
     for (size_t c = c_begin; c < c_end; ++c, ++it)
     {
         const int buf = static_cast<int>(it & 1);
+        float2 cur[2][8];
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+#pragma unroll
+            for (int h = 0; h < 8; ++h)
+                cur[q][h] = nxt[q][h];
+        if (c + 1 < c_end)
+            load_chunk(c + 1);
         if (it >= 2)
         {
             // MMAs of chunk it-2 read this buffer; their commit is use number (it-2)/2 of bars[buf]
@@ -192,42 +235,26 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
         }
         uint8_t* th = tiles + buf * 2 * TILE_BYTES;
         uint8_t* tl = th + TILE_BYTES;
-        const size_t p0 = c * TC_KC;
-        for (int w = tid; w < items; w += TC_THREADS)
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
         {
+            const int w = tid + q * TC_THREADS;
+            if (w >= items)
+                continue;
             const int t = w % T, g = w / T;
-            const size_t p = p0 + static_cast<size_t>(g) * 8;
-            const float2* src = ring + static_cast<size_t>(t) * npix + p;
-            float2 v[8];
-            if (p + 8 <= npix)
-            {
-                const float4* s4 = reinterpret_cast<const float4*>(src);
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                {
-                    const float4 f = __ldg(s4 + q);
-                    v[2 * q] = make_float2(f.x, f.y);
-                    v[2 * q + 1] = make_float2(f.z, f.w);
-                }
-            }
-            else
-            {
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    v[q] = (p + q < npix) ? __ldg(src + q) : make_float2(0.f, 0.f);
-            }
+            const float2* v = cur[q];
             uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
+            for (int h = 0; h < 4; ++h)
             {
-                const __nv_bfloat16 a0 = __float2bfloat16_rn(v[2 * q].x), a1 = __float2bfloat16_rn(v[2 * q + 1].x);
-                const __nv_bfloat16 b0 = __float2bfloat16_rn(v[2 * q].y), b1 = __float2bfloat16_rn(v[2 * q + 1].y);
-                rh[q] = pack_bf16(a0, a1);
-                ih[q] = pack_bf16(b0, b1);
-                rl[q] = pack_bf16(__float2bfloat16_rn(v[2 * q].x - __bfloat162float(a0)),
-                                  __float2bfloat16_rn(v[2 * q + 1].x - __bfloat162float(a1)));
-                il[q] = pack_bf16(__float2bfloat16_rn(v[2 * q].y - __bfloat162float(b0)),
-                                  __float2bfloat16_rn(v[2 * q + 1].y - __bfloat162float(b1)));
+                const __nv_bfloat16 a0 = __float2bfloat16_rn(v[2 * h].x), a1 = __float2bfloat16_rn(v[2 * h + 1].x);
+                const __nv_bfloat16 b0 = __float2bfloat16_rn(v[2 * h].y), b1 = __float2bfloat16_rn(v[2 * h + 1].y);
+                rh[h] = pack_bf16(a0, a1);
+                ih[h] = pack_bf16(b0, b1);
+                rl[h] = pack_bf16(__float2bfloat16_rn(v[2 * h].x - __bfloat162float(a0)),
+                                  __float2bfloat16_rn(v[2 * h + 1].x - __bfloat162float(a1)));
+                il[h] = pack_bf16(__float2bfloat16_rn(v[2 * h].y - __bfloat162float(b0)),
+                                  __float2bfloat16_rn(v[2 * h + 1].y - __bfloat162float(b1)));
             }
             const uint32_t ore = tile_offset(2 * t, g), oim = tile_offset(2 * t + 1, g);
             *reinterpret_cast<uint4*>(th + ore) = make_uint4(rh[0], rh[1], rh[2], rh[3]);

@@ -234,8 +234,10 @@ struct Tile
         }
     }
 
+    // tw: this stage's table, entry (j-1)*P + k = exp(-2 pi i j k / (P r)), so consecutive k
+    // (consecutive threads in row tiles) read consecutive entries
     template <int r, int P>
-    __device__ __forceinline__ static void butterflies(float2 (&x)[E], const float2* tw)
+    __device__ __forceinline__ static void butterflies(float2 (&x)[E], const float2* __restrict__ tw)
     {
         constexpr int Q = E / r;
 #pragma unroll
@@ -246,10 +248,9 @@ struct Tile
                 int f, i;
                 index<r>(static_cast<int>(threadIdx.x) + q * NT, f, i);
                 const int k = i % P;
-                constexpr int step = N / (P * r);
 #pragma unroll
                 for (int j = 1; j < r; ++j)
-                    x[q * r + j] = cmul(x[q * r + j], tw[j * k * step]);
+                    x[q * r + j] = cmul(x[q * r + j], __ldg(tw + (j - 1) * P + k));
             }
             dft<r>(&x[q * r]);
         }
@@ -288,7 +289,7 @@ struct Tile
             auto from_sm = [sm](int f, int n) { return sm[addr(f, n)]; };
             gather<first<Rest...>()>(x, from_sm);
             __syncthreads();
-            chain<P * r, Rest...>(x, sm, tw, dst);
+            chain<P * r, Rest...>(x, sm, P > 1 ? tw + P * (r - 1) : tw, dst);
         }
     }
 
@@ -318,15 +319,37 @@ struct Tile
     }
 };
 
-// Twiddle table tw[m] = exp(-2*pi*i*m/N), m < N, filled cooperatively by nthreads threads.
-template <int N>
-__device__ __forceinline__ void fill_twiddles(float2* tw, int nthreads)
+// Host-side layout of the per-stage twiddle tables of Plan<N>: stages with P > 1 in order, each
+// P * (r - 1) entries (j - 1) * P + k = exp(-2 pi i j k / (P r)).
+template <int... Rs>
+inline int twiddle_count(RadixList<Rs...>)
 {
-    for (int m = threadIdx.x; m < N; m += nthreads)
+    int total = 0, P = 1;
+    for (int r : {Rs...})
     {
-        float s, c;
-        sincospif(-2.0f * static_cast<float>(m) / static_cast<float>(N), &s, &c);
-        tw[m] = make_float2(c, s);
+        if (P > 1)
+            total += P * (r - 1);
+        P *= r;
+    }
+    return total;
+}
+
+template <int... Rs>
+inline void twiddle_fill(RadixList<Rs...>, float2* out)
+{
+    int P = 1;
+    for (int r : {Rs...})
+    {
+        if (P > 1)
+        {
+            for (int j = 1; j < r; ++j)
+                for (int k = 0; k < P; ++k)
+                {
+                    const double a = -2.0 * 3.14159265358979323846 * static_cast<double>(j) * k / (static_cast<double>(P) * r);
+                    *out++ = make_float2(static_cast<float>(cos(a)), static_cast<float>(sin(a)));
+                }
+        }
+        P *= r;
     }
 }
 

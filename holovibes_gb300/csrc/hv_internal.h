@@ -42,6 +42,7 @@ size_t cov_tc_workspace(int T, size_t npix);
 hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, cudaStream_t st);
 hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st);
 size_t pca_eigh_workspace(int T);
+void set_eig_precision(int p);
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
                    cudaStream_t st);
 

@@ -16,6 +16,9 @@
 // mask, divide and ring-copy passes disappear.
 #include <math.h>
 
+#include <mutex>
+#include <vector>
+
 #include "fft_smem.cuh"
 #include "hv_internal.h"
 
@@ -114,6 +117,7 @@ struct RowPass
     int rows;              // rows per frame
     int inverse;           // 1: conj in / conj out (unnormalised inverse)
     float scale;
+    const float2* tw;      // per-stage twiddle tables of the N-point plan (device)
 };
 
 template <int N, int F>
@@ -121,10 +125,8 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
 {
     using Tl = fft::Tile<N, F, false>;
     extern __shared__ float2 smem[];
-    float2* tw = smem;
-    float2* sm = smem + N;
-    fft::fill_twiddles<N>(tw, Tl::NT);
-    __syncthreads();
+    float2* sm = smem;
+    const float2* tw = p.tw;
 
     const int b = blockIdx.y;
     const int row0 = blockIdx.x * F;
@@ -165,6 +167,7 @@ struct ColPass
     int width;              // row length (number of columns)
     int mode;               // 0 forward, 1 inverse, 2 forward * postmul then inverse
     float scale;
+    const float2* tw;       // per-stage twiddle tables of the N-point plan (device)
 };
 
 template <int N, int F>
@@ -172,10 +175,8 @@ __global__ void __launch_bounds__(fft::Tile<N, F, true>::NT) k_fft_cols(ColPass 
 {
     using Tl = fft::Tile<N, F, true>;
     extern __shared__ float2 smem[];
-    float2* tw = smem;
-    float2* sm = smem + N;
-    fft::fill_twiddles<N>(tw, Tl::NT);
-    __syncthreads();
+    float2* sm = smem;
+    const float2* tw = p.tw;
 
     const int b = blockIdx.y;
     const int c0 = blockIdx.x * F;
@@ -241,6 +242,69 @@ __global__ void k_convert(const void* in, int kind, size_t frame_px, int batch, 
     }
 }
 
+// ====================================================================================== twiddles
+// All plans' per-stage twiddle tables live in one static device array, filled from the host (FP64
+// cos/sin rounded to FP32) by a synchronous copy the first time a size is used on a device: no
+// device allocation, so the allocation-free entry points can use the FFT too. That first use on a
+// device must not happen inside a stream capture.
+
+#define HV_FFT_SIZES(X)                                                                                                \
+    X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(48) X(96) X(192) X(384) X(768) X(1536)
+
+constexpr int kTwiddleCapacity = 32768;
+static __device__ float2 g_fft_twiddles[kTwiddleCapacity];
+
+namespace {
+
+constexpr int kMaxTwDevices = 64;
+std::mutex g_tw_mu;
+const float2* g_tw_base[kMaxTwDevices] = {};
+int g_tw_offset[8192];  // offset of size N's tables in g_fft_twiddles
+bool g_tw_layout_ready = false;
+std::vector<float2> g_tw_host;
+
+void tw_layout()
+{
+    if (g_tw_layout_ready)
+        return;
+    int off = 0;
+#define HV_TW(N)                                                                                                       \
+    {                                                                                                                  \
+        g_tw_offset[N] = off;                                                                                          \
+        const int cnt = fft::twiddle_count(typename fft::Plan<N>::List{});                                             \
+        g_tw_host.resize(off + cnt + 1);                                                                               \
+        fft::twiddle_fill(typename fft::Plan<N>::List{}, g_tw_host.data() + off);                                      \
+        off += cnt;                                                                                                    \
+    }
+    HV_FFT_SIZES(HV_TW)
+#undef HV_TW
+    g_tw_layout_ready = true;
+}
+
+template <int N>
+const float2* twiddles()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxTwDevices)
+        return nullptr;
+    std::lock_guard<std::mutex> g(g_tw_mu);
+    if (!g_tw_base[dev])
+    {
+        tw_layout();
+        if (g_tw_host.size() > static_cast<size_t>(kTwiddleCapacity))
+            return nullptr;
+        if (cudaMemcpyToSymbol(g_fft_twiddles, g_tw_host.data(), g_tw_host.size() * sizeof(float2)) != cudaSuccess)
+            return nullptr;
+        void* base = nullptr;
+        if (cudaGetSymbolAddress(&base, g_fft_twiddles) != cudaSuccess)
+            return nullptr;
+        g_tw_base[dev] = static_cast<const float2*>(base);
+    }
+    return g_tw_base[dev] + g_tw_offset[N];
+}
+
+}  // namespace
+
 // ====================================================================================== dispatch
 
 namespace {
@@ -268,12 +332,15 @@ hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
 {
     constexpr int F = row_lanes<N>();
     using Tl = fft::Tile<N, F, false>;
-    const size_t smem = (static_cast<size_t>(N) + static_cast<size_t>(F) * N) * sizeof(float2);
+    const size_t smem = static_cast<size_t>(F) * N * sizeof(float2);
     if (smem > 48 * 1024)
         HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_rows<N, F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
+    RowPass q = p;
+    if ((q.tw = twiddles<N>()) == nullptr)
+        return HV_ERR_CUDA;
     dim3 grid((p.rows + F - 1) / F, nframes);
-    k_fft_rows<N, F><<<grid, Tl::NT, smem, st>>>(p);
+    k_fft_rows<N, F><<<grid, Tl::NT, smem, st>>>(q);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
@@ -284,19 +351,19 @@ hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
 {
     constexpr int F = col_lanes<N>();
     using Tl = fft::Tile<N, F, true>;
-    const size_t smem = (static_cast<size_t>(N) + static_cast<size_t>(F) * N) * sizeof(float2);
+    const size_t smem = static_cast<size_t>(F) * N * sizeof(float2);
     if (smem > 48 * 1024)
         HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_cols<N, F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
+    ColPass q = p;
+    if ((q.tw = twiddles<N>()) == nullptr)
+        return HV_ERR_CUDA;
     dim3 grid((p.width + F - 1) / F, nframes);
-    k_fft_cols<N, F><<<grid, Tl::NT, smem, st>>>(p);
+    k_fft_cols<N, F><<<grid, Tl::NT, smem, st>>>(q);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
 }
-
-#define HV_FFT_SIZES(X)                                                                                                \
-    X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(48) X(96) X(192) X(384) X(768) X(1536)
 
 }  // namespace
 

@@ -23,7 +23,7 @@
 namespace hv {
 
 constexpr int TV_THREADS = 256;
-constexpr int TV_KC = 16;  // bins per register chunk
+constexpr int TV_KMAX = 16;  // bins per register chunk at most
 
 __device__ __forceinline__ float view_value(float2 X, int img_type)
 {
@@ -37,67 +37,53 @@ __device__ __forceinline__ float view_value(float2 X, int img_type)
     return atan2f(X.y, X.x);
 }
 
-// ring: [T][HW] complex; weights: [K][T] complex. One pixel per thread.
+// ring: [T][HW] complex; weights: [K][T] complex. One pixel per thread; the K bins are done in
+// chunks of KC (registers), the chunk's weights staged in shared memory as [T][KC].
+template <int KC>
 __global__ void __launch_bounds__(TV_THREADS) k_time_view(const float2* __restrict__ ring, int T, int W, int H,
                                                            const float2* __restrict__ weights, int K, int img_type,
                                                            float scale, int shift, float* __restrict__ out,
                                                            double* __restrict__ partials)
 {
-    extern __shared__ __align__(16) float2 wsm[];  // [T][TV_KC], read as float4 pairs
+    extern __shared__ __align__(16) float2 wsm[];  // [T][KC]
     __shared__ double red[TV_THREADS / 32];
     const size_t HW = static_cast<size_t>(W) * H;
     const size_t pix = blockIdx.x * static_cast<size_t>(TV_THREADS) + threadIdx.x;
     const bool valid = pix < HW;
     float acc_view = 0.f;
-    for (int k0 = 0; k0 < K; k0 += TV_KC)
+    for (int k0 = 0; k0 < K; k0 += KC)
     {
         __syncthreads();
-        for (int e = threadIdx.x; e < T * TV_KC; e += TV_THREADS)
+        for (int e = threadIdx.x; e < T * KC; e += TV_THREADS)
         {
-            const int t = e / TV_KC, kk = e - t * TV_KC;
+            const int t = e / KC, kk = e - t * KC;
             const int k = k0 + kk;
             wsm[e] = (k < K) ? weights[static_cast<size_t>(k) * T + t] : make_float2(0.f, 0.f);
         }
         __syncthreads();
-        float2 acc[TV_KC];
+        float2 acc[KC];
 #pragma unroll
-        for (int kk = 0; kk < TV_KC; ++kk)
+        for (int kk = 0; kk < KC; ++kk)
             acc[kk] = make_float2(0.f, 0.f);
-        const int kn = (K - k0) < TV_KC ? (K - k0) : TV_KC;
         if (valid)
         {
             const float2* src = ring + pix;
-            if (kn == 1)
-            {
 #pragma unroll 8
-                for (int t = 0; t < T; ++t)
-                {
-                    const float2 x = __ldg(src + static_cast<size_t>(t) * HW);
-                    const float2 w = wsm[t * TV_KC];
-                    acc[0].x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc[0].x));
-                    acc[0].y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc[0].y));
-                }
-            }
-            else
+            for (int t = 0; t < T; ++t)
             {
-#pragma unroll 2
-                for (int t = 0; t < T; ++t)
-                {
-                    const float2 x = __ldg(src + static_cast<size_t>(t) * HW);
-                    const float4* w4 = reinterpret_cast<const float4*>(wsm + t * TV_KC);
+                const float2 x = __ldg(src + static_cast<size_t>(t) * HW);
+                const float2* wt = wsm + t * KC;
 #pragma unroll
-                    for (int kk = 0; kk < TV_KC; kk += 2)
-                    {
-                        const float4 w = w4[kk / 2];
-                        acc[kk].x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc[kk].x));
-                        acc[kk].y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc[kk].y));
-                        acc[kk + 1].x = fmaf(x.x, w.z, fmaf(-x.y, w.w, acc[kk + 1].x));
-                        acc[kk + 1].y = fmaf(x.x, w.w, fmaf(x.y, w.z, acc[kk + 1].y));
-                    }
+                for (int kk = 0; kk < KC; ++kk)
+                {
+                    const float2 w = wt[kk];
+                    acc[kk].x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc[kk].x));
+                    acc[kk].y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc[kk].y));
                 }
             }
+            const int kn = (K - k0) < KC ? (K - k0) : KC;
 #pragma unroll
-            for (int kk = 0; kk < TV_KC; ++kk)
+            for (int kk = 0; kk < KC; ++kk)
                 if (kk < kn)
                     acc_view += view_value(acc[kk], img_type);
         }
@@ -140,6 +126,26 @@ int time_view_partials(int W, int H)
     return static_cast<int>((HW + TV_THREADS - 1) / TV_THREADS);
 }
 
+template <int KC>
+static hv_status launch_time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type,
+                                  float scale, int shift, float* out, double* partials, cudaStream_t st)
+{
+    const size_t smem = static_cast<size_t>(T) * KC * sizeof(float2);
+    if (smem > 200 * 1024)
+    {
+        set_last_error_msg("time window too large for the time-view kernel");
+        return HV_ERR_UNSUPPORTED;
+    }
+    if (smem > 48 * 1024)
+        HV_CUDA_TRY(cudaFuncSetAttribute(k_time_view<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+    const int grid = time_view_partials(W, H);
+    k_time_view<KC><<<grid, TV_THREADS, smem, st>>>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
 hv_status time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type, float scale,
                     int shift, float* out, double* partials, cudaStream_t st)
 {
@@ -153,20 +159,22 @@ hv_status time_view(const float2* ring, int T, int W, int H, const float2* weigh
         set_last_error_msg("fftshift needs even width and height");
         return HV_INVALID_VALUE;
     }
-    const size_t smem = static_cast<size_t>(T) * TV_KC * sizeof(float2);
-    if (smem > 200 * 1024)
-    {
-        set_last_error_msg("time window too large for the time-view kernel");
-        return HV_ERR_UNSUPPORTED;
-    }
-    if (smem > 48 * 1024)
-        HV_CUDA_TRY(cudaFuncSetAttribute(k_time_view, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem)));
-    const int grid = time_view_partials(W, H);
-    k_time_view<<<grid, TV_THREADS, smem, st>>>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials);
-    HV_LAUNCH_CHECK();
-    count_launch();
-    return HV_OK;
+    // fewest register chunks, then the smallest instantiated chunk that covers K / chunks
+    const int chunks = (K + TV_KMAX - 1) / TV_KMAX;
+    const int need = (K + chunks - 1) / chunks;
+    if (need <= 1)
+        return launch_time_view<1>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+    if (need <= 2)
+        return launch_time_view<2>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+    if (need <= 4)
+        return launch_time_view<4>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+    if (need <= 6)
+        return launch_time_view<6>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+    if (need <= 8)
+        return launch_time_view<8>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+    if (need <= 11)
+        return launch_time_view<11>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+    return launch_time_view<16>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
 }
 
 // ------------------------------------------------------------------------------ weights
@@ -564,32 +572,54 @@ __global__ void __launch_bounds__(JAC_THREADS) k_jacobi(double2* A, double2* V, 
         evals[i] = A[i * T + i].x;
 }
 
-// Shared-memory variant for T <= 64 (A and V resident in shared memory, one CTA). The step
-// update works on 2 x 2 blocks: for row pair k1 and column pair k2, the block of A becomes
-// J1^H B J2 and the mirrored block its conjugate transpose (A stays Hermitian), so each step is
-// one barrier-separated phase; steps whose rotations are all identities are skipped.
+// Shared-memory variant for T <= 64 (A and V resident in shared memory, one CTA), templated on
+// the sweep precision. The step update works on 2 x 2 blocks: for row pair k1 and column pair k2
+// the block of A becomes J1^H B J2 and the mirrored block its conjugate transpose (A stays
+// Hermitian), so each step is one barrier-separated phase; steps whose rotations are all
+// identities are skipped and the sweeps stop after a sweep without rotation. The skip threshold is
+// a few units of the working precision relative to sqrt(|a_pp a_qq|).
 constexpr int JS_THREADS = 256;
 constexpr int JS_MAX_T = 64;
 
+template <class R>
+struct Cx
+{
+    R x, y;
+};
+template <class R>
+__device__ __forceinline__ Cx<R> cxmul(Cx<R> a, Cx<R> b)
+{
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+
+template <class R>
+__device__ __forceinline__ R jac_threshold();
+template <>
+__device__ __forceinline__ double jac_threshold<double>() { return 1e-15; }
+template <>
+__device__ __forceinline__ float jac_threshold<float>() { return 2.5e-7f; }
+
+template <class R>
 __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __restrict__ Ain, double2* __restrict__ Vout,
                                                             int T, int Tp, double* __restrict__ evals)
 {
-    extern __shared__ double2 js[];
+    extern __shared__ __align__(16) unsigned char js_raw[];
+    Cx<R>* js = reinterpret_cast<Cx<R>*>(js_raw);
     const int LD = T + 1;
-    double2* A = js;
-    double2* V = js + T * LD;
+    Cx<R>* A = js;
+    Cx<R>* V = js + T * LD;
     __shared__ int pp[JS_MAX_T / 2], pq[JS_MAX_T / 2], act[JS_MAX_T / 2];
-    __shared__ double rc[JS_MAX_T / 2], rs[JS_MAX_T / 2], rcp[JS_MAX_T / 2], rsp[JS_MAX_T / 2];
+    __shared__ R rc[JS_MAX_T / 2], rs[JS_MAX_T / 2], rcp[JS_MAX_T / 2], rsp[JS_MAX_T / 2];
     __shared__ short2 blk[(JS_MAX_T / 2) * (JS_MAX_T / 2 + 1) / 2];
     const int tid = threadIdx.x;
     const int npairs = Tp / 2;
     for (int e = tid; e < T * T; e += JS_THREADS)
     {
         const int i = e / T, j = e % T;
-        A[i * LD + j] = Ain[e];
-        V[i * LD + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+        const double2 a = Ain[e];
+        A[i * LD + j] = {static_cast<R>(a.x), static_cast<R>(i == j ? 0.0 : a.y)};
+        V[i * LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
     }
-    // block table: e -> (k1, k2), k1 >= k2
     const int nblocks = npairs * (npairs + 1) / 2;
     for (int e = tid; e < nblocks; e += JS_THREADS)
     {
@@ -599,7 +629,7 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
         blk[e] = make_short2(static_cast<short>(k1), static_cast<short>(e - k1 * (k1 + 1) / 2));
     }
     __syncthreads();
-    // threshold Jacobi: stop after a sweep in which no rotation was needed
+    const R thr = jac_threshold<R>();
     for (int sweep = 0; sweep < JAC_MAX_SWEEPS; ++sweep)
     {
         int sweep_active = 0;
@@ -623,19 +653,19 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                 const int p = a < b ? a : b, q = a < b ? b : a;
                 pp[k] = p;
                 pq[k] = q;
-                double c = 1.0, s = 0.0, cph = 1.0, sph = 0.0;
+                R c = 1, s = 0, cph = 1, sph = 0;
                 if (q < T)
                 {
-                    const double2 apq = A[p * LD + q];
-                    const double mag = hypot(apq.x, apq.y);
-                    const double app = A[p * LD + p].x, aqq = A[q * LD + q].x;
-                    if (mag > 1e-300 && mag > 1e-15 * sqrt(fabs(app * aqq)))
+                    const Cx<R> apq = A[p * LD + q];
+                    const R mag = hypot(apq.x, apq.y);
+                    const R app = A[p * LD + p].x, aqq = A[q * LD + q].x;
+                    if (mag > R(1e-30) && mag > thr * sqrt(fabs(app * aqq)))
                     {
                         cph = apq.x / mag;
                         sph = apq.y / mag;
-                        const double tau = (aqq - app) / (2.0 * mag);
-                        const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                        c = 1.0 / sqrt(1.0 + t * t);
+                        const R tau = (aqq - app) / (R(2) * mag);
+                        const R t = (tau >= 0 ? R(1) : R(-1)) / (fabs(tau) + sqrt(R(1) + tau * tau));
+                        c = R(1) / sqrt(R(1) + t * t);
                         s = t * c;
                         active = 1;
                     }
@@ -657,39 +687,40 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                     continue;
                 const int r0 = pp[k1], r1 = pq[k1], c0 = pp[k2], c1 = pq[k2];
                 const bool hr1 = r1 < T, hc1 = c1 < T;
-                double2 B[2][2];
+                const Cx<R> z = {0, 0};
+                Cx<R> B[2][2];
                 B[0][0] = A[r0 * LD + c0];
-                B[0][1] = hc1 ? A[r0 * LD + c1] : make_double2(0, 0);
-                B[1][0] = hr1 ? A[r1 * LD + c0] : make_double2(0, 0);
-                B[1][1] = (hr1 && hc1) ? A[r1 * LD + c1] : make_double2(0, 0);
+                B[0][1] = hc1 ? A[r0 * LD + c1] : z;
+                B[1][0] = hr1 ? A[r1 * LD + c0] : z;
+                B[1][1] = (hr1 && hc1) ? A[r1 * LD + c1] : z;
                 // X = B J2, J2 = [[c, s], [-s e^{-i phi}, c e^{-i phi}]]
-                const double c2 = rc[k2], s2 = rs[k2];
-                const double2 em2 = make_double2(rcp[k2], -rsp[k2]);
-                double2 X[2][2];
+                const R c2 = rc[k2], s2 = rs[k2];
+                const Cx<R> em2 = {rcp[k2], -rsp[k2]};
+                Cx<R> X[2][2];
 #pragma unroll
                 for (int r = 0; r < 2; ++r)
                 {
-                    const double2 b1 = zmul(B[r][1], em2);
-                    X[r][0] = make_double2(c2 * B[r][0].x - s2 * b1.x, c2 * B[r][0].y - s2 * b1.y);
-                    X[r][1] = make_double2(s2 * B[r][0].x + c2 * b1.x, s2 * B[r][0].y + c2 * b1.y);
+                    const Cx<R> b1 = cxmul(B[r][1], em2);
+                    X[r][0] = {c2 * B[r][0].x - s2 * b1.x, c2 * B[r][0].y - s2 * b1.y};
+                    X[r][1] = {s2 * B[r][0].x + c2 * b1.x, s2 * B[r][0].y + c2 * b1.y};
                 }
                 // Y = J1^H X: row0 = c X0 - s e^{i phi} X1, row1 = s X0 + c e^{i phi} X1
-                const double c1r = rc[k1], s1r = rs[k1];
-                const double2 ep1 = make_double2(rcp[k1], rsp[k1]);
-                double2 Y[2][2];
+                const R c1r = rc[k1], s1r = rs[k1];
+                const Cx<R> ep1 = {rcp[k1], rsp[k1]};
+                Cx<R> Y[2][2];
 #pragma unroll
                 for (int cc = 0; cc < 2; ++cc)
                 {
-                    const double2 x1 = zmul(X[1][cc], ep1);
-                    Y[0][cc] = make_double2(c1r * X[0][cc].x - s1r * x1.x, c1r * X[0][cc].y - s1r * x1.y);
-                    Y[1][cc] = make_double2(s1r * X[0][cc].x + c1r * x1.x, s1r * X[0][cc].y + c1r * x1.y);
+                    const Cx<R> x1 = cxmul(X[1][cc], ep1);
+                    Y[0][cc] = {c1r * X[0][cc].x - s1r * x1.x, c1r * X[0][cc].y - s1r * x1.y};
+                    Y[1][cc] = {s1r * X[0][cc].x + c1r * x1.x, s1r * X[0][cc].y + c1r * x1.y};
                 }
                 if (k1 == k2 && act[k1])
                 {
-                    Y[0][1] = make_double2(0, 0);
-                    Y[1][0] = make_double2(0, 0);
-                    Y[0][0].y = 0.0;
-                    Y[1][1].y = 0.0;
+                    Y[0][1] = z;
+                    Y[1][0] = z;
+                    Y[0][0].y = 0;
+                    Y[1][1].y = 0;
                 }
                 A[r0 * LD + c0] = Y[0][0];
                 if (hc1)
@@ -700,13 +731,13 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                     A[r1 * LD + c1] = Y[1][1];
                 if (k1 != k2)
                 {
-                    A[c0 * LD + r0] = make_double2(Y[0][0].x, -Y[0][0].y);
+                    A[c0 * LD + r0] = {Y[0][0].x, -Y[0][0].y};
                     if (hc1)
-                        A[c1 * LD + r0] = make_double2(Y[0][1].x, -Y[0][1].y);
+                        A[c1 * LD + r0] = {Y[0][1].x, -Y[0][1].y};
                     if (hr1)
-                        A[c0 * LD + r1] = make_double2(Y[1][0].x, -Y[1][0].y);
+                        A[c0 * LD + r1] = {Y[1][0].x, -Y[1][0].y};
                     if (hr1 && hc1)
-                        A[c1 * LD + r1] = make_double2(Y[1][1].x, -Y[1][1].y);
+                        A[c1 * LD + r1] = {Y[1][1].x, -Y[1][1].y};
                 }
             }
             // V <- V J for the active pairs
@@ -716,11 +747,11 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                 if (!act[k])
                     continue;
                 const int p = pp[k], q = pq[k];
-                const double c = rc[k], s = rs[k];
-                const double2 em = make_double2(rcp[k], -rsp[k]);
-                const double2 vp = V[r * LD + p], vq = zmul(V[r * LD + q], em);
-                V[r * LD + p] = make_double2(c * vp.x - s * vq.x, c * vp.y - s * vq.y);
-                V[r * LD + q] = make_double2(s * vp.x + c * vq.x, s * vp.y + c * vq.y);
+                const R c = rc[k], s = rs[k];
+                const Cx<R> em = {rcp[k], -rsp[k]};
+                const Cx<R> vp = V[r * LD + p], vq = cxmul(V[r * LD + q], em);
+                V[r * LD + p] = {c * vp.x - s * vq.x, c * vp.y - s * vq.y};
+                V[r * LD + q] = {s * vp.x + c * vq.x, s * vp.y + c * vq.y};
             }
             __syncthreads();
         }
@@ -730,10 +761,55 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
     for (int e = tid; e < T * T; e += JS_THREADS)
     {
         const int i = e / T, j = e % T;
-        Vout[e] = V[i * LD + j];
+        Vout[e] = make_double2(static_cast<double>(V[i * LD + j].x), static_cast<double>(V[i * LD + j].y));
     }
     for (int i = tid; i < T; i += JS_THREADS)
-        evals[i] = A[i * LD + i].x;
+        evals[i] = static_cast<double>(A[i * LD + i].x);
+}
+
+// FP64 finish of each eigenpair from the FP64 covariance (intact in the shared-memory paths):
+// normalise the eigenvector column in FP64 and take its Rayleigh quotient v^H A v as the
+// eigenvalue, whose error is second order in the eigenvector error. One CTA per eigenpair.
+__global__ void k_eig_refine(const double2* __restrict__ A, double2* __restrict__ V, int T, double* __restrict__ evals)
+{
+    __shared__ double2 v[JS_MAX_T];
+    __shared__ double red[4];
+    const int i = blockIdx.x, tid = threadIdx.x;
+    double n2 = 0.0;
+    for (int t = tid; t < T; t += blockDim.x)
+    {
+        const double2 x = V[t * T + i];
+        v[t] = x;
+        n2 += x.x * x.x + x.y * x.y;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        n2 += __shfl_down_sync(0xffffffffu, n2, o);
+    if ((tid & 31) == 0)
+        red[tid >> 5] = n2;
+    __syncthreads();
+    const double inv = 1.0 / sqrt(red[0] + red[1] + red[2] + red[3]);
+    __syncthreads();
+    double lam = 0.0;
+    for (int t = tid; t < T; t += blockDim.x)
+    {
+        double2 av = make_double2(0.0, 0.0);
+        for (int s2 = 0; s2 < T; ++s2)
+        {
+            const double2 a = A[t * T + s2], x = v[s2];
+            av.x += a.x * x.x - a.y * x.y;
+            av.y += a.x * x.y + a.y * x.x;
+        }
+        const double2 x = v[t];
+        lam += (x.x * av.x + x.y * av.y) * inv * inv;
+        V[t * T + i] = make_double2(x.x * inv, x.y * inv);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        lam += __shfl_down_sync(0xffffffffu, lam, o);
+    if ((tid & 31) == 0)
+        red[tid >> 5] = lam;
+    __syncthreads();
+    if (tid == 0)
+        evals[i] = red[0] + red[1] + red[2] + red[3];
 }
 
 // Sort eigenpairs ascending (rank = number of smaller values, ties by index), write the
@@ -762,6 +838,10 @@ __global__ void k_eig_sort(const double* evals_in, const double2* V, int T, doub
     }
 }
 
+static int g_eig_precision = HV_EIG_FP32;
+
+void set_eig_precision(int p) { g_eig_precision = p; }
+
 size_t pca_eigh_workspace(int T)
 {
     const int Tp = (T % 2) ? T + 1 : T;
@@ -783,13 +863,27 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     double* ev_unsorted = reinterpret_cast<double*>(base + off);
     off += static_cast<size_t>(T) * sizeof(double);
     int* pairs = reinterpret_cast<int*>(base + off);
-    if (T <= JS_MAX_T)
+    if (T <= JS_MAX_T && g_eig_precision == HV_EIG_FP32)
+    {
+        const size_t smem = 2 * static_cast<size_t>(T) * (T + 1) * sizeof(float2);
+        if (smem > 48 * 1024)
+            HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem)));
+        k_jacobi_smem<float><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted);
+    }
+    else if (T <= JS_MAX_T)
     {
         const size_t smem = 2 * static_cast<size_t>(T) * (T + 1) * sizeof(double2);
         if (smem > 48 * 1024)
-            HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem)));
-        k_jacobi_smem<<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted);
+        k_jacobi_smem<double><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted);
+    }
+    if (T <= JS_MAX_T)
+    {
+        HV_LAUNCH_CHECK();
+        k_eig_refine<<<T, 128, 0, st>>>(cov, V, T, ev_unsorted);
+        count_launch();
     }
     else
         k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);

@@ -236,6 +236,13 @@ hv_status hv_pca_covariance_status(const void* work);
 hv_status hv_pca_eigh(void* cov_c128, int T, double* eigenvalues, void* eigenvectors_c128, int pmin, int pmax,
                       void* weights_c64, void* work, void* stream);
 size_t hv_pca_eigh_workspace(int T);
+/* Jacobi sweep precision for T <= 64 (process-wide). HV_EIG_FP32 (default): sweeps in FP32 in
+ * shared memory, then each eigenvector is normalised and its eigenvalue taken as the Rayleigh
+ * quotient against the FP64 covariance (GB300 runs FP64 at 1/64 of the FP32 rate, so FP64 sweeps
+ * cost milliseconds per window). HV_EIG_FP64: the sweeps themselves in FP64. T > 64 always sweeps
+ * in FP64 (global-memory kernel). */
+enum { HV_EIG_FP32 = 0, HV_EIG_FP64 = 1 };
+void hv_pca_eig_precision(int precision);
 
 /* 2-D phase unwrap of a float phase image, then rescale to [0, 65535]. Replaces unwrap_2d +
  * rescale_float_unwrap2d (tools_unwrap.cu:269-369, tools_conversion.cu:315-335). `work` must hold

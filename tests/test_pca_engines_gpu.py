@@ -45,8 +45,9 @@ def test_covariance_engine(cuda, mode, tol, T, npix):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("T", [2, 31, 64, 96])
-def test_jacobi_paths(cuda, T):
+def test_jacobi_paths(cuda, T, precision):
     rng = np.random.default_rng(T)
     X = rng.standard_normal((T, T)) + 1j * rng.standard_normal((T, T))
     A = X @ X.conj().T + np.diag(np.arange(T) * 3.0)
@@ -54,10 +55,17 @@ def test_jacobi_paths(cuda, T):
     evals = empty(T * 8)
     evecs = empty(T * T * 16)
     work = empty(hv.lib().hv_pca_eigh_workspace(T))
-    call("hv_pca_eigh", ptr(covd), T, ptr(evals), ptr(evecs), 0, 0, None, ptr(work), None)
+    hv.lib().hv_pca_eig_precision(precision)
+    try:
+        call("hv_pca_eigh", ptr(covd), T, ptr(evals), ptr(evecs), 0, 0, None, ptr(work), None)
+    finally:
+        hv.lib().hv_pca_eig_precision(0)
     ev = host(evals, np.float64, (T,))
     V = host(evecs, np.complex128, (T, T)).T
     w = np.linalg.eigvalsh(A)
-    assert np.abs(ev - w).max() <= 1e-9 * np.abs(w).max()
-    assert np.abs(V.conj().T @ V - np.eye(T)).max() < 1e-10
-    assert np.abs(A @ V - V * ev[None, :]).max() <= 1e-9 * np.abs(w).max()
+    fp64 = precision == 1 or T > 64
+    # FP32 sweeps: eigenvectors to ~1e-6, eigenvalues (Rayleigh quotients in FP64) to second order
+    tol_v, tol_w = (1e-10, 1e-9) if fp64 else (2e-5, 1e-7)
+    assert np.abs(ev - w).max() <= tol_w * np.abs(w).max()
+    assert np.abs(V.conj().T @ V - np.eye(T)).max() < tol_v
+    assert np.abs(A @ V - V * ev[None, :]).max() <= (1e-9 if fp64 else 3e-5) * np.abs(w).max()

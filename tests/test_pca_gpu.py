@@ -48,9 +48,11 @@ def test_covariance_and_eigh(cuda, T, H, W):
     assert np.all(np.diff(ev) >= -1e-9 * abs(ev).max())
     assert np.abs(ev - w_ref).max() <= 1e-6 * np.abs(w_ref).max()
     V = host(evecs, np.complex128, (T, T)).T  # stored column-major: V[:, j] = evecs[j]
-    # orthonormal and A V = V diag(w)
-    assert np.abs(V.conj().T @ V - np.eye(T)).max() < 1e-9
-    assert np.abs(ref @ V - V * ev[None, :]).max() <= 1e-6 * np.abs(w_ref).max()
+    # orthonormal and A V = V diag(w): FP32 sweeps (the default for T <= 64) give eigenvectors to
+    # ~1e-6; each column is normalised in FP64
+    assert np.abs(np.abs(np.diag(V.conj().T @ V)) - 1.0).max() < 1e-12
+    assert np.abs(V.conj().T @ V - np.eye(T)).max() < 2e-6
+    assert np.abs(ref @ V - V * ev[None, :]).max() <= 3e-5 * np.abs(w_ref).max()
     # fused projection + squared-modulus view on the selected components
     out = empty(npix * 4)
     call("hv_time_view", ptr(rd), T, W, H, ptr(wts), K, hv.IMG_SQUARED_MODULUS, 131071.0, 0, ptr(out), None, None)
