@@ -25,7 +25,10 @@ namespace hv {
 
 namespace {
 
-constexpr int TC_THREADS = 256;
+constexpr int TC_PRODUCERS = 256;            // 8 producer warps
+constexpr int TC_MMA_WARP = TC_PRODUCERS / 32;  // warp 8 issues the MMAs
+constexpr int TC_THREADS = TC_PRODUCERS + 32;
+constexpr int TC_STAGES = 3;
 constexpr int TC_KC = 64;           // pixels (K elements) per chunk
 constexpr int TC_ROWS = 128;        // M rows of the operand tile (2T <= 128, zero padded)
 constexpr int TILE_BYTES = TC_ROWS * TC_KC * 2;  // one BF16 tile: 16 KB
@@ -133,15 +136,25 @@ __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b)
     return static_cast<uint32_t>(__bfloat16_as_ushort(a)) | (static_cast<uint32_t>(__bfloat16_as_ushort(b)) << 16);
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // part: [gridDim.x][2T][2T] FP32 partial G; err: set to 1 when a bounded wait gave up.
+// Warps 0-7 produce (load with one chunk of register prefetch, split to BF16 hi/lo, store the
+// canonical tiles of stage it % TC_STAGES, arrive on full[s]); warp 8 lane 0 consumes (wait
+// full[s], 12 MMAs, commit to empty[s]); after the last chunk a commit to `done` releases the
+// epilogue (warps 0-3 read the TMEM accumulator lanes 32w..32w+31).
 __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict__ ring, int T, size_t npix,
                                                        size_t chunks_per_cta, int N, uint32_t tmem_cols,
                                                        float* __restrict__ part, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    // [buf][hi/lo] tiles
-    uint8_t* tiles = smem;
-    __shared__ __align__(8) uint64_t bars[2];
+    uint8_t* tiles = smem;  // [stage][hi/lo] tiles
+    __shared__ __align__(8) uint64_t full[TC_STAGES];
+    __shared__ __align__(8) uint64_t empty[TC_STAGES];
+    __shared__ __align__(8) uint64_t done;
     __shared__ uint32_t tmem_base;
     __shared__ int s_fail;
 
@@ -152,18 +165,23 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
     size_t c_end = c_begin + chunks_per_cta;
     if (c_end > nchunks)
         c_end = nchunks;
+    const size_t nmine = c_end > c_begin ? c_end - c_begin : 0;
 
     // zero all tiles once (rows >= 2T stay zero)
-    for (int i = tid; i < 4 * TILE_BYTES / 16; i += TC_THREADS)
+    for (int i = tid; i < TC_STAGES * 2 * TILE_BYTES / 16; i += TC_THREADS)
         reinterpret_cast<uint4*>(tiles)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0)
     {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int s2 = 0; s2 < TC_STAGES; ++s2)
+        {
+            mbar_init(&full[s2], TC_PRODUCERS);
+            mbar_init(&empty[s2], 1);
+        }
+        mbar_init(&done, 1);
         s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0)
+    if (warp == TC_MMA_WARP)
     {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(tmem_cols)
@@ -175,133 +193,121 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base;
-    const uint32_t idesc = instr_desc(TC_ROWS, N);
+    bool fail = false;
 
-    // work items per chunk: T rows x 8 k-groups (8 pixels each); at most 2 per thread (T <= 64).
-    // The loads of chunk c+1 are issued into registers before chunk c is split and stored, so
-    // global loads stay in flight while this CTA converts and the tensor cores run.
-    const int items = T * (TC_KC / 8);
-    float2 nxt[2][8];
-    auto load_chunk = [&](size_t c) {
-        const size_t p0 = c * TC_KC;
+    if (warp < TC_MMA_WARP)
+    {
+        // ------------------------------------------------------------------ producers
+        const int items = T * (TC_KC / 8);  // T rows x 8 k-groups of 8 pixels; <= 2 per thread (T <= 64)
+        float2 nxt[2][8];
+        auto load_chunk = [&](size_t c) {
+            const size_t p0 = c * TC_KC;
 #pragma unroll
-        for (int q = 0; q < 2; ++q)
-        {
-            const int w = tid + q * TC_THREADS;
-            if (w >= items)
-                continue;
-            const int t = w % T, g = w / T;
-            const size_t p = p0 + static_cast<size_t>(g) * 8;
-            const float2* src = ring + static_cast<size_t>(t) * npix + p;
-            if (p + 8 <= npix)
+            for (int q = 0; q < 2; ++q)
             {
-                const float4* s4 = reinterpret_cast<const float4*>(src);
+                const int w = tid + q * TC_PRODUCERS;
+                if (w >= items)
+                    continue;
+                const int t = w % T, g = w / T;
+                const size_t p = p0 + static_cast<size_t>(g) * 8;
+                const float2* src = ring + static_cast<size_t>(t) * npix + p;
+                if (p + 8 <= npix)
+                {
+                    const float4* s4 = reinterpret_cast<const float4*>(src);
+#pragma unroll
+                    for (int h = 0; h < 4; ++h)
+                    {
+                        const float4 f = __ldcs(s4 + h);
+                        nxt[q][2 * h] = make_float2(f.x, f.y);
+                        nxt[q][2 * h + 1] = make_float2(f.z, f.w);
+                    }
+                }
+                else
+                {
+#pragma unroll
+                    for (int h = 0; h < 8; ++h)
+                        nxt[q][h] = (p + h < npix) ? __ldg(src + h) : make_float2(0.f, 0.f);
+                }
+            }
+        };
+        if (nmine)
+            load_chunk(c_begin);
+        for (size_t it = 0; it < nmine; ++it)
+        {
+            const int st = static_cast<int>(it % TC_STAGES);
+            const size_t use = it / TC_STAGES;
+            float2 cur[2][8];
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+#pragma unroll
+                for (int h = 0; h < 8; ++h)
+                    cur[q][h] = nxt[q][h];
+            if (it + 1 < nmine)
+                load_chunk(c_begin + it + 1);
+            if (use >= 1 && !mbar_wait(&empty[st], static_cast<uint32_t>((use - 1) & 1)))
+                fail = true;
+            uint8_t* th = tiles + st * 2 * TILE_BYTES;
+            uint8_t* tl = th + TILE_BYTES;
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+            {
+                const int w = tid + q * TC_PRODUCERS;
+                if (w >= items)
+                    continue;
+                const int t = w % T, g = w / T;
+                const float2* v = cur[q];
+                uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
                 for (int h = 0; h < 4; ++h)
                 {
-                    const float4 f = __ldcs(s4 + h);
-                    nxt[q][2 * h] = make_float2(f.x, f.y);
-                    nxt[q][2 * h + 1] = make_float2(f.z, f.w);
+                    const __nv_bfloat16 a0 = __float2bfloat16_rn(v[2 * h].x), a1 = __float2bfloat16_rn(v[2 * h + 1].x);
+                    const __nv_bfloat16 b0 = __float2bfloat16_rn(v[2 * h].y), b1 = __float2bfloat16_rn(v[2 * h + 1].y);
+                    rh[h] = pack_bf16(a0, a1);
+                    ih[h] = pack_bf16(b0, b1);
+                    rl[h] = pack_bf16(__float2bfloat16_rn(v[2 * h].x - __bfloat162float(a0)),
+                                      __float2bfloat16_rn(v[2 * h + 1].x - __bfloat162float(a1)));
+                    il[h] = pack_bf16(__float2bfloat16_rn(v[2 * h].y - __bfloat162float(b0)),
+                                      __float2bfloat16_rn(v[2 * h + 1].y - __bfloat162float(b1)));
                 }
+                const uint32_t ore = tile_offset(2 * t, g), oim = tile_offset(2 * t + 1, g);
+                *reinterpret_cast<uint4*>(th + ore) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+                *reinterpret_cast<uint4*>(th + oim) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+                *reinterpret_cast<uint4*>(tl + ore) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+                *reinterpret_cast<uint4*>(tl + oim) = make_uint4(il[0], il[1], il[2], il[3]);
             }
-            else
-            {
-#pragma unroll
-                for (int h = 0; h < 8; ++h)
-                    nxt[q][h] = (p + h < npix) ? __ldg(src + h) : make_float2(0.f, 0.f);
-            }
+            fence_async_smem();
+            mbar_arrive(&full[st]);
         }
-    };
-    if (c_begin < c_end)
-        load_chunk(c_begin);
-    size_t it = 0;
-    bool fail = false;
-    for (size_t c = c_begin; c < c_end; ++c, ++it)
+    }
+    else if (lane == 0)
     {
-        const int buf = static_cast<int>(it & 1);
-        float2 cur[2][8];
-#pragma unroll
-        for (int q = 0; q < 2; ++q)
-#pragma unroll
-            for (int h = 0; h < 8; ++h)
-                cur[q][h] = nxt[q][h];
-        if (c + 1 < c_end)
-            load_chunk(c + 1);
-        if (it >= 2)
+        // ------------------------------------------------------------------ MMA issuer
+        const uint32_t idesc = instr_desc(TC_ROWS, N);
+        for (size_t it = 0; it < nmine; ++it)
         {
-            // MMAs of chunk it-2 read this buffer; their commit is use number (it-2)/2 of bars[buf]
-            if (!mbar_wait(&bars[buf], static_cast<uint32_t>(((it - 2) >> 1) & 1)))
+            const int st = static_cast<int>(it % TC_STAGES);
+            if (!mbar_wait(&full[st], static_cast<uint32_t>((it / TC_STAGES) & 1)))
                 fail = true;
-        }
-        uint8_t* th = tiles + buf * 2 * TILE_BYTES;
-        uint8_t* tl = th + TILE_BYTES;
-#pragma unroll
-        for (int q = 0; q < 2; ++q)
-        {
-            const int w = tid + q * TC_THREADS;
-            if (w >= items)
-                continue;
-            const int t = w % T, g = w / T;
-            const float2* v = cur[q];
-            uint32_t rh[4], rl[4], ih[4], il[4];
-#pragma unroll
-            for (int h = 0; h < 4; ++h)
-            {
-                const __nv_bfloat16 a0 = __float2bfloat16_rn(v[2 * h].x), a1 = __float2bfloat16_rn(v[2 * h + 1].x);
-                const __nv_bfloat16 b0 = __float2bfloat16_rn(v[2 * h].y), b1 = __float2bfloat16_rn(v[2 * h + 1].y);
-                rh[h] = pack_bf16(a0, a1);
-                ih[h] = pack_bf16(b0, b1);
-                rl[h] = pack_bf16(__float2bfloat16_rn(v[2 * h].x - __bfloat162float(a0)),
-                                  __float2bfloat16_rn(v[2 * h + 1].x - __bfloat162float(a1)));
-                il[h] = pack_bf16(__float2bfloat16_rn(v[2 * h].y - __bfloat162float(b0)),
-                                  __float2bfloat16_rn(v[2 * h + 1].y - __bfloat162float(b1)));
-            }
-            const uint32_t ore = tile_offset(2 * t, g), oim = tile_offset(2 * t + 1, g);
-            *reinterpret_cast<uint4*>(th + ore) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
-            *reinterpret_cast<uint4*>(th + oim) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
-            *reinterpret_cast<uint4*>(tl + ore) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
-            *reinterpret_cast<uint4*>(tl + oim) = make_uint4(il[0], il[1], il[2], il[3]);
-        }
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0)
-        {
             tc_fence_after();
-            const uint32_t ah = smem_u32(th), al = smem_u32(tl);
+            const uint32_t ah = smem_u32(tiles + st * 2 * TILE_BYTES), al = ah + TILE_BYTES;
 #pragma unroll
-            for (int s = 0; s < TC_KC / 16; ++s)
+            for (int s2 = 0; s2 < TC_KC / 16; ++s2)
             {
-                const uint64_t dh = smem_desc(ah + s * 256), dl = smem_desc(al + s * 256);
-                const uint32_t acc0 = (it > 0 || s > 0) ? 1u : 0u;
-                mma_bf16(tmem, dh, dh, idesc, acc0);  // Yh Yh^T
-                mma_bf16(tmem, dh, dl, idesc, 1u);    // Yh Yl^T
-                mma_bf16(tmem, dl, dh, idesc, 1u);    // Yl Yh^T
+                const uint64_t dh = smem_desc(ah + s2 * 256), dl = smem_desc(al + s2 * 256);
+                mma_bf16(tmem, dh, dh, idesc, (it > 0 || s2 > 0) ? 1u : 0u);  // Yh Yh^T
+                mma_bf16(tmem, dh, dl, idesc, 1u);                            // Yh Yl^T
+                mma_bf16(tmem, dl, dh, idesc, 1u);                            // Yl Yh^T
             }
-            mma_commit(&bars[buf]);
+            mma_commit(&empty[st]);
         }
+        mma_commit(&done);
     }
-    // drain: the last commit on each used buffer
-    const size_t used = it;
-    if (used >= 1)
-    {
-        const size_t last = used - 1;
-        if (!mbar_wait(&bars[last & 1], static_cast<uint32_t>((last >> 1) & 1)))
-            fail = true;
-    }
-    if (used >= 2)
-    {
-        const size_t prev = used - 2;
-        if (!mbar_wait(&bars[prev & 1], static_cast<uint32_t>((prev >> 1) & 1)))
-            fail = true;
-    }
-    if (fail)
-        s_fail = 1;
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    // epilogue: warps 0-3 read TMEM lanes 32w..32w+31 (row r of G), columns 0..N-1
+    // epilogue: wait for the last MMAs, warps 0-3 read row r = 32w + lane of G, columns 0..N-1
     if (warp < 4)
     {
+        if (!mbar_wait(&done, 0))
+            fail = true;
+        tc_fence_after();
         const int r = warp * 32 + lane;
         float* dst = part + static_cast<size_t>(blockIdx.x) * rows * rows;
         for (int c0 = 0; c0 < N; c0 += 16)
@@ -309,25 +315,20 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
             float v[16];
             const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
             tmem_ld16(taddr, v);
-            if (r < rows && used > 0)
+            if (r < rows)
             {
 #pragma unroll
                 for (int i = 0; i < 16; ++i)
                     if (c0 + i < rows)
-                        dst[static_cast<size_t>(r) * rows + c0 + i] = v[i];
-            }
-            else if (r < rows)
-            {
-#pragma unroll
-                for (int i = 0; i < 16; ++i)
-                    if (c0 + i < rows)
-                        dst[static_cast<size_t>(r) * rows + c0 + i] = 0.f;
+                        dst[static_cast<size_t>(r) * rows + c0 + i] = nmine ? v[i] : 0.f;
             }
         }
     }
+    if (fail)
+        atomicExch(&s_fail, 1);
     tc_fence_before();
     __syncthreads();
-    if (warp == 0)
+    if (warp == TC_MMA_WARP)
     {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols) : "memory");
@@ -413,7 +414,7 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
         return HV_ERR_UNSUPPORTED;
     }
     const TcPlan p = tc_plan(T, npix);
-    const size_t smem = 4 * static_cast<size_t>(TILE_BYTES) + 1024;
+    const size_t smem = static_cast<size_t>(TC_STAGES) * 2 * TILE_BYTES + 1024;
     HV_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     float* part = static_cast<float*>(work);
     k_cov_tc<<<p.ctas, TC_THREADS, smem, st>>>(ring, T, npix, p.chunks_per_cta, p.N, p.cols, part, err);

@@ -237,7 +237,7 @@ struct Tile
     // tw: this stage's table, entry (j-1)*P + k = exp(-2 pi i j k / (P r)), so consecutive k
     // (consecutive threads in row tiles) read consecutive entries
     template <int r, int P>
-    __device__ __forceinline__ static void butterflies(float2 (&x)[E], const float2* __restrict__ tw)
+    __device__ __forceinline__ static void butterflies(float2 (&x)[E], const float2* tw)
     {
         constexpr int Q = E / r;
 #pragma unroll
@@ -250,7 +250,7 @@ struct Tile
                 const int k = i % P;
 #pragma unroll
                 for (int j = 1; j < r; ++j)
-                    x[q * r + j] = cmul(x[q * r + j], __ldg(tw + (j - 1) * P + k));
+                    x[q * r + j] = cmul(x[q * r + j], tw[(j - 1) * P + k]);
             }
             dft<r>(&x[q * r]);
         }
@@ -316,6 +316,29 @@ struct Tile
     __device__ __forceinline__ static void run(float2* sm, const float2* tw, Src& src, Dst& dst)
     {
         run_list(typename Plan<N>::List{}, sm, tw, src, dst);
+    }
+
+    // Radix of the first stage and the (lane, sample) pairs a thread loads for it: element
+    // q*r0 + j of x holds sample i + j*N/r0 of lane f, (f, i) = index<r0>(thread + q*NT).
+    template <int r0, int... Rest>
+    __device__ __host__ static constexpr int first_of(RadixList<r0, Rest...>)
+    {
+        return r0;
+    }
+    static constexpr int R0 = first_of(typename Plan<N>::List{});
+
+    template <int r0, int... Rest, class Dst>
+    __device__ __forceinline__ static void run_regs_list(RadixList<r0, Rest...>, float2 (&x)[E], float2* sm,
+                                                         const float2* tw, Dst& dst)
+    {
+        chain<1, r0, Rest...>(x, sm, tw, dst);
+    }
+
+    // Transform of the tile whose first-stage inputs the caller already loaded into x.
+    template <class Dst>
+    __device__ __forceinline__ static void run_regs(float2 (&x)[E], float2* sm, const float2* tw, Dst& dst)
+    {
+        run_regs_list(typename Plan<N>::List{}, x, sm, tw, dst);
     }
 };
 

@@ -118,7 +118,19 @@ struct RowPass
     int inverse;           // 1: conj in / conj out (unnormalised inverse)
     float scale;
     const float2* tw;      // per-stage twiddle tables of the N-point plan (device)
+    int tw_count;
 };
+
+// Copies the plan's twiddle tables next to the tile in shared memory (read conflict-free:
+// consecutive threads read consecutive entries in row tiles, one broadcast entry in column tiles).
+__device__ __forceinline__ const float2* stage_twiddles(float2* dst, const float2* __restrict__ src, int count,
+                                                        int nthreads)
+{
+    for (int e = threadIdx.x; e < count; e += nthreads)
+        dst[e] = __ldg(src + e);
+    __syncthreads();
+    return dst;
+}
 
 template <int N, int F>
 __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass p)
@@ -126,24 +138,101 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
     using Tl = fft::Tile<N, F, false>;
     extern __shared__ float2 smem[];
     float2* sm = smem;
-    const float2* tw = p.tw;
+    const float2* tw = stage_twiddles(smem + F * N, p.tw, p.tw_count, Tl::NT);
 
     const int b = blockIdx.y;
     const int row0 = blockIdx.x * F;
     const size_t in_base = static_cast<size_t>(b) * p.in_frame;
     const int rows = p.rows;
-    const int kind = p.in_kind;
     const bool inv = p.inverse != 0;
-    auto src = [&](int f, int n) -> float2 {
+    constexpr int E = Tl::E, R0 = Tl::R0, Q0 = E / R0, M0 = N / R0;
+
+    // First-stage inputs: every load of the thread is issued before any is used (the input kind
+    // and the lens multiply are uniform branches outside the element loops).
+    float2 x[E];
+    size_t rb[Q0];  // element (q, j) sits at rb[q] + j * M0
+    bool ok[Q0];
+#pragma unroll
+    for (int q = 0; q < Q0; ++q)
+    {
+        int f, i;
+        Tl::template index<R0>(static_cast<int>(threadIdx.x) + q * Tl::NT, f, i);
         const int y = row0 + f;
-        if (y >= rows)
-            return make_float2(0.f, 0.f);
-        const size_t e = static_cast<size_t>(y) * N + n;
-        float2 v = load_pixel(p.in, in_base + e, kind);
-        if (p.premul)
-            v = cmul(v, __ldg(p.premul + e));
-        return inv ? cconj(v) : v;
-    };
+        ok[q] = y < rows;
+        rb[q] = static_cast<size_t>(ok[q] ? y : 0) * N + i;
+    }
+#define HV_EIDX(e) (rb[(e) / R0] + ((e) % R0) * M0)
+    switch (p.in_kind)
+    {
+    case IN_U8:
+    {
+        const uint8_t* in = static_cast<const uint8_t*>(p.in) + in_base;
+        uint8_t v[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            v[e] = __ldg(in + HV_EIDX(e));
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            x[e] = make_float2(static_cast<float>(v[e]) * 257.0f, 0.f);
+        break;
+    }
+    case IN_U16:
+    case IN_U16_BE:
+    {
+        const uint16_t* in = static_cast<const uint16_t*>(p.in) + in_base;
+        uint16_t v[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            v[e] = __ldg(in + HV_EIDX(e));
+        const bool swap = p.in_kind == IN_U16_BE;
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+        {
+            const uint16_t u = swap ? static_cast<uint16_t>((v[e] << 8) | (v[e] >> 8)) : v[e];
+            x[e] = make_float2(static_cast<float>(u), 0.f);
+        }
+        break;
+    }
+    case IN_F32:
+    {
+        const float* in = static_cast<const float*>(p.in) + in_base;
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            x[e] = make_float2(__ldg(in + HV_EIDX(e)), 0.f);
+        break;
+    }
+    default:
+    {
+        const float2* in = static_cast<const float2*>(p.in) + in_base;
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            x[e] = __ldg(in + HV_EIDX(e));
+        break;
+    }
+    }
+    if (p.premul)
+    {
+        float2 L[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            L[e] = __ldg(p.premul + HV_EIDX(e));
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            x[e] = cmul(x[e], L[e]);
+    }
+#undef HV_EIDX
+#pragma unroll
+    for (int q = 0; q < Q0; ++q)
+#pragma unroll
+        for (int j = 0; j < R0; ++j)
+        {
+            float2& v = x[q * R0 + j];
+            if (!ok[q])
+                v = make_float2(0.f, 0.f);
+            else if (inv)
+                v = cconj(v);
+        }
+
     float2* out = p.out + p.out_map.offset(b);
     const float sc = p.scale;
     auto dst = [&](int f, int n, float2 v) {
@@ -154,7 +243,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
             v = cconj(v);
         out[static_cast<size_t>(y) * N + n] = cscale(v, sc);
     };
-    Tl::run(sm, tw, src, dst);
+    Tl::run_regs(x, sm, tw, dst);
 }
 
 struct ColPass
@@ -168,6 +257,7 @@ struct ColPass
     int mode;               // 0 forward, 1 inverse, 2 forward * postmul then inverse
     float scale;
     const float2* tw;       // per-stage twiddle tables of the N-point plan (device)
+    int tw_count;
 };
 
 template <int N, int F>
@@ -176,7 +266,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, true>::NT) k_fft_cols(ColPass 
     using Tl = fft::Tile<N, F, true>;
     extern __shared__ float2 smem[];
     float2* sm = smem;
-    const float2* tw = p.tw;
+    const float2* tw = stage_twiddles(smem + F * N, p.tw, p.tw_count, Tl::NT);
 
     const int b = blockIdx.y;
     const int c0 = blockIdx.x * F;
@@ -332,13 +422,15 @@ hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
 {
     constexpr int F = row_lanes<N>();
     using Tl = fft::Tile<N, F, false>;
-    const size_t smem = static_cast<size_t>(F) * N * sizeof(float2);
+    const int tw_count = fft::twiddle_count(typename fft::Plan<N>::List{});
+    const size_t smem = (static_cast<size_t>(F) * N + tw_count) * sizeof(float2);
     if (smem > 48 * 1024)
         HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_rows<N, F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
     RowPass q = p;
     if ((q.tw = twiddles<N>()) == nullptr)
         return HV_ERR_CUDA;
+    q.tw_count = tw_count;
     dim3 grid((p.rows + F - 1) / F, nframes);
     k_fft_rows<N, F><<<grid, Tl::NT, smem, st>>>(q);
     HV_LAUNCH_CHECK();
@@ -351,13 +443,15 @@ hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
 {
     constexpr int F = col_lanes<N>();
     using Tl = fft::Tile<N, F, true>;
-    const size_t smem = static_cast<size_t>(F) * N * sizeof(float2);
+    const int tw_count = fft::twiddle_count(typename fft::Plan<N>::List{});
+    const size_t smem = (static_cast<size_t>(F) * N + tw_count) * sizeof(float2);
     if (smem > 48 * 1024)
         HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_cols<N, F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
     ColPass q = p;
     if ((q.tw = twiddles<N>()) == nullptr)
         return HV_ERR_CUDA;
+    q.tw_count = tw_count;
     dim3 grid((p.width + F - 1) / F, nframes);
     k_fft_cols<N, F><<<grid, Tl::NT, smem, st>>>(q);
     HV_LAUNCH_CHECK();
