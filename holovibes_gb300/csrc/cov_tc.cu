@@ -39,23 +39,25 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p)
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// Canonical no-swizzle K-major layout: element (r, k) of a 128 x 64 BF16 tile.
-// Core matrix = 8 rows x 8 k (16 B per row, 128 B); k-groups adjacent (LBO = 128 B),
-// row groups 8 k-groups apart (SBO = 1024 B).
+// K-major layout with the 128-byte swizzle: each of the 128 rows of a 128 x 64 BF16 tile is one
+// 128-byte line (64 k values), 8 lines form a 1024-byte atom (SBO = 1024 B), and the 16-byte
+// chunk c of row r is stored at chunk position c ^ (r & 7). A thread writing the 8 chunks of one
+// row therefore touches 8 different bank groups. Tiles start on 1024-byte boundaries.
 __device__ __forceinline__ uint32_t tile_offset(int r, int kgroup)
 {
-    return static_cast<uint32_t>((r >> 3) * 1024 + kgroup * 128 + (r & 7) * 16);
+    return static_cast<uint32_t>((r >> 3) * 1024 + (r & 7) * 128 + ((kgroup ^ (r & 7)) << 4));
 }
 
+// Descriptor of a K=16 slice: start = tile + 32 B * slice (the swizzle is applied on the address).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
 {
-    const uint64_t lbo = 128 >> 4, sbo = 1024 >> 4;
+    const uint64_t lbo = 1, sbo = 1024 >> 4;
     uint64_t d = 0;
     d |= static_cast<uint64_t>((addr & 0x3FFFF) >> 4);
     d |= lbo << 16;
     d |= sbo << 32;
     d |= 1ull << 46;  // descriptor version for tcgen05
-    // base offset 0, LBO mode 0, swizzle none (bits 61-63 = 0)
+    d |= 2ull << 61;  // 128-byte swizzle
     return d;
 }
 
@@ -151,7 +153,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
                                                        float* __restrict__ part, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t* tiles = smem;  // [stage][hi/lo] tiles
+    // [stage][hi/lo] tiles on a 1024-byte boundary (the swizzle atom); the launch adds 1 KB of slack
+    uint8_t* tiles = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
     __shared__ __align__(8) uint64_t full[TC_STAGES];
     __shared__ __align__(8) uint64_t empty[TC_STAGES];
     __shared__ __align__(8) uint64_t done;
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
                 const int w = tid + q * TC_PRODUCERS;
                 if (w >= items)
                     continue;
-                const int t = w % T, g = w / T;
+                const int g = w & 7, t = w >> 3;  // 8 threads read one frame's 512 contiguous bytes
                 const size_t p = p0 + static_cast<size_t>(g) * 8;
                 const float2* src = ring + static_cast<size_t>(t) * npix + p;
                 if (p + 8 <= npix)
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
                 const int w = tid + q * TC_PRODUCERS;
                 if (w >= items)
                     continue;
-                const int t = w % T, g = w / T;
+                const int g = w & 7, t = w >> 3;
                 const float2* v = cur[q];
                 uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
@@ -293,7 +296,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
 #pragma unroll
             for (int s2 = 0; s2 < TC_KC / 16; ++s2)
             {
-                const uint64_t dh = smem_desc(ah + s2 * 256), dl = smem_desc(al + s2 * 256);
+                const uint64_t dh = smem_desc(ah + s2 * 32), dl = smem_desc(al + s2 * 32);
                 mma_bf16(tmem, dh, dh, idesc, (it > 0 || s2 > 0) ? 1u : 0u);  // Yh Yh^T
                 mma_bf16(tmem, dh, dl, idesc, 1u);                            // Yh Yl^T
                 mma_bf16(tmem, dl, dh, idesc, 1u);                            // Yl Yh^T
