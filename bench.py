@@ -322,6 +322,7 @@ def run_ours(args):
         e0.record(stream)
         for i in range(args.steps):
             step(i)
+        pipe.join()  # the rendering stream joins the pipe stream before the closing event
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)

@@ -177,6 +177,7 @@ def _declare(L: C.CDLL) -> None:
         "hv_pipe_update_settings": (st, [vp, C.POINTER(Settings)]),
         "hv_pipe_request_autocontrast": (st, [vp]),
         "hv_pipe_sync": (st, [vp]),
+        "hv_pipe_join": (st, [vp]),
         "hv_pipe_get_contrast_range": (st, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "hv_pipe_get_float_frame": (st, [vp, vp]),
         "hv_pipe_get_ring": (st, [vp, vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
@@ -323,6 +324,10 @@ class Pipe:
 
     def sync(self) -> None:
         check(lib().hv_pipe_sync(self._p), "hv_pipe_sync")
+
+    def join(self) -> None:
+        """Make the pipe's stream wait on the device for all rendering enqueued so far."""
+        check(lib().hv_pipe_join(self._p), "hv_pipe_join")
 
     def contrast_range(self) -> tuple[float, float]:
         lo, hi = C.c_float(), C.c_float()

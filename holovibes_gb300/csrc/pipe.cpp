@@ -42,6 +42,8 @@ struct hv_pipe
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t render_stream = nullptr;  // == stream unless the double-buffered fast mode is on
+    cudaStream_t render_stream_owned = nullptr;
     bool own_stream = false;
 
     int W = 0, H = 0;
@@ -54,6 +56,13 @@ struct hv_pipe
     float2* lens = nullptr;
     float2* spatial = nullptr;
     float2* ring = nullptr;
+    // fast mode (batch == stride == window): two rings, spatial on `stream`, the window's time
+    // transform and rendering on `render_stream`, so the next batch's spatial passes overlap them
+    bool fast = false;
+    float2* rings[2] = {nullptr, nullptr};
+    cudaEvent_t ring_ready[2] = {nullptr, nullptr}, ring_free[2] = {nullptr, nullptr};
+    cudaEvent_t join_ev = nullptr;
+    uint64_t windows = 0;
     float2* weights = nullptr;
     double2* cov = nullptr;
     double* evals = nullptr;
@@ -122,6 +131,12 @@ void free_buffers(hv_pipe* p)
     for (void* v : p->allocs)
         cudaFree(v);
     p->allocs.clear();
+    for (cudaEvent_t* e : {&p->ring_ready[0], &p->ring_ready[1], &p->ring_free[0], &p->ring_free[1], &p->join_ev})
+        if (*e)
+        {
+            cudaEventDestroy(*e);
+            *e = nullptr;
+        }
     for (auto* vec : {&p->in_filled, &p->in_consumed, &p->out_ready, &p->out_freed})
     {
         for (cudaEvent_t e : *vec)
@@ -148,6 +163,8 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s)
     z.add(HW * 8);                                                      // lens
     z.add(s.space_transformation != HV_SPACE_NONE ? HW * 8 * B : 16);  // spatial
     z.add(HW * 8 * T);                                                  // ring
+    if (B == s.time_stride && B == T)
+        z.add(HW * 8 * T);  // second ring of the double-buffered fast mode
     z.add(static_cast<size_t>(K > 0 ? K : 1) * T * 8);                 // weights
     if (uses_pca(s))
     {
@@ -200,7 +217,14 @@ hv_status build(hv_pipe* p)
         return st;
     HV_ALLOC(p->lens, HW * sizeof(float2));
     HV_ALLOC(p->spatial, (s.space_transformation != HV_SPACE_NONE ? HW * p->B : 1) * sizeof(float2));
+    p->fast = p->B == p->S && p->B == p->T;
     HV_ALLOC(p->ring, HW * p->T * sizeof(float2));
+    p->rings[0] = p->ring;
+    p->rings[1] = nullptr;
+    if (p->fast)
+    {
+        HV_ALLOC(p->rings[1], HW * p->T * sizeof(float2));
+    }
     HV_ALLOC(p->weights, static_cast<size_t>(p->K) * p->T * sizeof(float2));
     if (uses_pca(s))
     {
@@ -245,6 +269,18 @@ hv_status build(hv_pipe* p)
 
     // ring starts zeroed like Queue::resize (queue.cc:131-134)
     HV_CUDA_TRY(cudaMemsetAsync(p->ring, 0, HW * p->T * sizeof(float2), p->stream));
+    if (p->fast)
+    {
+        HV_CUDA_TRY(cudaMemsetAsync(p->rings[1], 0, HW * p->T * sizeof(float2), p->stream));
+        for (int i = 0; i < 2; ++i)
+        {
+            HV_CUDA_TRY(cudaEventCreateWithFlags(&p->ring_ready[i], cudaEventDisableTiming));
+            HV_CUDA_TRY(cudaEventCreateWithFlags(&p->ring_free[i], cudaEventDisableTiming));
+        }
+    }
+    HV_CUDA_TRY(cudaEventCreateWithFlags(&p->join_ev, cudaEventDisableTiming));
+    p->render_stream = p->fast ? p->render_stream_owned : p->stream;
+    p->windows = 0;
     // lens (computed once per refresh, fourier_transform.cc:93-137)
     if (s.space_transformation == HV_SPACE_FRESNELTR)
         st = make_fresnel_lens(p->lens, p->W, p->H, s.lambda, s.z_distance, s.pixel_size, s.lens_mode, p->stream);
@@ -277,7 +313,7 @@ hv_status build(hv_pipe* p)
 hv_status render(hv_pipe* p)
 {
     const hv_settings& s = p->s;
-    cudaStream_t st = p->stream;
+    cudaStream_t st = p->render_stream;
     hv_status r;
     const bool pca = uses_pca(s);
     const bool unwrap = uses_unwrap(s);
@@ -381,6 +417,31 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
     if (p->batch_index != p->S)
         return HV_OK;
     p->batch_index = 0;
+    if (p->fast)
+    {
+        // batch == stride == window: every batch refills the whole ring in batch order (with B = T,
+        // Queue::enqueue_multiple always lands frame j in slot j), so two rings alternate. The
+        // spatial passes of batch k+1 run on `stream` while window k is transformed and rendered
+        // on `render_stream`; ring k % 2 is reused only after window k-2 finished with it.
+        const int r = static_cast<int>(p->windows & 1);
+        float2* ring = p->rings[r];
+        HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ring_free[r], 0));
+        hv_status st = spatial_transform(raw, p->kind, p->W, p->H, p->T, p->s.space_transformation, p->lens,
+                                         p->spatial, ring, 0, p->T, p->stream);
+        if (st != HV_OK)
+            return st;
+        HV_CUDA_TRY(cudaEventRecord(p->ring_ready[r], p->stream));
+        HV_CUDA_TRY(cudaStreamWaitEvent(p->render_stream, p->ring_ready[r], 0));
+        p->ring = ring;
+        p->ring_start = 0;
+        p->ring_size = p->T;
+        ++p->windows;
+        st = render(p);
+        if (st != HV_OK)
+            return st;
+        HV_CUDA_TRY(cudaEventRecord(p->ring_free[r], p->render_stream));
+        return HV_OK;
+    }
     // Queue::enqueue_multiple (queue.cc:332-380)
     int nb = p->B;
     const int T = p->T;
@@ -465,7 +526,8 @@ hv_pipe* hv_pipe_create(const hv_frame_desc* fd, const hv_settings* settings, vo
         }
         p->own_stream = true;
     }
-    if (cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&p->render_stream_owned, cudaStreamNonBlocking) != cudaSuccess)
     {
         out = HV_ERR_CUDA;
         hv_pipe_destroy(p);
@@ -488,9 +550,13 @@ void hv_pipe_destroy(hv_pipe* p)
         cudaStreamSynchronize(p->stream);
     if (p->copy_stream)
         cudaStreamSynchronize(p->copy_stream);
+    if (p->render_stream_owned)
+        cudaStreamSynchronize(p->render_stream_owned);
     free_buffers(p);
     if (p->copy_stream)
         cudaStreamDestroy(p->copy_stream);
+    if (p->render_stream_owned)
+        cudaStreamDestroy(p->render_stream_owned);
     if (p->own_stream && p->stream)
         cudaStreamDestroy(p->stream);
     delete p;
@@ -606,6 +672,7 @@ hv_status hv_pipe_update_settings(hv_pipe* p, const hv_settings* settings)
         return HV_NO_CHANGE;
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
     HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
     p->s = ns;
     return build(p);
 }
@@ -624,6 +691,19 @@ hv_status hv_pipe_sync(hv_pipe* p)
         return HV_INVALID_VALUE;
     HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    return HV_OK;
+}
+
+hv_status hv_pipe_join(hv_pipe* p)
+{
+    if (!p)
+        return HV_INVALID_VALUE;
+    if (p->render_stream != p->stream)
+    {
+        HV_CUDA_TRY(cudaEventRecord(p->join_ev, p->render_stream));
+        HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->join_ev, 0));
+    }
     return HV_OK;
 }
 
@@ -633,6 +713,7 @@ hv_status hv_pipe_get_contrast_range(hv_pipe* p, float* min_out, float* max_out)
         return HV_INVALID_VALUE;
     float r[2];
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
     HV_CUDA_TRY(cudaMemcpy(r, p->range, sizeof(r), cudaMemcpyDeviceToHost));
     if (min_out)
         *min_out = r[0];
@@ -648,6 +729,7 @@ hv_status hv_pipe_get_float_frame(hv_pipe* p, float* dst)
     if (!p->last_frame_valid)
         return HV_NO_IN_DATA;
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
     HV_CUDA_TRY(cudaMemcpy(dst, p->post, p->HW * sizeof(float), cudaMemcpyDeviceToHost));
     return HV_OK;
 }
@@ -657,6 +739,7 @@ hv_status hv_pipe_get_ring(hv_pipe* p, void* dst_host, int32_t* start, int32_t* 
     if (!p)
         return HV_INVALID_VALUE;
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
     if (dst_host)
         HV_CUDA_TRY(cudaMemcpy(dst_host, p->ring, p->HW * p->T * sizeof(float2), cudaMemcpyDeviceToHost));
     if (start)

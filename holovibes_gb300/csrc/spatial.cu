@@ -119,6 +119,7 @@ struct RowPass
     float scale;
     const float2* tw;      // per-stage twiddle tables of the N-point plan (device)
     int tw_count;
+    int stream_out;        // 1: output written with an evict-first hint (ring slots)
 };
 
 // Copies the plan's twiddle tables next to the tile in shared memory (read conflict-free:
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
         uint8_t v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e)
-            v[e] = __ldg(in + HV_EIDX(e));
+            v[e] = __ldcs(in + HV_EIDX(e));
 #pragma unroll
         for (int e = 0; e < E; ++e)
             x[e] = make_float2(static_cast<float>(v[e]) * 257.0f, 0.f);
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
         uint16_t v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e)
-            v[e] = __ldg(in + HV_EIDX(e));
+            v[e] = __ldcs(in + HV_EIDX(e));
         const bool swap = p.in_kind == IN_U16_BE;
 #pragma unroll
         for (int e = 0; e < E; ++e)
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
         const float* in = static_cast<const float*>(p.in) + in_base;
 #pragma unroll
         for (int e = 0; e < E; ++e)
-            x[e] = make_float2(__ldg(in + HV_EIDX(e)), 0.f);
+            x[e] = make_float2(__ldcs(in + HV_EIDX(e)), 0.f);
         break;
     }
     default:
@@ -235,13 +236,18 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
 
     float2* out = p.out + p.out_map.offset(b);
     const float sc = p.scale;
+    const bool stream_out = p.stream_out != 0;
     auto dst = [&](int f, int n, float2 v) {
         const int y = row0 + f;
         if (y >= rows)
             return;
         if (inv)
             v = cconj(v);
-        out[static_cast<size_t>(y) * N + n] = cscale(v, sc);
+        float2* o = out + static_cast<size_t>(y) * N + n;
+        if (stream_out)
+            __stcs(o, cscale(v, sc));
+        else
+            *o = cscale(v, sc);
     };
     Tl::run_regs(x, sm, tw, dst);
 }
@@ -258,6 +264,7 @@ struct ColPass
     float scale;
     const float2* tw;       // per-stage twiddle tables of the N-point plan (device)
     int tw_count;
+    int stream_out;         // 1: output written with an evict-first hint (ring slots)
 };
 
 template <int N, int F>
@@ -307,13 +314,18 @@ __global__ void __launch_bounds__(fft::Tile<N, F, true>::NT) k_fft_cols(ColPass 
             const float2 v = in[static_cast<size_t>(n) * W + c];
             return inv ? cconj(v) : v;
         };
+        const bool stream_out = p.stream_out != 0;
         auto dst = [&](int f, int n, float2 v) {
             const int c = c0 + f;
             if (c >= W)
                 return;
             if (inv)
                 v = cconj(v);
-            out[static_cast<size_t>(n) * W + c] = cscale(v, sc);
+            float2* o = out + static_cast<size_t>(n) * W + c;
+            if (stream_out)
+                __stcs(o, cscale(v, sc));
+            else
+                *o = cscale(v, sc);
         };
         Tl::run(sm, tw, src, dst);
     }
@@ -550,30 +562,54 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
         set_last_error_msg("frame width/height not supported by the shared-memory FFT");
         return HV_ERR_UNSUPPORTED;
     }
-    if (space == HV_SPACE_FRESNELTR)
+    // Sub-batches sized so the complex intermediate (sb frames) stays resident in the 129 MB L2
+    // between the passes; raw input is read and ring slots are written with streaming hints.
+    const size_t frame_c64 = HW * sizeof(float2);
+    int sb = static_cast<int>((48ull << 20) / frame_c64);
+    if (sb < 1)
+        sb = 1;
+    if (sb > batch)
+        sb = batch;
+    const size_t raw_frame_bytes = HW * static_cast<size_t>(in_kind_bytes(kind));
+    for (int b0 = 0; b0 < batch; b0 += sb)
     {
-        // x*L, forward rows -> work; forward columns -> ring slots
-        RowPass r{raw, kind, HW, work, work_map, lens, H, 0, 1.0f};
-        hv_status s = fft_rows(r, W, batch, st);
-        if (s != HV_OK)
-            return s;
-        ColPass c{work, HW, ring, ring_map, nullptr, W, 0, 1.0f};
-        return fft_cols(c, H, batch, st);
+        const int nb = (batch - b0) < sb ? (batch - b0) : sb;
+        const void* raw_b = static_cast<const uint8_t*>(raw) + static_cast<size_t>(b0) * raw_frame_bytes;
+        const FrameMap ring_b{HW, (slot0 + b0) % nslots, nslots};
+        const FrameMap work_b{HW, 0, nb};
+        hv_status s;
+        if (space == HV_SPACE_FRESNELTR)
+        {
+            // x*L, forward rows -> work; forward columns -> ring slots
+            RowPass r{raw_b, kind, HW, work, work_b, lens, H, 0, 1.0f};
+            if ((s = fft_rows(r, W, nb, st)) != HV_OK)
+                return s;
+            ColPass c{work, HW, ring, ring_b, nullptr, W, 0, 1.0f};
+            c.stream_out = 1;
+            if ((s = fft_cols(c, H, nb, st)) != HV_OK)
+                return s;
+        }
+        else if (space == HV_SPACE_ANGULARSP)
+        {
+            // forward rows -> work; columns: forward, *G, inverse (in place); inverse rows /(H*W) -> ring
+            RowPass r{raw_b, kind, HW, work, work_b, nullptr, H, 0, 1.0f};
+            if ((s = fft_rows(r, W, nb, st)) != HV_OK)
+                return s;
+            ColPass c{work, HW, work, work_b, lens, W, 2, 1.0f};
+            if ((s = fft_cols(c, H, nb, st)) != HV_OK)
+                return s;
+            RowPass r2{work, IN_C64, HW, ring, ring_b, nullptr, H, 1, 1.0f / static_cast<float>(HW)};
+            r2.stream_out = 1;
+            if ((s = fft_rows(r2, W, nb, st)) != HV_OK)
+                return s;
+        }
+        else
+        {
+            set_last_error_msg("unknown space transformation");
+            return HV_INVALID_VALUE;
+        }
     }
-    if (space == HV_SPACE_ANGULARSP)
-    {
-        // forward rows -> work; columns: forward, *G, inverse (in place); inverse rows /(H*W) -> ring
-        RowPass r{raw, kind, HW, work, work_map, nullptr, H, 0, 1.0f};
-        hv_status s = fft_rows(r, W, batch, st);
-        if (s != HV_OK)
-            return s;
-        ColPass c{work, HW, work, work_map, lens, W, 2, 1.0f};
-        s = fft_cols(c, H, batch, st);
-        if (s != HV_OK)
-            return s;
-        RowPass r2{work, IN_C64, HW, ring, ring_map, nullptr, H, 1, 1.0f / static_cast<float>(HW)};
-        return fft_rows(r2, W, batch, st);
-    }
+    return HV_OK;
     set_last_error_msg("unknown space transformation");
     return HV_INVALID_VALUE;
 }

@@ -814,27 +814,38 @@ __global__ void k_eig_refine(const double2* __restrict__ A, double2* __restrict_
 
 // Sort eigenpairs ascending (rank = number of smaller values, ties by index), write the
 // eigenvectors column-major like cusolverDnCheevd (evec[t + j*T]) and the PCA weights.
+// One CTA per eigenpair: the rank is counted once, the column is copied by all threads.
 __global__ void k_eig_sort(const double* evals_in, const double2* V, int T, double* evals, double2* evecs, int pmin,
                            int pmax, float2* weights)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < T; i += gridDim.x * blockDim.x)
+    __shared__ int s_rank;
+    const int i = blockIdx.x;
+    const double ei = evals_in[i];
+    if (threadIdx.x < 32)
     {
-        const double ei = evals_in[i];
         int rank = 0;
-        for (int j = 0; j < T; ++j)
+        for (int j = threadIdx.x; j < T; j += 32)
         {
             const double ej = evals_in[j];
             rank += (ej < ei) || (ej == ei && j < i);
         }
-        evals[rank] = ei;
-        for (int t = 0; t < T; ++t)
+        for (int o = 16; o > 0; o >>= 1)
+            rank += __shfl_down_sync(0xffffffffu, rank, o);
+        if (threadIdx.x == 0)
         {
-            const double2 v = V[t * T + i];  // column i of V (row-major)
-            evecs[static_cast<size_t>(rank) * T + t] = v;
-            if (weights && rank >= pmin && rank <= pmax)
-                weights[static_cast<size_t>(rank - pmin) * T + t] =
-                    make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+            s_rank = rank;
+            evals[rank] = ei;
         }
+    }
+    __syncthreads();
+    const int rank = s_rank;
+    for (int t = threadIdx.x; t < T; t += blockDim.x)
+    {
+        const double2 v = V[t * T + i];  // column i of V (row-major)
+        evecs[static_cast<size_t>(rank) * T + t] = v;
+        if (weights && rank >= pmin && rank <= pmax)
+            weights[static_cast<size_t>(rank - pmin) * T + t] =
+                make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
     }
 }
 
@@ -888,7 +899,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     else
         k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);
     HV_LAUNCH_CHECK();
-    k_eig_sort<<<(T + 127) / 128, 128, 0, st>>>(ev_unsorted, V, T, evals, evecs, pmin, pmax, weights);
+    k_eig_sort<<<T, 128, 0, st>>>(ev_unsorted, V, T, evals, evecs, pmin, pmax, weights);
     HV_LAUNCH_CHECK();
     count_launch(2);
     return HV_OK;

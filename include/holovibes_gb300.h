@@ -149,8 +149,13 @@ hv_status hv_pipe_update_settings(hv_pipe* p, const hv_settings* settings);
 /* Requests an autocontrast on the next output (Rendering::request_autocontrast,
  * Backend/sources/compute/rendering.cc:87-99). */
 hv_status hv_pipe_request_autocontrast(hv_pipe* p);
-/* Blocks until all work enqueued on the pipe's stream finished. */
+/* Blocks until all work enqueued on the pipe's streams finished. */
 hv_status hv_pipe_sync(hv_pipe* p);
+/* Makes the pipe's stream (hv_pipe_stream) wait, on the device, for all rendering enqueued so
+ * far. When batch == stride == time window the pipe double-buffers the ring and renders on a
+ * second stream so the next batch's spatial passes overlap the current window's time transform;
+ * work the caller chains on hv_pipe_stream after hv_pipe_join sees finished outputs. */
+hv_status hv_pipe_join(hv_pipe* p);
 /* Current XY contrast range (XYContrastRange setting) after the last autocontrast. */
 hv_status hv_pipe_get_contrast_range(hv_pipe* p, float* min_out, float* max_out);
 /* Copies the last float frame fed to the contrast stage (gpu_postprocess_frame) into dst (host). */
