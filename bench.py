@@ -37,7 +37,7 @@ DEFAULT_WORKLOAD = "cfg1"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
@@ -339,17 +339,23 @@ def run_ours(args):
     host_out = torch.empty(HW * 2, dtype=torch.uint8).pin_memory()
     while pipe.output_count():
         pipe.pull_into(host_out.data_ptr(), hv.MEM_HOST)
+    # acquisition-style loop with one batch in flight: push batch i (its H2D copy), then read the
+    # hologram of batch i-1 back to the host (D2H); latency = push start -> hologram on the host
     lat = []
     e2e_steps = args.steps
     if world > 1:
         torch.distributed.barrier()
+    pushed = []
     t0 = time.perf_counter()
     for i in range(e2e_steps):
-        ts = time.perf_counter()
+        pushed.append(time.perf_counter())
         pipe.enqueue_ptr(host_in[i % nb_unique].data_ptr(), B, hv.MEM_HOST)
-        if pipe.output_count():
+        while pipe.output_count() > 1:
             pipe.pull_into(host_out.data_ptr(), hv.MEM_HOST)
-            lat.append(time.perf_counter() - ts)
+            lat.append(time.perf_counter() - pushed.pop(0))
+    while pipe.output_count():
+        pipe.pull_into(host_out.data_ptr(), hv.MEM_HOST)
+        lat.append(time.perf_counter() - pushed.pop(0))
     pipe.sync()
     t_e2e = time.perf_counter() - t0
     if world > 1:
