@@ -253,8 +253,17 @@ def steps_for(hv, fd, s, dev_batch, stream):
     wts = buf(K * T * 8)
     L.hv_stft_weights(wts.data_ptr(), T, pmin, pmax, stream)
     view = buf(HW * 4)
-    out.append(("time_view", lambda: L.hv_time_view(ring.data_ptr(), T, W, H, wts.data_ptr(), K, s.image_type, 1.0,
-                                                    s.fft_shift, view.data_ptr(), None, stream), T * HW * 8 + HW * 4))
+    tc_ws = L.hv_time_view_tc_workspace(K, T)
+    if K >= 8 and tc_ws and HW % 2 == 0:
+        # the pipe's automatic engine for K >= 8 bins: tcgen05 (the call also re-splits the weights)
+        vw = buf(tc_ws)
+        out.append(("time_view_tc", lambda: L.hv_time_view_tc(ring.data_ptr(), T, W, H, wts.data_ptr(), K,
+                                                              s.image_type, 1.0, s.fft_shift, view.data_ptr(), None,
+                                                              vw.data_ptr(), stream), T * HW * 8 + HW * 4))
+    else:
+        out.append(("time_view", lambda: L.hv_time_view(ring.data_ptr(), T, W, H, wts.data_ptr(), K, s.image_type,
+                                                        1.0, s.fft_shift, view.data_ptr(), None, stream),
+                    T * HW * 8 + HW * 4))
     if s.time_transformation == hv.TIME_PCA:
         cov, cw = buf(T * T * 16), buf(L.hv_pca_cov_workspace(T, HW))
         out.append(("pca_covariance", lambda: L.hv_pca_covariance(ring.data_ptr(), T, HW, cov.data_ptr(),

@@ -192,6 +192,10 @@ def _declare(L: C.CDLL) -> None:
         "hv_fft_cols": (st, [vp, vp, i32, i32, i32, vp, i32, f32, i32, i32, vp]),
         "hv_time_view": (st, [vp, i32, i32, i32, vp, i32, i32, f32, i32, vp, vp, vp]),
         "hv_time_view_partials": (i32, [i32, i32]),
+        "hv_time_view_tc": (st, [vp, i32, i32, i32, vp, i32, i32, f32, i32, vp, vp, vp, vp]),
+        "hv_time_view_tc_workspace": (sz, [i32, i32]),
+        "hv_time_view_tc_status": (st, [vp]),
+        "hv_time_view_mode": (None, [i32]),
         "hv_stft_weights": (st, [vp, i32, i32, i32, vp]),
         "hv_pca_covariance": (st, [vp, i32, sz, vp, vp, vp]),
         "hv_pca_cov_workspace": (sz, [i32, sz]),

@@ -125,6 +125,38 @@ hv_status hv_time_view(const void* ring_c64, int T, int width, int height, const
 
 int hv_time_view_partials(int width, int height) { return time_view_partials(width, height); }
 
+void hv_time_view_mode(int mode) { set_view_mode(mode); }
+
+size_t hv_time_view_tc_workspace(int K, int T) { return view_tc_supported(K) ? view_tc_workspace(K, T) : 0; }
+
+hv_status hv_time_view_tc(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
+                          int img_type, float scale, int shift, float* out_f32, double* partials_f64, void* work,
+                          void* stream)
+{
+    if (!ring_c64 || !weights_c64 || !out_f32 || !work || img_type < 0 || img_type > HV_IMG_ARGUMENT || T <= 0 ||
+        width <= 0 || height <= 0)
+        return HV_INVALID_VALUE;
+    hv_status r = view_tc_prepare(static_cast<const float2*>(weights_c64), K, T, work, S(stream));
+    if (r != HV_OK)
+        return r;
+    return view_tc(static_cast<const float2*>(ring_c64), T, width, height, K, img_type, scale, shift, out_f32,
+                   partials_f64, work, S(stream));
+}
+
+hv_status hv_time_view_tc_status(const void* work)
+{
+    if (!work)
+        return HV_INVALID_VALUE;
+    int flag = 0;
+    HV_CUDA_TRY(cudaMemcpy(&flag, work, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag)
+    {
+        set_last_error_msg("tensor-core time view: a bounded wait gave up");
+        return HV_ERR_TIMEOUT;
+    }
+    return HV_OK;
+}
+
 hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* stream)
 {
     if (!weights_c64 || pmin < 0 || pmax < pmin || pmax >= T)

@@ -20,6 +20,7 @@
 
 #include "hv_common.cuh"
 #include "hv_internal.h"
+#include "tc_common.cuh"
 
 namespace hv {
 
@@ -32,116 +33,19 @@ constexpr int TC_STAGES = 3;
 constexpr int TC_KC = 64;           // pixels (K elements) per chunk
 constexpr int TC_ROWS = 128;        // M rows of the operand tile (2T <= 128, zero padded)
 constexpr int TILE_BYTES = TC_ROWS * TC_KC * 2;  // one BF16 tile: 16 KB
-constexpr uint32_t kSpinLimit = 1u << 26;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-// K-major layout with the 128-byte swizzle: each of the 128 rows of a 128 x 64 BF16 tile is one
-// 128-byte line (64 k values), 8 lines form a 1024-byte atom (SBO = 1024 B), and the 16-byte
-// chunk c of row r is stored at chunk position c ^ (r & 7). A thread writing the 8 chunks of one
-// row therefore touches 8 different bank groups. Tiles start on 1024-byte boundaries.
-__device__ __forceinline__ uint32_t tile_offset(int r, int kgroup)
-{
-    return static_cast<uint32_t>((r >> 3) * 1024 + (r & 7) * 128 + ((kgroup ^ (r & 7)) << 4));
-}
-
-// Descriptor of a K=16 slice: start = tile + 32 B * slice (the swizzle is applied on the address).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
-{
-    const uint64_t lbo = 1, sbo = 1024 >> 4;
-    uint64_t d = 0;
-    d |= static_cast<uint64_t>((addr & 0x3FFFF) >> 4);
-    d |= lbo << 16;
-    d |= sbo << 32;
-    d |= 1ull << 46;  // descriptor version for tcgen05
-    d |= 2ull << 61;  // 128-byte swizzle
-    return d;
-}
-
-// kind::f16 instruction descriptor: D F32, A/B BF16, both K-major, M x N.
-__host__ __device__ constexpr uint32_t instr_desc(int M, int N)
-{
-    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
-           (static_cast<uint32_t>(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-// Bounded wait for phase `parity` of the barrier; returns false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
-{
-    const uint32_t addr = smem_u32(bar);
-    for (uint32_t i = 0; i < kSpinLimit; ++i)
-    {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.b32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (done)
-            return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void fence_async_smem()
-{
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
-{
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i)
-        v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b)
-{
-    return static_cast<uint32_t>(__bfloat16_as_ushort(a)) | (static_cast<uint32_t>(__bfloat16_as_ushort(b)) << 16);
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
+using tc::fence_async_smem;
+using tc::mbar_arrive;
+using tc::mbar_init;
+using tc::mbar_wait;
+using tc::mma_bf16;
+using tc::mma_commit;
+using tc::smem_u32;
+using tc::tmem_ld16;
+__device__ __forceinline__ void tc_fence_before() { tc::fence_before(); }
+__device__ __forceinline__ void tc_fence_after() { tc::fence_after(); }
+__device__ __forceinline__ uint32_t tile_offset(int r, int kgroup) { return tc::sw128_offset(r, kgroup); }
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) { return tc::sw128_desc(addr); }
+using tc::instr_desc;
 
 // part: [gridDim.x][2T][2T] FP32 partial G; err: set to 1 when a bounded wait gave up.
 // Warps 0-7 produce (load with one chunk of register prefetch, split to BF16 hi/lo, store the
@@ -177,7 +81,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
     {
         for (int s2 = 0; s2 < TC_STAGES; ++s2)
         {
-            mbar_init(&full[s2], TC_PRODUCERS);
+            mbar_init(&full[s2], TC_PRODUCERS / 32);  // one arrival per producer warp
             mbar_init(&empty[s2], 1);
         }
         mbar_init(&done, 1);
@@ -263,14 +167,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
 #pragma unroll
                 for (int h = 0; h < 4; ++h)
                 {
-                    const __nv_bfloat16 a0 = __float2bfloat16_rn(v[2 * h].x), a1 = __float2bfloat16_rn(v[2 * h + 1].x);
-                    const __nv_bfloat16 b0 = __float2bfloat16_rn(v[2 * h].y), b1 = __float2bfloat16_rn(v[2 * h + 1].y);
-                    rh[h] = pack_bf16(a0, a1);
-                    ih[h] = pack_bf16(b0, b1);
-                    rl[h] = pack_bf16(__float2bfloat16_rn(v[2 * h].x - __bfloat162float(a0)),
-                                      __float2bfloat16_rn(v[2 * h + 1].x - __bfloat162float(a1)));
-                    il[h] = pack_bf16(__float2bfloat16_rn(v[2 * h].y - __bfloat162float(b0)),
-                                      __float2bfloat16_rn(v[2 * h + 1].y - __bfloat162float(b1)));
+                    tc::split2(v[2 * h].x, v[2 * h + 1].x, rh[h], rl[h]);
+                    tc::split2(v[2 * h].y, v[2 * h + 1].y, ih[h], il[h]);
                 }
                 const uint32_t ore = tile_offset(2 * t, g), oim = tile_offset(2 * t + 1, g);
                 *reinterpret_cast<uint4*>(th + ore) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
@@ -279,7 +177,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
                 *reinterpret_cast<uint4*>(tl + oim) = make_uint4(il[0], il[1], il[2], il[3]);
             }
             fence_async_smem();
-            mbar_arrive(&full[st]);
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(&full[st]);
         }
     }
     else if (lane == 0)

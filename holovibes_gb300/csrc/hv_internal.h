@@ -46,6 +46,15 @@ void set_eig_precision(int p);
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
                    cudaStream_t st);
 
+// view_tc.cu
+bool view_tc_supported(int K);
+void set_view_mode(int mode);
+bool view_engine_tc(int K, size_t HW);
+size_t view_tc_workspace(int K, int T);
+hv_status view_tc_prepare(const float2* weights, int K, int T, void* work, cudaStream_t st);
+hv_status view_tc(const float2* ring, int T, int W, int H, int K, int img_type, float scale, int shift, float* out,
+                  double* partials, void* work, cudaStream_t st);
+
 // render.cu
 size_t unwrap_workspace(int W, int H);
 hv_status unwrap_2d(const float* in, float* out, int W, int H, void* work, cudaStream_t st);

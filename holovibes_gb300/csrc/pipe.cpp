@@ -80,6 +80,8 @@ struct hv_pipe
     float* acc_ring = nullptr;
     float* range = nullptr;
     void* pct_work = nullptr;
+    bool view_on_tc = false;  // K-bin contraction on the tensor cores (hv_time_view_tc)
+    void* view_tc_work = nullptr;
 
     // input ring of batch slots
     uint8_t* in_ring = nullptr;
@@ -146,6 +148,7 @@ void free_buffers(hv_pipe* p)
 }
 
 bool uses_pca(const hv_settings& s) { return s.time_transformation == HV_TIME_PCA; }
+bool use_view_tc(int K, size_t HW) { return view_engine_tc(K, HW); }
 bool uses_unwrap(const hv_settings& s) { return s.image_type == HV_IMG_ARGUMENT && s.unwrap_2d; }
 
 struct Sizes
@@ -173,6 +176,8 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s)
         z.add(pca_eigh_workspace(T));
     }
     z.add(HW * 4 * 2);  // view + post
+    if (use_view_tc(K, HW))
+        z.add(view_tc_workspace(K, T));
     if (uses_unwrap(s))
     {
         z.add(HW * 4);
@@ -235,6 +240,11 @@ hv_status build(hv_pipe* p)
         HV_ALLOC(p->eig_work, pca_eigh_workspace(p->T));
     }
     HV_ALLOC(p->view, HW * sizeof(float));
+    p->view_on_tc = use_view_tc(p->K, p->HW);
+    if (p->view_on_tc)
+    {
+        HV_ALLOC(p->view_tc_work, view_tc_workspace(p->K, p->T));
+    }
     HV_ALLOC(p->post, HW * sizeof(float));
     if (uses_unwrap(s))
     {
@@ -294,6 +304,8 @@ hv_status build(hv_pipe* p)
         st = delta_weights(p->weights, p->T, p->pmin, p->pmax, p->stream);
     if (st != HV_OK)
         return st;
+    if (p->view_on_tc && !uses_pca(s) && (st = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, p->stream)) != HV_OK)
+        return st;
     float r0[4] = {s.contrast_min, s.contrast_max, 0.f, 0.f};
     HV_CUDA_TRY(cudaMemcpyAsync(p->range, r0, sizeof(r0), cudaMemcpyHostToDevice, p->stream));
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
@@ -323,6 +335,8 @@ hv_status render(hv_pipe* p)
             return r;
         if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, p->weights, p->eig_work, st)) != HV_OK)
             return r;
+        if (p->view_on_tc && (r = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, st)) != HV_OK)
+            return r;
     }
     // converts.cc:50-62: PCA views are scaled by (2 << 16) - 1
     const float scale = pca ? static_cast<float>((2 << 16) - 1) : 1.0f;
@@ -331,8 +345,10 @@ hv_status render(hv_pipe* p)
     const float* frame = p->view;
     if (!unwrap)
     {
-        if ((r = time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale, shift_in_view ? 1 : 0,
-                           p->view, renorm ? p->partials : nullptr, st)) != HV_OK)
+        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, scale, shift_in_view ? 1 : 0,
+                                         p->view, renorm ? p->partials : nullptr, p->view_tc_work, st)
+                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale,
+                                           shift_in_view ? 1 : 0, p->view, renorm ? p->partials : nullptr, st)) != HV_OK)
             return r;
         if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
                                           p->reduce_work, st)) != HV_OK)
@@ -340,8 +356,10 @@ hv_status render(hv_pipe* p)
     }
     else
     {
-        if ((r = time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, 1.0f, 0, p->view, nullptr, st)) !=
-            HV_OK)
+        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, 1.0f, 0, p->view, nullptr,
+                                         p->view_tc_work, st)
+                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, 1.0f, 0, p->view,
+                                           nullptr, st)) != HV_OK)
             return r;
         if ((r = unwrap_2d(p->view, p->unwrapped, p->W, p->H, p->unwrap_work, st)) != HV_OK)
             return r;

@@ -22,7 +22,7 @@
 
 namespace hv {
 
-constexpr int TV_THREADS = 256;
+constexpr int TV_THREADS = 128;  // one renormalisation partial per 128 pixels (same as the tensor-core view)
 constexpr int TV_KMAX = 16;  // bins per register chunk at most
 
 __device__ __forceinline__ float view_value(float2 X, int img_type)

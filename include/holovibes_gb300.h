@@ -220,6 +220,21 @@ hv_status hv_fft_cols(const void* in_c64, void* out_c64, int width, int height, 
 hv_status hv_time_view(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
                        int img_type, float scale, int shift, float* out_f32, double* partials_f64, void* stream);
 int hv_time_view_partials(int width, int height);
+/* hv_time_view on the tensor cores (tcgen05, split-BF16 with FP32 accumulation): the K-bin
+ * contraction runs as a 128-pixel x 2K x 2T GEMM per pixel tile. K <= 64, width * height even
+ * and at most 2^29, ring and work 16-byte aligned (HV_ERR_UNSUPPORTED otherwise: the ring is
+ * fetched with 2-D tensor copies). `work` needs hv_time_view_tc_workspace(K, T) bytes (pre-split
+ * weights and an error flag; 0 when K is unsupported); hv_time_view_tc_status(work) reports
+ * HV_ERR_TIMEOUT if a bounded device wait gave up. */
+hv_status hv_time_view_tc(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
+                          int img_type, float scale, int shift, float* out_f32, double* partials_f64, void* work,
+                          void* stream);
+size_t hv_time_view_tc_workspace(int K, int T);
+/* Engine of the pipe's time view (process-wide, read when a pipe is built): 0 = automatic (tensor
+ * cores for 8 <= K <= 64 selected bins, FP32 SIMT otherwise), 1 = SIMT, 2 = tensor cores wherever
+ * hv_time_view_tc supports the shape. */
+void hv_time_view_mode(int mode);
+hv_status hv_time_view_tc_status(const void* work);
 /* STFT weights W[k][t] = exp(-2*pi*i*(pmin+k)*t/T), k <= pmax-pmin, computed in FP64. */
 hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* stream);
 

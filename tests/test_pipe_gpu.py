@@ -61,6 +61,23 @@ CASES = {
                                                time_transformation_size=2, time_stride=2, batch_size=2, p_start=1,
                                                renorm=1, log_enabled=1, contrast_enabled=1, reticle_display=1,
                                                reticle_scale=0.5, contrast_lower=1.0, contrast_upper=99.0), 3),
+    # K >= 8 selected bins: the view runs on the tensor cores (automatic engine)
+    "as_stft_k11_tc": (64, 64, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=32,
+                                        time_stride=8, batch_size=8, z_distance=0.3, pixel_size=20.0, p_start=3,
+                                        p_width=10, renorm=1, fft_shift=1, contrast_enabled=1, contrast_lower=0.5,
+                                        contrast_upper=99.5), 6),
+    # all 32 PCA components: the squared-modulus sum is independent of the basis chosen inside
+    # near-degenerate eigenvalue clusters (a partial selection through such a cluster is not
+    # determined to 1e-4 by any finite-precision eigensolver; see test_pipe_view_engines_agree)
+    "fresnel_pca_all_sqmod_tc": (64, 64, 1, dict(space_transformation=1, time_transformation=2,
+                                                  time_transformation_size=32, time_stride=16, batch_size=16,
+                                                  lambda_=785e-9, z_distance=0.45, pixel_size=12.0, image_type=1,
+                                                  p_start=0, p_width=31, renorm=1, contrast_enabled=1,
+                                                  contrast_lower=0.5, contrast_upper=99.5), 4),
+    "as_stft_fast_k9_tc": (96, 64, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=16,
+                                            time_stride=16, batch_size=16, z_distance=0.3, pixel_size=20.0,
+                                            image_type=1, p_start=2, p_width=8, renorm=0, contrast_enabled=1,
+                                            contrast_lower=0.5, contrast_upper=99.5), 4),
     "fresnel_stft_ref32_big_endian": (128, 64, 2, dict(space_transformation=1, time_transformation=1,
                                                         time_transformation_size=4, time_stride=4, batch_size=4,
                                                         z_distance=0.3, pixel_size=20.0, p_start=2, p_width=1,
@@ -129,6 +146,40 @@ def test_pipe_matches_oracle(cuda, case):
     assert start == oracle.ring.start and size == oracle.ring.size
     assert rel_l2(ring, oracle.ring.data) <= 1e-4
     pipe.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("time,img,p_start,p_width", [(2, 0, 1, 8), (1, 2, 3, 10), (2, 1, 0, 15)])
+def test_pipe_view_engines_agree(cuda, time, img, p_start, p_width):
+    """The pipe with the tensor-core view and with the SIMT view on the same frames: the same
+    covariance, eigenvectors and weights feed both, so the frames agree to the view's precision."""
+    fd = hv.FrameDescriptor(64, 64, 1, 0)
+    s = hv.Settings.defaults().update(space_transformation=1, time_transformation=time, time_transformation_size=32,
+                                      time_stride=16, batch_size=16, lambda_=785e-9, z_distance=0.45,
+                                      pixel_size=12.0, image_type=img, p_start=p_start, p_width=p_width,
+                                      renorm=0 if img == hv.IMG_ARGUMENT else 1, contrast_enabled=0).validate(fd)
+    raw = Interferogram(width=64, height=64, seed=5, dtype=np.uint8, max_value=255, modes=12).frames(0, 64)
+    frames = {}
+    for mode in (1, 2):
+        hv.lib().hv_time_view_mode(mode)
+        try:
+            pipe = hv.Pipe(fd, s)
+            got = []
+            for b in range(4):
+                pipe.enqueue(raw[b * 16:(b + 1) * 16])
+                if pipe.output_count():
+                    pipe.pull()
+                    got.append(pipe.float_frame())
+            pipe.close()
+        finally:
+            hv.lib().hv_time_view_mode(0)
+        frames[mode] = got
+    assert len(frames[1]) == len(frames[2]) == 3
+    for a, b in zip(frames[1], frames[2]):
+        if img == hv.IMG_ARGUMENT:
+            assert np.mean(np.abs(wrapped_diff(a, b)) > 1e-3) < 5e-3
+        else:
+            assert rel_l2(b, a) <= 1e-4
 
 
 @pytest.mark.gpu
