@@ -215,6 +215,19 @@ def _declare(L: C.CDLL) -> None:
         "hv_percentile": (st, [vp, i32, i32, f32, f32, f32, vp, vp, vp]),
         "hv_percentile_workspace": (sz, [sz]),
         "hv_contrast_to_ushort": (st, [vp, vp, i32, i32, vp, sz, vp]),
+        "hv_server_create": (vp, [sz, i32, C.POINTER(C.c_int)]),
+        "hv_server_destroy": (None, [vp]),
+        "hv_server_stream_footprint": (sz, [C.POINTER(FrameDescriptor), C.POINTER(Settings)]),
+        "hv_server_open_stream": (st, [vp, C.POINTER(FrameDescriptor), C.POINTER(Settings), i64,
+                                       C.POINTER(C.c_int32)]),
+        "hv_server_close_stream": (st, [vp, C.c_int32]),
+        "hv_server_push": (st, [vp, C.c_int32, vp, sz, i32]),
+        "hv_server_output_count": (sz, [vp, C.c_int32]),
+        "hv_server_pull": (st, [vp, C.c_int32, vp, i32, i64]),
+        "hv_server_get_float_frame": (st, [vp, C.c_int32, vp]),
+        "hv_server_sync": (st, [vp, i64]),
+        "hv_server_get_stats": (st, [vp, C.POINTER(ServerStats)]),
+        "hv_server_reset_stats": (st, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -352,6 +365,110 @@ class Pipe:
 
     def kernel_launches(self) -> int:
         return int(lib().hv_pipe_kernel_launches(self._p))
+
+
+SERVER_NO_GRAPHS = 1
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("batches", C.c_uint64), ("outputs", C.c_uint64), ("graph_launches", C.c_uint64),
+                ("graph_kernels", C.c_uint64), ("eager_cycles", C.c_uint64), ("captures", C.c_uint64),
+                ("latency_samples", C.c_uint64), ("latency_p50_us", C.c_double), ("latency_p99_us", C.c_double),
+                ("streams", C.c_int32), ("buckets", C.c_int32), ("hbm_used", C.c_size_t), ("hbm_budget", C.c_size_t)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServedStream:
+    """One frame stream of a Server: same settings, kernels and outputs as a Pipe."""
+
+    def __init__(self, server: "Server", sid: int, fd: FrameDescriptor, settings: Settings):
+        self.server, self.id, self.fd, self.settings = server, sid, fd, settings
+
+    def enqueue(self, frames) -> None:
+        if hasattr(frames, "data_ptr"):
+            mem = MEM_DEVICE if getattr(frames, "is_cuda", False) else MEM_HOST
+            n = frames.numel() * frames.element_size() // self.fd.frame_size
+            check(lib().hv_server_push(self.server._s, self.id, frames.data_ptr(), n, mem), "hv_server_push")
+            return
+        arr = np.ascontiguousarray(frames)
+        n = arr.nbytes // self.fd.frame_size
+        check(lib().hv_server_push(self.server._s, self.id, arr.ctypes.data, n, MEM_HOST), "hv_server_push")
+
+    def enqueue_ptr(self, ptr: int, n: int, mem: int) -> None:
+        check(lib().hv_server_push(self.server._s, self.id, ptr, n, mem), "hv_server_push")
+
+    def output_count(self) -> int:
+        return int(lib().hv_server_output_count(self.server._s, self.id))
+
+    def pull(self, timeout_us: int = 10_000_000) -> np.ndarray:
+        out = np.empty((self.fd.height, self.fd.width), dtype=np.uint16)
+        check(lib().hv_server_pull(self.server._s, self.id, out.ctypes.data, MEM_HOST, timeout_us), "hv_server_pull")
+        return out
+
+    def pull_into(self, ptr: int, mem: int, timeout_us: int = 10_000_000) -> None:
+        check(lib().hv_server_pull(self.server._s, self.id, ptr, mem, timeout_us), "hv_server_pull")
+
+    def float_frame(self) -> np.ndarray:
+        out = np.empty((self.fd.height, self.fd.width), dtype=np.float32)
+        check(lib().hv_server_get_float_frame(self.server._s, self.id, out.ctypes.data), "hv_server_get_float_frame")
+        return out
+
+    def close(self) -> None:
+        if self.id is not None:
+            check(lib().hv_server_close_stream(self.server._s, self.id), "hv_server_close_stream")
+            self.id = None
+
+
+class Server:
+    """Serving engine: streams admitted by HBM footprint, grouped in shape buckets, cycles launched
+    by one engine thread (one CUDA graph launch per bucket for the steady streams)."""
+
+    def __init__(self, hbm_budget: int = 0, flags: int = 0):
+        status = C.c_int(0)
+        self._s = lib().hv_server_create(hbm_budget, flags, C.byref(status))
+        if not self._s:
+            raise HoloError(status.value, "hv_server_create")
+
+    @staticmethod
+    def footprint(fd: FrameDescriptor, settings: Settings) -> int:
+        return int(lib().hv_server_stream_footprint(C.byref(fd), C.byref(settings)))
+
+    def open_stream(self, fd: FrameDescriptor, settings: Settings, admit_timeout_us: int = 0) -> ServedStream:
+        sid = C.c_int32(0)
+        st = settings.copy()
+        check(lib().hv_server_open_stream(self._s, C.byref(fd), C.byref(st), admit_timeout_us, C.byref(sid)),
+              "hv_server_open_stream")
+        return ServedStream(self, sid.value, fd, st)
+
+    def sync(self, timeout_us: int = 30_000_000) -> None:
+        check(lib().hv_server_sync(self._s, timeout_us), "hv_server_sync")
+
+    def stats(self) -> dict:
+        out = ServerStats()
+        check(lib().hv_server_get_stats(self._s, C.byref(out)), "hv_server_get_stats")
+        return out.as_dict()
+
+    def reset_stats(self) -> None:
+        check(lib().hv_server_reset_stats(self._s), "hv_server_reset_stats")
+
+    def close(self) -> None:
+        if getattr(self, "_s", None):
+            lib().hv_server_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 __all__ = [n for n in dir() if not n.startswith("_")]

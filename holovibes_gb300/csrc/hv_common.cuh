@@ -72,9 +72,15 @@ struct FrameMap
     size_t frame_stride;  // elements between consecutive slots
     int slot0;            // slot of frame 0
     int nslots;           // ring capacity (frame b -> (slot0 + b) % nslots)
+    const int* slot0_dev = nullptr;  // device-side slot added to slot0 (a served cycle's ring_begin)
     __host__ __device__ __forceinline__ size_t offset(int b) const
     {
-        return static_cast<size_t>((slot0 + b) % nslots) * frame_stride;
+        int s0 = slot0;
+#ifdef __CUDA_ARCH__
+        if (slot0_dev)
+            s0 += *slot0_dev;
+#endif
+        return static_cast<size_t>((s0 + b) % nslots) * frame_stride;
     }
 };
 

@@ -9,6 +9,29 @@
 
 namespace hv {
 
+// Per-cycle control block of a served stream, in device memory. The kernels of a served cycle read
+// the values that change from cycle to cycle from here instead of from their launch arguments, so
+// a stream's (or a shape bucket's) whole cycle is captured once in a CUDA graph and replayed; the
+// host writes the blocks of a bucket with one copy before each launch. A null block means "use
+// the launch arguments, always active".
+struct CycleCtl
+{
+    long long raw_offset;  // byte offset of the batch in the stream's input ring
+    int active;            // the batch is processed this cycle (spatial passes run)
+    int render;            // the ring is full: the window is transformed and rendered
+    int ring_begin;        // ring slot of the batch's first frame
+    int acc_slot, acc_start, acc_count;  // accumulation queue (Queue::enqueue)
+    int pct_enable;        // the autocontrast percentile runs this cycle
+    int out_slot;          // output ring slot
+    int pad[4];
+};
+static_assert(sizeof(CycleCtl) == 56, "CycleCtl layout");
+
+#ifdef __CUDACC__
+__device__ __forceinline__ bool ctl_active(const CycleCtl* c) { return !c || c->active; }
+__device__ __forceinline__ bool ctl_render(const CycleCtl* c) { return !c || c->render; }
+#endif
+
 void set_last_error(const char* msg, const char* file, int line);
 void set_last_error_msg(const char* msg);
 void count_launch(uint64_t n = 1);
@@ -20,7 +43,8 @@ int raw_kind(int raw_bytes, int big_endian);
 hv_status make_fresnel_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st);
 hv_status make_spectral_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st);
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
-                            float2* work, float2* ring, int slot0, int nslots, cudaStream_t st);
+                            float2* work, float2* ring, int slot0, int nslots, cudaStream_t st,
+                            const CycleCtl* ctl = nullptr);
 hv_status fft2d(const float2* in, float2* out, int n0, int n1, int batch, int inverse, float scale, cudaStream_t st);
 hv_status fft_rows_pass(const void* in, int kind, float2* out, int W, int H, int batch, const float2* premul,
                         int inverse, float scale, int slot0, int nslots, cudaStream_t st);
@@ -30,7 +54,7 @@ hv_status fft_cols_pass(const float2* in, float2* out, int W, int H, int batch, 
 // time_transform.cu
 int time_view_partials(int W, int H);
 hv_status time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type, float scale,
-                    int shift, float* out, double* partials, cudaStream_t st);
+                    int shift, float* out, double* partials, cudaStream_t st, const CycleCtl* ctl = nullptr);
 hv_status stft_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
 hv_status delta_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
 size_t pca_cov_workspace(int T, size_t npix);
@@ -53,26 +77,26 @@ bool view_engine_tc(int K, size_t HW);
 size_t view_tc_workspace(int K, int T);
 hv_status view_tc_prepare(const float2* weights, int K, int T, void* work, cudaStream_t st);
 hv_status view_tc(const float2* ring, int T, int W, int H, int K, int img_type, float scale, int shift, float* out,
-                  double* partials, void* work, cudaStream_t st);
+                  double* partials, void* work, cudaStream_t st, const CycleCtl* ctl = nullptr);
 
 // render.cu
 size_t unwrap_workspace(int W, int H);
 hv_status unwrap_2d(const float* in, float* out, int W, int H, void* work, cudaStream_t st);
 size_t reduce_workspace(size_t n);
 hv_status renorm_factors(const float* frame, size_t n, int renorm_constant, const double* partials, int npartials,
-                         float* factors, void* work, cudaStream_t st);
+                         float* factors, void* work, cudaStream_t st, const CycleCtl* ctl = nullptr);
 hv_status renorm_shift_accumulate(const float* in, float* out, int W, int H, const float* factors, int shift,
                                   float* acc_ring, int A, int slot, int start, int count, int log_enabled,
-                                  cudaStream_t st, float prescale = 1.0f);
+                                  cudaStream_t st, float prescale = 1.0f, const CycleCtl* ctl = nullptr);
 hv_status shift_corners(float* frame, int W, int H, cudaStream_t st);
 hv_status accumulate(const float* frame, float* acc_ring, int A, int slot, int start, int count, float* out, size_t n,
                      cudaStream_t st);
 hv_status log10_map(float* frame, size_t n, cudaStream_t st);
 size_t percentile_workspace(size_t n);
 hv_status percentile(const float* frame, int W, int H, float lower, float upper, float reticle_scale, float* range,
-                     void* work, cudaStream_t st);
+                     void* work, cudaStream_t st, const CycleCtl* ctl = nullptr);
 hv_status contrast_to_ushort(const float* frame, const float* range, int invert, int apply, uint16_t* out, size_t n,
-                             cudaStream_t st);
+                             cudaStream_t st, const CycleCtl* ctl = nullptr);
 
 }  // namespace hv
 

@@ -26,7 +26,7 @@
 #include <thread>
 #include <vector>
 
-#include "hv_internal.h"
+#include "pipe_internal.h"
 
 namespace hv {
 void settings_default(hv_settings* s);
@@ -34,80 +34,6 @@ hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd);
 }  // namespace hv
 
 using namespace hv;
-
-struct hv_pipe
-{
-    hv_frame_desc fd{};
-    hv_settings s{};
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    cudaStream_t copy_stream = nullptr;
-    cudaStream_t render_stream = nullptr;  // == stream unless the double-buffered fast mode is on
-    cudaStream_t render_stream_owned = nullptr;
-    bool own_stream = false;
-
-    int W = 0, H = 0;
-    size_t HW = 0;
-    int depth = 2, kind = 0;
-    int B = 1, T = 1, S = 1, K = 1, pmin = 0, pmax = 0, A = 0;
-
-    // device buffers
-    std::vector<void*> allocs;
-    float2* lens = nullptr;
-    float2* spatial = nullptr;
-    float2* ring = nullptr;
-    // fast mode (batch == stride == window): two rings, spatial on `stream`, the window's time
-    // transform and rendering on `render_stream`, so the next batch's spatial passes overlap them
-    bool fast = false;
-    float2* rings[2] = {nullptr, nullptr};
-    cudaEvent_t ring_ready[2] = {nullptr, nullptr}, ring_free[2] = {nullptr, nullptr};
-    cudaEvent_t join_ev = nullptr;
-    uint64_t windows = 0;
-    float2* weights = nullptr;
-    double2* cov = nullptr;
-    double* evals = nullptr;
-    double2* evecs = nullptr;
-    void* cov_work = nullptr;
-    void* eig_work = nullptr;
-    float* view = nullptr;
-    float* unwrapped = nullptr;
-    void* unwrap_work = nullptr;
-    double* partials = nullptr;
-    int npartials = 0;
-    void* reduce_work = nullptr;
-    float* factors = nullptr;
-    float* post = nullptr;
-    float* acc_ring = nullptr;
-    float* range = nullptr;
-    void* pct_work = nullptr;
-    bool view_on_tc = false;  // K-bin contraction on the tensor cores (hv_time_view_tc)
-    void* view_tc_work = nullptr;
-
-    // input ring of batch slots
-    uint8_t* in_ring = nullptr;
-    int in_slots = 0;
-    size_t batch_bytes = 0;
-    std::vector<cudaEvent_t> in_filled, in_consumed;
-    int in_slot = 0;
-    int in_fill = 0;  // frames already in the current slot
-
-    // output ring
-    uint16_t* out_ring = nullptr;
-    int out_cap = 0;
-    std::vector<cudaEvent_t> out_ready, out_freed;
-    int out_head = 0, out_count = 0;
-    uint64_t out_overwritten = 0;
-
-    // cycle state
-    int ring_start = 0, ring_size = 0;
-    int batch_index = 0;
-    int acc_start = 0, acc_size = 0;
-    bool autocontrast_pending = false;
-    bool last_frame_valid = false;
-    uint64_t launches0 = 0;
-
-    std::mutex mu;
-};
 
 namespace {
 
@@ -157,7 +83,7 @@ struct Sizes
     void add(size_t b) { total += (b + 255) / 256 * 256; }
 };
 
-size_t footprint(const hv_frame_desc& fd, const hv_settings& s)
+size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = false)
 {
     const size_t HW = static_cast<size_t>(fd.width) * fd.height;
     const int B = s.batch_size, T = s.time_transformation_size;
@@ -166,7 +92,7 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s)
     z.add(HW * 8);                                                      // lens
     z.add(s.space_transformation != HV_SPACE_NONE ? HW * 8 * B : 16);  // spatial
     z.add(HW * 8 * T);                                                  // ring
-    if (B == s.time_stride && B == T)
+    if (!served && B == s.time_stride && B == T)
         z.add(HW * 8 * T);  // second ring of the double-buffered fast mode
     z.add(static_cast<size_t>(K > 0 ? K : 1) * T * 8);                 // weights
     if (uses_pca(s))
@@ -222,7 +148,7 @@ hv_status build(hv_pipe* p)
         return st;
     HV_ALLOC(p->lens, HW * sizeof(float2));
     HV_ALLOC(p->spatial, (s.space_transformation != HV_SPACE_NONE ? HW * p->B : 1) * sizeof(float2));
-    p->fast = p->B == p->S && p->B == p->T;
+    p->fast = !p->served && p->B == p->S && p->B == p->T;
     HV_ALLOC(p->ring, HW * p->T * sizeof(float2));
     p->rings[0] = p->ring;
     p->rings[1] = nullptr;
@@ -316,6 +242,11 @@ hv_status build(hv_pipe* p)
     p->autocontrast_pending = s.contrast_enabled && s.contrast_auto_refresh;
     p->in_slot = 0;
     p->in_fill = 0;
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        p->ready.clear();
+        p->in_free = p->in_slots;
+    }
     p->out_head = p->out_count = 0;
     p->last_frame_valid = false;
     return HV_OK;
@@ -489,6 +420,307 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
 
 }  // namespace
 
+// ==================================================================================== served mode
+// The serving engine (server.cpp) drives these pipes: push stages complete batches in the input
+// ring and queues them; the engine plans each cycle on the host (the same bookkeeping as
+// process_batch / render) into a device-side control block and launches the cycle's kernels,
+// replayed from a CUDA graph where every kernel of the cycle is gated by the block.
+
+namespace {
+
+int64_t now_us()
+{
+    return std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+// Copies frames into input slots; a complete slot is queued for the engine. Blocks (bounded) while
+// every slot holds a queued or in-flight batch.
+hv_status served_push(hv_pipe* p, const uint8_t* src, size_t n, cudaMemcpyKind kind)
+{
+    const size_t frame_bytes = p->HW * p->depth;
+    while (n > 0)
+    {
+        const int slot = p->in_slot;
+        if (p->in_fill == 0)
+        {
+            // claim the slot: wait until the engine released one (backpressure, 10 s bound)
+            const auto t0 = std::chrono::steady_clock::now();
+            for (;;)
+            {
+                {
+                    std::lock_guard<std::mutex> g(p->mu);
+                    if (p->in_free > 0)
+                    {
+                        --p->in_free;
+                        break;
+                    }
+                }
+                if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(10))
+                {
+                    set_last_error_msg("served push: no input slot freed within 10 s");
+                    return HV_ERR_TIMEOUT;
+                }
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+            }
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->in_consumed[slot], 0));
+        }
+        const size_t take = std::min(n, static_cast<size_t>(p->B - p->in_fill));
+        uint8_t* dst = p->in_ring + slot * p->batch_bytes + static_cast<size_t>(p->in_fill) * frame_bytes;
+        HV_CUDA_TRY(cudaMemcpyAsync(dst, src, take * frame_bytes, kind, p->copy_stream));
+        p->in_fill += static_cast<int>(take);
+        src += take * frame_bytes;
+        n -= take;
+        if (p->in_fill == p->B)
+        {
+            HV_CUDA_TRY(cudaEventRecord(p->in_filled[slot], p->copy_stream));
+            {
+                std::lock_guard<std::mutex> g(p->mu);
+                p->ready.push_back({slot, now_us()});
+            }
+            p->in_fill = 0;
+            p->in_slot = (slot + 1) % p->in_slots;
+            if (p->notify)
+                p->notify(p->notify_ctx);
+        }
+    }
+    // the caller may reuse host memory on return
+    if (kind == cudaMemcpyHostToDevice)
+        HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
+    return HV_OK;
+}
+
+}  // namespace
+
+namespace hv {
+
+size_t served_footprint(const hv_frame_desc& fd, const hv_settings& s) { return footprint(fd, s, true); }
+
+hv_pipe* pipe_create_served(const hv_frame_desc* fd, const hv_settings* settings, cudaStream_t stream,
+                            void (*notify)(void*), void* ctx, hv_status* status)
+{
+    hv_status dummy;
+    hv_status& out = status ? *status : dummy;
+    if (!fd || !settings || !stream)
+    {
+        out = HV_INVALID_VALUE;
+        return nullptr;
+    }
+    hv_pipe* p = new (std::nothrow) hv_pipe();
+    if (!p)
+    {
+        out = HV_FAILURE;
+        return nullptr;
+    }
+    p->served = true;
+    p->notify = notify;
+    p->notify_ctx = ctx;
+    p->fd = *fd;
+    p->s = *settings;
+    if ((out = settings_validate(&p->s, fd)) != HV_OK)
+    {
+        delete p;
+        return nullptr;
+    }
+    if (p->s.batch_size > p->s.time_transformation_size)
+    {
+        set_last_error_msg("served streams need batch_size <= time_transformation_size");
+        out = HV_INVALID_VALUE;
+        delete p;
+        return nullptr;
+    }
+    cudaGetDevice(&p->device);
+    p->stream = stream;
+    if (cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        out = HV_ERR_CUDA;
+        delete p;
+        return nullptr;
+    }
+    p->launches0 = launch_count();
+    if ((out = build(p)) != HV_OK)
+    {
+        hv_pipe_destroy(p);
+        return nullptr;
+    }
+    return p;
+}
+
+bool served_graphable(const hv_pipe* p)
+{
+    return p->s.time_transformation != HV_TIME_PCA && !uses_unwrap(p->s);
+}
+
+bool served_plan(hv_pipe* p, CycleCtl* ctl, ServedCycle* c)
+{
+    *c = ServedCycle{};
+    std::memset(ctl, 0, sizeof(*ctl));
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        if (p->ready.empty())
+            return false;
+        c->in_slot = p->ready.front().slot;
+        c->t_push_us = p->ready.front().t_push_us;
+        p->ready.pop_front();
+    }
+    ctl->raw_offset = static_cast<long long>(c->in_slot) * static_cast<long long>(p->batch_bytes);
+    // insert_wait_time_stride (pipe.cc:400-416): only the batch completing the stride is processed
+    p->batch_index += p->B;
+    if (p->batch_index != p->S)
+        return true;
+    p->batch_index = 0;
+    c->active = true;
+    ctl->active = 1;
+    // Queue::enqueue_multiple (queue.cc:332-380), B <= T
+    const int T = p->T;
+    ctl->ring_begin = (p->ring_start + p->ring_size) % T;
+    p->ring_size += p->B;
+    if (p->ring_size > T)
+    {
+        p->ring_start = (p->ring_start + p->ring_size - T) % T;
+        p->ring_size = T;
+    }
+    // insert_wait_time_transformation_size (pipe.cc:418-427)
+    if (p->ring_size < T)
+        return true;
+    c->render = true;
+    ctl->render = 1;
+    // accumulation queue (queue.cc:149-189)
+    if (p->A > 0)
+    {
+        ctl->acc_slot = (p->acc_start + p->acc_size) % p->A;
+        if (p->acc_size < p->A)
+            ++p->acc_size;
+        else
+            p->acc_start = (p->acc_start + 1) % p->A;
+        ctl->acc_start = p->acc_start;
+        ctl->acc_count = p->acc_size;
+    }
+    // autocontrast gating (rendering.cc:239-299)
+    const hv_settings& s = p->s;
+    if (s.contrast_enabled && p->autocontrast_pending)
+    {
+        const bool apply = p->A == 0 || p->acc_size == p->A || p->acc_size == 1;
+        if (apply)
+        {
+            ctl->pct_enable = 1;
+            if (p->A == 0 || p->acc_size == p->A)
+                p->autocontrast_pending = false;
+        }
+    }
+    // output slot (the oldest output is overwritten when the queue is full)
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        if (p->out_count == p->out_cap)
+        {
+            p->out_head = (p->out_head + 1) % p->out_cap;
+            --p->out_count;
+            ++p->out_overwritten;
+        }
+        c->out_slot = (p->out_head + p->out_count) % p->out_cap;
+    }
+    ctl->out_slot = c->out_slot;
+    return true;
+}
+
+hv_status served_prepare(hv_pipe* p, const ServedCycle& c, cudaStream_t st)
+{
+    HV_CUDA_TRY(cudaStreamWaitEvent(st, p->in_filled[c.in_slot], 0));
+    if (c.render)
+        HV_CUDA_TRY(cudaStreamWaitEvent(st, p->out_freed[c.out_slot], 0));
+    return HV_OK;
+}
+
+hv_status served_record(hv_pipe* p, const CycleCtl* ctl, const ServedCycle& c, bool gated, cudaStream_t st)
+{
+    const hv_settings& s = p->s;
+    hv_status r;
+    if (gated || c.active)
+    {
+        if ((r = spatial_transform(p->in_ring, p->kind, p->W, p->H, p->B, s.space_transformation, p->lens, p->spatial,
+                                   p->ring, 0, p->T, st, ctl)) != HV_OK)
+            return r;
+    }
+    if (!gated && !c.render)
+        return HV_OK;
+    const bool pca = uses_pca(s);
+    const bool unwrap = uses_unwrap(s);
+    if (pca)
+    {
+        // not gated by the block: served PCA cycles are launched eagerly (render cycles only)
+        if ((r = pca_covariance(p->ring, p->T, p->HW, p->cov, p->cov_work, st)) != HV_OK)
+            return r;
+        if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, p->weights, p->eig_work, st)) != HV_OK)
+            return r;
+        if (p->view_on_tc && (r = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, st)) != HV_OK)
+            return r;
+    }
+    const float scale = pca ? static_cast<float>((2 << 16) - 1) : 1.0f;
+    const bool shift_in_view = s.fft_shift && !unwrap;
+    const bool renorm = s.renorm != 0;
+    const float* frame = p->view;
+    if (!unwrap)
+    {
+        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, scale, shift_in_view ? 1 : 0,
+                                         p->view, renorm ? p->partials : nullptr, p->view_tc_work, st, ctl)
+                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale,
+                                           shift_in_view ? 1 : 0, p->view, renorm ? p->partials : nullptr, st, ctl)) !=
+            HV_OK)
+            return r;
+        if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
+                                          p->reduce_work, st, ctl)) != HV_OK)
+            return r;
+    }
+    else
+    {
+        // not gated by the block: served unwrap cycles are launched eagerly (render cycles only)
+        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, 1.0f, 0, p->view, nullptr,
+                                         p->view_tc_work, st, ctl)
+                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, 1.0f, 0, p->view,
+                                           nullptr, st, ctl)) != HV_OK)
+            return r;
+        if ((r = unwrap_2d(p->view, p->unwrapped, p->W, p->H, p->unwrap_work, st)) != HV_OK)
+            return r;
+        if (pca && (r = renorm_shift_accumulate(p->unwrapped, p->unwrapped, p->W, p->H, nullptr, 0, nullptr, 0, 0, 0, 0,
+                                                0, st, scale, ctl)) != HV_OK)
+            return r;
+        frame = p->unwrapped;
+        if (renorm && (r = renorm_factors(frame, p->HW, s.renorm_constant, nullptr, 0, p->factors, p->reduce_work, st,
+                                          ctl)) != HV_OK)
+            return r;
+    }
+    const int shift_after = (s.fft_shift && unwrap) ? 1 : 0;
+    if ((r = renorm_shift_accumulate(frame, p->post, p->W, p->H, renorm ? p->factors : nullptr, shift_after,
+                                     p->A > 0 ? p->acc_ring : nullptr, p->A, 0, 0, 0, s.log_enabled, st, 1.0f, ctl)) !=
+        HV_OK)
+        return r;
+    if (s.contrast_enabled && (gated || (ctl && c.render)))
+    {
+        // gated per cycle by ctl->pct_enable (autocontrast requests)
+        if ((r = percentile(p->post, p->W, p->H, s.contrast_lower, s.contrast_upper,
+                            s.reticle_display ? s.reticle_scale : 0.0f, p->range, p->pct_work, st, ctl)) != HV_OK)
+            return r;
+    }
+    return contrast_to_ushort(p->post, p->range, s.contrast_invert, s.contrast_enabled, p->out_ring, p->HW, st, ctl);
+}
+
+hv_status served_complete(hv_pipe* p, const ServedCycle& c, cudaStream_t st)
+{
+    HV_CUDA_TRY(cudaEventRecord(p->in_consumed[c.in_slot], st));
+    if (c.render)
+    {
+        HV_CUDA_TRY(cudaEventRecord(p->out_ready[c.out_slot], st));
+        p->last_frame_valid = true;
+    }
+    std::lock_guard<std::mutex> g(p->mu);
+    ++p->in_free;
+    if (c.render)
+        ++p->out_count;
+    return HV_OK;
+}
+
+}  // namespace hv
+
 // ==================================================================================== C ABI
 
 extern "C" {
@@ -588,6 +820,8 @@ hv_status hv_pipe_push_frames(hv_pipe* p, const void* frames, size_t n, int mem)
     const uint8_t* src = static_cast<const uint8_t*>(frames);
     const cudaMemcpyKind kind = mem == HV_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     hv_status r;
+    if (p->served)
+        return served_push(p, src, n, kind);
     while (n > 0)
     {
         if (mem == HV_MEM_DEVICE && p->in_fill == 0 && n >= static_cast<size_t>(p->B))

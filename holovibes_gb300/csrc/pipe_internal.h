@@ -1,0 +1,130 @@
+// Internal view of the Pipe for the serving engine (server.cpp): the pipe's state and the
+// served-mode entry points. Not part of the ABI.
+#pragma once
+
+#include <deque>
+#include <mutex>
+#include <vector>
+
+#include "hv_internal.h"
+
+struct hv_pipe
+{
+    hv_frame_desc fd{};
+    hv_settings s{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaStream_t render_stream = nullptr;  // == stream unless the double-buffered fast mode is on
+    cudaStream_t render_stream_owned = nullptr;
+    bool own_stream = false;
+
+    int W = 0, H = 0;
+    size_t HW = 0;
+    int depth = 2, kind = 0;
+    int B = 1, T = 1, S = 1, K = 1, pmin = 0, pmax = 0, A = 0;
+
+    // device buffers
+    std::vector<void*> allocs;
+    float2* lens = nullptr;
+    float2* spatial = nullptr;
+    float2* ring = nullptr;
+    // fast mode (batch == stride == window): two rings, spatial on `stream`, the window's time
+    // transform and rendering on `render_stream`, so the next batch's spatial passes overlap them
+    bool fast = false;
+    float2* rings[2] = {nullptr, nullptr};
+    cudaEvent_t ring_ready[2] = {nullptr, nullptr}, ring_free[2] = {nullptr, nullptr};
+    cudaEvent_t join_ev = nullptr;
+    uint64_t windows = 0;
+    float2* weights = nullptr;
+    double2* cov = nullptr;
+    double* evals = nullptr;
+    double2* evecs = nullptr;
+    void* cov_work = nullptr;
+    void* eig_work = nullptr;
+    float* view = nullptr;
+    float* unwrapped = nullptr;
+    void* unwrap_work = nullptr;
+    double* partials = nullptr;
+    int npartials = 0;
+    void* reduce_work = nullptr;
+    float* factors = nullptr;
+    float* post = nullptr;
+    float* acc_ring = nullptr;
+    float* range = nullptr;
+    void* pct_work = nullptr;
+    bool view_on_tc = false;  // K-bin contraction on the tensor cores (hv_time_view_tc)
+    void* view_tc_work = nullptr;
+
+    // input ring of batch slots
+    uint8_t* in_ring = nullptr;
+    int in_slots = 0;
+    size_t batch_bytes = 0;
+    std::vector<cudaEvent_t> in_filled, in_consumed;
+    int in_slot = 0;
+    int in_fill = 0;  // frames already in the current slot
+
+    // output ring
+    uint16_t* out_ring = nullptr;
+    int out_cap = 0;
+    std::vector<cudaEvent_t> out_ready, out_freed;
+    int out_head = 0, out_count = 0;
+    uint64_t out_overwritten = 0;
+
+    // cycle state
+    int ring_start = 0, ring_size = 0;
+    int batch_index = 0;
+    int acc_start = 0, acc_size = 0;
+    bool autocontrast_pending = false;
+    bool last_frame_valid = false;
+    uint64_t launches0 = 0;
+
+    std::mutex mu;
+
+    // served mode (driven by an hv_server): inputs are only staged by push; the server plans and
+    // launches the cycles (one per ready batch) with a device-side control block
+    bool served = false;
+    struct ReadyBatch
+    {
+        int slot;          // input ring slot
+        int64_t t_push_us; // steady-clock time the batch was complete
+    };
+    std::deque<ReadyBatch> ready;  // guarded by mu
+    int in_free = 0;               // input slots not holding a queued or in-flight batch (mu)
+    void (*notify)(void*) = nullptr;
+    void* notify_ctx = nullptr;
+};
+
+namespace hv {
+
+// One planned served cycle (host side of the control block).
+struct ServedCycle
+{
+    int in_slot = -1;
+    int64_t t_push_us = 0;
+    bool active = false;  // spatial passes run (stride gate passed)
+    bool render = false;  // the window is rendered into output slot out_slot
+    int out_slot = -1;
+};
+
+// Creates a pipe for a server: cycles are launched by the server on `stream` (no double-buffered
+// fast mode); push only stages batches. B <= T and S a multiple of B are required.
+hv_pipe* pipe_create_served(const hv_frame_desc* fd, const hv_settings* s, cudaStream_t stream,
+                            void (*notify)(void*), void* ctx, hv_status* status);
+// Device footprint of a served pipe.
+size_t served_footprint(const hv_frame_desc& fd, const hv_settings& s);
+// Whether the pipe's cycle can be captured in a CUDA graph (every kernel of its cycle is gated by the
+// control block): STFT or no time transform, no 2-D unwrap.
+bool served_graphable(const hv_pipe* p);
+// Takes the oldest ready batch (if any) and advances the host bookkeeping of the cycle (stride gate,
+// ring, accumulation queue, autocontrast gating, output slot); fills the control block.
+bool served_plan(hv_pipe* p, CycleCtl* ctl, ServedCycle* c);
+// Enqueues the cycle's kernels, reading the cycle's values from `ctl_dev`. With `gated`, the whole
+// cycle is recorded (for a graph) and the control block gates it; otherwise only the planned part.
+hv_status served_record(hv_pipe* p, const CycleCtl* ctl_dev, const ServedCycle& c, bool gated, cudaStream_t st);
+// After the cycle's launch on `st`: input slot release and output publication.
+hv_status served_complete(hv_pipe* p, const ServedCycle& c, cudaStream_t st);
+// Before the cycle's launch on `st`: wait for the batch's upload and for the output slot's reader.
+hv_status served_prepare(hv_pipe* p, const ServedCycle& c, cudaStream_t st);
+
+}  // namespace hv

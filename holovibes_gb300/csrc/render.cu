@@ -269,8 +269,10 @@ size_t reduce_workspace(size_t n)
     return static_cast<size_t>(ew_grid(n)) * sizeof(double) + 64;
 }
 
-__global__ void k_partial_sums(const float* in, size_t n, double* partials)
+__global__ void k_partial_sums(const float* in, size_t n, double* partials, const CycleCtl* ctl)
 {
+    if (!ctl_render(ctl))
+        return;
     __shared__ double red[EW_THREADS / 32];
     double s = 0.0;
     for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n;
@@ -291,8 +293,11 @@ __global__ void k_partial_sums(const float* in, size_t n, double* partials)
 }
 
 // factors[0] = 2^c, factors[1] = (float)N / (float)sum; x' = (x * factors[0]) * factors[1]
-__global__ void k_renorm_factors(const double* partials, int np, size_t n, int c, float* factors)
+__global__ void k_renorm_factors(const double* partials, int np, size_t n, int c, float* factors,
+                                 const CycleCtl* ctl)
 {
+    if (!ctl_render(ctl))
+        return;
     __shared__ double red[32];
     double s = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x)
@@ -313,19 +318,19 @@ __global__ void k_renorm_factors(const double* partials, int np, size_t n, int c
 }
 
 hv_status renorm_factors(const float* frame, size_t n, int renorm_constant, const double* partials, int npartials,
-                         float* factors, void* work, cudaStream_t st)
+                         float* factors, void* work, cudaStream_t st, const CycleCtl* ctl)
 {
     if (!partials)
     {
         double* p = static_cast<double*>(work);
         const int grid = ew_grid(n);
-        k_partial_sums<<<grid, EW_THREADS, 0, st>>>(frame, n, p);
+        k_partial_sums<<<grid, EW_THREADS, 0, st>>>(frame, n, p, ctl);
         HV_LAUNCH_CHECK();
         count_launch();
         partials = p;
         npartials = grid;
     }
-    k_renorm_factors<<<1, 1024, 0, st>>>(partials, npartials, n, renorm_constant, factors);
+    k_renorm_factors<<<1, 1024, 0, st>>>(partials, npartials, n, renorm_constant, factors, ctl);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
@@ -335,8 +340,17 @@ hv_status renorm_factors(const float* frame, size_t n, int renorm_constant, cons
 // accumulation into an A-frame ring (write slot, mean of `count` frames from `start`), optional log10.
 __global__ void k_renorm_shift_acc(const float* __restrict__ in, float* __restrict__ out, int W, int H,
                                    const float* __restrict__ factors, int shift, float* __restrict__ acc, int A,
-                                   int slot, int start, int count, int log_enabled, float prescale)
+                                   int slot, int start, int count, int log_enabled, float prescale,
+                                   const CycleCtl* ctl)
 {
+    if (!ctl_render(ctl))
+        return;
+    if (ctl)
+    {
+        slot = ctl->acc_slot;
+        start = ctl->acc_start;
+        count = ctl->acc_count;
+    }
     const size_t n = static_cast<size_t>(W) * H;
     float m0 = 1.f, m1 = 1.f;
     if (factors)
@@ -378,7 +392,7 @@ __global__ void k_renorm_shift_acc(const float* __restrict__ in, float* __restri
 
 hv_status renorm_shift_accumulate(const float* in, float* out, int W, int H, const float* factors, int shift,
                                   float* acc_ring, int A, int slot, int start, int count, int log_enabled,
-                                  cudaStream_t st, float prescale)
+                                  cudaStream_t st, float prescale, const CycleCtl* ctl)
 {
     if (shift && ((W & 1) || (H & 1)))
     {
@@ -392,7 +406,7 @@ hv_status renorm_shift_accumulate(const float* in, float* out, int W, int H, con
     }
     const size_t n = static_cast<size_t>(W) * H;
     k_renorm_shift_acc<<<ew_grid(n), EW_THREADS, 0, st>>>(in, out, W, H, factors, shift, acc_ring, A, slot, start,
-                                                          count, log_enabled, prescale);
+                                                          count, log_enabled, prescale, ctl);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
@@ -435,7 +449,7 @@ hv_status accumulate(const float* frame, float* acc_ring, int A, int slot, int s
         return HV_INVALID_VALUE;
     // 1-row frame of n pixels: no shift, no renorm
     k_renorm_shift_acc<<<ew_grid(n), EW_THREADS, 0, st>>>(frame, out, static_cast<int>(n), 1, nullptr, 0, acc_ring, A,
-                                                          slot, start, count, 0, 1.0f);
+                                                          slot, start, count, 0, 1.0f, nullptr);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
@@ -485,8 +499,11 @@ __device__ __forceinline__ bool in_reticle(size_t e, int W, int H, unsigned int 
 }
 
 __global__ void k_pct_hist(const float* __restrict__ f, int W, int H, unsigned int r2, int use_reticle,
-                           const PctState* __restrict__ st, int d, unsigned int* __restrict__ hist)
+                           const PctState* __restrict__ st, int d, unsigned int* __restrict__ hist,
+                           const CycleCtl* ctl)
 {
+    if (ctl && !(ctl->render && ctl->pct_enable))
+        return;
     __shared__ unsigned int sh[2][PCT_BINS];
     for (int i = threadIdx.x; i < 2 * PCT_BINS; i += blockDim.x)
         (&sh[0][0])[i] = 0u;
@@ -518,8 +535,10 @@ __global__ void k_pct_hist(const float* __restrict__ f, int W, int H, unsigned i
 
 // One CTA of 1024 threads: prefix scan of the histogram(s), choose the digit for each rank.
 __global__ void k_pct_select(unsigned int* __restrict__ hist, PctState* __restrict__ st, int d, float lower,
-                             float upper, float* __restrict__ range)
+                             float upper, float* __restrict__ range, const CycleCtl* ctl)
 {
+    if (ctl && !(ctl->render && ctl->pct_enable))
+        return;
     __shared__ unsigned int scan[PCT_BINS];
     __shared__ unsigned int warp_tot[32];
     const int nb = (d == 2) ? 1024 : PCT_BINS;
@@ -615,7 +634,7 @@ size_t percentile_workspace(size_t n)
 }
 
 hv_status percentile(const float* frame, int W, int H, float lower, float upper, float reticle_scale, float* range,
-                     void* work, cudaStream_t st)
+                     void* work, cudaStream_t st, const CycleCtl* ctl)
 {
     const size_t n = static_cast<size_t>(W) * H;
     if (n == 0)
@@ -640,9 +659,9 @@ hv_status percentile(const float* frame, int W, int H, float lower, float upper,
         grid = 152 * 4;
     for (int d = 0; d < 3; ++d)
     {
-        k_pct_hist<<<grid, EW_THREADS, 0, st>>>(frame, W, H, r2, use_reticle, state, d, hist + d * 2 * PCT_BINS);
+        k_pct_hist<<<grid, EW_THREADS, 0, st>>>(frame, W, H, r2, use_reticle, state, d, hist + d * 2 * PCT_BINS, ctl);
         HV_LAUNCH_CHECK();
-        k_pct_select<<<1, 1024, 0, st>>>(hist + d * 2 * PCT_BINS, state, d, lower, upper, range);
+        k_pct_select<<<1, 1024, 0, st>>>(hist + d * 2 * PCT_BINS, state, d, lower, upper, range, ctl);
         HV_LAUNCH_CHECK();
     }
     count_launch(6);
@@ -662,8 +681,12 @@ __device__ __forceinline__ uint16_t to_ushort(float x)
 }
 
 __global__ void k_contrast_ushort(const float* __restrict__ in, const float* __restrict__ range, int invert, int apply,
-                                  uint16_t* __restrict__ out, size_t n)
+                                  uint16_t* __restrict__ out, size_t n, const CycleCtl* ctl)
 {
+    if (!ctl_render(ctl))
+        return;
+    if (ctl)
+        out += static_cast<size_t>(ctl->out_slot) * n;
     float mn = 0.f, factor = 1.f;
     if (apply)
     {
@@ -688,9 +711,9 @@ __global__ void k_contrast_ushort(const float* __restrict__ in, const float* __r
 }
 
 hv_status contrast_to_ushort(const float* frame, const float* range, int invert, int apply, uint16_t* out, size_t n,
-                             cudaStream_t st)
+                             cudaStream_t st, const CycleCtl* ctl)
 {
-    k_contrast_ushort<<<ew_grid(n), EW_THREADS, 0, st>>>(frame, range, invert, apply, out, n);
+    k_contrast_ushort<<<ew_grid(n), EW_THREADS, 0, st>>>(frame, range, invert, apply, out, n, ctl);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;

@@ -120,6 +120,8 @@ struct RowPass
     const float2* tw;      // per-stage twiddle tables of the N-point plan (device)
     int tw_count;
     int stream_out;        // 1: output written with an evict-first hint (ring slots)
+    const CycleCtl* ctl = nullptr;  // served cycle: gate (active) and, with raw_from_ctl, the input offset
+    int raw_from_ctl = 0;           // 1: `in` is the input ring base, the batch is at ctl->raw_offset
 };
 
 // Copies the plan's twiddle tables next to the tile in shared memory (read conflict-free:
@@ -138,6 +140,10 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
 {
     using Tl = fft::Tile<N, F, false>;
     extern __shared__ float2 smem[];
+    if (!ctl_active(p.ctl))
+        return;
+    const void* p_in = p.raw_from_ctl ? static_cast<const void*>(static_cast<const uint8_t*>(p.in) + p.ctl->raw_offset)
+                                      : p.in;
     float2* sm = smem;
     const float2* tw = stage_twiddles(smem + F * N, p.tw, p.tw_count, Tl::NT);
 
@@ -167,7 +173,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
     {
     case IN_U8:
     {
-        const uint8_t* in = static_cast<const uint8_t*>(p.in) + in_base;
+        const uint8_t* in = static_cast<const uint8_t*>(p_in) + in_base;
         uint8_t v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e)
@@ -180,7 +186,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
     case IN_U16:
     case IN_U16_BE:
     {
-        const uint16_t* in = static_cast<const uint16_t*>(p.in) + in_base;
+        const uint16_t* in = static_cast<const uint16_t*>(p_in) + in_base;
         uint16_t v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e)
@@ -196,7 +202,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
     }
     case IN_F32:
     {
-        const float* in = static_cast<const float*>(p.in) + in_base;
+        const float* in = static_cast<const float*>(p_in) + in_base;
 #pragma unroll
         for (int e = 0; e < E; ++e)
             x[e] = make_float2(__ldcs(in + HV_EIDX(e)), 0.f);
@@ -204,7 +210,7 @@ __global__ void __launch_bounds__(fft::Tile<N, F, false>::NT) k_fft_rows(RowPass
     }
     default:
     {
-        const float2* in = static_cast<const float2*>(p.in) + in_base;
+        const float2* in = static_cast<const float2*>(p_in) + in_base;
 #pragma unroll
         for (int e = 0; e < E; ++e)
             x[e] = __ldg(in + HV_EIDX(e));
@@ -265,6 +271,7 @@ struct ColPass
     const float2* tw;       // per-stage twiddle tables of the N-point plan (device)
     int tw_count;
     int stream_out;         // 1: output written with an evict-first hint (ring slots)
+    const CycleCtl* ctl = nullptr;  // served cycle: gate (active)
 };
 
 template <int N, int F>
@@ -272,6 +279,8 @@ __global__ void __launch_bounds__(fft::Tile<N, F, true>::NT) k_fft_cols(ColPass 
 {
     using Tl = fft::Tile<N, F, true>;
     extern __shared__ float2 smem[];
+    if (!ctl_active(p.ctl))
+        return;
     float2* sm = smem;
     const float2* tw = stage_twiddles(smem + F * N, p.tw, p.tw_count, Tl::NT);
 
@@ -332,8 +341,13 @@ __global__ void __launch_bounds__(fft::Tile<N, F, true>::NT) k_fft_cols(ColPass 
 }
 
 // Raw -> complex into ring slots (space transformation NONE).
-__global__ void k_convert(const void* in, int kind, size_t frame_px, int batch, float2* ring, FrameMap map)
+__global__ void k_convert(const void* in, int kind, size_t frame_px, int batch, float2* ring, FrameMap map,
+                          const CycleCtl* ctl)
 {
+    if (!ctl_active(ctl))
+        return;
+    if (ctl)
+        in = static_cast<const uint8_t*>(in) + ctl->raw_offset;
     const size_t total = frame_px * batch;
     for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < total;
          e += static_cast<size_t>(gridDim.x) * blockDim.x)
@@ -540,10 +554,13 @@ int raw_kind(int raw_bytes, int big_endian)
 }
 
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
-                            float2* work, float2* ring, int slot0, int nslots, cudaStream_t st)
+                            float2* work, float2* ring, int slot0, int nslots, cudaStream_t st, const CycleCtl* ctl)
 {
+    // With a cycle control block, `raw` is the input ring base (the batch sits at ctl->raw_offset)
+    // and the ring slot of frame 0 is slot0 + ctl->ring_begin; every pass is gated by ctl->active.
+    const int* begin_dev = ctl ? &ctl->ring_begin : nullptr;
     const size_t HW = static_cast<size_t>(W) * H;
-    const FrameMap ring_map{HW, slot0, nslots};
+    const FrameMap ring_map{HW, slot0, nslots, begin_dev};
     const FrameMap work_map{HW, 0, batch > 0 ? batch : 1};
     if (batch <= 0)
         return HV_OK;
@@ -552,7 +569,7 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
         const size_t total = HW * batch;
         const int block = 256;
         const int grid = static_cast<int>((total + block - 1) / block < 152 * 16 ? (total + block - 1) / block : 152 * 16);
-        k_convert<<<grid, block, 0, st>>>(raw, kind, HW, batch, ring, ring_map);
+        k_convert<<<grid, block, 0, st>>>(raw, kind, HW, batch, ring, ring_map, ctl);
         HV_LAUNCH_CHECK();
         count_launch();
         return HV_OK;
@@ -575,17 +592,20 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
     {
         const int nb = (batch - b0) < sb ? (batch - b0) : sb;
         const void* raw_b = static_cast<const uint8_t*>(raw) + static_cast<size_t>(b0) * raw_frame_bytes;
-        const FrameMap ring_b{HW, (slot0 + b0) % nslots, nslots};
+        const FrameMap ring_b{HW, (slot0 + b0) % nslots, nslots, begin_dev};
         const FrameMap work_b{HW, 0, nb};
         hv_status s;
         if (space == HV_SPACE_FRESNELTR)
         {
             // x*L, forward rows -> work; forward columns -> ring slots
             RowPass r{raw_b, kind, HW, work, work_b, lens, H, 0, 1.0f};
+            r.ctl = ctl;
+            r.raw_from_ctl = ctl ? 1 : 0;
             if ((s = fft_rows(r, W, nb, st)) != HV_OK)
                 return s;
             ColPass c{work, HW, ring, ring_b, nullptr, W, 0, 1.0f};
             c.stream_out = 1;
+            c.ctl = ctl;
             if ((s = fft_cols(c, H, nb, st)) != HV_OK)
                 return s;
         }
@@ -593,13 +613,17 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
         {
             // forward rows -> work; columns: forward, *G, inverse (in place); inverse rows /(H*W) -> ring
             RowPass r{raw_b, kind, HW, work, work_b, nullptr, H, 0, 1.0f};
+            r.ctl = ctl;
+            r.raw_from_ctl = ctl ? 1 : 0;
             if ((s = fft_rows(r, W, nb, st)) != HV_OK)
                 return s;
             ColPass c{work, HW, work, work_b, lens, W, 2, 1.0f};
+            c.ctl = ctl;
             if ((s = fft_cols(c, H, nb, st)) != HV_OK)
                 return s;
             RowPass r2{work, IN_C64, HW, ring, ring_b, nullptr, H, 1, 1.0f / static_cast<float>(HW)};
             r2.stream_out = 1;
+            r2.ctl = ctl;
             if ((s = fft_rows(r2, W, nb, st)) != HV_OK)
                 return s;
         }

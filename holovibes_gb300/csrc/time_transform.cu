@@ -43,8 +43,10 @@ template <int KC>
 __global__ void __launch_bounds__(TV_THREADS) k_time_view(const float2* __restrict__ ring, int T, int W, int H,
                                                            const float2* __restrict__ weights, int K, int img_type,
                                                            float scale, int shift, float* __restrict__ out,
-                                                           double* __restrict__ partials)
+                                                           double* __restrict__ partials, const CycleCtl* ctl)
 {
+    if (!ctl_render(ctl))
+        return;
     extern __shared__ __align__(16) float2 wsm[];  // [T][KC]
     __shared__ double red[TV_THREADS / 32];
     const size_t HW = static_cast<size_t>(W) * H;
@@ -128,7 +130,8 @@ int time_view_partials(int W, int H)
 
 template <int KC>
 static hv_status launch_time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type,
-                                  float scale, int shift, float* out, double* partials, cudaStream_t st)
+                                  float scale, int shift, float* out, double* partials, cudaStream_t st,
+                                  const CycleCtl* ctl)
 {
     const size_t smem = static_cast<size_t>(T) * KC * sizeof(float2);
     if (smem > 200 * 1024)
@@ -140,14 +143,15 @@ static hv_status launch_time_view(const float2* ring, int T, int W, int H, const
         HV_CUDA_TRY(cudaFuncSetAttribute(k_time_view<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
     const int grid = time_view_partials(W, H);
-    k_time_view<KC><<<grid, TV_THREADS, smem, st>>>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials);
+    k_time_view<KC><<<grid, TV_THREADS, smem, st>>>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials,
+                                                    ctl);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
 }
 
 hv_status time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type, float scale,
-                    int shift, float* out, double* partials, cudaStream_t st)
+                    int shift, float* out, double* partials, cudaStream_t st, const CycleCtl* ctl)
 {
     if (T <= 0 || K <= 0 || W <= 0 || H <= 0)
     {
@@ -163,18 +167,18 @@ hv_status time_view(const float2* ring, int T, int W, int H, const float2* weigh
     const int chunks = (K + TV_KMAX - 1) / TV_KMAX;
     const int need = (K + chunks - 1) / chunks;
     if (need <= 1)
-        return launch_time_view<1>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+        return launch_time_view<1>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
     if (need <= 2)
-        return launch_time_view<2>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+        return launch_time_view<2>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
     if (need <= 4)
-        return launch_time_view<4>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+        return launch_time_view<4>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
     if (need <= 6)
-        return launch_time_view<6>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+        return launch_time_view<6>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
     if (need <= 8)
-        return launch_time_view<8>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+        return launch_time_view<8>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
     if (need <= 11)
-        return launch_time_view<11>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
-    return launch_time_view<16>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st);
+        return launch_time_view<11>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
+    return launch_time_view<16>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
 }
 
 // ------------------------------------------------------------------------------ weights

@@ -69,11 +69,14 @@ struct ViewTcArgs
     double* partials;     // one per tile, or null
     int* err;
     int raw_stages;
+    const CycleCtl* ctl;  // served cycle gate (render), or null
     int stacked;          // 1: D1 = Ah [Bh; Bl] (2N cols) + D2 = Al Bh;  0: D1 = Ah Bh + Al Bh, D2 = Ah Bl
 };
 
 __global__ void __launch_bounds__(V_THREADS, 1) k_view_tc(const __grid_constant__ CUtensorMap ring_map, ViewTcArgs a)
 {
+    if (!ctl_render(a.ctl))
+        return;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
     __shared__ __align__(8) uint64_t raw_full[V_MAX_RAW], raw_empty[V_MAX_RAW];
@@ -431,7 +434,7 @@ hv_status view_tc_prepare(const float2* weights, int K, int T, void* work, cudaS
 }
 
 hv_status view_tc(const float2* ring, int T, int W, int H, int K, int img_type, float scale, int shift, float* out,
-                  double* partials, void* work, cudaStream_t st)
+                  double* partials, void* work, cudaStream_t st, const CycleCtl* ctl)
 {
     if (!view_tc_supported(K))
         return HV_ERR_UNSUPPORTED;
@@ -471,6 +474,7 @@ hv_status view_tc(const float2* ring, int T, int W, int H, int K, int img_type, 
     a.bimg = static_cast<const uint8_t*>(work) + 256;
     a.out = out;
     a.partials = partials;
+    a.ctl = ctl;
     a.stacked = (3 * a.N <= static_cast<int>(V_ACC_COLS)) ? 1 : 0;
     const size_t a_bytes = V_A_STAGES * view_tc_a_stage_bytes(a.N);
     const size_t budget = 220 * 1024;

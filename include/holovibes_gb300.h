@@ -314,6 +314,55 @@ size_t hv_percentile_workspace(size_t n);
 hv_status hv_contrast_to_ushort(const float* frame, const float* range_f32, int invert, int apply_contrast,
                                 uint16_t* out, size_t n, void* stream);
 
+/* ================================================================================ serving
+ * No reference counterpart (the reference runs one Pipe per process on one compute thread,
+ * Backend/sources/core/pipe.cc:650-676). A server runs many frame streams on one GPU: each
+ * stream is a Pipe (same settings, kernels and outputs as hv_pipe_*) whose cycles are launched by
+ * one persistent engine thread. Streams are admitted by device footprint against an HBM budget;
+ * same-shape streams (width, height, depth, space / time transform, T, batch) share a bucket
+ * whose steady streams are replayed from one CUDA graph per engine pass (one launch per bucket),
+ * the others launched directly; buckets run on their own CUDA streams and overlap. Requirements
+ * per stream: batch_size <= time_transformation_size. All calls are thread-safe; push and pull of
+ * one stream from one thread each. */
+typedef struct hv_server hv_server;
+enum { HV_SERVER_NO_GRAPHS = 1 }; /* launch every cycle directly (for comparison) */
+typedef struct hv_server_stats
+{
+    uint64_t batches;        /* stream cycles planned (batches consumed) */
+    uint64_t outputs;        /* holograms rendered */
+    uint64_t graph_launches; /* bucket graph launches */
+    uint64_t graph_kernels;  /* kernel nodes executed by those launches */
+    uint64_t eager_cycles;   /* stream cycles launched directly */
+    uint64_t captures;       /* bucket graph captures */
+    uint64_t latency_samples;
+    double latency_p50_us;   /* batch complete (push) -> hologram ready, last 8192 outputs */
+    double latency_p99_us;
+    int32_t streams, buckets;
+    size_t hbm_used, hbm_budget;
+} hv_server_stats;
+/* hbm_budget_bytes = 0: 90% of the currently free device memory. */
+hv_server* hv_server_create(size_t hbm_budget_bytes, int flags, hv_status* status);
+void hv_server_destroy(hv_server* server);
+/* Device bytes a served stream holds (its admission cost); 0 for invalid settings. */
+size_t hv_server_stream_footprint(const hv_frame_desc* fd, const hv_settings* settings);
+/* Admits a stream: HV_ERR_ADMISSION when its footprint does not fit within admit_timeout_us
+ * (0: do not wait) while other streams hold the budget. */
+hv_status hv_server_open_stream(hv_server* server, const hv_frame_desc* fd, const hv_settings* settings,
+                                int64_t admit_timeout_us, int32_t* stream_id);
+hv_status hv_server_close_stream(hv_server* server, int32_t stream_id);
+/* Stages n frames (host or device memory, like hv_pipe_push_frames); blocks (10 s bound) while
+ * every input slot of the stream holds a batch not yet launched. */
+hv_status hv_server_push(hv_server* server, int32_t stream_id, const void* frames, size_t n, int mem);
+size_t hv_server_output_count(hv_server* server, int32_t stream_id);
+/* Oldest rendered hologram of the stream (waits up to timeout_us for one; < 0 waits without bound). */
+hv_status hv_server_pull(hv_server* server, int32_t stream_id, uint16_t* dst, int mem, int64_t timeout_us);
+/* Float frame fed to the contrast stage by the stream's last rendered cycle (after hv_server_sync). */
+hv_status hv_server_get_float_frame(hv_server* server, int32_t stream_id, float* dst);
+/* Waits until every staged batch has been launched and the device work has finished. */
+hv_status hv_server_sync(hv_server* server, int64_t timeout_us);
+hv_status hv_server_get_stats(hv_server* server, hv_server_stats* stats);
+hv_status hv_server_reset_stats(hv_server* server);
+
 #ifdef __cplusplus
 }
 #endif
