@@ -228,6 +228,7 @@ def _declare(L: C.CDLL) -> None:
         "hv_server_sync": (st, [vp, i64]),
         "hv_server_get_stats": (st, [vp, C.POINTER(ServerStats)]),
         "hv_server_reset_stats": (st, [vp]),
+        "hv_server_set_batch_window": (st, [vp, i64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -452,6 +453,9 @@ class Server:
 
     def reset_stats(self) -> None:
         check(lib().hv_server_reset_stats(self._s), "hv_server_reset_stats")
+
+    def set_batch_window(self, window_us: int) -> None:
+        check(lib().hv_server_set_batch_window(self._s, window_us), "hv_server_set_batch_window")
 
     def close(self) -> None:
         if getattr(self, "_s", None):

@@ -56,6 +56,8 @@ struct Member
     Bucket* bucket = nullptr;
     size_t footprint = 0;
     bool steady = false;  // ring full and one render done eagerly: eligible for the bucket graph
+    cudaGraphExec_t solo = nullptr;  // this stream's cycle alone (launched when few streams are ready)
+    size_t solo_kernels = 0;
 };
 
 struct Bucket
@@ -80,7 +82,9 @@ struct hv_server
 {
     size_t budget = 0, used = 0;
     int flags = 0;
-    std::mutex mu;  // membership, buckets, admission
+    int64_t batch_window_us = 1500;  // how long a partly ready bucket waits for its other streams
+    std::mutex mu;      // membership, buckets, admission (held by the engine during a pass)
+    std::mutex map_mu;  // the id -> stream map (push / pull lookups do not wait for the engine)
     std::condition_variable admit_cv;
     std::mutex work_mu;
     std::condition_variable work_cv;
@@ -196,29 +200,18 @@ hv_status make_bucket(const std::string& key, bool graphable, Bucket** out)
     return HV_OK;
 }
 
-// (Re)captures the bucket graph over its steady members: one branch per member.
-hv_status capture_bucket(hv_server* s, Bucket* b)
+// Captures the cycles of `ms` (members of `b`) as parallel branches of one graph.
+hv_status capture_members(hv_server* s, Bucket* b, const std::vector<Member*>& ms, cudaGraphExec_t* exec,
+                          size_t* kernels_out)
 {
-    std::vector<Member*> steady;
-    for (Member* m : b->members)
-        if (m->steady)
-            steady.push_back(m);
-    HV_CUDA_TRY(cudaStreamSynchronize(b->stream));
-    if (b->exec)
-    {
-        cudaGraphExecDestroy(b->exec);
-        b->exec = nullptr;
-    }
-    b->graph_members.clear();
-    b->graph_kernels = 0;
-    if (steady.empty())
-        return HV_OK;
+    *exec = nullptr;
+    *kernels_out = 0;
     HV_CUDA_TRY(cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal));
     hv_status r = HV_OK;
     cudaError_t e = cudaEventRecord(s->fork_ev, s->capture_stream);
-    for (size_t k = 0; k < steady.size() && e == cudaSuccess && r == HV_OK; ++k)
+    for (size_t k = 0; k < ms.size() && e == cudaSuccess && r == HV_OK; ++k)
     {
-        Member* m = steady[k];
+        Member* m = ms[k];
         const size_t idx = std::find(b->members.begin(), b->members.end(), m) - b->members.begin();
         e = cudaStreamWaitEvent(s->branch[k], s->fork_ev, 0);
         if (e == cudaSuccess)
@@ -253,26 +246,96 @@ hv_status capture_bucket(hv_server* s, Bucket* b)
         if (cudaGraphNodeGetType(n, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
             ++kernels;
     }
-    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    e = cudaGraphInstantiate(exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess)
     {
-        b->exec = nullptr;
+        *exec = nullptr;
         set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
         return HV_ERR_CUDA;
     }
-    b->graph_members = steady;
-    b->graph_kernels = kernels;
+    *kernels_out = kernels;
     ++s->captures;
     return HV_OK;
 }
 
-// One engine pass over a bucket: plan, upload the control blocks, launch.
-hv_status run_bucket(hv_server* s, Bucket* b, bool* did_work)
+void drop_graphs(Bucket* b)
+{
+    if (b->exec)
+    {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    b->graph_members.clear();
+    b->graph_kernels = 0;
+    for (Member* m : b->members)
+        if (m->solo)
+        {
+            cudaGraphExecDestroy(m->solo);
+            m->solo = nullptr;
+        }
+}
+
+// (Re)captures the bucket graph over its steady members (one branch per member) and the solo
+// graphs of steady members that have none.
+hv_status capture_bucket(hv_server* s, Bucket* b)
+{
+    std::vector<Member*> steady;
+    for (Member* m : b->members)
+        if (m->steady)
+            steady.push_back(m);
+    HV_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    if (b->exec)
+    {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    b->graph_members.clear();
+    b->graph_kernels = 0;
+    hv_status r;
+    for (Member* m : steady)
+        if (!m->solo && (r = capture_members(s, b, {m}, &m->solo, &m->solo_kernels)) != HV_OK)
+            return r;
+    if (steady.size() > 1 && (r = capture_members(s, b, steady, &b->exec, &b->graph_kernels)) != HV_OK)
+        return r;
+    b->graph_members = steady;
+    return HV_OK;
+}
+
+// One engine pass over a bucket: plan, upload the control blocks, launch. A bucket whose steady
+// streams are only partly ready waits up to batch_window_us (from its oldest ready batch) for the
+// others; then the bucket graph is launched when at least half of them are ready, else the solo
+// graphs of the ready ones. *wait_us receives the time left in a window that is still open.
+hv_status run_bucket(hv_server* s, Bucket* b, bool* did_work, int64_t* wait_us)
 {
     const size_t n = b->members.size();
     if (n == 0)
         return HV_OK;
+    const bool use_graph = b->graphable && !(s->flags & HV_SERVER_NO_GRAPHS);
+    if (use_graph)
+    {
+        size_t n_steady = 0, ready_steady = 0, ready_other = 0;
+        int64_t oldest = INT64_MAX;
+        for (Member* m : b->members)
+        {
+            std::lock_guard<std::mutex> g(m->p->mu);
+            n_steady += m->steady ? 1 : 0;
+            if (!m->p->ready.empty())
+            {
+                (m->steady ? ready_steady : ready_other) += 1;
+                oldest = std::min(oldest, m->p->ready.front().t_push_us);
+            }
+        }
+        if (ready_other == 0 && ready_steady > 0 && ready_steady < n_steady)
+        {
+            const int64_t left = oldest + s->batch_window_us - now_us();
+            if (left > 0)
+            {
+                *wait_us = std::min(*wait_us, left);
+                return HV_OK;
+            }
+        }
+    }
     const int ci = b->ctl_i;
     CycleCtl* host = b->ctl_host + static_cast<size_t>(ci) * kMaxMembers;
     // the pinned buffer is reused after its previous upload finished
@@ -296,7 +359,7 @@ hv_status run_bucket(hv_server* s, Bucket* b, bool* did_work)
     for (size_t i = 0; i < n; ++i)
         if (cyc[i].in_slot >= 0 && (r = served_prepare(b->members[i]->p, cyc[i], b->stream)) != HV_OK)
             return r;
-    const bool use_graph = b->graphable && !(s->flags & HV_SERVER_NO_GRAPHS);
+    std::vector<char> launched(n, 0);
     if (use_graph)
     {
         std::vector<Member*> steady;
@@ -305,14 +368,30 @@ hv_status run_bucket(hv_server* s, Bucket* b, bool* did_work)
                 steady.push_back(m);
         if (steady != b->graph_members && (r = capture_bucket(s, b)) != HV_OK)
             return r;
-        bool any_graph = false;
+        size_t k = 0;
         for (size_t i = 0; i < n; ++i)
-            any_graph = any_graph || (cyc[i].in_slot >= 0 && b->members[i]->steady);
-        if (any_graph && b->exec)
+            k += (cyc[i].in_slot >= 0 && b->members[i]->steady) ? 1 : 0;
+        if (k > 0 && b->exec && 2 * k >= steady.size())
         {
             HV_CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
             ++s->graph_launches;
             s->graph_kernels += b->graph_kernels;
+            for (size_t i = 0; i < n; ++i)
+                launched[i] = b->members[i]->steady ? 1 : 0;
+        }
+        else
+        {
+            for (size_t i = 0; i < n; ++i)
+            {
+                Member* m = b->members[i];
+                if (cyc[i].in_slot >= 0 && m->steady && m->solo)
+                {
+                    HV_CUDA_TRY(cudaGraphLaunch(m->solo, b->stream));
+                    ++s->graph_launches;
+                    s->graph_kernels += m->solo_kernels;
+                    launched[i] = 1;
+                }
+            }
         }
     }
     auto rec = std::make_unique<LatencyRecord>();
@@ -322,15 +401,14 @@ hv_status run_bucket(hv_server* s, Bucket* b, bool* did_work)
         if (cyc[i].in_slot < 0)
             continue;
         Member* m = b->members[i];
-        const bool in_graph = use_graph && m->steady && b->exec;
-        if (!in_graph)
+        if (!launched[i])
         {
             if ((r = served_record(m->p, b->ctl_dev + i, cyc[i], false, b->stream)) != HV_OK)
                 return r;
             if (cyc[i].active)
                 ++s->eager_cycles;
             if (cyc[i].render)
-                m->steady = true;  // joins the bucket graph from the next pass
+                m->steady = true;  // joins the graphs from the next pass
         }
         if ((r = served_complete(m->p, cyc[i], b->stream)) != HV_OK)
             return r;
@@ -349,23 +427,26 @@ hv_status run_bucket(hv_server* s, Bucket* b, bool* did_work)
 void engine_main(hv_server* s)
 {
     uint64_t seen = 0;
+    int64_t wait_us = 1000;
     while (!s->stop.load())
     {
         {
             std::unique_lock<std::mutex> lk(s->work_mu);
-            s->work_cv.wait_for(lk, std::chrono::milliseconds(1), [&] { return s->work_seq != seen || s->stop.load(); });
+            s->work_cv.wait_for(lk, std::chrono::microseconds(std::max<int64_t>(20, wait_us)),
+                                [&] { return s->work_seq != seen || s->stop.load(); });
             seen = s->work_seq;
         }
         // keep passing while any bucket found work (one batch per stream per pass)
         for (;;)
         {
             bool did = false;
+            wait_us = 1000;
             s->idle = false;
             {
                 std::lock_guard<std::mutex> g(s->mu);
                 for (Bucket* b : s->buckets)
                 {
-                    const hv_status r = run_bucket(s, b, &did);
+                    const hv_status r = run_bucket(s, b, &did, &wait_us);
                     if (r != HV_OK && s->engine_error == HV_OK)
                     {
                         s->engine_error = r;
@@ -376,13 +457,13 @@ void engine_main(hv_server* s)
             if (!did)
                 break;
         }
-        s->idle = true;
+        s->idle = wait_us >= 1000;
     }
 }
 
 Member* find_member(hv_server* s, int32_t id)
 {
-    std::lock_guard<std::mutex> g(s->mu);
+    std::lock_guard<std::mutex> g(s->map_mu);
     auto it = s->members.find(id);
     return it == s->members.end() ? nullptr : it->second;
 }
@@ -459,6 +540,8 @@ void hv_server_destroy(hv_server* s)
         cudaStreamSynchronize(b->stream);
     for (auto& kv : s->members)
     {
+        if (kv.second->solo)
+            cudaGraphExecDestroy(kv.second->solo);
         hv_pipe_destroy(kv.second->p);
         delete kv.second;
     }
@@ -551,7 +634,10 @@ hv_status hv_server_open_stream(hv_server* s, const hv_frame_desc* fd, const hv_
             m->bucket = bucket;
             m->footprint = fp;
             m->id = s->next_id++;
-            s->members[m->id] = m;
+            {
+                std::lock_guard<std::mutex> g2(s->map_mu);
+                s->members[m->id] = m;
+            }
             bucket->members.push_back(m);
         }
         else
@@ -583,21 +669,25 @@ hv_status hv_server_close_stream(hv_server* s, int32_t id)
     Bucket* empty_bucket = nullptr;
     {
         std::lock_guard<std::mutex> g(s->mu);
-        auto it = s->members.find(id);
-        if (it == s->members.end())
-            return HV_INVALID_VALUE;
-        m = it->second;
-        s->members.erase(it);
+        {
+            std::lock_guard<std::mutex> g2(s->map_mu);
+            auto it = s->members.find(id);
+            if (it == s->members.end())
+                return HV_INVALID_VALUE;
+            m = it->second;
+            s->members.erase(it);
+        }
         Bucket* b = m->bucket;
         b->members.erase(std::find(b->members.begin(), b->members.end(), m));
-        // the graph referenced this member's buffers: drop it (recaptured on the next pass)
+        // the graphs referenced this member's buffers and control-block indices: drop them
+        // (recaptured on the next pass)
         cudaStreamSynchronize(b->stream);
-        if (b->exec)
+        if (m->solo)
         {
-            cudaGraphExecDestroy(b->exec);
-            b->exec = nullptr;
+            cudaGraphExecDestroy(m->solo);
+            m->solo = nullptr;
         }
-        b->graph_members.clear();
+        drop_graphs(b);
         if (b->members.empty() && b->pending == 0)
         {
             s->buckets.erase(std::find(s->buckets.begin(), s->buckets.end(), b));
@@ -729,6 +819,14 @@ hv_status hv_server_get_stats(hv_server* s, hv_server_stats* out)
     out->hbm_used = s->used;
     out->hbm_budget = s->budget;
     return s->engine_error;
+}
+
+hv_status hv_server_set_batch_window(hv_server* s, int64_t window_us)
+{
+    if (!s || window_us < 0)
+        return HV_INVALID_VALUE;
+    s->batch_window_us = window_us;
+    return HV_OK;
 }
 
 hv_status hv_server_reset_stats(hv_server* s)

@@ -771,12 +771,283 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
         evals[i] = static_cast<double>(A[i * LD + i].x);
 }
 
+// Grid-wide variant for 64 < T <= JC_MAX_T: FP32 sweeps on two working copies of A (the step reads
+// one and writes the other) and on V in global memory (L2 resident), one cooperative grid. Every
+// CTA computes all of a step's rotations itself from the step's input copy, which no CTA writes
+// during the step (identical results: same inputs, same arithmetic), into shared memory, so a step
+// is one update phase over the grid's 2 x 2 blocks (each block read and written by one thread) and
+// one grid barrier. The barrier is a bounded sense-reversal barrier: a wait that exceeds about 2 s sets
+// the error flag and every later barrier returns at once, so the kernel ends.
+constexpr int JC_THREADS = 512;
+constexpr int JC_MAX_T = 512;
+
+// Loads of A and V in the grid kernel bypass L1 (other SMs wrote them before the last barrier).
+__device__ __forceinline__ Cx<float> ldcg(const Cx<float>* p)
+{
+    const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+    return {v.x, v.y};
+}
+
+struct GridBarrier
+{
+    unsigned int count;
+    unsigned int gen;
+    int err;
+};
+
+__device__ __forceinline__ void grid_barrier(GridBarrier* b)
+{
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        volatile unsigned int* vgen = &b->gen;
+        volatile int* verr = &b->err;
+        const unsigned int g = *vgen;
+        __threadfence();
+        if (atomicAdd(&b->count, 1u) == gridDim.x - 1)
+        {
+            b->count = 0;
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        }
+        else
+        {
+            uint64_t t0 = 0;
+            for (unsigned int i = 0; *vgen == g && !*verr; ++i)
+            {
+                if ((i & 1023u) == 1023u)
+                {
+                    uint64_t now;
+                    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+                    if (t0 == 0)
+                        t0 = now;
+                    else if (now - t0 > 2000000000ull)
+                        *verr = 1;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(JC_THREADS) k_jacobi_grid(const double2* __restrict__ Ain, Cx<float>* A0,
+                                                            Cx<float>* A1, Cx<float>* V, int T, int Tp,
+                                                            GridBarrier* bar, double2* __restrict__ Vout,
+                                                            double* __restrict__ evals)
+{
+    Cx<float>* A = A0;   // input of the current step
+    Cx<float>* An = A1;  // output of the current step
+    using R = float;
+    __shared__ int pp[JC_MAX_T / 2], pq[JC_MAX_T / 2], act[JC_MAX_T / 2];
+    __shared__ R rc[JC_MAX_T / 2], rs[JC_MAX_T / 2], rcp[JC_MAX_T / 2], rsp[JC_MAX_T / 2];
+    const int tid = threadIdx.x;
+    const size_t gtid = static_cast<size_t>(blockIdx.x) * JC_THREADS + tid;
+    const size_t gsz = static_cast<size_t>(gridDim.x) * JC_THREADS;
+    const int npairs = Tp / 2;
+    const size_t TT = static_cast<size_t>(T) * T;
+    for (size_t e = gtid; e < TT; e += gsz)
+    {
+        const int i = static_cast<int>(e / T), j = static_cast<int>(e % T);
+        const double2 a = Ain[e];
+        A0[e] = {static_cast<R>(a.x), static_cast<R>(i == j ? 0.0 : a.y)};
+        V[e] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
+    }
+    // rotations below the FP32 round-off floor of the matrix (relative to its largest diagonal
+    // entry) are not applied: in near-degenerate noise subspaces the relative test alone never
+    // stops; the FP64 Rayleigh finish recovers the eigenvalues
+    __shared__ R s_floor;
+    if (tid < 32)
+    {
+        R mx = 0;
+        for (int i = tid; i < T; i += 32)
+            mx = fmaxf(mx, fabsf(static_cast<R>(Ain[static_cast<size_t>(i) * T + i].x)));
+        for (int o = 16; o > 0; o >>= 1)
+            mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        if (tid == 0)
+            s_floor = mx * R(1e-6);
+    }
+    grid_barrier(bar);
+    const R thr = jac_threshold<R>();
+    const R abs_floor = s_floor;
+    const size_t nblocks = static_cast<size_t>(npairs) * (npairs + 1) / 2;
+    for (int sweep = 0; sweep < JAC_MAX_SWEEPS; ++sweep)
+    {
+        int sweep_active = 0;
+        for (int step = 0; step < Tp - 1; ++step)
+        {
+            int active = 0;
+            for (int k = tid; k < npairs; k += JC_THREADS)
+            {
+                int a, b;
+                if (k == 0)
+                {
+                    a = Tp - 1;
+                    b = step % (Tp - 1);
+                }
+                else
+                {
+                    a = (step + k) % (Tp - 1);
+                    b = (step - k + (Tp - 1)) % (Tp - 1);
+                }
+                const int p = a < b ? a : b, q = a < b ? b : a;
+                pp[k] = p;
+                pq[k] = q;
+                R c = 1, s = 0, cph = 1, sph = 0;
+                int on = 0;
+                if (q < T)
+                {
+                    const Cx<R> apq = ldcg(A + static_cast<size_t>(p) * T + q);
+                    const R mag = hypotf(apq.x, apq.y);
+                    const R app = ldcg(A + static_cast<size_t>(p) * T + p).x, aqq = ldcg(A + static_cast<size_t>(q) * T + q).x;
+                    if (mag > abs_floor && mag > R(1e-30) && mag > thr * sqrtf(fabsf(app * aqq)))
+                    {
+                        cph = apq.x / mag;
+                        sph = apq.y / mag;
+                        const R tau = (aqq - app) / (R(2) * mag);
+                        const R t = (tau >= 0 ? R(1) : R(-1)) / (fabsf(tau) + sqrtf(R(1) + tau * tau));
+                        c = R(1) / sqrtf(R(1) + t * t);
+                        s = t * c;
+                        on = 1;
+                    }
+                }
+                rc[k] = c;
+                rs[k] = s;
+                rcp[k] = cph;
+                rsp[k] = sph;
+                act[k] = on;
+                active |= on;
+            }
+            if (!__syncthreads_or(active))
+                continue;  // uniform over the grid: every CTA computed the same rotations
+            sweep_active = 1;
+            // A <- J^H A J on the 2 x 2 blocks (k1 >= k2, plus the mirror block)
+            for (size_t e = gtid; e < nblocks; e += gsz)
+            {
+                int k1 = static_cast<int>((sqrtf(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
+                while (static_cast<size_t>(k1) * (k1 + 1) / 2 > e)
+                    --k1;
+                while (static_cast<size_t>(k1 + 1) * (k1 + 2) / 2 <= e)
+                    ++k1;
+                const int k2 = static_cast<int>(e - static_cast<size_t>(k1) * (k1 + 1) / 2);
+                const int r0 = pp[k1], r1 = pq[k1], c0 = pp[k2], c1 = pq[k2];
+                const bool hr1 = r1 < T, hc1 = c1 < T;
+                const Cx<R> z = {0, 0};
+                auto in = [&](int r, int c) -> const Cx<R>* { return A + static_cast<size_t>(r) * T + c; };
+                auto at = [&](int r, int c) -> Cx<R>& { return An[static_cast<size_t>(r) * T + c]; };
+                Cx<R> B[2][2];
+                B[0][0] = ldcg(in(r0, c0));
+                B[0][1] = hc1 ? ldcg(in(r0, c1)) : z;
+                B[1][0] = hr1 ? ldcg(in(r1, c0)) : z;
+                B[1][1] = (hr1 && hc1) ? ldcg(in(r1, c1)) : z;
+                if (!act[k1] && !act[k2])
+                {
+                    // unchanged block: copied to the step's output (with its mirror)
+                    at(r0, c0) = B[0][0];
+                    if (hc1)
+                        at(r0, c1) = B[0][1];
+                    if (hr1)
+                        at(r1, c0) = B[1][0];
+                    if (hr1 && hc1)
+                        at(r1, c1) = B[1][1];
+                    if (k1 != k2)
+                    {
+                        at(c0, r0) = {B[0][0].x, -B[0][0].y};
+                        if (hc1)
+                            at(c1, r0) = {B[0][1].x, -B[0][1].y};
+                        if (hr1)
+                            at(c0, r1) = {B[1][0].x, -B[1][0].y};
+                        if (hr1 && hc1)
+                            at(c1, r1) = {B[1][1].x, -B[1][1].y};
+                    }
+                    continue;
+                }
+                const R c2 = rc[k2], s2 = rs[k2];
+                const Cx<R> em2 = {rcp[k2], -rsp[k2]};
+                Cx<R> X[2][2];
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+                {
+                    const Cx<R> b1 = cxmul(B[r][1], em2);
+                    X[r][0] = {c2 * B[r][0].x - s2 * b1.x, c2 * B[r][0].y - s2 * b1.y};
+                    X[r][1] = {s2 * B[r][0].x + c2 * b1.x, s2 * B[r][0].y + c2 * b1.y};
+                }
+                const R c1r = rc[k1], s1r = rs[k1];
+                const Cx<R> ep1 = {rcp[k1], rsp[k1]};
+                Cx<R> Y[2][2];
+#pragma unroll
+                for (int cc = 0; cc < 2; ++cc)
+                {
+                    const Cx<R> x1 = cxmul(X[1][cc], ep1);
+                    Y[0][cc] = {c1r * X[0][cc].x - s1r * x1.x, c1r * X[0][cc].y - s1r * x1.y};
+                    Y[1][cc] = {s1r * X[0][cc].x + c1r * x1.x, s1r * X[0][cc].y + c1r * x1.y};
+                }
+                if (k1 == k2 && act[k1])
+                {
+                    Y[0][1] = z;
+                    Y[1][0] = z;
+                    Y[0][0].y = 0;
+                    Y[1][1].y = 0;
+                }
+                at(r0, c0) = Y[0][0];
+                if (hc1)
+                    at(r0, c1) = Y[0][1];
+                if (hr1)
+                    at(r1, c0) = Y[1][0];
+                if (hr1 && hc1)
+                    at(r1, c1) = Y[1][1];
+                if (k1 != k2)
+                {
+                    at(c0, r0) = {Y[0][0].x, -Y[0][0].y};
+                    if (hc1)
+                        at(c1, r0) = {Y[0][1].x, -Y[0][1].y};
+                    if (hr1)
+                        at(c0, r1) = {Y[1][0].x, -Y[1][0].y};
+                    if (hr1 && hc1)
+                        at(c1, r1) = {Y[1][1].x, -Y[1][1].y};
+                }
+            }
+            // V <- V J for the active pairs
+            for (size_t e = gtid; e < static_cast<size_t>(npairs) * T; e += gsz)
+            {
+                const int k = static_cast<int>(e / T), r = static_cast<int>(e % T);
+                if (!act[k])
+                    continue;
+                const int p = pp[k], q = pq[k];
+                if (q >= T)
+                    continue;
+                const R c = rc[k], s = rs[k];
+                const Cx<R> em = {rcp[k], -rsp[k]};
+                Cx<R>* row = V + static_cast<size_t>(r) * T;
+                const Cx<R> vp = ldcg(row + p), vq = cxmul(ldcg(row + q), em);
+                row[p] = {c * vp.x - s * vq.x, c * vp.y - s * vq.y};
+                row[q] = {s * vp.x + c * vq.x, s * vp.y + c * vq.y};
+            }
+            grid_barrier(bar);
+            Cx<float>* t = A;
+            A = An;
+            An = t;
+            if (*reinterpret_cast<volatile int*>(&bar->err))
+                break;
+        }
+        if (!sweep_active || *reinterpret_cast<volatile int*>(&bar->err))
+            break;
+    }
+    for (size_t e = gtid; e < TT; e += gsz)
+    {
+        const Cx<R> v = ldcg(V + e);
+        Vout[e] = make_double2(static_cast<double>(v.x), static_cast<double>(v.y));
+    }
+    for (size_t i = gtid; i < static_cast<size_t>(T); i += gsz)
+        evals[i] = static_cast<double>(ldcg(A + i * T + i).x);
+}
+
 // FP64 finish of each eigenpair from the FP64 covariance (intact in the shared-memory paths):
 // normalise the eigenvector column in FP64 and take its Rayleigh quotient v^H A v as the
 // eigenvalue, whose error is second order in the eigenvector error. One CTA per eigenpair.
 __global__ void k_eig_refine(const double2* __restrict__ A, double2* __restrict__ V, int T, double* __restrict__ evals)
 {
-    __shared__ double2 v[JS_MAX_T];
+    __shared__ double2 v[JC_MAX_T];
     __shared__ double red[4];
     const int i = blockIdx.x, tid = threadIdx.x;
     double n2 = 0.0;
@@ -860,8 +1131,11 @@ void set_eig_precision(int p) { g_eig_precision = p; }
 size_t pca_eigh_workspace(int T)
 {
     const int Tp = (T % 2) ? T + 1 : T;
-    return static_cast<size_t>(T) * T * sizeof(double2) + static_cast<size_t>(2 * Tp) * sizeof(double) +
-           static_cast<size_t>(T) * sizeof(double) + static_cast<size_t>(Tp) * sizeof(int) + 256;
+    size_t bytes = static_cast<size_t>(T) * T * sizeof(double2) + static_cast<size_t>(2 * Tp) * sizeof(double) +
+                   static_cast<size_t>(T) * sizeof(double) + static_cast<size_t>(Tp) * sizeof(int) + 256;
+    if (T > JS_MAX_T && T <= JC_MAX_T)
+        bytes += 3 * static_cast<size_t>(T) * T * sizeof(float2) + 256;  // FP32 A (x2) and V, grid barrier
+    return bytes;
 }
 
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
@@ -894,14 +1168,38 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
                                              static_cast<int>(smem)));
         k_jacobi_smem<double><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted);
     }
-    if (T <= JS_MAX_T)
+    else if (T <= JC_MAX_T && g_eig_precision == HV_EIG_FP32)
+    {
+        // FP32 sweeps over a cooperative grid (A and V copies in the workspace), then the FP64 finish
+        size_t off2 = (off + static_cast<size_t>(Tp) * sizeof(int) + 255) & ~static_cast<size_t>(255);
+        Cx<float>* A32 = reinterpret_cast<Cx<float>*>(base + off2);
+        off2 += static_cast<size_t>(T) * T * sizeof(float2);
+        Cx<float>* A32b = reinterpret_cast<Cx<float>*>(base + off2);
+        off2 += static_cast<size_t>(T) * T * sizeof(float2);
+        Cx<float>* V32 = reinterpret_cast<Cx<float>*>(base + off2);
+        off2 += static_cast<size_t>(T) * T * sizeof(float2);
+        GridBarrier* bar = reinterpret_cast<GridBarrier*>(base + off2);
+        HV_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), st));
+        int sms = 0;
+        HV_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+        const size_t npairs = static_cast<size_t>(Tp / 2);
+        const size_t items = npairs * (npairs + 1) / 2 + npairs * T;
+        int nb = static_cast<int>((items + 2 * JC_THREADS - 1) / (2 * JC_THREADS));
+        nb = nb < 1 ? 1 : (nb > sms ? sms : nb);
+        int Ti = T, Tpi = Tp;
+        const double2* cin = cov;
+        void* args[] = {&cin, &A32, &A32b, &V32, &Ti, &Tpi, &bar, &V, &ev_unsorted};
+        HV_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_jacobi_grid), nb, JC_THREADS, args, 0, st));
+        count_launch();
+    }
+    if (T <= JS_MAX_T || (T <= JC_MAX_T && g_eig_precision == HV_EIG_FP32))
     {
         HV_LAUNCH_CHECK();
         k_eig_refine<<<T, 128, 0, st>>>(cov, V, T, ev_unsorted);
         count_launch();
     }
     else
-        k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);
+        k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);  // FP64 sweeps
     HV_LAUNCH_CHECK();
     k_eig_sort<<<T, 128, 0, st>>>(ev_unsorted, V, T, evals, evecs, pmin, pmax, weights);
     HV_LAUNCH_CHECK();

@@ -323,7 +323,7 @@ hv_status hv_contrast_to_ushort(const float* frame, const float* range_f32, int 
  * whose steady streams are replayed from one CUDA graph per engine pass (one launch per bucket),
  * the others launched directly; buckets run on their own CUDA streams and overlap. Requirements
  * per stream: batch_size <= time_transformation_size. All calls are thread-safe; push and pull of
- * one stream from one thread each. */
+ * one stream from one thread each, and a stream is not closed while it is being pushed or pulled. */
 typedef struct hv_server hv_server;
 enum { HV_SERVER_NO_GRAPHS = 1 }; /* launch every cycle directly (for comparison) */
 typedef struct hv_server_stats
@@ -362,6 +362,10 @@ hv_status hv_server_get_float_frame(hv_server* server, int32_t stream_id, float*
 hv_status hv_server_sync(hv_server* server, int64_t timeout_us);
 hv_status hv_server_get_stats(hv_server* server, hv_server_stats* stats);
 hv_status hv_server_reset_stats(hv_server* server);
+/* Continuous batching: a bucket whose graph-replayed streams are only partly ready waits up to
+ * window_us (default 1500) after its oldest ready batch for the others, then launches the bucket
+ * graph (at least half ready) or the ready streams' own graphs. 0 launches immediately. */
+hv_status hv_server_set_batch_window(hv_server* server, int64_t window_us);
 
 #ifdef __cplusplus
 }
