@@ -9,13 +9,17 @@
 // BF16, and G ~= Yh Yh^T + Yh Yl^T + Yl Yh^T (the Yl Yl^T term is below FP32 resolution), so
 // three BF16 MMAs with FP32 accumulation per K step recover ~16-bit-mantissa accuracy.
 //
-// Kernel: one CTA per SM-slot walks a contiguous range of 64-pixel chunks. All warps load a chunk
-// (coalesced float2), split it and write Yh / Yl into shared memory in the no-swizzle K-major
-// canonical layout (8-row x 16-byte core matrices); one thread issues the MMAs
-// (M = 128 rows of Y, rows >= 2T are zero; N = 2T rounded to 16; K = 16) into a TMEM
-// accumulator; tcgen05.commit signals an mbarrier per buffer so loads of chunk c+2 wait only
-// for the MMAs of chunk c (two buffers). Every wait is bounded and reports through an error flag.
-// Per-CTA partial G tiles are summed in FP64 by k_cov_tc_reduce.
+// Kernel: one CTA per SM walks a contiguous range of 64-pixel chunks (K slices of Y):
+//   warp 9     loader: one 2-D tensor copy (TMA) per pair of chunks (T x 128 complex samples, rows
+//              of 1 KB) into a ring of R raw stages (zero fill past the frame)
+//   warps 0-7  converters: raw samples -> Yh / Yl tiles of an A stage (128-byte-swizzled K-major,
+//              rows >= 2T stay zero), each warp releasing its part of the raw and A stages
+//   warp 8     MMA issuer (M = 128 rows of Y, N = 2T rounded to 16, K = 16) into three TMEM
+//              accumulators (Yh Yh^T, Yh Yl^T, Yl Yh^T: independent chains, summed by the
+//              epilogue), tcgen05.commit frees the A stage; after the last chunk a commit to
+//              `done` releases the epilogue (warps 0-3 read the accumulator lanes 32w..32w+31)
+// Every wait is bounded in time and reports through the error flag. Per-CTA partial G tiles are
+// summed in FP64 by k_cov_tc_reduce.
 #include <cuda_bf16.h>
 
 #include "hv_common.cuh"
@@ -26,10 +30,13 @@ namespace hv {
 
 namespace {
 
-constexpr int TC_PRODUCERS = 256;            // 8 producer warps
-constexpr int TC_MMA_WARP = TC_PRODUCERS / 32;  // warp 8 issues the MMAs
-constexpr int TC_THREADS = TC_PRODUCERS + 32;
-constexpr int TC_STAGES = 3;
+constexpr int TC_CONVERTERS = 256;              // warps 0-7
+constexpr int TC_MMA_WARP = TC_CONVERTERS / 32;  // warp 8 issues the MMAs
+constexpr int TC_LOAD_WARP = TC_MMA_WARP + 1;    // warp 9 issues the tensor copies
+constexpr int TC_THREADS = TC_CONVERTERS + 64;
+constexpr int TC_A_STAGES = 2;
+constexpr int TC_A_STAGES_PACKED = 4;
+constexpr int TC_MAX_RAW = 8;
 constexpr int TC_KC = 64;           // pixels (K elements) per chunk
 constexpr int TC_ROWS = 128;        // M rows of the operand tile (2T <= 128, zero padded)
 constexpr int TILE_BYTES = TC_ROWS * TC_KC * 2;  // one BF16 tile: 16 KB
@@ -48,44 +55,55 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) { return tc::sw128_
 using tc::instr_desc;
 
 // part: [gridDim.x][2T][2T] FP32 partial G; err: set to 1 when a bounded wait gave up.
-// Warps 0-7 produce (load with one chunk of register prefetch, split to BF16 hi/lo, store the
-// canonical tiles of stage it % TC_STAGES, arrive on full[s]); warp 8 lane 0 consumes (wait
-// full[s], 12 MMAs, commit to empty[s]); after the last chunk a commit to `done` releases the
-// epilogue (warps 0-3 read the TMEM accumulator lanes 32w..32w+31).
-__global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict__ ring, int T, size_t npix,
-                                                       size_t chunks_per_cta, int N, uint32_t tmem_cols,
-                                                       float* __restrict__ part, int* __restrict__ err)
+__global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc(const __grid_constant__ CUtensorMap ring_map, int T,
+                                                          size_t npix, size_t chunks_per_cta, int N, uint32_t tmem_cols,
+                                                          int raw_stages, int packed, float* __restrict__ part,
+                                                          int* __restrict__ err)
 {
+    // packed (2T <= 64): one 128-row tile per stage, Yh in rows 0..63 and Yl in rows 64..127, and
+    // one 128 x 128 MMA per K step gives [[Yh Yh^T, Yh Yl^T], [Yl Yh^T, Yl Yl^T]];
+    // otherwise two tiles (Yh, Yl) and three MMAs into three accumulators
+    const int A_STAGES = packed ? TC_A_STAGES_PACKED : TC_A_STAGES;
+    const uint32_t a_stage_bytes = packed ? TILE_BYTES : 2 * TILE_BYTES;
     extern __shared__ __align__(1024) uint8_t smem[];
-    // [stage][hi/lo] tiles on a 1024-byte boundary (the swizzle atom); the launch adds 1 KB of slack
+    // A stages ([hi | lo] tiles) then the raw stages, on 1024-byte boundaries; 1 KB of launch slack
     uint8_t* tiles = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
-    __shared__ __align__(8) uint64_t full[TC_STAGES];
-    __shared__ __align__(8) uint64_t empty[TC_STAGES];
-    __shared__ __align__(8) uint64_t done;
+    const uint32_t raw_bytes = static_cast<uint32_t>(T) * TC_KC * 16;  // a pair of chunks: T rows of 1 KB
+    uint8_t* raw_base = tiles + A_STAGES * a_stage_bytes;
+    __shared__ __align__(8) uint64_t raw_full[TC_MAX_RAW], raw_empty[TC_MAX_RAW];
+    __shared__ __align__(8) uint64_t a_full[TC_A_STAGES_PACKED], a_empty[TC_A_STAGES_PACKED];
+    __shared__ __align__(8) uint64_t done, drain;
     __shared__ uint32_t tmem_base;
-    __shared__ int s_fail;
+    __shared__ int s_abort;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int rows = 2 * T;
+    const int rows = 2 * T, R = raw_stages;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
     const size_t c_begin = blockIdx.x * chunks_per_cta;
     size_t c_end = c_begin + chunks_per_cta;
     if (c_end > nchunks)
         c_end = nchunks;
-    const size_t nmine = c_end > c_begin ? c_end - c_begin : 0;
+    const int nmine = static_cast<int>(c_end > c_begin ? c_end - c_begin : 0);
+    volatile int* abort = &s_abort;
 
-    // zero all tiles once (rows >= 2T stay zero)
-    for (int i = tid; i < TC_STAGES * 2 * TILE_BYTES / 16; i += TC_THREADS)
+    // zero the A tiles once (rows >= 2T stay zero)
+    for (int i = tid; i < A_STAGES * static_cast<int>(a_stage_bytes) / 16; i += TC_THREADS)
         reinterpret_cast<uint4*>(tiles)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0)
     {
-        for (int s2 = 0; s2 < TC_STAGES; ++s2)
+        for (int i = 0; i < R; ++i)
         {
-            mbar_init(&full[s2], TC_PRODUCERS / 32);  // one arrival per producer warp
-            mbar_init(&empty[s2], 1);
+            mbar_init(&raw_full[i], 1);
+            mbar_init(&raw_empty[i], TC_CONVERTERS / 32);
+        }
+        for (int i = 0; i < A_STAGES; ++i)
+        {
+            mbar_init(&a_full[i], TC_CONVERTERS / 32);
+            mbar_init(&a_empty[i], 1);
         }
         mbar_init(&done, 1);
-        s_fail = 0;
+        mbar_init(&drain, 1);
+        s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == TC_MMA_WARP)
@@ -100,124 +118,140 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base;
-    bool fail = false;
 
-    if (warp < TC_MMA_WARP)
+    if (warp == TC_LOAD_WARP)
     {
-        // ------------------------------------------------------------------ producers
-        const int items = T * (TC_KC / 8);  // T rows x 8 k-groups of 8 pixels; <= 2 per thread (T <= 64)
-        float2 nxt[2][8];
-        auto load_chunk = [&](size_t c) {
-            const size_t p0 = c * TC_KC;
-#pragma unroll
-            for (int q = 0; q < 2; ++q)
-            {
-                const int w = tid + q * TC_PRODUCERS;
-                if (w >= items)
-                    continue;
-                const int g = w & 7, t = w >> 3;  // 8 threads read one frame's 512 contiguous bytes
-                const size_t p = p0 + static_cast<size_t>(g) * 8;
-                const float2* src = ring + static_cast<size_t>(t) * npix + p;
-                if (p + 8 <= npix)
-                {
-                    const float4* s4 = reinterpret_cast<const float4*>(src);
-#pragma unroll
-                    for (int h = 0; h < 4; ++h)
-                    {
-                        const float4 f = __ldcs(s4 + h);
-                        nxt[q][2 * h] = make_float2(f.x, f.y);
-                        nxt[q][2 * h + 1] = make_float2(f.z, f.w);
-                    }
-                }
-                else
-                {
-#pragma unroll
-                    for (int h = 0; h < 8; ++h)
-                        nxt[q][h] = (p + h < npix) ? __ldg(src + h) : make_float2(0.f, 0.f);
-                }
-            }
-        };
-        if (nmine)
-            load_chunk(c_begin);
-        for (size_t it = 0; it < nmine; ++it)
+        // ------------------------------------------------------------------ loader (TMA)
+        if (lane == 0)
         {
-            const int st = static_cast<int>(it % TC_STAGES);
-            const size_t use = it / TC_STAGES;
-            float2 cur[2][8];
-#pragma unroll
-            for (int q = 0; q < 2; ++q)
-#pragma unroll
-                for (int h = 0; h < 8; ++h)
-                    cur[q][h] = nxt[q][h];
-            if (it + 1 < nmine)
-                load_chunk(c_begin + it + 1);
-            if (use >= 1 && !mbar_wait(&empty[st], static_cast<uint32_t>((use - 1) & 1)))
-                fail = true;
-            uint8_t* th = tiles + st * 2 * TILE_BYTES;
-            uint8_t* tl = th + TILE_BYTES;
-#pragma unroll
-            for (int q = 0; q < 2; ++q)
+            asm volatile("prefetch.tensormap [%0];" ::"l"(&ring_map) : "memory");
+            const int npairs = (nmine + 1) / 2;
+            for (int m = 0; m < npairs; ++m)
             {
-                const int w = tid + q * TC_PRODUCERS;
-                if (w >= items)
-                    continue;
-                const int g = w & 7, t = w >> 3;
-                const float2* v = cur[q];
-                uint32_t rh[4], rl[4], ih[4], il[4];
-#pragma unroll
-                for (int h = 0; h < 4; ++h)
-                {
-                    tc::split2(v[2 * h].x, v[2 * h + 1].x, rh[h], rl[h]);
-                    tc::split2(v[2 * h].y, v[2 * h + 1].y, ih[h], il[h]);
-                }
-                const uint32_t ore = tile_offset(2 * t, g), oim = tile_offset(2 * t + 1, g);
-                *reinterpret_cast<uint4*>(th + ore) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
-                *reinterpret_cast<uint4*>(th + oim) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
-                *reinterpret_cast<uint4*>(tl + ore) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
-                *reinterpret_cast<uint4*>(tl + oim) = make_uint4(il[0], il[1], il[2], il[3]);
+                const int r = m % R;
+                if (m >= R)
+                    mbar_wait(&raw_empty[r], static_cast<uint32_t>(((m / R) - 1) & 1), abort);
+                tc::mbar_arrive_expect_tx(&raw_full[r], raw_bytes);
+                tc::tma_load_2d(raw_base + r * raw_bytes, &ring_map, static_cast<int>(2 * TC_KC * (c_begin + 2 * m)), 0,
+                                &raw_full[r]);
+            }
+        }
+        __syncwarp();
+    }
+    else if (warp < TC_MMA_WARP)
+    {
+        // ------------------------------------------------------------------ converters
+        // one raw row (frame t: 64 complex samples, 512 B) per warp iteration: lane l reads 16 B
+        // (pixels 2l, 2l+1), splits Re and Im into BF16 hi / lo pairs and writes 32-bit words
+        // j = l & 3 of chunk g = l >> 2 in rows 2t (Re) and 2t+1 (Im): conflict-free reads and writes
+        for (int it = 0; it < nmine; ++it)
+        {
+            const int m = it >> 1, half = it & 1;  // chunk it is half `half` of raw pair m
+            const int r = m % R, st = it % A_STAGES;
+            if (half == 0)
+                mbar_wait(&raw_full[r], static_cast<uint32_t>((m / R) & 1), abort);
+            if (it >= A_STAGES)
+                mbar_wait(&a_empty[st], static_cast<uint32_t>(((it / A_STAGES) - 1) & 1), abort);
+            const uint8_t* raw = raw_base + r * raw_bytes + half * (TC_KC * 8);
+            uint8_t* th = tiles + st * a_stage_bytes;
+            uint8_t* tl = packed ? th : th + TILE_BYTES;
+            const int lo_row = packed ? 64 : 0;  // Yl rows: 64.. of the same tile, or the lo tile
+            const int g = lane >> 2;
+            const uint32_t j4 = static_cast<uint32_t>(lane & 3) * 4u;
+            for (int t = warp; t < T; t += TC_CONVERTERS / 32)
+            {
+                const float4 f = reinterpret_cast<const float4*>(raw + t * (TC_KC * 16))[lane];
+                uint32_t reh, rel, imh, iml;
+                tc::split2(f.x, f.z, reh, rel);
+                tc::split2(f.y, f.w, imh, iml);
+                const uint32_t ore = tile_offset(2 * t, g) + j4, oim = tile_offset(2 * t + 1, g) + j4;
+                const uint32_t lre = tile_offset(lo_row + 2 * t, g) + j4, lim = tile_offset(lo_row + 2 * t + 1, g) + j4;
+                *reinterpret_cast<uint32_t*>(th + ore) = reh;
+                *reinterpret_cast<uint32_t*>(th + oim) = imh;
+                *reinterpret_cast<uint32_t*>(tl + lre) = rel;
+                *reinterpret_cast<uint32_t*>(tl + lim) = iml;
             }
             fence_async_smem();
             __syncwarp();
             if (lane == 0)
-                mbar_arrive(&full[st]);
+            {
+                if (half == 1 || it == nmine - 1)
+                    mbar_arrive(&raw_empty[r]);  // both halves of the pair converted
+                mbar_arrive(&a_full[st]);
+            }
         }
     }
     else if (lane == 0)
     {
         // ------------------------------------------------------------------ MMA issuer
-        const uint32_t idesc = instr_desc(TC_ROWS, N);
-        for (size_t it = 0; it < nmine; ++it)
+        const uint32_t idesc = instr_desc(TC_ROWS, packed ? TC_ROWS : N);
+        for (int it = 0; it < nmine; ++it)
         {
-            const int st = static_cast<int>(it % TC_STAGES);
-            if (!mbar_wait(&full[st], static_cast<uint32_t>((it / TC_STAGES) & 1)))
-                fail = true;
+            const int st = it % A_STAGES;
+            mbar_wait(&a_full[st], static_cast<uint32_t>((it / A_STAGES) & 1), abort);
             tc_fence_after();
-            const uint32_t ah = smem_u32(tiles + st * 2 * TILE_BYTES), al = ah + TILE_BYTES;
+            const uint32_t ah = smem_u32(tiles + st * a_stage_bytes), al = ah + TILE_BYTES;
+            if (packed)
+            {
+#pragma unroll
+                for (int s2 = 0; s2 < TC_KC / 16; ++s2)
+                {
+                    const uint64_t d = smem_desc(ah + s2 * 32);
+                    mma_bf16(tmem, d, d, idesc, (it > 0 || s2 > 0) ? 1u : 0u);  // [Yh; Yl] [Yh; Yl]^T
+                }
+                mma_commit(&a_empty[st]);
+                continue;
+            }
 #pragma unroll
             for (int s2 = 0; s2 < TC_KC / 16; ++s2)
             {
                 const uint64_t dh = smem_desc(ah + s2 * 32), dl = smem_desc(al + s2 * 32);
-                mma_bf16(tmem, dh, dh, idesc, (it > 0 || s2 > 0) ? 1u : 0u);  // Yh Yh^T
-                mma_bf16(tmem, dh, dl, idesc, 1u);                            // Yh Yl^T
-                mma_bf16(tmem, dl, dh, idesc, 1u);                            // Yl Yh^T
+                const uint32_t acc = (it > 0 || s2 > 0) ? 1u : 0u;
+                // three independent accumulator chains (consecutive MMAs do not wait on each other)
+                mma_bf16(tmem, dh, dh, idesc, acc);                                      // Yh Yh^T
+                mma_bf16(tmem + static_cast<uint32_t>(N), dh, dl, idesc, acc);           // Yh Yl^T
+                mma_bf16(tmem + static_cast<uint32_t>(2 * N), dl, dh, idesc, acc);       // Yl Yh^T
             }
-            mma_commit(&empty[st]);
+            mma_commit(&a_empty[st]);
         }
         mma_commit(&done);
     }
     // epilogue: wait for the last MMAs, warps 0-3 read row r = 32w + lane of G, columns 0..N-1
     if (warp < 4)
     {
-        if (!mbar_wait(&done, 0))
-            fail = true;
+        mbar_wait(&done, 0, abort);
         tc_fence_after();
         const int r = warp * 32 + lane;
-        float* dst = part + static_cast<size_t>(blockIdx.x) * rows * rows;
-        for (int c0 = 0; c0 < N; c0 += 16)
+        if (packed)
         {
-            float v[16];
+            // partial layout [128][64]: row i < 64 holds Yh Yh^T + Yh Yl^T, row 64 + i holds Yl Yh^T
+            float* dstp = part + static_cast<size_t>(blockIdx.x) * TC_ROWS * 64 + static_cast<size_t>(r) * 64;
+            for (int c0 = 0; c0 < 64; c0 += 16)
+            {
+                float v[16], w1[16];
+                const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
+                tmem_ld16(taddr, v);
+                tmem_ld16(taddr + 64u, w1);
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                {
+                    if (r < 64)
+                        v[i] += w1[i];
+                    dstp[c0 + i] = nmine ? v[i] : 0.f;
+                }
+            }
+        }
+        float* dst = part + static_cast<size_t>(blockIdx.x) * rows * rows;
+        for (int c0 = 0; c0 < (packed ? 0 : N); c0 += 16)
+        {
+            float v[16], w1[16], w2[16];
             const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
             tmem_ld16(taddr, v);
+            tmem_ld16(taddr + static_cast<uint32_t>(N), w1);
+            tmem_ld16(taddr + static_cast<uint32_t>(2 * N), w2);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                v[i] += w1[i] + w2[i];
             if (r < rows)
             {
 #pragma unroll
@@ -227,22 +261,42 @@ __global__ void __launch_bounds__(TC_THREADS) k_cov_tc(const float2* __restrict_
             }
         }
     }
-    if (fail)
-        atomicExch(&s_fail, 1);
     tc_fence_before();
     __syncthreads();
+    if (s_abort)
+    {
+        // a wait gave up: let the copies and MMAs already issued finish before shared and tensor
+        // memory are released (bounded waits)
+        if (warp == TC_LOAD_WARP && lane == 0)
+        {
+            const int npairs = (nmine + 1) / 2;
+            for (int m = npairs - R > 0 ? npairs - R : 0; m < npairs; ++m)
+                mbar_wait(&raw_full[m % R], static_cast<uint32_t>((m / R) & 1));
+            atomicExch(err, 1);
+        }
+        if (warp == TC_MMA_WARP && lane == 0)
+        {
+            mma_commit(&drain);
+            mbar_wait(&drain, 0);
+        }
+        __syncthreads();
+    }
     if (warp == TC_MMA_WARP)
     {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols) : "memory");
     }
-    if (tid == 0 && s_fail)
-        atomicExch(err, 1);
 }
 
 // cov[i][j] (complex128, row-major, both triangles, zeroed before) += a slice of the FP32
 // partial G tiles, summed in FP64.
-__global__ void k_cov_tc_reduce(const float* __restrict__ part, int T, int nparts, int per_slice,
+__device__ __forceinline__ float cov_g(const float* P, int R, int packed, int a, int b)
+{
+    // element (a, b) of G from one CTA's partial: packed [128][64] rows a and 64 + a, else [R][R]
+    return packed ? P[a * 64 + b] + P[(64 + a) * 64 + b] : P[a * R + b];
+}
+
+__global__ void k_cov_tc_reduce(const float* __restrict__ part, int T, int nparts, int per_slice, int packed,
                                 double2* __restrict__ cov)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -257,13 +311,14 @@ __global__ void k_cov_tc_reduce(const float* __restrict__ part, int T, int npart
     const int c0 = blockIdx.y * per_slice;
     const int c1 = min(nparts, c0 + per_slice);
 #pragma unroll 4
+    const size_t stride = packed ? static_cast<size_t>(TC_ROWS) * 64 : static_cast<size_t>(R) * R;
     for (int c = c0; c < c1; ++c)
     {
-        const float* G = part + static_cast<size_t>(c) * R * R;
-        g00 += G[(2 * i) * R + 2 * j];
-        g11 += G[(2 * i + 1) * R + 2 * j + 1];
-        g01 += G[(2 * i) * R + 2 * j + 1];
-        g10 += G[(2 * i + 1) * R + 2 * j];
+        const float* G = part + static_cast<size_t>(c) * stride;
+        g00 += cov_g(G, R, packed, 2 * i, 2 * j);
+        g11 += cov_g(G, R, packed, 2 * i + 1, 2 * j + 1);
+        g01 += cov_g(G, R, packed, 2 * i, 2 * j + 1);
+        g10 += cov_g(G, R, packed, 2 * i + 1, 2 * j);
     }
     atomicAdd(&cov[e].x, g00 + g11);
     if (i != j)
@@ -275,14 +330,29 @@ struct TcPlan
     int ctas;
     size_t chunks_per_cta;
     int N;
+    int packed;
     uint32_t cols;
 };
+
+int sm_count()
+{
+    static int sms = 0;
+    if (sms == 0)
+    {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+            v = 152;
+        sms = v;
+    }
+    return sms;
+}
 
 TcPlan tc_plan(int T, size_t npix)
 {
     TcPlan p;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    int ctas = 152 * 2;
+    int ctas = sm_count();  // one persistent CTA per SM
     if (static_cast<size_t>(ctas) > nchunks)
         ctas = static_cast<int>(nchunks);
     if (ctas < 1)
@@ -290,8 +360,9 @@ TcPlan tc_plan(int T, size_t npix)
     p.chunks_per_cta = (nchunks + ctas - 1) / ctas;
     p.ctas = static_cast<int>((nchunks + p.chunks_per_cta - 1) / p.chunks_per_cta);
     p.N = (2 * T + 15) / 16 * 16;
-    uint32_t cols = 32;
-    while (cols < static_cast<uint32_t>(p.N))
+    p.packed = 2 * T <= 64 ? 1 : 0;
+    uint32_t cols = 32;  // packed: one 128-column accumulator; else three accumulators of N columns
+    while (cols < static_cast<uint32_t>(p.packed ? TC_ROWS : 3 * p.N))
         cols <<= 1;
     p.cols = cols;
     return p;
@@ -304,7 +375,8 @@ bool cov_tc_supported(int T) { return T >= 1 && 2 * T <= TC_ROWS; }
 size_t cov_tc_workspace(int T, size_t npix)
 {
     const TcPlan p = tc_plan(T, npix);
-    return static_cast<size_t>(p.ctas) * 4 * T * T * sizeof(float) + 256;
+    const size_t per = p.packed ? static_cast<size_t>(TC_ROWS) * 64 : static_cast<size_t>(4) * T * T;
+    return static_cast<size_t>(p.ctas) * per * sizeof(float) + 256;
 }
 
 hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, cudaStream_t st)
@@ -316,15 +388,34 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
         set_last_error_msg("tensor-core covariance needs 16-byte aligned frames of a multiple of 8 pixels");
         return HV_ERR_UNSUPPORTED;
     }
+    if (npix > (1ull << 29))
+    {
+        set_last_error_msg("tensor-core covariance: at most 2^29 pixels per frame");
+        return HV_ERR_UNSUPPORTED;
+    }
     const TcPlan p = tc_plan(T, npix);
-    const size_t smem = static_cast<size_t>(TC_STAGES) * 2 * TILE_BYTES + 1024;
+    // raw stages: T x 64 complex samples (T x 512 B) each, as many as fit beside the two A stages
+    const size_t raw_bytes = static_cast<size_t>(T) * TC_KC * 16;  // pairs of 64-pixel chunks
+    const size_t a_bytes = p.packed ? static_cast<size_t>(TC_A_STAGES_PACKED) * TILE_BYTES
+                                    : static_cast<size_t>(TC_A_STAGES) * 2 * TILE_BYTES;
+    int raw = static_cast<int>((200 * 1024 - a_bytes) / raw_bytes);
+    raw = raw > TC_MAX_RAW ? TC_MAX_RAW : (raw < 2 ? 2 : raw);
+    const size_t smem = a_bytes + raw * raw_bytes + 1024;
+    CUtensorMap map;
+    if (!tc::encode_tmap_2d_f32(&map, ring, 2 * npix, static_cast<uint64_t>(T), npix * 8, 4 * TC_KC,
+                                static_cast<uint32_t>(T)))
+    {
+        set_last_error_msg("tensor-core covariance: cuTensorMapEncodeTiled failed");
+        return HV_ERR_CUDA;
+    }
     HV_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     float* part = static_cast<float*>(work);
-    k_cov_tc<<<p.ctas, TC_THREADS, smem, st>>>(ring, T, npix, p.chunks_per_cta, p.N, p.cols, part, err);
+    k_cov_tc<<<p.ctas, TC_THREADS, smem, st>>>(map, T, npix, p.chunks_per_cta, p.N, p.cols, raw, p.packed, part, err);
     HV_LAUNCH_CHECK();
     const int slices = p.ctas < 16 ? p.ctas : 16;
     const int per = (p.ctas + slices - 1) / slices;
-    k_cov_tc_reduce<<<dim3((T * T + 255) / 256, (p.ctas + per - 1) / per), 256, 0, st>>>(part, T, p.ctas, per, cov);
+    k_cov_tc_reduce<<<dim3((T * T + 255) / 256, (p.ctas + per - 1) / per), 256, 0, st>>>(part, T, p.ctas, per,
+                                                                                       p.packed, cov);
     HV_LAUNCH_CHECK();
     count_launch(2);
     return HV_OK;
