@@ -229,6 +229,19 @@ def _declare(L: C.CDLL) -> None:
         "hv_server_get_stats": (st, [vp, C.POINTER(ServerStats)]),
         "hv_server_reset_stats": (st, [vp]),
         "hv_server_set_batch_window": (st, [vp, i64]),
+        "hv_holo_open": (st, [C.c_char_p, C.POINTER(vp)]),
+        "hv_holo_close": (None, [vp]),
+        "hv_holo_get_header": (st, [vp, C.POINTER(HoloHeader), C.POINTER(FrameDescriptor)]),
+        "hv_holo_read_frames": (st, [vp, u64, u64, vp]),
+        "hv_holo_get_footer": (st, [vp, C.c_char_p, sz, C.POINTER(sz)]),
+        "hv_holo_get_settings": (st, [vp, C.POINTER(Settings)]),
+        "hv_holo_create": (st, [C.c_char_p, C.POINTER(FrameDescriptor), i32, C.POINTER(vp)]),
+        "hv_holo_write_frames": (st, [vp, vp, u64]),
+        "hv_holo_finish": (st, [vp, C.c_char_p]),
+        "hv_holo_make_footer": (st, [C.POINTER(Settings), i32, i32, C.c_char_p, sz, C.POINTER(sz)]),
+        "hv_holo_convert_footer": (st, [C.c_char_p, i32, C.c_char_p, sz, C.POINTER(sz)]),
+        "hv_settings_to_json": (st, [C.POINTER(Settings), C.c_char_p, sz, C.POINTER(sz)]),
+        "hv_settings_convert_json": (st, [C.c_char_p, C.c_char_p, sz, C.POINTER(sz)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -369,6 +382,99 @@ class Pipe:
 
 
 SERVER_NO_GRAPHS = 1
+HOLO_RAW, HOLO_PROCESSED, HOLO_MOMENTS = 0, 1, 2
+
+
+class HoloHeader(C.Structure):
+    _fields_ = [("magic", C.c_char * 4), ("version", C.c_uint16), ("bits_per_pixel", C.c_uint16),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("img_nb", C.c_uint32),
+                ("total_data_size", C.c_uint64), ("endianness", C.c_uint8), ("data_type", C.c_uint8)]
+
+
+def _string_call(name: str, *args) -> str:
+    """Calls an entry point that returns a string into a caller buffer (query, then fill)."""
+    n = C.c_size_t(0)
+    check(getattr(lib(), name)(*args, None, 0, C.byref(n)), name)
+    buf = C.create_string_buffer(n.value + 1)
+    check(getattr(lib(), name)(*args, buf, n.value + 1, C.byref(n)), name)
+    return buf.value.decode()
+
+
+class HoloFile:
+    """A .holo recording (Backend/includes/io/holo_file.hh), footer converted to the current version."""
+
+    def __init__(self, path: str):
+        h = C.c_void_p()
+        check(lib().hv_holo_open(str(path).encode(), C.byref(h)), "hv_holo_open")
+        self._h = h
+        self.header = HoloHeader()
+        self.fd = FrameDescriptor()
+        check(lib().hv_holo_get_header(self._h, C.byref(self.header), C.byref(self.fd)), "hv_holo_get_header")
+
+    @property
+    def nb_frames(self) -> int:
+        return int(self.header.img_nb)
+
+    def read(self, first: int = 0, n: int | None = None) -> np.ndarray:
+        n = self.nb_frames - first if n is None else n
+        dt = {1: np.uint8, 2: np.uint16, 4: np.float32}.get(self.fd.depth, np.uint8)
+        out = np.empty((n, self.fd.height, self.fd.width * self.fd.depth // np.dtype(dt).itemsize), dtype=dt)
+        check(lib().hv_holo_read_frames(self._h, first, n, out.ctypes.data), "hv_holo_read_frames")
+        return out
+
+    def footer(self) -> dict:
+        import json as _json
+        return _json.loads(_string_call("hv_holo_get_footer", self._h))
+
+    def settings(self, base: "Settings | None" = None) -> "Settings":
+        s = (base or Settings.defaults()).copy()
+        check(lib().hv_holo_get_settings(self._h, C.byref(s)), "hv_holo_get_settings")
+        return s
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().hv_holo_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def write_holo(path: str, fd: FrameDescriptor, frames, settings: "Settings | None" = None, input_fps: int = 0,
+               camera_fps: int = 0, data_type: int = HOLO_RAW, footer: str | None = None) -> None:
+    """Writes frames (numpy, n x H x W of fd.depth bytes per pixel) with the reference's footer."""
+    w = C.c_void_p()
+    check(lib().hv_holo_create(str(path).encode(), C.byref(fd), data_type, C.byref(w)), "hv_holo_create")
+    arr = np.ascontiguousarray(frames)
+    n = arr.nbytes // fd.frame_size
+    st = lib().hv_holo_write_frames(w, arr.ctypes.data, n)
+    if footer is None and settings is not None:
+        footer = _string_call("hv_holo_make_footer", C.byref(settings), input_fps, camera_fps)
+    st2 = lib().hv_holo_finish(w, footer.encode() if footer else None)
+    check(st, "hv_holo_write_frames")
+    check(st2, "hv_holo_finish")
+
+
+def convert_holo_footer(footer_json: str, version: int) -> str:
+    return _string_call("hv_holo_convert_footer", footer_json.encode(), version)
+
+
+def settings_to_json(settings: "Settings") -> str:
+    return _string_call("hv_settings_to_json", C.byref(settings))
+
+
+def convert_settings_json(text: str) -> str:
+    return _string_call("hv_settings_convert_json", text.encode())
+
 
 
 class ServerStats(C.Structure):

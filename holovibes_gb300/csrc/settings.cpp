@@ -19,267 +19,10 @@
 #include <vector>
 
 #include "hv_internal.h"
+#include "json_lite.h"
+#include "settings_internal.h"
 
 namespace hv {
-namespace json {
-
-struct Value
-{
-    enum Kind { Null, Bool, Number, String, Array, Object } kind = Null;
-    bool b = false;
-    double num = 0.0;
-    std::string str;
-    std::vector<Value> arr;
-    std::vector<std::pair<std::string, Value>> obj;  // insertion order
-
-    const Value* find(const std::string& k) const
-    {
-        for (const auto& kv : obj)
-            if (kv.first == k)
-                return &kv.second;
-        return nullptr;
-    }
-    Value* find(const std::string& k)
-    {
-        for (auto& kv : obj)
-            if (kv.first == k)
-                return &kv.second;
-        return nullptr;
-    }
-};
-
-struct Parser
-{
-    const char* p;
-    const char* end;
-    std::string err;
-
-    void ws()
-    {
-        while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r'))
-            ++p;
-    }
-    bool fail(const char* m)
-    {
-        if (err.empty())
-            err = m;
-        return false;
-    }
-    bool lit(const char* s)
-    {
-        const size_t n = std::strlen(s);
-        if (static_cast<size_t>(end - p) < n || std::strncmp(p, s, n) != 0)
-            return false;
-        p += n;
-        return true;
-    }
-    bool string(std::string& out)
-    {
-        if (p >= end || *p != '"')
-            return fail("expected string");
-        ++p;
-        while (p < end && *p != '"')
-        {
-            char c = *p++;
-            if (c == '\\')
-            {
-                if (p >= end)
-                    return fail("bad escape");
-                const char e = *p++;
-                switch (e)
-                {
-                case '"': out += '"'; break;
-                case '\\': out += '\\'; break;
-                case '/': out += '/'; break;
-                case 'b': out += '\b'; break;
-                case 'f': out += '\f'; break;
-                case 'n': out += '\n'; break;
-                case 'r': out += '\r'; break;
-                case 't': out += '\t'; break;
-                case 'u':
-                {
-                    if (end - p < 4)
-                        return fail("bad unicode escape");
-                    unsigned int cp = 0;
-                    for (int i = 0; i < 4; ++i)
-                    {
-                        const char h = p[i];
-                        cp <<= 4;
-                        if (h >= '0' && h <= '9')
-                            cp |= static_cast<unsigned int>(h - '0');
-                        else if (h >= 'a' && h <= 'f')
-                            cp |= static_cast<unsigned int>(h - 'a' + 10);
-                        else if (h >= 'A' && h <= 'F')
-                            cp |= static_cast<unsigned int>(h - 'A' + 10);
-                        else
-                            return fail("bad unicode escape");
-                    }
-                    p += 4;
-                    if (cp < 0x80)
-                        out += static_cast<char>(cp);
-                    else if (cp < 0x800)
-                    {
-                        out += static_cast<char>(0xC0 | (cp >> 6));
-                        out += static_cast<char>(0x80 | (cp & 0x3F));
-                    }
-                    else
-                    {
-                        out += static_cast<char>(0xE0 | (cp >> 12));
-                        out += static_cast<char>(0x80 | ((cp >> 6) & 0x3F));
-                        out += static_cast<char>(0x80 | (cp & 0x3F));
-                    }
-                    break;
-                }
-                default: return fail("bad escape");
-                }
-            }
-            else
-                out += c;
-        }
-        if (p >= end)
-            return fail("unterminated string");
-        ++p;
-        return true;
-    }
-    bool value(Value& v, int depth)
-    {
-        if (depth > 64)
-            return fail("nesting too deep");
-        ws();
-        if (p >= end)
-            return fail("unexpected end");
-        const char c = *p;
-        if (c == '{')
-        {
-            ++p;
-            v.kind = Value::Object;
-            ws();
-            if (p < end && *p == '}')
-            {
-                ++p;
-                return true;
-            }
-            for (;;)
-            {
-                ws();
-                std::string k;
-                if (!string(k))
-                    return false;
-                ws();
-                if (p >= end || *p != ':')
-                    return fail("expected ':'");
-                ++p;
-                Value child;
-                if (!value(child, depth + 1))
-                    return false;
-                Value* existing = v.find(k);
-                if (existing)
-                    *existing = std::move(child);
-                else
-                    v.obj.emplace_back(std::move(k), std::move(child));
-                ws();
-                if (p < end && *p == ',')
-                {
-                    ++p;
-                    continue;
-                }
-                if (p < end && *p == '}')
-                {
-                    ++p;
-                    return true;
-                }
-                return fail("expected ',' or '}'");
-            }
-        }
-        if (c == '[')
-        {
-            ++p;
-            v.kind = Value::Array;
-            ws();
-            if (p < end && *p == ']')
-            {
-                ++p;
-                return true;
-            }
-            for (;;)
-            {
-                Value child;
-                if (!value(child, depth + 1))
-                    return false;
-                v.arr.push_back(std::move(child));
-                ws();
-                if (p < end && *p == ',')
-                {
-                    ++p;
-                    continue;
-                }
-                if (p < end && *p == ']')
-                {
-                    ++p;
-                    return true;
-                }
-                return fail("expected ',' or ']'");
-            }
-        }
-        if (c == '"')
-        {
-            v.kind = Value::String;
-            return string(v.str);
-        }
-        if (lit("true"))
-        {
-            v.kind = Value::Bool;
-            v.b = true;
-            return true;
-        }
-        if (lit("false"))
-        {
-            v.kind = Value::Bool;
-            v.b = false;
-            return true;
-        }
-        if (lit("null"))
-        {
-            v.kind = Value::Null;
-            return true;
-        }
-        // number
-        const char* s = p;
-        if (p < end && (*p == '-' || *p == '+'))
-            ++p;
-        while (p < end && (std::isdigit(static_cast<unsigned char>(*p)) || *p == '.' || *p == 'e' || *p == 'E' ||
-                           *p == '-' || *p == '+'))
-            ++p;
-        if (p == s)
-            return fail("unexpected character");
-        std::string num(s, p);
-        char* e = nullptr;
-        v.kind = Value::Number;
-        v.num = std::strtod(num.c_str(), &e);
-        if (!e || *e != '\0')
-            return fail("bad number");
-        return true;
-    }
-};
-
-static bool parse(const char* text, Value& out, std::string& err)
-{
-    Parser ps{text, text + std::strlen(text), {}};
-    if (!ps.value(out, 0))
-    {
-        err = ps.err;
-        return false;
-    }
-    ps.ws();
-    if (ps.p != ps.end)
-    {
-        err = "trailing characters";
-        return false;
-    }
-    return true;
-}
-
-}  // namespace json
 
 // Default ComputeSettings document: the key layout of the reference's ComputeSettings
 // serialisation (version V1) with the reference's default values.
@@ -330,20 +73,32 @@ static const char* kDefaultComputeSettings = R"JSON({
  }
 })JSON";
 
-static bool merge(json::Value& base, const json::Value& upd, std::string& err, const std::string& path)
+// lenient: keys absent from the default document are skipped instead of refused (.holo footers
+// written by other versions carry settings this build does not use)
+static bool merge(json::Value& base, const json::Value& upd, std::string& err, const std::string& path,
+                  bool lenient = false)
 {
     for (const auto& kv : upd.obj)
     {
         json::Value* b = base.find(kv.first);
         if (!b)
         {
+            if (lenient)
+                continue;
             err = "key '" + path + kv.first + "' is not a compute setting";
             return false;
         }
         if (b->kind == json::Value::Object && kv.second.kind == json::Value::Object)
         {
-            if (!merge(*b, kv.second, err, path + kv.first + "."))
+            if (!merge(*b, kv.second, err, path + kv.first + ".", lenient))
                 return false;
+        }
+        else if (b->kind == json::Value::Object || kv.second.kind == json::Value::Object)
+        {
+            if (lenient)
+                continue;
+            err = "key '" + path + kv.first + "' has the wrong type";
+            return false;
         }
         else
             *b = kv.second;
@@ -461,13 +216,20 @@ hv_status settings_from_json(const char* text, hv_settings* s)
 {
     if (!text || !s)
         return HV_INVALID_VALUE;
-    json::Value doc, base;
+    json::Value doc;
     std::string err;
     if (!json::parse(text, doc, err))
     {
         set_last_error_msg(("invalid json: " + err).c_str());
         return HV_FAILURE;
     }
+    return settings_from_value(doc, s, false);
+}
+
+hv_status settings_from_value(const json::Value& doc, hv_settings* s, bool lenient)
+{
+    json::Value base;
+    std::string err;
     if (doc.kind != json::Value::Object || doc.obj.empty())
     {
         set_last_error_msg("empty compute settings");
@@ -475,7 +237,7 @@ hv_status settings_from_json(const char* text, hv_settings* s)
     }
     json::parse(kDefaultComputeSettings, base, err);
     // seed the base with the caller's current settings so a partial document keeps them
-    if (!merge(base, doc, err, ""))
+    if (!merge(base, doc, err, "", lenient))
     {
         set_last_error_msg(err.c_str());
         return HV_FAILURE;
@@ -571,6 +333,136 @@ hv_status settings_from_json(const char* text, hv_settings* s)
     }
     *s = out;
     return HV_OK;
+}
+
+
+// ------------------------------------------------------------------------------ serialisation
+static json::Value* ensure(json::Value& root, std::initializer_list<const char*> path)
+{
+    json::Value* v = &root;
+    for (const char* k : path)
+    {
+        if (v->kind != json::Value::Object)
+        {
+            *v = json::Value{};
+            v->kind = json::Value::Object;
+        }
+        json::Value* c = v->find(k);
+        if (!c)
+        {
+            v->obj.emplace_back(k, json::Value{});
+            c = &v->obj.back().second;
+        }
+        v = c;
+    }
+    return v;
+}
+
+static void set_num(json::Value& root, std::initializer_list<const char*> path, double x)
+{
+    json::Value* v = ensure(root, path);
+    *v = json::Value{};
+    v->kind = json::Value::Number;
+    v->num = x;
+}
+
+static void set_bool(json::Value& root, std::initializer_list<const char*> path, bool b)
+{
+    json::Value* v = ensure(root, path);
+    *v = json::Value{};
+    v->kind = json::Value::Bool;
+    v->b = b;
+}
+
+static void set_str(json::Value& root, std::initializer_list<const char*> path, const char* x)
+{
+    json::Value* v = ensure(root, path);
+    *v = json::Value{};
+    v->kind = json::Value::String;
+    v->str = x;
+}
+
+// The compute-settings document (current layout, version v1) of a settings record: the default
+// document with every field this build reads set from `s` (ComputeSettingsApi::
+// compute_settings_to_json, compute_settings.cc:38-99, for the keys of this path).
+void settings_to_value(const hv_settings* s, json::Value& doc)
+{
+    std::string err;
+    doc = json::Value{};
+    json::parse(kDefaultComputeSettings, doc, err);
+    static const char* space[] = {"NONE", "FRESNELTR", "ANGULARSP"};
+    static const char* time[] = {"NONE", "STFT", "PCA", "SSA_STFT"};
+    static const char* img[] = {"MODULUS", "SQUARED_MODULUS", "ARGUMENT"};
+    set_str(doc, {"image_rendering", "image_mode"}, "HOLOGRAM");
+    set_str(doc, {"image_rendering", "space_transformation"},
+            space[s->space_transformation >= 0 && s->space_transformation <= 2 ? s->space_transformation : 0]);
+    set_str(doc, {"image_rendering", "time_transformation"},
+            time[s->time_transformation >= 0 && s->time_transformation <= 3 ? s->time_transformation : 0]);
+    set_num(doc, {"image_rendering", "time_transformation_size"}, s->time_transformation_size);
+    set_num(doc, {"image_rendering", "time_transformation_stride"}, s->time_stride);
+    set_num(doc, {"image_rendering", "batch_size"}, s->batch_size);
+    set_num(doc, {"image_rendering", "lambda"}, s->lambda);
+    set_num(doc, {"image_rendering", "propagation_distance"}, s->z_distance);
+    set_str(doc, {"view", "image_type"}, img[s->image_type >= 0 && s->image_type <= 2 ? s->image_type : 0]);
+    set_bool(doc, {"view", "fft_shift"}, s->fft_shift != 0);
+    set_bool(doc, {"view", "renorm"}, s->renorm != 0);
+    set_num(doc, {"view", "z", "start"}, s->p_start);
+    set_num(doc, {"view", "z", "width"}, s->p_width);
+    set_num(doc, {"view", "window", "xy", "output_image_accumulation"}, s->accumulation);
+    set_bool(doc, {"view", "window", "xy", "log_enabled"}, s->log_enabled != 0);
+    set_bool(doc, {"view", "window", "xy", "contrast", "enabled"}, s->contrast_enabled != 0);
+    set_bool(doc, {"view", "window", "xy", "contrast", "auto_refresh"}, s->contrast_auto_refresh != 0);
+    set_bool(doc, {"view", "window", "xy", "contrast", "invert"}, s->contrast_invert != 0);
+    set_num(doc, {"view", "window", "xy", "contrast", "min"}, s->contrast_min);
+    set_num(doc, {"view", "window", "xy", "contrast", "max"}, s->contrast_max);
+    set_bool(doc, {"view", "reticle", "display_enabled"}, s->reticle_display != 0);
+    set_num(doc, {"view", "reticle", "scale"}, s->reticle_scale);
+    set_num(doc, {"advanced", "contrast", "lower"}, s->contrast_lower);
+    set_num(doc, {"advanced", "contrast", "upper"}, s->contrast_upper);
+    set_num(doc, {"advanced", "renorm_constant"}, s->renorm_constant);
+    set_num(doc, {"advanced", "buffer_size", "output"}, s->output_buffer_size);
+    set_num(doc, {"advanced", "buffer_size", "input"}, s->input_buffer_size);
+}
+
+// Compute-settings documents without a "version" key are version v0: v1 dropped three keys and
+// added the version tag and the registration block (ComputeSettingsConverter,
+// compute_settings_converter.cc:8-100 with its patch table assets/json_patches_settings). Returns
+// false for an unknown version.
+bool settings_convert_to_current(json::Value& doc)
+{
+    if (doc.kind != json::Value::Object)
+        return false;
+    const json::Value* ver = doc.find("version");
+    if (ver)
+        return ver->kind == json::Value::String && ver->str == "v1";
+    auto drop = [&](std::initializer_list<const char*> path) {
+        json::Value* v = &doc;
+        const char* last = nullptr;
+        json::Value* parent = nullptr;
+        for (const char* k : path)
+        {
+            if (!v || v->kind != json::Value::Object)
+                return;
+            parent = v;
+            last = k;
+            v = v->find(k);
+        }
+        if (!v || !parent)
+            return;
+        for (size_t i = 0; i < parent->obj.size(); ++i)
+            if (parent->obj[i].first == last)
+            {
+                parent->obj.erase(parent->obj.begin() + static_cast<std::ptrdiff_t>(i));
+                return;
+            }
+    };
+    drop({"image_rendering", "input_filter", "enabled"});
+    drop({"image_rendering", "convolution", "enabled"});
+    drop({"advanced", "record_mode"});
+    set_str(doc, {"version"}, "v1");
+    set_bool(doc, {"view", "registration", "registration_enabled"}, false);
+    set_num(doc, {"view", "registration", "registration_zone"}, 0.7);
+    return true;
 }
 
 hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd)

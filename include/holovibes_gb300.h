@@ -367,6 +367,52 @@ hv_status hv_server_reset_stats(hv_server* server);
  * graph (at least half ready) or the ready streams' own graphs. 0 launches immediately. */
 hv_status hv_server_set_batch_window(hv_server* server, int64_t window_us);
 
+/* ================================================================================ .holo files
+ * The reference's recording format (Backend/includes/io/holo_file.hh:1-81): a 64-byte header,
+ * the raw frames, a JSON footer {"compute_settings": {...}, "info": {...}}. Reading replaces
+ * InputHoloFile (input_holo_file.cc:18-157) and converts footers of versions 2..6 and compute
+ * settings of version v0 to the current layout like HoloFileConverter / ComputeSettingsConverter
+ * (holo_file_converter.cc, compute_settings_converter.cc), for the keys of this path; writing
+ * replaces OutputHoloFile (output_holo_file.cc:10-131). Host-only: no GPU is used. Strings are
+ * returned into caller buffers: *len receives the length; a call with buf = NULL, cap = 0 only
+ * queries it. */
+enum { HV_HOLO_RAW = 0, HV_HOLO_PROCESSED = 1, HV_HOLO_MOMENTS = 2 }; /* header data_type */
+typedef struct hv_holo_header
+{
+    char magic[4];            /* "HOLO" */
+    uint16_t version;         /* 7 when written here */
+    uint16_t bits_per_pixel;  /* 8 * bytes per pixel */
+    uint32_t width, height, img_nb;
+    uint64_t total_data_size; /* width * height * img_nb * bytes per pixel */
+    uint8_t endianness;       /* 1: big endian frames */
+    uint8_t data_type;        /* HV_HOLO_*, 0 for files older than version 7 */
+} hv_holo_header;
+typedef struct hv_holo_file hv_holo_file;
+hv_status hv_holo_open(const char* path, hv_holo_file** file);
+void hv_holo_close(hv_holo_file* file);
+hv_status hv_holo_get_header(const hv_holo_file* file, hv_holo_header* header, hv_frame_desc* fd);
+/* n frames from frame `first` into host memory (n * frame bytes). */
+hv_status hv_holo_read_frames(hv_holo_file* file, uint64_t first, uint64_t n, void* dst);
+/* The footer converted to the current version (an empty object when the file has none). */
+hv_status hv_holo_get_footer(const hv_holo_file* file, char* buf, size_t cap, size_t* len);
+/* The footer's compute settings applied over *settings (keys this build does not use are skipped)
+ * and the pixel size from info.pixel_pitch.x; HV_NO_IN_DATA when the file has no footer. */
+hv_status hv_holo_get_settings(const hv_holo_file* file, hv_settings* settings);
+typedef struct hv_holo_writer hv_holo_writer;
+hv_status hv_holo_create(const char* path, const hv_frame_desc* fd, int data_type, hv_holo_writer** writer);
+hv_status hv_holo_write_frames(hv_holo_writer* writer, const void* frames, uint64_t n);
+/* Appends the footer (may be NULL), writes the final image count into the header, closes and frees. */
+hv_status hv_holo_finish(hv_holo_writer* writer, const char* footer_json);
+/* The footer the reference writes for these settings (OutputHoloFile::export_compute_settings). */
+hv_status hv_holo_make_footer(const hv_settings* settings, int input_fps, int camera_fps, char* buf, size_t cap,
+                              size_t* len);
+/* A footer of `version` converted to the current version. */
+hv_status hv_holo_convert_footer(const char* footer_json, int version, char* buf, size_t cap, size_t* len);
+/* The compute-settings document (current layout, v1) of a settings record, and the conversion of
+ * a compute-settings document to the current version. */
+hv_status hv_settings_to_json(const hv_settings* settings, char* buf, size_t cap, size_t* len);
+hv_status hv_settings_convert_json(const char* json, char* buf, size_t cap, size_t* len);
+
 #ifdef __cplusplus
 }
 #endif
