@@ -382,6 +382,7 @@ class Pipe:
 
 
 SERVER_NO_GRAPHS = 1
+SERVER_STREAM_GRAPHS = 2
 HOLO_RAW, HOLO_PROCESSED, HOLO_MOMENTS = 0, 1, 2
 
 

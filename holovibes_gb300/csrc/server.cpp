@@ -58,7 +58,54 @@ struct Member
     bool steady = false;  // ring full and one render done eagerly: eligible for the bucket graph
     cudaGraphExec_t solo = nullptr;  // this stream's cycle alone (launched when few streams are ready)
     size_t solo_kernels = 0;
+    // per-stream launches (HV_SERVER_STREAM_GRAPHS): the stream's own CUDA stream and control block
+    cudaStream_t own = nullptr;
+    CycleCtl* ctl_dev = nullptr;
+    CycleCtl* ctl_host = nullptr;  // pinned ring of kCtlRing blocks
+    cudaEvent_t ctl_ev[kCtlRing] = {};
+    int ctl_i = 0;
 };
+
+void destroy_member_stream(Member* m)
+{
+    if (m->own)
+        cudaStreamSynchronize(m->own);
+    for (cudaEvent_t& e : m->ctl_ev)
+        if (e)
+        {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    if (m->ctl_dev)
+        cudaFree(m->ctl_dev);
+    if (m->ctl_host)
+        cudaFreeHost(m->ctl_host);
+    if (m->own)
+        cudaStreamDestroy(m->own);
+    m->own = nullptr;
+    m->ctl_dev = nullptr;
+    m->ctl_host = nullptr;
+}
+
+hv_status make_member_stream(Member* m)
+{
+    cudaError_t e = cudaStreamCreateWithFlags(&m->own, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&m->ctl_dev, sizeof(CycleCtl));
+    if (e == cudaSuccess)
+        e = cudaMemset(m->ctl_dev, 0, sizeof(CycleCtl));
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&m->ctl_host, kCtlRing * sizeof(CycleCtl));
+    for (int i = 0; i < kCtlRing && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&m->ctl_ev[i], cudaEventDisableTiming);
+    if (e != cudaSuccess)
+    {
+        set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+        destroy_member_stream(m);
+        return e == cudaErrorMemoryAllocation ? HV_ERR_OOM : HV_ERR_CUDA;
+    }
+    return HV_OK;
+}
 
 struct Bucket
 {
@@ -202,7 +249,7 @@ hv_status make_bucket(const std::string& key, bool graphable, Bucket** out)
 
 // Captures the cycles of `ms` (members of `b`) as parallel branches of one graph.
 hv_status capture_members(hv_server* s, Bucket* b, const std::vector<Member*>& ms, cudaGraphExec_t* exec,
-                          size_t* kernels_out)
+                          size_t* kernels_out, bool own_blocks = false)
 {
     *exec = nullptr;
     *kernels_out = 0;
@@ -213,9 +260,10 @@ hv_status capture_members(hv_server* s, Bucket* b, const std::vector<Member*>& m
     {
         Member* m = ms[k];
         const size_t idx = std::find(b->members.begin(), b->members.end(), m) - b->members.begin();
+        const CycleCtl* ctl = own_blocks ? m->ctl_dev : b->ctl_dev + idx;
         e = cudaStreamWaitEvent(s->branch[k], s->fork_ev, 0);
         if (e == cudaSuccess)
-            r = served_record(m->p, b->ctl_dev + idx, ServedCycle{}, true, s->branch[k]);
+            r = served_record(m->p, ctl, ServedCycle{}, true, s->branch[k]);
         if (e == cudaSuccess && r == HV_OK)
             e = cudaEventRecord(s->join_ev[k], s->branch[k]);
         if (e == cudaSuccess)
@@ -424,6 +472,59 @@ hv_status run_bucket(hv_server* s, Bucket* b, bool* did_work, int64_t* wait_us)
     return HV_OK;
 }
 
+// HV_SERVER_STREAM_GRAPHS: every stream runs on its own CUDA stream like independent Pipes (no
+// barrier between the streams' cycles); per ready batch: the stream's control block is uploaded
+// on its stream, then its own graph (steady) or its kernels (warm-up, PCA, unwrap) are launched.
+hv_status run_bucket_streams(hv_server* s, Bucket* b, bool* did_work)
+{
+    hv_status r;
+    for (Member* m : b->members)
+    {
+        CycleCtl* host = m->ctl_host + m->ctl_i;
+        HV_CUDA_TRY(cudaEventSynchronize(m->ctl_ev[m->ctl_i]));
+        ServedCycle cyc;
+        if (!served_plan(m->p, host, &cyc))
+            continue;
+        *did_work = true;
+        cudaStream_t st = m->own;
+        HV_CUDA_TRY(cudaMemcpyAsync(m->ctl_dev, host, sizeof(CycleCtl), cudaMemcpyHostToDevice, st));
+        HV_CUDA_TRY(cudaEventRecord(m->ctl_ev[m->ctl_i], st));
+        m->ctl_i = (m->ctl_i + 1) % kCtlRing;
+        if ((r = served_prepare(m->p, cyc, st)) != HV_OK)
+            return r;
+        const bool graph = b->graphable && !(s->flags & HV_SERVER_NO_GRAPHS);
+        if (graph && m->steady && !m->solo && (r = capture_members(s, b, {m}, &m->solo, &m->solo_kernels, true)) != HV_OK)
+            return r;
+        if (graph && m->steady && m->solo)
+        {
+            HV_CUDA_TRY(cudaGraphLaunch(m->solo, st));
+            ++s->graph_launches;
+            s->graph_kernels += m->solo_kernels;
+        }
+        else
+        {
+            if ((r = served_record(m->p, m->ctl_dev, cyc, false, st)) != HV_OK)
+                return r;
+            if (cyc.active)
+                ++s->eager_cycles;
+            if (cyc.render)
+                m->steady = true;
+        }
+        if ((r = served_complete(m->p, cyc, st)) != HV_OK)
+            return r;
+        ++s->batches;
+        if (cyc.render)
+        {
+            auto rec = std::make_unique<LatencyRecord>();
+            rec->s = s;
+            rec->t_push.push_back(cyc.t_push_us);
+            HV_CUDA_TRY(cudaLaunchHostFunc(st, record_latencies, rec.get()));
+            rec.release();
+        }
+    }
+    return HV_OK;
+}
+
 void engine_main(hv_server* s)
 {
     uint64_t seen = 0;
@@ -446,7 +547,8 @@ void engine_main(hv_server* s)
                 std::lock_guard<std::mutex> g(s->mu);
                 for (Bucket* b : s->buckets)
                 {
-                    const hv_status r = run_bucket(s, b, &did, &wait_us);
+                    const hv_status r = (s->flags & HV_SERVER_STREAM_GRAPHS) ? run_bucket_streams(s, b, &did)
+                                                                             : run_bucket(s, b, &did, &wait_us);
                     if (r != HV_OK && s->engine_error == HV_OK)
                     {
                         s->engine_error = r;
@@ -543,6 +645,7 @@ void hv_server_destroy(hv_server* s)
         if (kv.second->solo)
             cudaGraphExecDestroy(kv.second->solo);
         hv_pipe_destroy(kv.second->p);
+        destroy_member_stream(kv.second);
         delete kv.second;
     }
     s->members.clear();
@@ -616,13 +719,24 @@ hv_status hv_server_open_stream(hv_server* s, const hv_frame_desc* fd, const hv_
         }
         ++bucket->pending;
     }
-    hv_pipe* p = pipe_create_served(fd, &vs, bucket->stream, notify_engine, s, &r);
-    Member* m = p ? new (std::nothrow) Member() : nullptr;
-    if (p && !m)
-    {
-        hv_pipe_destroy(p);
-        p = nullptr;
+    Member* m = new (std::nothrow) Member();
+    hv_pipe* p = nullptr;
+    if (!m)
         r = HV_FAILURE;
+    else if ((s->flags & HV_SERVER_STREAM_GRAPHS) && (r = make_member_stream(m)) != HV_OK)
+    {
+        delete m;
+        m = nullptr;
+    }
+    if (m)
+    {
+        p = pipe_create_served(fd, &vs, m->own ? m->own : bucket->stream, notify_engine, s, &r);
+        if (!p)
+        {
+            destroy_member_stream(m);
+            delete m;
+            m = nullptr;
+        }
     }
     Bucket* drop = nullptr;
     {
@@ -680,14 +794,17 @@ hv_status hv_server_close_stream(hv_server* s, int32_t id)
         Bucket* b = m->bucket;
         b->members.erase(std::find(b->members.begin(), b->members.end(), m));
         // the graphs referenced this member's buffers and control-block indices: drop them
-        // (recaptured on the next pass)
+        // (recaptured on the next pass); per-stream graphs of the others use their own blocks
         cudaStreamSynchronize(b->stream);
+        if (m->own)
+            cudaStreamSynchronize(m->own);
         if (m->solo)
         {
             cudaGraphExecDestroy(m->solo);
             m->solo = nullptr;
         }
-        drop_graphs(b);
+        if (!(s->flags & HV_SERVER_STREAM_GRAPHS))
+            drop_graphs(b);
         if (b->members.empty() && b->pending == 0)
         {
             s->buckets.erase(std::find(s->buckets.begin(), s->buckets.end(), b));
@@ -696,6 +813,7 @@ hv_status hv_server_close_stream(hv_server* s, int32_t id)
     }
     // the pipe synchronises the bucket's stream: destroy it while the stream exists
     hv_pipe_destroy(m->p);
+    destroy_member_stream(m);
     if (empty_bucket)
         destroy_bucket(empty_bucket);
     {
@@ -782,7 +900,12 @@ hv_status hv_server_sync(hv_server* s, int64_t timeout_us)
     }
     std::lock_guard<std::mutex> g(s->mu);
     for (Bucket* b : s->buckets)
+    {
         HV_CUDA_TRY(cudaStreamSynchronize(b->stream));
+        for (Member* m : b->members)
+            if (m->own)
+                HV_CUDA_TRY(cudaStreamSynchronize(m->own));
+    }
     return s->engine_error;
 }
 

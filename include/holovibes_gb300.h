@@ -325,7 +325,10 @@ hv_status hv_contrast_to_ushort(const float* frame, const float* range_f32, int 
  * per stream: batch_size <= time_transformation_size. All calls are thread-safe; push and pull of
  * one stream from one thread each, and a stream is not closed while it is being pushed or pulled. */
 typedef struct hv_server hv_server;
-enum { HV_SERVER_NO_GRAPHS = 1 }; /* launch every cycle directly (for comparison) */
+/* HV_SERVER_NO_GRAPHS: launch every cycle directly (for comparison).
+ * HV_SERVER_STREAM_GRAPHS: every stream on its own CUDA stream, replaying its own graph (no
+ * barrier between the streams' cycles) instead of one graph per bucket. */
+enum { HV_SERVER_NO_GRAPHS = 1, HV_SERVER_STREAM_GRAPHS = 2 };
 typedef struct hv_server_stats
 {
     uint64_t batches;        /* stream cycles planned (batches consumed) */

@@ -127,11 +127,26 @@ def test_graphs_and_direct_launches_agree(cuda):
     names = ["as_stft_mod", "as_stft_acc", "stride_drop"]
     g_out, _, g_stats = _served(names)
     e_out, _, e_stats = _served(names, flags=hv.SERVER_NO_GRAPHS)
-    assert g_stats["graph_launches"] > 0 and e_stats["graph_launches"] == 0
+    s_out, _, s_stats = _served(names, flags=hv.SERVER_STREAM_GRAPHS)
+    assert g_stats["graph_launches"] > 0 and e_stats["graph_launches"] == 0 and s_stats["graph_launches"] > 0
     for n in names:
-        assert len(g_out[n]) == len(e_out[n]) > 0
-        for a, b in zip(g_out[n], e_out[n]):
+        assert len(g_out[n]) == len(e_out[n]) == len(s_out[n]) > 0
+        for a, b, c in zip(g_out[n], e_out[n], s_out[n]):
             assert np.array_equal(a, b), n
+            assert np.array_equal(a, c), n
+
+
+@pytest.mark.gpu
+def test_stream_graph_mode_mix_matches_plain(cuda):
+    names = sorted(STREAMS)
+    outs, last_float, stats = _served(names, flags=hv.SERVER_STREAM_GRAPHS)
+    for n in names:
+        ref, ref_f = _plain(n)
+        assert len(outs[n]) == len(ref) > 0, n
+        for a, b in zip(outs[n], ref):
+            assert np.array_equal(a, b), n
+        assert np.array_equal(last_float[n], ref_f[-1]), n
+    assert stats["graph_launches"] > 0
 
 
 @pytest.mark.gpu
