@@ -44,6 +44,7 @@ STATUS_NAMES = {
 SPACE_NONE, SPACE_FRESNELTR, SPACE_ANGULARSP = 0, 1, 2
 TIME_NONE, TIME_STFT, TIME_PCA, TIME_SSA_STFT = 0, 1, 2, 3
 IMG_MODULUS, IMG_SQUARED_MODULUS, IMG_ARGUMENT = 0, 1, 2
+IMG_MOMENTS_0, IMG_MOMENTS_1, IMG_MOMENTS_2 = 5, 6, 7
 LENS_FP64, LENS_REF32 = 0, 1
 EIG_FP32, EIG_FP64 = 0, 1
 MEM_HOST, MEM_DEVICE = 0, 1
@@ -94,6 +95,7 @@ class Settings(C.Structure):
         ("contrast_upper", C.c_float), ("reticle_display", C.c_int32), ("reticle_scale", C.c_float),
         ("unwrap_2d", C.c_int32), ("lens_mode", C.c_int32), ("output_buffer_size", C.c_int32),
         ("input_buffer_size", C.c_int32),
+        ("camera_fps", C.c_int32),
     ]
 
     @classmethod
@@ -196,6 +198,10 @@ def _declare(L: C.CDLL) -> None:
         "hv_time_view_tc_workspace": (sz, [i32, i32]),
         "hv_time_view_tc_status": (st, [vp]),
         "hv_time_view_mode": (None, [i32]),
+        "hv_unpack_12_to_16": (st, [vp, sz, vp, sz, vp]),
+        "hv_unpack_10_to_16": (st, [vp, sz, vp, sz, vp]),
+        "hv_moment_bin_weights": (st, [vp, i32, i32, i32, i32, f32, vp]),
+        "hv_time_moments": (st, [vp, i32, i32, i32, vp, i32, vp, i32, vp, vp, vp]),
         "hv_stft_weights": (st, [vp, i32, i32, i32, vp]),
         "hv_pca_covariance": (st, [vp, i32, sz, vp, vp, vp]),
         "hv_pca_cov_workspace": (sz, [i32, sz]),

@@ -127,6 +127,33 @@ int hv_time_view_partials(int width, int height) { return time_view_partials(wid
 
 void hv_time_view_mode(int mode) { set_view_mode(mode); }
 
+hv_status hv_moment_bin_weights(float* bin_w_f32, int T, int pmin, int pmax, int img_type, float camera_fps,
+                                void* stream)
+{
+    if (!is_moment(img_type))
+        return HV_WRONG_IMG_TYPE;
+    return moment_bin_weights(bin_w_f32, T, pmin, pmax, img_type - HV_IMG_MOMENTS_0, camera_fps, S(stream));
+}
+
+hv_status hv_time_moments(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
+                          const float* bin_w_f32, int shift, float* out_f32, double* partials_f64, void* stream)
+{
+    if (!ring_c64 || !weights_c64 || !bin_w_f32 || !out_f32)
+        return HV_INVALID_VALUE;
+    return time_view(static_cast<const float2*>(ring_c64), T, width, height, static_cast<const float2*>(weights_c64), K,
+                     HV_IMG_MOMENTS_0, 1.0f, shift, out_f32, partials_f64, S(stream), nullptr, bin_w_f32);
+}
+
+hv_status hv_unpack_12_to_16(const void* in, size_t in_bytes, uint16_t* out, size_t out_count, void* stream)
+{
+    return unpack_packed(12, in, in_bytes, out, out_count, S(stream));
+}
+
+hv_status hv_unpack_10_to_16(const void* in, size_t in_bytes, uint16_t* out, size_t out_count, void* stream)
+{
+    return unpack_packed(10, in, in_bytes, out, out_count, S(stream));
+}
+
 size_t hv_time_view_tc_workspace(int K, int T) { return view_tc_supported(K) ? view_tc_workspace(K, T) : 0; }
 
 hv_status hv_time_view_tc(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,

@@ -512,10 +512,18 @@ hv_status hv_holo_get_settings(const hv_holo_file* h, hv_settings* s)
             return r;
     }
     if (json::Value* info = child(footer, "info"))
+    {
         if (json::Value* pp = child(*info, "pixel_pitch"))
             if (json::Value* x = child(*pp, "x"))
                 if (x->kind == json::Value::Number)
                     s->pixel_size = static_cast<float>(x->num);  // pixels are square
+        // camera_fps defaults to input_fps (InputHoloFile::import_info)
+        json::Value* fps = child(*info, "camera_fps");
+        if (!fps || fps->kind != json::Value::Number)
+            fps = child(*info, "input_fps");
+        if (fps && fps->kind == json::Value::Number)
+            s->camera_fps = static_cast<int32_t>(fps->num);
+    }
     return HV_OK;
 }
 

@@ -51,10 +51,16 @@ hv_status fft_rows_pass(const void* in, int kind, float2* out, int W, int H, int
 hv_status fft_cols_pass(const float2* in, float2* out, int W, int H, int batch, const float2* postmul, int mode,
                         float scale, int slot0, int nslots, cudaStream_t st);
 
+// ingest.cu
+hv_status unpack_packed(int bits, const void* in, size_t in_bytes, uint16_t* out, size_t out_count, cudaStream_t st);
+
 // time_transform.cu
 int time_view_partials(int W, int H);
 hv_status time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type, float scale,
-                    int shift, float* out, double* partials, cudaStream_t st, const CycleCtl* ctl = nullptr);
+                    int shift, float* out, double* partials, cudaStream_t st, const CycleCtl* ctl = nullptr,
+                    const float* bin_w = nullptr);
+hv_status moment_bin_weights(float* bin_w, int T, int pmin, int pmax, int order, float camera_fps, cudaStream_t st);
+inline bool is_moment(int img_type) { return img_type >= HV_IMG_MOMENTS_0 && img_type <= HV_IMG_MOMENTS_2; }
 hv_status stft_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
 hv_status delta_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
 size_t pca_cov_workspace(int T, size_t npix);
@@ -77,7 +83,8 @@ bool view_engine_tc(int K, size_t HW);
 size_t view_tc_workspace(int K, int T);
 hv_status view_tc_prepare(const float2* weights, int K, int T, void* work, cudaStream_t st);
 hv_status view_tc(const float2* ring, int T, int W, int H, int K, int img_type, float scale, int shift, float* out,
-                  double* partials, void* work, cudaStream_t st, const CycleCtl* ctl = nullptr);
+                  double* partials, void* work, cudaStream_t st, const CycleCtl* ctl = nullptr,
+                  const float* bin_w = nullptr);
 
 // render.cu
 size_t unwrap_workspace(int W, int H);

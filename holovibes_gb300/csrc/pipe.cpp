@@ -102,6 +102,8 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
         z.add(pca_eigh_workspace(T));
     }
     z.add(HW * 4 * 2);  // view + post
+    if (is_moment(s.image_type))
+        z.add(static_cast<size_t>(K > 0 ? K : 1) * sizeof(float));
     if (use_view_tc(K, HW))
         z.add(view_tc_workspace(K, T));
     if (uses_unwrap(s))
@@ -166,6 +168,11 @@ hv_status build(hv_pipe* p)
         HV_ALLOC(p->eig_work, pca_eigh_workspace(p->T));
     }
     HV_ALLOC(p->view, HW * sizeof(float));
+    p->bin_w = nullptr;
+    if (is_moment(s.image_type))
+    {
+        HV_ALLOC(p->bin_w, static_cast<size_t>(p->K) * sizeof(float));
+    }
     p->view_on_tc = use_view_tc(p->K, p->HW);
     if (p->view_on_tc)
     {
@@ -232,6 +239,9 @@ hv_status build(hv_pipe* p)
         return st;
     if (p->view_on_tc && !uses_pca(s) && (st = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, p->stream)) != HV_OK)
         return st;
+    if (p->bin_w && (st = moment_bin_weights(p->bin_w, p->T, p->pmin, p->pmax, s.image_type - HV_IMG_MOMENTS_0,
+                                             static_cast<float>(s.camera_fps), p->stream)) != HV_OK)
+        return st;
     float r0[4] = {s.contrast_min, s.contrast_max, 0.f, 0.f};
     HV_CUDA_TRY(cudaMemcpyAsync(p->range, r0, sizeof(r0), cudaMemcpyHostToDevice, p->stream));
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
@@ -270,16 +280,20 @@ hv_status render(hv_pipe* p)
             return r;
     }
     // converts.cc:50-62: PCA views are scaled by (2 << 16) - 1
-    const float scale = pca ? static_cast<float>((2 << 16) - 1) : 1.0f;
+    // PCA views are scaled by (2 << 16) - 1 (converts.cc:50-62); a moment replaces the frame after
+    // that scaling (pipe.cc:346, fourier_transform.cc:317-338) and is not scaled
+    const float scale = (pca && !p->bin_w) ? static_cast<float>((2 << 16) - 1) : 1.0f;
     const bool shift_in_view = s.fft_shift && !unwrap;
     const bool renorm = s.renorm != 0;
     const float* frame = p->view;
     if (!unwrap)
     {
         if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, scale, shift_in_view ? 1 : 0,
-                                         p->view, renorm ? p->partials : nullptr, p->view_tc_work, st)
+                                         p->view, renorm ? p->partials : nullptr, p->view_tc_work, st, nullptr,
+                                         p->bin_w)
                                : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale,
-                                           shift_in_view ? 1 : 0, p->view, renorm ? p->partials : nullptr, st)) != HV_OK)
+                                           shift_in_view ? 1 : 0, p->view, renorm ? p->partials : nullptr, st,
+                                           nullptr, p->bin_w)) != HV_OK)
             return r;
         if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
                                           p->reduce_work, st)) != HV_OK)
@@ -655,17 +669,19 @@ hv_status served_record(hv_pipe* p, const CycleCtl* ctl, const ServedCycle& c, b
         if (p->view_on_tc && (r = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, st)) != HV_OK)
             return r;
     }
-    const float scale = pca ? static_cast<float>((2 << 16) - 1) : 1.0f;
+    // PCA views are scaled by (2 << 16) - 1 (converts.cc:50-62); a moment replaces the frame after
+    // that scaling (pipe.cc:346, fourier_transform.cc:317-338) and is not scaled
+    const float scale = (pca && !p->bin_w) ? static_cast<float>((2 << 16) - 1) : 1.0f;
     const bool shift_in_view = s.fft_shift && !unwrap;
     const bool renorm = s.renorm != 0;
     const float* frame = p->view;
     if (!unwrap)
     {
         if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, scale, shift_in_view ? 1 : 0,
-                                         p->view, renorm ? p->partials : nullptr, p->view_tc_work, st, ctl)
+                                         p->view, renorm ? p->partials : nullptr, p->view_tc_work, st, ctl, p->bin_w)
                                : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale,
-                                           shift_in_view ? 1 : 0, p->view, renorm ? p->partials : nullptr, st, ctl)) !=
-            HV_OK)
+                                           shift_in_view ? 1 : 0, p->view, renorm ? p->partials : nullptr, st, ctl,
+                                           p->bin_w)) != HV_OK)
             return r;
         if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
                                           p->reduce_work, st, ctl)) != HV_OK)

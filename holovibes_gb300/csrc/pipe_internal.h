@@ -54,6 +54,7 @@ struct hv_pipe
     float* range = nullptr;
     void* pct_work = nullptr;
     bool view_on_tc = false;  // K-bin contraction on the tensor cores (hv_time_view_tc)
+    float* bin_w = nullptr;   // moments: per-bin weights f_k^n (null for the other views)
     void* view_tc_work = nullptr;
 
     // input ring of batch slots

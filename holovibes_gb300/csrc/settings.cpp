@@ -173,7 +173,13 @@ int img_from_string(const std::string& s)
         return HV_IMG_SQUARED_MODULUS;
     if (s == "ARGUMENT")
         return HV_IMG_ARGUMENT;
-    if (s == "PHASE_INCREASE" || s == "COMPOSITE" || s == "MOMENTS_0" || s == "MOMENTS_1" || s == "MOMENTS_2")
+    if (s == "MOMENTS_0")
+        return HV_IMG_MOMENTS_0;
+    if (s == "MOMENTS_1")
+        return HV_IMG_MOMENTS_1;
+    if (s == "MOMENTS_2")
+        return HV_IMG_MOMENTS_2;
+    if (s == "PHASE_INCREASE" || s == "COMPOSITE")
         return 100;  // reference image types outside this path
     return -1;
 }
@@ -210,6 +216,7 @@ void settings_default(hv_settings* s)
     s->lens_mode = HV_LENS_FP64;
     s->output_buffer_size = 1024;
     s->input_buffer_size = 512;
+    s->camera_fps = 0;  // settings::CameraFps{0} (holovibes.hh:446)
 }
 
 hv_status settings_from_json(const char* text, hv_settings* s)
@@ -392,7 +399,8 @@ void settings_to_value(const hv_settings* s, json::Value& doc)
     json::parse(kDefaultComputeSettings, doc, err);
     static const char* space[] = {"NONE", "FRESNELTR", "ANGULARSP"};
     static const char* time[] = {"NONE", "STFT", "PCA", "SSA_STFT"};
-    static const char* img[] = {"MODULUS", "SQUARED_MODULUS", "ARGUMENT"};
+    static const char* img[] = {"MODULUS", "SQUARED_MODULUS", "ARGUMENT", "PHASE_INCREASE", "COMPOSITE",
+                                "MOMENTS_0", "MOMENTS_1", "MOMENTS_2"};
     set_str(doc, {"image_rendering", "image_mode"}, "HOLOGRAM");
     set_str(doc, {"image_rendering", "space_transformation"},
             space[s->space_transformation >= 0 && s->space_transformation <= 2 ? s->space_transformation : 0]);
@@ -403,7 +411,7 @@ void settings_to_value(const hv_settings* s, json::Value& doc)
     set_num(doc, {"image_rendering", "batch_size"}, s->batch_size);
     set_num(doc, {"image_rendering", "lambda"}, s->lambda);
     set_num(doc, {"image_rendering", "propagation_distance"}, s->z_distance);
-    set_str(doc, {"view", "image_type"}, img[s->image_type >= 0 && s->image_type <= 2 ? s->image_type : 0]);
+    set_str(doc, {"view", "image_type"}, img[s->image_type >= 0 && s->image_type <= 7 ? s->image_type : 0]);
     set_bool(doc, {"view", "fft_shift"}, s->fft_shift != 0);
     set_bool(doc, {"view", "renorm"}, s->renorm != 0);
     set_num(doc, {"view", "z", "start"}, s->p_start);
@@ -500,11 +508,14 @@ hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd)
         s->accumulation = 0;
     if (s->output_buffer_size < 1)
         s->output_buffer_size = 1;
-    if (s->image_type != HV_IMG_MODULUS && s->image_type != HV_IMG_SQUARED_MODULUS && s->image_type != HV_IMG_ARGUMENT)
+    if (s->image_type != HV_IMG_MODULUS && s->image_type != HV_IMG_SQUARED_MODULUS && s->image_type != HV_IMG_ARGUMENT &&
+        s->image_type != HV_IMG_MOMENTS_0 && s->image_type != HV_IMG_MOMENTS_1 && s->image_type != HV_IMG_MOMENTS_2)
     {
-        set_last_error_msg("image type outside the hologram path (modulus, squared modulus, argument)");
+        set_last_error_msg("image type outside the hologram path (modulus, squared modulus, argument, moments)");
         return HV_WRONG_IMG_TYPE;
     }
+    if (s->camera_fps < 0)
+        s->camera_fps = 0;
     if (s->time_transformation == HV_TIME_SSA_STFT)
     {
         set_last_error_msg("SSA_STFT is not implemented");

@@ -17,6 +17,8 @@
 // buffer of the reference never exists.
 #include <math.h>
 
+#include <vector>
+
 #include "hv_common.cuh"
 #include "hv_internal.h"
 
@@ -43,8 +45,10 @@ template <int KC>
 __global__ void __launch_bounds__(TV_THREADS) k_time_view(const float2* __restrict__ ring, int T, int W, int H,
                                                            const float2* __restrict__ weights, int K, int img_type,
                                                            float scale, int shift, float* __restrict__ out,
-                                                           double* __restrict__ partials, const CycleCtl* ctl)
+                                                           double* __restrict__ partials, const CycleCtl* ctl,
+                                                           const float* __restrict__ bin_w)
 {
+    // bin_w (moments): out = sum_k |X_k|^2 bin_w[k] instead of the mean of the view over the bins
     if (!ctl_render(ctl))
         return;
     extern __shared__ __align__(16) float2 wsm[];  // [T][KC]
@@ -84,16 +88,26 @@ __global__ void __launch_bounds__(TV_THREADS) k_time_view(const float2* __restri
                 }
             }
             const int kn = (K - k0) < KC ? (K - k0) : KC;
+            if (bin_w)
+            {
 #pragma unroll
-            for (int kk = 0; kk < KC; ++kk)
-                if (kk < kn)
-                    acc_view += view_value(acc[kk], img_type);
+                for (int kk = 0; kk < KC; ++kk)
+                    if (kk < kn)
+                        acc_view += (acc[kk].x * acc[kk].x + acc[kk].y * acc[kk].y) * __ldg(bin_w + k0 + kk);
+            }
+            else
+            {
+#pragma unroll
+                for (int kk = 0; kk < KC; ++kk)
+                    if (kk < kn)
+                        acc_view += view_value(acc[kk], img_type);
+            }
         }
     }
     float v = 0.f;
     if (valid)
     {
-        v = acc_view / static_cast<float>(K);
+        v = bin_w ? acc_view : acc_view / static_cast<float>(K);
         if (scale != 1.0f)
             v = v * scale;
         const int x = static_cast<int>(pix % W);
@@ -131,7 +145,7 @@ int time_view_partials(int W, int H)
 template <int KC>
 static hv_status launch_time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type,
                                   float scale, int shift, float* out, double* partials, cudaStream_t st,
-                                  const CycleCtl* ctl)
+                                  const CycleCtl* ctl, const float* bin_w)
 {
     const size_t smem = static_cast<size_t>(T) * KC * sizeof(float2);
     if (smem > 200 * 1024)
@@ -144,14 +158,14 @@ static hv_status launch_time_view(const float2* ring, int T, int W, int H, const
                                          static_cast<int>(smem)));
     const int grid = time_view_partials(W, H);
     k_time_view<KC><<<grid, TV_THREADS, smem, st>>>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials,
-                                                    ctl);
+                                                    ctl, bin_w);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
 }
 
 hv_status time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type, float scale,
-                    int shift, float* out, double* partials, cudaStream_t st, const CycleCtl* ctl)
+                    int shift, float* out, double* partials, cudaStream_t st, const CycleCtl* ctl, const float* bin_w)
 {
     if (T <= 0 || K <= 0 || W <= 0 || H <= 0)
     {
@@ -167,18 +181,18 @@ hv_status time_view(const float2* ring, int T, int W, int H, const float2* weigh
     const int chunks = (K + TV_KMAX - 1) / TV_KMAX;
     const int need = (K + chunks - 1) / chunks;
     if (need <= 1)
-        return launch_time_view<1>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
+        return launch_time_view<1>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
     if (need <= 2)
-        return launch_time_view<2>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
+        return launch_time_view<2>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
     if (need <= 4)
-        return launch_time_view<4>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
+        return launch_time_view<4>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
     if (need <= 6)
-        return launch_time_view<6>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
+        return launch_time_view<6>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
     if (need <= 8)
-        return launch_time_view<8>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
+        return launch_time_view<8>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
     if (need <= 11)
-        return launch_time_view<11>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
-    return launch_time_view<16>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl);
+        return launch_time_view<11>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
+    return launch_time_view<16>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
 }
 
 // ------------------------------------------------------------------------------ weights
@@ -202,6 +216,34 @@ __global__ void k_delta_weights(float2* w, int T, int pmin, int K)
         return;
     const int k = e / T, t = e - k * T;
     w[e] = make_float2(t == pmin + k ? 1.f : 0.f, 0.f);
+}
+
+// f_k^n of the bins pmin..pmax with the Nyquist compensation, in the reference's float arithmetic:
+// d = (float)camera_fps / T, f1 = i d for the first half and -(T - i) d (even T) or (i - T) d
+// (odd T) for the second (icompute.cc:26-69); the Nyquist bin of an even window counts twice for
+// orders 0 and 2 and not at all for order 1 (tools_compute.cu:60-69).
+hv_status moment_bin_weights(float* bin_w, int T, int pmin, int pmax, int order, float camera_fps, cudaStream_t st)
+{
+    if (T <= 0 || pmin < 0 || pmax < pmin || pmax >= T || order < 0 || order > 2 || !bin_w)
+        return HV_INVALID_VALUE;
+    const float d = camera_fps / static_cast<float>(T);
+    std::vector<float> w(static_cast<size_t>(pmax - pmin + 1));
+    const bool even = T % 2 == 0;
+    for (int i = pmin; i <= pmax; ++i)
+    {
+        float f1;
+        if (even)
+            f1 = i < T / 2 ? static_cast<float>(i) * d : -(static_cast<float>(T) - static_cast<float>(i)) * d;
+        else
+            f1 = i < (T + 1) / 2 ? static_cast<float>(i) * d : (static_cast<float>(i) - static_cast<float>(T)) * d;
+        float f = order == 0 ? 1.0f : (order == 1 ? f1 : f1 * f1);
+        if (even && i == T / 2)
+            f = order == 1 ? 0.0f : 2.0f * f;
+        w[static_cast<size_t>(i - pmin)] = f;
+    }
+    HV_CUDA_TRY(cudaMemcpyAsync(bin_w, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    HV_CUDA_TRY(cudaStreamSynchronize(st));  // the host table goes out of scope
+    return HV_OK;
 }
 
 hv_status stft_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st)

@@ -70,6 +70,7 @@ struct ViewTcArgs
     int* err;
     int raw_stages;
     const CycleCtl* ctl;  // served cycle gate (render), or null
+    const float* bin_w;   // moments: out = sum_k |X_k|^2 bin_w[k] (else the mean of the view)
     int stacked;          // 1: D1 = Ah [Bh; Bl] (2N cols) + D2 = Al Bh;  0: D1 = Ah Bh + Al Bh, D2 = Ah Bl
 };
 
@@ -282,7 +283,8 @@ __global__ void __launch_bounds__(V_THREADS, 1) k_view_tc(const __grid_constant_
                 {
                     const int k = c0 / 2 + i;
                     if (k < a.K)
-                        sum += view_value_tc(d[2 * i], d[2 * i + 1], a.img_type);
+                        sum += a.bin_w ? (d[2 * i] * d[2 * i] + d[2 * i + 1] * d[2 * i + 1]) * __ldg(a.bin_w + k)
+                                       : view_value_tc(d[2 * i], d[2 * i + 1], a.img_type);
                 }
             }
             tc::fence_before();
@@ -293,7 +295,7 @@ __global__ void __launch_bounds__(V_THREADS, 1) k_view_tc(const __grid_constant_
             float v = 0.f;
             if (P < a.HW)
             {
-                v = sum / static_cast<float>(a.K);
+                v = a.bin_w ? sum : sum / static_cast<float>(a.K);
                 if (a.scale != 1.0f)
                     v = v * a.scale;
                 size_t dst = P;
@@ -434,7 +436,7 @@ hv_status view_tc_prepare(const float2* weights, int K, int T, void* work, cudaS
 }
 
 hv_status view_tc(const float2* ring, int T, int W, int H, int K, int img_type, float scale, int shift, float* out,
-                  double* partials, void* work, cudaStream_t st, const CycleCtl* ctl)
+                  double* partials, void* work, cudaStream_t st, const CycleCtl* ctl, const float* bin_w)
 {
     if (!view_tc_supported(K))
         return HV_ERR_UNSUPPORTED;
@@ -475,6 +477,7 @@ hv_status view_tc(const float2* ring, int T, int W, int H, int K, int img_type, 
     a.out = out;
     a.partials = partials;
     a.ctl = ctl;
+    a.bin_w = bin_w;
     a.stacked = (3 * a.N <= static_cast<int>(V_ACC_COLS)) ? 1 : 0;
     const size_t a_bytes = V_A_STAGES * view_tc_a_stage_bytes(a.N);
     const size_t budget = 220 * 1024;

@@ -61,7 +61,18 @@ enum { HV_SPACE_NONE = 0, HV_SPACE_FRESNELTR = 1, HV_SPACE_ANGULARSP = 2 };
 /* TimeTransformation (Backend/includes/enum/enum_time_transformation.hh:16-22). */
 enum { HV_TIME_NONE = 0, HV_TIME_STFT = 1, HV_TIME_PCA = 2, HV_TIME_SSA_STFT = 3 };
 /* ImgType (Backend/includes/enum/enum_img_type.hh:16-26); only the first three are on this path. */
-enum { HV_IMG_MODULUS = 0, HV_IMG_SQUARED_MODULUS = 1, HV_IMG_ARGUMENT = 2 };
+/* ImgType values of the reference (enum_img_type.hh:15-25); PHASE_INCREASE (3) and COMPOSITE (4)
+ * are outside this path. Moments: sum over the selected bins of |X_k|^2 f_k^n (f_k the signed
+ * FFT frequency in units of camera_fps / T), replacing the view frame. */
+enum
+{
+    HV_IMG_MODULUS = 0,
+    HV_IMG_SQUARED_MODULUS = 1,
+    HV_IMG_ARGUMENT = 2,
+    HV_IMG_MOMENTS_0 = 5,
+    HV_IMG_MOMENTS_1 = 6,
+    HV_IMG_MOMENTS_2 = 7
+};
 /* Lens phase precision: FP64 (exact phase, reduced mod 2*pi) or the reference's float32 expression. */
 enum { HV_LENS_FP64 = 0, HV_LENS_REF32 = 1 };
 /* Memory kinds for hv_pipe_push_frames / hv_pipe_pull_output. */
@@ -101,6 +112,7 @@ typedef struct hv_settings
     int32_t lens_mode;               /* HV_LENS_FP64 (default) or HV_LENS_REF32 */
     int32_t output_buffer_size;      /* advanced.buffer_size.output: output frames kept */
     int32_t input_buffer_size;       /* advanced.buffer_size.input: raw frames kept */
+    int32_t camera_fps;              /* CameraFps input setting (.holo info.camera_fps): moment frequencies */
 } hv_settings;
 
 /* ------------------------------------------------------------------------------------------
@@ -235,6 +247,22 @@ size_t hv_time_view_tc_workspace(int K, int T);
  * hv_time_view_tc supports the shape. */
 void hv_time_view_mode(int mode);
 hv_status hv_time_view_tc_status(const void* work);
+/* Packed camera data to 16-bit pixels (device buffers): 12-bit pairs in 3 bytes or 10-bit
+ * quadruples in 5 bytes, MSB first, each value left-aligned in 16 bits; out_count pixels are
+ * written where their bytes lie inside in_bytes. Replaces unpack_12_to_16bit / unpack_10_to_16bit
+ * (unpack.cu:4-60, file_frame_read_worker.cc:220-240). */
+hv_status hv_unpack_12_to_16(const void* in, size_t in_bytes, uint16_t* out, size_t out_count, void* stream);
+hv_status hv_unpack_10_to_16(const void* in, size_t in_bytes, uint16_t* out, size_t out_count, void* stream);
+/* Moments of order n = img_type - HV_IMG_MOMENTS_0: per-bin weights f_k^n of the bins pmin..pmax
+ * with the Nyquist compensation (bin T/2 of an even window twice for n = 0, 2, not at all for
+ * n = 1), written as pmax - pmin + 1 floats at bin_w_f32 (device); and the moment frame
+ * out = sum_k |X_k|^2 bin_w[k] with the same ring / weights conventions as hv_time_view.
+ * Replaces fft_freqs + tensor_multiply_vector_nyquist_compensation (icompute.cc:26-69,
+ * tools_compute.cu:38-97, fourier_transform.cc:244-338). */
+hv_status hv_moment_bin_weights(float* bin_w_f32, int T, int pmin, int pmax, int img_type, float camera_fps,
+                                void* stream);
+hv_status hv_time_moments(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
+                          const float* bin_w_f32, int shift, float* out_f32, double* partials_f64, void* stream);
 /* STFT weights W[k][t] = exp(-2*pi*i*(pmin+k)*t/T), k <= pmax-pmin, computed in FP64. */
 hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* stream);
 

@@ -67,6 +67,31 @@ def convert_frames(raw: np.ndarray) -> np.ndarray:
     raise TypeError(f"unsupported raw dtype {raw.dtype}")
 
 
+def unpack_12_to_16(packed: np.ndarray, n: int) -> np.ndarray:
+    """unpack_12_to_16bit (unpack.cu:4-16): 12-bit pairs in 3 bytes, MSB first, left-aligned in 16 bits."""
+    b = np.zeros(((n + 1) // 2) * 3, np.uint32)
+    b[:min(len(packed), len(b))] = packed[:len(b)]
+    b0, b1, b2 = b[0::3], b[1::3], b[2::3]
+    out = np.empty(((n + 1) // 2) * 2, np.uint32)
+    out[0::2] = (b0 << 8) | (b1 & 0xF0)
+    out[1::2] = ((b1 & 0x0F) << 12) | (b2 << 4)
+    return (out[:n] & 0xFFFF).astype(np.uint16)
+
+
+def unpack_10_to_16(packed: np.ndarray, n: int) -> np.ndarray:
+    """unpack_10_to_16bit (unpack.cu:18-32): 10-bit quadruples in 5 bytes, MSB first, left-aligned."""
+    g = (n + 3) // 4
+    b = np.zeros(g * 5, np.uint32)
+    b[:min(len(packed), len(b))] = packed[:len(b)]
+    b0, b1, b2, b3, b4 = (b[i::5] for i in range(5))
+    out = np.empty(g * 4, np.uint32)
+    out[0::4] = (b0 << 8) | (b1 & 0xC0)
+    out[1::4] = ((b1 & 0x3F) << 10) | ((b2 & 0xF0) << 2)
+    out[2::4] = ((b2 & 0x0F) << 12) | ((b3 & 0xFC) << 4)
+    out[3::4] = ((b3 & 0x03) << 14) | (b4 << 6)
+    return (out[:n] & 0xFFFF).astype(np.uint16)
+
+
 def byteswap16(raw: np.ndarray) -> np.ndarray:
     """Big-endian 16-bit input (Backend/sources/data_struct/queue.cc:191-202, tools_conversion.cu endianness_conversion)."""
     return ((raw.astype(np.uint16) << 8) | (raw.astype(np.uint16) >> 8)).astype(np.uint16)
@@ -327,6 +352,39 @@ def view(planes: np.ndarray, img_type: str) -> np.ndarray:
 
 
 # ----------------------------------------------------------------------------------------
+# Moments 0/1/2 (fourier_transform.cc:244-338, icompute.cc:26-69 fft_freqs,
+# tools_compute.cu:38-97, converts.cc:112-125, pipe.cc:429-454)
+# ----------------------------------------------------------------------------------------
+
+
+def fft_freqs(T: int, camera_fps: float) -> np.ndarray:
+    """f1 of ICompute::fft_freqs: [0, 1, ..., n/2-1, -n/2, ..., -1] * fs/n for even n (the Nyquist
+    bin kept negative), [0, ..., (n-1)/2, -(n-1)/2, ..., -1] * fs/n for odd n; d in float32."""
+    d = float(F32(camera_fps) / F32(T))
+    k = np.arange(T, dtype=np.float64)
+    if T % 2 == 0:
+        f1 = np.where(k < T // 2, k, -(T - k))
+    else:
+        f1 = np.where(k < (T + 1) // 2, k, k - T)
+    return f1 * d
+
+
+def moments(planes: np.ndarray, pmin: int, T: int, camera_fps: float, order: int) -> np.ndarray:
+    """Moment of order 0, 1 or 2 of the selected bins pmin.. (planes[k] = X_{pmin+k}):
+    sum_k |X_k|^2 f1[k]^order, with the Nyquist bin (even T) counted twice for orders 0 and 2 and
+    not at all for order 1 (tensor_multiply_vector_nyquist_compensation)."""
+    f1 = fft_freqs(T, camera_fps)
+    f = {0: np.ones(T), 1: f1, 2: f1 * f1}[order]
+    p2 = np.abs(planes) ** 2
+    idx = pmin + np.arange(planes.shape[0])
+    w = f[idx].copy()
+    if T % 2 == 0:
+        ny = (idx == T // 2)
+        w[ny] = 0.0 if order == 1 else 2.0 * w[ny]
+    return np.tensordot(w, p2, axes=(0, 0))
+
+
+# ----------------------------------------------------------------------------------------
 # a17: 2-D phase unwrap (tools_unwrap.cu:79-95,269-369; tools.cu:50-68) + rescale
 #      (tools_conversion.cu:315-335)
 # ----------------------------------------------------------------------------------------
@@ -508,6 +566,7 @@ class OracleSettings:
     reticle_scale: float = 0.5
     unwrap_2d: bool = False
     lens_mode: str = "fp64"
+    camera_fps: float = 0.0  # moments: frequencies in units of camera_fps / T
 
 
 @dataclass
@@ -564,10 +623,14 @@ class OraclePipe:
             planes = pca_project(self.ring.data, V, pmin, pmax)
         else:
             planes = self.ring.data[pmin:pmax + 1]
-        img = view(planes, s.image_type)
+        if s.image_type.startswith("MOMENTS_"):
+            # the moment replaces the post-processing frame after the PCA scaling (pipe.cc:346)
+            img = moments(planes, pmin, T, s.camera_fps, int(s.image_type[-1]))
+        else:
+            img = view(planes, s.image_type)
         if s.image_type == "ARGUMENT" and s.unwrap_2d:
             img = rescale_unwrap2d(unwrap_2d(img))
-        if s.time_transformation == "PCA":
+        if s.time_transformation == "PCA" and not s.image_type.startswith("MOMENTS_"):
             img = img * PCA_SCALE
         if s.renorm:
             img = renormalize(img, s.renorm_constant)

@@ -115,3 +115,27 @@ def test_pca_pipeline_dominant_components():
     P = O.pca_project(ring, V, T - 2, T - 1)
     # the two dominant components carry the whole signal
     assert np.isclose((np.abs(P) ** 2).sum(), (np.abs(ring) ** 2).sum(), rtol=1e-9)
+
+
+def test_unpack_known_values():
+    """Packed camera formats, MSB first (unpack.cu:4-32): hand-computed groups."""
+    import holovibes_oracle as O
+
+    got12 = O.unpack_12_to_16(np.array([0xAB, 0xCD, 0xEF], np.uint8), 2)
+    assert got12.tolist() == [0xABC0, 0xDEF0]
+    got10 = O.unpack_10_to_16(np.array([0xFF, 0xC0, 0x3F, 0xF0, 0x0F], np.uint8), 4)
+    # 10-bit values 0x3FF, 0x000, 0x3FF, 0x00F... left-aligned
+    assert got10.tolist() == [0xFFC0, 0x0000 | ((0x3F & 0xF0) << 2), ((0x3F & 0x0F) << 12) | ((0xF0 & 0xFC) << 4),
+                              ((0xF0 & 0x03) << 14) | (0x0F << 6)]
+
+
+def test_moment_frequencies():
+    """fft_freqs (icompute.cc:26-69): even windows keep the Nyquist bin negative."""
+    import holovibes_oracle as O
+
+    assert O.fft_freqs(8, 1000.0).tolist() == [0, 125, 250, 375, -500, -375, -250, -125]
+    assert O.fft_freqs(5, 1000.0).tolist() == [0, 200, 400, -400, -200]
+    X = np.ones((8, 1, 1), complex)
+    assert O.moments(X, 0, 8, 1000.0, 0)[0, 0] == 9.0  # Nyquist bin counted twice
+    assert O.moments(X, 0, 8, 1000.0, 1)[0, 0] == 0.0
+    assert O.moments(X, 0, 8, 1000.0, 2)[0, 0] == 937500.0

@@ -14,7 +14,7 @@ from gpu_util import rel_l2, wrapped_diff
 import holovibes_gb300 as hv
 from holovibes_gb300.synthetic import Interferogram
 
-IMG = {0: "MODULUS", 1: "SQUARED_MODULUS", 2: "ARGUMENT"}
+IMG = {0: "MODULUS", 1: "SQUARED_MODULUS", 2: "ARGUMENT", 5: "MOMENTS_0", 6: "MOMENTS_1", 7: "MOMENTS_2"}
 SPACE = {0: "NONE", 1: "FRESNELTR", 2: "ANGULARSP"}
 TIME = {0: "NONE", 1: "STFT", 2: "PCA"}
 
@@ -30,7 +30,7 @@ def _oracle_settings(fd, s):
         contrast_auto_refresh=bool(s.contrast_auto_refresh), contrast_invert=bool(s.contrast_invert),
         contrast_min=s.contrast_min, contrast_max=s.contrast_max, contrast_lower=s.contrast_lower,
         contrast_upper=s.contrast_upper, reticle_display=bool(s.reticle_display), reticle_scale=s.reticle_scale,
-        unwrap_2d=bool(s.unwrap_2d), lens_mode="fp64" if s.lens_mode == 0 else "ref32")
+        unwrap_2d=bool(s.unwrap_2d), lens_mode="fp64" if s.lens_mode == 0 else "ref32", camera_fps=s.camera_fps)
 
 
 CASES = {
@@ -78,6 +78,24 @@ CASES = {
                                             time_stride=16, batch_size=16, z_distance=0.3, pixel_size=20.0,
                                             image_type=1, p_start=2, p_width=8, renorm=0, contrast_enabled=1,
                                             contrast_lower=0.5, contrast_upper=99.5), 4),
+    # moments over a frequency band (fourier_transform.cc:244-338): SIMT (K < 8) and tensor cores.
+    # Moment 1 is signed and its image sum nearly cancels, so renormalising it (divide by the mean)
+    # amplifies FP32 round-off without bound; it runs without renorm, moment 0 with it.
+    "as_stft_moment1_k5": (64, 64, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=16,
+                                            time_stride=8, batch_size=8, z_distance=0.3, pixel_size=20.0, image_type=6,
+                                            p_start=6, p_width=4, camera_fps=1000, renorm=0, contrast_enabled=1,
+                                            contrast_lower=0.5, contrast_upper=99.5), 4),
+    "as_stft_moment2_k17_tc": (64, 64, 2, dict(space_transformation=2, time_transformation=1,
+                                                time_transformation_size=32, time_stride=16, batch_size=16,
+                                                z_distance=0.3, pixel_size=20.0, image_type=7, p_start=2,
+                                                p_width=16, camera_fps=2000, renorm=0, fft_shift=1,
+                                                contrast_enabled=1, contrast_lower=0.5, contrast_upper=99.5), 4),
+    "fresnel_stft_moment0_nyquist": (64, 64, 1, dict(space_transformation=1, time_transformation=1,
+                                                      time_transformation_size=16, time_stride=16, batch_size=16,
+                                                      lambda_=785e-9, z_distance=0.45, pixel_size=12.0, image_type=5,
+                                                      p_start=4, p_width=8, camera_fps=500, renorm=1,
+                                                      contrast_enabled=1, contrast_lower=0.5,
+                                                      contrast_upper=99.5), 3),
     "fresnel_stft_ref32_big_endian": (128, 64, 2, dict(space_transformation=1, time_transformation=1,
                                                         time_transformation_size=4, time_stride=4, batch_size=4,
                                                         z_distance=0.3, pixel_size=20.0, p_start=2, p_width=1,
