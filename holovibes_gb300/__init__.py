@@ -43,7 +43,7 @@ STATUS_NAMES = {
 
 SPACE_NONE, SPACE_FRESNELTR, SPACE_ANGULARSP = 0, 1, 2
 TIME_NONE, TIME_STFT, TIME_PCA, TIME_SSA_STFT = 0, 1, 2, 3
-IMG_MODULUS, IMG_SQUARED_MODULUS, IMG_ARGUMENT = 0, 1, 2
+IMG_MODULUS, IMG_SQUARED_MODULUS, IMG_ARGUMENT, IMG_PHASE_INCREASE = 0, 1, 2, 3
 IMG_MOMENTS_0, IMG_MOMENTS_1, IMG_MOMENTS_2 = 5, 6, 7
 LENS_FP64, LENS_REF32 = 0, 1
 EIG_FP32, EIG_FP64 = 0, 1
@@ -96,6 +96,8 @@ class Settings(C.Structure):
         ("unwrap_2d", C.c_int32), ("lens_mode", C.c_int32), ("output_buffer_size", C.c_int32),
         ("input_buffer_size", C.c_int32),
         ("camera_fps", C.c_int32),
+        ("q_start", C.c_int32),
+        ("q_width", C.c_int32),
     ]
 
     @classmethod
@@ -203,6 +205,10 @@ def _declare(L: C.CDLL) -> None:
         "hv_moment_bin_weights": (st, [vp, i32, i32, i32, i32, f32, vp]),
         "hv_time_moments": (st, [vp, i32, i32, i32, vp, i32, vp, i32, vp, vp, vp]),
         "hv_stft_weights": (st, [vp, i32, i32, i32, vp]),
+        "hv_ssa_weights": (st, [vp, i32, i32, i32, i32, i32, vp, vp]),
+        "hv_phase_increase": (st, [vp, i32, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp]),
+        "hv_phase_increase_workspace": (sz, [sz]),
+        "hv_rescale_float": (st, [vp, sz, vp, f32, vp, vp]),
         "hv_pca_covariance": (st, [vp, i32, sz, vp, vp, vp]),
         "hv_pca_cov_workspace": (sz, [i32, sz]),
         "hv_pca_covariance_mode": (None, [i32]),

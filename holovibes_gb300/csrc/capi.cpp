@@ -144,6 +144,38 @@ hv_status hv_time_moments(const void* ring_c64, int T, int width, int height, co
                      HV_IMG_MOMENTS_0, 1.0f, shift, out_f32, partials_f64, S(stream), nullptr, bin_w_f32);
 }
 
+hv_status hv_ssa_weights(const void* eigenvectors_c128, int T, int q_start, int q_width, int pmin, int pmax,
+                         void* weights_c64, void* stream)
+{
+    if (!eigenvectors_c128 || !weights_c64 || T <= 0 || pmin < 0 || pmax < pmin || pmax >= T || q_width < 0 ||
+        q_start < 0)
+        return HV_INVALID_VALUE;
+    // fourier_transform.cc:409-412: width 0 keeps every column
+    const int qmin = q_width != 0 ? q_start : 0, qn = q_width != 0 ? q_width : T;
+    if (qmin + qn > T)
+        return HV_INVALID_VALUE;
+    return ssa_weights(static_cast<const double2*>(eigenvectors_c128), T, qmin, qn, pmin, pmax - pmin + 1,
+                       static_cast<float2*>(weights_c64), S(stream));
+}
+
+hv_status hv_phase_increase(const void* ring_c64, int T, int width, int height, const void* w_c64, void* pred_c64,
+                            float* hist_f32, int first, int use_hist, float* out_f32, void* minmax, void* stream)
+{
+    if (width <= 0 || height <= 0)
+        return HV_INVALID_VALUE;
+    return phase_increase(static_cast<const float2*>(ring_c64), T, static_cast<size_t>(width) * height,
+                          static_cast<const float2*>(w_c64), static_cast<float2*>(pred_c64), hist_f32, first, use_hist,
+                          out_f32, static_cast<float2*>(minmax), S(stream));
+}
+
+size_t hv_phase_increase_workspace(size_t npix) { return phase_increase_minmax_count(npix) * sizeof(float2); }
+
+hv_status hv_rescale_float(const float* in_f32, size_t npix, const void* minmax, float post_scale, float* out_f32,
+                           void* stream)
+{
+    return rescale_float(in_f32, npix, static_cast<const float2*>(minmax), post_scale, out_f32, S(stream));
+}
+
 hv_status hv_unpack_12_to_16(const void* in, size_t in_bytes, uint16_t* out, size_t out_count, void* stream)
 {
     return unpack_packed(12, in, in_bytes, out, out_count, S(stream));

@@ -63,6 +63,14 @@ hv_status moment_bin_weights(float* bin_w, int T, int pmin, int pmax, int order,
 inline bool is_moment(int img_type) { return img_type >= HV_IMG_MOMENTS_0 && img_type <= HV_IMG_MOMENTS_2; }
 hv_status stft_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
 hv_status delta_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);
+// SSA_STFT projection weights of the bins pmin..pmin+K-1 from the eigenvector columns qmin..qmin+qn-1.
+hv_status ssa_weights(const double2* evecs, int T, int qmin, int qn, int pmin, int K, float2* weights, cudaStream_t st);
+// Phase increase of the p plane (weights row w) against the previous window's plane; per-CTA
+// min / max partials in mm (phase_increase_minmax_count(HW) entries).
+size_t phase_increase_minmax_count(size_t HW);
+hv_status phase_increase(const float2* ring, int T, size_t HW, const float2* w, float2* pred, float* hist, int first,
+                         int use_hist, float* out, float2* mm, cudaStream_t st);
+hv_status rescale_float(const float* in, size_t HW, const float2* mm, float post_scale, float* out, cudaStream_t st);
 size_t pca_cov_workspace(int T, size_t npix);
 void set_cov_mode(int mode);
 hv_status pca_cov_status(const void* work);

@@ -74,7 +74,13 @@ void free_buffers(hv_pipe* p)
 }
 
 bool uses_pca(const hv_settings& s) { return s.time_transformation == HV_TIME_PCA; }
-bool use_view_tc(int K, size_t HW) { return view_engine_tc(K, HW); }
+// PCA and SSA_STFT both run the covariance and the eigensolve every window
+bool uses_eig(const hv_settings& s)
+{
+    return s.time_transformation == HV_TIME_PCA || s.time_transformation == HV_TIME_SSA_STFT;
+}
+bool uses_phase_increase(const hv_settings& s) { return s.image_type == HV_IMG_PHASE_INCREASE; }
+bool use_view_tc(const hv_settings& s, int K, size_t HW) { return !uses_phase_increase(s) && view_engine_tc(K, HW); }
 bool uses_unwrap(const hv_settings& s) { return s.image_type == HV_IMG_ARGUMENT && s.unwrap_2d; }
 
 struct Sizes
@@ -95,7 +101,7 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
     if (!served && B == s.time_stride && B == T)
         z.add(HW * 8 * T);  // second ring of the double-buffered fast mode
     z.add(static_cast<size_t>(K > 0 ? K : 1) * T * 8);                 // weights
-    if (uses_pca(s))
+    if (uses_eig(s))
     {
         z.add(static_cast<size_t>(T) * T * 16 * 2 + T * 8);
         z.add(pca_cov_workspace(T, HW));
@@ -104,12 +110,17 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
     z.add(HW * 4 * 2);  // view + post
     if (is_moment(s.image_type))
         z.add(static_cast<size_t>(K > 0 ? K : 1) * sizeof(float));
-    if (use_view_tc(K, HW))
+    if (use_view_tc(s, K, HW))
         z.add(view_tc_workspace(K, T));
-    if (uses_unwrap(s))
-    {
+    if (uses_unwrap(s) || uses_phase_increase(s))
         z.add(HW * 4);
+    if (uses_unwrap(s) || (uses_phase_increase(s) && s.unwrap_2d))
         z.add(unwrap_workspace(fd.width, fd.height));
+    if (uses_phase_increase(s))
+    {
+        z.add(HW * 8);
+        z.add(HW * 4);
+        z.add(phase_increase_minmax_count(HW) * 8);
     }
     z.add(static_cast<size_t>(time_view_partials(fd.width, fd.height)) * 8);
     z.add(reduce_workspace(HW));
@@ -142,6 +153,9 @@ hv_status build(hv_pipe* p)
     if (p->pmax > p->T - 1)
         p->pmax = p->T - 1;  // the reference reads past the buffer there; validation keeps p + width < T
     p->K = p->pmax - p->pmin + 1;
+    // SSA_STFT eigenvector range (fourier_transform.cc:409-412): width 0 keeps every column
+    p->qmin = s.q_width != 0 ? s.q_start : 0;
+    p->qn = s.q_width != 0 ? s.q_width : p->T;
     p->A = s.accumulation > 1 ? s.accumulation : 0;
     const size_t HW = p->HW;
     hv_status st;
@@ -159,7 +173,7 @@ hv_status build(hv_pipe* p)
         HV_ALLOC(p->rings[1], HW * p->T * sizeof(float2));
     }
     HV_ALLOC(p->weights, static_cast<size_t>(p->K) * p->T * sizeof(float2));
-    if (uses_pca(s))
+    if (uses_eig(s))
     {
         HV_ALLOC(p->cov, static_cast<size_t>(p->T) * p->T * sizeof(double2));
         HV_ALLOC(p->evecs, static_cast<size_t>(p->T) * p->T * sizeof(double2));
@@ -173,16 +187,26 @@ hv_status build(hv_pipe* p)
     {
         HV_ALLOC(p->bin_w, static_cast<size_t>(p->K) * sizeof(float));
     }
-    p->view_on_tc = use_view_tc(p->K, p->HW);
+    p->view_on_tc = use_view_tc(s, p->K, p->HW);
     if (p->view_on_tc)
     {
         HV_ALLOC(p->view_tc_work, view_tc_workspace(p->K, p->T));
     }
     HV_ALLOC(p->post, HW * sizeof(float));
-    if (uses_unwrap(s))
+    if (uses_unwrap(s) || uses_phase_increase(s))
     {
         HV_ALLOC(p->unwrapped, HW * sizeof(float));
+    }
+    if (uses_unwrap(s) || (uses_phase_increase(s) && s.unwrap_2d))
+    {
         HV_ALLOC(p->unwrap_work, unwrap_workspace(p->W, p->H));
+    }
+    p->pi_count = 0;
+    if (uses_phase_increase(s))
+    {
+        HV_ALLOC(p->pi_pred, HW * sizeof(float2));
+        HV_ALLOC(p->pi_hist, HW * sizeof(float));
+        HV_ALLOC(p->pi_minmax, phase_increase_minmax_count(HW) * sizeof(float2));
     }
     p->npartials = time_view_partials(p->W, p->H);
     HV_ALLOC(p->partials, static_cast<size_t>(p->npartials) * sizeof(double));
@@ -237,7 +261,7 @@ hv_status build(hv_pipe* p)
         st = delta_weights(p->weights, p->T, p->pmin, p->pmax, p->stream);
     if (st != HV_OK)
         return st;
-    if (p->view_on_tc && !uses_pca(s) && (st = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, p->stream)) != HV_OK)
+    if (p->view_on_tc && !uses_eig(s) && (st = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, p->stream)) != HV_OK)
         return st;
     if (p->bin_w && (st = moment_bin_weights(p->bin_w, p->T, p->pmin, p->pmax, s.image_type - HV_IMG_MOMENTS_0,
                                              static_cast<float>(s.camera_fps), p->stream)) != HV_OK)
@@ -262,60 +286,113 @@ hv_status build(hv_pipe* p)
     return HV_OK;
 }
 
+// Time transform and view of one full ring, up to the renormalisation factors
+// (fourier_transform.cc:194-242,340-460, converts.cc:19-62,251-300, postprocessing.cc:135-155):
+// sets *frame to the float frame that the fused renorm / shift / accumulation pass reads and
+// *shift_after when that pass applies the fftshift (the view kernels apply it themselves
+// otherwise). `ctl` gates the kernels of a served cycle (null for the plain pipe).
+hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const float** frame, int* shift_after)
+{
+    const hv_settings& s = p->s;
+    hv_status r;
+    const bool pca = uses_pca(s);
+    const bool unwrap = uses_unwrap(s);
+    const bool pinc = uses_phase_increase(s);
+    if (uses_eig(s))
+    {
+        // not gated by the block: served PCA / SSA_STFT cycles are launched eagerly (render cycles only)
+        if ((r = pca_covariance(p->ring, p->T, p->HW, p->cov, p->cov_work, st)) != HV_OK)
+            return r;
+        if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, pca ? p->weights : nullptr,
+                          p->eig_work, st)) != HV_OK)
+            return r;
+        if (!pca && (r = ssa_weights(p->evecs, p->T, p->qmin, p->qn, p->pmin, p->K, p->weights, st)) != HV_OK)
+            return r;
+        if (p->view_on_tc && (r = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, st)) != HV_OK)
+            return r;
+    }
+    // PCA views are scaled by (2 << 16) - 1 (converts.cc:50-62); a moment replaces the frame after
+    // that scaling (pipe.cc:346, fourier_transform.cc:317-338) and is not scaled
+    const float scale = (pca && !p->bin_w) ? static_cast<float>((2 << 16) - 1) : 1.0f;
+    const bool renorm = s.renorm != 0;
+    *frame = p->view;
+    *shift_after = 0;
+    if (pinc)
+    {
+        // phase increase of the p plane (weights row 0), not gated by the block: its history makes
+        // every served cycle an eager one
+        const bool first = p->pi_count == 0;
+        if ((r = phase_increase(p->ring, p->T, p->HW, p->weights, p->pi_pred, p->pi_hist, first ? 1 : 0,
+                                first ? 0 : 1, p->view, p->pi_minmax, st)) != HV_OK)
+            return r;
+        ++p->pi_count;
+        if (s.unwrap_2d && first)
+        {
+            // the first window's increments are all 0: its unwrapped frame is the zero frame (the
+            // reference unwraps and rescales rounding residues there)
+            HV_CUDA_TRY(cudaMemsetAsync(p->unwrapped, 0, p->HW * sizeof(float), st));
+        }
+        else if (s.unwrap_2d)
+        {
+            if ((r = unwrap_2d(p->view, p->unwrapped, p->W, p->H, p->unwrap_work, st)) != HV_OK)
+                return r;
+            if (pca && (r = renorm_shift_accumulate(p->unwrapped, p->unwrapped, p->W, p->H, nullptr, 0, nullptr, 0, 0,
+                                                    0, 0, 0, st, scale, ctl)) != HV_OK)
+                return r;
+        }
+        else if ((r = rescale_float(p->view, p->HW, p->pi_minmax, scale, p->unwrapped, st)) != HV_OK)
+            return r;
+        *frame = p->unwrapped;
+        *shift_after = s.fft_shift ? 1 : 0;
+        if (renorm && (r = renorm_factors(*frame, p->HW, s.renorm_constant, nullptr, 0, p->factors, p->reduce_work, st,
+                                          ctl)) != HV_OK)
+            return r;
+        return HV_OK;
+    }
+    if (!unwrap)
+    {
+        const int shift_in_view = s.fft_shift ? 1 : 0;
+        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, scale, shift_in_view, p->view,
+                                         renorm ? p->partials : nullptr, p->view_tc_work, st, ctl, p->bin_w)
+                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale,
+                                           shift_in_view, p->view, renorm ? p->partials : nullptr, st, ctl,
+                                           p->bin_w)) != HV_OK)
+            return r;
+        if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
+                                          p->reduce_work, st, ctl)) != HV_OK)
+            return r;
+        return HV_OK;
+    }
+    // not gated by the block: served unwrap cycles are launched eagerly (render cycles only)
+    if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, 1.0f, 0, p->view, nullptr,
+                                     p->view_tc_work, st, ctl)
+                           : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, 1.0f, 0, p->view,
+                                       nullptr, st, ctl)) != HV_OK)
+        return r;
+    if ((r = unwrap_2d(p->view, p->unwrapped, p->W, p->H, p->unwrap_work, st)) != HV_OK)
+        return r;
+    if (pca && (r = renorm_shift_accumulate(p->unwrapped, p->unwrapped, p->W, p->H, nullptr, 0, nullptr, 0, 0, 0, 0, 0,
+                                            st, scale, ctl)) != HV_OK)
+        return r;
+    *frame = p->unwrapped;
+    *shift_after = s.fft_shift ? 1 : 0;
+    if (renorm && (r = renorm_factors(*frame, p->HW, s.renorm_constant, nullptr, 0, p->factors, p->reduce_work, st,
+                                      ctl)) != HV_OK)
+        return r;
+    return HV_OK;
+}
+
 // Rendering of one output from a full ring (pipe.cc:334-374).
 hv_status render(hv_pipe* p)
 {
     const hv_settings& s = p->s;
     cudaStream_t st = p->render_stream;
     hv_status r;
-    const bool pca = uses_pca(s);
-    const bool unwrap = uses_unwrap(s);
-    if (pca)
-    {
-        if ((r = pca_covariance(p->ring, p->T, p->HW, p->cov, p->cov_work, st)) != HV_OK)
-            return r;
-        if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, p->weights, p->eig_work, st)) != HV_OK)
-            return r;
-        if (p->view_on_tc && (r = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, st)) != HV_OK)
-            return r;
-    }
-    // converts.cc:50-62: PCA views are scaled by (2 << 16) - 1
-    // PCA views are scaled by (2 << 16) - 1 (converts.cc:50-62); a moment replaces the frame after
-    // that scaling (pipe.cc:346, fourier_transform.cc:317-338) and is not scaled
-    const float scale = (pca && !p->bin_w) ? static_cast<float>((2 << 16) - 1) : 1.0f;
-    const bool shift_in_view = s.fft_shift && !unwrap;
     const bool renorm = s.renorm != 0;
-    const float* frame = p->view;
-    if (!unwrap)
-    {
-        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, scale, shift_in_view ? 1 : 0,
-                                         p->view, renorm ? p->partials : nullptr, p->view_tc_work, st, nullptr,
-                                         p->bin_w)
-                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale,
-                                           shift_in_view ? 1 : 0, p->view, renorm ? p->partials : nullptr, st,
-                                           nullptr, p->bin_w)) != HV_OK)
-            return r;
-        if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
-                                          p->reduce_work, st)) != HV_OK)
-            return r;
-    }
-    else
-    {
-        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, 1.0f, 0, p->view, nullptr,
-                                         p->view_tc_work, st)
-                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, 1.0f, 0, p->view,
-                                           nullptr, st)) != HV_OK)
-            return r;
-        if ((r = unwrap_2d(p->view, p->unwrapped, p->W, p->H, p->unwrap_work, st)) != HV_OK)
-            return r;
-        if (pca && (r = renorm_shift_accumulate(p->unwrapped, p->unwrapped, p->W, p->H, nullptr, 0, nullptr, 0, 0, 0, 0,
-                                                0, st, scale)) != HV_OK)
-            return r;
-        frame = p->unwrapped;
-        if (renorm && (r = renorm_factors(frame, p->HW, s.renorm_constant, nullptr, 0, p->factors, p->reduce_work, st)) !=
-                          HV_OK)
-            return r;
-    }
+    const float* frame = nullptr;
+    int shift_after = 0;
+    if ((r = render_view(p, st, nullptr, &frame, &shift_after)) != HV_OK)
+        return r;
     // accumulation queue bookkeeping (Queue::enqueue, queue.cc:149-189)
     int slot = 0, start = 0, count = 0;
     if (p->A > 0)
@@ -328,7 +405,6 @@ hv_status render(hv_pipe* p)
         start = p->acc_start;
         count = p->acc_size;
     }
-    const int shift_after = (s.fft_shift && unwrap) ? 1 : 0;
     if ((r = renorm_shift_accumulate(frame, p->post, p->W, p->H, renorm ? p->factors : nullptr, shift_after,
                                      p->A > 0 ? p->acc_ring : nullptr, p->A, slot, start, count, s.log_enabled, st,
                                      1.0f)) != HV_OK)
@@ -562,7 +638,7 @@ hv_pipe* pipe_create_served(const hv_frame_desc* fd, const hv_settings* settings
 
 bool served_graphable(const hv_pipe* p)
 {
-    return p->s.time_transformation != HV_TIME_PCA && !uses_unwrap(p->s);
+    return !uses_eig(p->s) && !uses_unwrap(p->s) && !uses_phase_increase(p->s);
 }
 
 bool served_plan(hv_pipe* p, CycleCtl* ctl, ServedCycle* c)
@@ -657,55 +733,11 @@ hv_status served_record(hv_pipe* p, const CycleCtl* ctl, const ServedCycle& c, b
     }
     if (!gated && !c.render)
         return HV_OK;
-    const bool pca = uses_pca(s);
-    const bool unwrap = uses_unwrap(s);
-    if (pca)
-    {
-        // not gated by the block: served PCA cycles are launched eagerly (render cycles only)
-        if ((r = pca_covariance(p->ring, p->T, p->HW, p->cov, p->cov_work, st)) != HV_OK)
-            return r;
-        if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, p->weights, p->eig_work, st)) != HV_OK)
-            return r;
-        if (p->view_on_tc && (r = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, st)) != HV_OK)
-            return r;
-    }
-    // PCA views are scaled by (2 << 16) - 1 (converts.cc:50-62); a moment replaces the frame after
-    // that scaling (pipe.cc:346, fourier_transform.cc:317-338) and is not scaled
-    const float scale = (pca && !p->bin_w) ? static_cast<float>((2 << 16) - 1) : 1.0f;
-    const bool shift_in_view = s.fft_shift && !unwrap;
     const bool renorm = s.renorm != 0;
-    const float* frame = p->view;
-    if (!unwrap)
-    {
-        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, scale, shift_in_view ? 1 : 0,
-                                         p->view, renorm ? p->partials : nullptr, p->view_tc_work, st, ctl, p->bin_w)
-                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale,
-                                           shift_in_view ? 1 : 0, p->view, renorm ? p->partials : nullptr, st, ctl,
-                                           p->bin_w)) != HV_OK)
-            return r;
-        if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
-                                          p->reduce_work, st, ctl)) != HV_OK)
-            return r;
-    }
-    else
-    {
-        // not gated by the block: served unwrap cycles are launched eagerly (render cycles only)
-        if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, 1.0f, 0, p->view, nullptr,
-                                         p->view_tc_work, st, ctl)
-                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, 1.0f, 0, p->view,
-                                           nullptr, st, ctl)) != HV_OK)
-            return r;
-        if ((r = unwrap_2d(p->view, p->unwrapped, p->W, p->H, p->unwrap_work, st)) != HV_OK)
-            return r;
-        if (pca && (r = renorm_shift_accumulate(p->unwrapped, p->unwrapped, p->W, p->H, nullptr, 0, nullptr, 0, 0, 0, 0,
-                                                0, st, scale, ctl)) != HV_OK)
-            return r;
-        frame = p->unwrapped;
-        if (renorm && (r = renorm_factors(frame, p->HW, s.renorm_constant, nullptr, 0, p->factors, p->reduce_work, st,
-                                          ctl)) != HV_OK)
-            return r;
-    }
-    const int shift_after = (s.fft_shift && unwrap) ? 1 : 0;
+    const float* frame = nullptr;
+    int shift_after = 0;
+    if ((r = render_view(p, st, ctl, &frame, &shift_after)) != HV_OK)
+        return r;
     if ((r = renorm_shift_accumulate(frame, p->post, p->W, p->H, renorm ? p->factors : nullptr, shift_after,
                                      p->A > 0 ? p->acc_ring : nullptr, p->A, 0, 0, 0, s.log_enabled, st, 1.0f, ctl)) !=
         HV_OK)

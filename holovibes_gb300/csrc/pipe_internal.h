@@ -23,6 +23,7 @@ struct hv_pipe
     size_t HW = 0;
     int depth = 2, kind = 0;
     int B = 1, T = 1, S = 1, K = 1, pmin = 0, pmax = 0, A = 0;
+    int qmin = 0, qn = 1;  // SSA_STFT eigenvector columns kept
 
     // device buffers
     std::vector<void*> allocs;
@@ -56,6 +57,11 @@ struct hv_pipe
     bool view_on_tc = false;  // K-bin contraction on the tensor cores (hv_time_view_tc)
     float* bin_w = nullptr;   // moments: per-bin weights f_k^n (null for the other views)
     void* view_tc_work = nullptr;
+    // phase increase: previous p plane, previous increment, min / max partials, windows rendered
+    float2* pi_pred = nullptr;
+    float* pi_hist = nullptr;
+    float2* pi_minmax = nullptr;
+    uint64_t pi_count = 0;
 
     // input ring of batch slots
     uint8_t* in_ring = nullptr;
@@ -115,7 +121,7 @@ hv_pipe* pipe_create_served(const hv_frame_desc* fd, const hv_settings* s, cudaS
 // Device footprint of a served pipe.
 size_t served_footprint(const hv_frame_desc& fd, const hv_settings& s);
 // Whether the pipe's cycle can be captured in a CUDA graph (every kernel of its cycle is gated by the
-// control block): STFT or no time transform, no 2-D unwrap.
+// control block): STFT or no time transform, no 2-D unwrap, no phase increase.
 bool served_graphable(const hv_pipe* p);
 // Takes the oldest ready batch (if any) and advances the host bookkeeping of the cycle (stride gate,
 // ring, accumulation queue, autocontrast gating, output slot); fills the control block.

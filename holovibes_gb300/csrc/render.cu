@@ -155,7 +155,10 @@ __global__ void k_unwrap_rescale(float* io, size_t n, const unsigned int* minmax
     {
         const float in = io[e];
         float r;
-        if (mn < 0.f)
+        // a constant frame maps to 0 (the reference divides 0 by 0 there)
+        if (mx == mn)
+            r = 0.0f;
+        else if (mn < 0.f)
             r = __fdiv_rn(__fadd_rn(in, fabsf(mn)), __fadd_rn(fabsf(mn), mx)) * 65535.0f;
         else
             r = __fdiv_rn(__fsub_rn(in, mn), __fsub_rn(mx, mn)) * 65535.0f;
@@ -313,7 +316,8 @@ __global__ void k_renorm_factors(const double* partials, int np, size_t n, int c
         for (int i = 0; i < (blockDim.x + 31) / 32; ++i)
             t += red[i];
         factors[0] = static_cast<float>(1 << c);
-        factors[1] = __fdiv_rn(static_cast<float>(n), static_cast<float>(t));
+        // a zero-sum frame (all zero) stays zero instead of the reference's N / 0 = inf, 0 * inf = NaN
+        factors[1] = t != 0.0 ? __fdiv_rn(static_cast<float>(n), static_cast<float>(t)) : 0.0f;
     }
 }
 

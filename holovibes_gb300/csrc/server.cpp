@@ -456,7 +456,7 @@ hv_status run_bucket(hv_server* s, Bucket* b, bool* did_work, int64_t* wait_us)
             if (cyc[i].active)
                 ++s->eager_cycles;
             if (cyc[i].render)
-                m->steady = true;  // joins the graphs from the next pass
+                m->steady = served_graphable(m->p);  // joins the graphs from the next pass
         }
         if ((r = served_complete(m->p, cyc[i], b->stream)) != HV_OK)
             return r;
@@ -508,7 +508,7 @@ hv_status run_bucket_streams(hv_server* s, Bucket* b, bool* did_work)
             if (cyc.active)
                 ++s->eager_cycles;
             if (cyc.render)
-                m->steady = true;
+                m->steady = served_graphable(m->p);
         }
         if ((r = served_complete(m->p, cyc, st)) != HV_OK)
             return r;
@@ -709,7 +709,9 @@ hv_status hv_server_open_stream(hv_server* s, const hv_frame_desc* fd, const hv_
             }
         if (!bucket)
         {
-            const bool graphable = vs.time_transformation != HV_TIME_PCA && !(vs.image_type == HV_IMG_ARGUMENT && vs.unwrap_2d);
+            // the key fixes the time transformation; members whose own cycle is not fully gated
+            // (unwrap, phase increase) never become steady and stay eager
+            const bool graphable = vs.time_transformation != HV_TIME_PCA && vs.time_transformation != HV_TIME_SSA_STFT;
             if ((r = make_bucket(key, graphable, &bucket)) != HV_OK)
             {
                 s->used -= fp;

@@ -173,14 +173,16 @@ int img_from_string(const std::string& s)
         return HV_IMG_SQUARED_MODULUS;
     if (s == "ARGUMENT")
         return HV_IMG_ARGUMENT;
+    if (s == "PHASE_INCREASE")
+        return HV_IMG_PHASE_INCREASE;
     if (s == "MOMENTS_0")
         return HV_IMG_MOMENTS_0;
     if (s == "MOMENTS_1")
         return HV_IMG_MOMENTS_1;
     if (s == "MOMENTS_2")
         return HV_IMG_MOMENTS_2;
-    if (s == "PHASE_INCREASE" || s == "COMPOSITE")
-        return 100;  // reference image types outside this path
+    if (s == "COMPOSITE")
+        return 100;  // reference image type outside this path
     return -1;
 }
 
@@ -299,6 +301,8 @@ hv_status settings_from_value(const json::Value& doc, hv_settings* s, bool lenie
         {{"view", "renorm"}, 2, &out.renorm},
         {{"view", "z", "start"}, 0, &out.p_start},
         {{"view", "z", "width"}, 0, &out.p_width},
+        {{"view", "z2", "start"}, 0, &out.q_start},
+        {{"view", "z2", "width"}, 0, &out.q_width},
         {{"view", "window", "xy", "output_image_accumulation"}, 0, &out.accumulation},
         {{"view", "window", "xy", "log_enabled"}, 2, &out.log_enabled},
         {{"view", "window", "xy", "contrast", "enabled"}, 2, &out.contrast_enabled},
@@ -416,6 +420,8 @@ void settings_to_value(const hv_settings* s, json::Value& doc)
     set_bool(doc, {"view", "renorm"}, s->renorm != 0);
     set_num(doc, {"view", "z", "start"}, s->p_start);
     set_num(doc, {"view", "z", "width"}, s->p_width);
+    set_num(doc, {"view", "z2", "start"}, s->q_start);
+    set_num(doc, {"view", "z2", "width"}, s->q_width);
     set_num(doc, {"view", "window", "xy", "output_image_accumulation"}, s->accumulation);
     set_bool(doc, {"view", "window", "xy", "log_enabled"}, s->log_enabled != 0);
     set_bool(doc, {"view", "window", "xy", "contrast", "enabled"}, s->contrast_enabled != 0);
@@ -504,23 +510,28 @@ hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd)
         s->p_start = upper;
     if (s->p_start < 0)
         s->p_start = 0;
+    // check_q_limits (transform_api.cc:208-225)
+    upper = T - 1;
+    if (s->q_width > upper)
+        s->q_width = upper;
+    if (s->q_width < 0)
+        s->q_width = 0;
+    upper -= s->q_width;
+    if (s->q_start > upper)
+        s->q_start = upper;
+    if (s->q_start < 0)
+        s->q_start = 0;
     if (s->accumulation < 0)
         s->accumulation = 0;
     if (s->output_buffer_size < 1)
         s->output_buffer_size = 1;
-    if (s->image_type != HV_IMG_MODULUS && s->image_type != HV_IMG_SQUARED_MODULUS && s->image_type != HV_IMG_ARGUMENT &&
-        s->image_type != HV_IMG_MOMENTS_0 && s->image_type != HV_IMG_MOMENTS_1 && s->image_type != HV_IMG_MOMENTS_2)
+    if (s->image_type < HV_IMG_MODULUS || s->image_type > HV_IMG_MOMENTS_2 || s->image_type == 4)
     {
-        set_last_error_msg("image type outside the hologram path (modulus, squared modulus, argument, moments)");
+        set_last_error_msg("image type outside the hologram path (composite or unknown)");
         return HV_WRONG_IMG_TYPE;
     }
     if (s->camera_fps < 0)
         s->camera_fps = 0;
-    if (s->time_transformation == HV_TIME_SSA_STFT)
-    {
-        set_last_error_msg("SSA_STFT is not implemented");
-        return HV_ERR_UNSUPPORTED;
-    }
     if (fd)
     {
         if (fd->width == 0 || fd->height == 0)
@@ -541,7 +552,7 @@ hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd)
             set_last_error_msg("fftshift needs even width and height");
             return HV_INVALID_VALUE;
         }
-        if (s->unwrap_2d && s->image_type == HV_IMG_ARGUMENT &&
+        if (s->unwrap_2d && (s->image_type == HV_IMG_ARGUMENT || s->image_type == HV_IMG_PHASE_INCREASE) &&
             (!fft_size_supported(fd->width) || !fft_size_supported(fd->height)))
         {
             set_last_error_msg("frame size not supported by the unwrap FFT");

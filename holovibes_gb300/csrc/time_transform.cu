@@ -9,6 +9,10 @@
 //   views          Backend/cuda_sources/tools_conversion.cu:11-103,199-232 (mean over [pmin, pmax]
 //                  of hypotf, hypotf^2 or atan2)
 //   PCA x131071    Backend/sources/compute/converts.cc:50-62
+//   SSA_STFT       Backend/sources/compute/fourier_transform.cc:379-444: eigenvectors q..q+q_acc of
+//                  H^H H kept, tmp = V V^H, p_acc = FFT_t(H tmp)
+//   phase increase Backend/cuda_sources/tools_unwrap.cu:210-267, converts.cc:251-300,
+//                  rescale_float tools_conversion.cu:245-313
 //
 // GB300 design: only the K = pmax - pmin + 1 bins the view reads are computed, as a dense
 // contraction X[k][pix] = sum_t W[k][t] ring[t][pix] with W = DFT twiddles (STFT) or the selected
@@ -1246,6 +1250,207 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     k_eig_sort<<<T, 128, 0, st>>>(ev_unsorted, V, T, evals, evecs, pmin, pmax, weights);
     HV_LAUNCH_CHECK();
     count_launch(2);
+    return HV_OK;
+}
+
+// ------------------------------------------------------------------------------ SSA_STFT
+// p_acc = FFT_t(H V_q V_q^H) (fourier_transform.cc:379-444) restricted to the bins pmin..pmin+K-1
+// is one more set of projection weights over the ring:
+//   w[k][s] = sum_{j in q} V[s][j] c[j][k],   c[j][k] = sum_t conj(V[t][j]) exp(-2 pi i (pmin+k) t / T),
+// computed in FP64 from the FP64 eigenvectors (column-major, evecs[j*T + t]); one CTA per bin.
+__global__ void k_ssa_weights(const double2* __restrict__ evecs, int T, int qmin, int qn, int pmin, float2* w)
+{
+    extern __shared__ double2 s_c[];  // qn coefficients of this bin
+    const int k = blockIdx.x;
+    const long long p = pmin + k;
+    for (int j = threadIdx.x; j < qn; j += blockDim.x)
+    {
+        const double2* v = evecs + static_cast<size_t>(qmin + j) * T;
+        double cr = 0.0, ci = 0.0;
+        for (int t = 0; t < T; ++t)
+        {
+            const long long m = (p * t) % T;
+            double sn, cs;
+            sincospi(-2.0 * static_cast<double>(m) / static_cast<double>(T), &sn, &cs);
+            const double2 x = v[t];
+            // conj(x) * (cs + i sn)
+            cr += x.x * cs + x.y * sn;
+            ci += x.x * sn - x.y * cs;
+        }
+        s_c[j] = make_double2(cr, ci);
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < T; s += blockDim.x)
+    {
+        double wr = 0.0, wi = 0.0;
+        for (int j = 0; j < qn; ++j)
+        {
+            const double2 v = evecs[static_cast<size_t>(qmin + j) * T + s];
+            const double2 c = s_c[j];
+            wr += v.x * c.x - v.y * c.y;
+            wi += v.x * c.y + v.y * c.x;
+        }
+        w[static_cast<size_t>(k) * T + s] = make_float2(static_cast<float>(wr), static_cast<float>(wi));
+    }
+}
+
+hv_status ssa_weights(const double2* evecs, int T, int qmin, int qn, int pmin, int K, float2* weights, cudaStream_t st)
+{
+    if (T <= 0 || K <= 0 || qmin < 0 || qn < 1 || qmin + qn > T || pmin < 0 || pmin + K > T || !evecs || !weights)
+        return HV_INVALID_VALUE;
+    if (static_cast<size_t>(qn) * sizeof(double2) > 48 * 1024)
+    {
+        set_last_error_msg("ssa_weights: more than 3072 eigenvectors kept");
+        return HV_ERR_UNSUPPORTED;
+    }
+    k_ssa_weights<<<K, 256, static_cast<size_t>(qn) * sizeof(double2), st>>>(evecs, T, qmin, qn, pmin, weights);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+// ------------------------------------------------------------------------------ phase increase
+// The stored p plane X = sum_t ring[t] w[t] (fourier_transform.cc:446-460, w = the first row of
+// the view's weights), d = arg(X conj(pred)) (kernel_compute_angle_mult), out = d + the previous
+// d (a history of one frame: UnwrappingResources capacity 1, kernel_correct_angles), pred = X.
+// `first` gives d = 0 (pred = X); `use_hist` is off until one d is stored. Per-CTA min / max of
+// out go to mm[blockIdx.x] for the rescale.
+constexpr int PI_THREADS = 256;
+
+__global__ void __launch_bounds__(PI_THREADS) k_phase_increase(const float2* __restrict__ ring, int T, size_t HW,
+                                                               const float2* __restrict__ w, float2* pred, float* hist,
+                                                               int first, int use_hist, float* out, float2* mm)
+{
+    extern __shared__ float2 s_w[];
+    __shared__ float s_mn[PI_THREADS / 32], s_mx[PI_THREADS / 32];
+    for (int t = threadIdx.x; t < T; t += blockDim.x)
+        s_w[t] = w[t];
+    __syncthreads();
+    const size_t i = static_cast<size_t>(blockIdx.x) * PI_THREADS + threadIdx.x;
+    float mn = INFINITY, mx = -INFINITY;
+    if (i < HW)
+    {
+        float xr = 0.f, xi = 0.f;
+        for (int t = 0; t < T; ++t)
+        {
+            const float2 x = __ldcs(ring + static_cast<size_t>(t) * HW + i);
+            const float2 c = s_w[t];
+            xr = fmaf(x.x, c.x, fmaf(-x.y, c.y, xr));
+            xi = fmaf(x.x, c.y, fmaf(x.y, c.x, xi));
+        }
+        // the first window compares the plane with itself: its increment is 0 (the reference takes
+        // atan2 of the rounding residue of X conj(X) there)
+        float d = 0.0f;
+        if (!first)
+        {
+            const float2 pr = pred[i];
+            const float re = xr * pr.x + xi * pr.y;
+            const float im = xi * pr.x - xr * pr.y;
+            d = atan2f(im, re);
+        }
+        const float o = use_hist ? d + hist[i] : d;
+        hist[i] = d;
+        pred[i] = make_float2(xr, xi);
+        out[i] = o;
+        mn = mx = o;
+    }
+    for (int off = 16; off > 0; off >>= 1)
+    {
+        mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, off));
+        mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        s_mn[threadIdx.x >> 5] = mn;
+        s_mx[threadIdx.x >> 5] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        for (int k = 1; k < PI_THREADS / 32; ++k)
+        {
+            mn = fminf(mn, s_mn[k]);
+            mx = fmaxf(mx, s_mx[k]);
+        }
+        mm[blockIdx.x] = make_float2(mn, mx);
+    }
+}
+
+// rescale_float (tools_conversion.cu:275-313): out = (in + |min|) * 65535 / (|max| + |min|), with
+// min and max from the first 128 blocks of 128 pixels of the reference's reduction, i.e. over
+// pixels [0, min(HW, 16384)) (the whole frame below that size, where the reference reads past its
+// block results). Then the PCA scale (converts.cc:50-62) as a separate rounding. Every CTA
+// reduces the min / max partials of the prefix itself.
+__global__ void k_rescale_float(const float* __restrict__ in, size_t HW, const float2* __restrict__ mm, int nmm,
+                                float post_scale, float* __restrict__ out)
+{
+    __shared__ float s_mn, s_mx;
+    if (threadIdx.x < 32)
+    {
+        float mn = INFINITY, mx = -INFINITY;
+        for (int k = threadIdx.x; k < nmm; k += 32)
+        {
+            const float2 v = mm[k];
+            mn = fminf(mn, v.x);
+            mx = fmaxf(mx, v.y);
+        }
+        for (int off = 16; off > 0; off >>= 1)
+        {
+            mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, off));
+            mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
+        }
+        if (threadIdx.x == 0)
+        {
+            s_mn = mn;
+            s_mx = mx;
+        }
+    }
+    __syncthreads();
+    const float amin = fabsf(s_mn), den = __fadd_rn(fabsf(s_mx), amin);
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < HW;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        // an all-zero prefix (the first window) maps to 0 instead of the reference's 0 / 0
+        float v = den > 0.0f ? __fdiv_rn(__fmul_rn(__fadd_rn(in[i], amin), 65535.0f), den) : 0.0f;
+        if (post_scale != 1.0f)
+            v = __fmul_rn(v, post_scale);
+        out[i] = v;
+    }
+}
+
+size_t phase_increase_minmax_count(size_t HW) { return (HW + PI_THREADS - 1) / PI_THREADS; }
+
+hv_status phase_increase(const float2* ring, int T, size_t HW, const float2* w, float2* pred, float* hist, int first,
+                         int use_hist, float* out, float2* mm, cudaStream_t st)
+{
+    if (T <= 0 || HW == 0 || !ring || !w || !pred || !hist || !out || !mm)
+        return HV_INVALID_VALUE;
+    const size_t grid = phase_increase_minmax_count(HW);
+    if (grid > 0x7fffffffu)
+        return HV_INVALID_VALUE;
+    if (static_cast<size_t>(T) * sizeof(float2) > 40 * 1024)
+    {
+        set_last_error_msg("phase_increase: time window above 5120 frames");
+        return HV_ERR_UNSUPPORTED;
+    }
+    k_phase_increase<<<static_cast<unsigned>(grid), PI_THREADS, static_cast<size_t>(T) * sizeof(float2), st>>>(
+        ring, T, HW, w, pred, hist, first, use_hist, out, mm);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+hv_status rescale_float(const float* in, size_t HW, const float2* mm, float post_scale, float* out, cudaStream_t st)
+{
+    if (HW == 0 || !in || !mm || !out)
+        return HV_INVALID_VALUE;
+    const size_t prefix = HW < 16384 ? HW : 16384;
+    const int nmm = static_cast<int>((prefix + PI_THREADS - 1) / PI_THREADS);
+    size_t grid = (HW + 255) / 256;
+    grid = grid < 152 * 16 ? grid : 152 * 16;
+    k_rescale_float<<<static_cast<unsigned>(grid), 256, 0, st>>>(in, HW, mm, nmm, post_scale, out);
+    HV_LAUNCH_CHECK();
+    count_launch();
     return HV_OK;
 }
 

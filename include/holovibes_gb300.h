@@ -60,15 +60,17 @@ typedef struct hv_frame_desc
 enum { HV_SPACE_NONE = 0, HV_SPACE_FRESNELTR = 1, HV_SPACE_ANGULARSP = 2 };
 /* TimeTransformation (Backend/includes/enum/enum_time_transformation.hh:16-22). */
 enum { HV_TIME_NONE = 0, HV_TIME_STFT = 1, HV_TIME_PCA = 2, HV_TIME_SSA_STFT = 3 };
-/* ImgType (Backend/includes/enum/enum_img_type.hh:16-26); only the first three are on this path. */
-/* ImgType values of the reference (enum_img_type.hh:15-25); PHASE_INCREASE (3) and COMPOSITE (4)
- * are outside this path. Moments: sum over the selected bins of |X_k|^2 f_k^n (f_k the signed
- * FFT frequency in units of camera_fps / T), replacing the view frame. */
+/* ImgType values of the reference (Backend/includes/enum/enum_img_type.hh:15-25); COMPOSITE (4)
+ * is outside this path. Moments: sum over the selected bins of |X_k|^2 f_k^n (f_k the signed
+ * FFT frequency in units of camera_fps / T), replacing the view frame. Phase increase: the phase
+ * of the p plane against the previous window's (plus the previous increment), rescaled to
+ * [0, 65535] (converts.cc:251-300). */
 enum
 {
     HV_IMG_MODULUS = 0,
     HV_IMG_SQUARED_MODULUS = 1,
     HV_IMG_ARGUMENT = 2,
+    HV_IMG_PHASE_INCREASE = 3,
     HV_IMG_MOMENTS_0 = 5,
     HV_IMG_MOMENTS_1 = 6,
     HV_IMG_MOMENTS_2 = 7
@@ -113,6 +115,8 @@ typedef struct hv_settings
     int32_t output_buffer_size;      /* advanced.buffer_size.output: output frames kept */
     int32_t input_buffer_size;       /* advanced.buffer_size.input: raw frames kept */
     int32_t camera_fps;              /* CameraFps input setting (.holo info.camera_fps): moment frequencies */
+    int32_t q_start;                 /* view.z2.start: first eigenvector kept by SSA_STFT */
+    int32_t q_width;                 /* view.z2.width: eigenvectors kept by SSA_STFT (0 = all) */
 } hv_settings;
 
 /* ------------------------------------------------------------------------------------------
@@ -263,6 +267,27 @@ hv_status hv_moment_bin_weights(float* bin_w_f32, int T, int pmin, int pmax, int
                                 void* stream);
 hv_status hv_time_moments(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
                           const float* bin_w_f32, int shift, float* out_f32, double* partials_f64, void* stream);
+/* SSA_STFT weights (fourier_transform.cc:379-444): with V the eigenvectors of hv_pca_eigh
+ * (complex128, column-major, ascending eigenvalues) and Q the columns q_start..q_start+q_width-1
+ * (all T columns when q_width == 0), p_acc = FFT_t(H V_Q V_Q^H), so bin pmin+k of p_acc is the
+ * ring contracted with W[k][s] = sum_{j in Q} V[s][j] sum_t conj(V[t][j]) exp(-2*pi*i*(pmin+k)*t/T).
+ * Writes W for k <= pmax-pmin (complex64, same layout as hv_stft_weights); FP64 arithmetic. */
+hv_status hv_ssa_weights(const void* eigenvectors_c128, int T, int q_start, int q_width, int pmin, int pmax,
+                         void* weights_c64, void* stream);
+/* Phase increase (phase_increase, tools_unwrap.cu:210-267, with the one-frame history that
+ * converts.cc:251-263 sets up): X = sum_t ring[t] w[t] (the stored p plane, w = one row of
+ * weights), d = arg(X conj(pred)), out = d + hist when use_hist, then hist = d and pred = X.
+ * first != 0 takes pred = X. pred (complex64) and hist (float) are W*H device buffers kept by the
+ * caller between windows; `minmax` needs hv_phase_increase_workspace(W*H) bytes and feeds
+ * hv_rescale_float. */
+hv_status hv_phase_increase(const void* ring_c64, int T, int width, int height, const void* w_c64, void* pred_c64,
+                            float* hist_f32, int first, int use_hist, float* out_f32, void* minmax, void* stream);
+size_t hv_phase_increase_workspace(size_t npix);
+/* rescale_float (tools_conversion.cu:275-313) of a frame written by hv_phase_increase:
+ * out = (in + |min|) * 65535 / (|max| + |min|) * post_scale, min / max over the first
+ * min(npix, 16384) pixels as the reference's block reduction reads them. */
+hv_status hv_rescale_float(const float* in_f32, size_t npix, const void* minmax, float post_scale, float* out_f32,
+                           void* stream);
 /* STFT weights W[k][t] = exp(-2*pi*i*(pmin+k)*t/T), k <= pmax-pmin, computed in FP64. */
 hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* stream);
 

@@ -332,6 +332,73 @@ def pca_project(storage: np.ndarray, V: np.ndarray, pmin: int, pmax: int) -> np.
 
 
 # ----------------------------------------------------------------------------------------
+# SSA_STFT (fourier_transform.cc:379-444)
+# ----------------------------------------------------------------------------------------
+
+
+def ssa_q_range(q_start: int, q_width: int, T: int) -> tuple[int, int]:
+    """Eigenvector columns kept (fourier_transform.cc:409-412): [q, q + q_acc), every column
+    when the width is 0."""
+    return (q_start, q_width) if q_width != 0 else (0, T)
+
+
+def ssa_stft_bins(storage: np.ndarray, V: np.ndarray, q_start: int, q_width: int, pmin: int, pmax: int) -> np.ndarray:
+    """V's columns outside [q, q + q_acc) zeroed (cudaMemsetAsync :413-415), tmp = V V^H
+    (matrix_multiply_complex OP_N / OP_C), P = H tmp, then the STFT of P along time (stft plan
+    over the p_acc buffer); bins pmin..pmax."""
+    T = storage.shape[0]
+    q, qn = ssa_q_range(q_start, q_width, T)
+    Vq = np.zeros_like(V)
+    Vq[:, q:q + qn] = V[:, q:q + qn]
+    tmp = Vq @ Vq.conj().T
+    Hm = storage.reshape(T, -1).T  # [HW, T] column-major H
+    P = Hm @ tmp
+    return stft_bins(P.T.reshape(storage.shape), pmin, pmax)
+
+
+# ----------------------------------------------------------------------------------------
+# phase increase (tools_unwrap.cu:210-267, converts.cc:251-300, tools_conversion.cu:245-313)
+# ----------------------------------------------------------------------------------------
+
+
+class PhaseIncrease:
+    """phase_increase with UnwrappingResources of capacity 1 (converts.cc:257-259): the newest
+    increment d = atan2 of cur * conj(pred) (kernel_compute_angle_mult), corrected by the one
+    stored increment (kernel_correct_angles), then stored; pred <- cur. The first call takes
+    pred = cur (the function's first_time copy), so its increment is 0 (exactly 0 here; the
+    reference takes atan2 of the rounding residue of cur * conj(cur))."""
+
+    def __init__(self):
+        self.pred = None
+        self.hist = None
+
+    def push(self, cur: np.ndarray) -> np.ndarray:
+        if self.pred is None:
+            d = np.zeros(cur.shape)
+        else:
+            cp = cur * np.conj(self.pred)
+            d = np.arctan2(cp.imag, cp.real)
+        out = d + self.hist if self.hist is not None else d.copy()
+        self.hist = d
+        self.pred = cur.copy()
+        return out
+
+
+def rescale_float(img: np.ndarray) -> np.ndarray:
+    """rescale_float (tools_conversion.cu:275-313): (x + |min|) * 65535 / (|max| + |min|) in
+    float32, min / max taken from the first 128 block results of 128 pixels each, i.e. over the
+    first min(N, 16384) pixels (the whole frame below that: the reference reads past its results)."""
+    f = img.astype(F32)
+    n = min(f.size, 16384)
+    head = f.reshape(-1)[:n]
+    amin = np.abs(head.min())
+    amax = np.abs(head.max())
+    if amax + amin == 0:
+        return np.zeros_like(f)  # an all-zero prefix (first window): 0 instead of 0 / 0
+    return ((f + amin) * F32(65535.0)) / (amax + amin)
+
+
+# ----------------------------------------------------------------------------------------
 # a13-a16: views (tools_conversion.cu:11-103,199-218; converts.cc:50-62)
 # ----------------------------------------------------------------------------------------
 
@@ -436,6 +503,8 @@ def unwrap_2d(phase: np.ndarray) -> np.ndarray:
 def rescale_unwrap2d(img: np.ndarray) -> np.ndarray:
     """(in+|min|)/(|min|+max)*65535 if min<0 else (in-min)/(max-min)*65535 (tools_conversion.cu:315-335)."""
     mn, mx = img.min(), img.max()
+    if mx == mn:
+        return np.zeros_like(img)  # a constant frame: 0 instead of 0 / 0
     if mn < 0:
         return (img + abs(mn)) / (abs(mn) + mx) * 65535.0
     return (img - mn) / (mx - mn) * 65535.0
@@ -447,8 +516,11 @@ def rescale_unwrap2d(img: np.ndarray) -> np.ndarray:
 
 
 def renormalize(img: np.ndarray, renorm_constant: int) -> np.ndarray:
-    """x <- x * 2^c * N / sum(x)."""
-    return img * float(1 << renorm_constant) * (img.size / img.sum(dtype=np.float64))
+    """x <- x * 2^c * N / sum(x); a zero-sum frame becomes 0 (the reference's N / 0 gives NaN)."""
+    total = img.sum(dtype=np.float64)
+    if total == 0:
+        return np.zeros_like(img)
+    return img * float(1 << renorm_constant) * (img.size / total)
 
 
 # ----------------------------------------------------------------------------------------
@@ -567,6 +639,8 @@ class OracleSettings:
     unwrap_2d: bool = False
     lens_mode: str = "fp64"
     camera_fps: float = 0.0  # moments: frequencies in units of camera_fps / T
+    q_start: int = 0  # SSA_STFT eigenvector range (view.z2)
+    q_width: int = 0
 
 
 @dataclass
@@ -595,6 +669,7 @@ class OraclePipe:
         self.autocontrast_pending = s.contrast_enabled and s.contrast_auto_refresh
         self.crange = (s.contrast_min, s.contrast_max)
         self.last_V = None
+        self.phase_increase = PhaseIncrease() if s.image_type == "PHASE_INCREASE" else None
 
     def process_batch(self, raw: np.ndarray, convert_f32=True) -> OracleOutput | None:
         s = self.s
@@ -621,11 +696,25 @@ class OraclePipe:
             _, V = pca_eigh(cov)
             self.last_V = V
             planes = pca_project(self.ring.data, V, pmin, pmax)
+        elif s.time_transformation == "SSA_STFT":
+            cov = pca_covariance(self.ring.data)
+            _, V = pca_eigh(cov)
+            self.last_V = V
+            planes = ssa_stft_bins(self.ring.data, V, s.q_start, s.q_width, pmin, pmax)
         else:
             planes = self.ring.data[pmin:pmax + 1]
         if s.image_type.startswith("MOMENTS_"):
             # the moment replaces the post-processing frame after the PCA scaling (pipe.cc:346)
             img = moments(planes, pmin, T, s.camera_fps, int(s.image_type[-1]))
+        elif s.image_type == "PHASE_INCREASE":
+            # the stored p plane (fourier_transform.cc:446-460): bin / component p_start
+            first = self.phase_increase.pred is None
+            d = self.phase_increase.push(planes[0])
+            if s.unwrap_2d:
+                # the first window's increments are all 0: the zero frame, not an unwrap of residues
+                img = np.zeros(d.shape) if first else rescale_unwrap2d(unwrap_2d(d))
+            else:
+                img = rescale_float(d).astype(np.float64)
         else:
             img = view(planes, s.image_type)
         if s.image_type == "ARGUMENT" and s.unwrap_2d:

@@ -50,8 +50,15 @@ def test_validate_rules():
         hv.Settings.defaults().update(space_transformation=2).validate(hv.FrameDescriptor(1000, 512, 2))
     assert e.value.status == hv.HV_ERR_UNSUPPORTED
     with pytest.raises(hv.HoloError) as e:
-        hv.Settings.defaults().update(image_type=3).validate(fd)
+        hv.Settings.defaults().update(image_type=4).validate(fd)  # COMPOSITE is outside the path
     assert e.value.status == hv.HV_WRONG_IMG_TYPE
+    # check_q_limits (transform_api.cc:208-225): width <= T-1, start <= T-1-width
+    q = hv.Settings.defaults().update(time_transformation=3, time_transformation_size=16, q_start=15,
+                                      q_width=20).validate(fd)
+    assert (q.q_width, q.q_start) == (15, 0)
+    q = hv.Settings.defaults().update(time_transformation=3, time_transformation_size=16, q_start=14,
+                                      q_width=2).validate(fd)
+    assert (q.q_width, q.q_start) == (2, 13)
 
 
 def test_footprint_scales_with_ring():

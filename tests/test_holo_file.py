@@ -18,14 +18,14 @@ def _settings():
         lambda_=785e-9, z_distance=0.45, pixel_size=12.0, image_type=1, p_start=3, p_width=2, fft_shift=1, renorm=1,
         renorm_constant=6, accumulation=3, log_enabled=0, contrast_enabled=1, contrast_auto_refresh=1,
         contrast_invert=1, contrast_min=3.0, contrast_max=4000.0, contrast_lower=0.5, contrast_upper=99.5,
-        reticle_display=1, reticle_scale=0.4, output_buffer_size=64, input_buffer_size=128)
+        reticle_display=1, reticle_scale=0.4, output_buffer_size=64, input_buffer_size=128, q_start=3, q_width=4)
 
 
 FIELDS = ["space_transformation", "time_transformation", "time_transformation_size", "time_stride", "batch_size",
           "lambda_", "z_distance", "pixel_size", "image_type", "p_start", "p_width", "fft_shift", "renorm",
           "renorm_constant", "accumulation", "log_enabled", "contrast_enabled", "contrast_auto_refresh",
           "contrast_invert", "contrast_min", "contrast_max", "contrast_lower", "contrast_upper", "reticle_display",
-          "reticle_scale", "output_buffer_size", "input_buffer_size"]
+          "reticle_scale", "output_buffer_size", "input_buffer_size", "q_start", "q_width"]
 
 
 def test_header_layout_and_round_trip(tmp_path):
@@ -47,6 +47,7 @@ def test_header_layout_and_round_trip(tmp_path):
     assert cs["image_rendering"]["space_transformation"] == "ANGULARSP"
     assert cs["view"]["image_type"] == "SQUARED_MODULUS"
     assert cs["view"]["z"] == {"width": 2, "start": 3}
+    assert cs["view"]["z2"] == {"width": 4, "start": 3}
     with hv.HoloFile(path) as f:
         assert f.nb_frames == 7 and (f.fd.width, f.fd.height, f.fd.depth, f.fd.byte_endian) == (40, 24, 2, 0)
         assert np.array_equal(f.read(), frames)

@@ -139,3 +139,40 @@ def test_moment_frequencies():
     assert O.moments(X, 0, 8, 1000.0, 0)[0, 0] == 9.0  # Nyquist bin counted twice
     assert O.moments(X, 0, 8, 1000.0, 1)[0, 0] == 0.0
     assert O.moments(X, 0, 8, 1000.0, 2)[0, 0] == 937500.0
+
+
+def test_ssa_all_columns_is_stft():
+    """SSA_STFT with q width 0 keeps every eigenvector: V V^H = I, so the bins are the STFT's."""
+    import holovibes_oracle as O
+
+    rng = np.random.default_rng(3)
+    ring = rng.standard_normal((12, 5, 7)) + 1j * rng.standard_normal((12, 5, 7))
+    _, V = O.pca_eigh(O.pca_covariance(ring))
+    got = O.ssa_stft_bins(ring, V, 4, 0, 2, 6)
+    assert np.allclose(got, O.stft_bins(ring, 2, 6), rtol=1e-10, atol=1e-10)
+    # a kept range of columns projects onto that eigenspace before the STFT
+    P = O.ssa_stft_bins(ring, V, 9, 3, 0, 11)
+    Vq = V[:, 9:12]
+    proj = (ring.reshape(12, -1).T @ Vq @ Vq.conj().T).T.reshape(ring.shape)
+    assert np.allclose(P, np.fft.fft(proj, axis=0), rtol=1e-10, atol=1e-10)
+
+
+def test_phase_increase_history_and_rescale():
+    """phase_increase (tools_unwrap.cu:210-267) with a one-frame history: out_n = d_n + d_{n-1},
+    the first increment 0; rescale_float's min / max over the first 16384 pixels only."""
+    import holovibes_oracle as O
+
+    pi = O.PhaseIncrease()
+    X0 = np.exp(1j * np.array([0.1, 1.0, -2.0]))
+    X1 = X0 * np.exp(1j * np.array([0.2, 0.5, -1.5]))
+    X2 = X1 * np.exp(1j * np.array([0.3, 0.25, 3.0]))
+    assert np.allclose(pi.push(X0), 0.0)
+    assert np.allclose(pi.push(X1), [0.2, 0.5, -1.5])
+    d2 = np.angle(np.exp(1j * np.array([0.3, 0.25, 3.0])))
+    assert np.allclose(pi.push(X2), d2 + np.array([0.2, 0.5, -1.5]))
+    img = np.zeros(20000, np.float32)
+    img[:16384] = np.linspace(-1.0, 2.0, 16384)
+    img[17000] = 50.0  # past the prefix: not part of the range
+    r = O.rescale_float(img)
+    assert r[0] == 0.0 and np.isclose(r[16383], 65535.0 * 3.0 / 3.0)
+    assert r[17000] > 65535.0

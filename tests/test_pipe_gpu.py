@@ -14,9 +14,10 @@ from gpu_util import rel_l2, wrapped_diff
 import holovibes_gb300 as hv
 from holovibes_gb300.synthetic import Interferogram
 
-IMG = {0: "MODULUS", 1: "SQUARED_MODULUS", 2: "ARGUMENT", 5: "MOMENTS_0", 6: "MOMENTS_1", 7: "MOMENTS_2"}
+IMG = {0: "MODULUS", 1: "SQUARED_MODULUS", 2: "ARGUMENT", 3: "PHASE_INCREASE", 5: "MOMENTS_0", 6: "MOMENTS_1",
+       7: "MOMENTS_2"}
 SPACE = {0: "NONE", 1: "FRESNELTR", 2: "ANGULARSP"}
-TIME = {0: "NONE", 1: "STFT", 2: "PCA"}
+TIME = {0: "NONE", 1: "STFT", 2: "PCA", 3: "SSA_STFT"}
 
 
 def _oracle_settings(fd, s):
@@ -30,7 +31,8 @@ def _oracle_settings(fd, s):
         contrast_auto_refresh=bool(s.contrast_auto_refresh), contrast_invert=bool(s.contrast_invert),
         contrast_min=s.contrast_min, contrast_max=s.contrast_max, contrast_lower=s.contrast_lower,
         contrast_upper=s.contrast_upper, reticle_display=bool(s.reticle_display), reticle_scale=s.reticle_scale,
-        unwrap_2d=bool(s.unwrap_2d), lens_mode="fp64" if s.lens_mode == 0 else "ref32", camera_fps=s.camera_fps)
+        unwrap_2d=bool(s.unwrap_2d), lens_mode="fp64" if s.lens_mode == 0 else "ref32", camera_fps=s.camera_fps,
+        q_start=s.q_start, q_width=s.q_width)
 
 
 CASES = {
@@ -96,6 +98,41 @@ CASES = {
                                                       p_start=4, p_width=8, camera_fps=500, renorm=1,
                                                       contrast_enabled=1, contrast_lower=0.5,
                                                       contrast_upper=99.5), 3),
+    # SSA_STFT (fourier_transform.cc:379-444): the kept eigenvector ranges sit between well
+    # separated eigenvalues of these windows (a range that splits a near-degenerate cluster is
+    # ill-conditioned, like PCA component selection); width 0 keeps every column (= STFT)
+    "as_ssa_stft_mod_q13": (64, 64, 2, dict(space_transformation=2, time_transformation=3, time_transformation_size=16,
+                                             time_stride=8, batch_size=8, z_distance=0.3, pixel_size=20.0, q_start=13,
+                                             q_width=2, p_start=1, p_width=2, renorm=1, contrast_enabled=1,
+                                             contrast_lower=0.5, contrast_upper=99.5), 4),
+    "fresnel_ssa_sqmod_k9_tc": (64, 64, 1, dict(space_transformation=1, time_transformation=3,
+                                                 time_transformation_size=32, time_stride=16, batch_size=16,
+                                                 lambda_=785e-9, z_distance=0.45, pixel_size=12.0, image_type=1,
+                                                 q_start=29, q_width=2, p_start=2, p_width=8, renorm=1, fft_shift=1,
+                                                 contrast_enabled=1, contrast_lower=0.5, contrast_upper=99.5), 4),
+    "as_ssa_all_q_arg": (64, 64, 2, dict(space_transformation=2, time_transformation=3, time_transformation_size=16,
+                                          time_stride=8, batch_size=8, z_distance=0.3, pixel_size=20.0, image_type=2,
+                                          q_width=0, p_start=3, renorm=0, contrast_enabled=1), 3),
+    # phase increase (converts.cc:251-300): history across windows, the rescale over the first
+    # 16384 pixels (the 256 x 256 case), and the 2-D unwrap variant
+    "as_stft_phase_increase": (64, 64, 2, dict(space_transformation=2, time_transformation=1,
+                                                time_transformation_size=16, time_stride=4, batch_size=4,
+                                                z_distance=0.3, pixel_size=20.0, image_type=3, p_start=2, renorm=1,
+                                                fft_shift=1, contrast_enabled=1, contrast_lower=0.5,
+                                                contrast_upper=99.5), 8),
+    "as_stft_phase_increase_256": (256, 256, 2, dict(space_transformation=2, time_transformation=1,
+                                                      time_transformation_size=4, time_stride=4, batch_size=4,
+                                                      z_distance=0.3, pixel_size=20.0, image_type=3, p_start=1,
+                                                      renorm=0, accumulation=2, contrast_enabled=1), 4),
+    "fresnel_stft_phase_increase_unwrap": (64, 64, 1, dict(space_transformation=1, time_transformation=1,
+                                                            time_transformation_size=8, time_stride=4, batch_size=4,
+                                                            lambda_=785e-9, z_distance=0.45, pixel_size=12.0,
+                                                            image_type=3, p_start=1, unwrap_2d=1, renorm=0,
+                                                            contrast_enabled=1), 5),
+    "as_ssa_phase_increase": (64, 64, 2, dict(space_transformation=2, time_transformation=3,
+                                               time_transformation_size=16, time_stride=8, batch_size=8,
+                                               z_distance=0.3, pixel_size=20.0, image_type=3, q_start=13, q_width=2,
+                                               p_start=1, renorm=1, contrast_enabled=1), 5),
     "fresnel_stft_ref32_big_endian": (128, 64, 2, dict(space_transformation=1, time_transformation=1,
                                                         time_transformation_size=4, time_stride=4, batch_size=4,
                                                         z_distance=0.3, pixel_size=20.0, p_start=2, p_width=1,
@@ -143,6 +180,13 @@ def test_pipe_matches_oracle(cuda, case):
         if s.image_type == hv.IMG_ARGUMENT and not s.unwrap_2d:
             d = np.abs(wrapped_diff(got_f, ref.float_frame))
             assert np.mean(d > 1e-3) < 5e-3, case
+        elif s.image_type == hv.IMG_PHASE_INCREASE:
+            # an increment on the +-pi branch cut may land on the other side (a jump of 2 pi before
+            # the rescale) on a few pixels; the rest within the float bar
+            d = np.abs(got_f - ref.float_frame)
+            bad = d > 1e-3 * np.abs(ref.float_frame).max()
+            assert np.mean(bad) < 5e-3, case
+            assert rel_l2(got_f[~bad], ref.float_frame[~bad]) <= 1e-4, case
         else:
             assert rel_l2(got_f, ref.float_frame) <= 1e-4, case
         # contrast stage bit-exact on the GPU's own float frame
