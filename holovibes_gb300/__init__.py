@@ -98,6 +98,11 @@ class Settings(C.Structure):
         ("camera_fps", C.c_int32),
         ("q_start", C.c_int32),
         ("q_width", C.c_int32),
+        ("filter2d_enabled", C.c_int32),
+        ("filter2d_n1", C.c_int32),
+        ("filter2d_n2", C.c_int32),
+        ("filter2d_smooth_low", C.c_int32),
+        ("filter2d_smooth_high", C.c_int32),
     ]
 
     @classmethod
@@ -191,6 +196,8 @@ def _declare(L: C.CDLL) -> None:
         "hv_fresnel_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
         "hv_angular_spectrum_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
         "hv_spatial_transform": (st, [vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, i32, i32, vp]),
+        "hv_filter2d_mask": (st, [vp, i32, i32, i32, i32, i32, i32, i32, vp]),
+        "hv_spatial_transform_filter2d": (st, [vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, i32, vp]),
         "hv_fft2d": (st, [vp, vp, i32, i32, i32, i32, f32, vp]),
         "hv_fft_rows": (st, [vp, i32, i32, vp, i32, i32, i32, vp, i32, f32, i32, i32, vp]),
         "hv_fft_cols": (st, [vp, vp, i32, i32, i32, vp, i32, f32, i32, i32, vp]),

@@ -85,6 +85,31 @@ hv_status hv_spatial_transform(const void* raw, int raw_bytes, int big_endian, i
                              static_cast<float2*>(work_c64), static_cast<float2*>(ring_c64), slot0, nslots, S(stream));
 }
 
+hv_status hv_filter2d_mask(void* dst_c64, int width, int height, int n1, int n2, int smooth_low, int smooth_high,
+                           int multiply, void* stream)
+{
+    return filter2d_mask(static_cast<float2*>(dst_c64), width, height, n1, n2, smooth_low, smooth_high, multiply,
+                         S(stream));
+}
+
+hv_status hv_spatial_transform_filter2d(const void* raw, int raw_bytes, int big_endian, int width, int height,
+                                        int batch, int space, const void* lens_c64, const void* mask_c64,
+                                        void* work_c64, void* work2_c64, void* ring_c64, int slot0, int nslots,
+                                        void* stream)
+{
+    const int kind = raw_kind(raw_bytes, big_endian);
+    if (!raw || !ring_c64 || !work_c64 || kind < 0 || width <= 0 || height <= 0 || batch < 0 || nslots <= 0 ||
+        slot0 < 0 || slot0 >= nslots || batch > nslots)
+        return HV_INVALID_VALUE;
+    if (space != HV_SPACE_ANGULARSP && !mask_c64)
+        return HV_INVALID_VALUE;
+    if (space != HV_SPACE_NONE && !lens_c64)
+        return HV_INVALID_VALUE;
+    return spatial_transform(raw, kind, width, height, batch, space, static_cast<const float2*>(lens_c64),
+                             static_cast<float2*>(work_c64), static_cast<float2*>(ring_c64), slot0, nslots, S(stream),
+                             nullptr, static_cast<const float2*>(mask_c64), static_cast<float2*>(work2_c64));
+}
+
 hv_status hv_fft2d(const void* in_c64, void* out_c64, int n0, int n1, int batch, int inverse, float scale,
                    void* stream)
 {

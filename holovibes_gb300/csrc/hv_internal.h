@@ -44,7 +44,11 @@ hv_status make_fresnel_lens(float2* lens, int W, int H, float lam, float z, floa
 hv_status make_spectral_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st);
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
                             float2* work, float2* ring, int slot0, int nslots, cudaStream_t st,
-                            const CycleCtl* ctl = nullptr);
+                            const CycleCtl* ctl = nullptr, const float2* f2d_mask = nullptr,
+                            float2* work2 = nullptr);
+// filter2D band-pass mask in FFT layout: written as complex (multiply = 0) or multiplied into dst.
+hv_status filter2d_mask(float2* dst, int W, int H, int n1, int n2, int smooth_low, int smooth_high, int multiply,
+                        cudaStream_t st);
 hv_status fft2d(const float2* in, float2* out, int n0, int n1, int batch, int inverse, float scale, cudaStream_t st);
 hv_status fft_rows_pass(const void* in, int kind, float2* out, int W, int H, int batch, const float2* premul,
                         int inverse, float scale, int slot0, int nslots, cudaStream_t st);

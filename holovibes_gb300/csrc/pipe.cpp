@@ -82,6 +82,9 @@ bool uses_eig(const hv_settings& s)
 bool uses_phase_increase(const hv_settings& s) { return s.image_type == HV_IMG_PHASE_INCREASE; }
 bool use_view_tc(const hv_settings& s, int K, size_t HW) { return !uses_phase_increase(s) && view_engine_tc(K, HW); }
 bool uses_unwrap(const hv_settings& s) { return s.image_type == HV_IMG_ARGUMENT && s.unwrap_2d; }
+// filter2D outside the AS transfer function: its own mask and passes (fourier_transform.cc:55-58)
+bool uses_f2d_mask(const hv_settings& s) { return s.filter2d_enabled && s.space_transformation != HV_SPACE_ANGULARSP; }
+bool uses_spatial(const hv_settings& s) { return s.space_transformation != HV_SPACE_NONE || s.filter2d_enabled; }
 
 struct Sizes
 {
@@ -96,7 +99,11 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
     const int K = (s.p_width != 0 ? std::min(s.p_start + s.p_width, T) : s.p_start) - s.p_start + 1;
     Sizes z;
     z.add(HW * 8);                                                      // lens
-    z.add(s.space_transformation != HV_SPACE_NONE ? HW * 8 * B : 16);  // spatial
+    z.add(uses_spatial(s) ? HW * 8 * B : 16);  // spatial
+    if (uses_f2d_mask(s))
+        z.add(HW * 8);
+    if (uses_f2d_mask(s) && s.space_transformation == HV_SPACE_FRESNELTR)
+        z.add(HW * 8 * B);  // second spatial buffer
     z.add(HW * 8 * T);                                                  // ring
     if (!served && B == s.time_stride && B == T)
         z.add(HW * 8 * T);  // second ring of the double-buffered fast mode
@@ -163,7 +170,17 @@ hv_status build(hv_pipe* p)
     if ((st = dalloc(p, ptr, bytes)) != HV_OK)                                                                         \
         return st;
     HV_ALLOC(p->lens, HW * sizeof(float2));
-    HV_ALLOC(p->spatial, (s.space_transformation != HV_SPACE_NONE ? HW * p->B : 1) * sizeof(float2));
+    HV_ALLOC(p->spatial, (uses_spatial(s) ? HW * p->B : 1) * sizeof(float2));
+    p->f2d_mask = nullptr;
+    p->work2 = nullptr;
+    if (uses_f2d_mask(s))
+    {
+        HV_ALLOC(p->f2d_mask, HW * sizeof(float2));
+        if (s.space_transformation == HV_SPACE_FRESNELTR)
+        {
+            HV_ALLOC(p->work2, HW * p->B * sizeof(float2));
+        }
+    }
     p->fast = !p->served && p->B == p->S && p->B == p->T;
     HV_ALLOC(p->ring, HW * p->T * sizeof(float2));
     p->rings[0] = p->ring;
@@ -255,6 +272,18 @@ hv_status build(hv_pipe* p)
         st = make_spectral_lens(p->lens, p->W, p->H, s.lambda, s.z_distance, s.pixel_size, s.lens_mode, p->stream);
     if (st != HV_OK)
         return st;
+    // filter2D mask (fourier_transform.cc:36-58): multiplied into G for AS, else used by its passes
+    if (s.filter2d_enabled)
+    {
+        if (s.space_transformation == HV_SPACE_ANGULARSP)
+            st = filter2d_mask(p->lens, p->W, p->H, s.filter2d_n1, s.filter2d_n2, s.filter2d_smooth_low,
+                               s.filter2d_smooth_high, 1, p->stream);
+        else
+            st = filter2d_mask(p->f2d_mask, p->W, p->H, s.filter2d_n1, s.filter2d_n2, s.filter2d_smooth_low,
+                               s.filter2d_smooth_high, 0, p->stream);
+        if (st != HV_OK)
+            return st;
+    }
     if (s.time_transformation == HV_TIME_STFT)
         st = stft_weights(p->weights, p->T, p->pmin, p->pmax, p->stream);
     else if (s.time_transformation == HV_TIME_NONE)
@@ -466,7 +495,7 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
         float2* ring = p->rings[r];
         HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ring_free[r], 0));
         hv_status st = spatial_transform(raw, p->kind, p->W, p->H, p->T, p->s.space_transformation, p->lens,
-                                         p->spatial, ring, 0, p->T, p->stream);
+                                         p->spatial, ring, 0, p->T, p->stream, nullptr, p->f2d_mask, p->work2);
         if (st != HV_OK)
             return st;
         HV_CUDA_TRY(cudaEventRecord(p->ring_ready[r], p->stream));
@@ -493,7 +522,7 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
     }
     const int begin = (p->ring_start + p->ring_size) % T;
     hv_status r = spatial_transform(raw, p->kind, p->W, p->H, nb, p->s.space_transformation, p->lens, p->spatial,
-                                    p->ring, begin, T, p->stream);
+                                    p->ring, begin, T, p->stream, nullptr, p->f2d_mask, p->work2);
     if (r != HV_OK)
         return r;
     p->ring_size += nb;
@@ -728,7 +757,7 @@ hv_status served_record(hv_pipe* p, const CycleCtl* ctl, const ServedCycle& c, b
     if (gated || c.active)
     {
         if ((r = spatial_transform(p->in_ring, p->kind, p->W, p->H, p->B, s.space_transformation, p->lens, p->spatial,
-                                   p->ring, 0, p->T, st, ctl)) != HV_OK)
+                                   p->ring, 0, p->T, st, ctl, p->f2d_mask, p->work2)) != HV_OK)
             return r;
     }
     if (!gated && !c.render)

@@ -29,6 +29,8 @@ struct hv_pipe
     std::vector<void*> allocs;
     float2* lens = nullptr;
     float2* spatial = nullptr;
+    float2* f2d_mask = nullptr;  // filter2D mask in FFT layout (Fresnel / no propagation)
+    float2* work2 = nullptr;     // second spatial buffer of the filtered Fresnel passes
     float2* ring = nullptr;
     // fast mode (batch == stride == window): two rings, spatial on `stream`, the window's time
     // transform and rendering on `render_stream`, so the next batch's spatial passes overlap them

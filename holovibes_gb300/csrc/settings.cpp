@@ -219,6 +219,14 @@ void settings_default(hv_settings* s)
     s->output_buffer_size = 1024;
     s->input_buffer_size = 512;
     s->camera_fps = 0;  // settings::CameraFps{0} (holovibes.hh:446)
+    s->q_start = 0;
+    s->q_width = 0;
+    // Filter2dN1{0}, Filter2dN2{1}, Filter2dSmoothLow{0}, Filter2dSmoothHigh{1} (holovibes.hh:405-408)
+    s->filter2d_enabled = 0;
+    s->filter2d_n1 = 0;
+    s->filter2d_n2 = 1;
+    s->filter2d_smooth_low = 0;
+    s->filter2d_smooth_high = 1;
 }
 
 hv_status settings_from_json(const char* text, hv_settings* s)
@@ -303,6 +311,11 @@ hv_status settings_from_value(const json::Value& doc, hv_settings* s, bool lenie
         {{"view", "z", "width"}, 0, &out.p_width},
         {{"view", "z2", "start"}, 0, &out.q_start},
         {{"view", "z2", "width"}, 0, &out.q_width},
+        {{"image_rendering", "filter2d", "enabled"}, 2, &out.filter2d_enabled},
+        {{"image_rendering", "filter2d", "inner_radius"}, 0, &out.filter2d_n1},
+        {{"image_rendering", "filter2d", "outer_radius"}, 0, &out.filter2d_n2},
+        {{"advanced", "filter2d_smooth", "low"}, 0, &out.filter2d_smooth_low},
+        {{"advanced", "filter2d_smooth", "high"}, 0, &out.filter2d_smooth_high},
         {{"view", "window", "xy", "output_image_accumulation"}, 0, &out.accumulation},
         {{"view", "window", "xy", "log_enabled"}, 2, &out.log_enabled},
         {{"view", "window", "xy", "contrast", "enabled"}, 2, &out.contrast_enabled},
@@ -422,6 +435,11 @@ void settings_to_value(const hv_settings* s, json::Value& doc)
     set_num(doc, {"view", "z", "width"}, s->p_width);
     set_num(doc, {"view", "z2", "start"}, s->q_start);
     set_num(doc, {"view", "z2", "width"}, s->q_width);
+    set_bool(doc, {"image_rendering", "filter2d", "enabled"}, s->filter2d_enabled != 0);
+    set_num(doc, {"image_rendering", "filter2d", "inner_radius"}, s->filter2d_n1);
+    set_num(doc, {"image_rendering", "filter2d", "outer_radius"}, s->filter2d_n2);
+    set_num(doc, {"advanced", "filter2d_smooth", "low"}, s->filter2d_smooth_low);
+    set_num(doc, {"advanced", "filter2d_smooth", "high"}, s->filter2d_smooth_high);
     set_num(doc, {"view", "window", "xy", "output_image_accumulation"}, s->accumulation);
     set_bool(doc, {"view", "window", "xy", "log_enabled"}, s->log_enabled != 0);
     set_bool(doc, {"view", "window", "xy", "contrast", "enabled"}, s->contrast_enabled != 0);
@@ -532,6 +550,13 @@ hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd)
     }
     if (s->camera_fps < 0)
         s->camera_fps = 0;
+    // Filter2dApi::set_filter2d_n1 / n2 (filter2d_api.cc:27-63): 0 <= n1 < n2
+    if (s->filter2d_enabled && (s->filter2d_n1 < 0 || s->filter2d_n2 <= s->filter2d_n1 ||
+                                s->filter2d_smooth_low < 0 || s->filter2d_smooth_high < 0))
+    {
+        set_last_error_msg("filter2d radii must satisfy 0 <= inner < outer, smoothing >= 0");
+        return HV_INVALID_VALUE;
+    }
     if (fd)
     {
         if (fd->width == 0 || fd->height == 0)
@@ -551,6 +576,19 @@ hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd)
         {
             set_last_error_msg("fftshift needs even width and height");
             return HV_INVALID_VALUE;
+        }
+        if (s->filter2d_enabled)
+        {
+            if ((fd->width & 1) || (fd->height & 1))
+            {
+                set_last_error_msg("filter2d needs even width and height (shifted mask)");
+                return HV_INVALID_VALUE;
+            }
+            if (!fft_size_supported(fd->width) || !fft_size_supported(fd->height))
+            {
+                set_last_error_msg("frame size not supported by the shared-memory FFT");
+                return HV_ERR_UNSUPPORTED;
+            }
         }
         if (s->unwrap_2d && (s->image_type == HV_IMG_ARGUMENT || s->image_type == HV_IMG_PHASE_INCREASE) &&
             (!fft_size_supported(fd->width) || !fft_size_supported(fd->height)))

@@ -7,6 +7,9 @@
 //   Fresnel        Backend/cuda_sources/fresnel_transform.cu:65-83   (x*L then forward FFT2, no 1/N)
 //   angular spec.  Backend/cuda_sources/angular_spectrum.cu:33-63     (FFT2, *G, inverse FFT2, /(H*W))
 //   ring enqueue   Backend/sources/data_struct/queue.cc:332-380
+//   filter2D       Backend/cuda_sources/filter2D.cu:28-115, fourier_transform.cc:30-72,121-137
+//                  (circular band-pass mask, shifted to FFT layout; x <- IFFT2(FFT2(x) M)
+//                  unnormalised before Fresnel / no propagation, folded into G for AS)
 //
 // GB300 design: no cuFFT. A batch of B frames goes through two or three shared-memory passes:
 //   row pass   : raw u8/u16/f32 -> complex (+ Fresnel lens) -> forward row FFT
@@ -541,6 +544,56 @@ hv_status make_spectral_lens(float2* lens, int W, int H, float lam, float z, flo
     return HV_OK;
 }
 
+// ====================================================================================== filter2D
+
+// Band-pass mask of kernel_update_filter2d_circles_mask (filter2D.cu:52-88) in the reference's
+// float arithmetic: r = hypotf(x - W/2, y - H/2), A = 1 inside radius n2 with a cosine roll-off of
+// width sh, B the same for n1 / sl, mask = A (1 - B); written quadrant-swapped (FFT layout, the
+// shift_corners of update_filter2d_circles_mask) as complex (multiply = 0) or multiplied into an
+// FFT-layout complex array in place (multiply = 1: the AS transfer function, fourier_transform.cc:134-137).
+__global__ void k_filter2d_mask(float2* dst, int W, int H, int n1, int n2, int sl, int sh, int multiply)
+{
+    const int X = blockIdx.x * blockDim.x + threadIdx.x, Y = blockIdx.y;
+    if (X >= W || Y >= H)
+        return;
+    const int x = (X + W / 2) % W, y = (Y + H / 2) % H;  // source of the quadrant swap (even W, H)
+    const float rx = static_cast<float>(x) - static_cast<float>(W / 2);
+    const float ry = static_cast<float>(y) - static_cast<float>(H / 2);
+    const float len = hypotf(rx, ry);
+    float a = 0.0f, b = 0.0f;
+    if (len < static_cast<float>(n2))
+        a = 1.0f;
+    else if (len < static_cast<float>(n2 + sh))
+        a = cosf(static_cast<float>(static_cast<double>(__fdiv_rn(len - static_cast<float>(n2), static_cast<float>(sh))) *
+                                    1.57079632679489661923));
+    if (len < static_cast<float>(n1))
+        b = 1.0f;
+    else if (len < static_cast<float>(n1 + sl))
+        b = cosf(static_cast<float>(static_cast<double>(__fdiv_rn(len - static_cast<float>(n1), static_cast<float>(sl))) *
+                                    1.57079632679489661923));
+    const float m = a * (1.0f - b);
+    float2* o = dst + static_cast<size_t>(Y) * W + X;
+    if (multiply)
+    {
+        const float2 v = *o;
+        *o = make_float2(v.x * m, v.y * m);
+    }
+    else
+        *o = make_float2(m, 0.0f);
+}
+
+hv_status filter2d_mask(float2* dst, int W, int H, int n1, int n2, int smooth_low, int smooth_high, int multiply,
+                        cudaStream_t st)
+{
+    if (!dst || W <= 0 || H <= 0 || (W & 1) || (H & 1) || n1 < 0 || n2 <= n1 || smooth_low < 0 || smooth_high < 0)
+        return HV_INVALID_VALUE;
+    dim3 block(128), grid((W + 127) / 128, H);
+    k_filter2d_mask<<<grid, block, 0, st>>>(dst, W, H, n1, n2, smooth_low, smooth_high, multiply);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
 int raw_kind(int raw_bytes, int big_endian)
 {
     switch (raw_bytes)
@@ -554,7 +607,8 @@ int raw_kind(int raw_bytes, int big_endian)
 }
 
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
-                            float2* work, float2* ring, int slot0, int nslots, cudaStream_t st, const CycleCtl* ctl)
+                            float2* work, float2* ring, int slot0, int nslots, cudaStream_t st, const CycleCtl* ctl,
+                            const float2* f2d_mask, float2* work2)
 {
     // With a cycle control block, `raw` is the input ring base (the batch sits at ctl->raw_offset)
     // and the ring slot of frame 0 is slot0 + ctl->ring_begin; every pass is gated by ctl->active.
@@ -564,7 +618,12 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
     const FrameMap work_map{HW, 0, batch > 0 ? batch : 1};
     if (batch <= 0)
         return HV_OK;
-    if (space == HV_SPACE_NONE)
+    // filter2D before Fresnel or without propagation (fourier_transform.cc:55-58, filter2D.cu:28-46);
+    // for AS the mask is part of the transfer function and nothing changes here
+    const bool f2d = f2d_mask && space != HV_SPACE_ANGULARSP;
+    if (f2d && (!work || (space == HV_SPACE_FRESNELTR && !work2)))
+        return HV_INVALID_VALUE;
+    if (space == HV_SPACE_NONE && !f2d)
     {
         const size_t total = HW * batch;
         const int block = 256;
@@ -595,6 +654,44 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
         const FrameMap ring_b{HW, (slot0 + b0) % nslots, nslots, begin_dev};
         const FrameMap work_b{HW, 0, nb};
         hv_status s;
+        if (f2d)
+        {
+            // forward rows -> work; columns: forward, *M, inverse (in place); then the unnormalised
+            // inverse rows: -> ring slots (no propagation) or -> work2, *L and forward rows -> work,
+            // forward columns -> ring slots (Fresnel)
+            RowPass r{raw_b, kind, HW, work, work_b, nullptr, H, 0, 1.0f};
+            r.ctl = ctl;
+            r.raw_from_ctl = ctl ? 1 : 0;
+            if ((s = fft_rows(r, W, nb, st)) != HV_OK)
+                return s;
+            ColPass c{work, HW, work, work_b, f2d_mask, W, 2, 1.0f};
+            c.ctl = ctl;
+            if ((s = fft_cols(c, H, nb, st)) != HV_OK)
+                return s;
+            if (space == HV_SPACE_NONE)
+            {
+                RowPass r2{work, IN_C64, HW, ring, ring_b, nullptr, H, 1, 1.0f};
+                r2.stream_out = 1;
+                r2.ctl = ctl;
+                if ((s = fft_rows(r2, W, nb, st)) != HV_OK)
+                    return s;
+                continue;
+            }
+            RowPass r2{work, IN_C64, HW, work2, work_b, nullptr, H, 1, 1.0f};
+            r2.ctl = ctl;
+            if ((s = fft_rows(r2, W, nb, st)) != HV_OK)
+                return s;
+            RowPass r3{work2, IN_C64, HW, work, work_b, lens, H, 0, 1.0f};
+            r3.ctl = ctl;
+            if ((s = fft_rows(r3, W, nb, st)) != HV_OK)
+                return s;
+            ColPass c2{work, HW, ring, ring_b, nullptr, W, 0, 1.0f};
+            c2.stream_out = 1;
+            c2.ctl = ctl;
+            if ((s = fft_cols(c2, H, nb, st)) != HV_OK)
+                return s;
+            continue;
+        }
         if (space == HV_SPACE_FRESNELTR)
         {
             // x*L, forward rows -> work; forward columns -> ring slots

@@ -117,6 +117,11 @@ typedef struct hv_settings
     int32_t camera_fps;              /* CameraFps input setting (.holo info.camera_fps): moment frequencies */
     int32_t q_start;                 /* view.z2.start: first eigenvector kept by SSA_STFT */
     int32_t q_width;                 /* view.z2.width: eigenvectors kept by SSA_STFT (0 = all) */
+    int32_t filter2d_enabled;        /* image_rendering.filter2d.enabled */
+    int32_t filter2d_n1;             /* image_rendering.filter2d.inner_radius (pixels, frequency domain) */
+    int32_t filter2d_n2;             /* image_rendering.filter2d.outer_radius */
+    int32_t filter2d_smooth_low;     /* advanced.filter2d_smooth.low: cosine roll-off of the inner edge */
+    int32_t filter2d_smooth_high;    /* advanced.filter2d_smooth.high: cosine roll-off of the outer edge */
 } hv_settings;
 
 /* ------------------------------------------------------------------------------------------
@@ -199,6 +204,22 @@ hv_status hv_fresnel_lens(void* lens_c64, int width, int height, float lambda, f
  * (Backend/cuda_sources/angular_spectrum.cu:14-31, masks.cu:31-59, fourier_transform.cc:121-137). */
 hv_status hv_angular_spectrum_lens(void* lens_c64, int width, int height, float lambda, float z,
                                    float pixel_size_um, int lens_mode, void* stream);
+
+/* filter2D band-pass mask (kernel_update_filter2d_circles_mask + shift_corners, filter2D.cu:52-115):
+ * m = A (1 - B), A = 1 for r < n2 with a cosine roll-off over smooth_high pixels, B the same for
+ * n1 / smooth_low, r the distance to the frame centre; written in FFT layout as complex64 (m, 0)
+ * when multiply == 0, or multiplied into the complex64 array (an FFT-layout transfer function)
+ * when multiply != 0. Even width and height, 0 <= n1 < n2 (Filter2dApi::set_filter2d_n1/n2). */
+hv_status hv_filter2d_mask(void* dst_c64, int width, int height, int n1, int n2, int smooth_low, int smooth_high,
+                           int multiply, void* stream);
+/* hv_spatial_transform with filter2D (fourier_transform.cc:30-72, filter2D.cu:28-46): for
+ * FRESNELTR and NONE the frames first become IFFT2(FFT2(x) M) (unnormalised inverse), M = mask_c64
+ * from hv_filter2d_mask; for ANGULARSP pass the transfer function multiplied by the mask and no
+ * mask here. FRESNELTR also needs `work2_c64` (batch*W*H complex64). */
+hv_status hv_spatial_transform_filter2d(const void* raw, int raw_bytes, int big_endian, int width, int height,
+                                        int batch, int space, const void* lens_c64, const void* mask_c64,
+                                        void* work_c64, void* work2_c64, void* ring_c64, int slot0, int nslots,
+                                        void* stream);
 
 /* Fused raw->complex convert + spatial propagation of `batch` frames, written into slots
  * (slot0 + b) % nslots of a ring of complex64 frames. Replaces input_queue_to_input_buffer

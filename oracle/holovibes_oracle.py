@@ -216,8 +216,42 @@ def angular_spectrum(frames: np.ndarray, lens: np.ndarray) -> np.ndarray:
     return ifft2(fft2(frames, axes=(-2, -1)) * lens[None], axes=(-2, -1))
 
 
-def spatial_transform(frames: np.ndarray, kind: str, lens: np.ndarray | None) -> np.ndarray:
-    """Dispatch of FourierTransform::insert_fft (fourier_transform.cc:30-72)."""
+def filter2d_mask(W: int, H: int, n1: int, n2: int, smooth_low: int, smooth_high: int) -> np.ndarray:
+    """kernel_update_filter2d_circles_mask (filter2D.cu:52-88) in its float32 arithmetic, then
+    shift_corners (filter2D.cu:113): r = hypotf(x - W/2, y - H/2); A = 1 for r < n2, else
+    cos((r - n2) / smooth_high * pi/2) for r < n2 + smooth_high (the product in double, rounded to
+    float for cosf), else 0; B the same with n1 / smooth_low; mask = A * (1 - B)."""
+    x = np.arange(W, dtype=F32) - F32(W // 2)
+    y = np.arange(H, dtype=F32) - F32(H // 2)
+    r = np.hypot(x[None, :], y[:, None]).astype(F32)
+
+    def disc(radius, smooth):
+        out = np.zeros((H, W), F32)
+        out[r < F32(radius)] = 1.0
+        band = (r >= F32(radius)) & (r < F32(radius + smooth))
+        if smooth > 0:
+            q = ((r[band] - F32(radius)) / F32(smooth)).astype(F32)
+            out[band] = np.cos((q.astype(np.float64) * (math.pi / 2)).astype(F32))
+        return out
+
+    a = disc(n2, smooth_high)
+    b = disc(n1, smooth_low)
+    return shift_corners((a * (F32(1.0) - b)).astype(F32))
+
+
+def filter2d(frames: np.ndarray, mask: np.ndarray) -> np.ndarray:
+    """filter2D (filter2D.cu:28-46): forward FFT2, * mask, cuFFT's unnormalised inverse."""
+    H, W = frames.shape[-2:]
+    return ifft2(fft2(frames, axes=(-2, -1)) * mask[None], axes=(-2, -1)) * (H * W)
+
+
+def spatial_transform(frames: np.ndarray, kind: str, lens: np.ndarray | None,
+                      f2d_mask: np.ndarray | None = None) -> np.ndarray:
+    """Dispatch of FourierTransform::insert_fft (fourier_transform.cc:30-72). With filter2D, the
+    frames are filtered first for FRESNELTR and NONE; for ANGULARSP the mask is already part of
+    the transfer function (`lens`)."""
+    if f2d_mask is not None and kind != "ANGULARSP":
+        frames = filter2d(frames, f2d_mask)
     if kind == "NONE":
         return frames
     if kind == "FRESNELTR":
@@ -641,6 +675,11 @@ class OracleSettings:
     camera_fps: float = 0.0  # moments: frequencies in units of camera_fps / T
     q_start: int = 0  # SSA_STFT eigenvector range (view.z2)
     q_width: int = 0
+    filter2d_enabled: bool = False
+    filter2d_n1: int = 0
+    filter2d_n2: int = 1
+    filter2d_smooth_low: int = 0
+    filter2d_smooth_high: int = 1
 
 
 @dataclass
@@ -665,6 +704,13 @@ class OraclePipe:
             self.lens = fresnel_lens(W, H, s.lam, s.z, s.pixel_size, s.lens_mode)
         elif s.space_transformation == "ANGULARSP":
             self.lens = angular_spectrum_lens(W, H, s.lam, s.z, s.pixel_size, s.lens_mode)
+        self.f2d_mask = None
+        if s.filter2d_enabled:
+            m = filter2d_mask(W, H, s.filter2d_n1, s.filter2d_n2, s.filter2d_smooth_low, s.filter2d_smooth_high)
+            if s.space_transformation == "ANGULARSP":
+                self.lens = self.lens * m  # apply_mask on the shifted lens (fourier_transform.cc:136-137)
+            else:
+                self.f2d_mask = m.astype(np.float64)
         self.acc = Accumulator(s.accumulation, (H, W)) if s.accumulation > 1 else None
         self.autocontrast_pending = s.contrast_enabled and s.contrast_auto_refresh
         self.crange = (s.contrast_min, s.contrast_max)
@@ -679,7 +725,7 @@ class OraclePipe:
             return None
         self.batch_index = 0
         frames = convert_frames(raw)
-        frames = spatial_transform(frames, s.space_transformation, self.lens)
+        frames = spatial_transform(frames, s.space_transformation, self.lens, self.f2d_mask)
         self.ring.enqueue_multiple(frames)
         if self.ring.size < s.time_transformation_size:
             return None

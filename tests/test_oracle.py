@@ -176,3 +176,21 @@ def test_phase_increase_history_and_rescale():
     r = O.rescale_float(img)
     assert r[0] == 0.0 and np.isclose(r[16383], 65535.0 * 3.0 / 3.0)
     assert r[17000] > 65535.0
+
+
+def test_filter2d_mask_shape():
+    """filter2D band-pass (filter2D.cu:52-88): 0 inside n1, 1 between n1 and n2 (no smoothing),
+    0 outside, centred on (W/2, H/2) before the quadrant swap."""
+    import holovibes_oracle as O
+
+    m = O.shift_corners(O.filter2d_mask(16, 16, 2, 5, 0, 0))  # back to centred layout
+    assert m[8, 8] == 0.0 and m[8, 10] == 1.0 and m[8, 11] == 1.0 and m[8, 13] == 0.0
+    s = O.shift_corners(O.filter2d_mask(32, 32, 2, 5, 0, 4))
+    # roll-off between 5 and 9 pixels: cos((r - 5) / 4 * pi / 2)
+    assert np.isclose(s[16, 16 + 7], np.cos(2 / 4 * np.pi / 2), atol=1e-6) and s[16, 16 + 9] == 0.0
+    # the AS path folds the mask into G; a filtered frame keeps only the band's frequencies
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((1, 32, 32))
+    y = O.filter2d(x, O.filter2d_mask(32, 32, 2, 5, 0, 0))
+    spec = np.abs(np.fft.fftshift(np.fft.fft2(y[0])))
+    assert spec[16, 16] < 1e-9 and spec[16, 16 + 12] < 1e-9

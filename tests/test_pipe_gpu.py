@@ -32,7 +32,9 @@ def _oracle_settings(fd, s):
         contrast_min=s.contrast_min, contrast_max=s.contrast_max, contrast_lower=s.contrast_lower,
         contrast_upper=s.contrast_upper, reticle_display=bool(s.reticle_display), reticle_scale=s.reticle_scale,
         unwrap_2d=bool(s.unwrap_2d), lens_mode="fp64" if s.lens_mode == 0 else "ref32", camera_fps=s.camera_fps,
-        q_start=s.q_start, q_width=s.q_width)
+        q_start=s.q_start, q_width=s.q_width, filter2d_enabled=bool(s.filter2d_enabled), filter2d_n1=s.filter2d_n1,
+        filter2d_n2=s.filter2d_n2, filter2d_smooth_low=s.filter2d_smooth_low,
+        filter2d_smooth_high=s.filter2d_smooth_high)
 
 
 CASES = {
@@ -133,6 +135,21 @@ CASES = {
                                                time_transformation_size=16, time_stride=8, batch_size=8,
                                                z_distance=0.3, pixel_size=20.0, image_type=3, q_start=13, q_width=2,
                                                p_start=1, renorm=1, contrast_enabled=1), 5),
+    # filter2D (fourier_transform.cc:30-72): before Fresnel, without propagation, inside G for AS
+    "fresnel_f2d_stft_mod": (64, 64, 1, dict(space_transformation=1, time_transformation=1, time_transformation_size=8,
+                                              time_stride=8, batch_size=8, lambda_=785e-9, z_distance=0.45,
+                                              pixel_size=12.0, p_start=1, p_width=1, filter2d_enabled=1,
+                                              filter2d_n1=3, filter2d_n2=20, filter2d_smooth_low=2,
+                                              filter2d_smooth_high=4, renorm=1, contrast_enabled=1), 3),
+    "none_f2d_stft_sqmod": (64, 64, 2, dict(space_transformation=0, time_transformation=1, time_transformation_size=8,
+                                             time_stride=4, batch_size=4, image_type=1, p_start=2,
+                                             filter2d_enabled=1, filter2d_n1=0, filter2d_n2=12, renorm=1,
+                                             fft_shift=1, contrast_enabled=1), 4),
+    "as_f2d_pca_mod": (64, 64, 2, dict(space_transformation=2, time_transformation=2, time_transformation_size=16,
+                                        time_stride=16, batch_size=16, z_distance=0.3, pixel_size=20.0, image_type=0,
+                                        p_start=15, p_width=0, filter2d_enabled=1, filter2d_n1=5, filter2d_n2=28,
+                                        filter2d_smooth_low=0, filter2d_smooth_high=3, renorm=1,
+                                        contrast_enabled=1), 2),
     "fresnel_stft_ref32_big_endian": (128, 64, 2, dict(space_transformation=1, time_transformation=1,
                                                         time_transformation_size=4, time_stride=4, batch_size=4,
                                                         z_distance=0.3, pixel_size=20.0, p_start=2, p_width=1,
