@@ -201,6 +201,20 @@ hv_status hv_rescale_float(const float* in_f32, size_t npix, const void* minmax,
     return rescale_float(in_f32, npix, static_cast<const float2*>(minmax), post_scale, out_f32, S(stream));
 }
 
+hv_status hv_time_cuts(const void* ring_c64, int T, int width, int height, const void* weights_c64, int xmin, int xmax,
+                       int ymin, int ymax, int img_type, float* xz_f32, float* yz_f32, void* work, void* stream)
+{
+    return time_cuts(static_cast<const float2*>(ring_c64), T, width, height, static_cast<const float2*>(weights_c64),
+                     xmin, xmax, ymin, ymax, img_type, xz_f32, yz_f32, work, S(stream));
+}
+
+size_t hv_time_cuts_workspace(int width, int height, int T, int xmin, int xmax, int ymin, int ymax)
+{
+    if (width <= 0 || height <= 0 || T <= 0 || xmax < xmin || ymax < ymin)
+        return 0;
+    return cuts_workspace(width, height, T, xmax - xmin + 1, ymax - ymin + 1);
+}
+
 hv_status hv_unpack_12_to_16(const void* in, size_t in_bytes, uint16_t* out, size_t out_count, void* stream)
 {
     return unpack_packed(12, in, in_bytes, out, out_count, S(stream));

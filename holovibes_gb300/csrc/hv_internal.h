@@ -114,6 +114,15 @@ hv_status log10_map(float* frame, size_t n, cudaStream_t st);
 size_t percentile_workspace(size_t n);
 hv_status percentile(const float* frame, int W, int H, float lower, float upper, float reticle_scale, float* range,
                      void* work, cudaStream_t st, const CycleCtl* ctl = nullptr);
+hv_status percentile_pitched(const float* frame, int W, int H, int pitch, float lower, float upper,
+                             float reticle_scale, float* range, void* work, cudaStream_t st,
+                             const CycleCtl* ctl = nullptr);
+// Time-transformation cuts (XZ: T x W, YZ: H x T) from all T weight rows; work: cuts_workspace bytes.
+bool cuts_supported(int T);
+size_t cuts_workspace(int W, int H, int T, int nx, int ny);
+hv_status time_cuts(const float2* ring, int T, int W, int H, const float2* weights_all, int xmin, int xmax, int ymin,
+                    int ymax, int img_type, float* xz, float* yz, void* work, cudaStream_t st);
+hv_status evecs_to_weights(const double2* evecs, int T, float2* w, cudaStream_t st);
 hv_status contrast_to_ushort(const float* frame, const float* range, int invert, int apply, uint16_t* out, size_t n,
                              cudaStream_t st, const CycleCtl* ctl = nullptr);
 

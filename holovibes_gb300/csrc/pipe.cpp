@@ -65,7 +65,8 @@ void free_buffers(hv_pipe* p)
             cudaEventDestroy(*e);
             *e = nullptr;
         }
-    for (auto* vec : {&p->in_filled, &p->in_consumed, &p->out_ready, &p->out_freed})
+    for (auto* vec : {&p->in_filled, &p->in_consumed, &p->out_ready, &p->out_freed, &p->cut[0].out_ready,
+                      &p->cut[0].out_freed, &p->cut[1].out_ready, &p->cut[1].out_freed})
     {
         for (cudaEvent_t e : *vec)
             cudaEventDestroy(e);
@@ -128,6 +129,19 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
         z.add(HW * 8);
         z.add(HW * 4);
         z.add(phase_increase_minmax_count(HW) * 8);
+    }
+    if (s.cuts_enabled)
+    {
+        const size_t ct = static_cast<size_t>(T) * (fd.width + fd.height);  // XZ + YZ pixels
+        z.add(static_cast<size_t>(T) * T * 8);
+        z.add(cuts_workspace(fd.width, fd.height, T, s.x_width + 1, s.y_width + 1));
+        z.add(ct * 4);
+        z.add(static_cast<size_t>(T) * fd.width * 4 * (s.xz_accumulation > 1 ? s.xz_accumulation : 0));
+        z.add(static_cast<size_t>(T) * fd.height * 4 * (s.yz_accumulation > 1 ? s.yz_accumulation : 0));
+        z.add(64);
+        z.add(64);
+        z.add(ct * 2 * static_cast<size_t>(std::max(1, s.cuts_buffer_size)));
+        z.add(percentile_workspace(std::max(HW, static_cast<size_t>(T) * std::max(fd.width, fd.height))));
     }
     z.add(static_cast<size_t>(time_view_partials(fd.width, fd.height)) * 8);
     z.add(reduce_workspace(HW));
@@ -234,7 +248,34 @@ hv_status build(hv_pipe* p)
         HV_ALLOC(p->acc_ring, HW * p->A * sizeof(float));
     }
     HV_ALLOC(p->range, 4 * sizeof(float));
-    HV_ALLOC(p->pct_work, percentile_workspace(HW));
+    p->cuts = s.cuts_enabled != 0;
+    size_t pct_n = HW;
+    if (p->cuts)
+    {
+        HV_ALLOC(p->w_all, static_cast<size_t>(p->T) * p->T * sizeof(float2));
+        HV_ALLOC(p->cut_work, cuts_workspace(p->W, p->H, p->T, s.x_width + 1, s.y_width + 1));
+        const int accs[2] = {s.xz_accumulation, s.yz_accumulation};
+        for (int v = 0; v < 2; ++v)
+        {
+            hv_pipe::CutView& c = p->cut[v];
+            c.w = v == 0 ? p->W : p->T;
+            c.h = v == 0 ? p->T : p->H;
+            const size_t px = static_cast<size_t>(c.w) * c.h;
+            pct_n = std::max(pct_n, px);
+            HV_ALLOC(c.post, px * sizeof(float));
+            HV_CUDA_TRY(cudaMemsetAsync(c.post, 0, px * sizeof(float), p->stream));
+            c.A = accs[v] > 1 ? accs[v] : 0;
+            c.acc_ring = nullptr;
+            if (c.A > 0)
+            {
+                HV_ALLOC(c.acc_ring, px * c.A * sizeof(float));
+            }
+            HV_ALLOC(c.range, 4 * sizeof(float));
+            c.out_cap = std::max(1, s.cuts_buffer_size);
+            HV_ALLOC(c.out_ring, px * sizeof(uint16_t) * c.out_cap);
+        }
+    }
+    HV_ALLOC(p->pct_work, percentile_workspace(pct_n));
     p->in_slots = std::max(2, s.input_buffer_size / std::max(1, p->B));
     p->batch_bytes = HW * p->depth * p->B;
     HV_ALLOC(p->in_ring, p->batch_bytes * p->in_slots);
@@ -250,6 +291,10 @@ hv_status build(hv_pipe* p)
     if ((st = mk_events(p->in_filled, p->in_slots)) != HV_OK || (st = mk_events(p->in_consumed, p->in_slots)) != HV_OK ||
         (st = mk_events(p->out_ready, p->out_cap)) != HV_OK || (st = mk_events(p->out_freed, p->out_cap)) != HV_OK)
         return st;
+    for (int v = 0; p->cuts && v < 2; ++v)
+        if ((st = mk_events(p->cut[v].out_ready, p->cut[v].out_cap)) != HV_OK ||
+            (st = mk_events(p->cut[v].out_freed, p->cut[v].out_cap)) != HV_OK)
+            return st;
 
     // ring starts zeroed like Queue::resize (queue.cc:131-134)
     HV_CUDA_TRY(cudaMemsetAsync(p->ring, 0, HW * p->T * sizeof(float2), p->stream));
@@ -297,6 +342,30 @@ hv_status build(hv_pipe* p)
         return st;
     float r0[4] = {s.contrast_min, s.contrast_max, 0.f, 0.f};
     HV_CUDA_TRY(cudaMemcpyAsync(p->range, r0, sizeof(r0), cudaMemcpyHostToDevice, p->stream));
+    if (p->cuts)
+    {
+        // p_acc rows for the cuts: every STFT bin, or the ring itself without a time transform;
+        // PCA / SSA_STFT rows are rebuilt from each window's eigenvectors
+        if (s.time_transformation == HV_TIME_STFT)
+            st = stft_weights(p->w_all, p->T, 0, p->T - 1, p->stream);
+        else if (s.time_transformation == HV_TIME_NONE)
+            st = delta_weights(p->w_all, p->T, 0, p->T - 1, p->stream);
+        if (st != HV_OK)
+            return st;
+        const float rxz[4] = {s.xz_contrast_min, s.xz_contrast_max, 0.f, 0.f};
+        const float ryz[4] = {s.yz_contrast_min, s.yz_contrast_max, 0.f, 0.f};
+        HV_CUDA_TRY(cudaMemcpyAsync(p->cut[0].range, rxz, sizeof(rxz), cudaMemcpyHostToDevice, p->stream));
+        HV_CUDA_TRY(cudaMemcpyAsync(p->cut[1].range, ryz, sizeof(ryz), cudaMemcpyHostToDevice, p->stream));
+        // Rendering::request_autocontrast (rendering.cc:87-99)
+        p->cut[0].autocontrast_pending = s.xz_contrast_enabled && s.xz_contrast_auto_refresh;
+        p->cut[1].autocontrast_pending = s.yz_contrast_enabled && s.yz_contrast_auto_refresh;
+        for (int v = 0; v < 2; ++v)
+        {
+            p->cut[v].acc_start = p->cut[v].acc_size = 0;
+            p->cut[v].out_head = p->cut[v].out_count = 0;
+            p->cut[v].valid = false;
+        }
+    }
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
 
     p->ring_start = p->ring_size = 0;
@@ -411,6 +480,93 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
     return HV_OK;
 }
 
+// XZ / YZ cuts of the window just rendered (fourier_transform.cc:462-503, image_accumulation.cc:159-257,
+// rendering.cc:75-340, converts.cc:321-350, pipe.cc:504-514): slices at the cursor band, then per
+// view accumulation, log10, autocontrast (bins frame_index_offset .. T-1-offset, or the reticle
+// disc for XZ), contrast and uint16 into the view's own output queue.
+hv_status render_cuts(hv_pipe* p, cudaStream_t st)
+{
+    const hv_settings& s = p->s;
+    hv_status r;
+    if (s.time_transformation == HV_TIME_PCA && (r = evecs_to_weights(p->evecs, p->T, p->w_all, st)) != HV_OK)
+        return r;
+    if (s.time_transformation == HV_TIME_SSA_STFT &&
+        (r = ssa_weights(p->evecs, p->T, p->qmin, p->qn, 0, p->T, p->w_all, st)) != HV_OK)
+        return r;
+    if (s.x_start < p->W && s.y_start < p->H &&
+        (r = time_cuts(p->ring, p->T, p->W, p->H, p->w_all, s.x_start, s.x_start + s.x_width, s.y_start,
+                       s.y_start + s.y_width, s.image_type, p->cut[0].post, p->cut[1].post, p->cut_work, st)) != HV_OK)
+        return r;
+    for (int v = 0; v < 2; ++v)
+    {
+        hv_pipe::CutView& c = p->cut[v];
+        const size_t px = static_cast<size_t>(c.w) * c.h;
+        const int log_on = v == 0 ? s.xz_log_enabled : s.yz_log_enabled;
+        const int contrast_on = v == 0 ? s.xz_contrast_enabled : s.yz_contrast_enabled;
+        const int invert = v == 0 ? s.xz_contrast_invert : s.yz_contrast_invert;
+        int slot = 0, start = 0, count = 0;
+        if (c.A > 0)
+        {
+            slot = (c.acc_start + c.acc_size) % c.A;
+            if (c.acc_size < c.A)
+                ++c.acc_size;
+            else
+                c.acc_start = (c.acc_start + 1) % c.A;
+            start = c.acc_start;
+            count = c.acc_size;
+        }
+        if ((c.A > 0 || log_on) &&
+            (r = renorm_shift_accumulate(c.post, c.post, c.w, c.h, nullptr, 0, c.A > 0 ? c.acc_ring : nullptr, c.A,
+                                         slot, start, count, log_on, st, 1.0f)) != HV_OK)
+            return r;
+        if (contrast_on && c.autocontrast_pending)
+        {
+            const bool apply = c.A == 0 || c.acc_size == c.A || c.acc_size == 1;
+            if (apply)
+            {
+                // percentile.cu:139-250: bins offset .. T-1-offset (the whole window when that is empty)
+                int off = s.cuts_contrast_offset;
+                if (2 * off >= p->T)
+                    off = 0;
+                if (v == 0 && s.reticle_display)
+                    r = percentile(c.post, c.w, c.h, s.contrast_lower, s.contrast_upper, s.reticle_scale, c.range,
+                                   p->pct_work, st);
+                else if (v == 0)
+                    r = percentile(c.post + static_cast<size_t>(off) * c.w, c.w, c.h - 2 * off, s.contrast_lower,
+                                   s.contrast_upper, 0.0f, c.range, p->pct_work, st);
+                else
+                    r = percentile_pitched(c.post + off, c.w - 2 * off, c.h, c.w, s.contrast_lower, s.contrast_upper,
+                                           0.0f, c.range, p->pct_work, st);
+                if (r != HV_OK)
+                    return r;
+                if (c.A == 0 || c.acc_size == c.A)
+                    c.autocontrast_pending = false;
+            }
+        }
+        int slot_out;
+        {
+            std::lock_guard<std::mutex> g(p->mu);
+            if (c.out_count == c.out_cap)
+            {
+                c.out_head = (c.out_head + 1) % c.out_cap;
+                --c.out_count;
+                ++c.out_overwritten;
+            }
+            slot_out = (c.out_head + c.out_count) % c.out_cap;
+        }
+        HV_CUDA_TRY(cudaStreamWaitEvent(st, c.out_freed[slot_out], 0));
+        if ((r = contrast_to_ushort(c.post, c.range, invert, contrast_on, c.out_ring + slot_out * px, px, st)) != HV_OK)
+            return r;
+        HV_CUDA_TRY(cudaEventRecord(c.out_ready[slot_out], st));
+        {
+            std::lock_guard<std::mutex> g(p->mu);
+            ++c.out_count;
+        }
+        c.valid = true;
+    }
+    return HV_OK;
+}
+
 // Rendering of one output from a full ring (pipe.cc:334-374).
 hv_status render(hv_pipe* p)
 {
@@ -474,7 +630,7 @@ hv_status render(hv_pipe* p)
         ++p->out_count;
     }
     p->last_frame_valid = true;
-    return HV_OK;
+    return p->cuts ? render_cuts(p, st) : HV_OK;
 }
 
 // One batch of B raw frames at device address `raw` (pipe.cc:295-334).
@@ -638,6 +794,13 @@ hv_pipe* pipe_create_served(const hv_frame_desc* fd, const hv_settings* settings
     p->s = *settings;
     if ((out = settings_validate(&p->s, fd)) != HV_OK)
     {
+        delete p;
+        return nullptr;
+    }
+    if (p->s.cuts_enabled)
+    {
+        set_last_error_msg("served streams render the XY view only (time cuts: use a Pipe)");
+        out = HV_ERR_UNSUPPORTED;
         delete p;
         return nullptr;
     }
@@ -1011,6 +1174,11 @@ hv_status hv_pipe_request_autocontrast(hv_pipe* p)
     if (!p)
         return HV_INVALID_VALUE;
     p->autocontrast_pending = p->s.contrast_enabled != 0;
+    if (p->cuts)
+    {
+        p->cut[0].autocontrast_pending = p->s.xz_contrast_enabled != 0;
+        p->cut[1].autocontrast_pending = p->s.yz_contrast_enabled != 0;
+    }
     return HV_OK;
 }
 
@@ -1060,6 +1228,78 @@ hv_status hv_pipe_get_float_frame(hv_pipe* p, float* dst)
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
     HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
     HV_CUDA_TRY(cudaMemcpy(dst, p->post, p->HW * sizeof(float), cudaMemcpyDeviceToHost));
+    return HV_OK;
+}
+
+size_t hv_pipe_cut_output_count(hv_pipe* p, int which)
+{
+    if (!p || !p->cuts || which < 0 || which > 1)
+        return 0;
+    std::lock_guard<std::mutex> g(p->mu);
+    return static_cast<size_t>(p->cut[which].out_count);
+}
+
+hv_status hv_pipe_pull_cut(hv_pipe* p, int which, uint16_t* dst, int mem, int64_t timeout_us)
+{
+    if (!p || !dst || which < 0 || which > 1)
+        return HV_INVALID_VALUE;
+    if (!p->cuts)
+        return HV_NO_IN_DATA;
+    hv_pipe::CutView& c = p->cut[which];
+    int slot;
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        if (c.out_count == 0)
+            return timeout_us > 0 ? HV_ERR_TIMEOUT : HV_NO_IN_DATA;
+        slot = c.out_head;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;)
+    {
+        const cudaError_t e = cudaEventQuery(c.out_ready[slot]);
+        if (e == cudaSuccess)
+            break;
+        if (e != cudaErrorNotReady)
+        {
+            set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+            return HV_ERR_CUDA;
+        }
+        const auto us =
+            std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_us >= 0 && us > timeout_us)
+            return HV_ERR_TIMEOUT;
+        std::this_thread::yield();
+    }
+    const size_t px = static_cast<size_t>(c.w) * c.h;
+    HV_CUDA_TRY(cudaMemcpyAsync(dst, c.out_ring + slot * px, px * sizeof(uint16_t),
+                                mem == HV_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                p->copy_stream));
+    HV_CUDA_TRY(cudaEventRecord(c.out_freed[slot], p->copy_stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        if (c.out_head == slot && c.out_count > 0)
+        {
+            c.out_head = (c.out_head + 1) % c.out_cap;
+            --c.out_count;
+        }
+    }
+    return HV_OK;
+}
+
+hv_status hv_pipe_get_cut_float_frame(hv_pipe* p, int which, float* dst, float* range_out)
+{
+    if (!p || which < 0 || which > 1)
+        return HV_INVALID_VALUE;
+    if (!p->cuts || !p->cut[which].valid)
+        return HV_NO_IN_DATA;
+    const hv_pipe::CutView& c = p->cut[which];
+    HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    if (dst)
+        HV_CUDA_TRY(cudaMemcpy(dst, c.post, static_cast<size_t>(c.w) * c.h * sizeof(float), cudaMemcpyDeviceToHost));
+    if (range_out)
+        HV_CUDA_TRY(cudaMemcpy(range_out, c.range, 2 * sizeof(float), cudaMemcpyDeviceToHost));
     return HV_OK;
 }
 

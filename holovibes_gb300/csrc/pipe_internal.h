@@ -65,6 +65,27 @@ struct hv_pipe
     float2* pi_minmax = nullptr;
     uint64_t pi_count = 0;
 
+    // time-transformation cuts (XZ: T x W, YZ: H x T): slices, accumulation rings, contrast
+    // ranges and output queues of their own (gpu_output_queue_xz / _yz, icompute.cc:195-213)
+    struct CutView
+    {
+        int w = 0, h = 0;  // image width and height (XZ: W x T, YZ: T x H)
+        float* post = nullptr;
+        float* acc_ring = nullptr;
+        int A = 0, acc_start = 0, acc_size = 0;
+        float* range = nullptr;
+        bool autocontrast_pending = false;
+        uint16_t* out_ring = nullptr;
+        int out_cap = 0, out_head = 0, out_count = 0;
+        uint64_t out_overwritten = 0;
+        std::vector<cudaEvent_t> out_ready, out_freed;
+        bool valid = false;
+    };
+    bool cuts = false;
+    float2* w_all = nullptr;  // all T weight rows: bins (STFT / SSA_STFT), components (PCA), identity (NONE)
+    void* cut_work = nullptr;
+    CutView cut[2];           // 0: XZ, 1: YZ
+
     // input ring of batch slots
     uint8_t* in_ring = nullptr;
     int in_slots = 0;

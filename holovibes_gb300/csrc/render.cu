@@ -502,7 +502,7 @@ __device__ __forceinline__ bool in_reticle(size_t e, int W, int H, unsigned int 
     return static_cast<unsigned int>(dx * dx + dy * dy) <= r2;
 }
 
-__global__ void k_pct_hist(const float* __restrict__ f, int W, int H, unsigned int r2, int use_reticle,
+__global__ void k_pct_hist(const float* __restrict__ f, int W, int H, int pitch, unsigned int r2, int use_reticle,
                            const PctState* __restrict__ st, int d, unsigned int* __restrict__ hist,
                            const CycleCtl* ctl)
 {
@@ -522,7 +522,8 @@ __global__ void k_pct_hist(const float* __restrict__ f, int W, int H, unsigned i
     {
         if (!in_reticle(e, W, H, r2, use_reticle))
             continue;
-        const unsigned int k = float_key(f[e]);
+        const size_t a = pitch == W ? e : (e / W) * static_cast<size_t>(pitch) + e % W;
+        const unsigned int k = float_key(f[a]);
         const unsigned int dig = (k >> sft) & dm;
         if ((k & hm) == pre0)
             atomicAdd(&sh[0][dig], 1u);
@@ -640,8 +641,16 @@ size_t percentile_workspace(size_t n)
 hv_status percentile(const float* frame, int W, int H, float lower, float upper, float reticle_scale, float* range,
                      void* work, cudaStream_t st, const CycleCtl* ctl)
 {
+    return percentile_pitched(frame, W, H, W, lower, upper, reticle_scale, range, work, st, ctl);
+}
+
+// The W x H sub-image of rows `pitch` floats apart (the YZ cut's columns between the offsets,
+// compute_percentile_yz_view's cudaMemcpy2DAsync, percentile.cu:230-250).
+hv_status percentile_pitched(const float* frame, int W, int H, int pitch, float lower, float upper,
+                             float reticle_scale, float* range, void* work, cudaStream_t st, const CycleCtl* ctl)
+{
     const size_t n = static_cast<size_t>(W) * H;
-    if (n == 0)
+    if (n == 0 || pitch < W)
         return HV_INVALID_VALUE;
     unsigned int* hist = static_cast<unsigned int*>(work);  // 3 passes x 2 ranks x PCT_BINS
     PctState* state = reinterpret_cast<PctState*>(hist + 3 * 2 * PCT_BINS);
@@ -663,7 +672,8 @@ hv_status percentile(const float* frame, int W, int H, float lower, float upper,
         grid = 152 * 4;
     for (int d = 0; d < 3; ++d)
     {
-        k_pct_hist<<<grid, EW_THREADS, 0, st>>>(frame, W, H, r2, use_reticle, state, d, hist + d * 2 * PCT_BINS, ctl);
+        k_pct_hist<<<grid, EW_THREADS, 0, st>>>(frame, W, H, pitch, r2, use_reticle, state, d, hist + d * 2 * PCT_BINS,
+                                                ctl);
         HV_LAUNCH_CHECK();
         k_pct_select<<<1, 1024, 0, st>>>(hist + d * 2 * PCT_BINS, state, d, lower, upper, range, ctl);
         HV_LAUNCH_CHECK();

@@ -227,6 +227,19 @@ void settings_default(hv_settings* s)
     s->filter2d_n2 = 1;
     s->filter2d_smooth_low = 0;
     s->filter2d_smooth_high = 1;
+    // XZ / YZ windows: View_XZ / View_YZ defaults (view_struct.hh), CutsContrastPOffset{2},
+    // TimeTransformationCutsOutputBufferSize{512}
+    s->cuts_enabled = 0;
+    s->x_start = s->x_width = s->y_start = s->y_width = 0;
+    s->xz_accumulation = s->yz_accumulation = 1;
+    s->xz_log_enabled = s->yz_log_enabled = 0;
+    s->xz_contrast_enabled = s->yz_contrast_enabled = 0;
+    s->xz_contrast_auto_refresh = s->yz_contrast_auto_refresh = 1;
+    s->xz_contrast_invert = s->yz_contrast_invert = 0;
+    s->xz_contrast_min = s->yz_contrast_min = 1.0f;
+    s->xz_contrast_max = s->yz_contrast_max = 65535.0f;
+    s->cuts_contrast_offset = 2;
+    s->cuts_buffer_size = 512;
 }
 
 hv_status settings_from_json(const char* text, hv_settings* s)
@@ -316,6 +329,26 @@ hv_status settings_from_value(const json::Value& doc, hv_settings* s, bool lenie
         {{"image_rendering", "filter2d", "outer_radius"}, 0, &out.filter2d_n2},
         {{"advanced", "filter2d_smooth", "low"}, 0, &out.filter2d_smooth_low},
         {{"advanced", "filter2d_smooth", "high"}, 0, &out.filter2d_smooth_high},
+        {{"view", "x", "start"}, 0, &out.x_start},
+        {{"view", "x", "width"}, 0, &out.x_width},
+        {{"view", "y", "start"}, 0, &out.y_start},
+        {{"view", "y", "width"}, 0, &out.y_width},
+        {{"view", "window", "xz", "output_image_accumulation"}, 0, &out.xz_accumulation},
+        {{"view", "window", "yz", "output_image_accumulation"}, 0, &out.yz_accumulation},
+        {{"view", "window", "xz", "log_enabled"}, 2, &out.xz_log_enabled},
+        {{"view", "window", "yz", "log_enabled"}, 2, &out.yz_log_enabled},
+        {{"view", "window", "xz", "contrast", "enabled"}, 2, &out.xz_contrast_enabled},
+        {{"view", "window", "xz", "contrast", "auto_refresh"}, 2, &out.xz_contrast_auto_refresh},
+        {{"view", "window", "xz", "contrast", "invert"}, 2, &out.xz_contrast_invert},
+        {{"view", "window", "xz", "contrast", "min"}, 1, &out.xz_contrast_min},
+        {{"view", "window", "xz", "contrast", "max"}, 1, &out.xz_contrast_max},
+        {{"view", "window", "yz", "contrast", "enabled"}, 2, &out.yz_contrast_enabled},
+        {{"view", "window", "yz", "contrast", "auto_refresh"}, 2, &out.yz_contrast_auto_refresh},
+        {{"view", "window", "yz", "contrast", "invert"}, 2, &out.yz_contrast_invert},
+        {{"view", "window", "yz", "contrast", "min"}, 1, &out.yz_contrast_min},
+        {{"view", "window", "yz", "contrast", "max"}, 1, &out.yz_contrast_max},
+        {{"advanced", "contrast", "frame_index_offset"}, 0, &out.cuts_contrast_offset},
+        {{"advanced", "buffer_size", "time_transformation_cuts"}, 0, &out.cuts_buffer_size},
         {{"view", "window", "xy", "output_image_accumulation"}, 0, &out.accumulation},
         {{"view", "window", "xy", "log_enabled"}, 2, &out.log_enabled},
         {{"view", "window", "xy", "contrast", "enabled"}, 2, &out.contrast_enabled},
@@ -440,6 +473,26 @@ void settings_to_value(const hv_settings* s, json::Value& doc)
     set_num(doc, {"image_rendering", "filter2d", "outer_radius"}, s->filter2d_n2);
     set_num(doc, {"advanced", "filter2d_smooth", "low"}, s->filter2d_smooth_low);
     set_num(doc, {"advanced", "filter2d_smooth", "high"}, s->filter2d_smooth_high);
+    set_num(doc, {"view", "x", "start"}, s->x_start);
+    set_num(doc, {"view", "x", "width"}, s->x_width);
+    set_num(doc, {"view", "y", "start"}, s->y_start);
+    set_num(doc, {"view", "y", "width"}, s->y_width);
+    for (int w = 0; w < 2; ++w)
+    {
+        const char* win = w == 0 ? "xz" : "yz";
+        set_num(doc, {"view", "window", win, "output_image_accumulation"}, w == 0 ? s->xz_accumulation : s->yz_accumulation);
+        set_bool(doc, {"view", "window", win, "log_enabled"}, (w == 0 ? s->xz_log_enabled : s->yz_log_enabled) != 0);
+        set_bool(doc, {"view", "window", win, "contrast", "enabled"},
+                 (w == 0 ? s->xz_contrast_enabled : s->yz_contrast_enabled) != 0);
+        set_bool(doc, {"view", "window", win, "contrast", "auto_refresh"},
+                 (w == 0 ? s->xz_contrast_auto_refresh : s->yz_contrast_auto_refresh) != 0);
+        set_bool(doc, {"view", "window", win, "contrast", "invert"},
+                 (w == 0 ? s->xz_contrast_invert : s->yz_contrast_invert) != 0);
+        set_num(doc, {"view", "window", win, "contrast", "min"}, w == 0 ? s->xz_contrast_min : s->yz_contrast_min);
+        set_num(doc, {"view", "window", win, "contrast", "max"}, w == 0 ? s->xz_contrast_max : s->yz_contrast_max);
+    }
+    set_num(doc, {"advanced", "contrast", "frame_index_offset"}, s->cuts_contrast_offset);
+    set_num(doc, {"advanced", "buffer_size", "time_transformation_cuts"}, s->cuts_buffer_size);
     set_num(doc, {"view", "window", "xy", "output_image_accumulation"}, s->accumulation);
     set_bool(doc, {"view", "window", "xy", "log_enabled"}, s->log_enabled != 0);
     set_bool(doc, {"view", "window", "xy", "contrast", "enabled"}, s->contrast_enabled != 0);
@@ -550,6 +603,19 @@ hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd)
     }
     if (s->camera_fps < 0)
         s->camera_fps = 0;
+    if (s->xz_accumulation < 0)
+        s->xz_accumulation = 0;
+    if (s->yz_accumulation < 0)
+        s->yz_accumulation = 0;
+    if (s->cuts_contrast_offset < 0)
+        s->cuts_contrast_offset = 0;
+    if (s->cuts_buffer_size < 1)
+        s->cuts_buffer_size = 1;
+    if (s->cuts_enabled && !cuts_supported(s->time_transformation_size))
+    {
+        set_last_error_msg("time cuts: time window above 512 frames");
+        return HV_ERR_UNSUPPORTED;
+    }
     // Filter2dApi::set_filter2d_n1 / n2 (filter2d_api.cc:27-63): 0 <= n1 < n2
     if (s->filter2d_enabled && (s->filter2d_n1 < 0 || s->filter2d_n2 <= s->filter2d_n1 ||
                                 s->filter2d_smooth_low < 0 || s->filter2d_smooth_high < 0))
@@ -575,6 +641,17 @@ hv_status settings_validate(hv_settings* s, const hv_frame_desc* fd)
         if (s->fft_shift && ((fd->width & 1) || (fd->height & 1)))
         {
             set_last_error_msg("fftshift needs even width and height");
+            return HV_INVALID_VALUE;
+        }
+        // the cursor band must stay inside the frame (fill_32bit_slices reads x + y W up to xmax,
+        // ymax); a cursor outside the frame leaves the cuts as they are (fourier_transform.cc:484)
+        if (s->cuts_enabled && (s->x_width < 0 || s->y_width < 0 || s->x_start < 0 || s->y_start < 0 ||
+                                (s->x_start < static_cast<int>(fd->width) &&
+                                 s->x_start + s->x_width >= static_cast<int>(fd->width)) ||
+                                (s->y_start < static_cast<int>(fd->height) &&
+                                 s->y_start + s->y_width >= static_cast<int>(fd->height))))
+        {
+            set_last_error_msg("time cuts: cursor band outside the frame");
             return HV_INVALID_VALUE;
         }
         if (s->filter2d_enabled)

@@ -122,6 +122,27 @@ typedef struct hv_settings
     int32_t filter2d_n2;             /* image_rendering.filter2d.outer_radius */
     int32_t filter2d_smooth_low;     /* advanced.filter2d_smooth.low: cosine roll-off of the inner edge */
     int32_t filter2d_smooth_high;    /* advanced.filter2d_smooth.high: cosine roll-off of the outer edge */
+    int32_t cuts_enabled;            /* CutsViewEnabled: XZ (T x W) and YZ (H x T) time-transformation cuts */
+    int32_t x_start;                 /* view.x.start: first column of the YZ cut's band */
+    int32_t x_width;                 /* view.x.width: the band is columns x_start .. x_start + x_width */
+    int32_t y_start;                 /* view.y.start: first row of the XZ cut's band */
+    int32_t y_width;                 /* view.y.width */
+    int32_t xz_accumulation;         /* view.window.xz.output_image_accumulation */
+    int32_t yz_accumulation;         /* view.window.yz.output_image_accumulation */
+    int32_t xz_log_enabled;          /* view.window.xz.log_enabled */
+    int32_t yz_log_enabled;          /* view.window.yz.log_enabled */
+    int32_t xz_contrast_enabled;     /* view.window.xz.contrast.enabled */
+    int32_t xz_contrast_auto_refresh;
+    int32_t xz_contrast_invert;
+    float xz_contrast_min;
+    float xz_contrast_max;
+    int32_t yz_contrast_enabled;     /* view.window.yz.contrast.* */
+    int32_t yz_contrast_auto_refresh;
+    int32_t yz_contrast_invert;
+    float yz_contrast_min;
+    float yz_contrast_max;
+    int32_t cuts_contrast_offset;    /* advanced.contrast.frame_index_offset: bins skipped at both ends */
+    int32_t cuts_buffer_size;        /* advanced.buffer_size.time_transformation_cuts: cut outputs kept */
 } hv_settings;
 
 /* ------------------------------------------------------------------------------------------
@@ -181,6 +202,16 @@ hv_status hv_pipe_join(hv_pipe* p);
 hv_status hv_pipe_get_contrast_range(hv_pipe* p, float* min_out, float* max_out);
 /* Copies the last float frame fed to the contrast stage (gpu_postprocess_frame) into dst (host). */
 hv_status hv_pipe_get_float_frame(hv_pipe* p, float* dst);
+/* Time-transformation cuts (CutsViewEnabled): each rendered window also produces an XZ image
+ * (T rows x W, row t = bin / component t) and a YZ image (H rows x T) into their own output
+ * queues (gpu_output_queue_xz / _yz, Backend/sources/core/pipe.cc:504-514). which: 0 = XZ, 1 = YZ. */
+enum { HV_CUT_XZ = 0, HV_CUT_YZ = 1 };
+size_t hv_pipe_cut_output_count(hv_pipe* p, int which);
+/* Copies the oldest cut output (W*T or H*T uint16) into dst; as hv_pipe_pull_output. */
+hv_status hv_pipe_pull_cut(hv_pipe* p, int which, uint16_t* dst, int mem, int64_t timeout_us);
+/* The last cut float image fed to its contrast stage (host dst, may be NULL) and the view's
+ * contrast range (range_out[2], may be NULL). */
+hv_status hv_pipe_get_cut_float_frame(hv_pipe* p, int which, float* dst, float* range_out);
 /* Copies the time ring storage (T frames of complex64, slot order) and its start/size. */
 hv_status hv_pipe_get_ring(hv_pipe* p, void* dst_host, int32_t* start, int32_t* size);
 /* Number of kernels this pipe launched since creation. */
@@ -309,6 +340,15 @@ size_t hv_phase_increase_workspace(size_t npix);
  * min(npix, 16384) pixels as the reference's block reduction reads them. */
 hv_status hv_rescale_float(const float* in_f32, size_t npix, const void* minmax, float post_scale, float* out_f32,
                            void* stream);
+/* XZ / YZ slices (fill_32bit_slices, stft.cu:17-115): with X_t(x, y) = sum_s ring[s][y W + x]
+ * weights[t][s] for every t < T (weights: all T rows, e.g. hv_stft_weights(w, T, 0, T-1), the
+ * eigenvector columns for PCA, hv_ssa_weights with pmin 0, pmax T-1),
+ * xz[t][x] = mean over y in [ymin, ymax] of view(X_t(x, y)), yz[y][t] = mean over x in [xmin, xmax];
+ * view: hypotf (modulus, phase increase), hypotf^2 (squared modulus), atanf(Im/Re) + pi/2
+ * (argument), 0 for other types. T <= 512; `work` needs hv_time_cuts_workspace bytes. */
+hv_status hv_time_cuts(const void* ring_c64, int T, int width, int height, const void* weights_c64, int xmin, int xmax,
+                       int ymin, int ymax, int img_type, float* xz_f32, float* yz_f32, void* work, void* stream);
+size_t hv_time_cuts_workspace(int width, int height, int T, int xmin, int xmax, int ymin, int ymax);
 /* STFT weights W[k][t] = exp(-2*pi*i*(pmin+k)*t/T), k <= pmax-pmin, computed in FP64. */
 hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* stream);
 

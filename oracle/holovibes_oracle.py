@@ -433,6 +433,48 @@ def rescale_float(img: np.ndarray) -> np.ndarray:
 
 
 # ----------------------------------------------------------------------------------------
+# time-transformation cuts (stft.cu:17-115, fourier_transform.cc:462-503)
+# ----------------------------------------------------------------------------------------
+
+
+def cut_view(X: np.ndarray, img_type: str) -> np.ndarray:
+    """fill_32bit_slices' per-element view: hypotf for MODULUS / PHASE_INCREASE / COMPOSITE, its
+    square for SQUARED_MODULUS, atanf(Im / Re) + pi/2 for ARGUMENT (float32 quotient and atan,
+    the pi/2 added in double), 0 for the others."""
+    if img_type in ("MODULUS", "PHASE_INCREASE", "COMPOSITE"):
+        return np.abs(X)
+    if img_type == "SQUARED_MODULUS":
+        return np.abs(X) ** 2
+    if img_type == "ARGUMENT":
+        with np.errstate(divide="ignore", invalid="ignore"):
+            q = (X.imag.astype(F32) / X.real.astype(F32)).astype(F32)
+        return (np.arctan(q).astype(F32).astype(np.float64) + math.pi / 2).astype(F32).astype(np.float64)
+    return np.zeros(X.shape)
+
+
+def time_cuts(p_acc: np.ndarray, xmin: int, xmax: int, ymin: int, ymax: int, img_type: str):
+    """XZ[t][x] = mean over y in [ymin, ymax] of view(p_acc[t][y][x]) (T x W) and
+    YZ[y][t] = mean over x in [xmin, xmax] (H x T), p_acc holding all T bins / components."""
+    v_xz = cut_view(p_acc[:, ymin:ymax + 1, :], img_type)  # [T, ny, W]
+    v_yz = cut_view(p_acc[:, :, xmin:xmax + 1], img_type)  # [T, H, nx]
+    return v_xz.mean(axis=1), v_yz.mean(axis=2).T
+
+
+def all_bins(storage: np.ndarray, time_transformation: str, V: np.ndarray | None = None, q_start: int = 0,
+             q_width: int = 0) -> np.ndarray:
+    """The reference's gpu_p_acc_buffer with every bin / component: the STFT (stft.cu:9-15), H V
+    (PCA), FFT_t(H V_Q V_Q^H) (SSA_STFT), the ring itself (NONE, fourier_transform.cc:213-224)."""
+    T = storage.shape[0]
+    if time_transformation == "STFT":
+        return stft_bins(storage, 0, T - 1)
+    if time_transformation == "PCA":
+        return pca_project(storage, V, 0, T - 1)
+    if time_transformation == "SSA_STFT":
+        return ssa_stft_bins(storage, V, q_start, q_width, 0, T - 1)
+    return storage.copy()
+
+
+# ----------------------------------------------------------------------------------------
 # a13-a16: views (tools_conversion.cu:11-103,199-218; converts.cc:50-62)
 # ----------------------------------------------------------------------------------------
 
@@ -680,6 +722,26 @@ class OracleSettings:
     filter2d_n2: int = 1
     filter2d_smooth_low: int = 0
     filter2d_smooth_high: int = 1
+    cuts_enabled: bool = False
+    x_start: int = 0
+    x_width: int = 0
+    y_start: int = 0
+    y_width: int = 0
+    xz_accumulation: int = 1
+    yz_accumulation: int = 1
+    xz_log_enabled: bool = False
+    yz_log_enabled: bool = False
+    xz_contrast_enabled: bool = False
+    xz_contrast_auto_refresh: bool = True
+    xz_contrast_invert: bool = False
+    xz_contrast_min: float = 1.0
+    xz_contrast_max: float = 65535.0
+    yz_contrast_enabled: bool = False
+    yz_contrast_auto_refresh: bool = True
+    yz_contrast_invert: bool = False
+    yz_contrast_min: float = 1.0
+    yz_contrast_max: float = 65535.0
+    cuts_contrast_offset: int = 2
 
 
 @dataclass
@@ -688,6 +750,71 @@ class OracleOutput:
     contrast: tuple
     ushort: np.ndarray
     autocontrast_applied: bool = False
+    cuts: list | None = None  # [XZ, YZ] CutOutput when the cuts are enabled
+
+
+@dataclass
+class CutOutput:
+    float_frame: np.ndarray  # XZ: T x W, YZ: H x T, fed to the view's contrast stage
+    contrast: tuple
+    ushort: np.ndarray
+    autocontrast_applied: bool = False
+
+
+def cut_autocontrast(img32: np.ndarray, which: int, s: "OracleSettings") -> tuple[float, float]:
+    """autocontrast_caller for XZ / YZ (rendering.cc:305-340, percentile.cu:139-250): the bins
+    offset .. T-1-offset (rows of XZ, columns of YZ; the whole window when that range is empty),
+    or for XZ the reticle disc of the whole T x W image when the reticle is displayed."""
+    T = s.time_transformation_size
+    off = s.cuts_contrast_offset if 2 * s.cuts_contrast_offset < T else 0
+    if which == 0 and s.reticle_display:
+        return autocontrast(img32, s.contrast_lower, s.contrast_upper, s.reticle_scale)
+    if which == 0:
+        return autocontrast(img32[off:T - off], s.contrast_lower, s.contrast_upper)
+    return autocontrast(img32[:, off:T - off], s.contrast_lower, s.contrast_upper)
+
+
+class CutModel:
+    """One cut window's post-processing (image_accumulation.cc:159-257, rendering.cc:75-340,
+    percentile.cu:139-250, converts.cc:321-350): accumulation, log10, autocontrast gated like the
+    XY view on its own queue (bins offset .. T-1-offset; XZ over the reticle disc when the
+    reticle is displayed), contrast and uint16."""
+
+    def __init__(self, s: "OracleSettings", which: int):
+        self.which = which
+        p = "xz" if which == 0 else "yz"
+        self.A = getattr(s, p + "_accumulation")
+        self.log = getattr(s, p + "_log_enabled")
+        self.enabled = getattr(s, p + "_contrast_enabled")
+        self.invert = getattr(s, p + "_contrast_invert")
+        self.pending = self.enabled and getattr(s, p + "_contrast_auto_refresh")
+        self.crange = (getattr(s, p + "_contrast_min"), getattr(s, p + "_contrast_max"))
+        T = s.time_transformation_size
+        shape = (T, s.width) if which == 0 else (s.height, T)
+        self.acc = Accumulator(self.A, shape) if self.A > 1 else None
+        self.s = s
+        self.img = np.zeros(shape)
+
+    def push(self, img: np.ndarray | None) -> CutOutput:
+        s = self.s
+        if img is not None:
+            self.img = img
+        img = self.img
+        if self.acc is not None:
+            img = self.acc.push(img)
+        if self.log:
+            img = log10_view(img)
+        img32 = img.astype(F32)
+        applied = False
+        if self.enabled and self.pending:
+            r = self.acc.ring if self.acc is not None else None
+            if r is None or r.is_full() or r.size == 1:
+                applied = True
+                self.crange = cut_autocontrast(img32, self.which, s)
+                if r is None or r.is_full():
+                    self.pending = False
+        c = apply_contrast(img32, self.crange[0], self.crange[1], self.invert) if self.enabled else img32
+        return CutOutput(float_frame=img, contrast=self.crange, ushort=float_to_ushort(c), autocontrast_applied=applied)
 
 
 class OraclePipe:
@@ -716,6 +843,7 @@ class OraclePipe:
         self.crange = (s.contrast_min, s.contrast_max)
         self.last_V = None
         self.phase_increase = PhaseIncrease() if s.image_type == "PHASE_INCREASE" else None
+        self.cut_models = [CutModel(s, 0), CutModel(s, 1)] if s.cuts_enabled else None
 
     def process_batch(self, raw: np.ndarray, convert_f32=True) -> OracleOutput | None:
         s = self.s
@@ -787,8 +915,16 @@ class OraclePipe:
             c = apply_contrast(img32, self.crange[0], self.crange[1], s.contrast_invert)
         else:
             c = img32
+        cuts = None
+        if self.cut_models is not None:
+            slices = (None, None)
+            if s.x_start < s.width and s.y_start < s.height:
+                p_acc = all_bins(self.ring.data, s.time_transformation, self.last_V, s.q_start, s.q_width)
+                slices = time_cuts(p_acc, s.x_start, s.x_start + s.x_width, s.y_start, s.y_start + s.y_width,
+                                   s.image_type)
+            cuts = [m.push(sl) for m, sl in zip(self.cut_models, slices)]
         return OracleOutput(float_frame=img, contrast=self.crange, ushort=float_to_ushort(c),
-                            autocontrast_applied=applied)
+                            autocontrast_applied=applied, cuts=cuts)
 
     def _should_autocontrast(self) -> bool:
         """should_apply_contrast (rendering.hh:168-181)."""

@@ -34,7 +34,15 @@ def _oracle_settings(fd, s):
         unwrap_2d=bool(s.unwrap_2d), lens_mode="fp64" if s.lens_mode == 0 else "ref32", camera_fps=s.camera_fps,
         q_start=s.q_start, q_width=s.q_width, filter2d_enabled=bool(s.filter2d_enabled), filter2d_n1=s.filter2d_n1,
         filter2d_n2=s.filter2d_n2, filter2d_smooth_low=s.filter2d_smooth_low,
-        filter2d_smooth_high=s.filter2d_smooth_high)
+        filter2d_smooth_high=s.filter2d_smooth_high, cuts_enabled=bool(s.cuts_enabled), x_start=s.x_start,
+        x_width=s.x_width, y_start=s.y_start, y_width=s.y_width, xz_accumulation=s.xz_accumulation,
+        yz_accumulation=s.yz_accumulation, xz_log_enabled=bool(s.xz_log_enabled),
+        yz_log_enabled=bool(s.yz_log_enabled), xz_contrast_enabled=bool(s.xz_contrast_enabled),
+        xz_contrast_auto_refresh=bool(s.xz_contrast_auto_refresh), xz_contrast_invert=bool(s.xz_contrast_invert),
+        xz_contrast_min=s.xz_contrast_min, xz_contrast_max=s.xz_contrast_max,
+        yz_contrast_enabled=bool(s.yz_contrast_enabled), yz_contrast_auto_refresh=bool(s.yz_contrast_auto_refresh),
+        yz_contrast_invert=bool(s.yz_contrast_invert), yz_contrast_min=s.yz_contrast_min,
+        yz_contrast_max=s.yz_contrast_max, cuts_contrast_offset=s.cuts_contrast_offset)
 
 
 CASES = {
@@ -150,6 +158,24 @@ CASES = {
                                         p_start=15, p_width=0, filter2d_enabled=1, filter2d_n1=5, filter2d_n2=28,
                                         filter2d_smooth_low=0, filter2d_smooth_high=3, renorm=1,
                                         contrast_enabled=1), 2),
+    # XZ / YZ time cuts (stft.cu:17-115): bands of several rows / columns, per-view accumulation,
+    # log, autocontrast over the offset bins or the reticle disc
+    "as_stft_cuts_mod": (64, 48, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=16,
+                                          time_stride=8, batch_size=8, z_distance=0.3, pixel_size=20.0, p_start=1,
+                                          renorm=1, contrast_enabled=1, cuts_enabled=1, x_start=10, x_width=2,
+                                          y_start=20, y_width=3, xz_accumulation=2, xz_contrast_enabled=1,
+                                          yz_contrast_enabled=1, yz_log_enabled=1, cuts_contrast_offset=2), 5),
+    "fresnel_stft_cuts_arg_reticle": (64, 64, 1, dict(space_transformation=1, time_transformation=1,
+                                                       time_transformation_size=8, time_stride=4, batch_size=4,
+                                                       lambda_=785e-9, z_distance=0.45, pixel_size=12.0, image_type=2,
+                                                       p_start=1, renorm=0, contrast_enabled=1, reticle_display=1,
+                                                       reticle_scale=0.6, cuts_enabled=1, x_start=40, y_start=7,
+                                                       xz_contrast_enabled=1, yz_contrast_enabled=1,
+                                                       yz_contrast_invert=1, yz_accumulation=3), 5),
+    "none_cuts_sqmod": (32, 32, 2, dict(space_transformation=0, time_transformation=0, time_transformation_size=4,
+                                         time_stride=4, batch_size=4, image_type=1, p_start=1, renorm=1,
+                                         contrast_enabled=0, cuts_enabled=1, x_start=31, y_start=0, y_width=31,
+                                         xz_contrast_enabled=0, yz_contrast_enabled=1, cuts_contrast_offset=2), 3),
     "fresnel_stft_ref32_big_endian": (128, 64, 2, dict(space_transformation=1, time_transformation=1,
                                                         time_transformation_size=4, time_stride=4, batch_size=4,
                                                         z_distance=0.3, pixel_size=20.0, p_start=2, p_width=1,
@@ -166,6 +192,33 @@ def _raw(W, H, depth, n, seed):
     else:
         g = Interferogram(width=W, height=H, seed=seed)
     return g.frames(0, n)
+
+
+def _check_cuts(pipe, s, ref, case):
+    """XZ / YZ: float images against the oracle (argument: atan(Im/Re) jumps by pi where Re
+    changes sign, allowed on a few elements), contrast range and uint16 output bit-exact on the
+    GPU's own float images."""
+    for which in (hv.CUT_XZ, hv.CUT_YZ):
+        cref = ref.cuts[which]
+        got_f, got_range = pipe.cut_float_frame(which)
+        assert got_f.shape == cref.float_frame.shape, case
+        if s.image_type == hv.IMG_ARGUMENT:
+            d = np.abs(got_f - cref.float_frame)
+            assert np.mean(d > 1e-3) < 1e-2, (case, which)
+        else:
+            assert rel_l2(got_f, cref.float_frame) <= 1e-4, (case, which)
+        enabled = s.xz_contrast_enabled if which == hv.CUT_XZ else s.yz_contrast_enabled
+        invert = s.xz_contrast_invert if which == hv.CUT_XZ else s.yz_contrast_invert
+        if enabled:
+            if cref.autocontrast_applied:
+                expected = O.cut_autocontrast(got_f, which, _oracle_settings(pipe.fd, s))
+                assert np.float32(got_range[0]) == np.float32(expected[0]), (case, which)
+                assert np.float32(got_range[1]) == np.float32(expected[1]), (case, which)
+            u16 = O.float_to_ushort(O.apply_contrast(got_f, got_range[0], got_range[1], bool(invert)))
+        else:
+            u16 = O.float_to_ushort(got_f)
+        assert pipe.cut_output_count(which) == 1, case
+        assert np.array_equal(pipe.pull_cut(which), u16), (case, which)
 
 
 @pytest.mark.gpu
@@ -220,6 +273,8 @@ def test_pipe_matches_oracle(cuda, case):
         else:
             ref_u16 = O.float_to_ushort(got_f)
         assert np.array_equal(got_u16, ref_u16), case
+        if s.cuts_enabled:
+            _check_cuts(pipe, s, ref, case)
     assert outputs > 0
     ring, start, size = pipe.ring()
     assert start == oracle.ring.start and size == oracle.ring.size
