@@ -40,6 +40,7 @@ constexpr int TC_MAX_RAW = 8;
 constexpr int TC_KC = 64;           // pixels (K elements) per chunk
 constexpr int TC_ROWS = 128;        // M rows of the operand tile (2T <= 128, zero padded)
 constexpr int TILE_BYTES = TC_ROWS * TC_KC * 2;  // one BF16 tile: 16 KB
+constexpr int COV_TC_MAX_T = 1024;               // tiled kernel: (T / 64)^2 / 2 tiles of 128 x 128
 using tc::fence_async_smem;
 using tc::mbar_arrive;
 using tc::mbar_init;
@@ -310,8 +311,8 @@ __global__ void k_cov_tc_reduce(const float* __restrict__ part, int T, int npart
     double g00 = 0, g11 = 0, g01 = 0, g10 = 0;
     const int c0 = blockIdx.y * per_slice;
     const int c1 = min(nparts, c0 + per_slice);
-#pragma unroll 4
     const size_t stride = packed ? static_cast<size_t>(TC_ROWS) * 64 : static_cast<size_t>(R) * R;
+#pragma unroll 4
     for (int c = c0; c < c1; ++c)
     {
         const float* G = part + static_cast<size_t>(c) * stride;
@@ -323,6 +324,277 @@ __global__ void k_cov_tc_reduce(const float* __restrict__ part, int T, int npart
     atomicAdd(&cov[e].x, g00 + g11);
     if (i != j)
         atomicAdd(&cov[e].y, mirror ? -(g01 - g10) : (g01 - g10));
+}
+
+int sm_count();
+
+// ------------------------------------------------------------------------------ tiled (T > 64)
+// G (2T x 2T) in 128 x 128 tiles (bm, bn), bm <= bn: operand A = Y rows of frames 64 bm .. 64 bm + 63,
+// B = frames 64 bn .. (the same as A on diagonal tiles; frames >= T are zero-filled by the tensor
+// copy). CTA (split ks, tile tp) walks the 64-pixel chunks of split ks: the loader brings the A
+// and B chunks ([64 frames][64 px] complex, 32 KB each) into a ring of R raw stages, the eight
+// converter warps split them into Ah / Al / Bh / Bl (one converted stage), the MMA warp issues
+// Ah Bh^T, Ah Bl^T, Al Bh^T (M = N = 128, K = 16) into three TMEM accumulators. The CTAs of one
+// split stream the same chunks at the same time, so each chunk comes from HBM about once and the
+// other tiles read it from L2.
+constexpr int TT_FRAMES = 64;                          // frames per operand tile (128 rows of Y)
+constexpr uint32_t TT_RAW_HALF = TT_FRAMES * TC_KC * 8;  // one [64 frames][64 px] complex chunk: 32 KB
+constexpr int TT_MAX_RAW = 3;
+
+__device__ __forceinline__ void tile_pair(int tp, int nb, int& bm, int& bn)
+{
+    int m = 0, rem = tp;
+    while (rem >= nb - m)
+    {
+        rem -= nb - m;
+        ++m;
+    }
+    bm = m;
+    bn = m + rem;
+}
+
+// part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * npairs + tp)
+__global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc_tiled(const __grid_constant__ CUtensorMap ring_map,
+                                                                size_t npix, int nb, int npairs,
+                                                                size_t chunks_per_split, int raw_stages,
+                                                                float* __restrict__ part, int* __restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* tiles = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);  // Ah, Al, Bh, Bl (16 KB each)
+    uint8_t* raw_base = tiles + 4 * TILE_BYTES;
+    __shared__ __align__(8) uint64_t raw_full[TT_MAX_RAW], raw_empty[TT_MAX_RAW];
+    __shared__ __align__(8) uint64_t a_full, a_empty, done, drain;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int R = raw_stages;
+    const int tp = static_cast<int>(blockIdx.x % static_cast<unsigned>(npairs));
+    const int ks = static_cast<int>(blockIdx.x / static_cast<unsigned>(npairs));
+    int bm, bn;
+    tile_pair(tp, nb, bm, bn);
+    const bool diag = bm == bn;
+    const uint32_t raw_bytes = 2 * TT_RAW_HALF;
+    const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
+    const size_t c_begin = static_cast<size_t>(ks) * chunks_per_split;
+    size_t c_end = c_begin + chunks_per_split;
+    if (c_end > nchunks)
+        c_end = nchunks;
+    const int nmine = static_cast<int>(c_end > c_begin ? c_end - c_begin : 0);
+    volatile int* abort = &s_abort;
+    constexpr uint32_t N = TC_ROWS;  // accumulator columns per product
+
+    if (tid == 0)
+    {
+        for (int i = 0; i < R; ++i)
+        {
+            mbar_init(&raw_full[i], 1);
+            mbar_init(&raw_empty[i], TC_CONVERTERS / 32);
+        }
+        mbar_init(&a_full, TC_CONVERTERS / 32);
+        mbar_init(&a_empty, 1);
+        mbar_init(&done, 1);
+        mbar_init(&drain, 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == TC_MMA_WARP)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(512u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == TC_LOAD_WARP)
+    {
+        // ------------------------------------------------------------------ loader (TMA)
+        if (lane == 0)
+        {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(&ring_map) : "memory");
+            for (int m = 0; m < nmine; ++m)
+            {
+                const int r = m % R;
+                if (m >= R)
+                    mbar_wait(&raw_empty[r], static_cast<uint32_t>(((m / R) - 1) & 1), abort);
+                if (*abort)
+                    break;
+                const int x = static_cast<int>(2 * TC_KC * (c_begin + m));
+                tc::mbar_arrive_expect_tx(&raw_full[r], diag ? TT_RAW_HALF : raw_bytes);
+                uint8_t* dst = raw_base + r * raw_bytes;
+                tc::tma_load_2d(dst, &ring_map, x, bm * TT_FRAMES, &raw_full[r]);
+                if (!diag)
+                    tc::tma_load_2d(dst + TT_RAW_HALF, &ring_map, x, bn * TT_FRAMES, &raw_full[r]);
+            }
+        }
+        __syncwarp();
+    }
+    else if (warp < TC_MMA_WARP)
+    {
+        // ------------------------------------------------------------------ converters
+        // row t of a raw chunk (frame t: 64 complex samples, 512 B): lane l reads pixels 2l, 2l+1
+        // and writes 32-bit words of rows 2t (Re) and 2t + 1 (Im), K group l / 4
+        const int g = lane >> 2;
+        const uint32_t j4 = static_cast<uint32_t>(lane & 3) * 4u;
+        for (int it = 0; it < nmine; ++it)
+        {
+            const int r = it % R;
+            mbar_wait(&raw_full[r], static_cast<uint32_t>((it / R) & 1), abort);
+            if (it >= 1)
+                mbar_wait(&a_empty, static_cast<uint32_t>((it - 1) & 1), abort);
+            if (*abort)
+                break;
+            const uint8_t* raw = raw_base + r * raw_bytes;
+            for (int op = 0; op < (diag ? 1 : 2); ++op)
+            {
+                const uint8_t* src = raw + op * TT_RAW_HALF;
+                uint8_t* th = tiles + (2 * op) * TILE_BYTES;
+                uint8_t* tl = th + TILE_BYTES;
+                for (int t = warp; t < TT_FRAMES; t += TC_CONVERTERS / 32)
+                {
+                    const float4 f = reinterpret_cast<const float4*>(src + t * (TC_KC * 8))[lane];
+                    uint32_t reh, rel, imh, iml;
+                    tc::split2(f.x, f.z, reh, rel);
+                    tc::split2(f.y, f.w, imh, iml);
+                    const uint32_t ore = tile_offset(2 * t, g) + j4, oim = tile_offset(2 * t + 1, g) + j4;
+                    *reinterpret_cast<uint32_t*>(th + ore) = reh;
+                    *reinterpret_cast<uint32_t*>(th + oim) = imh;
+                    *reinterpret_cast<uint32_t*>(tl + ore) = rel;
+                    *reinterpret_cast<uint32_t*>(tl + oim) = iml;
+                }
+            }
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0)
+            {
+                mbar_arrive(&raw_empty[r]);
+                mbar_arrive(&a_full);
+            }
+        }
+    }
+    else if (lane == 0)
+    {
+        // ------------------------------------------------------------------ MMA issuer
+        const uint32_t idesc = instr_desc(TC_ROWS, TC_ROWS);
+        const uint32_t ah = smem_u32(tiles), al = ah + TILE_BYTES;
+        const uint32_t bh = diag ? ah : ah + 2 * TILE_BYTES, bl = diag ? al : ah + 3 * TILE_BYTES;
+        for (int it = 0; it < nmine; ++it)
+        {
+            mbar_wait(&a_full, static_cast<uint32_t>(it & 1), abort);
+            if (*abort)
+                break;
+            tc_fence_after();
+#pragma unroll
+            for (int s2 = 0; s2 < TC_KC / 16; ++s2)
+            {
+                const uint64_t dah = smem_desc(ah + s2 * 32), dal = smem_desc(al + s2 * 32);
+                const uint64_t dbh = smem_desc(bh + s2 * 32), dbl = smem_desc(bl + s2 * 32);
+                const uint32_t acc = (it > 0 || s2 > 0) ? 1u : 0u;
+                mma_bf16(tmem, dah, dbh, idesc, acc);          // Ah Bh^T
+                mma_bf16(tmem + N, dah, dbl, idesc, acc);      // Ah Bl^T
+                mma_bf16(tmem + 2 * N, dal, dbh, idesc, acc);  // Al Bh^T
+            }
+            mma_commit(&a_empty);
+        }
+        mma_commit(&done);
+    }
+    // epilogue: warps 0-3 read rows 32w .. 32w + 31 of the tile
+    if (warp < 4)
+    {
+        mbar_wait(&done, 0, abort);
+        tc_fence_after();
+        const int r = warp * 32 + lane;
+        float* dst = part + static_cast<size_t>(blockIdx.x) * TC_ROWS * TC_ROWS + static_cast<size_t>(r) * TC_ROWS;
+        for (int c0 = 0; c0 < TC_ROWS; c0 += 16)
+        {
+            float v[16], w1[16], w2[16];
+            const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
+            tmem_ld16(taddr, v);
+            tmem_ld16(taddr + N, w1);
+            tmem_ld16(taddr + 2 * N, w2);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                dst[c0 + i] = nmine ? v[i] + w1[i] + w2[i] : 0.f;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (s_abort)
+    {
+        // a wait gave up: the copies and MMAs already issued finish before shared and tensor memory
+        // are released (bounded waits)
+        if (warp == TC_LOAD_WARP && lane == 0)
+        {
+            for (int m = nmine - R > 0 ? nmine - R : 0; m < nmine; ++m)
+                mbar_wait(&raw_full[m % R], static_cast<uint32_t>((m / R) & 1));
+            atomicExch(err, 1);
+        }
+        if (warp == TC_MMA_WARP && lane == 0)
+        {
+            mma_commit(&drain);
+            mbar_wait(&drain, 0);
+        }
+        __syncthreads();
+    }
+    if (warp == TC_MMA_WARP)
+    {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+    }
+}
+
+// cov[i][j] from the tiled partials: row 2i of G is row 2 (i % 64) of tile row i / 64; the upper
+// triangle (i <= j) is read from tile (i / 64, j / 64) and mirrored. Sums in FP64 over the splits.
+__global__ void k_cov_tc_tiled_reduce(const float* __restrict__ part, int T, int nb, int npairs, int nsplit,
+                                      double2* __restrict__ cov)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= T * T)
+        return;
+    const int ei = e / T, ej = e % T;
+    const bool mirror = ei > ej;
+    const int i = mirror ? ej : ei, j = mirror ? ei : ej;
+    const int bm = i / TT_FRAMES, bn = j / TT_FRAMES;
+    const int tp = bm * nb - bm * (bm - 1) / 2 + (bn - bm);  // rows 0 .. bm-1 hold nb, nb-1, ... tiles
+    const int ri = 2 * (i % TT_FRAMES), cj = 2 * (j % TT_FRAMES);
+    double g00 = 0, g11 = 0, g01 = 0, g10 = 0;
+    for (int k = 0; k < nsplit; ++k)
+    {
+        const float* G = part + (static_cast<size_t>(k) * npairs + tp) * TC_ROWS * TC_ROWS;
+        g00 += G[ri * TC_ROWS + cj];
+        g11 += G[(ri + 1) * TC_ROWS + cj + 1];
+        g01 += G[ri * TC_ROWS + cj + 1];
+        g10 += G[(ri + 1) * TC_ROWS + cj];
+    }
+    const double im = i == j ? 0.0 : (g01 - g10);
+    cov[e] = make_double2(g00 + g11, mirror ? -im : im);
+}
+
+struct TiledPlan
+{
+    int nb, npairs, nsplit;
+    size_t chunks_per_split;
+};
+
+TiledPlan tiled_plan(int T, size_t npix)
+{
+    TiledPlan p;
+    p.nb = (T + TT_FRAMES - 1) / TT_FRAMES;
+    p.npairs = p.nb * (p.nb + 1) / 2;
+    const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
+    int ns = sm_count() / p.npairs;  // one wave of persistent CTAs
+    if (ns < 1)
+        ns = 1;
+    if (static_cast<size_t>(ns) > nchunks)
+        ns = static_cast<int>(nchunks);
+    p.chunks_per_split = (nchunks + ns - 1) / ns;
+    p.nsplit = static_cast<int>((nchunks + p.chunks_per_split - 1) / p.chunks_per_split);
+    return p;
 }
 
 struct TcPlan
@@ -370,10 +642,15 @@ TcPlan tc_plan(int T, size_t npix)
 
 }  // namespace
 
-bool cov_tc_supported(int T) { return T >= 1 && 2 * T <= TC_ROWS; }
+bool cov_tc_supported(int T) { return T >= 1 && T <= COV_TC_MAX_T; }
 
 size_t cov_tc_workspace(int T, size_t npix)
 {
+    if (2 * T > TC_ROWS)
+    {
+        const TiledPlan q = tiled_plan(T, npix);
+        return static_cast<size_t>(q.nsplit) * q.npairs * TC_ROWS * TC_ROWS * sizeof(float) + 256;
+    }
     const TcPlan p = tc_plan(T, npix);
     const size_t per = p.packed ? static_cast<size_t>(TC_ROWS) * 64 : static_cast<size_t>(4) * T * T;
     return static_cast<size_t>(p.ctas) * per * sizeof(float) + 256;
@@ -392,6 +669,29 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
     {
         set_last_error_msg("tensor-core covariance: at most 2^29 pixels per frame");
         return HV_ERR_UNSUPPORTED;
+    }
+    if (2 * T > TC_ROWS)
+    {
+        const TiledPlan q = tiled_plan(T, npix);
+        CUtensorMap tmap;
+        if (!tc::encode_tmap_2d_f32(&tmap, ring, 2 * npix, static_cast<uint64_t>(T), npix * 8, 2 * TC_KC,
+                                    static_cast<uint32_t>(TT_FRAMES)))
+        {
+            set_last_error_msg("tensor-core covariance: cuTensorMapEncodeTiled failed");
+            return HV_ERR_CUDA;
+        }
+        const int raw = 2;
+        const size_t smem = 4 * static_cast<size_t>(TILE_BYTES) + raw * 2 * static_cast<size_t>(TT_RAW_HALF) + 1024;
+        HV_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+        float* tpart = static_cast<float*>(work);
+        k_cov_tc_tiled<<<q.nsplit * q.npairs, TC_THREADS, smem, st>>>(tmap, npix, q.nb, q.npairs, q.chunks_per_split,
+                                                                      raw, tpart, err);
+        HV_LAUNCH_CHECK();
+        k_cov_tc_tiled_reduce<<<(T * T + 255) / 256, 256, 0, st>>>(tpart, T, q.nb, q.npairs, q.nsplit, cov);
+        HV_LAUNCH_CHECK();
+        count_launch(2);
+        return HV_OK;
     }
     const TcPlan p = tc_plan(T, npix);
     // raw stages: T x 64 complex samples (T x 512 B) each, as many as fit beside the two A stages

@@ -1,4 +1,5 @@
-"""The two covariance engines (FP32 SIMT and tcgen05 split-BF16 tensor cores) and the two Jacobi
+"""The two covariance engines (FP32 SIMT and tcgen05 split-BF16 tensor cores: one tile for T <= 64,
+128 x 128 tiles of the Gram matrix above) and the two Jacobi
 paths (shared-memory for T <= 64, global-memory beyond) against the FP64 oracle.
 Tolerances: SIMT covariance rel-L2 <= 1e-6, tensor-core (BF16x3, FP32 accumulation) <= 2e-5;
 eigenvalues within 1e-6 of the largest (FP64 Jacobi on the FP64-summed covariance)."""
@@ -25,7 +26,9 @@ def _ring(T, npix, seed):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode,tol", [(1, 1e-6), (2, 2e-5)])
-@pytest.mark.parametrize("T,npix", [(32, 65536), (64, 4096), (17, 1000), (1, 64), (32, 64 * 1024 + 8)])
+@pytest.mark.parametrize("T,npix", [(32, 65536), (64, 4096), (17, 1000), (1, 64), (32, 64 * 1024 + 8),
+                                    # tiled tensor-core kernel (T > 64): 128 x 128 tiles of G, split K
+                                    (65, 1000), (96, 8192), (128, 65536), (200, 4104), (512, 16384)])
 def test_covariance_engine(cuda, mode, tol, T, npix):
     ring = _ring(T, npix, T * 3 + mode)
     rd = dev(ring)
