@@ -650,37 +650,41 @@ template <>
 __device__ __forceinline__ float jac_threshold<float>() { return 2.5e-7f; }
 
 template <class R>
-__global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __restrict__ Ain, double2* __restrict__ Vout,
-                                                            int T, int Tp, double* __restrict__ evals)
+struct JacScratch
 {
-    extern __shared__ __align__(16) unsigned char js_raw[];
-    Cx<R>* js = reinterpret_cast<Cx<R>*>(js_raw);
-    const int LD = T + 1;
-    Cx<R>* A = js;
-    Cx<R>* V = js + T * LD;
-    __shared__ int pp[JS_MAX_T / 2], pq[JS_MAX_T / 2], act[JS_MAX_T / 2];
-    __shared__ R rc[JS_MAX_T / 2], rs[JS_MAX_T / 2], rcp[JS_MAX_T / 2], rsp[JS_MAX_T / 2];
-    __shared__ short2 blk[(JS_MAX_T / 2) * (JS_MAX_T / 2 + 1) / 2];
+    int pp[JS_MAX_T / 2], pq[JS_MAX_T / 2], act[JS_MAX_T / 2];
+    R rc[JS_MAX_T / 2], rs[JS_MAX_T / 2], rcp[JS_MAX_T / 2], rsp[JS_MAX_T / 2];
+    short2 blk[(JS_MAX_T / 2) * (JS_MAX_T / 2 + 1) / 2];
+};
+
+// Cyclic sweeps over the T x T Hermitian A (T <= 64, shared memory, leading dimension LD) with the
+// round-robin pairing, accumulating V <- V J; at most max_sweeps sweeps, ending after a sweep
+// without rotation. A rotation is applied when |a_pq| exceeds both the relative threshold and
+// `floor`. Every thread of the block (NT of them) calls it; returns whether any rotation was applied.
+__device__ __forceinline__ float jhypot(float a, float b) { return hypotf(a, b); }
+__device__ __forceinline__ double jhypot(double a, double b) { return hypot(a, b); }
+__device__ __forceinline__ float jsqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double jsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float jabs(float a) { return fabsf(a); }
+__device__ __forceinline__ double jabs(double a) { return fabs(a); }
+
+template <class R, int NT>
+__device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T, int Tp, int LD, JacScratch<R>& sc, R floor, int max_sweeps)
+{
     const int tid = threadIdx.x;
     const int npairs = Tp / 2;
-    for (int e = tid; e < T * T; e += JS_THREADS)
-    {
-        const int i = e / T, j = e % T;
-        const double2 a = Ain[e];
-        A[i * LD + j] = {static_cast<R>(a.x), static_cast<R>(i == j ? 0.0 : a.y)};
-        V[i * LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
-    }
     const int nblocks = npairs * (npairs + 1) / 2;
-    for (int e = tid; e < nblocks; e += JS_THREADS)
+    for (int e = tid; e < nblocks; e += NT)
     {
         int k1 = 0;
         while ((k1 + 1) * (k1 + 2) / 2 <= e)
             ++k1;
-        blk[e] = make_short2(static_cast<short>(k1), static_cast<short>(e - k1 * (k1 + 1) / 2));
+        sc.blk[e] = make_short2(static_cast<short>(k1), static_cast<short>(e - k1 * (k1 + 1) / 2));
     }
     __syncthreads();
     const R thr = jac_threshold<R>();
-    for (int sweep = 0; sweep < JAC_MAX_SWEEPS; ++sweep)
+    bool any = false;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep)
     {
         int sweep_active = 0;
         for (int step = 0; step < Tp - 1; ++step)
@@ -701,41 +705,41 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                     b = (step - k + (Tp - 1)) % (Tp - 1);
                 }
                 const int p = a < b ? a : b, q = a < b ? b : a;
-                pp[k] = p;
-                pq[k] = q;
+                sc.pp[k] = p;
+                sc.pq[k] = q;
                 R c = 1, s = 0, cph = 1, sph = 0;
                 if (q < T)
                 {
                     const Cx<R> apq = A[p * LD + q];
-                    const R mag = hypot(apq.x, apq.y);
+                    const R mag = jhypot(apq.x, apq.y);
                     const R app = A[p * LD + p].x, aqq = A[q * LD + q].x;
-                    if (mag > R(1e-30) && mag > thr * sqrt(fabs(app * aqq)))
+                    if (mag > R(1e-30) && mag > floor && mag > thr * jsqrt(jabs(app * aqq)))
                     {
                         cph = apq.x / mag;
                         sph = apq.y / mag;
                         const R tau = (aqq - app) / (R(2) * mag);
-                        const R t = (tau >= 0 ? R(1) : R(-1)) / (fabs(tau) + sqrt(R(1) + tau * tau));
-                        c = R(1) / sqrt(R(1) + t * t);
+                        const R t = (tau >= 0 ? R(1) : R(-1)) / (jabs(tau) + jsqrt(R(1) + tau * tau));
+                        c = R(1) / jsqrt(R(1) + t * t);
                         s = t * c;
                         active = 1;
                     }
                 }
-                rc[k] = c;
-                rs[k] = s;
-                rcp[k] = cph;
-                rsp[k] = sph;
-                act[k] = active;
+                sc.rc[k] = c;
+                sc.rs[k] = s;
+                sc.rcp[k] = cph;
+                sc.rsp[k] = sph;
+                sc.act[k] = active;
             }
             if (!__syncthreads_or(active))
                 continue;
             sweep_active = 1;
             // A <- J^H A J, block by block (k1 >= k2) with the mirror block
-            for (int e = tid; e < nblocks; e += JS_THREADS)
+            for (int e = tid; e < nblocks; e += NT)
             {
-                const int k1 = blk[e].x, k2 = blk[e].y;
-                if (!act[k1] && !act[k2])
+                const int k1 = sc.blk[e].x, k2 = sc.blk[e].y;
+                if (!sc.act[k1] && !sc.act[k2])
                     continue;
-                const int r0 = pp[k1], r1 = pq[k1], c0 = pp[k2], c1 = pq[k2];
+                const int r0 = sc.pp[k1], r1 = sc.pq[k1], c0 = sc.pp[k2], c1 = sc.pq[k2];
                 const bool hr1 = r1 < T, hc1 = c1 < T;
                 const Cx<R> z = {0, 0};
                 Cx<R> B[2][2];
@@ -744,8 +748,8 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                 B[1][0] = hr1 ? A[r1 * LD + c0] : z;
                 B[1][1] = (hr1 && hc1) ? A[r1 * LD + c1] : z;
                 // X = B J2, J2 = [[c, s], [-s e^{-i phi}, c e^{-i phi}]]
-                const R c2 = rc[k2], s2 = rs[k2];
-                const Cx<R> em2 = {rcp[k2], -rsp[k2]};
+                const R c2 = sc.rc[k2], s2 = sc.rs[k2];
+                const Cx<R> em2 = {sc.rcp[k2], -sc.rsp[k2]};
                 Cx<R> X[2][2];
 #pragma unroll
                 for (int r = 0; r < 2; ++r)
@@ -755,8 +759,8 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                     X[r][1] = {s2 * B[r][0].x + c2 * b1.x, s2 * B[r][0].y + c2 * b1.y};
                 }
                 // Y = J1^H X: row0 = c X0 - s e^{i phi} X1, row1 = s X0 + c e^{i phi} X1
-                const R c1r = rc[k1], s1r = rs[k1];
-                const Cx<R> ep1 = {rcp[k1], rsp[k1]};
+                const R c1r = sc.rc[k1], s1r = sc.rs[k1];
+                const Cx<R> ep1 = {sc.rcp[k1], sc.rsp[k1]};
                 Cx<R> Y[2][2];
 #pragma unroll
                 for (int cc = 0; cc < 2; ++cc)
@@ -765,7 +769,7 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                     Y[0][cc] = {c1r * X[0][cc].x - s1r * x1.x, c1r * X[0][cc].y - s1r * x1.y};
                     Y[1][cc] = {s1r * X[0][cc].x + c1r * x1.x, s1r * X[0][cc].y + c1r * x1.y};
                 }
-                if (k1 == k2 && act[k1])
+                if (k1 == k2 && sc.act[k1])
                 {
                     Y[0][1] = z;
                     Y[1][0] = z;
@@ -791,14 +795,14 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
                 }
             }
             // V <- V J for the active pairs
-            for (int e = tid; e < npairs * T; e += JS_THREADS)
+            for (int e = tid; e < npairs * T; e += NT)
             {
                 const int k = e / T, r = e % T;
-                if (!act[k])
+                if (!sc.act[k])
                     continue;
-                const int p = pp[k], q = pq[k];
-                const R c = rc[k], s = rs[k];
-                const Cx<R> em = {rcp[k], -rsp[k]};
+                const int p = sc.pp[k], q = sc.pq[k];
+                const R c = sc.rc[k], s = sc.rs[k];
+                const Cx<R> em = {sc.rcp[k], -sc.rsp[k]};
                 const Cx<R> vp = V[r * LD + p], vq = cxmul(V[r * LD + q], em);
                 V[r * LD + p] = {c * vp.x - s * vq.x, c * vp.y - s * vq.y};
                 V[r * LD + q] = {s * vp.x + c * vq.x, s * vp.y + c * vq.y};
@@ -807,7 +811,32 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
         }
         if (!sweep_active)
             break;
+        any = true;
     }
+    return any;
+}
+
+template <class R>
+__global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __restrict__ Ain, double2* __restrict__ Vout,
+                                                            int T, int Tp, double* __restrict__ evals)
+{
+    extern __shared__ __align__(16) unsigned char js_raw[];
+    Cx<R>* js = reinterpret_cast<Cx<R>*>(js_raw);
+    const int LD = T + 1;
+    Cx<R>* A = js;
+    Cx<R>* V = js + T * LD;
+    __shared__ JacScratch<R> sc;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < T * T; e += JS_THREADS)
+    {
+        const int i = e / T, j = e % T;
+        const double2 a = Ain[e];
+        A[i * LD + j] = {static_cast<R>(a.x), static_cast<R>(i == j ? 0.0 : a.y)};
+        V[i * LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
+    }
+    __syncthreads();
+    smem_sweeps<R, JS_THREADS>(A, V, T, Tp, LD, sc, R(0), JAC_MAX_SWEEPS);
+    __syncthreads();
     for (int e = tid; e < T * T; e += JS_THREADS)
     {
         const int i = e / T, j = e % T;
@@ -817,13 +846,9 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
         evals[i] = static_cast<double>(A[i * LD + i].x);
 }
 
-// Grid-wide variant for 64 < T <= JC_MAX_T: FP32 sweeps on two working copies of A (the step reads
-// one and writes the other) and on V in global memory (L2 resident), one cooperative grid. Every
-// CTA computes all of a step's rotations itself from the step's input copy, which no CTA writes
-// during the step (identical results: same inputs, same arithmetic), into shared memory, so a step
-// is one update phase over the grid's 2 x 2 blocks (each block read and written by one thread) and
-// one grid barrier. The barrier is a bounded sense-reversal barrier: a wait that exceeds about 2 s sets
-// the error flag and every later barrier returns at once, so the kernel ends.
+// Grid-wide kernels (64 < T <= JC_MAX_T) synchronise through a bounded sense-reversal barrier: a
+// wait that exceeds about 2 s sets the error flag and every later barrier returns at once, so the
+// kernel ends.
 constexpr int JC_THREADS = 512;
 constexpr int JC_MAX_T = 512;
 
@@ -877,216 +902,273 @@ __device__ __forceinline__ void grid_barrier(GridBarrier* b)
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(JC_THREADS) k_jacobi_grid(const double2* __restrict__ Ain, Cx<float>* A0,
-                                                            Cx<float>* A1, Cx<float>* V, int T, int Tp,
-                                                            GridBarrier* bar, double2* __restrict__ Vout,
-                                                            double* __restrict__ evals)
+// Block-cyclic variant for 64 < T <= JC_MAX_T: the indices form blocks of 32 (T rounded up to 64
+// with zero rows and columns, which no rotation ever touches), and a sweep pairs the blocks in the
+// round-robin order. A step (one of nblk - 1 per sweep) has two grid phases:
+//   1. each of the nblk / 2 block pairs (I, J) loads its 64 x 64 subproblem A[I u J][I u J] into
+//      shared memory and runs one cyclic sweep of 2 x 2 rotations on it (smem_sweeps), giving the
+//      pair's unitary U (64 x 64);
+//   2. every CTA applies the step's unitaries to 64 x 64 blocks: A[P][Q] <- U_P^H A[P][Q] U_Q for
+//      pair groups P <= Q (and the mirror), V[rows][P] <- V[rows][P] U_P, from one copy of A and V
+//      into the other.
+// A sweep thus covers every index pair like a scalar sweep, with nblk - 1 grid steps instead of
+// T - 1. FP32, the same absolute floor as the scalar kernels; the sweeps end after one without a
+// rotation. Bounded grid barriers as above.
+constexpr int BJ_B = 32;                 // indices per block
+constexpr int BJ_S = 2 * BJ_B;           // subproblem size
+constexpr int BJ_LD = BJ_S + 1;          // shared-memory leading dimension
+constexpr int BJ_THREADS = JS_THREADS;   // smem_sweeps is instantiated for this block size
+constexpr int BJ_MAX_SWEEPS = 40;
+constexpr size_t BJ_SMEM = 3 * static_cast<size_t>(BJ_S) * BJ_LD * sizeof(float2);
+
+__device__ __forceinline__ void bj_pair(int step, int k, int nblk, int& I, int& J)
 {
-    Cx<float>* A = A0;   // input of the current step
-    Cx<float>* An = A1;  // output of the current step
+    int a, b;
+    if (k == 0)
+    {
+        a = nblk - 1;
+        b = step % (nblk - 1);
+    }
+    else
+    {
+        a = (step + k) % (nblk - 1);
+        b = (step - k + (nblk - 1)) % (nblk - 1);
+    }
+    I = a < b ? a : b;
+    J = a < b ? b : a;
+}
+
+// index i < 64 of pair group (I, J): block I then block J
+__device__ __forceinline__ int bj_index(int I, int J, int i) { return i < BJ_B ? I * BJ_B + i : J * BJ_B + i - BJ_B; }
+
+// C = op(A) B for 64 x 64 shared-memory matrices (leading dimension BJ_LD), op(A) = A or A^H.
+// Thread t computes rows 4 (t / 16) .. + 3 and columns t % 16 + 16 j (conflict-free B rows).
+template <bool AH>
+__device__ __forceinline__ void bj_gemm(const Cx<float>* A, const Cx<float>* B, Cx<float>* C)
+{
+    const int r0 = (threadIdx.x >> 4) * 4, cb = threadIdx.x & 15;
+    float2 acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            acc[i][j] = make_float2(0.f, 0.f);
+    for (int k = 0; k < BJ_S; ++k)
+    {
+        Cx<float> a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+        {
+            if (AH)
+            {
+                const Cx<float> v = A[k * BJ_LD + r0 + i];
+                a[i] = {v.x, -v.y};
+            }
+            else
+                a[i] = A[(r0 + i) * BJ_LD + k];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            b[j] = B[k * BJ_LD + cb + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+            {
+                acc[i][j].x = fmaf(a[i].x, b[j].x, fmaf(-a[i].y, b[j].y, acc[i][j].x));
+                acc[i][j].y = fmaf(a[i].x, b[j].y, fmaf(a[i].y, b[j].x, acc[i][j].y));
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            C[(r0 + i) * BJ_LD + cb + 16 * j] = {acc[i][j].x, acc[i][j].y};
+}
+
+__global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __restrict__ Ain, int T, int Tp,
+                                                             Cx<float>* A0, Cx<float>* A1, Cx<float>* V0,
+                                                             Cx<float>* V1, Cx<float>* U, int* flags,
+                                                             GridBarrier* bar, double2* __restrict__ Vout,
+                                                             double* __restrict__ evals)
+{
     using R = float;
-    __shared__ int pp[JC_MAX_T / 2], pq[JC_MAX_T / 2], act[JC_MAX_T / 2];
-    __shared__ R rc[JC_MAX_T / 2], rs[JC_MAX_T / 2], rcp[JC_MAX_T / 2], rsp[JC_MAX_T / 2];
+    extern __shared__ __align__(16) unsigned char bj_raw[];
+    Cx<R>* sm0 = reinterpret_cast<Cx<R>*>(bj_raw);
+    Cx<R>* sm1 = sm0 + BJ_S * BJ_LD;
+    Cx<R>* sm2 = sm1 + BJ_S * BJ_LD;
+    __shared__ JacScratch<R> sc;
+    __shared__ R s_floor;
+    __shared__ int s_rot;
     const int tid = threadIdx.x;
-    const size_t gtid = static_cast<size_t>(blockIdx.x) * JC_THREADS + tid;
-    const size_t gsz = static_cast<size_t>(gridDim.x) * JC_THREADS;
-    const int npairs = Tp / 2;
-    const size_t TT = static_cast<size_t>(T) * T;
+    const size_t gtid = static_cast<size_t>(blockIdx.x) * BJ_THREADS + tid;
+    const size_t gsz = static_cast<size_t>(gridDim.x) * BJ_THREADS;
+    const size_t TT = static_cast<size_t>(Tp) * Tp;
+    const int nblk = Tp / BJ_B, npb = nblk / 2;
     for (size_t e = gtid; e < TT; e += gsz)
     {
-        const int i = static_cast<int>(e / T), j = static_cast<int>(e % T);
-        const double2 a = Ain[e];
+        const int i = static_cast<int>(e / Tp), j = static_cast<int>(e % Tp);
+        const double2 a = (i < T && j < T) ? Ain[static_cast<size_t>(i) * T + j] : make_double2(0.0, 0.0);
         A0[e] = {static_cast<R>(a.x), static_cast<R>(i == j ? 0.0 : a.y)};
-        V[e] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
+        V0[e] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
     }
-    // rotations below the FP32 round-off floor of the matrix (relative to its largest diagonal
-    // entry) are not applied: in near-degenerate noise subspaces the relative test alone never
-    // stops; the FP64 Rayleigh finish recovers the eigenvalues
-    __shared__ R s_floor;
+    if (gtid == 0)
+    {
+        flags[0] = 0;
+        flags[1] = 0;
+        flags[2] = 0;
+    }
+    // rotations below the FP32 round-off level of the matrix are not applied: 3e-7 of its trace
+    // (>= the largest eigenvalue of a covariance). The FP32 block updates of a large matrix leave
+    // off-diagonal entries near that size, which would keep the sweeps going; at this floor the
+    // eigenvectors of separated eigenvalues keep FP32 accuracy (residual ~3e-6 of the largest
+    // eigenvalue at T = 512, the level of the sweeps' own round-off)
     if (tid < 32)
     {
-        R mx = 0;
+        double tr = 0;
         for (int i = tid; i < T; i += 32)
-            mx = fmaxf(mx, fabsf(static_cast<R>(Ain[static_cast<size_t>(i) * T + i].x)));
+            tr += fabs(Ain[static_cast<size_t>(i) * T + i].x);
         for (int o = 16; o > 0; o >>= 1)
-            mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+            tr += __shfl_down_sync(0xffffffffu, tr, o);
         if (tid == 0)
-            s_floor = mx * R(1e-6);
+            s_floor = static_cast<R>(tr * 3e-7);
     }
     grid_barrier(bar);
-    const R thr = jac_threshold<R>();
-    const R abs_floor = s_floor;
-    const size_t nblocks = static_cast<size_t>(npairs) * (npairs + 1) / 2;
-    for (int sweep = 0; sweep < JAC_MAX_SWEEPS; ++sweep)
+    Cx<R>*A = A0, *An = A1, *V = V0, *Vn = V1;
+    const int na = npb * (npb + 1) / 2, nrow = Tp / BJ_S;
+    for (int sweep = 0; sweep < BJ_MAX_SWEEPS; ++sweep)
     {
-        int sweep_active = 0;
-        for (int step = 0; step < Tp - 1; ++step)
+        // three rotating flags: sweep s sets flags[s % 3] and every CTA reads it after the sweep's last
+        // barrier; the one zeroed here was last read before the previous sweep's barriers
+        if (gtid == 0)
+            flags[(sweep + 1) % 3] = 0;
+        for (int step = 0; step < nblk - 1; ++step)
         {
-            int active = 0;
-            for (int k = tid; k < npairs; k += JC_THREADS)
+            // phase 1: one sweep on each pair's subproblem
+            for (int k = blockIdx.x; k < npb; k += gridDim.x)
             {
-                int a, b;
-                if (k == 0)
+                int I, J;
+                bj_pair(step, k, nblk, I, J);
+                for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
                 {
-                    a = Tp - 1;
-                    b = step % (Tp - 1);
+                    const int i = e / BJ_S, j = e % BJ_S;
+                    sm0[i * BJ_LD + j] =
+                        ldcg(A + static_cast<size_t>(bj_index(I, J, i)) * Tp + static_cast<size_t>(bj_index(I, J, j)));
+                    sm1[i * BJ_LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
+                }
+                __syncthreads();
+                const bool rot = smem_sweeps<R, BJ_THREADS>(sm0, sm1, BJ_S, BJ_S, BJ_LD, sc, s_floor, 1);
+                for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
+                {
+                    const int i = e / BJ_S, j = e % BJ_S;
+                    const Cx<R> u = sm1[i * BJ_LD + j];
+                    reinterpret_cast<float2*>(U)[static_cast<size_t>(k) * BJ_S * BJ_S + e] = make_float2(u.x, u.y);
+                }
+                if (rot && tid == 0)
+                    atomicExch(&flags[sweep % 3], 1);
+                __syncthreads();
+            }
+            grid_barrier(bar);
+            // phase 2: apply the unitaries of the step to A (pair groups P <= Q) and V (row chunks)
+            for (int it = blockIdx.x; it < na + nrow * npb; it += gridDim.x)
+            {
+                const Cx<R>* Ug = U;
+                if (it < na)
+                {
+                    int P = 0, rem = it;
+                    while (rem >= npb - P)
+                    {
+                        rem -= npb - P;
+                        ++P;
+                    }
+                    const int Q = P + rem;
+                    int IP, JP, IQ, JQ;
+                    bj_pair(step, P, nblk, IP, JP);
+                    bj_pair(step, Q, nblk, IQ, JQ);
+                    for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
+                    {
+                        const int i = e / BJ_S, j = e % BJ_S;
+                        sm0[i * BJ_LD + j] = ldcg(A + static_cast<size_t>(bj_index(IP, JP, i)) * Tp +
+                                                  static_cast<size_t>(bj_index(IQ, JQ, j)));
+                        sm1[i * BJ_LD + j] = ldcg(Ug + static_cast<size_t>(Q) * BJ_S * BJ_S + e);
+                    }
+                    __syncthreads();
+                    bj_gemm<false>(sm0, sm1, sm2);  // X = A[P][Q] U_Q
+                    __syncthreads();
+                    if (P != Q)
+                    {
+                        for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
+                            sm1[(e / BJ_S) * BJ_LD + e % BJ_S] = ldcg(Ug + static_cast<size_t>(P) * BJ_S * BJ_S + e);
+                        __syncthreads();
+                    }
+                    bj_gemm<true>(sm1, sm2, sm0);  // Y = U_P^H X
+                    __syncthreads();
+                    for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
+                    {
+                        const int i = e / BJ_S, j = e % BJ_S;
+                        const int gi = bj_index(IP, JP, i), gj = bj_index(IQ, JQ, j);
+                        Cx<R> y = sm0[i * BJ_LD + j];
+                        if (P == Q)
+                        {
+                            // exactly Hermitian diagonal group: average with the mirror element
+                            const Cx<R> w = sm0[j * BJ_LD + i];
+                            y = {R(0.5) * (y.x + w.x), i == j ? R(0) : R(0.5) * (y.y - w.y)};
+                        }
+                        An[static_cast<size_t>(gi) * Tp + gj] = y;
+                        if (P != Q)
+                            An[static_cast<size_t>(gj) * Tp + gi] = {y.x, -y.y};
+                    }
                 }
                 else
                 {
-                    a = (step + k) % (Tp - 1);
-                    b = (step - k + (Tp - 1)) % (Tp - 1);
-                }
-                const int p = a < b ? a : b, q = a < b ? b : a;
-                pp[k] = p;
-                pq[k] = q;
-                R c = 1, s = 0, cph = 1, sph = 0;
-                int on = 0;
-                if (q < T)
-                {
-                    const Cx<R> apq = ldcg(A + static_cast<size_t>(p) * T + q);
-                    const R mag = hypotf(apq.x, apq.y);
-                    const R app = ldcg(A + static_cast<size_t>(p) * T + p).x, aqq = ldcg(A + static_cast<size_t>(q) * T + q).x;
-                    if (mag > abs_floor && mag > R(1e-30) && mag > thr * sqrtf(fabsf(app * aqq)))
+                    const int v = it - na, rc = v / npb, P = v % npb;
+                    int IP, JP;
+                    bj_pair(step, P, nblk, IP, JP);
+                    for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
                     {
-                        cph = apq.x / mag;
-                        sph = apq.y / mag;
-                        const R tau = (aqq - app) / (R(2) * mag);
-                        const R t = (tau >= 0 ? R(1) : R(-1)) / (fabsf(tau) + sqrtf(R(1) + tau * tau));
-                        c = R(1) / sqrtf(R(1) + t * t);
-                        s = t * c;
-                        on = 1;
+                        const int i = e / BJ_S, j = e % BJ_S;
+                        sm0[i * BJ_LD + j] =
+                            ldcg(V + static_cast<size_t>(rc * BJ_S + i) * Tp + static_cast<size_t>(bj_index(IP, JP, j)));
+                        sm1[i * BJ_LD + j] = ldcg(Ug + static_cast<size_t>(P) * BJ_S * BJ_S + e);
+                    }
+                    __syncthreads();
+                    bj_gemm<false>(sm0, sm1, sm2);  // V[rows][P] U_P
+                    __syncthreads();
+                    for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
+                    {
+                        const int i = e / BJ_S, j = e % BJ_S;
+                        Vn[static_cast<size_t>(rc * BJ_S + i) * Tp + static_cast<size_t>(bj_index(IP, JP, j))] =
+                            sm2[i * BJ_LD + j];
                     }
                 }
-                rc[k] = c;
-                rs[k] = s;
-                rcp[k] = cph;
-                rsp[k] = sph;
-                act[k] = on;
-                active |= on;
-            }
-            if (!__syncthreads_or(active))
-                continue;  // uniform over the grid: every CTA computed the same rotations
-            sweep_active = 1;
-            // A <- J^H A J on the 2 x 2 blocks (k1 >= k2, plus the mirror block)
-            for (size_t e = gtid; e < nblocks; e += gsz)
-            {
-                int k1 = static_cast<int>((sqrtf(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
-                while (static_cast<size_t>(k1) * (k1 + 1) / 2 > e)
-                    --k1;
-                while (static_cast<size_t>(k1 + 1) * (k1 + 2) / 2 <= e)
-                    ++k1;
-                const int k2 = static_cast<int>(e - static_cast<size_t>(k1) * (k1 + 1) / 2);
-                const int r0 = pp[k1], r1 = pq[k1], c0 = pp[k2], c1 = pq[k2];
-                const bool hr1 = r1 < T, hc1 = c1 < T;
-                const Cx<R> z = {0, 0};
-                auto in = [&](int r, int c) -> const Cx<R>* { return A + static_cast<size_t>(r) * T + c; };
-                auto at = [&](int r, int c) -> Cx<R>& { return An[static_cast<size_t>(r) * T + c]; };
-                Cx<R> B[2][2];
-                B[0][0] = ldcg(in(r0, c0));
-                B[0][1] = hc1 ? ldcg(in(r0, c1)) : z;
-                B[1][0] = hr1 ? ldcg(in(r1, c0)) : z;
-                B[1][1] = (hr1 && hc1) ? ldcg(in(r1, c1)) : z;
-                if (!act[k1] && !act[k2])
-                {
-                    // unchanged block: copied to the step's output (with its mirror)
-                    at(r0, c0) = B[0][0];
-                    if (hc1)
-                        at(r0, c1) = B[0][1];
-                    if (hr1)
-                        at(r1, c0) = B[1][0];
-                    if (hr1 && hc1)
-                        at(r1, c1) = B[1][1];
-                    if (k1 != k2)
-                    {
-                        at(c0, r0) = {B[0][0].x, -B[0][0].y};
-                        if (hc1)
-                            at(c1, r0) = {B[0][1].x, -B[0][1].y};
-                        if (hr1)
-                            at(c0, r1) = {B[1][0].x, -B[1][0].y};
-                        if (hr1 && hc1)
-                            at(c1, r1) = {B[1][1].x, -B[1][1].y};
-                    }
-                    continue;
-                }
-                const R c2 = rc[k2], s2 = rs[k2];
-                const Cx<R> em2 = {rcp[k2], -rsp[k2]};
-                Cx<R> X[2][2];
-#pragma unroll
-                for (int r = 0; r < 2; ++r)
-                {
-                    const Cx<R> b1 = cxmul(B[r][1], em2);
-                    X[r][0] = {c2 * B[r][0].x - s2 * b1.x, c2 * B[r][0].y - s2 * b1.y};
-                    X[r][1] = {s2 * B[r][0].x + c2 * b1.x, s2 * B[r][0].y + c2 * b1.y};
-                }
-                const R c1r = rc[k1], s1r = rs[k1];
-                const Cx<R> ep1 = {rcp[k1], rsp[k1]};
-                Cx<R> Y[2][2];
-#pragma unroll
-                for (int cc = 0; cc < 2; ++cc)
-                {
-                    const Cx<R> x1 = cxmul(X[1][cc], ep1);
-                    Y[0][cc] = {c1r * X[0][cc].x - s1r * x1.x, c1r * X[0][cc].y - s1r * x1.y};
-                    Y[1][cc] = {s1r * X[0][cc].x + c1r * x1.x, s1r * X[0][cc].y + c1r * x1.y};
-                }
-                if (k1 == k2 && act[k1])
-                {
-                    Y[0][1] = z;
-                    Y[1][0] = z;
-                    Y[0][0].y = 0;
-                    Y[1][1].y = 0;
-                }
-                at(r0, c0) = Y[0][0];
-                if (hc1)
-                    at(r0, c1) = Y[0][1];
-                if (hr1)
-                    at(r1, c0) = Y[1][0];
-                if (hr1 && hc1)
-                    at(r1, c1) = Y[1][1];
-                if (k1 != k2)
-                {
-                    at(c0, r0) = {Y[0][0].x, -Y[0][0].y};
-                    if (hc1)
-                        at(c1, r0) = {Y[0][1].x, -Y[0][1].y};
-                    if (hr1)
-                        at(c0, r1) = {Y[1][0].x, -Y[1][0].y};
-                    if (hr1 && hc1)
-                        at(c1, r1) = {Y[1][1].x, -Y[1][1].y};
-                }
-            }
-            // V <- V J for the active pairs
-            for (size_t e = gtid; e < static_cast<size_t>(npairs) * T; e += gsz)
-            {
-                const int k = static_cast<int>(e / T), r = static_cast<int>(e % T);
-                if (!act[k])
-                    continue;
-                const int p = pp[k], q = pq[k];
-                if (q >= T)
-                    continue;
-                const R c = rc[k], s = rs[k];
-                const Cx<R> em = {rcp[k], -rsp[k]};
-                Cx<R>* row = V + static_cast<size_t>(r) * T;
-                const Cx<R> vp = ldcg(row + p), vq = cxmul(ldcg(row + q), em);
-                row[p] = {c * vp.x - s * vq.x, c * vp.y - s * vq.y};
-                row[q] = {s * vp.x + c * vq.x, s * vp.y + c * vq.y};
+                __syncthreads();
             }
             grid_barrier(bar);
-            Cx<float>* t = A;
+            Cx<R>* t = A;
             A = An;
             An = t;
-            if (*reinterpret_cast<volatile int*>(&bar->err))
-                break;
+            t = V;
+            V = Vn;
+            Vn = t;
         }
-        if (!sweep_active || *reinterpret_cast<volatile int*>(&bar->err))
+        if (tid == 0)
+            s_rot = *reinterpret_cast<volatile int*>(&flags[sweep % 3]);
+        __syncthreads();
+        if (!s_rot)
+            break;  // the same value in every CTA: read after the sweep's last barrier
+        if (reinterpret_cast<volatile int*>(&bar->err)[0])
             break;
     }
-    for (size_t e = gtid; e < TT; e += gsz)
+    for (size_t e = gtid; e < static_cast<size_t>(T) * T; e += gsz)
     {
-        const Cx<R> v = ldcg(V + e);
+        const int i = static_cast<int>(e / T), j = static_cast<int>(e % T);
+        const Cx<R> v = ldcg(V + static_cast<size_t>(i) * Tp + j);
         Vout[e] = make_double2(static_cast<double>(v.x), static_cast<double>(v.y));
     }
     for (size_t i = gtid; i < static_cast<size_t>(T); i += gsz)
-        evals[i] = static_cast<double>(ldcg(A + i * T + i).x);
+        evals[i] = static_cast<double>(ldcg(A + i * Tp + i).x);
 }
+
 
 // FP64 finish of each eigenpair from the FP64 covariance (intact in the shared-memory paths):
 // normalise the eigenvector column in FP64 and take its Rayleigh quotient v^H A v as the
@@ -1180,7 +1262,12 @@ size_t pca_eigh_workspace(int T)
     size_t bytes = static_cast<size_t>(T) * T * sizeof(double2) + static_cast<size_t>(2 * Tp) * sizeof(double) +
                    static_cast<size_t>(T) * sizeof(double) + static_cast<size_t>(Tp) * sizeof(int) + 256;
     if (T > JS_MAX_T && T <= JC_MAX_T)
-        bytes += 3 * static_cast<size_t>(T) * T * sizeof(float2) + 256;  // FP32 A (x2) and V, grid barrier
+    {
+        // block Jacobi: FP32 A and V (two copies each) of the size rounded up to 64, the step's
+        // unitaries, convergence flags and the grid barrier
+        const size_t Tb = (static_cast<size_t>(T) + BJ_S - 1) / BJ_S * BJ_S;
+        bytes += 256 + 4 * Tb * Tb * sizeof(float2) + (Tb / BJ_S) * BJ_S * BJ_S * sizeof(float2) + 256;
+    }
     return bytes;
 }
 
@@ -1216,26 +1303,39 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     }
     else if (T <= JC_MAX_T && g_eig_precision == HV_EIG_FP32)
     {
-        // FP32 sweeps over a cooperative grid (A and V copies in the workspace), then the FP64 finish
+        // FP32 block-cyclic sweeps over a cooperative grid (A and V copies in the workspace), then
+        // the FP64 finish
+        const int Tb = (T + BJ_S - 1) / BJ_S * BJ_S;
+        const size_t tb2 = static_cast<size_t>(Tb) * Tb * sizeof(float2);
         size_t off2 = (off + static_cast<size_t>(Tp) * sizeof(int) + 255) & ~static_cast<size_t>(255);
-        Cx<float>* A32 = reinterpret_cast<Cx<float>*>(base + off2);
-        off2 += static_cast<size_t>(T) * T * sizeof(float2);
-        Cx<float>* A32b = reinterpret_cast<Cx<float>*>(base + off2);
-        off2 += static_cast<size_t>(T) * T * sizeof(float2);
-        Cx<float>* V32 = reinterpret_cast<Cx<float>*>(base + off2);
-        off2 += static_cast<size_t>(T) * T * sizeof(float2);
-        GridBarrier* bar = reinterpret_cast<GridBarrier*>(base + off2);
-        HV_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), st));
+        Cx<float>* A0 = reinterpret_cast<Cx<float>*>(base + off2);
+        Cx<float>* A1 = reinterpret_cast<Cx<float>*>(base + off2 + tb2);
+        Cx<float>* V0 = reinterpret_cast<Cx<float>*>(base + off2 + 2 * tb2);
+        Cx<float>* V1 = reinterpret_cast<Cx<float>*>(base + off2 + 3 * tb2);
+        off2 += 4 * tb2;
+        Cx<float>* U = reinterpret_cast<Cx<float>*>(base + off2);
+        off2 += static_cast<size_t>(Tb / BJ_S) * BJ_S * BJ_S * sizeof(float2);
+        int* flags = reinterpret_cast<int*>(base + off2);
+        GridBarrier* bar = reinterpret_cast<GridBarrier*>(base + off2 + 64);
+        HV_CUDA_TRY(cudaMemsetAsync(base + off2, 0, 128, st));
+        static int max_per_sm = -1;
+        if (max_per_sm < 0)
+        {
+            HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(BJ_SMEM)));
+            HV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, k_jacobi_block, BJ_THREADS, BJ_SMEM));
+        }
         int sms = 0;
         HV_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
-        const size_t npairs = static_cast<size_t>(Tp / 2);
-        const size_t items = npairs * (npairs + 1) / 2 + npairs * T;
-        int nb = static_cast<int>((items + 2 * JC_THREADS - 1) / (2 * JC_THREADS));
-        nb = nb < 1 ? 1 : (nb > sms ? sms : nb);
-        int Ti = T, Tpi = Tp;
+        const int npb = Tb / BJ_S, na = npb * (npb + 1) / 2;
+        int nb = na + (Tb / BJ_S) * npb;  // phase-2 items: A blocks and V blocks
+        const int cap = sms * (max_per_sm > 0 ? max_per_sm : 1);
+        nb = nb > cap ? cap : nb;
+        int Ti = T, Tbi = Tb;
         const double2* cin = cov;
-        void* args[] = {&cin, &A32, &A32b, &V32, &Ti, &Tpi, &bar, &V, &ev_unsorted};
-        HV_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_jacobi_grid), nb, JC_THREADS, args, 0, st));
+        void* args[] = {&cin, &Ti, &Tbi, &A0, &A1, &V0, &V1, &U, &flags, &bar, &V, &ev_unsorted};
+        HV_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_jacobi_block), nb, BJ_THREADS, args, BJ_SMEM,
+                                                st));
         count_launch();
     }
     if (T <= JS_MAX_T || (T <= JC_MAX_T && g_eig_precision == HV_EIG_FP32))
