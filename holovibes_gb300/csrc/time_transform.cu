@@ -668,9 +668,47 @@ __device__ __forceinline__ double jsqrt(double a) { return sqrt(a); }
 __device__ __forceinline__ float jabs(float a) { return fabsf(a); }
 __device__ __forceinline__ double jabs(double a) { return fabs(a); }
 
-template <class R, int NT>
-__device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T, int Tp, int LD, JacScratch<R>& sc, R floor, int max_sweeps)
+// Pair k of step `step` of a sweep over Tp indices. Round-robin order; with `split` (Tp = 2h, the
+// two halves already nearly diagonal) the h cross steps (i, h + (i + step) mod h) come first, then
+// the h - 1 round-robin steps inside both halves at once.
+__device__ __forceinline__ void sweep_pair(int step, int k, int Tp, bool split, int& p, int& q)
 {
+    int n = Tp, s = step, kk = k, base = 0;
+    if (split)
+    {
+        const int h = Tp / 2;
+        if (step < h)
+        {
+            p = k;
+            q = h + (k + step) % h;
+            return;
+        }
+        n = h;
+        s = step - h;
+        kk = k % (h / 2);
+        base = (k / (h / 2)) * h;
+    }
+    int a, b;
+    if (kk == 0)
+    {
+        a = n - 1;
+        b = s % (n - 1);
+    }
+    else
+    {
+        a = (s + kk) % (n - 1);
+        b = (s - kk + (n - 1)) % (n - 1);
+    }
+    p = base + (a < b ? a : b);
+    q = base + (a < b ? b : a);
+}
+
+// N > 0 fixes T = Tp = N and LD = N + 1 at compile time (index arithmetic by shifts).
+template <class R, int NT, int N = 0>
+__device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScratch<R>& sc, R floor, int max_sweeps,
+                            bool split = false)
+{
+    const int T = N > 0 ? N : T_, Tp = N > 0 ? N : Tp_, LD = N > 0 ? N + 1 : LD_;
     const int tid = threadIdx.x;
     const int npairs = Tp / 2;
     const int nblocks = npairs * (npairs + 1) / 2;
@@ -693,18 +731,8 @@ __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T, int Tp, int LD, JacScratc
             if (tid < npairs)
             {
                 const int k = tid;
-                int a, b;
-                if (k == 0)
-                {
-                    a = Tp - 1;
-                    b = step % (Tp - 1);
-                }
-                else
-                {
-                    a = (step + k) % (Tp - 1);
-                    b = (step - k + (Tp - 1)) % (Tp - 1);
-                }
-                const int p = a < b ? a : b, q = a < b ? b : a;
+                int p, q;
+                sweep_pair(step, k, Tp, split, p, q);
                 sc.pp[k] = p;
                 sc.pq[k] = q;
                 R c = 1, s = 0, cph = 1, sph = 0;
@@ -906,8 +934,9 @@ __device__ __forceinline__ void grid_barrier(GridBarrier* b)
 // with zero rows and columns, which no rotation ever touches), and a sweep pairs the blocks in the
 // round-robin order. A step (one of nblk - 1 per sweep) has two grid phases:
 //   1. each of the nblk / 2 block pairs (I, J) loads its 64 x 64 subproblem A[I u J][I u J] into
-//      shared memory and runs one cyclic sweep of 2 x 2 rotations on it (smem_sweeps), giving the
-//      pair's unitary U (64 x 64);
+//      shared memory and runs one cyclic sweep of 2 x 2 rotations on it (smem_sweeps; the I x J
+//      pairs first, then the pairs inside I and J, which earlier steps left nearly diagonal and
+//      whose steps are mostly skipped), giving the pair's unitary U (64 x 64);
 //   2. every CTA applies the step's unitaries to 64 x 64 blocks: A[P][Q] <- U_P^H A[P][Q] U_Q for
 //      pair groups P <= Q (and the mirror), V[rows][P] <- V[rows][P] U_P, from one copy of A and V
 //      into the other.
@@ -917,7 +946,7 @@ __device__ __forceinline__ void grid_barrier(GridBarrier* b)
 constexpr int BJ_B = 32;                 // indices per block
 constexpr int BJ_S = 2 * BJ_B;           // subproblem size
 constexpr int BJ_LD = BJ_S + 1;          // shared-memory leading dimension
-constexpr int BJ_THREADS = JS_THREADS;   // smem_sweeps is instantiated for this block size
+constexpr int BJ_THREADS = 512;
 constexpr int BJ_MAX_SWEEPS = 40;
 constexpr size_t BJ_SMEM = 3 * static_cast<size_t>(BJ_S) * BJ_LD * sizeof(float2);
 
@@ -942,22 +971,24 @@ __device__ __forceinline__ void bj_pair(int step, int k, int nblk, int& I, int& 
 __device__ __forceinline__ int bj_index(int I, int J, int i) { return i < BJ_B ? I * BJ_B + i : J * BJ_B + i - BJ_B; }
 
 // C = op(A) B for 64 x 64 shared-memory matrices (leading dimension BJ_LD), op(A) = A or A^H.
-// Thread t computes rows 4 (t / 16) .. + 3 and columns t % 16 + 16 j (conflict-free B rows).
+// Thread t computes rows BJ_RPT (t / 16) .. + BJ_RPT - 1 and columns t % 16 + 16 j (conflict-free B rows).
+constexpr int BJ_RPT = BJ_S * BJ_S / (BJ_THREADS * 4);  // rows per thread
+static_assert(BJ_RPT * 16 * (BJ_THREADS / 16) == BJ_S * BJ_S / 4 && BJ_RPT * (BJ_THREADS / 16) == BJ_S, "gemm map");
 template <bool AH>
 __device__ __forceinline__ void bj_gemm(const Cx<float>* A, const Cx<float>* B, Cx<float>* C)
 {
-    const int r0 = (threadIdx.x >> 4) * 4, cb = threadIdx.x & 15;
-    float2 acc[4][4];
+    const int r0 = (threadIdx.x >> 4) * BJ_RPT, cb = threadIdx.x & 15;
+    float2 acc[BJ_RPT][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < BJ_RPT; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             acc[i][j] = make_float2(0.f, 0.f);
     for (int k = 0; k < BJ_S; ++k)
     {
-        Cx<float> a[4], b[4];
+        Cx<float> a[BJ_RPT], b[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < BJ_RPT; ++i)
         {
             if (AH)
             {
@@ -971,7 +1002,7 @@ __device__ __forceinline__ void bj_gemm(const Cx<float>* A, const Cx<float>* B, 
         for (int j = 0; j < 4; ++j)
             b[j] = B[k * BJ_LD + cb + 16 * j];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < BJ_RPT; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j)
             {
@@ -980,7 +1011,7 @@ __device__ __forceinline__ void bj_gemm(const Cx<float>* A, const Cx<float>* B, 
             }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < BJ_RPT; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             C[(r0 + i) * BJ_LD + cb + 16 * j] = {acc[i][j].x, acc[i][j].y};
@@ -989,7 +1020,8 @@ __device__ __forceinline__ void bj_gemm(const Cx<float>* A, const Cx<float>* B, 
 __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __restrict__ Ain, int T, int Tp,
                                                              Cx<float>* A0, Cx<float>* A1, Cx<float>* V0,
                                                              Cx<float>* V1, Cx<float>* U, int* flags,
-                                                             GridBarrier* bar, double2* __restrict__ Vout,
+                                                             double* fro2, GridBarrier* bar,
+                                                             double2* __restrict__ Vout,
                                                              double* __restrict__ evals)
 {
     using R = float;
@@ -1005,35 +1037,37 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
     const size_t gsz = static_cast<size_t>(gridDim.x) * BJ_THREADS;
     const size_t TT = static_cast<size_t>(Tp) * Tp;
     const int nblk = Tp / BJ_B, npb = nblk / 2;
+    // the squared Frobenius norm is summed on the way (FP64, one atomic per CTA into fro2)
+    __shared__ double s_fro[BJ_THREADS / 32];
+    double fro = 0.0;
     for (size_t e = gtid; e < TT; e += gsz)
     {
         const int i = static_cast<int>(e / Tp), j = static_cast<int>(e % Tp);
         const double2 a = (i < T && j < T) ? Ain[static_cast<size_t>(i) * T + j] : make_double2(0.0, 0.0);
+        fro += a.x * a.x + (i == j ? 0.0 : a.y * a.y);
         A0[e] = {static_cast<R>(a.x), static_cast<R>(i == j ? 0.0 : a.y)};
         V0[e] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
     }
-    if (gtid == 0)
+    for (int o = 16; o > 0; o >>= 1)
+        fro += __shfl_down_sync(0xffffffffu, fro, o);
+    if ((tid & 31) == 0)
+        s_fro[tid >> 5] = fro;
+    __syncthreads();
+    if (tid == 0)
     {
-        flags[0] = 0;
-        flags[1] = 0;
-        flags[2] = 0;
-    }
-    // rotations below the FP32 round-off level of the matrix are not applied: 3e-7 of its trace
-    // (>= the largest eigenvalue of a covariance). The FP32 block updates of a large matrix leave
-    // off-diagonal entries near that size, which would keep the sweeps going; at this floor the
-    // eigenvectors of separated eigenvalues keep FP32 accuracy (residual ~3e-6 of the largest
-    // eigenvalue at T = 512, the level of the sweeps' own round-off)
-    if (tid < 32)
-    {
-        double tr = 0;
-        for (int i = tid; i < T; i += 32)
-            tr += fabs(Ain[static_cast<size_t>(i) * T + i].x);
-        for (int o = 16; o > 0; o >>= 1)
-            tr += __shfl_down_sync(0xffffffffu, tr, o);
-        if (tid == 0)
-            s_floor = static_cast<R>(tr * 3e-7);
+        double t = 0.0;
+        for (int w = 0; w < BJ_THREADS / 32; ++w)
+            t += s_fro[w];
+        atomicAdd(fro2, t);
     }
     grid_barrier(bar);
+    // rotations below the FP32 round-off level of the matrix are not applied: 5e-7 of its Frobenius
+    // norm. The FP32 block updates leave off-diagonal entries near that size, which would keep the
+    // sweeps going; at this floor the eigenvectors of separated eigenvalues keep FP32 accuracy
+    // (residual ~3e-6 of the largest eigenvalue at T = 512, the level of the sweeps' own round-off)
+    if (tid == 0)
+        s_floor = static_cast<R>(sqrt(*reinterpret_cast<volatile double*>(fro2)) * 5e-7);
+    __syncthreads();
     Cx<R>*A = A0, *An = A1, *V = V0, *Vn = V1;
     const int na = npb * (npb + 1) / 2, nrow = Tp / BJ_S;
     for (int sweep = 0; sweep < BJ_MAX_SWEEPS; ++sweep)
@@ -1057,7 +1091,7 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
                     sm1[i * BJ_LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
                 }
                 __syncthreads();
-                const bool rot = smem_sweeps<R, BJ_THREADS>(sm0, sm1, BJ_S, BJ_S, BJ_LD, sc, s_floor, 1);
+                const bool rot = smem_sweeps<R, BJ_THREADS, BJ_S>(sm0, sm1, BJ_S, BJ_S, BJ_LD, sc, s_floor, 1, true);
                 for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
                 {
                     const int i = e / BJ_S, j = e % BJ_S;
@@ -1315,7 +1349,8 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         off2 += 4 * tb2;
         Cx<float>* U = reinterpret_cast<Cx<float>*>(base + off2);
         off2 += static_cast<size_t>(Tb / BJ_S) * BJ_S * BJ_S * sizeof(float2);
-        int* flags = reinterpret_cast<int*>(base + off2);
+        int* flags = reinterpret_cast<int*>(base + off2);  // three sweep flags (zeroed by the kernel)
+        double* fro2 = reinterpret_cast<double*>(base + off2 + 32);
         GridBarrier* bar = reinterpret_cast<GridBarrier*>(base + off2 + 64);
         HV_CUDA_TRY(cudaMemsetAsync(base + off2, 0, 128, st));
         static int max_per_sm = -1;
@@ -1333,7 +1368,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         nb = nb > cap ? cap : nb;
         int Ti = T, Tbi = Tb;
         const double2* cin = cov;
-        void* args[] = {&cin, &Ti, &Tbi, &A0, &A1, &V0, &V1, &U, &flags, &bar, &V, &ev_unsorted};
+        void* args[] = {&cin, &Ti, &Tbi, &A0, &A1, &V0, &V1, &U, &flags, &fro2, &bar, &V, &ev_unsorted};
         HV_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_jacobi_block), nb, BJ_THREADS, args, BJ_SMEM,
                                                 st));
         count_launch();
