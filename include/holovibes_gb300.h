@@ -357,8 +357,9 @@ hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* st
  * `work` must hold hv_pca_cov_workspace(T, W*H) bytes. */
 hv_status hv_pca_covariance(const void* ring_c64, int T, size_t npix, void* cov_c128, void* work, void* stream);
 size_t hv_pca_cov_workspace(int T, size_t npix);
-/* Covariance engine: 0 = automatic (tcgen05 split-BF16 tensor cores for T <= 64 and frames of a
- * multiple of 8 pixels, else FP32 SIMT), 1 = FP32 SIMT, 2 = tensor cores only. Process-wide. */
+/* Covariance engine: 0 = automatic (tcgen05 split-BF16 tensor cores for T <= 1024 and frames of a
+ * multiple of 8 pixels: one tile for T <= 64, 128 x 128 tiles of the Gram matrix above; else FP32
+ * SIMT), 1 = FP32 SIMT, 2 = tensor cores only. Process-wide. */
 void hv_pca_covariance_mode(int mode);
 /* After the covariance's stream work finished: HV_ERR_TIMEOUT when a bounded device wait in the
  * tensor-core kernel gave up (results invalid), HV_OK otherwise. Synchronous read of `work`. */
@@ -370,11 +371,11 @@ hv_status hv_pca_covariance_status(const void* work);
 hv_status hv_pca_eigh(void* cov_c128, int T, double* eigenvalues, void* eigenvectors_c128, int pmin, int pmax,
                       void* weights_c64, void* work, void* stream);
 size_t hv_pca_eigh_workspace(int T);
-/* Jacobi sweep precision for T <= 64 (process-wide). HV_EIG_FP32 (default): sweeps in FP32 in
- * shared memory, then each eigenvector is normalised and its eigenvalue taken as the Rayleigh
- * quotient against the FP64 covariance (GB300 runs FP64 at 1/64 of the FP32 rate, so FP64 sweeps
- * cost milliseconds per window). HV_EIG_FP64: the sweeps themselves in FP64. T > 64 always sweeps
- * in FP64 (global-memory kernel). */
+/* Jacobi sweep precision (process-wide). HV_EIG_FP32 (default): FP32 sweeps (T <= 64: one CTA,
+ * shared memory; 64 < T <= 512: block-cyclic Jacobi over a cooperative grid), then each eigenvector
+ * is normalised and its eigenvalue taken as the Rayleigh quotient against the FP64 covariance
+ * (GB300 runs FP64 at 1/64 of the FP32 rate, so FP64 sweeps cost milliseconds per window).
+ * HV_EIG_FP64, and any T above 512: the sweeps themselves in FP64. */
 enum { HV_EIG_FP32 = 0, HV_EIG_FP64 = 1 };
 void hv_pca_eig_precision(int precision);
 
