@@ -432,8 +432,9 @@ SERVE_WORKLOADS = {
 }
 
 
-def serve_streams(name: str):
-    """(fd, settings, batches[nb][B*frame_bytes] uint8) per stream, seeded."""
+def serve_streams(name: str, only: int | None = None):
+    """(fd, settings, batches[nb][B*frame_bytes] uint8) per stream, seeded; `only` keeps one stream
+    (the same one as in the full list)."""
     import holovibes_gb300 as hv
     from holovibes_gb300.synthetic import Interferogram
 
@@ -457,11 +458,82 @@ def serve_streams(name: str):
         if tt == 2:
             over.update(p_start=T - 4, p_width=3, image_type=1)
         s = hv.Settings.defaults().update(**over).validate(fd)
+        if only is not None and i != only:
+            continue
         g = Interferogram(width=W, height=H, seed=100 + i, dtype=np.uint8 if depth == 1 else np.uint16,
                           max_value=255 if depth == 1 else 4095, z=z, lam=lam, modes=6 if tt == 2 else 0)
         frames = g.frames(0, 2 * B)
         out.append((fd, s, frames.reshape(2, -1).view(np.uint8)))
     return out
+
+
+def _plain_process(idx: int, workload: str, steps: int, warmup: int, barrier, queue) -> None:
+    """One stream on one hv_pipe in its own process (one CUDA context), as the reference is run:
+    one Holovibes instance, one compute pipeline, per stream. Same client loop as the in-process
+    arms: push one batch from pinned memory, read back the holograms."""
+    import torch
+
+    import holovibes_gb300 as hv
+
+    try:
+        torch.cuda.set_device(0)
+        (fd, s, b), = serve_streams(workload, only=idx)
+        pinned = torch.from_numpy(b.copy()).pin_memory()
+        out = torch.empty(fd.width * fd.height * 2, dtype=torch.uint8).pin_memory()
+        pipe = hv.Pipe(fd, s)
+        B = s.batch_size
+        for k in range(s.time_transformation_size // B + warmup):
+            pipe.enqueue_ptr(pinned[k % 2].data_ptr(), B, hv.MEM_HOST)
+            while pipe.output_count():
+                pipe.pull_into(out.data_ptr(), hv.MEM_HOST)
+        pipe.sync()
+        while pipe.output_count():
+            pipe.pull_into(out.data_ptr(), hv.MEM_HOST)
+        barrier.wait(timeout=600)
+        lat, pushed = [], []
+        t0 = time.perf_counter()
+        for k in range(steps):
+            pushed.append(time.perf_counter())
+            pipe.enqueue_ptr(pinned[k % 2].data_ptr(), B, hv.MEM_HOST)
+            while pipe.output_count():
+                pipe.pull_into(out.data_ptr(), hv.MEM_HOST)
+                if pushed:
+                    lat.append(time.perf_counter() - pushed.pop(0))
+        pipe.sync()
+        while pipe.output_count():
+            pipe.pull_into(out.data_ptr(), hv.MEM_HOST)
+            if pushed:
+                lat.append(time.perf_counter() - pushed.pop(0))
+        t1 = time.perf_counter()
+        pipe.close()
+        queue.put((idx, steps * B, t0, t1, lat))
+    except Exception as e:  # reported to the parent, which fails the arm
+        queue.put((idx, -1, 0.0, 0.0, repr(e)))
+
+
+def run_plain_processes(args, nstreams: int, steps: int) -> dict:
+    """Aggregate input frames/s of one plain pipe per process over all streams (wall clock from
+    the first timed push to the last hologram of any process)."""
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(nstreams)
+    queue = ctx.Queue()
+    procs = [ctx.Process(target=_plain_process, args=(i, args.workload, steps, args.warmup, barrier, queue))
+             for i in range(nstreams)]
+    for p in procs:
+        p.start()
+    res = [queue.get(timeout=900) for _ in procs]
+    for p in procs:
+        p.join(60)
+    bad = [r for r in res if r[1] < 0]
+    if bad:
+        raise RuntimeError(f"plain process failed: {bad[0][4]}")
+    t0 = min(r[2] for r in res)
+    t1 = max(r[3] for r in res)
+    lat = np.array([x for r in res for x in r[4]]) * 1e3
+    return {"frames_per_s": sum(r[1] for r in res) / (t1 - t0), "processes": nstreams,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}}
 
 
 def run_serving(args):
@@ -549,6 +621,9 @@ def run_serving(args):
                              "graph_kernels": g1["graph_kernels"] - g0["graph_kernels"],
                              "eager_cycles": g1["eager_cycles"] - g0["eager_cycles"],
                              "buckets": g1["buckets"]}
+    # one plain pipe per process (the reference's deployment: one instance per stream); outside
+    # the clock sampler's window so the processes' start-up is not sampled
+    results["plain_per_process"] = run_plain_processes(args, len(streams), steps)
     window_ms = min(1e3 * s.time_transformation_size / (results["served"]["frames_per_s"] / len(streams))
                     for (_, s, _) in streams)
     v = results["served"]["frames_per_s"]
@@ -565,6 +640,8 @@ def run_serving(args):
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "serving": {"served": results["served"], "plain": results["plain"],
                     "served_over_plain": v / results["plain"]["frames_per_s"],
+                    "plain_per_process": results["plain_per_process"],
+                    "served_over_plain_per_process": v / results["plain_per_process"]["frames_per_s"],
                     "shortest_window_ms_at_served_rate": window_ms},
         "gpu_launches": int(results["served"]["graph_kernels"]),
         "roofline": None, "cpu_baseline": None, "clocks": clk.summary(),
