@@ -877,7 +877,6 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
 // Grid-wide kernels (64 < T <= JC_MAX_T) synchronise through a bounded sense-reversal barrier: a
 // wait that exceeds about 2 s sets the error flag and every later barrier returns at once, so the
 // kernel ends.
-constexpr int JC_THREADS = 512;
 constexpr int JC_MAX_T = 512;
 
 // Loads of A and V in the grid kernel bypass L1 (other SMs wrote them before the last barrier).
