@@ -332,12 +332,16 @@ int sm_count();
 // G (2T x 2T) in 128 x 128 tiles (bm, bn), bm <= bn: operand A = Y rows of frames 64 bm .. 64 bm + 63,
 // B = frames 64 bn .. (the same as A on diagonal tiles; frames >= T are zero-filled by the tensor
 // copy). CTA (split ks, tile tp) walks the 64-pixel chunks of split ks: the loader brings the A
-// and B chunks ([64 frames][64 px] complex, 32 KB each) into a ring of R raw stages, the eight
+// and B chunks ([64 frames][64 px] complex, 32 KB each) into a ring of R raw stages, the sixteen
 // converter warps split them into Ah / Al / Bh / Bl (one converted stage), the MMA warp issues
 // Ah Bh^T, Ah Bl^T, Al Bh^T (M = N = 128, K = 16) into three TMEM accumulators. The CTAs of one
 // split stream the same chunks at the same time, so each chunk comes from HBM about once and the
 // other tiles read it from L2.
 constexpr int TT_FRAMES = 64;                          // frames per operand tile (128 rows of Y)
+constexpr int TT_CONVERTERS = 512;                     // warps 0-15 convert
+constexpr int TT_MMA_WARP = TT_CONVERTERS / 32;        // warp 16 issues the MMAs
+constexpr int TT_LOAD_WARP = TT_MMA_WARP + 1;          // warp 17 issues the tensor copies
+constexpr int TT_THREADS = TT_CONVERTERS + 64;
 constexpr uint32_t TT_RAW_HALF = TT_FRAMES * TC_KC * 8;  // one [64 frames][64 px] complex chunk: 32 KB
 constexpr int TT_MAX_RAW = 3;
 
@@ -354,7 +358,7 @@ __device__ __forceinline__ void tile_pair(int tp, int nb, int& bm, int& bn)
 }
 
 // part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * npairs + tp)
-__global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc_tiled(const __grid_constant__ CUtensorMap ring_map,
+__global__ void __launch_bounds__(TT_THREADS, 1) k_cov_tc_tiled(const __grid_constant__ CUtensorMap ring_map,
                                                                 size_t npix, int nb, int npairs,
                                                                 size_t chunks_per_split, int raw_stages,
                                                                 float* __restrict__ part, int* __restrict__ err)
@@ -389,16 +393,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc_tiled(const __grid_con
         for (int i = 0; i < R; ++i)
         {
             mbar_init(&raw_full[i], 1);
-            mbar_init(&raw_empty[i], TC_CONVERTERS / 32);
+            mbar_init(&raw_empty[i], TT_CONVERTERS / 32);
         }
-        mbar_init(&a_full, TC_CONVERTERS / 32);
+        mbar_init(&a_full, TT_CONVERTERS / 32);
         mbar_init(&a_empty, 1);
         mbar_init(&done, 1);
         mbar_init(&drain, 1);
         s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == TC_MMA_WARP)
+    if (warp == TT_MMA_WARP)
     {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(512u)
@@ -411,7 +415,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc_tiled(const __grid_con
     tc_fence_after();
     const uint32_t tmem = tmem_base;
 
-    if (warp == TC_LOAD_WARP)
+    if (warp == TT_LOAD_WARP)
     {
         // ------------------------------------------------------------------ loader (TMA)
         if (lane == 0)
@@ -434,7 +438,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc_tiled(const __grid_con
         }
         __syncwarp();
     }
-    else if (warp < TC_MMA_WARP)
+    else if (warp < TT_MMA_WARP)
     {
         // ------------------------------------------------------------------ converters
         // row t of a raw chunk (frame t: 64 complex samples, 512 B): lane l reads pixels 2l, 2l+1
@@ -455,7 +459,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc_tiled(const __grid_con
                 const uint8_t* src = raw + op * TT_RAW_HALF;
                 uint8_t* th = tiles + (2 * op) * TILE_BYTES;
                 uint8_t* tl = th + TILE_BYTES;
-                for (int t = warp; t < TT_FRAMES; t += TC_CONVERTERS / 32)
+                for (int t = warp; t < TT_FRAMES; t += TT_CONVERTERS / 32)
                 {
                     const float4 f = reinterpret_cast<const float4*>(src + t * (TC_KC * 8))[lane];
                     uint32_t reh, rel, imh, iml;
@@ -528,20 +532,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc_tiled(const __grid_con
     {
         // a wait gave up: the copies and MMAs already issued finish before shared and tensor memory
         // are released (bounded waits)
-        if (warp == TC_LOAD_WARP && lane == 0)
+        if (warp == TT_LOAD_WARP && lane == 0)
         {
             for (int m = nmine - R > 0 ? nmine - R : 0; m < nmine; ++m)
                 mbar_wait(&raw_full[m % R], static_cast<uint32_t>((m / R) & 1));
             atomicExch(err, 1);
         }
-        if (warp == TC_MMA_WARP && lane == 0)
+        if (warp == TT_MMA_WARP && lane == 0)
         {
             mma_commit(&drain);
             mbar_wait(&drain, 0);
         }
         __syncthreads();
     }
-    if (warp == TC_MMA_WARP)
+    if (warp == TT_MMA_WARP)
     {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
@@ -685,7 +689,7 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
         HV_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
         float* tpart = static_cast<float*>(work);
-        k_cov_tc_tiled<<<q.nsplit * q.npairs, TC_THREADS, smem, st>>>(tmap, npix, q.nb, q.npairs, q.chunks_per_split,
+        k_cov_tc_tiled<<<q.nsplit * q.npairs, TT_THREADS, smem, st>>>(tmap, npix, q.nb, q.npairs, q.chunks_per_split,
                                                                       raw, tpart, err);
         HV_LAUNCH_CHECK();
         k_cov_tc_tiled_reduce<<<(T * T + 255) / 256, 256, 0, st>>>(tpart, T, q.nb, q.npairs, q.nsplit, cov);
