@@ -650,24 +650,59 @@ template <>
 __device__ __forceinline__ float jac_threshold<float>() { return 2.5e-7f; }
 
 template <class R>
+struct JacRot
+{
+    R c, s, cph, sph;  // J = [[c, s], [-s e^{-i phi}, c e^{-i phi}]], e^{i phi} = cph + i sph
+};
+
+template <class R>
 struct JacScratch
 {
-    int pp[JS_MAX_T / 2], pq[JS_MAX_T / 2], act[JS_MAX_T / 2];
-    R rc[JS_MAX_T / 2], rs[JS_MAX_T / 2], rcp[JS_MAX_T / 2], rsp[JS_MAX_T / 2];
+    int2 pq[JS_MAX_T / 2];  // the step's pairs (p < q)
+    int act[JS_MAX_T / 2];
+    JacRot<R> rot[JS_MAX_T / 2];
     short2 blk[(JS_MAX_T / 2) * (JS_MAX_T / 2 + 1) / 2];
 };
+
+// Rotation annihilating a_pq of the 2 x 2 Hermitian block [[app, apq], [conj(apq), aqq]] when |apq|
+// exceeds the relative threshold thr * sqrt(|app aqq|) and `floor` (and is not 0); returns false (identity)
+// otherwise. The FP32 form uses reciprocal square roots and one division (the sweeps only need an
+// orthogonal rotation to FP32 accuracy; the eigenpairs are finished in FP64).
+__device__ __forceinline__ bool jac_rotation(Cx<float> apq, float app, float aqq, float thr, float floor,
+                                             JacRot<float>& r)
+{
+    const float m2 = apq.x * apq.x + apq.y * apq.y;
+    if (!(m2 > 0.0f) || !(m2 > floor * floor) || !(m2 > thr * thr * fabsf(app * aqq)))
+        return false;
+    const float inv = rsqrtf(m2);
+    r.cph = apq.x * inv;
+    r.sph = apq.y * inv;
+    const float tau = 0.5f * (aqq - app) * inv;
+    const float t = copysignf(1.0f, tau) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.0f)));
+    r.c = rsqrtf(fmaf(t, t, 1.0f));
+    r.s = t * r.c;
+    return true;
+}
+
+__device__ __forceinline__ bool jac_rotation(Cx<double> apq, double app, double aqq, double thr, double floor,
+                                             JacRot<double>& r)
+{
+    const double mag = hypot(apq.x, apq.y);
+    if (!(mag > 1e-30) || !(mag > floor) || !(mag > thr * sqrt(fabs(app * aqq))))
+        return false;
+    r.cph = apq.x / mag;
+    r.sph = apq.y / mag;
+    const double tau = (aqq - app) / (2.0 * mag);
+    const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+    r.c = 1.0 / sqrt(1.0 + t * t);
+    r.s = t * r.c;
+    return true;
+}
 
 // Cyclic sweeps over the T x T Hermitian A (T <= 64, shared memory, leading dimension LD) with the
 // round-robin pairing, accumulating V <- V J; at most max_sweeps sweeps, ending after a sweep
 // without rotation. A rotation is applied when |a_pq| exceeds both the relative threshold and
 // `floor`. Every thread of the block (NT of them) calls it; returns whether any rotation was applied.
-__device__ __forceinline__ float jhypot(float a, float b) { return hypotf(a, b); }
-__device__ __forceinline__ double jhypot(double a, double b) { return hypot(a, b); }
-__device__ __forceinline__ float jsqrt(float a) { return sqrtf(a); }
-__device__ __forceinline__ double jsqrt(double a) { return sqrt(a); }
-__device__ __forceinline__ float jabs(float a) { return fabsf(a); }
-__device__ __forceinline__ double jabs(double a) { return fabs(a); }
-
 // Pair k of step `step` of a sweep over Tp indices. Round-robin order; with `split` (Tp = 2h, the
 // two halves already nearly diagonal) the h cross steps (i, h + (i + step) mod h) come first, then
 // the h - 1 round-robin steps inside both halves at once.
@@ -733,29 +768,11 @@ __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScr
                 const int k = tid;
                 int p, q;
                 sweep_pair(step, k, Tp, split, p, q);
-                sc.pp[k] = p;
-                sc.pq[k] = q;
-                R c = 1, s = 0, cph = 1, sph = 0;
-                if (q < T)
-                {
-                    const Cx<R> apq = A[p * LD + q];
-                    const R mag = jhypot(apq.x, apq.y);
-                    const R app = A[p * LD + p].x, aqq = A[q * LD + q].x;
-                    if (mag > R(1e-30) && mag > floor && mag > thr * jsqrt(jabs(app * aqq)))
-                    {
-                        cph = apq.x / mag;
-                        sph = apq.y / mag;
-                        const R tau = (aqq - app) / (R(2) * mag);
-                        const R t = (tau >= 0 ? R(1) : R(-1)) / (jabs(tau) + jsqrt(R(1) + tau * tau));
-                        c = R(1) / jsqrt(R(1) + t * t);
-                        s = t * c;
-                        active = 1;
-                    }
-                }
-                sc.rc[k] = c;
-                sc.rs[k] = s;
-                sc.rcp[k] = cph;
-                sc.rsp[k] = sph;
+                sc.pq[k] = make_int2(p, q);
+                JacRot<R> r = {1, 0, 1, 0};
+                if (q < T && jac_rotation(A[p * LD + q], A[p * LD + p].x, A[q * LD + q].x, thr, floor, r))
+                    active = 1;
+                sc.rot[k] = r;
                 sc.act[k] = active;
             }
             if (!__syncthreads_or(active))
@@ -767,7 +784,8 @@ __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScr
                 const int k1 = sc.blk[e].x, k2 = sc.blk[e].y;
                 if (!sc.act[k1] && !sc.act[k2])
                     continue;
-                const int r0 = sc.pp[k1], r1 = sc.pq[k1], c0 = sc.pp[k2], c1 = sc.pq[k2];
+                const int2 P1 = sc.pq[k1], P2 = sc.pq[k2];
+                const int r0 = P1.x, r1 = P1.y, c0 = P2.x, c1 = P2.y;
                 const bool hr1 = r1 < T, hc1 = c1 < T;
                 const Cx<R> z = {0, 0};
                 Cx<R> B[2][2];
@@ -776,8 +794,9 @@ __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScr
                 B[1][0] = hr1 ? A[r1 * LD + c0] : z;
                 B[1][1] = (hr1 && hc1) ? A[r1 * LD + c1] : z;
                 // X = B J2, J2 = [[c, s], [-s e^{-i phi}, c e^{-i phi}]]
-                const R c2 = sc.rc[k2], s2 = sc.rs[k2];
-                const Cx<R> em2 = {sc.rcp[k2], -sc.rsp[k2]};
+                const JacRot<R> J1 = sc.rot[k1], J2 = sc.rot[k2];
+                const R c2 = J2.c, s2 = J2.s;
+                const Cx<R> em2 = {J2.cph, -J2.sph};
                 Cx<R> X[2][2];
 #pragma unroll
                 for (int r = 0; r < 2; ++r)
@@ -787,8 +806,8 @@ __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScr
                     X[r][1] = {s2 * B[r][0].x + c2 * b1.x, s2 * B[r][0].y + c2 * b1.y};
                 }
                 // Y = J1^H X: row0 = c X0 - s e^{i phi} X1, row1 = s X0 + c e^{i phi} X1
-                const R c1r = sc.rc[k1], s1r = sc.rs[k1];
-                const Cx<R> ep1 = {sc.rcp[k1], sc.rsp[k1]};
+                const R c1r = J1.c, s1r = J1.s;
+                const Cx<R> ep1 = {J1.cph, J1.sph};
                 Cx<R> Y[2][2];
 #pragma unroll
                 for (int cc = 0; cc < 2; ++cc)
@@ -828,9 +847,10 @@ __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScr
                 const int k = e / T, r = e % T;
                 if (!sc.act[k])
                     continue;
-                const int p = sc.pp[k], q = sc.pq[k];
-                const R c = sc.rc[k], s = sc.rs[k];
-                const Cx<R> em = {sc.rcp[k], -sc.rsp[k]};
+                const int p = sc.pq[k].x, q = sc.pq[k].y;
+                const JacRot<R> J = sc.rot[k];
+                const R c = J.c, s = J.s;
+                const Cx<R> em = {J.cph, -J.sph};
                 const Cx<R> vp = V[r * LD + p], vq = cxmul(V[r * LD + q], em);
                 V[r * LD + p] = {c * vp.x - s * vq.x, c * vp.y - s * vq.y};
                 V[r * LD + q] = {s * vp.x + c * vq.x, s * vp.y + c * vq.y};
