@@ -74,6 +74,9 @@ struct ViewTcArgs
     int stacked;          // 1: D1 = Ah [Bh; Bl] (2N cols) + D2 = Al Bh;  0: D1 = Ah Bh + Al Bh, D2 = Ah Bl
 };
 
+// MOM: moments epilogue (sum_k |X_k|^2 bin_w[k]); a compile-time instantiation, because the
+// epilogue is on the kernel's critical path and a runtime branch there cost about 20% in time.
+template <bool MOM>
 __global__ void __launch_bounds__(V_THREADS, 1) k_view_tc(const __grid_constant__ CUtensorMap ring_map, ViewTcArgs a)
 {
     if (!ctl_render(a.ctl))
@@ -283,8 +286,12 @@ __global__ void __launch_bounds__(V_THREADS, 1) k_view_tc(const __grid_constant_
                 {
                     const int k = c0 / 2 + i;
                     if (k < a.K)
-                        sum += a.bin_w ? (d[2 * i] * d[2 * i] + d[2 * i + 1] * d[2 * i + 1]) * __ldg(a.bin_w + k)
-                                       : view_value_tc(d[2 * i], d[2 * i + 1], a.img_type);
+                    {
+                        if constexpr (MOM)
+                            sum += (d[2 * i] * d[2 * i] + d[2 * i + 1] * d[2 * i + 1]) * __ldg(a.bin_w + k);
+                        else
+                            sum += view_value_tc(d[2 * i], d[2 * i + 1], a.img_type);
+                    }
                 }
             }
             tc::fence_before();
@@ -295,7 +302,7 @@ __global__ void __launch_bounds__(V_THREADS, 1) k_view_tc(const __grid_constant_
             float v = 0.f;
             if (P < a.HW)
             {
-                v = a.bin_w ? sum : sum / static_cast<float>(a.K);
+                v = MOM ? sum : sum / static_cast<float>(a.K);
                 if (a.scale != 1.0f)
                     v = v * a.scale;
                 size_t dst = P;
@@ -488,14 +495,15 @@ hv_status view_tc(const float2* ring, int T, int W, int H, int K, int img_type, 
         return HV_ERR_UNSUPPORTED;
     a.raw_stages = raw;
     const size_t smem = raw * static_cast<size_t>(V_RAW) + a_bytes + 1024;
-    HV_CUDA_TRY(cudaFuncSetAttribute(k_view_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    auto kern = bin_w ? k_view_tc<true> : k_view_tc<false>;
+    HV_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int sms = 0;
     HV_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
     int grid = a.ntiles < sms ? a.ntiles : sms;
     if (grid < 1)
         grid = 1;
     HV_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(int), st));
-    k_view_tc<<<grid, V_THREADS, smem, st>>>(map, a);
+    kern<<<grid, V_THREADS, smem, st>>>(map, a);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
