@@ -54,6 +54,19 @@ def dist_env():
     return world, rank, local
 
 
+def replica_throughput(ms_local: float, frames_per_rank: int, world: int, device: str = "cuda"):
+    """Replicas (one independent pipe per GPU, no collective on the data path): the slowest
+    rank's time (max over ranks) and the whole job's frames / that time. (ms, frames/s)."""
+    import torch
+
+    ms = ms_local
+    if world > 1:
+        t = torch.tensor([ms_local], device=device, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, frames_per_rank * world / (ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
 
@@ -345,14 +358,8 @@ def run_ours(args):
         pipe.join()  # the rendering stream joins the pipe stream before the closing event
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
     launches = pipe.kernel_launches() - launches0
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    frames_total = args.steps * B * world
-    value = frames_total / (ms * 1e-3)
+    ms, value = replica_throughput(e0.elapsed_time(e1), args.steps * B, world)
 
     # e2e through the public API from pinned host memory, with per-step latency
     host_in = torch.from_numpy(batches.reshape(nb_unique, -1).view(np.uint8)).pin_memory()
@@ -377,12 +384,7 @@ def run_ours(args):
         pipe.pull_into(host_out.data_ptr(), hv.MEM_HOST)
         lat.append(time.perf_counter() - pushed.pop(0))
     pipe.sync()
-    t_e2e = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([t_e2e], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e_value = e2e_steps * B * world / t_e2e
+    t_e2e_ms, e2e_value = replica_throughput((time.perf_counter() - t0) * 1e3, e2e_steps * B, world)
     lat_ms = np.array(lat) * 1e3 if lat else np.array([float("nan")])
 
     peak_gbs, _, peak_src = measured_peaks()
