@@ -12,9 +12,11 @@ function cites the reference file:line it follows (paths relative to the Holovib
 Parity status: UNPINNED by reference golden vectors. The reference's own test data are
 Git-LFS pointers with no committed ``R_ref.holo`` outputs, and its numeric kernels call
 cuFFT / cuBLAS / cuSOLVER / thrust, so no reference output exists to pin against. The
-oracle is anchored on the reference's call sites (cited below) and, on the GPU, the
-library-anchor tests run the same library calls (cuFFT, cuSOLVER via torch) in the
-reference's order and compare them with this module.
+oracle is anchored on the reference's call sites (cited below) and, on the GPU,
+``tests/test_library_anchor_gpu.py`` replays the reference's call sequences through those
+same libraries (cuFFT, cuBLAS, cuSOLVER and a device sort, reached through torch) and compares
+them with this module: Fresnel and angular-spectrum propagation, the STFT over the ring's
+storage order, the PCA covariance / eigensolve / projection and the percentile selection.
 
 Stages that the reference computes in float32 on the host/GPU with integer or float
 truncation (percentile index, contrast factor, float->ushort) are restated here in
