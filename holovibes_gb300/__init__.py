@@ -48,7 +48,7 @@ IMG_MOMENTS_0, IMG_MOMENTS_1, IMG_MOMENTS_2 = 5, 6, 7
 LENS_FP64, LENS_REF32 = 0, 1
 EIG_FP32, EIG_FP64 = 0, 1
 MEM_HOST, MEM_DEVICE = 0, 1
-CUT_XZ, CUT_YZ = 0, 1
+VIEW_XZ, VIEW_YZ, VIEW_FILTER2D = 0, 1, 2
 
 SPACE_NAMES = {"NONE": 0, "None": 0, "FRESNELTR": 1, "FFT1": 1, "1FFT": 1, "Fresnel Tr.": 1,
                "ANGULARSP": 2, "FFT2": 2, "2FFT": 2, "Angular SP.": 2}
@@ -125,6 +125,13 @@ class Settings(C.Structure):
         ("yz_contrast_max", C.c_float),
         ("cuts_contrast_offset", C.c_int32),
         ("cuts_buffer_size", C.c_int32),
+        ("filter2d_view_enabled", C.c_int32),
+        ("filter2d_log_enabled", C.c_int32),
+        ("filter2d_contrast_enabled", C.c_int32),
+        ("filter2d_contrast_auto_refresh", C.c_int32),
+        ("filter2d_contrast_invert", C.c_int32),
+        ("filter2d_contrast_min", C.c_float),
+        ("filter2d_contrast_max", C.c_float),
     ]
 
     @classmethod
@@ -211,9 +218,9 @@ def _declare(L: C.CDLL) -> None:
         "hv_pipe_join": (st, [vp]),
         "hv_pipe_get_contrast_range": (st, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "hv_pipe_get_float_frame": (st, [vp, vp]),
-        "hv_pipe_cut_output_count": (sz, [vp, i32]),
-        "hv_pipe_pull_cut": (st, [vp, i32, vp, i32, i64]),
-        "hv_pipe_get_cut_float_frame": (st, [vp, i32, vp, vp]),
+        "hv_pipe_view_output_count": (sz, [vp, i32]),
+        "hv_pipe_pull_view": (st, [vp, i32, vp, i32, i64]),
+        "hv_pipe_get_view_float_frame": (st, [vp, i32, vp, vp]),
         "hv_time_cuts": (st, [vp, i32, i32, i32, vp, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
         "hv_time_cuts_workspace": (sz, [i32, i32, i32, i32, i32, i32, i32]),
         "hv_pipe_get_ring": (st, [vp, vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
@@ -416,23 +423,28 @@ class Pipe:
         check(lib().hv_pipe_get_float_frame(self._p, out.ctypes.data), "hv_pipe_get_float_frame")
         return out
 
-    def _cut_shape(self, which: int) -> tuple[int, int]:
+    def _view_shape(self, which: int) -> tuple[int, int]:
         T = self.settings.time_transformation_size
-        return (T, self.fd.width) if which == CUT_XZ else (self.fd.height, T)
+        if which == VIEW_XZ:
+            return T, self.fd.width
+        if which == VIEW_YZ:
+            return self.fd.height, T
+        return self.fd.height, self.fd.width
 
-    def cut_output_count(self, which: int) -> int:
-        return int(lib().hv_pipe_cut_output_count(self._p, which))
+    def view_output_count(self, which: int) -> int:
+        return int(lib().hv_pipe_view_output_count(self._p, which))
 
-    def pull_cut(self, which: int, timeout_us: int = 10_000_000) -> np.ndarray:
-        """Oldest XZ (T x W) or YZ (H x T) uint16 cut output."""
-        out = np.empty(self._cut_shape(which), dtype=np.uint16)
-        check(lib().hv_pipe_pull_cut(self._p, which, out.ctypes.data, MEM_HOST, timeout_us), "hv_pipe_pull_cut")
+    def pull_view(self, which: int, timeout_us: int = 10_000_000) -> np.ndarray:
+        """Oldest uint16 output of a secondary view: XZ (T x W), YZ (H x T) or filter2D (H x W)."""
+        out = np.empty(self._view_shape(which), dtype=np.uint16)
+        check(lib().hv_pipe_pull_view(self._p, which, out.ctypes.data, MEM_HOST, timeout_us), "hv_pipe_pull_view")
         return out
 
-    def cut_float_frame(self, which: int) -> tuple[np.ndarray, tuple[float, float]]:
-        out = np.empty(self._cut_shape(which), dtype=np.float32)
+    def view_float_frame(self, which: int) -> tuple[np.ndarray, tuple[float, float]]:
+        out = np.empty(self._view_shape(which), dtype=np.float32)
         rng = (C.c_float * 2)()
-        check(lib().hv_pipe_get_cut_float_frame(self._p, which, out.ctypes.data, rng), "hv_pipe_get_cut_float_frame")
+        check(lib().hv_pipe_get_view_float_frame(self._p, which, out.ctypes.data, rng),
+              "hv_pipe_get_view_float_frame")
         return out, (rng[0], rng[1])
 
     def ring(self) -> tuple[np.ndarray, int, int]:

@@ -125,6 +125,10 @@ hv_status time_cuts(const float2* ring, int T, int W, int H, const float2* weigh
 hv_status evecs_to_weights(const double2* evecs, int T, float2* w, cudaStream_t st);
 hv_status contrast_to_ushort(const float* frame, const float* range, int invert, int apply, uint16_t* out, size_t n,
                              cudaStream_t st, const CycleCtl* ctl = nullptr);
+// filter2D view: |shift(spec x mult)| into out (W x H); contrast then trunc(x * 65535) saturated
+hv_status filter2d_view_frame(const float2* spec, const float2* mult, int W, int H, float* out, cudaStream_t st);
+hv_status contrast_to_ushort_normalized(const float* frame, const float* range, int invert, int apply, uint16_t* out,
+                                        size_t n, cudaStream_t st);
 
 }  // namespace hv
 

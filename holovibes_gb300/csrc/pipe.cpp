@@ -65,8 +65,9 @@ void free_buffers(hv_pipe* p)
             cudaEventDestroy(*e);
             *e = nullptr;
         }
-    for (auto* vec : {&p->in_filled, &p->in_consumed, &p->out_ready, &p->out_freed, &p->cut[0].out_ready,
-                      &p->cut[0].out_freed, &p->cut[1].out_ready, &p->cut[1].out_freed})
+    for (auto* vec : {&p->in_filled, &p->in_consumed, &p->out_ready, &p->out_freed, &p->views[0].out_ready,
+                      &p->views[0].out_freed, &p->views[1].out_ready, &p->views[1].out_freed, &p->views[2].out_ready,
+                      &p->views[2].out_freed})
     {
         for (cudaEvent_t e : *vec)
             cudaEventDestroy(e);
@@ -86,6 +87,8 @@ bool uses_unwrap(const hv_settings& s) { return s.image_type == HV_IMG_ARGUMENT 
 // filter2D outside the AS transfer function: its own mask and passes (fourier_transform.cc:55-58)
 bool uses_f2d_mask(const hv_settings& s) { return s.filter2d_enabled && s.space_transformation != HV_SPACE_ANGULARSP; }
 bool uses_spatial(const hv_settings& s) { return s.space_transformation != HV_SPACE_NONE || s.filter2d_enabled; }
+// the filter2D view exists only with the filter (Pipe::insert_filter2d_view, pipe.cc:526-529)
+bool uses_f2d_view(const hv_settings& s) { return s.filter2d_enabled && s.filter2d_view_enabled; }
 
 struct Sizes
 {
@@ -142,6 +145,13 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
         z.add(64);
         z.add(ct * 2 * static_cast<size_t>(std::max(1, s.cuts_buffer_size)));
         z.add(percentile_workspace(std::max(HW, static_cast<size_t>(T) * std::max(fd.width, fd.height))));
+    }
+    if (uses_f2d_view(s))
+    {
+        z.add(HW * 8 * 2);
+        z.add(HW * 4);
+        z.add(64);
+        z.add(HW * 2 * static_cast<size_t>(std::max(1, s.output_buffer_size)));
     }
     z.add(static_cast<size_t>(time_view_partials(fd.width, fd.height)) * 8);
     z.add(reduce_workspace(HW));
@@ -257,7 +267,7 @@ hv_status build(hv_pipe* p)
         const int accs[2] = {s.xz_accumulation, s.yz_accumulation};
         for (int v = 0; v < 2; ++v)
         {
-            hv_pipe::CutView& c = p->cut[v];
+            hv_pipe::SecondaryView& c = p->views[v];
             c.w = v == 0 ? p->W : p->T;
             c.h = v == 0 ? p->T : p->H;
             const size_t px = static_cast<size_t>(c.w) * c.h;
@@ -275,6 +285,22 @@ hv_status build(hv_pipe* p)
             HV_ALLOC(c.out_ring, px * sizeof(uint16_t) * c.out_cap);
         }
     }
+    p->f2d_view = uses_f2d_view(s);
+    if (p->f2d_view)
+    {
+        hv_pipe::SecondaryView& c = p->views[HV_VIEW_FILTER2D];
+        c.w = p->W;
+        c.h = p->H;
+        HV_ALLOC(p->f2d_spec[0], HW * sizeof(float2));
+        HV_ALLOC(p->f2d_spec[1], HW * sizeof(float2));
+        HV_ALLOC(c.post, HW * sizeof(float));
+        HV_CUDA_TRY(cudaMemsetAsync(c.post, 0, HW * sizeof(float), p->stream));
+        c.A = 0;
+        c.acc_ring = nullptr;
+        HV_ALLOC(c.range, 4 * sizeof(float));
+        c.out_cap = std::max(1, s.output_buffer_size);  // gpu_filter2d_view_queue (pipe.cc:222)
+        HV_ALLOC(c.out_ring, HW * sizeof(uint16_t) * c.out_cap);
+    }
     HV_ALLOC(p->pct_work, percentile_workspace(pct_n));
     p->in_slots = std::max(2, s.input_buffer_size / std::max(1, p->B));
     p->batch_bytes = HW * p->depth * p->B;
@@ -291,10 +317,14 @@ hv_status build(hv_pipe* p)
     if ((st = mk_events(p->in_filled, p->in_slots)) != HV_OK || (st = mk_events(p->in_consumed, p->in_slots)) != HV_OK ||
         (st = mk_events(p->out_ready, p->out_cap)) != HV_OK || (st = mk_events(p->out_freed, p->out_cap)) != HV_OK)
         return st;
-    for (int v = 0; p->cuts && v < 2; ++v)
-        if ((st = mk_events(p->cut[v].out_ready, p->cut[v].out_cap)) != HV_OK ||
-            (st = mk_events(p->cut[v].out_freed, p->cut[v].out_cap)) != HV_OK)
+    for (int v = 0; v < 3; ++v)
+    {
+        if ((v < 2 && !p->cuts) || (v == HV_VIEW_FILTER2D && !p->f2d_view))
+            continue;
+        if ((st = mk_events(p->views[v].out_ready, p->views[v].out_cap)) != HV_OK ||
+            (st = mk_events(p->views[v].out_freed, p->views[v].out_cap)) != HV_OK)
             return st;
+    }
 
     // ring starts zeroed like Queue::resize (queue.cc:131-134)
     HV_CUDA_TRY(cudaMemsetAsync(p->ring, 0, HW * p->T * sizeof(float2), p->stream));
@@ -354,17 +384,28 @@ hv_status build(hv_pipe* p)
             return st;
         const float rxz[4] = {s.xz_contrast_min, s.xz_contrast_max, 0.f, 0.f};
         const float ryz[4] = {s.yz_contrast_min, s.yz_contrast_max, 0.f, 0.f};
-        HV_CUDA_TRY(cudaMemcpyAsync(p->cut[0].range, rxz, sizeof(rxz), cudaMemcpyHostToDevice, p->stream));
-        HV_CUDA_TRY(cudaMemcpyAsync(p->cut[1].range, ryz, sizeof(ryz), cudaMemcpyHostToDevice, p->stream));
+        HV_CUDA_TRY(cudaMemcpyAsync(p->views[0].range, rxz, sizeof(rxz), cudaMemcpyHostToDevice, p->stream));
+        HV_CUDA_TRY(cudaMemcpyAsync(p->views[1].range, ryz, sizeof(ryz), cudaMemcpyHostToDevice, p->stream));
         // Rendering::request_autocontrast (rendering.cc:87-99)
-        p->cut[0].autocontrast_pending = s.xz_contrast_enabled && s.xz_contrast_auto_refresh;
-        p->cut[1].autocontrast_pending = s.yz_contrast_enabled && s.yz_contrast_auto_refresh;
+        p->views[0].autocontrast_pending = s.xz_contrast_enabled && s.xz_contrast_auto_refresh;
+        p->views[1].autocontrast_pending = s.yz_contrast_enabled && s.yz_contrast_auto_refresh;
         for (int v = 0; v < 2; ++v)
         {
-            p->cut[v].acc_start = p->cut[v].acc_size = 0;
-            p->cut[v].out_head = p->cut[v].out_count = 0;
-            p->cut[v].valid = false;
+            p->views[v].acc_start = p->views[v].acc_size = 0;
+            p->views[v].out_head = p->views[v].out_count = 0;
+            p->views[v].valid = false;
         }
+    }
+    if (p->f2d_view)
+    {
+        hv_pipe::SecondaryView& c = p->views[HV_VIEW_FILTER2D];
+        const float rf[4] = {s.filter2d_contrast_min, s.filter2d_contrast_max, 0.f, 0.f};
+        HV_CUDA_TRY(cudaMemcpyAsync(c.range, rf, sizeof(rf), cudaMemcpyHostToDevice, p->stream));
+        // Rendering::request_autocontrast (rendering.cc:87-99): once per refresh
+        c.autocontrast_pending = s.filter2d_contrast_enabled && s.filter2d_contrast_auto_refresh;
+        c.out_head = c.out_count = 0;
+        c.valid = false;
+        p->f2d_buf = 0;
     }
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
 
@@ -480,6 +521,36 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
     return HV_OK;
 }
 
+// Queues one output of a secondary view from its float image (the oldest output is overwritten
+// when the queue is full, like Queue::enqueue).
+template <class Convert>
+hv_status queue_view_output(hv_pipe* p, hv_pipe::SecondaryView& c, cudaStream_t st, Convert convert)
+{
+    const size_t px = static_cast<size_t>(c.w) * c.h;
+    int slot_out;
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        if (c.out_count == c.out_cap)
+        {
+            c.out_head = (c.out_head + 1) % c.out_cap;
+            --c.out_count;
+            ++c.out_overwritten;
+        }
+        slot_out = (c.out_head + c.out_count) % c.out_cap;
+    }
+    HV_CUDA_TRY(cudaStreamWaitEvent(st, c.out_freed[slot_out], 0));
+    hv_status r = convert(c.out_ring + slot_out * px, px);
+    if (r != HV_OK)
+        return r;
+    HV_CUDA_TRY(cudaEventRecord(c.out_ready[slot_out], st));
+    {
+        std::lock_guard<std::mutex> g(p->mu);
+        ++c.out_count;
+    }
+    c.valid = true;
+    return HV_OK;
+}
+
 // XZ / YZ cuts of the window just rendered (fourier_transform.cc:462-503, image_accumulation.cc:159-257,
 // rendering.cc:75-340, converts.cc:321-350, pipe.cc:504-514): slices at the cursor band, then per
 // view accumulation, log10, autocontrast (bins frame_index_offset .. T-1-offset, or the reticle
@@ -495,12 +566,11 @@ hv_status render_cuts(hv_pipe* p, cudaStream_t st)
         return r;
     if (s.x_start < p->W && s.y_start < p->H &&
         (r = time_cuts(p->ring, p->T, p->W, p->H, p->w_all, s.x_start, s.x_start + s.x_width, s.y_start,
-                       s.y_start + s.y_width, s.image_type, p->cut[0].post, p->cut[1].post, p->cut_work, st)) != HV_OK)
+                       s.y_start + s.y_width, s.image_type, p->views[0].post, p->views[1].post, p->cut_work, st)) != HV_OK)
         return r;
     for (int v = 0; v < 2; ++v)
     {
-        hv_pipe::CutView& c = p->cut[v];
-        const size_t px = static_cast<size_t>(c.w) * c.h;
+        hv_pipe::SecondaryView& c = p->views[v];
         const int log_on = v == 0 ? s.xz_log_enabled : s.yz_log_enabled;
         const int contrast_on = v == 0 ? s.xz_contrast_enabled : s.yz_contrast_enabled;
         const int invert = v == 0 ? s.xz_contrast_invert : s.yz_contrast_invert;
@@ -543,28 +613,39 @@ hv_status render_cuts(hv_pipe* p, cudaStream_t st)
                     c.autocontrast_pending = false;
             }
         }
-        int slot_out;
-        {
-            std::lock_guard<std::mutex> g(p->mu);
-            if (c.out_count == c.out_cap)
-            {
-                c.out_head = (c.out_head + 1) % c.out_cap;
-                --c.out_count;
-                ++c.out_overwritten;
-            }
-            slot_out = (c.out_head + c.out_count) % c.out_cap;
-        }
-        HV_CUDA_TRY(cudaStreamWaitEvent(st, c.out_freed[slot_out], 0));
-        if ((r = contrast_to_ushort(c.post, c.range, invert, contrast_on, c.out_ring + slot_out * px, px, st)) != HV_OK)
+        if ((r = queue_view_output(p, c, st, [&](uint16_t* dst, size_t n) {
+                 return contrast_to_ushort(c.post, c.range, invert, contrast_on, dst, n, st);
+             })) != HV_OK)
             return r;
-        HV_CUDA_TRY(cudaEventRecord(c.out_ready[slot_out], st));
-        {
-            std::lock_guard<std::mutex> g(p->mu);
-            ++c.out_count;
-        }
-        c.valid = true;
     }
     return HV_OK;
+}
+
+// The filter2D view of the window just rendered (pipe.cc:526-546, rendering.cc:75-340,
+// converts.cc:355-367): |shift(stored spectrum)|, log10, autocontrast once per refresh over the
+// whole frame, contrast, then float_to_ushort_normalized.
+hv_status render_f2d_view(hv_pipe* p, cudaStream_t st)
+{
+    const hv_settings& s = p->s;
+    hv_pipe::SecondaryView& c = p->views[HV_VIEW_FILTER2D];
+    hv_status r;
+    const float2* mult = s.space_transformation == HV_SPACE_ANGULARSP ? p->lens : p->f2d_mask;
+    if ((r = filter2d_view_frame(p->f2d_spec[p->f2d_buf], mult, p->W, p->H, c.post, st)) != HV_OK)
+        return r;
+    if (s.filter2d_log_enabled &&
+        (r = renorm_shift_accumulate(c.post, c.post, c.w, c.h, nullptr, 0, nullptr, 0, 0, 0, 0, 1, st, 1.0f)) != HV_OK)
+        return r;
+    if (s.filter2d_contrast_enabled && c.autocontrast_pending)
+    {
+        if ((r = percentile(c.post, c.w, c.h, s.contrast_lower, s.contrast_upper, 0.0f, c.range, p->pct_work, st)) !=
+            HV_OK)
+            return r;
+        c.autocontrast_pending = false;
+    }
+    return queue_view_output(p, c, st, [&](uint16_t* dst, size_t px) {
+        return contrast_to_ushort_normalized(c.post, c.range, s.filter2d_contrast_invert, s.filter2d_contrast_enabled,
+                                             dst, px, st);
+    });
 }
 
 // Rendering of one output from a full ring (pipe.cc:334-374).
@@ -630,7 +711,21 @@ hv_status render(hv_pipe* p)
         ++p->out_count;
     }
     p->last_frame_valid = true;
-    return p->cuts ? render_cuts(p, st) : HV_OK;
+    if (p->cuts && (r = render_cuts(p, st)) != HV_OK)
+        return r;
+    return p->f2d_view ? render_f2d_view(p, st) : HV_OK;
+}
+
+// Masked spectrum of the batch's first frame (filter2D's store_frame: FFT2(x0) then the mask, or
+// the masked transfer function for AS; filter2D.cu:36-44, angular_spectrum.cu:50-55): the forward
+// FFT of frame 0 into f2d_spec[buf] (the mask is applied by the view kernel). Runs on the pipe's
+// stream right after the batch's spatial passes, with the spatial buffer as scratch.
+hv_status capture_f2d_spectrum(hv_pipe* p, const uint8_t* raw0, int buf)
+{
+    hv_status r = fft_rows_pass(raw0, p->kind, p->spatial, p->W, p->H, 1, nullptr, 0, 1.0f, 0, 1, p->stream);
+    if (r != HV_OK)
+        return r;
+    return fft_cols_pass(p->spatial, p->f2d_spec[buf], p->W, p->H, 1, nullptr, 0, 1.0f, 0, 1, p->stream);
 }
 
 // One batch of B raw frames at device address `raw` (pipe.cc:295-334).
@@ -654,6 +749,9 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
                                          p->spatial, ring, 0, p->T, p->stream, nullptr, p->f2d_mask, p->work2);
         if (st != HV_OK)
             return st;
+        p->f2d_buf = r;  // one spectrum per ring: window k's render reads it while batch k+1 runs
+        if (p->f2d_view && (st = capture_f2d_spectrum(p, raw, r)) != HV_OK)
+            return st;
         HV_CUDA_TRY(cudaEventRecord(p->ring_ready[r], p->stream));
         HV_CUDA_TRY(cudaStreamWaitEvent(p->render_stream, p->ring_ready[r], 0));
         p->ring = ring;
@@ -670,6 +768,7 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
     int nb = p->B;
     const int T = p->T;
     const size_t frame_bytes = p->HW * p->depth;
+    const uint8_t* raw0 = raw;  // the batch's first frame (filter2D view)
     if (nb > T)
     {
         raw += static_cast<size_t>(nb - T) * frame_bytes;
@@ -690,6 +789,8 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
     // insert_wait_time_transformation_size (pipe.cc:418-427)
     if (p->ring_size < T)
         return HV_OK;
+    if (p->f2d_view && (r = capture_f2d_spectrum(p, raw0, 0)) != HV_OK)
+        return r;
     return render(p);
 }
 
@@ -797,9 +898,9 @@ hv_pipe* pipe_create_served(const hv_frame_desc* fd, const hv_settings* settings
         delete p;
         return nullptr;
     }
-    if (p->s.cuts_enabled)
+    if (p->s.cuts_enabled || (p->s.filter2d_enabled && p->s.filter2d_view_enabled))
     {
-        set_last_error_msg("served streams render the XY view only (time cuts: use a Pipe)");
+        set_last_error_msg("served streams render the XY view only (time cuts, filter2D view: use a Pipe)");
         out = HV_ERR_UNSUPPORTED;
         delete p;
         return nullptr;
@@ -1176,9 +1277,11 @@ hv_status hv_pipe_request_autocontrast(hv_pipe* p)
     p->autocontrast_pending = p->s.contrast_enabled != 0;
     if (p->cuts)
     {
-        p->cut[0].autocontrast_pending = p->s.xz_contrast_enabled != 0;
-        p->cut[1].autocontrast_pending = p->s.yz_contrast_enabled != 0;
+        p->views[0].autocontrast_pending = p->s.xz_contrast_enabled != 0;
+        p->views[1].autocontrast_pending = p->s.yz_contrast_enabled != 0;
     }
+    if (p->f2d_view)
+        p->views[HV_VIEW_FILTER2D].autocontrast_pending = p->s.filter2d_contrast_enabled != 0;
     return HV_OK;
 }
 
@@ -1231,21 +1334,27 @@ hv_status hv_pipe_get_float_frame(hv_pipe* p, float* dst)
     return HV_OK;
 }
 
-size_t hv_pipe_cut_output_count(hv_pipe* p, int which)
+// a secondary view exists: the cuts (0, 1) or the filter2D view (2)
+static bool has_view(const hv_pipe* p, int which)
 {
-    if (!p || !p->cuts || which < 0 || which > 1)
-        return 0;
-    std::lock_guard<std::mutex> g(p->mu);
-    return static_cast<size_t>(p->cut[which].out_count);
+    return (which == HV_VIEW_XZ || which == HV_VIEW_YZ) ? p->cuts : (which == HV_VIEW_FILTER2D && p->f2d_view);
 }
 
-hv_status hv_pipe_pull_cut(hv_pipe* p, int which, uint16_t* dst, int mem, int64_t timeout_us)
+size_t hv_pipe_view_output_count(hv_pipe* p, int which)
 {
-    if (!p || !dst || which < 0 || which > 1)
+    if (!p || which < 0 || which > 2 || !has_view(p, which))
+        return 0;
+    std::lock_guard<std::mutex> g(p->mu);
+    return static_cast<size_t>(p->views[which].out_count);
+}
+
+hv_status hv_pipe_pull_view(hv_pipe* p, int which, uint16_t* dst, int mem, int64_t timeout_us)
+{
+    if (!p || !dst || which < 0 || which > 2)
         return HV_INVALID_VALUE;
-    if (!p->cuts)
+    if (!has_view(p, which))
         return HV_NO_IN_DATA;
-    hv_pipe::CutView& c = p->cut[which];
+    hv_pipe::SecondaryView& c = p->views[which];
     int slot;
     {
         std::lock_guard<std::mutex> g(p->mu);
@@ -1287,13 +1396,13 @@ hv_status hv_pipe_pull_cut(hv_pipe* p, int which, uint16_t* dst, int mem, int64_
     return HV_OK;
 }
 
-hv_status hv_pipe_get_cut_float_frame(hv_pipe* p, int which, float* dst, float* range_out)
+hv_status hv_pipe_get_view_float_frame(hv_pipe* p, int which, float* dst, float* range_out)
 {
-    if (!p || which < 0 || which > 1)
+    if (!p || which < 0 || which > 2)
         return HV_INVALID_VALUE;
-    if (!p->cuts || !p->cut[which].valid)
+    if (!has_view(p, which) || !p->views[which].valid)
         return HV_NO_IN_DATA;
-    const hv_pipe::CutView& c = p->cut[which];
+    const hv_pipe::SecondaryView& c = p->views[which];
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
     HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
     if (dst)

@@ -65,9 +65,10 @@ struct hv_pipe
     float2* pi_minmax = nullptr;
     uint64_t pi_count = 0;
 
-    // time-transformation cuts (XZ: T x W, YZ: H x T): slices, accumulation rings, contrast
-    // ranges and output queues of their own (gpu_output_queue_xz / _yz, icompute.cc:195-213)
-    struct CutView
+    // secondary views, each with its float image, accumulation ring, contrast range and output
+    // queue: the time-transformation cuts (XZ: T x W, YZ: H x T; gpu_output_queue_xz / _yz,
+    // icompute.cc:195-213) and the filter2D view (W x H, gpu_filter2d_view_queue, pipe.cc:215-224)
+    struct SecondaryView
     {
         int w = 0, h = 0;  // image width and height (XZ: W x T, YZ: T x H)
         float* post = nullptr;
@@ -84,7 +85,10 @@ struct hv_pipe
     bool cuts = false;
     float2* w_all = nullptr;  // all T weight rows: bins (STFT / SSA_STFT), components (PCA), identity (NONE)
     void* cut_work = nullptr;
-    CutView cut[2];           // 0: XZ, 1: YZ
+    bool f2d_view = false;
+    float2* f2d_spec[2] = {nullptr, nullptr};  // masked spectrum of the batch's first frame (per fast-mode ring)
+    int f2d_buf = 0;
+    SecondaryView views[3];   // HV_VIEW_XZ, HV_VIEW_YZ, HV_VIEW_FILTER2D
 
     // input ring of batch slots
     uint8_t* in_ring = nullptr;

@@ -724,6 +724,73 @@ __global__ void k_contrast_ushort(const float* __restrict__ in, const float* __r
     }
 }
 
+// ====================================================================================== filter2D view
+
+// The filter2D view frame (Pipe::insert_filter2d_view, pipe.cc:526-546): the stored spectrum
+// (spectrum x multiplier, FFT layout: apply_mask by the mask or by the masked transfer function)
+// quadrant-swapped (shift_corners) and taken to its modulus (complex_to_modulus with one bin).
+__global__ void k_f2d_view(const float2* __restrict__ spec, const float2* __restrict__ mult, int W, int H,
+                           float* __restrict__ out)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= W)
+        return;
+    const size_t src = static_cast<size_t>((y + H / 2) % H) * W + (x + W / 2) % W;
+    const float2 a = spec[src], m = mult[src];
+    const float re = a.x * m.x - a.y * m.y, im = a.x * m.y + a.y * m.x;
+    out[static_cast<size_t>(y) * W + x] = hypotf(re, im);
+}
+
+hv_status filter2d_view_frame(const float2* spec, const float2* mult, int W, int H, float* out, cudaStream_t st)
+{
+    if ((W & 1) || (H & 1))
+        return HV_INVALID_VALUE;
+    dim3 block(128), grid((W + 127) / 128, H);
+    k_f2d_view<<<grid, block, 0, st>>>(spec, mult, W, H, out);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+// Contrast (apply_contrast_correction when `apply`) then float_to_ushort_normalized
+// (tools_conversion.cu:389-393): trunc(x * 65535) saturated to [0, 65535] (NaN -> 0), the
+// filter2D view's conversion.
+__global__ void k_contrast_ushort_normalized(const float* __restrict__ in, const float* __restrict__ range, int invert,
+                                             int apply, uint16_t* __restrict__ out, size_t n)
+{
+    float mn = 0.f, factor = 1.f;
+    if (apply)
+    {
+        float lo = range[0], hi = range[1];
+        if (invert)
+        {
+            const float t = lo;
+            lo = hi;
+            hi = t;
+        }
+        mn = lo;
+        factor = __fdiv_rn(65535.0f, __fadd_rn(__fsub_rn(hi, lo), FLT_EPSILON));
+    }
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n;
+         e += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        float v = in[e];
+        if (apply)
+            v = __fmul_rn(factor, __fsub_rn(v, mn));
+        const float w = __fmul_rn(v, 65535.0f);
+        out[e] = w >= 65535.0f ? static_cast<uint16_t>(65535) : (w > 0.0f ? static_cast<uint16_t>(w) : static_cast<uint16_t>(0));
+    }
+}
+
+hv_status contrast_to_ushort_normalized(const float* frame, const float* range, int invert, int apply, uint16_t* out,
+                                        size_t n, cudaStream_t st)
+{
+    k_contrast_ushort_normalized<<<ew_grid(n), EW_THREADS, 0, st>>>(frame, range, invert, apply, out, n);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
 hv_status contrast_to_ushort(const float* frame, const float* range, int invert, int apply, uint16_t* out, size_t n,
                              cudaStream_t st, const CycleCtl* ctl)
 {

@@ -240,6 +240,14 @@ void settings_default(hv_settings* s)
     s->xz_contrast_max = s->yz_contrast_max = 65535.0f;
     s->cuts_contrast_offset = 2;
     s->cuts_buffer_size = 512;
+    // filter2D view window: View_Window defaults (view_struct.hh)
+    s->filter2d_view_enabled = 0;
+    s->filter2d_log_enabled = 0;
+    s->filter2d_contrast_enabled = 0;
+    s->filter2d_contrast_auto_refresh = 1;
+    s->filter2d_contrast_invert = 0;
+    s->filter2d_contrast_min = 1.0f;
+    s->filter2d_contrast_max = 65535.0f;
 }
 
 hv_status settings_from_json(const char* text, hv_settings* s)
@@ -349,6 +357,12 @@ hv_status settings_from_value(const json::Value& doc, hv_settings* s, bool lenie
         {{"view", "window", "yz", "contrast", "max"}, 1, &out.yz_contrast_max},
         {{"advanced", "contrast", "frame_index_offset"}, 0, &out.cuts_contrast_offset},
         {{"advanced", "buffer_size", "time_transformation_cuts"}, 0, &out.cuts_buffer_size},
+        {{"view", "window", "filter2d", "log_enabled"}, 2, &out.filter2d_log_enabled},
+        {{"view", "window", "filter2d", "contrast", "enabled"}, 2, &out.filter2d_contrast_enabled},
+        {{"view", "window", "filter2d", "contrast", "auto_refresh"}, 2, &out.filter2d_contrast_auto_refresh},
+        {{"view", "window", "filter2d", "contrast", "invert"}, 2, &out.filter2d_contrast_invert},
+        {{"view", "window", "filter2d", "contrast", "min"}, 1, &out.filter2d_contrast_min},
+        {{"view", "window", "filter2d", "contrast", "max"}, 1, &out.filter2d_contrast_max},
         {{"view", "window", "xy", "output_image_accumulation"}, 0, &out.accumulation},
         {{"view", "window", "xy", "log_enabled"}, 2, &out.log_enabled},
         {{"view", "window", "xy", "contrast", "enabled"}, 2, &out.contrast_enabled},
@@ -493,6 +507,12 @@ void settings_to_value(const hv_settings* s, json::Value& doc)
     }
     set_num(doc, {"advanced", "contrast", "frame_index_offset"}, s->cuts_contrast_offset);
     set_num(doc, {"advanced", "buffer_size", "time_transformation_cuts"}, s->cuts_buffer_size);
+    set_bool(doc, {"view", "window", "filter2d", "log_enabled"}, s->filter2d_log_enabled != 0);
+    set_bool(doc, {"view", "window", "filter2d", "contrast", "enabled"}, s->filter2d_contrast_enabled != 0);
+    set_bool(doc, {"view", "window", "filter2d", "contrast", "auto_refresh"}, s->filter2d_contrast_auto_refresh != 0);
+    set_bool(doc, {"view", "window", "filter2d", "contrast", "invert"}, s->filter2d_contrast_invert != 0);
+    set_num(doc, {"view", "window", "filter2d", "contrast", "min"}, s->filter2d_contrast_min);
+    set_num(doc, {"view", "window", "filter2d", "contrast", "max"}, s->filter2d_contrast_max);
     set_num(doc, {"view", "window", "xy", "output_image_accumulation"}, s->accumulation);
     set_bool(doc, {"view", "window", "xy", "log_enabled"}, s->log_enabled != 0);
     set_bool(doc, {"view", "window", "xy", "contrast", "enabled"}, s->contrast_enabled != 0);

@@ -143,6 +143,13 @@ typedef struct hv_settings
     float yz_contrast_max;
     int32_t cuts_contrast_offset;    /* advanced.contrast.frame_index_offset: bins skipped at both ends */
     int32_t cuts_buffer_size;        /* advanced.buffer_size.time_transformation_cuts: cut outputs kept */
+    int32_t filter2d_view_enabled;   /* Filter2dViewEnabled: queue the filter2D view (needs filter2d_enabled) */
+    int32_t filter2d_log_enabled;    /* view.window.filter2d.log_enabled */
+    int32_t filter2d_contrast_enabled; /* view.window.filter2d.contrast.* */
+    int32_t filter2d_contrast_auto_refresh;
+    int32_t filter2d_contrast_invert;
+    float filter2d_contrast_min;
+    float filter2d_contrast_max;
 } hv_settings;
 
 /* ------------------------------------------------------------------------------------------
@@ -202,16 +209,17 @@ hv_status hv_pipe_join(hv_pipe* p);
 hv_status hv_pipe_get_contrast_range(hv_pipe* p, float* min_out, float* max_out);
 /* Copies the last float frame fed to the contrast stage (gpu_postprocess_frame) into dst (host). */
 hv_status hv_pipe_get_float_frame(hv_pipe* p, float* dst);
-/* Time-transformation cuts (CutsViewEnabled): each rendered window also produces an XZ image
- * (T rows x W, row t = bin / component t) and a YZ image (H rows x T) into their own output
- * queues (gpu_output_queue_xz / _yz, Backend/sources/core/pipe.cc:504-514). which: 0 = XZ, 1 = YZ. */
-enum { HV_CUT_XZ = 0, HV_CUT_YZ = 1 };
-size_t hv_pipe_cut_output_count(hv_pipe* p, int which);
-/* Copies the oldest cut output (W*T or H*T uint16) into dst; as hv_pipe_pull_output. */
-hv_status hv_pipe_pull_cut(hv_pipe* p, int which, uint16_t* dst, int mem, int64_t timeout_us);
-/* The last cut float image fed to its contrast stage (host dst, may be NULL) and the view's
- * contrast range (range_out[2], may be NULL). */
-hv_status hv_pipe_get_cut_float_frame(hv_pipe* p, int which, float* dst, float* range_out);
+/* Secondary views, each rendered window, each into its own output queue (pipe.cc:504-521):
+ * the time-transformation cuts (CutsViewEnabled) XZ (T rows x W, row t = bin / component t) and
+ * YZ (H rows x T), and the filter2D view (Filter2dViewEnabled: the modulus of the masked spectrum
+ * of the batch's first frame, quadrant-swapped, W x H). */
+enum { HV_VIEW_XZ = 0, HV_VIEW_YZ = 1, HV_VIEW_FILTER2D = 2 };
+size_t hv_pipe_view_output_count(hv_pipe* p, int which);
+/* Copies the oldest output of a secondary view (uint16) into dst; as hv_pipe_pull_output. */
+hv_status hv_pipe_pull_view(hv_pipe* p, int which, uint16_t* dst, int mem, int64_t timeout_us);
+/* The view's last float image fed to its contrast stage (host dst, may be NULL) and its contrast
+ * range (range_out[2], may be NULL). */
+hv_status hv_pipe_get_view_float_frame(hv_pipe* p, int which, float* dst, float* range_out);
 /* Copies the time ring storage (T frames of complex64, slot order) and its start/size. */
 hv_status hv_pipe_get_ring(hv_pipe* p, void* dst_host, int32_t* start, int32_t* size);
 /* Number of kernels this pipe launched since creation. */

@@ -744,6 +744,13 @@ class OracleSettings:
     yz_contrast_min: float = 1.0
     yz_contrast_max: float = 65535.0
     cuts_contrast_offset: int = 2
+    filter2d_view_enabled: bool = False
+    filter2d_log_enabled: bool = False
+    filter2d_contrast_enabled: bool = False
+    filter2d_contrast_auto_refresh: bool = True
+    filter2d_contrast_invert: bool = False
+    filter2d_contrast_min: float = 1.0
+    filter2d_contrast_max: float = 65535.0
 
 
 @dataclass
@@ -753,6 +760,7 @@ class OracleOutput:
     ushort: np.ndarray
     autocontrast_applied: bool = False
     cuts: list | None = None  # [XZ, YZ] CutOutput when the cuts are enabled
+    filter2d_view: "CutOutput | None" = None  # the filter2D view when enabled
 
 
 @dataclass
@@ -761,6 +769,24 @@ class CutOutput:
     contrast: tuple
     ushort: np.ndarray
     autocontrast_applied: bool = False
+
+
+def float_to_ushort_normalized(img32: np.ndarray) -> np.ndarray:
+    """float_to_ushort_normalized (tools_conversion.cu:389-393): x * 65535 in float32 converted to
+    ushort, i.e. truncated and saturated to [0, 65535] (NaN -> 0)."""
+    w = (np.asarray(img32, F32) * F32(65535.0)).astype(F32)
+    out = np.zeros(w.shape, np.uint16)
+    with np.errstate(invalid="ignore"):
+        pos = w > 0
+        out[pos] = np.minimum(np.trunc(w[pos]), 65535).astype(np.uint16)
+    return out
+
+
+def filter2d_view_frame(frame0: np.ndarray, mult: np.ndarray) -> np.ndarray:
+    """The filter2D view (pipe.cc:526-546): the stored spectrum of the batch's first frame
+    (FFT2(x0) times the mask, or the masked transfer function for AS: filter2D.cu:36-44,
+    angular_spectrum.cu:50-55), shift_corners, complex_to_modulus over one bin."""
+    return np.abs(shift_corners(fft2(frame0) * mult))
 
 
 def cut_autocontrast(img32: np.ndarray, which: int, s: "OracleSettings") -> tuple[float, float]:
@@ -846,6 +872,10 @@ class OraclePipe:
         self.last_V = None
         self.phase_increase = PhaseIncrease() if s.image_type == "PHASE_INCREASE" else None
         self.cut_models = [CutModel(s, 0), CutModel(s, 1)] if s.cuts_enabled else None
+        self.f2d_view = s.filter2d_enabled and s.filter2d_view_enabled
+        self.f2d_pending = s.filter2d_contrast_enabled and s.filter2d_contrast_auto_refresh
+        self.f2d_range = (s.filter2d_contrast_min, s.filter2d_contrast_max)
+        self.frame0 = None
 
     def process_batch(self, raw: np.ndarray, convert_f32=True) -> OracleOutput | None:
         s = self.s
@@ -855,6 +885,7 @@ class OraclePipe:
             return None
         self.batch_index = 0
         frames = convert_frames(raw)
+        self.frame0 = frames[0]
         frames = spatial_transform(frames, s.space_transformation, self.lens, self.f2d_mask)
         self.ring.enqueue_multiple(frames)
         if self.ring.size < s.time_transformation_size:
@@ -925,8 +956,24 @@ class OraclePipe:
                 slices = time_cuts(p_acc, s.x_start, s.x_start + s.x_width, s.y_start, s.y_start + s.y_width,
                                    s.image_type)
             cuts = [m.push(sl) for m, sl in zip(self.cut_models, slices)]
+        f2d = None
+        if self.f2d_view:
+            mult = self.lens if s.space_transformation == "ANGULARSP" else self.f2d_mask
+            fimg = filter2d_view_frame(self.frame0, mult)
+            if s.filter2d_log_enabled:
+                fimg = log10_view(fimg)
+            f32 = fimg.astype(F32)
+            f_applied = False
+            if s.filter2d_contrast_enabled and self.f2d_pending:
+                self.f2d_range = autocontrast(f32, s.contrast_lower, s.contrast_upper)
+                self.f2d_pending = False
+                f_applied = True
+            fc = (apply_contrast(f32, self.f2d_range[0], self.f2d_range[1], s.filter2d_contrast_invert)
+                  if s.filter2d_contrast_enabled else f32)
+            f2d = CutOutput(float_frame=fimg, contrast=self.f2d_range, ushort=float_to_ushort_normalized(fc),
+                            autocontrast_applied=f_applied)
         return OracleOutput(float_frame=img, contrast=self.crange, ushort=float_to_ushort(c),
-                            autocontrast_applied=applied, cuts=cuts)
+                            autocontrast_applied=applied, cuts=cuts, filter2d_view=f2d)
 
     def _should_autocontrast(self) -> bool:
         """should_apply_contrast (rendering.hh:168-181)."""

@@ -42,7 +42,12 @@ def _oracle_settings(fd, s):
         xz_contrast_min=s.xz_contrast_min, xz_contrast_max=s.xz_contrast_max,
         yz_contrast_enabled=bool(s.yz_contrast_enabled), yz_contrast_auto_refresh=bool(s.yz_contrast_auto_refresh),
         yz_contrast_invert=bool(s.yz_contrast_invert), yz_contrast_min=s.yz_contrast_min,
-        yz_contrast_max=s.yz_contrast_max, cuts_contrast_offset=s.cuts_contrast_offset)
+        yz_contrast_max=s.yz_contrast_max, cuts_contrast_offset=s.cuts_contrast_offset,
+        filter2d_view_enabled=bool(s.filter2d_view_enabled), filter2d_log_enabled=bool(s.filter2d_log_enabled),
+        filter2d_contrast_enabled=bool(s.filter2d_contrast_enabled),
+        filter2d_contrast_auto_refresh=bool(s.filter2d_contrast_auto_refresh),
+        filter2d_contrast_invert=bool(s.filter2d_contrast_invert), filter2d_contrast_min=s.filter2d_contrast_min,
+        filter2d_contrast_max=s.filter2d_contrast_max)
 
 
 CASES = {
@@ -148,16 +153,19 @@ CASES = {
                                               time_stride=8, batch_size=8, lambda_=785e-9, z_distance=0.45,
                                               pixel_size=12.0, p_start=1, p_width=1, filter2d_enabled=1,
                                               filter2d_n1=3, filter2d_n2=20, filter2d_smooth_low=2,
-                                              filter2d_smooth_high=4, renorm=1, contrast_enabled=1), 3),
+                                              filter2d_smooth_high=4, renorm=1, contrast_enabled=1,
+                                              filter2d_view_enabled=1, filter2d_log_enabled=1,
+                                              filter2d_contrast_enabled=1), 3),
     "none_f2d_stft_sqmod": (64, 64, 2, dict(space_transformation=0, time_transformation=1, time_transformation_size=8,
                                              time_stride=4, batch_size=4, image_type=1, p_start=2,
                                              filter2d_enabled=1, filter2d_n1=0, filter2d_n2=12, renorm=1,
-                                             fft_shift=1, contrast_enabled=1), 4),
+                                             fft_shift=1, contrast_enabled=1, filter2d_view_enabled=1), 4),
     "as_f2d_pca_mod": (64, 64, 2, dict(space_transformation=2, time_transformation=2, time_transformation_size=16,
                                         time_stride=16, batch_size=16, z_distance=0.3, pixel_size=20.0, image_type=0,
                                         p_start=15, p_width=0, filter2d_enabled=1, filter2d_n1=5, filter2d_n2=28,
                                         filter2d_smooth_low=0, filter2d_smooth_high=3, renorm=1,
-                                        contrast_enabled=1), 2),
+                                        contrast_enabled=1, filter2d_view_enabled=1, filter2d_log_enabled=1,
+                                        filter2d_contrast_enabled=1, filter2d_contrast_invert=1), 2),
     # XZ / YZ time cuts (stft.cu:17-115): bands of several rows / columns, per-view accumulation,
     # log, autocontrast over the offset bins or the reticle disc
     "as_stft_cuts_mod": (64, 48, 2, dict(space_transformation=2, time_transformation=1, time_transformation_size=16,
@@ -198,17 +206,17 @@ def _check_cuts(pipe, s, ref, case):
     """XZ / YZ: float images against the oracle (argument: atan(Im/Re) jumps by pi where Re
     changes sign, allowed on a few elements), contrast range and uint16 output bit-exact on the
     GPU's own float images."""
-    for which in (hv.CUT_XZ, hv.CUT_YZ):
+    for which in (hv.VIEW_XZ, hv.VIEW_YZ):
         cref = ref.cuts[which]
-        got_f, got_range = pipe.cut_float_frame(which)
+        got_f, got_range = pipe.view_float_frame(which)
         assert got_f.shape == cref.float_frame.shape, case
         if s.image_type == hv.IMG_ARGUMENT:
             d = np.abs(got_f - cref.float_frame)
             assert np.mean(d > 1e-3) < 1e-2, (case, which)
         else:
             assert rel_l2(got_f, cref.float_frame) <= 1e-4, (case, which)
-        enabled = s.xz_contrast_enabled if which == hv.CUT_XZ else s.yz_contrast_enabled
-        invert = s.xz_contrast_invert if which == hv.CUT_XZ else s.yz_contrast_invert
+        enabled = s.xz_contrast_enabled if which == hv.VIEW_XZ else s.yz_contrast_enabled
+        invert = s.xz_contrast_invert if which == hv.VIEW_XZ else s.yz_contrast_invert
         if enabled:
             if cref.autocontrast_applied:
                 expected = O.cut_autocontrast(got_f, which, _oracle_settings(pipe.fd, s))
@@ -217,8 +225,29 @@ def _check_cuts(pipe, s, ref, case):
             u16 = O.float_to_ushort(O.apply_contrast(got_f, got_range[0], got_range[1], bool(invert)))
         else:
             u16 = O.float_to_ushort(got_f)
-        assert pipe.cut_output_count(which) == 1, case
-        assert np.array_equal(pipe.pull_cut(which), u16), (case, which)
+        assert pipe.view_output_count(which) == 1, case
+        assert np.array_equal(pipe.pull_view(which), u16), (case, which)
+
+
+def _check_filter2d_view(pipe, s, ref, case):
+    """The filter2D view: float image against the oracle, range and normalised uint16 bit-exact on
+    the GPU's own float image."""
+    fref = ref.filter2d_view
+    got_f, got_range = pipe.view_float_frame(hv.VIEW_FILTER2D)
+    # the mask's zero band gives exact zeros, log10 of which is -inf on both sides
+    fin = np.isfinite(fref.float_frame)
+    assert np.array_equal(np.isfinite(got_f), fin), case
+    assert rel_l2(got_f[fin], fref.float_frame[fin]) <= 1e-4, case
+    if s.filter2d_contrast_enabled:
+        if fref.autocontrast_applied:
+            expected = O.autocontrast(got_f, s.contrast_lower, s.contrast_upper)
+            assert np.float32(got_range[0]) == np.float32(expected[0]), case
+            assert np.float32(got_range[1]) == np.float32(expected[1]), case
+        c = O.apply_contrast(got_f, got_range[0], got_range[1], bool(s.filter2d_contrast_invert))
+    else:
+        c = got_f
+    assert pipe.view_output_count(hv.VIEW_FILTER2D) == 1, case
+    assert np.array_equal(pipe.pull_view(hv.VIEW_FILTER2D), O.float_to_ushort_normalized(c)), case
 
 
 @pytest.mark.gpu
@@ -275,6 +304,8 @@ def test_pipe_matches_oracle(cuda, case):
         assert np.array_equal(got_u16, ref_u16), case
         if s.cuts_enabled:
             _check_cuts(pipe, s, ref, case)
+        if s.filter2d_enabled and s.filter2d_view_enabled:
+            _check_filter2d_view(pipe, s, ref, case)
     assert outputs > 0
     ring, start, size = pipe.ring()
     assert start == oracle.ring.start and size == oracle.ring.size
