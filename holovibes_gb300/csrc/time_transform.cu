@@ -1245,18 +1245,20 @@ __global__ void k_eig_refine(const double2* __restrict__ A, double2* __restrict_
     __syncthreads();
     const double inv = 1.0 / sqrt(red[0] + red[1] + red[2] + red[3]);
     __syncthreads();
+    // v^H A v of the Hermitian A: sum_t a_tt |v_t|^2 + 2 Re sum_{t<s} conj(v_t) a_ts v_s (upper
+    // triangle only: half the FP64 multiply-adds of the full product)
     double lam = 0.0;
     for (int t = tid; t < T; t += blockDim.x)
     {
         double2 av = make_double2(0.0, 0.0);
-        for (int s2 = 0; s2 < T; ++s2)
+        for (int s2 = t + 1; s2 < T; ++s2)
         {
             const double2 a = A[t * T + s2], x = v[s2];
             av.x += a.x * x.x - a.y * x.y;
             av.y += a.x * x.y + a.y * x.x;
         }
         const double2 x = v[t];
-        lam += (x.x * av.x + x.y * av.y) * inv * inv;
+        lam += (2.0 * (x.x * av.x + x.y * av.y) + A[t * T + t].x * (x.x * x.x + x.y * x.y)) * inv * inv;
         V[t * T + i] = make_double2(x.x * inv, x.y * inv);
     }
     for (int o = 16; o > 0; o >>= 1)
