@@ -738,10 +738,11 @@ __device__ __forceinline__ void sweep_pair(int step, int k, int Tp, bool split, 
     q = base + (a < b ? b : a);
 }
 
-// N > 0 fixes T = Tp = N and LD = N + 1 at compile time (index arithmetic by shifts).
+// N > 0 fixes T = Tp = N and LD = N + 1 at compile time (index arithmetic by shifts). A sweep runs
+// the steps [step_begin, step_end) of its ordering (step_end < 0: all Tp - 1 steps).
 template <class R, int NT, int N = 0>
 __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScratch<R>& sc, R floor, int max_sweeps,
-                            bool split = false)
+                            bool split = false, int step_begin = 0, int step_end = -1)
 {
     const int T = N > 0 ? N : T_, Tp = N > 0 ? N : Tp_, LD = N > 0 ? N + 1 : LD_;
     const int tid = threadIdx.x;
@@ -760,7 +761,8 @@ __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScr
     for (int sweep = 0; sweep < max_sweeps; ++sweep)
     {
         int sweep_active = 0;
-        for (int step = 0; step < Tp - 1; ++step)
+        const int s_end = step_end < 0 ? Tp - 1 : step_end;
+        for (int step = step_begin; step < s_end; ++step)
         {
             int active = 0;
             if (tid < npairs)
@@ -953,14 +955,14 @@ __device__ __forceinline__ void grid_barrier(GridBarrier* b)
 // with zero rows and columns, which no rotation ever touches), and a sweep pairs the blocks in the
 // round-robin order. A step (one of nblk - 1 per sweep) has two grid phases:
 //   1. each of the nblk / 2 block pairs (I, J) loads its 64 x 64 subproblem A[I u J][I u J] into
-//      shared memory and runs one cyclic sweep of 2 x 2 rotations on it (smem_sweeps; the I x J
-//      pairs first, then the pairs inside I and J, which earlier steps left nearly diagonal and
-//      whose steps are mostly skipped), giving the pair's unitary U (64 x 64);
+//      shared memory and applies one pass of 2 x 2 rotations to it (smem_sweeps over part of the
+//      split ordering, see below), giving the pair's unitary U (64 x 64);
 //   2. every CTA applies the step's unitaries to 64 x 64 blocks: A[P][Q] <- U_P^H A[P][Q] U_Q for
 //      pair groups P <= Q (and the mirror), V[rows][P] <- V[rows][P] U_P, from one copy of A and V
 //      into the other.
-// A sweep thus covers every index pair like a scalar sweep, with nblk - 1 grid steps instead of
-// T - 1. FP32, the same absolute floor as the scalar kernels; the sweeps end after one without a
+// The nblk - 1 round-robin steps rotate only the I x J pairs (32 inner steps each) and one more
+// step pairs blocks (2k, 2k + 1) to rotate the pairs inside every block (31 inner steps), so a
+// sweep visits every index pair once, like a scalar sweep, with nblk grid steps instead of T - 1. FP32, the same absolute floor as the scalar kernels; the sweeps end after one without a
 // rotation. Bounded grid barriers as above.
 constexpr int BJ_B = 32;                 // indices per block
 constexpr int BJ_S = 2 * BJ_B;           // subproblem size
@@ -984,6 +986,19 @@ __device__ __forceinline__ void bj_pair(int step, int k, int nblk, int& I, int& 
     }
     I = a < b ? a : b;
     J = a < b ? b : a;
+}
+
+// Blocks of pair k in step `step` of a sweep: the round-robin pairs for the nblk - 1 cross steps,
+// then one step pairing blocks (2k, 2k + 1) for the pairs inside each block.
+__device__ __forceinline__ void bj_step_pair(int step, int k, int nblk, int& I, int& J)
+{
+    if (step < nblk - 1)
+        bj_pair(step, k, nblk, I, J);
+    else
+    {
+        I = 2 * k;
+        J = 2 * k + 1;
+    }
 }
 
 // index i < 64 of pair group (I, J): block I then block J
@@ -1095,13 +1110,16 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
         // barrier; the one zeroed here was last read before the previous sweep's barriers
         if (gtid == 0)
             flags[(sweep + 1) % 3] = 0;
-        for (int step = 0; step < nblk - 1; ++step)
+        for (int step = 0; step < nblk; ++step)
         {
+            // cross steps rotate the I x J pairs (first half of the split ordering), the last step
+            // the pairs inside each block (second half): every pair once per sweep
+            const bool diag_step = step == nblk - 1;
             // phase 1: one sweep on each pair's subproblem
             for (int k = blockIdx.x; k < npb; k += gridDim.x)
             {
                 int I, J;
-                bj_pair(step, k, nblk, I, J);
+                bj_step_pair(step, k, nblk, I, J);
                 for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
                 {
                     const int i = e / BJ_S, j = e % BJ_S;
@@ -1110,7 +1128,8 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
                     sm1[i * BJ_LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
                 }
                 __syncthreads();
-                const bool rot = smem_sweeps<R, BJ_THREADS, BJ_S>(sm0, sm1, BJ_S, BJ_S, BJ_LD, sc, s_floor, 1, true);
+                const bool rot = smem_sweeps<R, BJ_THREADS, BJ_S>(sm0, sm1, BJ_S, BJ_S, BJ_LD, sc, s_floor, 1, true,
+                                                                  diag_step ? BJ_B : 0, diag_step ? -1 : BJ_B);
                 for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
                 {
                     const int i = e / BJ_S, j = e % BJ_S;
@@ -1136,8 +1155,8 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
                     }
                     const int Q = P + rem;
                     int IP, JP, IQ, JQ;
-                    bj_pair(step, P, nblk, IP, JP);
-                    bj_pair(step, Q, nblk, IQ, JQ);
+                    bj_step_pair(step, P, nblk, IP, JP);
+                    bj_step_pair(step, Q, nblk, IQ, JQ);
                     for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
                     {
                         const int i = e / BJ_S, j = e % BJ_S;
@@ -1176,7 +1195,7 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
                 {
                     const int v = it - na, rc = v / npb, P = v % npb;
                     int IP, JP;
-                    bj_pair(step, P, nblk, IP, JP);
+                    bj_step_pair(step, P, nblk, IP, JP);
                     for (int e = tid; e < BJ_S * BJ_S; e += BJ_THREADS)
                     {
                         const int i = e / BJ_S, j = e % BJ_S;
