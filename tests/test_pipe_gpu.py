@@ -390,3 +390,26 @@ def test_pipe_update_settings_and_errors(cuda):
         hv.Pipe(fd, bad)
     assert e.value.status == hv.HV_WRONG_IMG_TYPE
     p.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("W,H", [(4096, 4096), (1536, 2048)])
+def test_pipe_largest_frames(cuda, W, H):
+    """The largest frames of the shared-memory FFT (4096 points per axis) through the whole pipe
+    (AS + STFT, T = B = S = 4): float frame within rel-L2 1e-4 of the oracle, uint16 bit-exact on
+    the GPU's float frame. Uniform 12-bit noise frames (the generator is slow at this size)."""
+    fd = hv.FrameDescriptor(W, H, 2, 0)
+    s = hv.Settings.defaults().update(space_transformation=2, time_transformation=1, time_transformation_size=4,
+                                      time_stride=4, batch_size=4, z_distance=0.3, pixel_size=20.0, p_start=1,
+                                      renorm=1, fft_shift=1, contrast_enabled=1, contrast_lower=0.5,
+                                      contrast_upper=99.5).validate(fd)
+    raw = np.random.default_rng(W + H).integers(0, 4096, (4, H, W), dtype=np.uint16)
+    ref = O.OraclePipe(_oracle_settings(fd, s)).process_batch(raw)
+    pipe = hv.Pipe(fd, s)
+    pipe.enqueue(raw)
+    got_u16 = pipe.pull()
+    got_f = pipe.float_frame()
+    pipe.close()
+    assert rel_l2(got_f, ref.float_frame) <= 1e-4
+    expected = O.autocontrast(got_f, s.contrast_lower, s.contrast_upper)
+    assert np.array_equal(got_u16, O.float_to_ushort(O.apply_contrast(got_f, expected[0], expected[1])))
