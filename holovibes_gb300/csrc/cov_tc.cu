@@ -612,15 +612,13 @@ struct TcPlan
 
 int sm_count()
 {
-    static int sms = 0;
-    if (sms == 0)
-    {
+    static const int sms = [] {
         int dev = 0, v = 0;
         cudaGetDevice(&dev);
         if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
             v = 152;
-        sms = v;
-    }
+        return v;
+    }();
     return sms;
 }
 

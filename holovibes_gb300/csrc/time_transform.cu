@@ -21,6 +21,7 @@
 // buffer of the reference never exists.
 #include <math.h>
 
+#include <atomic>
 #include <vector>
 
 #include "hv_common.cuh"
@@ -398,7 +399,7 @@ __global__ void k_cov_reduce(const float2* __restrict__ part, int T, int tiles1d
         atomicAdd(&cov[e].y, mirror ? -im : im);
 }
 
-static int g_cov_mode = 0;  // 0 auto (tensor cores when supported), 1 SIMT, 2 tensor cores
+static std::atomic<int> g_cov_mode{0};  // 0 auto (tensor cores when supported), 1 SIMT, 2 tensor cores
 
 constexpr size_t COV_FLAGS = 256;
 
@@ -421,7 +422,8 @@ hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, v
     HV_CUDA_TRY(cudaMemsetAsync(cov, 0, static_cast<size_t>(T) * T * sizeof(double2), st));
     HV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
     const bool tc_ok = cov_tc_supported(T) && npix % 8 == 0 && (reinterpret_cast<uintptr_t>(ring) & 15) == 0;
-    if ((g_cov_mode == 0 && tc_ok) || g_cov_mode == 2)
+    const int mode = g_cov_mode.load();
+    if ((mode == 0 && tc_ok) || mode == 2)
     {
         if (!tc_ok)
         {
@@ -1326,7 +1328,7 @@ __global__ void k_eig_sort(const double* evals_in, const double2* V, int T, doub
     }
 }
 
-static int g_eig_precision = HV_EIG_FP32;
+static std::atomic<int> g_eig_precision{HV_EIG_FP32};
 
 void set_eig_precision(int p) { g_eig_precision = p; }
 
@@ -1350,6 +1352,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
 {
     if (T <= 0 || !work)
         return HV_INVALID_VALUE;
+    const int prec = g_eig_precision.load();  // one read: a concurrent switch cannot split the dispatch
     const int Tp = (T % 2) ? T + 1 : T;
     char* base = static_cast<char*>(work);
     double2* V = reinterpret_cast<double2*>(base);
@@ -1359,7 +1362,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     double* ev_unsorted = reinterpret_cast<double*>(base + off);
     off += static_cast<size_t>(T) * sizeof(double);
     int* pairs = reinterpret_cast<int*>(base + off);
-    if (T <= JS_MAX_T && g_eig_precision == HV_EIG_FP32)
+    if (T <= JS_MAX_T && prec == HV_EIG_FP32)
     {
         const size_t smem = 2 * static_cast<size_t>(T) * (T + 1) * sizeof(float2);
         if (smem > 48 * 1024)
@@ -1375,7 +1378,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
                                              static_cast<int>(smem)));
         k_jacobi_smem<double><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted);
     }
-    else if (T <= JC_MAX_T && g_eig_precision == HV_EIG_FP32)
+    else if (T <= JC_MAX_T && prec == HV_EIG_FP32)
     {
         // FP32 block-cyclic sweeps over a cooperative grid (A and V copies in the workspace), then
         // the FP64 finish
@@ -1393,13 +1396,15 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         double* fro2 = reinterpret_cast<double*>(base + off2 + 32);
         GridBarrier* bar = reinterpret_cast<GridBarrier*>(base + off2 + 64);
         HV_CUDA_TRY(cudaMemsetAsync(base + off2, 0, 128, st));
-        static int max_per_sm = -1;
-        if (max_per_sm < 0)
-        {
-            HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(BJ_SMEM)));
-            HV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, k_jacobi_block, BJ_THREADS, BJ_SMEM));
-        }
+        HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(BJ_SMEM)));
+        // co-resident CTAs per SM (the cooperative grid must fit); thread-safe one-time query
+        static const int max_per_sm = [] {
+            int v = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_jacobi_block, BJ_THREADS, BJ_SMEM) != cudaSuccess)
+                v = 1;
+            return v;
+        }();
         int sms = 0;
         HV_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
         const int npb = Tb / BJ_S, na = npb * (npb + 1) / 2;
@@ -1413,7 +1418,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
                                                 st));
         count_launch();
     }
-    if (T <= JS_MAX_T || (T <= JC_MAX_T && g_eig_precision == HV_EIG_FP32))
+    if (T <= JS_MAX_T || (T <= JC_MAX_T && prec == HV_EIG_FP32))
     {
         HV_LAUNCH_CHECK();
         k_eig_refine<<<T, 128, 0, st>>>(cov, V, T, ev_unsorted);

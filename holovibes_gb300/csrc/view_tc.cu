@@ -25,6 +25,8 @@
 //              mean + scale, fftshift placement, per-tile renormalisation partial sum
 // All waits are bounded in time; a wait that gives up stops every role and sets the error flag.
 #include "hv_common.cuh"
+#include <atomic>
+
 #include "hv_internal.h"
 #include "tc_common.cuh"
 
@@ -406,7 +408,7 @@ size_t view_tc_a_stage_bytes(int N)
 // N = 2K rounded up to 16 must fit the two accumulator parts in 256 TMEM columns (K <= 64).
 bool view_tc_supported(int K) { return K >= 1 && view_tc_n(K) <= 128; }
 
-static int g_view_mode = 0;  // 0 automatic (tensor cores for K >= 8), 1 SIMT, 2 tensor cores
+static std::atomic<int> g_view_mode{0};  // 0 automatic (tensor cores for K >= 8), 1 SIMT, 2 tensor cores
 
 void set_view_mode(int mode) { g_view_mode = mode; }
 
