@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    ap.add_argument("--server-mode", default="stream", choices=["bucket", "stream", "eager"],
+                    help="serving workloads: one CUDA graph per stream on its own CUDA stream (default), one "
+                         "graph per shape bucket, or no graphs")
     return ap.parse_args()
 
 
@@ -593,7 +596,8 @@ def run_serving(args):
                             "latency_ms": {"p50": float(np.percentile(np.array(lat) * 1e3, 50)),
                                            "p99": float(np.percentile(np.array(lat) * 1e3, 99))}}
         # ---- served
-        srv = hv.Server()
+        flags = {"bucket": 0, "stream": hv.SERVER_STREAM_GRAPHS, "eager": hv.SERVER_NO_GRAPHS}[args.server_mode]
+        srv = hv.Server(flags=flags)
         sts = [srv.open_stream(fd, s) for (fd, s, _) in streams]
         push = lambda i, ptr, n: sts[i].enqueue_ptr(ptr, n, hv.MEM_HOST)
         count = lambda i: sts[i].output_count()
@@ -605,6 +609,7 @@ def run_serving(args):
                 st.pull_into(outs[i].data_ptr(), hv.MEM_HOST)
         srv.reset_stats()
         g0 = srv.stats()
+        k0 = hv.kernel_launches()
         lat = []
         t0 = drive(push, count, pull, steps, lat)
         srv.sync()
@@ -613,6 +618,7 @@ def run_serving(args):
                 st.pull_into(outs[i].data_ptr(), hv.MEM_HOST)
         el = time.perf_counter() - t0
         g1 = srv.stats()
+        eager_kernels = hv.kernel_launches() - k0
         srv.close()
         results["served"] = {"frames_per_s": steps * frames_per_step / el,
                              "latency_ms": {"p50": float(np.percentile(np.array(lat) * 1e3, 50)),
@@ -622,6 +628,7 @@ def run_serving(args):
                              "graph_launches": g1["graph_launches"] - g0["graph_launches"],
                              "graph_kernels": g1["graph_kernels"] - g0["graph_kernels"],
                              "eager_cycles": g1["eager_cycles"] - g0["eager_cycles"],
+                             "eager_kernels": eager_kernels,
                              "buckets": g1["buckets"]}
     # one plain pipe per process (the reference's deployment: one instance per stream); outside
     # the clock sampler's window so the processes' start-up is not sampled
@@ -637,6 +644,7 @@ def run_serving(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FFT, views), bf16x3/f32 (PCA covariance)",
         "data": "synthetic (seeded interferograms, one seed per stream)",
         "config": {"workload": f"{args.workload}: {SERVE_WORKLOADS[args.workload]}", "streams": len(streams),
+                   "server_mode": args.server_mode,
                    "frames_per_step": frames_per_step, "parallelism": "one GPU, streams overlapped",
                    "l2": "time rings of all streams exceed L2"},
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -645,7 +653,7 @@ def run_serving(args):
                     "plain_per_process": results["plain_per_process"],
                     "served_over_plain_per_process": v / results["plain_per_process"]["frames_per_s"],
                     "shortest_window_ms_at_served_rate": window_ms},
-        "gpu_launches": int(results["served"]["graph_kernels"]),
+        "gpu_launches": int(results["served"]["graph_kernels"] + results["served"]["eager_kernels"]),
         "roofline": None, "cpu_baseline": None, "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
