@@ -227,6 +227,8 @@ def _declare(L: C.CDLL) -> None:
         "hv_pipe_kernel_launches": (u64, [vp]),
         "hv_pipe_stream": (vp, [vp]),
         "hv_fft_size_supported": (i32, [i32]),
+        "hv_fft_engine_mode": (None, [i32]),
+        "hv_spatial_sub_batch_mb": (None, [i32]),
         "hv_fresnel_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
         "hv_angular_spectrum_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
         "hv_spatial_transform": (st, [vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, i32, i32, vp]),
@@ -325,6 +327,16 @@ def kernel_launches() -> int:
 
 def fft_size_supported(n: int) -> bool:
     return bool(lib().hv_fft_size_supported(n))
+
+
+def fft_engine_mode(mode: int) -> None:
+    """Engine of the 1024-point spatial FFT passes: 0 automatic (warp engine), 1 tile engine."""
+    lib().hv_fft_engine_mode(int(mode))
+
+
+def spatial_sub_batch_mb(mb: int) -> None:
+    """Spatial-stage batching: 0 one launch per pass (default), n > 0 sub-batches of <= n MB."""
+    lib().hv_spatial_sub_batch_mb(int(mb))
 
 
 # ---------------------------------------------------------------------------------- Pipe

@@ -53,6 +53,10 @@ hv_status hv_settings_validate(hv_settings* s, const hv_frame_desc* fd) { return
 
 int hv_fft_size_supported(int n) { return fft_size_supported(n) ? 1 : 0; }
 
+void hv_fft_engine_mode(int mode) { set_fft_engine(mode); }
+
+void hv_spatial_sub_batch_mb(int mb) { set_spatial_sub_batch_mb(mb); }
+
 hv_status hv_fresnel_lens(void* lens_c64, int width, int height, float lambda, float z, float pixel_size_um,
                           int lens_mode, void* stream)
 {

@@ -19,10 +19,12 @@
 // mask, divide and ring-copy passes disappear.
 #include <math.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
 #include "fft_smem.cuh"
+#include "fft_warp.cuh"
 #include "hv_internal.h"
 
 namespace hv {
@@ -343,6 +345,232 @@ __global__ void __launch_bounds__(fft::Tile<N, F, true>::NT) k_fft_cols(ColPass 
     }
 }
 
+// ------------------------------------------------------------------ 1024-point warp engine
+// Rows: one warp per row (8 per CTA), the transpose in the warp's own 32 x 33 shared-memory
+// block (padding 33: conflict-free both ways). Columns: 8 adjacent columns per CTA, thread
+// (c, g) = (t & 7, t >> 3) holds group g of column c (a warp load covers 4 rows x 64 B); the
+// transpose goes through a [k1][n2][c] block with rows padded to 264 entries (conflict-free).
+constexpr int W32_ROWS = 8;
+constexpr int W32_COLS = 8;
+constexpr int W32_THREADS = 256;
+constexpr int W32_ROW_PAD = 33;
+constexpr int W32_COL_PAD = 32 * W32_COLS + 8;
+constexpr size_t W32_ROW_SMEM = (fftw::TW_COUNT + static_cast<size_t>(W32_ROWS) * 32 * W32_ROW_PAD) * sizeof(float2);
+constexpr size_t W32_COL_SMEM = (fftw::TW_COUNT + static_cast<size_t>(32) * W32_COL_PAD) * sizeof(float2);
+
+__global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
+{
+    extern __shared__ float2 smem[];
+    if (!ctl_active(p.ctl))
+        return;
+    const float2* tw = stage_twiddles(smem, p.tw, fftw::TW_COUNT, W32_THREADS);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y = blockIdx.x * W32_ROWS + warp;
+    if (y >= p.rows)
+        return;
+    float2* buf = smem + fftw::TW_COUNT + warp * 32 * W32_ROW_PAD;
+    const int b = blockIdx.y;
+    const void* p_in = p.raw_from_ctl ? static_cast<const void*>(static_cast<const uint8_t*>(p.in) + p.ctl->raw_offset)
+                                      : p.in;
+    const size_t e0 = static_cast<size_t>(b) * p.in_frame + static_cast<size_t>(y) * fftw::N + lane;
+    const bool inv = p.inverse != 0;
+
+    float2 x[32];
+    if (p.in_kind == IN_C64)
+    {
+        const float2* in = static_cast<const float2*>(p_in) + e0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            x[j] = __ldg(in + 32 * j);
+        if (p.premul)
+        {
+            const float2* L = p.premul + static_cast<size_t>(y) * fftw::N + lane;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                x[j] = cmul(x[j], __ldg(L + 32 * j));
+        }
+    }
+    else
+    {
+        float v[32];
+        switch (p.in_kind)
+        {
+        case IN_U8:
+        {
+            const uint8_t* in = static_cast<const uint8_t*>(p_in) + e0;
+            uint8_t u[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                u[j] = __ldcs(in + 32 * j);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                v[j] = static_cast<float>(u[j]) * 257.0f;
+            break;
+        }
+        case IN_U16:
+        case IN_U16_BE:
+        {
+            const uint16_t* in = static_cast<const uint16_t*>(p_in) + e0;
+            uint16_t u[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                u[j] = __ldcs(in + 32 * j);
+            const bool swap = p.in_kind == IN_U16_BE;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                v[j] = static_cast<float>(swap ? static_cast<uint16_t>((u[j] << 8) | (u[j] >> 8)) : u[j]);
+            break;
+        }
+        default:
+        {
+            const float* in = static_cast<const float*>(p_in) + e0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                v[j] = __ldcs(in + 32 * j);
+            break;
+        }
+        }
+        if (p.premul)
+        {
+            const float2* L = p.premul + static_cast<size_t>(y) * fftw::N + lane;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+            {
+                const float2 l = __ldg(L + 32 * j);
+                x[j] = make_float2(v[j] * l.x, v[j] * l.y);
+            }
+        }
+        else
+        {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                x[j] = make_float2(v[j], 0.f);
+        }
+    }
+    if (inv)
+    {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            x[j] = cconj(x[j]);
+    }
+
+    fftw::stage_a(x, tw, lane);
+    {
+        float2* w = buf + lane * W32_ROW_PAD;
+#pragma unroll
+        for (int k1 = 0; k1 < 32; ++k1)
+            w[k1] = x[k1];
+        __syncwarp();
+        const float2* r = buf + lane;
+#pragma unroll
+        for (int n2 = 0; n2 < 32; ++n2)
+            x[n2] = r[n2 * W32_ROW_PAD];
+    }
+    fftw::dft32(x);
+
+    float2* o = p.out + p.out_map.offset(b) + static_cast<size_t>(y) * fftw::N + lane;
+    const float sc = p.scale;
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2)
+    {
+        float2 v = x[k2];
+        if (inv)
+            v = cconj(v);
+        v = cscale(v, sc);
+        if (p.stream_out)
+            __stcs(o + 32 * k2, v);
+        else
+            o[32 * k2] = v;
+    }
+}
+
+// Column transpose through shared memory: thread (c, g) writes z[g][k1] for every k1, then reads
+// z[n2][g] for every n2 (g now the k1 it owns). Ends with a barrier so the block can be reused.
+__device__ __forceinline__ void w32_col_exchange(float2 (&x)[32], float2* S, int c, int g)
+{
+    float2* w = S + g * W32_COLS + c;
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1)
+        w[k1 * W32_COL_PAD] = x[k1];
+    __syncthreads();
+    const float2* r = S + g * W32_COL_PAD + c;
+#pragma unroll
+    for (int n2 = 0; n2 < 32; ++n2)
+        x[n2] = r[n2 * W32_COLS];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(W32_THREADS, 2) k_fft_cols_w32(ColPass p)
+{
+    extern __shared__ float2 smem[];
+    if (!ctl_active(p.ctl))
+        return;
+    const float2* tw = stage_twiddles(smem, p.tw, fftw::TW_COUNT, W32_THREADS);
+    float2* S = smem + fftw::TW_COUNT;
+    const int c = threadIdx.x & (W32_COLS - 1), g = threadIdx.x / W32_COLS;
+    const int W = p.width;
+    const int col = blockIdx.x * W32_COLS + c;
+    const bool in_range = col < W;
+    const int b = blockIdx.y;
+    // element (g + 32 j) of column `col` sits at g W + col + j (32 W)
+    const size_t e0 = static_cast<size_t>(g) * W + col;
+    const size_t step = static_cast<size_t>(32) * W;
+    const float2* in = p.in + static_cast<size_t>(b) * p.in_frame + e0;
+    const bool inv_in = p.mode == 1;
+
+    float2 x[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+        x[j] = in_range ? in[j * step] : make_float2(0.f, 0.f);
+    if (inv_in)
+    {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            x[j] = cconj(x[j]);
+    }
+    fftw::stage_a(x, tw, g);
+    w32_col_exchange(x, S, c, g);
+    fftw::dft32(x);
+
+    float2* o = p.out + p.out_map.offset(b) + e0;
+    const float sc = p.scale;
+    if (p.mode == 2)
+    {
+        // * G, conjugate, inverse transform (stage B left X[g + 32 k2], stage A's input shape)
+        const float2* Gm = p.postmul + e0;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2)
+        {
+            const float2 gv = in_range ? __ldg(Gm + k2 * step) : make_float2(0.f, 0.f);
+            x[k2] = cconj(cmul(x[k2], gv));
+        }
+        fftw::stage_a(x, tw, g);
+        w32_col_exchange(x, S, c, g);
+        fftw::dft32(x);
+        if (in_range)
+        {
+#pragma unroll
+            for (int k2 = 0; k2 < 32; ++k2)
+                o[k2 * step] = cscale(cconj(x[k2]), sc);
+        }
+        return;
+    }
+    if (!in_range)
+        return;
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2)
+    {
+        float2 v = x[k2];
+        if (inv_in)
+            v = cconj(v);
+        v = cscale(v, sc);
+        if (p.stream_out)
+            __stcs(o + k2 * step, v);
+        else
+            o[k2 * step] = v;
+    }
+}
+
 // Raw -> complex into ring slots (space transformation NONE).
 __global__ void k_convert(const void* in, int kind, size_t frame_px, int batch, float2* ring, FrameMap map,
                           const CycleCtl* ctl)
@@ -379,6 +607,7 @@ constexpr int kMaxTwDevices = 64;
 std::mutex g_tw_mu;
 const float2* g_tw_base[kMaxTwDevices] = {};
 int g_tw_offset[8192];  // offset of size N's tables in g_fft_twiddles
+int g_tw_w32_offset = 0;  // offset of the 1024-point warp engine's table
 bool g_tw_layout_ready = false;
 std::vector<float2> g_tw_host;
 
@@ -397,11 +626,15 @@ void tw_layout()
     }
     HV_FFT_SIZES(HV_TW)
 #undef HV_TW
+    g_tw_w32_offset = off;
+    g_tw_host.resize(off + fftw::TW_COUNT + 1);
+    fftw::twiddle_fill(g_tw_host.data() + off);
+    off += fftw::TW_COUNT;
     g_tw_layout_ready = true;
 }
 
-template <int N>
-const float2* twiddles()
+// Base of the twiddle array on the current device (uploaded on first use), or null.
+const float2* twiddle_base()
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxTwDevices)
@@ -419,7 +652,20 @@ const float2* twiddles()
             return nullptr;
         g_tw_base[dev] = static_cast<const float2*>(base);
     }
-    return g_tw_base[dev] + g_tw_offset[N];
+    return g_tw_base[dev];
+}
+
+template <int N>
+const float2* twiddles()
+{
+    const float2* base = twiddle_base();
+    return base ? base + g_tw_offset[N] : nullptr;
+}
+
+const float2* twiddles_w32()
+{
+    const float2* base = twiddle_base();
+    return base ? base + g_tw_w32_offset : nullptr;
 }
 
 }  // namespace
@@ -446,9 +692,42 @@ constexpr int col_lanes()
     return f;
 }
 
+std::atomic<int> g_fft_engine{0};  // 0 automatic (warp engine for 1024-point transforms), 1 tile engine only
+
+hv_status launch_rows_w32(const RowPass& p, int nframes, cudaStream_t st)
+{
+    HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_rows_w32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(W32_ROW_SMEM)));
+    RowPass q = p;
+    if ((q.tw = twiddles_w32()) == nullptr)
+        return HV_ERR_CUDA;
+    q.tw_count = fftw::TW_COUNT;
+    dim3 grid((p.rows + W32_ROWS - 1) / W32_ROWS, nframes);
+    k_fft_rows_w32<<<grid, W32_THREADS, W32_ROW_SMEM, st>>>(q);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+hv_status launch_cols_w32(const ColPass& p, int nframes, cudaStream_t st)
+{
+    HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_cols_w32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(W32_COL_SMEM)));
+    ColPass q = p;
+    if ((q.tw = twiddles_w32()) == nullptr)
+        return HV_ERR_CUDA;
+    q.tw_count = fftw::TW_COUNT;
+    dim3 grid((p.width + W32_COLS - 1) / W32_COLS, nframes);
+    k_fft_cols_w32<<<grid, W32_THREADS, W32_COL_SMEM, st>>>(q);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
 template <int N>
 hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
 {
+    if constexpr (N == fftw::N)
+        if (g_fft_engine.load() == 0)
+            return launch_rows_w32(p, nframes, st);
     constexpr int F = row_lanes<N>();
     using Tl = fft::Tile<N, F, false>;
     const int tw_count = fft::twiddle_count(typename fft::Plan<N>::List{});
@@ -470,6 +749,9 @@ hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
 template <int N>
 hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
 {
+    if constexpr (N == fftw::N)
+        if (g_fft_engine.load() == 0)
+            return launch_cols_w32(p, nframes, st);
     constexpr int F = col_lanes<N>();
     using Tl = fft::Tile<N, F, true>;
     const int tw_count = fft::twiddle_count(typename fft::Plan<N>::List{});
@@ -489,6 +771,8 @@ hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
 }
 
 }  // namespace
+
+void set_fft_engine(int mode) { g_fft_engine = mode; }
 
 bool fft_size_supported(int n)
 {
@@ -606,6 +890,9 @@ int raw_kind(int raw_bytes, int big_endian)
     }
 }
 
+static std::atomic<int> g_spatial_sub_mb{0};
+void set_spatial_sub_batch_mb(int mb) { g_spatial_sub_mb = mb < 0 ? 0 : mb; }
+
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
                             float2* work, float2* ring, int slot0, int nslots, cudaStream_t st, const CycleCtl* ctl,
                             const float2* f2d_mask, float2* work2)
@@ -638,10 +925,12 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
         set_last_error_msg("frame width/height not supported by the shared-memory FFT");
         return HV_ERR_UNSUPPORTED;
     }
-    // Sub-batches sized so the complex intermediate (sb frames) stays resident in the 129 MB L2
-    // between the passes; raw input is read and ring slots are written with streaming hints.
+    // One launch per pass over the whole batch when g_spatial_sub_mb is 0; otherwise sub-batches
+    // whose complex intermediate (sb frames) fits in that many MB of L2 between the passes. Raw
+    // input is read and ring slots are written with streaming hints.
     const size_t frame_c64 = HW * sizeof(float2);
-    int sb = static_cast<int>((48ull << 20) / frame_c64);
+    const int sub_mb = g_spatial_sub_mb.load();
+    int sb = sub_mb > 0 ? static_cast<int>((static_cast<size_t>(sub_mb) << 20) / frame_c64) : batch;
     if (sb < 1)
         sb = 1;
     if (sb > batch)

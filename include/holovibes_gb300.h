@@ -232,6 +232,14 @@ void* hv_pipe_stream(hv_pipe* p);
 
 /* Supported transform lengths for the shared-memory FFT (each of width and height). */
 int hv_fft_size_supported(int n);
+/* Engine of the 1024-point spatial FFT passes (process-wide, read at every launch): 0 = automatic
+ * (32 x 32 warp engine: 32 samples per thread, one transpose), 1 = the shared-memory Stockham tile
+ * engine used for every other length. Both compute the same transform to FP32 round-off. */
+void hv_fft_engine_mode(int mode);
+/* Batching of the spatial stage's passes (process-wide, read at every call): 0 = one launch per
+ * pass over the whole batch (default: the fewest partial waves), n > 0 = sub-batches whose complex
+ * intermediate fits in n MB (kept in L2 between the passes). Results are identical either way. */
+void hv_spatial_sub_batch_mb(int mb);
 
 /* Fresnel quadratic lens, H x W complex64, centre-cropped from the max(W,H) square.
  * Replaces fresnel_transform_lens + kernel_quadratic_lens (Backend/cuda_sources/fresnel_transform.cu:14-63,
