@@ -393,6 +393,7 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
     else
     {
         float v[32];
+        bool pre_done = false;  // x already holds the converted, premultiplied samples
         switch (p.in_kind)
         {
         case IN_U8:
@@ -402,6 +403,22 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
 #pragma unroll
             for (int j = 0; j < 32; ++j)
                 u[j] = __ldcs(in + 32 * j);
+            if (p.premul)
+            {
+                // the lens loads go out before the pixels are used: one memory round trip, not two
+                const float2* L = p.premul + static_cast<size_t>(y) * fftw::N + lane;
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    x[j] = __ldg(L + 32 * j);
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                {
+                    const float f = static_cast<float>(u[j]) * 257.0f;
+                    x[j] = make_float2(f * x[j].x, f * x[j].y);
+                }
+                pre_done = true;
+                break;
+            }
 #pragma unroll
             for (int j = 0; j < 32; ++j)
                 v[j] = static_cast<float>(u[j]) * 257.0f;
@@ -430,7 +447,10 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
             break;
         }
         }
-        if (p.premul)
+        if (pre_done)
+        {
+        }
+        else if (p.premul)
         {
             const float2* L = p.premul + static_cast<size_t>(y) * fftw::N + lane;
 #pragma unroll
