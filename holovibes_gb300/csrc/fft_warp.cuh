@@ -1,26 +1,24 @@
-// 1024-point FFT with 32 samples per thread: N = 32 x 32, two in-register 32-point DFTs and one
-// shared-memory transpose between them.
+// 512- and 1024-point FFTs with 32 samples per thread: N = NG x 32 (NG = 16 or 32), stage-A
+// DFTs of length NG, one shared-memory transpose, a 32-point stage-B DFT.
 //
-// A thread owns one "group" n2 (0..31) of a transform and holds x[n2 + 32 j], j = 0..31. Stage A
-// is a 32-point DFT over j, then the twiddle w1024^(n2 k1); after the transpose the thread owns
-// group k1 and holds z[n2][k1] for every n2; stage B is a 32-point DFT over n2 and leaves
-// X[k1 + 32 k2] in element k2 (natural order, stride 32: the same shape as stage A's input, so a
-// forward transform can be followed by an inverse one without another exchange).
+// A transform is owned by NG threads; thread g (0..NG-1) holds samples n = g + NG i, i = 0..31.
+// Decomposition n = n2 + 32 n1 (n2 < 32, n1 < NG), k = k1 + NG k2 (k1 < NG, k2 < 32):
+//   stage A  z[n2][k1] = w_N^(n2 k1) * sum_n1 x[n2 + 32 n1] w_NG^(n1 k1)   (thread g computes the
+//            groups n2 = g, and n2 = g + 16 when NG = 16: its samples g + 16 i split by parity of i)
+//   stage B  X[k1 + NG k2] = sum_n2 z[n2][k1] w_32^(n2 k2)                  (thread g owns k1 = g)
+// so after stage B thread g holds X[g + NG k2] in element k2: the same shape as stage A's input,
+// which lets a forward transform be followed by an inverse one without another exchange.
 //
-// Compared with the Stockham tile engine (16 x 8 x 8 at 16 samples per thread) this halves the
-// shared-memory exchanges, replaces the per-element index arithmetic (lane / sample decoding,
-// swizzles, twiddle indices) with compile-time register offsets and, for rows, keeps every
-// exchange inside one warp (__syncwarp, no CTA barrier).
+// Compared with the Stockham tile engine (16 x 8 x 8 at 16 samples per thread for N = 1024) this
+// halves the shared-memory exchanges, replaces the per-element index arithmetic (lane / sample
+// decoding, swizzles, twiddle indices) with compile-time register offsets and, for rows, keeps
+// every exchange inside one warp (__syncwarp, no CTA barrier).
 #pragma once
 
 #include "fft_smem.cuh"
 
 namespace hv {
 namespace fftw {
-
-constexpr int N = 1024;
-constexpr int G = 32;                // groups (threads) per transform
-constexpr int TW_COUNT = 31 * 32;    // table entry (k1 - 1) * 32 + n2 = exp(-2 pi i n2 k1 / 1024)
 
 // cos / sin of 2 pi r / 32 for r = 0..7
 __host__ __device__ constexpr float c32(int r)
@@ -88,26 +86,63 @@ __device__ __forceinline__ void dft32(float2 (&x)[32])
     }
 }
 
-// Stage A of a transform: x[j] = input sample n2 + 32 j on entry, z[n2][k1] * w1024^(n2 k1) in
-// element k1 on return. tw: shared-memory table, this thread's entries at tw[(k1 - 1) * 32 + n2].
-__device__ __forceinline__ void stage_a(float2 (&x)[32], const float2* tw, int n2)
+template <int N>
+struct Warp
 {
-    dft32(x);
-    const float2* t = tw + n2;
-#pragma unroll
-    for (int k1 = 1; k1 < 32; ++k1)
-        x[k1] = cmul(x[k1], t[(k1 - 1) * 32]);
-}
+    static_assert(N == 512 || N == 1024, "warp FFT lengths");
+    static constexpr int NG = N / 32;               // threads per transform = stage-B outputs per thread
+    static constexpr int TW_COUNT = (NG - 1) * 32;  // entry (k1 - 1) * 32 + n2 = exp(-2 pi i n2 k1 / N)
 
-inline void twiddle_fill(float2* out)
-{
-    for (int k1 = 1; k1 < 32; ++k1)
-        for (int n2 = 0; n2 < 32; ++n2)
+    // stage-A element e of thread g holds z[n2][k1] with n2 = g + 16 (e / 16) for NG = 16
+    __device__ __forceinline__ static int n2_of(int e, int g) { return NG == 32 ? g : g + 16 * (e >> 4); }
+    __device__ __host__ static constexpr int k1_of(int e) { return NG == 32 ? e : (e & 15); }
+
+    // x[i] = sample g + NG i on entry; z[n2_of(e)][k1_of(e)] * w_N^(n2 k1) in element e on return.
+    // tw: shared-memory table of this length.
+    __device__ __forceinline__ static void stage_a(float2 (&x)[32], const float2* tw, int g)
+    {
+        if constexpr (NG == 32)
         {
-            const double a = -2.0 * 3.14159265358979323846 * static_cast<double>(n2) * k1 / static_cast<double>(N);
-            *out++ = make_float2(static_cast<float>(cos(a)), static_cast<float>(sin(a)));
+            dft32(x);
+            const float2* t = tw + g;
+#pragma unroll
+            for (int k1 = 1; k1 < 32; ++k1)
+                x[k1] = cmul(x[k1], t[(k1 - 1) * 32]);
         }
-}
+        else
+        {
+            float2 a[16], b[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+            {
+                a[j] = x[2 * j];      // group g:      samples g + 32 j
+                b[j] = x[2 * j + 1];  // group g + 16: samples g + 16 + 32 j
+            }
+            fft::dft16(a);
+            fft::dft16(b);
+            const float2* ta = tw + g;
+            const float2* tb = tw + g + 16;
+            x[0] = a[0];
+            x[16] = b[0];
+#pragma unroll
+            for (int k1 = 1; k1 < 16; ++k1)
+            {
+                x[k1] = cmul(a[k1], ta[(k1 - 1) * 32]);
+                x[16 + k1] = cmul(b[k1], tb[(k1 - 1) * 32]);
+            }
+        }
+    }
+
+    static void twiddle_fill(float2* out)
+    {
+        for (int k1 = 1; k1 < NG; ++k1)
+            for (int n2 = 0; n2 < 32; ++n2)
+            {
+                const double a = -2.0 * 3.14159265358979323846 * static_cast<double>(n2) * k1 / static_cast<double>(N);
+                *out++ = make_float2(static_cast<float>(cos(a)), static_cast<float>(sin(a)));
+            }
+    }
+};
 
 }  // namespace fftw
 }  // namespace hv

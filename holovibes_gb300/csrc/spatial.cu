@@ -345,34 +345,53 @@ __global__ void __launch_bounds__(fft::Tile<N, F, true>::NT) k_fft_cols(ColPass 
     }
 }
 
-// ------------------------------------------------------------------ 1024-point warp engine
-// Rows: one warp per row (8 per CTA), the transpose in the warp's own 32 x 33 shared-memory
-// block (padding 33: conflict-free both ways). Columns: 8 adjacent columns per CTA, thread
-// (c, g) = (t & 7, t >> 3) holds group g of column c (a warp load covers 4 rows x 64 B); the
-// transpose goes through a [k1][n2][c] block with rows padded to 264 entries (conflict-free).
-constexpr int W32_ROWS = 8;
-constexpr int W32_COLS = 8;
+// ------------------------------------------------------------------ warp engine (N = 512, 1024)
+// Rows: 32 / NG rows per warp (1 or 2), 8 warps per CTA; lane (r, g) = (lane / NG, lane % NG);
+// the transpose in the warp's own [row][n2][k1] block, k1 rows padded to NG + 1 entries
+// (conflict-free both ways). Columns: 256 / NG adjacent columns per CTA (8 or 16), thread
+// (c, g) = (t % C, t / C) holds samples g + NG i of column c (a warp load covers 32 / C rows of
+// C * 8 bytes); the transpose goes through a [k1][n2][c] block (conflict-free: k1 rows padded
+// to 264 entries when C = 8).
+constexpr int W32_WARPS = 8;
 constexpr int W32_THREADS = 256;
-constexpr int W32_ROW_PAD = 33;
-constexpr int W32_COL_PAD = 32 * W32_COLS + 8;
-constexpr size_t W32_ROW_SMEM = (fftw::TW_COUNT + static_cast<size_t>(W32_ROWS) * 32 * W32_ROW_PAD) * sizeof(float2);
-constexpr size_t W32_COL_SMEM = (fftw::TW_COUNT + static_cast<size_t>(32) * W32_COL_PAD) * sizeof(float2);
 
+template <int N>
+struct W32Geom
+{
+    static constexpr int NG = fftw::Warp<N>::NG;
+    static constexpr int RPW = 32 / NG;                 // rows per warp
+    static constexpr int ROWS = W32_WARPS * RPW;        // rows per CTA
+    static constexpr int ROW_PAD = NG + 1;
+    static constexpr int ROW_BUF = RPW * 32 * ROW_PAD;  // per warp
+    static constexpr int COLS = W32_THREADS / NG;       // columns per CTA
+    static constexpr int COL_PAD = 32 * COLS + (COLS == 8 ? 8 : 0);
+    static constexpr int TW = fftw::Warp<N>::TW_COUNT;
+    static constexpr size_t ROW_SMEM = (TW + static_cast<size_t>(W32_WARPS) * ROW_BUF) * sizeof(float2);
+    static constexpr size_t COL_SMEM = (TW + static_cast<size_t>(NG) * COL_PAD) * sizeof(float2);
+};
+
+template <int N>
 __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
 {
+    using Gm = W32Geom<N>;
+    using Wp = fftw::Warp<N>;
+    constexpr int NG = Gm::NG;
     extern __shared__ float2 smem[];
     if (!ctl_active(p.ctl))
         return;
-    const float2* tw = stage_twiddles(smem, p.tw, fftw::TW_COUNT, W32_THREADS);
+    const float2* tw = stage_twiddles(smem, p.tw, Gm::TW, W32_THREADS);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int y = blockIdx.x * W32_ROWS + warp;
-    if (y >= p.rows)
-        return;
-    float2* buf = smem + fftw::TW_COUNT + warp * 32 * W32_ROW_PAD;
+    const int r = lane / NG, g = lane % NG;
+    const int y = blockIdx.x * Gm::ROWS + warp * Gm::RPW + r;
+    // lanes of a row past the frame's last row compute on zeros and store nothing (they take part
+    // in the warp's transpose)
+    const bool row_ok = y < p.rows;
+    const int yc = row_ok ? y : 0;
+    float2* buf = smem + Gm::TW + warp * Gm::ROW_BUF + r * 32 * Gm::ROW_PAD;
     const int b = blockIdx.y;
     const void* p_in = p.raw_from_ctl ? static_cast<const void*>(static_cast<const uint8_t*>(p.in) + p.ctl->raw_offset)
                                       : p.in;
-    const size_t e0 = static_cast<size_t>(b) * p.in_frame + static_cast<size_t>(y) * fftw::N + lane;
+    const size_t e0 = static_cast<size_t>(b) * p.in_frame + static_cast<size_t>(yc) * N + g;
     const bool inv = p.inverse != 0;
 
     float2 x[32];
@@ -381,13 +400,13 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
         const float2* in = static_cast<const float2*>(p_in) + e0;
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-            x[j] = __ldg(in + 32 * j);
+            x[j] = __ldg(in + NG * j);
         if (p.premul)
         {
-            const float2* L = p.premul + static_cast<size_t>(y) * fftw::N + lane;
+            const float2* L = p.premul + static_cast<size_t>(yc) * N + g;
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-                x[j] = cmul(x[j], __ldg(L + 32 * j));
+                x[j] = cmul(x[j], __ldg(L + NG * j));
         }
     }
     else
@@ -402,14 +421,14 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
             uint8_t u[32];
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-                u[j] = __ldcs(in + 32 * j);
+                u[j] = __ldcs(in + NG * j);
             if (p.premul)
             {
                 // the lens loads go out before the pixels are used: one memory round trip, not two
-                const float2* L = p.premul + static_cast<size_t>(y) * fftw::N + lane;
+                const float2* L = p.premul + static_cast<size_t>(yc) * N + g;
 #pragma unroll
                 for (int j = 0; j < 32; ++j)
-                    x[j] = __ldg(L + 32 * j);
+                    x[j] = __ldg(L + NG * j);
 #pragma unroll
                 for (int j = 0; j < 32; ++j)
                 {
@@ -431,7 +450,7 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
             uint16_t u[32];
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-                u[j] = __ldcs(in + 32 * j);
+                u[j] = __ldcs(in + NG * j);
             const bool swap = p.in_kind == IN_U16_BE;
 #pragma unroll
             for (int j = 0; j < 32; ++j)
@@ -443,7 +462,7 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
             const float* in = static_cast<const float*>(p_in) + e0;
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-                v[j] = __ldcs(in + 32 * j);
+                v[j] = __ldcs(in + NG * j);
             break;
         }
         }
@@ -452,11 +471,11 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
         }
         else if (p.premul)
         {
-            const float2* L = p.premul + static_cast<size_t>(y) * fftw::N + lane;
+            const float2* L = p.premul + static_cast<size_t>(yc) * N + g;
 #pragma unroll
             for (int j = 0; j < 32; ++j)
             {
-                const float2 l = __ldg(L + 32 * j);
+                const float2 l = __ldg(L + NG * j);
                 x[j] = make_float2(v[j] * l.x, v[j] * l.y);
             }
         }
@@ -474,21 +493,20 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
             x[j] = cconj(x[j]);
     }
 
-    fftw::stage_a(x, tw, lane);
-    {
-        float2* w = buf + lane * W32_ROW_PAD;
+    Wp::stage_a(x, tw, g);
+    // transpose: z[n2][k1] at buf[n2 * ROW_PAD + k1]; thread g then reads z[n2][g] for every n2
 #pragma unroll
-        for (int k1 = 0; k1 < 32; ++k1)
-            w[k1] = x[k1];
-        __syncwarp();
-        const float2* r = buf + lane;
+    for (int e = 0; e < 32; ++e)
+        buf[Wp::n2_of(e, g) * Gm::ROW_PAD + Wp::k1_of(e)] = x[e];
+    __syncwarp();
 #pragma unroll
-        for (int n2 = 0; n2 < 32; ++n2)
-            x[n2] = r[n2 * W32_ROW_PAD];
-    }
+    for (int n2 = 0; n2 < 32; ++n2)
+        x[n2] = buf[n2 * Gm::ROW_PAD + g];
     fftw::dft32(x);
 
-    float2* o = p.out + p.out_map.offset(b) + static_cast<size_t>(y) * fftw::N + lane;
+    if (!row_ok)
+        return;
+    float2* o = p.out + p.out_map.offset(b) + static_cast<size_t>(y) * N + g;
     const float sc = p.scale;
 #pragma unroll
     for (int k2 = 0; k2 < 32; ++k2)
@@ -498,43 +516,49 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
             v = cconj(v);
         v = cscale(v, sc);
         if (p.stream_out)
-            __stcs(o + 32 * k2, v);
+            __stcs(o + NG * k2, v);
         else
-            o[32 * k2] = v;
+            o[NG * k2] = v;
     }
 }
 
-// Column transpose through shared memory: thread (c, g) writes z[g][k1] for every k1, then reads
-// z[n2][g] for every n2 (g now the k1 it owns). Ends with a barrier so the block can be reused.
+// Column transpose through shared memory: thread (c, g) writes its z[n2][k1], then reads z[n2][g]
+// for every n2 (g now the k1 it owns). Ends with a barrier so the block can be reused.
+template <int N>
 __device__ __forceinline__ void w32_col_exchange(float2 (&x)[32], float2* S, int c, int g)
 {
-    float2* w = S + g * W32_COLS + c;
+    using Gm = W32Geom<N>;
+    using Wp = fftw::Warp<N>;
 #pragma unroll
-    for (int k1 = 0; k1 < 32; ++k1)
-        w[k1 * W32_COL_PAD] = x[k1];
+    for (int e = 0; e < 32; ++e)
+        S[Wp::k1_of(e) * Gm::COL_PAD + Wp::n2_of(e, g) * Gm::COLS + c] = x[e];
     __syncthreads();
-    const float2* r = S + g * W32_COL_PAD + c;
+    const float2* rd = S + g * Gm::COL_PAD + c;
 #pragma unroll
     for (int n2 = 0; n2 < 32; ++n2)
-        x[n2] = r[n2 * W32_COLS];
+        x[n2] = rd[n2 * Gm::COLS];
     __syncthreads();
 }
 
+template <int N>
 __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_cols_w32(ColPass p)
 {
+    using Gm = W32Geom<N>;
+    using Wp = fftw::Warp<N>;
+    constexpr int NG = Gm::NG;
     extern __shared__ float2 smem[];
     if (!ctl_active(p.ctl))
         return;
-    const float2* tw = stage_twiddles(smem, p.tw, fftw::TW_COUNT, W32_THREADS);
-    float2* S = smem + fftw::TW_COUNT;
-    const int c = threadIdx.x & (W32_COLS - 1), g = threadIdx.x / W32_COLS;
+    const float2* tw = stage_twiddles(smem, p.tw, Gm::TW, W32_THREADS);
+    float2* S = smem + Gm::TW;
+    const int c = threadIdx.x % Gm::COLS, g = threadIdx.x / Gm::COLS;
     const int W = p.width;
-    const int col = blockIdx.x * W32_COLS + c;
+    const int col = blockIdx.x * Gm::COLS + c;
     const bool in_range = col < W;
     const int b = blockIdx.y;
-    // element (g + 32 j) of column `col` sits at g W + col + j (32 W)
+    // sample g + NG j of column `col` sits at g W + col + j (NG W)
     const size_t e0 = static_cast<size_t>(g) * W + col;
-    const size_t step = static_cast<size_t>(32) * W;
+    const size_t step = static_cast<size_t>(NG) * W;
     const float2* in = p.in + static_cast<size_t>(b) * p.in_frame + e0;
     const bool inv_in = p.mode == 1;
 
@@ -548,24 +572,24 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_cols_w32(ColPass p)
         for (int j = 0; j < 32; ++j)
             x[j] = cconj(x[j]);
     }
-    fftw::stage_a(x, tw, g);
-    w32_col_exchange(x, S, c, g);
+    Wp::stage_a(x, tw, g);
+    w32_col_exchange<N>(x, S, c, g);
     fftw::dft32(x);
 
     float2* o = p.out + p.out_map.offset(b) + e0;
     const float sc = p.scale;
     if (p.mode == 2)
     {
-        // * G, conjugate, inverse transform (stage B left X[g + 32 k2], stage A's input shape)
-        const float2* Gm = p.postmul + e0;
+        // * G, conjugate, inverse transform (stage B left X[g + NG k2], stage A's input shape)
+        const float2* Gp = p.postmul + e0;
 #pragma unroll
         for (int k2 = 0; k2 < 32; ++k2)
         {
-            const float2 gv = in_range ? __ldg(Gm + k2 * step) : make_float2(0.f, 0.f);
+            const float2 gv = in_range ? __ldg(Gp + k2 * step) : make_float2(0.f, 0.f);
             x[k2] = cconj(cmul(x[k2], gv));
         }
-        fftw::stage_a(x, tw, g);
-        w32_col_exchange(x, S, c, g);
+        Wp::stage_a(x, tw, g);
+        w32_col_exchange<N>(x, S, c, g);
         fftw::dft32(x);
         if (in_range)
         {
@@ -627,7 +651,7 @@ constexpr int kMaxTwDevices = 64;
 std::mutex g_tw_mu;
 const float2* g_tw_base[kMaxTwDevices] = {};
 int g_tw_offset[8192];  // offset of size N's tables in g_fft_twiddles
-int g_tw_w32_offset = 0;  // offset of the 1024-point warp engine's table
+int g_tw_w32_offset[2] = {};  // offsets of the warp engine's tables (N = 512, 1024)
 bool g_tw_layout_ready = false;
 std::vector<float2> g_tw_host;
 
@@ -646,10 +670,14 @@ void tw_layout()
     }
     HV_FFT_SIZES(HV_TW)
 #undef HV_TW
-    g_tw_w32_offset = off;
-    g_tw_host.resize(off + fftw::TW_COUNT + 1);
-    fftw::twiddle_fill(g_tw_host.data() + off);
-    off += fftw::TW_COUNT;
+    g_tw_w32_offset[1] = off;
+    g_tw_host.resize(off + fftw::Warp<1024>::TW_COUNT + 1);
+    fftw::Warp<1024>::twiddle_fill(g_tw_host.data() + off);
+    off += fftw::Warp<1024>::TW_COUNT;
+    g_tw_w32_offset[0] = off;
+    g_tw_host.resize(off + fftw::Warp<512>::TW_COUNT + 1);
+    fftw::Warp<512>::twiddle_fill(g_tw_host.data() + off);
+    off += fftw::Warp<512>::TW_COUNT;
     g_tw_layout_ready = true;
 }
 
@@ -682,10 +710,11 @@ const float2* twiddles()
     return base ? base + g_tw_offset[N] : nullptr;
 }
 
+template <int N>
 const float2* twiddles_w32()
 {
     const float2* base = twiddle_base();
-    return base ? base + g_tw_w32_offset : nullptr;
+    return base ? base + g_tw_w32_offset[N == 1024 ? 1 : 0] : nullptr;
 }
 
 }  // namespace
@@ -712,31 +741,37 @@ constexpr int col_lanes()
     return f;
 }
 
-std::atomic<int> g_fft_engine{0};  // 0 automatic (warp engine for 1024-point transforms), 1 tile engine only
+std::atomic<int> g_fft_engine{0};  // 0 automatic (warp engine for 512- and 1024-point transforms), 1 tile engine only
 
+template <int N>
 hv_status launch_rows_w32(const RowPass& p, int nframes, cudaStream_t st)
 {
-    HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_rows_w32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(W32_ROW_SMEM)));
+    using Gm = W32Geom<N>;
+    HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_rows_w32<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(Gm::ROW_SMEM)));
     RowPass q = p;
-    if ((q.tw = twiddles_w32()) == nullptr)
+    if ((q.tw = twiddles_w32<N>()) == nullptr)
         return HV_ERR_CUDA;
-    q.tw_count = fftw::TW_COUNT;
-    dim3 grid((p.rows + W32_ROWS - 1) / W32_ROWS, nframes);
-    k_fft_rows_w32<<<grid, W32_THREADS, W32_ROW_SMEM, st>>>(q);
+    q.tw_count = Gm::TW;
+    dim3 grid((p.rows + Gm::ROWS - 1) / Gm::ROWS, nframes);
+    k_fft_rows_w32<N><<<grid, W32_THREADS, Gm::ROW_SMEM, st>>>(q);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
 }
 
+template <int N>
 hv_status launch_cols_w32(const ColPass& p, int nframes, cudaStream_t st)
 {
-    HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_cols_w32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(W32_COL_SMEM)));
+    using Gm = W32Geom<N>;
+    HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_cols_w32<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(Gm::COL_SMEM)));
     ColPass q = p;
-    if ((q.tw = twiddles_w32()) == nullptr)
+    if ((q.tw = twiddles_w32<N>()) == nullptr)
         return HV_ERR_CUDA;
-    q.tw_count = fftw::TW_COUNT;
-    dim3 grid((p.width + W32_COLS - 1) / W32_COLS, nframes);
-    k_fft_cols_w32<<<grid, W32_THREADS, W32_COL_SMEM, st>>>(q);
+    q.tw_count = Gm::TW;
+    dim3 grid((p.width + Gm::COLS - 1) / Gm::COLS, nframes);
+    k_fft_cols_w32<N><<<grid, W32_THREADS, Gm::COL_SMEM, st>>>(q);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
@@ -745,9 +780,9 @@ hv_status launch_cols_w32(const ColPass& p, int nframes, cudaStream_t st)
 template <int N>
 hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
 {
-    if constexpr (N == fftw::N)
+    if constexpr (N == 512 || N == 1024)
         if (g_fft_engine.load() == 0)
-            return launch_rows_w32(p, nframes, st);
+            return launch_rows_w32<N>(p, nframes, st);
     constexpr int F = row_lanes<N>();
     using Tl = fft::Tile<N, F, false>;
     const int tw_count = fft::twiddle_count(typename fft::Plan<N>::List{});
@@ -769,9 +804,9 @@ hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
 template <int N>
 hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
 {
-    if constexpr (N == fftw::N)
+    if constexpr (N == 512 || N == 1024)
         if (g_fft_engine.load() == 0)
-            return launch_cols_w32(p, nframes, st);
+            return launch_cols_w32<N>(p, nframes, st);
     constexpr int F = col_lanes<N>();
     using Tl = fft::Tile<N, F, true>;
     const int tw_count = fft::twiddle_count(typename fft::Plan<N>::List{});

@@ -1,4 +1,4 @@
-"""1024-point spatial FFT passes on both engines (hv_fft_engine_mode 0: 32 x 32 warp engine,
+"""512- and 1024-point spatial FFT passes on both engines (hv_fft_engine_mode 0: warp engine,
 1: shared-memory Stockham tiles) against numpy's FP64 FFT and against each other: the 2-D
 transform, the row pass with every input encoding, the lens premultiply, inverse, scale and ring
 slots, the column pass in its three modes (forward, inverse, forward * G * inverse) and frame
@@ -27,8 +27,9 @@ def _c64(rng, shape):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("engine", [0, 1], indirect=True)
-@pytest.mark.parametrize("n0,n1", [(1024, 1024), (1024, 768), (768, 1024), (1024, 48), (16, 1024), (1024, 2048)])
-def test_fft2d_1024(cuda, engine, n0, n1):
+@pytest.mark.parametrize("n0,n1", [(1024, 1024), (1024, 768), (768, 1024), (1024, 48), (16, 1024), (1024, 2048),
+                                   (512, 512), (512, 768), (768, 512), (512, 48), (16, 512), (512, 1024)])
+def test_fft2d_warp_lengths(cuda, engine, n0, n1):
     rng = np.random.default_rng(n0 + 3 * n1)
     B = 2
     x = _c64(rng, (B, n0, n1))
@@ -40,8 +41,7 @@ def test_fft2d_1024(cuda, engine, n0, n1):
     assert rel_l2(host(yd, np.complex64, x.shape), x) <= 1e-5
 
 
-def _rows(raw, in_bytes, big_endian, H, B, premul, inverse, scale, slot0, nslots):
-    W = 1024
+def _rows(raw, in_bytes, big_endian, W, H, B, premul, inverse, scale, slot0, nslots):
     out = zeros(nslots * H * W * 8)
     call("hv_fft_rows", ptr(dev(raw)), in_bytes, big_endian, ptr(out), W, H, B,
          ptr(dev(premul)) if premul is not None else None, inverse, scale, slot0, nslots, None)
@@ -52,8 +52,9 @@ def _rows(raw, in_bytes, big_endian, H, B, premul, inverse, scale, slot0, nslots
 @pytest.mark.parametrize("dtype,big_endian", [(np.uint8, 0), (np.uint16, 0), (np.uint16, 1), (np.float32, 0),
                                               (np.complex64, 0)])
 @pytest.mark.parametrize("H,use_premul,inverse", [(13, True, 0), (8, False, 1), (40, True, 1)])
-def test_row_pass_1024_engines(cuda, dtype, big_endian, H, use_premul, inverse):
-    W, B, nslots, slot0 = 1024, 3, 4, 2
+@pytest.mark.parametrize("W", [512, 1024])
+def test_row_pass_engines(cuda, dtype, big_endian, W, H, use_premul, inverse):
+    B, nslots, slot0 = 3, 4, 2
     rng = np.random.default_rng(H + int(big_endian))
     if dtype == np.complex64:
         raw = _c64(rng, (B, H, W))
@@ -71,7 +72,8 @@ def test_row_pass_1024_engines(cuda, dtype, big_endian, H, use_premul, inverse):
     for mode in (0, 1):
         hv.fft_engine_mode(mode)
         try:
-            got[mode] = _rows(raw_in, np.dtype(dtype).itemsize, big_endian, H, B, premul, inverse, 0.5, slot0, nslots)
+            got[mode] = _rows(raw_in, np.dtype(dtype).itemsize, big_endian, W, H, B, premul, inverse, 0.5, slot0,
+                              nslots)
         finally:
             hv.fft_engine_mode(0)
         for b in range(B):
@@ -81,10 +83,11 @@ def test_row_pass_1024_engines(cuda, dtype, big_endian, H, use_premul, inverse):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("W", [1024, 48, 96])
+@pytest.mark.parametrize("W", [1024, 48, 96, 16])
 @pytest.mark.parametrize("mode", [0, 1, 2])
-def test_col_pass_1024_engines(cuda, W, mode):
-    H, B, nslots, slot0 = 1024, 2, 3, 1
+@pytest.mark.parametrize("H", [512, 1024])
+def test_col_pass_engines(cuda, W, H, mode):
+    B, nslots, slot0 = 2, 3, 1
     rng = np.random.default_rng(W + 10 * mode)
     x = _c64(rng, (B, H, W))
     G = _c64(rng, (H, W)) if mode == 2 else None
@@ -114,11 +117,11 @@ def test_col_pass_1024_engines(cuda, W, mode):
 @pytest.mark.gpu
 @pytest.mark.parametrize("engine", [0, 1], indirect=True)
 @pytest.mark.parametrize("space", [hv.SPACE_FRESNELTR, hv.SPACE_ANGULARSP])
-def test_spatial_1024_engines(cuda, engine, space):
-    """The fused spatial stage at 1024 x 1024 u8 (the Fresnel + PCA workload's frames) on both engines."""
+@pytest.mark.parametrize("W,H", [(1024, 1024), (512, 512), (1024, 512)])
+def test_spatial_engines(cuda, engine, space, W, H):
+    """The fused spatial stage on u8 frames (1024 x 1024: the Fresnel + PCA workload's frames)."""
     from holovibes_gb300.synthetic import Interferogram
 
-    W = H = 1024
     B = 3
     raw = (Interferogram(width=W, height=H, seed=5).frames(0, B) >> 4).astype(np.uint8)
     lens = empty(W * H * 8)
@@ -134,3 +137,26 @@ def test_spatial_1024_engines(cuda, engine, space):
     name = {1: "FRESNELTR", 2: "ANGULARSP"}[space]
     ref = O.spatial_transform(O.convert_frames(raw), name, ref_lens)
     assert rel_l2(host(ring, np.complex64, (B, H, W)), ref) <= 1e-5
+
+
+@pytest.mark.gpu
+def test_spatial_sub_batches_bit_identical(cuda):
+    """hv_spatial_sub_batch_mb only changes how the batch is split into launches: every frame goes
+    through the same kernels, so ring contents are bit-identical with and without sub-batches."""
+    W = H = 1024
+    B = 5
+    rng = np.random.default_rng(11)
+    raw = dev((rng.random((B, H, W)) * 255).astype(np.uint8))
+    lens = empty(W * H * 8)
+    call("hv_fresnel_lens", ptr(lens), W, H, 785e-9, 0.45, 12.0, 0, None)
+    rings = []
+    for mb in (0, 16):  # 16 MB: two frames per sub-batch, the last one alone
+        hv.spatial_sub_batch_mb(mb)
+        try:
+            work, ring = empty(B * H * W * 8), zeros(B * H * W * 8)
+            call("hv_spatial_transform", ptr(raw), 1, 0, W, H, B, hv.SPACE_FRESNELTR, ptr(lens), ptr(work), ptr(ring),
+                 3, B, None)
+            rings.append(host(ring, np.complex64, (B, H, W)))
+        finally:
+            hv.spatial_sub_batch_mb(0)
+    assert np.array_equal(rings[0], rings[1])
