@@ -144,5 +144,122 @@ struct Warp
     }
 };
 
+// ------------------------------------------------------------------------- N = 768 = 24 x 32
+// Two orders, each with 32 samples at most per thread:
+//   V24 (DFT24 first): thread g < 32 holds samples g + 32 i (i < 24); stage A = DFT24 and the
+//        twiddle w768^(g k1) (k1 < 24); after the transpose thread k1 < 24 holds z[n2][k1] for
+//        n2 < 32, stage B = DFT32, leaving X[k1 + 24 k2] (k2 < 32) in element k2.
+//   V32 (DFT32 first): thread g < 24 holds samples g + 24 i (i < 32); stage A = DFT32 and the
+//        twiddle w768^(g k1) (k1 < 32); after the transpose thread k1 < 32 holds z[n2][k1] for
+//        n2 < 24, stage B = DFT24, leaving X[k1 + 32 k2] (k2 < 24) in element k2.
+// V24's output has V32's input shape and the other way round (the AS middle pass: V24 forward,
+// * G, V32 inverse, no extra exchange).
+
+// cos / sin of 2 pi r / 24 for r = 0..5
+__host__ __device__ constexpr float c24(int r)
+{
+    return r == 0   ? 1.0f
+           : r == 1 ? 0.965925826289068286749743199728897367f
+           : r == 2 ? 0.866025403784438646763723170752936183f
+           : r == 3 ? 0.707106781186547524400844362104849039f
+           : r == 4 ? 0.5f
+                    : 0.258819045102520762348898837624048328f;
+}
+__host__ __device__ constexpr float s24(int r) { return r == 0 ? 0.0f : c24(6 - r); }
+
+// a * w24^m, w24 = exp(-2 pi i / 24) (w24^6 = -i); m is a constant after unrolling
+__device__ __forceinline__ float2 w24mul(int m, float2 a)
+{
+    const int r = m % 6, q = (m / 6) & 3;
+    float2 b;
+    if (r == 0)
+        b = a;
+    else if (r == 3)
+        b = fft::w8mul<1>(a);
+    else
+    {
+        const float c = c24(r), s = s24(r);
+        b = make_float2(fmaf(a.y, s, a.x * c), fmaf(-a.x, s, a.y * c));  // a * (c - i s)
+    }
+    if (q == 1)
+        return cmul_negi(b);
+    if (q == 2)
+        return make_float2(-b.x, -b.y);
+    if (q == 3)
+        return cmul_posi(b);
+    return b;
+}
+
+// Forward 24-point DFT in place on x[0..23] (natural order): n = 3 n1 + n2, k = k1 + 8 k2; DFT8
+// over n1, twiddle w24^(n2 k1), DFT3 over n2.
+__device__ __forceinline__ void dft24(float2* x)
+{
+    float2 a[3][8];
+#pragma unroll
+    for (int n2 = 0; n2 < 3; ++n2)
+    {
+#pragma unroll
+        for (int n1 = 0; n1 < 8; ++n1)
+            a[n2][n1] = x[3 * n1 + n2];
+        fft::dft8(a[n2]);
+    }
+#pragma unroll
+    for (int n2 = 1; n2 < 3; ++n2)
+#pragma unroll
+        for (int k1 = 1; k1 < 8; ++k1)
+            a[n2][k1] = w24mul(n2 * k1, a[n2][k1]);
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1)
+    {
+        fft::dft3(a[0][k1], a[1][k1], a[2][k1]);
+        x[k1] = a[0][k1];
+        x[k1 + 8] = a[1][k1];
+        x[k1 + 16] = a[2][k1];
+    }
+}
+
+struct W768
+{
+    static constexpr int N = 768;
+    static constexpr int TW24 = 23 * 32;  // V24 entry (k1 - 1) * 32 + g = exp(-2 pi i g k1 / 768), g < 32
+    static constexpr int TW32 = 31 * 24;  // V32 entry (k1 - 1) * 24 + g, g < 24 (stored after V24's)
+    static constexpr int TW_COUNT = TW24 + TW32;
+
+    // V24 stage A: x[i] = sample g + 32 i (i < 24) -> z[g][k1] * w^(g k1) in x[k1] (k1 < 24)
+    __device__ __forceinline__ static void stage_a24(float2 (&x)[32], const float2* tw, int g)
+    {
+        dft24(x);
+        const float2* t = tw + g;
+#pragma unroll
+        for (int k1 = 1; k1 < 24; ++k1)
+            x[k1] = cmul(x[k1], t[(k1 - 1) * 32]);
+    }
+    // V32 stage A: x[i] = sample g + 24 i (i < 32, g < 24) -> z[g][k1] * w^(g k1) in x[k1]
+    __device__ __forceinline__ static void stage_a32(float2 (&x)[32], const float2* tw, int g)
+    {
+        dft32(x);
+        const float2* t = tw + TW24 + g;
+#pragma unroll
+        for (int k1 = 1; k1 < 32; ++k1)
+            x[k1] = cmul(x[k1], t[(k1 - 1) * 24]);
+    }
+
+    static void twiddle_fill(float2* out)
+    {
+        for (int k1 = 1; k1 < 24; ++k1)
+            for (int g = 0; g < 32; ++g)
+            {
+                const double a = -2.0 * 3.14159265358979323846 * static_cast<double>(g) * k1 / static_cast<double>(N);
+                *out++ = make_float2(static_cast<float>(cos(a)), static_cast<float>(sin(a)));
+            }
+        for (int k1 = 1; k1 < 32; ++k1)
+            for (int g = 0; g < 24; ++g)
+            {
+                const double a = -2.0 * 3.14159265358979323846 * static_cast<double>(g) * k1 / static_cast<double>(N);
+                *out++ = make_float2(static_cast<float>(cos(a)), static_cast<float>(sin(a)));
+            }
+    }
+};
+
 }  // namespace fftw
 }  // namespace hv

@@ -370,6 +370,113 @@ struct W32Geom
     static constexpr size_t COL_SMEM = (TW + static_cast<size_t>(NG) * COL_PAD) * sizeof(float2);
 };
 
+// First-stage samples of one row: x[j] = converted sample at e0 + STRIDE j (j < NS) of the input,
+// times premul[l0 + STRIDE j] when the pass has one, conjugated for an inverse pass. Every load of
+// the thread is issued before any is used (the input kind is a uniform branch).
+template <int NS, int STRIDE>
+__device__ __forceinline__ void load_row_samples(const RowPass& p, const void* p_in, size_t e0, size_t l0,
+                                                 float2 (&x)[32])
+{
+    const bool inv = p.inverse != 0;
+    if (p.in_kind == IN_C64)
+    {
+        const float2* in = static_cast<const float2*>(p_in) + e0;
+#pragma unroll
+        for (int j = 0; j < NS; ++j)
+            x[j] = __ldg(in + STRIDE * j);
+        if (p.premul)
+        {
+            const float2* L = p.premul + l0;
+#pragma unroll
+            for (int j = 0; j < NS; ++j)
+                x[j] = cmul(x[j], __ldg(L + STRIDE * j));
+        }
+    }
+    else
+    {
+        float v[NS];
+        bool pre_done = false;  // x already holds the converted, premultiplied samples
+        switch (p.in_kind)
+        {
+        case IN_U8:
+        {
+            const uint8_t* in = static_cast<const uint8_t*>(p_in) + e0;
+            uint8_t u[NS];
+#pragma unroll
+            for (int j = 0; j < NS; ++j)
+                u[j] = __ldcs(in + STRIDE * j);
+            if (p.premul)
+            {
+                // the lens loads go out before the pixels are used: one memory round trip, not two
+                const float2* L = p.premul + l0;
+#pragma unroll
+                for (int j = 0; j < NS; ++j)
+                    x[j] = __ldg(L + STRIDE * j);
+#pragma unroll
+                for (int j = 0; j < NS; ++j)
+                {
+                    const float f = static_cast<float>(u[j]) * 257.0f;
+                    x[j] = make_float2(f * x[j].x, f * x[j].y);
+                }
+                pre_done = true;
+                break;
+            }
+#pragma unroll
+            for (int j = 0; j < NS; ++j)
+                v[j] = static_cast<float>(u[j]) * 257.0f;
+            break;
+        }
+        case IN_U16:
+        case IN_U16_BE:
+        {
+            const uint16_t* in = static_cast<const uint16_t*>(p_in) + e0;
+            uint16_t u[NS];
+#pragma unroll
+            for (int j = 0; j < NS; ++j)
+                u[j] = __ldcs(in + STRIDE * j);
+            const bool swap = p.in_kind == IN_U16_BE;
+#pragma unroll
+            for (int j = 0; j < NS; ++j)
+                v[j] = static_cast<float>(swap ? static_cast<uint16_t>((u[j] << 8) | (u[j] >> 8)) : u[j]);
+            break;
+        }
+        default:
+        {
+            const float* in = static_cast<const float*>(p_in) + e0;
+#pragma unroll
+            for (int j = 0; j < NS; ++j)
+                v[j] = __ldcs(in + STRIDE * j);
+            break;
+        }
+        }
+        if (pre_done)
+        {
+        }
+        else if (p.premul)
+        {
+            const float2* L = p.premul + l0;
+#pragma unroll
+            for (int j = 0; j < NS; ++j)
+            {
+                const float2 l = __ldg(L + STRIDE * j);
+                x[j] = make_float2(v[j] * l.x, v[j] * l.y);
+            }
+        }
+        else
+        {
+#pragma unroll
+            for (int j = 0; j < NS; ++j)
+                x[j] = make_float2(v[j], 0.f);
+        }
+    }
+    if (inv)
+    {
+#pragma unroll
+        for (int j = 0; j < NS; ++j)
+            x[j] = cconj(x[j]);
+    }
+}
+
 template <int N>
 __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
 {
@@ -395,104 +502,7 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32(RowPass p)
     const bool inv = p.inverse != 0;
 
     float2 x[32];
-    if (p.in_kind == IN_C64)
-    {
-        const float2* in = static_cast<const float2*>(p_in) + e0;
-#pragma unroll
-        for (int j = 0; j < 32; ++j)
-            x[j] = __ldg(in + NG * j);
-        if (p.premul)
-        {
-            const float2* L = p.premul + static_cast<size_t>(yc) * N + g;
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                x[j] = cmul(x[j], __ldg(L + NG * j));
-        }
-    }
-    else
-    {
-        float v[32];
-        bool pre_done = false;  // x already holds the converted, premultiplied samples
-        switch (p.in_kind)
-        {
-        case IN_U8:
-        {
-            const uint8_t* in = static_cast<const uint8_t*>(p_in) + e0;
-            uint8_t u[32];
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                u[j] = __ldcs(in + NG * j);
-            if (p.premul)
-            {
-                // the lens loads go out before the pixels are used: one memory round trip, not two
-                const float2* L = p.premul + static_cast<size_t>(yc) * N + g;
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    x[j] = __ldg(L + NG * j);
-#pragma unroll
-                for (int j = 0; j < 32; ++j)
-                {
-                    const float f = static_cast<float>(u[j]) * 257.0f;
-                    x[j] = make_float2(f * x[j].x, f * x[j].y);
-                }
-                pre_done = true;
-                break;
-            }
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                v[j] = static_cast<float>(u[j]) * 257.0f;
-            break;
-        }
-        case IN_U16:
-        case IN_U16_BE:
-        {
-            const uint16_t* in = static_cast<const uint16_t*>(p_in) + e0;
-            uint16_t u[32];
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                u[j] = __ldcs(in + NG * j);
-            const bool swap = p.in_kind == IN_U16_BE;
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                v[j] = static_cast<float>(swap ? static_cast<uint16_t>((u[j] << 8) | (u[j] >> 8)) : u[j]);
-            break;
-        }
-        default:
-        {
-            const float* in = static_cast<const float*>(p_in) + e0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                v[j] = __ldcs(in + NG * j);
-            break;
-        }
-        }
-        if (pre_done)
-        {
-        }
-        else if (p.premul)
-        {
-            const float2* L = p.premul + static_cast<size_t>(yc) * N + g;
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-            {
-                const float2 l = __ldg(L + NG * j);
-                x[j] = make_float2(v[j] * l.x, v[j] * l.y);
-            }
-        }
-        else
-        {
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-                x[j] = make_float2(v[j], 0.f);
-        }
-    }
-    if (inv)
-    {
-#pragma unroll
-        for (int j = 0; j < 32; ++j)
-            x[j] = cconj(x[j]);
-    }
-
+    load_row_samples<32, NG>(p, p_in, e0, static_cast<size_t>(yc) * N + g, x);
     Wp::stage_a(x, tw, g);
     // transpose: z[n2][k1] at buf[n2 * ROW_PAD + k1]; thread g then reads z[n2][g] for every n2
 #pragma unroll
@@ -615,6 +625,154 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_cols_w32(ColPass p)
     }
 }
 
+// ------------------------------------------------------------------ warp engine, N = 768
+// Rows: one warp per row (V24: 32 lanes load and run DFT24, lanes 0..23 run the DFT32 and store).
+// Columns: 8 columns per CTA, thread (c, g) = (t & 7, t >> 3); forward = V24 (warps 6-7 idle in
+// stage B), the AS middle pass continues with V32 (warps 6-7 idle in its stage A).
+constexpr int W768_ROWS = 8;
+constexpr int W768_ROW_PAD = 25;
+constexpr int W768_COLS = 8;
+constexpr int W768_COL_PAD = 32 * W768_COLS + 8;
+constexpr size_t W768_ROW_SMEM =
+    (fftw::W768::TW_COUNT + static_cast<size_t>(W768_ROWS) * 32 * W768_ROW_PAD) * sizeof(float2);
+constexpr size_t W768_COL_SMEM = (fftw::W768::TW_COUNT + static_cast<size_t>(32) * W768_COL_PAD) * sizeof(float2);
+
+__global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w768(RowPass p)
+{
+    using W = fftw::W768;
+    extern __shared__ float2 smem[];
+    if (!ctl_active(p.ctl))
+        return;
+    const float2* tw = stage_twiddles(smem, p.tw, W::TW_COUNT, W32_THREADS);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int y = blockIdx.x * W768_ROWS + warp;
+    if (y >= p.rows)
+        return;
+    float2* buf = smem + W::TW_COUNT + warp * 32 * W768_ROW_PAD;
+    const int b = blockIdx.y;
+    const void* p_in = p.raw_from_ctl ? static_cast<const void*>(static_cast<const uint8_t*>(p.in) + p.ctl->raw_offset)
+                                      : p.in;
+    const size_t l0 = static_cast<size_t>(y) * W::N + lane;
+    float2 x[32];
+    load_row_samples<24, 32>(p, p_in, static_cast<size_t>(b) * p.in_frame + l0, l0, x);
+    W::stage_a24(x, tw, lane);
+#pragma unroll
+    for (int k1 = 0; k1 < 24; ++k1)
+        buf[lane * W768_ROW_PAD + k1] = x[k1];
+    __syncwarp();
+    if (lane >= 24)
+        return;
+#pragma unroll
+    for (int n2 = 0; n2 < 32; ++n2)
+        x[n2] = buf[n2 * W768_ROW_PAD + lane];
+    fftw::dft32(x);
+    const bool inv = p.inverse != 0;
+    float2* o = p.out + p.out_map.offset(b) + l0;
+    const float sc = p.scale;
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2)
+    {
+        float2 v = x[k2];
+        if (inv)
+            v = cconj(v);
+        v = cscale(v, sc);
+        if (p.stream_out)
+            __stcs(o + 24 * k2, v);
+        else
+            o[24 * k2] = v;
+    }
+}
+
+__global__ void __launch_bounds__(W32_THREADS, 2) k_fft_cols_w768(ColPass p)
+{
+    using W7 = fftw::W768;
+    extern __shared__ float2 smem[];
+    if (!ctl_active(p.ctl))
+        return;
+    const float2* tw = stage_twiddles(smem, p.tw, W7::TW_COUNT, W32_THREADS);
+    float2* S = smem + W7::TW_COUNT;
+    const int c = threadIdx.x & (W768_COLS - 1), g = threadIdx.x / W768_COLS;
+    const int W = p.width;
+    const int col = blockIdx.x * W768_COLS + c;
+    const bool in_range = col < W;
+    const int b = blockIdx.y;
+    const size_t Ws = static_cast<size_t>(W);
+    const float2* in = p.in + static_cast<size_t>(b) * p.in_frame + col;
+    float2* o = p.out + p.out_map.offset(b) + col;
+    const bool inv_in = p.mode == 1;
+    const bool active_b = g < 24;  // stage B of V24 / stage A of V32
+
+    // V24 forward: samples g + 32 i (i < 24)
+    float2 x[32];
+#pragma unroll
+    for (int i = 0; i < 24; ++i)
+        x[i] = in_range ? in[(static_cast<size_t>(g) + 32 * i) * Ws] : make_float2(0.f, 0.f);
+    if (inv_in)
+    {
+#pragma unroll
+        for (int i = 0; i < 24; ++i)
+            x[i] = cconj(x[i]);
+    }
+    W7::stage_a24(x, tw, g);
+#pragma unroll
+    for (int k1 = 0; k1 < 24; ++k1)
+        S[k1 * W768_COL_PAD + g * W768_COLS + c] = x[k1];
+    __syncthreads();
+    if (active_b)
+    {
+#pragma unroll
+        for (int n2 = 0; n2 < 32; ++n2)
+            x[n2] = S[g * W768_COL_PAD + n2 * W768_COLS + c];
+        fftw::dft32(x);  // X[g + 24 k2], k2 < 32
+    }
+    __syncthreads();
+    const float sc = p.scale;
+    if (p.mode != 2)
+    {
+        if (!active_b || !in_range)
+            return;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2)
+        {
+            float2 v = x[k2];
+            if (inv_in)
+                v = cconj(v);
+            v = cscale(v, sc);
+            float2* d = o + (static_cast<size_t>(g) + 24 * k2) * Ws;
+            if (p.stream_out)
+                __stcs(d, v);
+            else
+                *d = v;
+        }
+        return;
+    }
+    // * G, conjugate, V32 inverse (samples g + 24 i, i < 32, g < 24)
+    if (active_b)
+    {
+        const float2* Gp = p.postmul + col;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2)
+        {
+            const float2 gv = in_range ? __ldg(Gp + (static_cast<size_t>(g) + 24 * k2) * Ws) : make_float2(0.f, 0.f);
+            x[k2] = cconj(cmul(x[k2], gv));
+        }
+        W7::stage_a32(x, tw, g);
+#pragma unroll
+        for (int k1 = 0; k1 < 32; ++k1)
+            S[k1 * W768_COL_PAD + g * W768_COLS + c] = x[k1];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n2 = 0; n2 < 24; ++n2)
+        x[n2] = S[g * W768_COL_PAD + n2 * W768_COLS + c];
+    fftw::dft24(x);  // X[g + 32 k2], k2 < 24
+    if (!in_range)
+        return;
+#pragma unroll
+    for (int k2 = 0; k2 < 24; ++k2)
+        o[(static_cast<size_t>(g) + 32 * k2) * Ws] = cscale(cconj(x[k2]), sc);
+}
+
 // Raw -> complex into ring slots (space transformation NONE).
 __global__ void k_convert(const void* in, int kind, size_t frame_px, int batch, float2* ring, FrameMap map,
                           const CycleCtl* ctl)
@@ -652,6 +810,7 @@ std::mutex g_tw_mu;
 const float2* g_tw_base[kMaxTwDevices] = {};
 int g_tw_offset[8192];  // offset of size N's tables in g_fft_twiddles
 int g_tw_w32_offset[2] = {};  // offsets of the warp engine's tables (N = 512, 1024)
+int g_tw_w768_offset = 0;    // offset of the warp engine's N = 768 tables
 bool g_tw_layout_ready = false;
 std::vector<float2> g_tw_host;
 
@@ -678,6 +837,10 @@ void tw_layout()
     g_tw_host.resize(off + fftw::Warp<512>::TW_COUNT + 1);
     fftw::Warp<512>::twiddle_fill(g_tw_host.data() + off);
     off += fftw::Warp<512>::TW_COUNT;
+    g_tw_w768_offset = off;
+    g_tw_host.resize(off + fftw::W768::TW_COUNT + 1);
+    fftw::W768::twiddle_fill(g_tw_host.data() + off);
+    off += fftw::W768::TW_COUNT;
     g_tw_layout_ready = true;
 }
 
@@ -708,6 +871,12 @@ const float2* twiddles()
 {
     const float2* base = twiddle_base();
     return base ? base + g_tw_offset[N] : nullptr;
+}
+
+const float2* twiddles_w768()
+{
+    const float2* base = twiddle_base();
+    return base ? base + g_tw_w768_offset : nullptr;
 }
 
 template <int N>
@@ -741,7 +910,7 @@ constexpr int col_lanes()
     return f;
 }
 
-std::atomic<int> g_fft_engine{0};  // 0 automatic (warp engine for 512- and 1024-point transforms), 1 tile engine only
+std::atomic<int> g_fft_engine{0};  // 0 automatic (warp engine for 512-, 768- and 1024-point transforms), 1 tile engine only
 
 template <int N>
 hv_status launch_rows_w32(const RowPass& p, int nframes, cudaStream_t st)
@@ -777,9 +946,42 @@ hv_status launch_cols_w32(const ColPass& p, int nframes, cudaStream_t st)
     return HV_OK;
 }
 
+hv_status launch_rows_w768(const RowPass& p, int nframes, cudaStream_t st)
+{
+    HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_rows_w768, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(W768_ROW_SMEM)));
+    RowPass q = p;
+    if ((q.tw = twiddles_w768()) == nullptr)
+        return HV_ERR_CUDA;
+    q.tw_count = fftw::W768::TW_COUNT;
+    dim3 grid((p.rows + W768_ROWS - 1) / W768_ROWS, nframes);
+    k_fft_rows_w768<<<grid, W32_THREADS, W768_ROW_SMEM, st>>>(q);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+hv_status launch_cols_w768(const ColPass& p, int nframes, cudaStream_t st)
+{
+    HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_cols_w768, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(W768_COL_SMEM)));
+    ColPass q = p;
+    if ((q.tw = twiddles_w768()) == nullptr)
+        return HV_ERR_CUDA;
+    q.tw_count = fftw::W768::TW_COUNT;
+    dim3 grid((p.width + W768_COLS - 1) / W768_COLS, nframes);
+    k_fft_cols_w768<<<grid, W32_THREADS, W768_COL_SMEM, st>>>(q);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
 template <int N>
 hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
 {
+    if constexpr (N == 768)
+        if (g_fft_engine.load() == 0)
+            return launch_rows_w768(p, nframes, st);
     if constexpr (N == 512 || N == 1024)
         if (g_fft_engine.load() == 0)
             return launch_rows_w32<N>(p, nframes, st);
@@ -804,6 +1006,9 @@ hv_status launch_rows(const RowPass& p, int nframes, cudaStream_t st)
 template <int N>
 hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
 {
+    if constexpr (N == 768)
+        if (g_fft_engine.load() == 0)
+            return launch_cols_w768(p, nframes, st);
     if constexpr (N == 512 || N == 1024)
         if (g_fft_engine.load() == 0)
             return launch_cols_w32<N>(p, nframes, st);

@@ -1,4 +1,4 @@
-"""512- and 1024-point spatial FFT passes on both engines (hv_fft_engine_mode 0: warp engine,
+"""512-, 768- and 1024-point spatial FFT passes on both engines (hv_fft_engine_mode 0: warp engine,
 1: shared-memory Stockham tiles) against numpy's FP64 FFT and against each other: the 2-D
 transform, the row pass with every input encoding, the lens premultiply, inverse, scale and ring
 slots, the column pass in its three modes (forward, inverse, forward * G * inverse) and frame
@@ -28,7 +28,8 @@ def _c64(rng, shape):
 @pytest.mark.gpu
 @pytest.mark.parametrize("engine", [0, 1], indirect=True)
 @pytest.mark.parametrize("n0,n1", [(1024, 1024), (1024, 768), (768, 1024), (1024, 48), (16, 1024), (1024, 2048),
-                                   (512, 512), (512, 768), (768, 512), (512, 48), (16, 512), (512, 1024)])
+                                   (512, 512), (512, 768), (768, 512), (512, 48), (16, 512), (512, 1024),
+                                   (768, 768), (768, 48), (16, 768), (768, 2048)])
 def test_fft2d_warp_lengths(cuda, engine, n0, n1):
     rng = np.random.default_rng(n0 + 3 * n1)
     B = 2
@@ -52,7 +53,7 @@ def _rows(raw, in_bytes, big_endian, W, H, B, premul, inverse, scale, slot0, nsl
 @pytest.mark.parametrize("dtype,big_endian", [(np.uint8, 0), (np.uint16, 0), (np.uint16, 1), (np.float32, 0),
                                               (np.complex64, 0)])
 @pytest.mark.parametrize("H,use_premul,inverse", [(13, True, 0), (8, False, 1), (40, True, 1)])
-@pytest.mark.parametrize("W", [512, 1024])
+@pytest.mark.parametrize("W", [512, 768, 1024])
 def test_row_pass_engines(cuda, dtype, big_endian, W, H, use_premul, inverse):
     B, nslots, slot0 = 3, 4, 2
     rng = np.random.default_rng(H + int(big_endian))
@@ -85,7 +86,7 @@ def test_row_pass_engines(cuda, dtype, big_endian, W, H, use_premul, inverse):
 @pytest.mark.gpu
 @pytest.mark.parametrize("W", [1024, 48, 96, 16])
 @pytest.mark.parametrize("mode", [0, 1, 2])
-@pytest.mark.parametrize("H", [512, 1024])
+@pytest.mark.parametrize("H", [512, 768, 1024])
 def test_col_pass_engines(cuda, W, H, mode):
     B, nslots, slot0 = 2, 3, 1
     rng = np.random.default_rng(W + 10 * mode)
@@ -117,7 +118,7 @@ def test_col_pass_engines(cuda, W, H, mode):
 @pytest.mark.gpu
 @pytest.mark.parametrize("engine", [0, 1], indirect=True)
 @pytest.mark.parametrize("space", [hv.SPACE_FRESNELTR, hv.SPACE_ANGULARSP])
-@pytest.mark.parametrize("W,H", [(1024, 1024), (512, 512), (1024, 512)])
+@pytest.mark.parametrize("W,H", [(1024, 1024), (512, 512), (1024, 512), (768, 768), (1024, 768)])
 def test_spatial_engines(cuda, engine, space, W, H):
     """The fused spatial stage on u8 frames (1024 x 1024: the Fresnel + PCA workload's frames)."""
     from holovibes_gb300.synthetic import Interferogram
