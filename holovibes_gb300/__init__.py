@@ -228,6 +228,7 @@ def _declare(L: C.CDLL) -> None:
         "hv_pipe_stream": (vp, [vp]),
         "hv_fft_size_supported": (i32, [i32]),
         "hv_fft_engine_mode": (None, [i32]),
+        "hv_fft_status": (st, []),
         "hv_spatial_sub_batch_mb": (None, [i32]),
         "hv_fresnel_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
         "hv_angular_spectrum_lens": (st, [vp, i32, i32, f32, f32, f32, i32, vp]),
@@ -330,7 +331,8 @@ def fft_size_supported(n: int) -> bool:
 
 
 def fft_engine_mode(mode: int) -> None:
-    """Engine of the 1024-point spatial FFT passes: 0 automatic (warp engine), 1 tile engine."""
+    """Engine of the 512/768/1024-point spatial FFT passes: 0 automatic (warp engine, TMA-fed
+    1024-point columns), 1 tile engine, 2 warp engine with register-loading columns."""
     lib().hv_fft_engine_mode(int(mode))
 
 

@@ -55,6 +55,8 @@ int hv_fft_size_supported(int n) { return fft_size_supported(n) ? 1 : 0; }
 
 void hv_fft_engine_mode(int mode) { set_fft_engine(mode); }
 
+hv_status hv_fft_status(void) { return fft_status(); }
+
 void hv_spatial_sub_batch_mb(int mb) { set_spatial_sub_batch_mb(mb); }
 
 hv_status hv_fresnel_lens(void* lens_c64, int width, int height, float lambda, float z, float pixel_size_um,

@@ -714,8 +714,8 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
     float* part = static_cast<float*>(work);
     k_cov_tc<<<p.ctas, TC_THREADS, smem, st>>>(map, T, npix, p.chunks_per_cta, p.N, p.cols, raw, p.packed, part, err);
     HV_LAUNCH_CHECK();
-    const int slices = p.ctas < 16 ? p.ctas : 16;
-    const int per = (p.ctas + slices - 1) / slices;
+    // four partials per thread (independent loads), the slices combined by FP64 atomics
+    const int per = p.ctas < 4 ? p.ctas : 4;
     k_cov_tc_reduce<<<dim3((T * T + 255) / 256, (p.ctas + per - 1) / per), 256, 0, st>>>(part, T, p.ctas, per,
                                                                                        p.packed, cov);
     HV_LAUNCH_CHECK();

@@ -92,6 +92,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
 bool view_tc_supported(int K);
 void set_view_mode(int mode);
 void set_fft_engine(int mode);
+hv_status fft_status();
 void set_spatial_sub_batch_mb(int mb);
 bool view_engine_tc(int K, size_t HW);
 size_t view_tc_workspace(int K, int T);

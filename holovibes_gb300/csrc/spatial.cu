@@ -25,6 +25,7 @@
 
 #include "fft_smem.cuh"
 #include "fft_warp.cuh"
+#include "tc_common.cuh"
 #include "hv_internal.h"
 
 namespace hv {
@@ -625,6 +626,154 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_cols_w32(ColPass p)
     }
 }
 
+// ------------------------------------------------------------------ warp engine, TMA-fed columns
+// Persistent column pass (N = 1024): one CTA per SM walks the tiles blockIdx.x, + gridDim.x, ...
+// (a tile = 8 columns x 1024 rows of one frame, 64 KB). The tile two steps ahead is loaded by TMA
+// (four 256-row boxes) into one of two staging buffers while the current tile is transformed
+// from registers, so the column reads stream without the per-tile load latency of the
+// register-loading kernel. The waits are bounded; a wait that gives up sets g_fft_wait_error,
+// lets the copies already issued land and ends the CTA.
+__device__ int g_fft_wait_error = 0;
+
+constexpr int WT_N = 1024;
+constexpr int WT_COLS = W32Geom<WT_N>::COLS;
+constexpr int WT_TILE = WT_N * WT_COLS;  // float2 per tile
+constexpr size_t WT_SMEM = 1024 + (2 * static_cast<size_t>(WT_TILE) + fftw::Warp<WT_N>::NG * W32Geom<WT_N>::COL_PAD +
+                                   fftw::Warp<WT_N>::TW_COUNT) * sizeof(float2) + 64;
+
+__global__ void __launch_bounds__(W32_THREADS, 1) k_fft_cols_w32_tma(const __grid_constant__ CUtensorMap tmap,
+                                                                       ColPass p, int tiles_x, int ntiles)
+{
+    using Gm = W32Geom<WT_N>;
+    using Wp = fftw::Warp<WT_N>;
+    constexpr int NG = Gm::NG;
+    constexpr int COLS = Gm::COLS;
+    extern __shared__ unsigned char smem_raw[];
+    if (!ctl_active(p.ctl))
+        return;
+    float2* stage = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    float2* S = stage + 2 * WT_TILE;
+    float2* tws = S + NG * Gm::COL_PAD;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tws + Gm::TW);
+    __shared__ int s_abort;
+    volatile int* abort = &s_abort;
+    const int tid = threadIdx.x;
+    if (tid == 0)
+    {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int e = tid; e < Gm::TW; e += W32_THREADS)
+        tws[e] = __ldg(p.tw + e);
+    tc::fence_async_smem();
+    __syncthreads();
+
+    auto issue = [&](int t, int sb) {
+        const int fb = t / tiles_x, tx = t - fb * tiles_x;
+        tc::mbar_arrive_expect_tx(&bar[sb], WT_TILE * sizeof(float2));
+#pragma unroll
+        for (int q = 0; q < WT_N / 256; ++q)
+            tc::tma_load_2d(stage + sb * WT_TILE + q * 256 * COLS, &tmap, tx * COLS * 2, fb * WT_N + q * 256, &bar[sb]);
+    };
+    if (tid == 0)
+    {
+        if (static_cast<int>(blockIdx.x) < ntiles)
+            issue(blockIdx.x, 0);
+        if (static_cast<int>(blockIdx.x + gridDim.x) < ntiles)
+            issue(blockIdx.x + gridDim.x, 1);
+    }
+    const int c = tid % COLS, g = tid / COLS;
+    const int W = p.width;
+    const size_t step = static_cast<size_t>(NG) * W;
+    const bool inv_in = p.mode == 1;
+    const float sc = p.scale;
+    int k = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k)
+    {
+        const int sb = k & 1;
+        // every thread waits; the CTA agrees on the outcome so that all of it leaves together
+        const bool landed = tc::mbar_wait(&bar[sb], static_cast<uint32_t>((k >> 1) & 1), abort);
+        if (!__syncthreads_and(landed))
+        {
+            if (tid == 0)
+                s_abort = 1;
+            break;
+        }
+        float2 x[32];
+        {
+            const float2* src = stage + sb * WT_TILE + g * COLS + c;  // row g + NG j at (g + NG j) * COLS
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                x[j] = src[j * NG * COLS];
+        }
+        __syncthreads();  // stage sb fully read: refill it with the tile two steps ahead
+        if (tid == 0 && t + 2 * static_cast<int>(gridDim.x) < ntiles)
+            issue(t + 2 * gridDim.x, sb);
+        if (inv_in)
+        {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                x[j] = cconj(x[j]);
+        }
+        const int fb = t / tiles_x, tx = t - fb * tiles_x;
+        const int col = tx * COLS + c;
+        const bool in_range = col < W;
+        const size_t e0 = static_cast<size_t>(g) * W + col;
+        Wp::stage_a(x, tws, g);
+        w32_col_exchange<WT_N>(x, S, c, g);
+        fftw::dft32(x);
+        float2* o = p.out + p.out_map.offset(fb) + e0;
+        if (p.mode == 2)
+        {
+            const float2* Gp = p.postmul + e0;
+#pragma unroll
+            for (int k2 = 0; k2 < 32; ++k2)
+            {
+                const float2 gv = in_range ? __ldg(Gp + k2 * step) : make_float2(0.f, 0.f);
+                x[k2] = cconj(cmul(x[k2], gv));
+            }
+            Wp::stage_a(x, tws, g);
+            w32_col_exchange<WT_N>(x, S, c, g);
+            fftw::dft32(x);
+            if (in_range)
+            {
+#pragma unroll
+                for (int k2 = 0; k2 < 32; ++k2)
+                    o[k2 * step] = cscale(cconj(x[k2]), sc);
+            }
+            continue;
+        }
+        if (!in_range)
+            continue;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2)
+        {
+            float2 v = x[k2];
+            if (inv_in)
+                v = cconj(v);
+            v = cscale(v, sc);
+            if (p.stream_out)
+                __stcs(o + k2 * step, v);
+            else
+                o[k2 * step] = v;
+        }
+    }
+    __syncthreads();
+    if (s_abort && tid == 0)
+    {
+        // a wait gave up at step k: let the (at most two) copies still in flight land before the
+        // CTA's shared memory is released (bounded waits without the abort shortcut)
+        const int t = blockIdx.x + k * gridDim.x;
+        if (t < ntiles)
+            tc::mbar_wait(&bar[k & 1], static_cast<uint32_t>((k >> 1) & 1));
+        if (t + static_cast<int>(gridDim.x) < ntiles)
+            tc::mbar_wait(&bar[(k + 1) & 1], static_cast<uint32_t>(((k + 1) >> 1) & 1));
+        atomicExch(&g_fft_wait_error, 1);
+    }
+}
+
 // ------------------------------------------------------------------ warp engine, N = 768
 // Rows: one warp per row (V24: 32 lanes load and run DFT24, lanes 0..23 run the DFT32 and store).
 // Columns: 8 columns per CTA, thread (c, g) = (t & 7, t >> 3); forward = V24 (warps 6-7 idle in
@@ -929,9 +1078,68 @@ hv_status launch_rows_w32(const RowPass& p, int nframes, cudaStream_t st)
     return HV_OK;
 }
 
+std::atomic<int> g_fft_cols_tma{1};  // 1: TMA-fed persistent column pass where it applies
+
+// Persistent TMA-fed column pass for N = 1024; false when it does not apply (the caller then
+// launches the register-loading kernel).
+bool launch_cols_w32_tma(const ColPass& p, int nframes, cudaStream_t st, hv_status* status)
+{
+    // forward / inverse passes only: the AS middle pass (two transforms per tile) is compute-bound
+    // at one CTA of 8 warps per SM and stays on the register-loading kernel (2 CTAs per SM)
+    if (!g_fft_cols_tma.load() || p.mode == 2 || p.in_frame != static_cast<size_t>(p.width) * WT_N ||
+        (p.width % WT_COLS) != 0)
+        return false;
+    CUtensorMap map;
+    if (!tc::encode_tmap_2d_f32(&map, p.in, static_cast<uint64_t>(p.width) * 2, static_cast<uint64_t>(nframes) * WT_N,
+                                static_cast<uint64_t>(p.width) * sizeof(float2), WT_COLS * 2, 256))
+        return false;
+    static const int sms = [] {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 0;
+        return n;
+    }();
+    if (sms <= 0)
+        return false;
+    *status = HV_OK;
+    const cudaError_t e = cudaFuncSetAttribute(k_fft_cols_w32_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(WT_SMEM));
+    if (e != cudaSuccess)
+    {
+        *status = HV_ERR_CUDA;
+        return true;
+    }
+    ColPass q = p;
+    if ((q.tw = twiddles_w32<WT_N>()) == nullptr)
+    {
+        *status = HV_ERR_CUDA;
+        return true;
+    }
+    q.tw_count = fftw::Warp<WT_N>::TW_COUNT;
+    const int tiles_x = p.width / WT_COLS;
+    const int ntiles = tiles_x * nframes;
+    const int grid = ntiles < sms ? ntiles : sms;
+    k_fft_cols_w32_tma<<<grid, W32_THREADS, WT_SMEM, st>>>(map, q, tiles_x, ntiles);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess)
+    {
+        set_last_error_msg(cudaGetErrorString(le));
+        *status = HV_ERR_CUDA;
+        return true;
+    }
+    count_launch();
+    return true;
+}
+
 template <int N>
 hv_status launch_cols_w32(const ColPass& p, int nframes, cudaStream_t st)
 {
+    if constexpr (N == WT_N)
+    {
+        hv_status r;
+        if (launch_cols_w32_tma(p, nframes, st, &r))
+            return r;
+    }
     using Gm = W32Geom<N>;
     HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_cols_w32<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(Gm::COL_SMEM)));
@@ -1032,7 +1240,18 @@ hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
 
 }  // namespace
 
-void set_fft_engine(int mode) { g_fft_engine = mode; }
+void set_fft_engine(int mode)
+{
+    g_fft_engine = mode == 2 ? 0 : mode;
+    g_fft_cols_tma = mode == 2 ? 0 : 1;
+}
+
+hv_status fft_status()
+{
+    int err = 0;
+    HV_CUDA_TRY(cudaMemcpyFromSymbol(&err, g_fft_wait_error, sizeof(int)));
+    return err ? HV_ERR_TIMEOUT : HV_OK;
+}
 
 bool fft_size_supported(int n)
 {

@@ -232,10 +232,15 @@ void* hv_pipe_stream(hv_pipe* p);
 
 /* Supported transform lengths for the shared-memory FFT (each of width and height). */
 int hv_fft_size_supported(int n);
-/* Engine of the 1024-point spatial FFT passes (process-wide, read at every launch): 0 = automatic
- * (32 x 32 warp engine: 32 samples per thread, one transpose), 1 = the shared-memory Stockham tile
- * engine used for every other length. Both compute the same transform to FP32 round-off. */
+/* Engine of the 512-, 768- and 1024-point spatial FFT passes (process-wide, read at every launch):
+ * 0 = automatic (warp engine: 32 samples per thread, one transpose; the 1024-point column pass
+ * persistent and fed by TMA), 1 = the shared-memory Stockham tile engine used for every other
+ * length, 2 = the warp engine with register-loading column passes only. All compute the same
+ * transform to FP32 round-off (0 and 2 bit-identically). */
 void hv_fft_engine_mode(int mode);
+/* HV_ERR_TIMEOUT when a bounded wait of a TMA-fed FFT pass gave up since the library was loaded
+ * (its CTA stopped early; the pass's output is incomplete), HV_OK otherwise. Synchronous. */
+hv_status hv_fft_status(void);
 /* Batching of the spatial stage's passes (process-wide, read at every call): 0 = one launch per
  * pass over the whole batch (default: the fewest partial waves), n > 0 = sub-batches whose complex
  * intermediate fits in n MB (kept in L2 between the passes). Results are identical either way. */

@@ -101,7 +101,7 @@ def test_col_pass_engines(cuda, W, H, mode):
         ref = np.conj(np.fft.fft(np.conj(np.fft.fft(xr, axis=-2) * G.astype(np.complex128)[None]), axis=-2))
     ref = ref * 0.25
     got = {}
-    for eng in (0, 1):
+    for eng in (0, 1, 2):
         hv.fft_engine_mode(eng)
         try:
             out = zeros(nslots * H * W * 8)
@@ -113,6 +113,10 @@ def test_col_pass_engines(cuda, W, H, mode):
         for b in range(B):
             assert rel_l2(got[eng][(slot0 + b) % nslots], ref[b]) <= 1e-5, (eng, b)
     assert rel_l2(got[0], got[1]) <= 2e-6
+    # the TMA-fed persistent column pass (engine 0 at H = 1024) and the register-loading one
+    # (engine 2) run the same arithmetic
+    assert np.array_equal(got[0], got[2])
+    assert hv.lib().hv_fft_status() == hv.HV_OK
 
 
 @pytest.mark.gpu
