@@ -332,7 +332,7 @@ def fft_size_supported(n: int) -> bool:
 
 def fft_engine_mode(mode: int) -> None:
     """Engine of the 512/768/1024-point spatial FFT passes: 0 automatic (warp engine, TMA-fed
-    1024-point columns), 1 tile engine, 2 warp engine with register-loading columns."""
+    1024-point passes), 1 tile engine, 2 warp engine with register-loading passes only."""
     lib().hv_fft_engine_mode(int(mode))
 
 

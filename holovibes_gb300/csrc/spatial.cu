@@ -774,6 +774,151 @@ __global__ void __launch_bounds__(W32_THREADS, 1) k_fft_cols_w32_tma(const __gri
     }
 }
 
+// Persistent row pass (N = 1024, 8-/16-bit camera input, optional premultiply): tile = 8 rows of
+// one frame (one row per warp), two CTAs per SM, CTA i takes the contiguous tile range
+// [i per, (i + 1) per) (row block major, frame minor). The raw rows of the tile two steps ahead
+// (8 or 16 KB) are loaded by TMA during the current tile; the lens rows come from L2 with their
+// loads issued before the staged pixels are used. Bounded waits as in k_fft_cols_w32_tma.
+// (Staging the lens rows in shared memory as well, one CTA per SM, measured slower.)
+constexpr int RT_ROWS = 8;
+constexpr size_t RT_RAW_MAX = static_cast<size_t>(RT_ROWS) * WT_N * 2;  // 16-bit input
+constexpr int RT_XBUF = W32Geom<WT_N>::ROW_BUF;                          // per warp (32 x 33)
+constexpr size_t RT_SMEM =
+    1024 + 2 * RT_RAW_MAX + (static_cast<size_t>(W32_WARPS) * RT_XBUF + fftw::Warp<WT_N>::TW_COUNT) * sizeof(float2) + 64;
+
+template <int ESIZE>
+__global__ void __launch_bounds__(W32_THREADS, 2) k_fft_rows_w32_tma(const __grid_constant__ CUtensorMap raw_map,
+                                                                       RowPass p, int nframes, int ntiles, int per)
+{
+    using Wp = fftw::Warp<WT_N>;
+    extern __shared__ unsigned char smem_raw[];
+    if (!ctl_active(p.ctl))
+        return;
+    unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char* raw_st = base;  // 2 x RT_RAW_MAX
+    float2* xbuf = reinterpret_cast<float2*>(base + 2 * RT_RAW_MAX);
+    float2* tws = xbuf + W32_WARPS * RT_XBUF;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tws + Wp::TW_COUNT);
+    __shared__ int s_abort;
+    volatile int* abort = &s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0)
+    {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int e = tid; e < Wp::TW_COUNT; e += W32_THREADS)
+        tws[e] = __ldg(p.tw + e);
+    tc::fence_async_smem();
+    __syncthreads();
+
+    const int t0 = blockIdx.x * per;
+    const int t1 = min(t0 + per, ntiles);
+    constexpr uint32_t RAW_TILE = RT_ROWS * WT_N * ESIZE;
+    auto issue_raw = [&](int t, int sb) {
+        const int rb = t / nframes, f = t - rb * nframes;
+        tc::mbar_arrive_expect_tx(&bar[sb], RAW_TILE);
+#pragma unroll
+        for (int q = 0; q < WT_N / 256; ++q)
+            tc::tma_load_2d(raw_st + sb * RT_RAW_MAX + q * RT_ROWS * 256 * ESIZE, &raw_map, q * 256,
+                            f * p.rows + rb * RT_ROWS, &bar[sb]);
+    };
+    if (tid == 0 && t0 < t1)
+    {
+        issue_raw(t0, 0);
+        if (t0 + 1 < t1)
+            issue_raw(t0 + 1, 1);
+    }
+    const bool inv = p.inverse != 0;
+    const bool swap = ESIZE == 2 && p.in_kind == IN_U16_BE;
+    const float sc = p.scale;
+    int k = 0;
+    for (int t = t0; t < t1; ++t, ++k)
+    {
+        const int sb = k & 1;
+        const int rb = t / nframes, f = t - rb * nframes;
+        const size_t row = static_cast<size_t>(rb * RT_ROWS + warp) * WT_N + lane;
+        float2 x[32];
+        if (p.premul)
+        {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                x[j] = __ldg(p.premul + row + 32 * j);
+        }
+        const bool landed = tc::mbar_wait(&bar[sb], static_cast<uint32_t>((k >> 1) & 1), abort);
+        if (!__syncthreads_and(landed))
+        {
+            if (tid == 0)
+                s_abort = 1;
+            break;
+        }
+        // sample n = lane + 32 j of row `warp`: box j / 8 at (warp * 256 + lane + 32 (j % 8))
+        {
+            const unsigned char* rs = raw_st + sb * RT_RAW_MAX;
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+            {
+                const int off = (j >> 3) * RT_ROWS * 256 + warp * 256 + lane + 32 * (j & 7);
+                float v;
+                if constexpr (ESIZE == 1)
+                    v = static_cast<float>(rs[off]) * 257.0f;
+                else
+                {
+                    uint16_t u = reinterpret_cast<const uint16_t*>(rs)[off];
+                    if (swap)
+                        u = static_cast<uint16_t>((u << 8) | (u >> 8));
+                    v = static_cast<float>(u);
+                }
+                x[j] = p.premul ? make_float2(v * x[j].x, v * x[j].y) : make_float2(v, 0.f);
+                if (inv)
+                    x[j] = cconj(x[j]);
+            }
+        }
+        __syncthreads();  // raw stage sb fully read: refill it with the tile two steps ahead
+        if (tid == 0 && t + 2 < t1)
+            issue_raw(t + 2, sb);
+
+        Wp::stage_a(x, tws, lane);
+        float2* buf = xbuf + warp * RT_XBUF;
+#pragma unroll
+        for (int e = 0; e < 32; ++e)
+            buf[lane * W32Geom<WT_N>::ROW_PAD + e] = x[e];
+        __syncwarp();
+#pragma unroll
+        for (int n2 = 0; n2 < 32; ++n2)
+            x[n2] = buf[n2 * W32Geom<WT_N>::ROW_PAD + lane];
+        __syncwarp();  // the block is rewritten by the next tile
+        fftw::dft32(x);
+
+        float2* o = p.out + p.out_map.offset(f) + row;
+#pragma unroll
+        for (int k2 = 0; k2 < 32; ++k2)
+        {
+            float2 v = x[k2];
+            if (inv)
+                v = cconj(v);
+            v = cscale(v, sc);
+            if (p.stream_out)
+                __stcs(o + 32 * k2, v);
+            else
+                o[32 * k2] = v;
+        }
+    }
+    __syncthreads();
+    if (s_abort && tid == 0)
+    {
+        // copies still in flight at the failed step k land before the shared memory is released
+        const int t = t0 + k;
+        if (t < t1)
+            tc::mbar_wait(&bar[k & 1], static_cast<uint32_t>((k >> 1) & 1));
+        if (t + 1 < t1)
+            tc::mbar_wait(&bar[(k + 1) & 1], static_cast<uint32_t>(((k + 1) >> 1) & 1));
+        atomicExch(&g_fft_wait_error, 1);
+    }
+}
+
 // ------------------------------------------------------------------ warp engine, N = 768
 // Rows: one warp per row (V24: 32 lanes load and run DFT24, lanes 0..23 run the DFT32 and store).
 // Columns: 8 columns per CTA, thread (c, g) = (t & 7, t >> 3); forward = V24 (warps 6-7 idle in
@@ -1061,9 +1206,80 @@ constexpr int col_lanes()
 
 std::atomic<int> g_fft_engine{0};  // 0 automatic (warp engine for 512-, 768- and 1024-point transforms), 1 tile engine only
 
+std::atomic<int> g_fft_tma{1};  // 1: TMA-fed persistent row / column passes where they apply
+
+int device_sms()
+{
+    static const int sms = [] {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 0;
+        return n;
+    }();
+    return sms;
+}
+
+// Persistent TMA-fed row pass for N = 1024 (8-/16-bit input outside served cycles); false when it
+// does not apply (the caller then launches the register-loading kernel).
+bool launch_rows_w32_tma(const RowPass& p, int nframes, cudaStream_t st, hv_status* status)
+{
+    const int esize = p.in_kind == IN_U8 ? 1 : (p.in_kind == IN_U16 || p.in_kind == IN_U16_BE) ? 2 : 0;
+    if (!g_fft_tma.load() || esize == 0 || p.raw_from_ctl || (p.rows % RT_ROWS) != 0 ||
+        p.in_frame != static_cast<size_t>(p.rows) * WT_N)
+        return false;
+    const int sms = device_sms();
+    if (sms <= 0)
+        return false;
+    CUtensorMap raw_map;
+    if (!tc::encode_tmap_2d(&raw_map, esize == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16,
+                            p.in, WT_N, static_cast<uint64_t>(nframes) * p.rows, static_cast<uint64_t>(WT_N) * esize,
+                            256, RT_ROWS))
+        return false;
+    *status = HV_OK;
+    const int ntiles = (p.rows / RT_ROWS) * nframes;
+    const int per = (ntiles + 2 * sms - 1) / (2 * sms);  // two CTAs per SM
+    const int grid = (ntiles + per - 1) / per;
+    RowPass q = p;
+    if ((q.tw = twiddles_w32<WT_N>()) == nullptr)
+    {
+        *status = HV_ERR_CUDA;
+        return true;
+    }
+    q.tw_count = fftw::Warp<WT_N>::TW_COUNT;
+    cudaError_t e;
+    if (esize == 1)
+    {
+        e = cudaFuncSetAttribute(k_fft_rows_w32_tma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RT_SMEM));
+        if (e == cudaSuccess)
+            k_fft_rows_w32_tma<1><<<grid, W32_THREADS, RT_SMEM, st>>>(raw_map, q, nframes, ntiles, per);
+    }
+    else
+    {
+        e = cudaFuncSetAttribute(k_fft_rows_w32_tma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RT_SMEM));
+        if (e == cudaSuccess)
+            k_fft_rows_w32_tma<2><<<grid, W32_THREADS, RT_SMEM, st>>>(raw_map, q, nframes, ntiles, per);
+    }
+    if (e == cudaSuccess)
+        e = cudaGetLastError();
+    if (e != cudaSuccess)
+    {
+        set_last_error_msg(cudaGetErrorString(e));
+        *status = HV_ERR_CUDA;
+        return true;
+    }
+    count_launch();
+    return true;
+}
+
 template <int N>
 hv_status launch_rows_w32(const RowPass& p, int nframes, cudaStream_t st)
 {
+    if constexpr (N == WT_N)
+    {
+        hv_status r;
+        if (launch_rows_w32_tma(p, nframes, st, &r))
+            return r;
+    }
     using Gm = W32Geom<N>;
     HV_CUDA_TRY(cudaFuncSetAttribute(k_fft_rows_w32<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(Gm::ROW_SMEM)));
@@ -1078,27 +1294,20 @@ hv_status launch_rows_w32(const RowPass& p, int nframes, cudaStream_t st)
     return HV_OK;
 }
 
-std::atomic<int> g_fft_cols_tma{1};  // 1: TMA-fed persistent column pass where it applies
-
 // Persistent TMA-fed column pass for N = 1024; false when it does not apply (the caller then
 // launches the register-loading kernel).
 bool launch_cols_w32_tma(const ColPass& p, int nframes, cudaStream_t st, hv_status* status)
 {
     // forward / inverse passes only: the AS middle pass (two transforms per tile) is compute-bound
     // at one CTA of 8 warps per SM and stays on the register-loading kernel (2 CTAs per SM)
-    if (!g_fft_cols_tma.load() || p.mode == 2 || p.in_frame != static_cast<size_t>(p.width) * WT_N ||
+    if (!g_fft_tma.load() || p.mode == 2 || p.in_frame != static_cast<size_t>(p.width) * WT_N ||
         (p.width % WT_COLS) != 0)
         return false;
     CUtensorMap map;
     if (!tc::encode_tmap_2d_f32(&map, p.in, static_cast<uint64_t>(p.width) * 2, static_cast<uint64_t>(nframes) * WT_N,
                                 static_cast<uint64_t>(p.width) * sizeof(float2), WT_COLS * 2, 256))
         return false;
-    static const int sms = [] {
-        int dev = 0, n = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            return 0;
-        return n;
-    }();
+    const int sms = device_sms();
     if (sms <= 0)
         return false;
     *status = HV_OK;
@@ -1243,7 +1452,7 @@ hv_status launch_cols(const ColPass& p, int nframes, cudaStream_t st)
 void set_fft_engine(int mode)
 {
     g_fft_engine = mode == 2 ? 0 : mode;
-    g_fft_cols_tma = mode == 2 ? 0 : 1;
+    g_fft_tma = mode == 2 ? 0 : 1;
 }
 
 hv_status fft_status()

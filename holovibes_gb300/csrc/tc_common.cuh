@@ -194,11 +194,11 @@ __device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t&
     lo = *reinterpret_cast<const uint32_t*>(&l2);
 }
 
-// Host: encodes the tensor map of a row-major FP32 matrix (`rows` rows of `cols` floats, row pitch
-// `pitch_bytes`, a multiple of 16) for TMA boxes of box_rows x box_cols, no swizzle, zero fill
-// out of range. The driver entry point is resolved once through the runtime.
-inline bool encode_tmap_2d_f32(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows, uint64_t pitch_bytes,
-                               uint32_t box_cols, uint32_t box_rows)
+// Host: encodes the tensor map of a row-major matrix of `dtype` elements (`rows` rows of `cols`
+// elements, row pitch `pitch_bytes`, a multiple of 16) for TMA boxes of box_rows x box_cols, no
+// swizzle, zero fill out of range. The driver entry point is resolved once through the runtime.
+inline bool encode_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, uint64_t cols, uint64_t rows,
+                           uint64_t pitch_bytes, uint32_t box_cols, uint32_t box_rows)
 {
     static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
         void* p = nullptr;
@@ -214,9 +214,15 @@ inline bool encode_tmap_2d_f32(CUtensorMap* map, const void* base, uint64_t cols
     const cuuint64_t strides[1] = {pitch_bytes};
     const cuuint32_t box[2] = {box_cols, box_rows};
     const cuuint32_t estr[2] = {1, 1};
-    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+    return fn(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+inline bool encode_tmap_2d_f32(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows, uint64_t pitch_bytes,
+                               uint32_t box_cols, uint32_t box_rows)
+{
+    return encode_tmap_2d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, base, cols, rows, pitch_bytes, box_cols, box_rows);
 }
 
 }  // namespace tc

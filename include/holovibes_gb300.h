@@ -233,10 +233,11 @@ void* hv_pipe_stream(hv_pipe* p);
 /* Supported transform lengths for the shared-memory FFT (each of width and height). */
 int hv_fft_size_supported(int n);
 /* Engine of the 512-, 768- and 1024-point spatial FFT passes (process-wide, read at every launch):
- * 0 = automatic (warp engine: 32 samples per thread, one transpose; the 1024-point column pass
- * persistent and fed by TMA), 1 = the shared-memory Stockham tile engine used for every other
- * length, 2 = the warp engine with register-loading column passes only. All compute the same
- * transform to FP32 round-off (0 and 2 bit-identically). */
+ * 0 = automatic (warp engine: 32 samples per thread, one transpose; the 1024-point forward /
+ * inverse column passes and the 1024-point row passes of 8-/16-bit camera frames persistent and
+ * fed by TMA), 1 = the shared-memory Stockham tile engine used for every other length, 2 = the
+ * warp engine with register-loading passes only. All compute the same transform to FP32
+ * round-off (0 and 2 bit-identically). */
 void hv_fft_engine_mode(int mode);
 /* HV_ERR_TIMEOUT when a bounded wait of a TMA-fed FFT pass gave up since the library was loaded
  * (its CTA stopped early; the pass's output is incomplete), HV_OK otherwise. Synchronous. */

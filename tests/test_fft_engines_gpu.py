@@ -70,7 +70,7 @@ def test_row_pass_engines(cuda, dtype, big_endian, W, H, use_premul, inverse):
         x = x * premul.astype(np.complex128)[None]
     ref = (np.conj(np.fft.fft(np.conj(x), axis=-1)) if inverse else np.fft.fft(x, axis=-1)) * 0.5
     got = {}
-    for mode in (0, 1):
+    for mode in (0, 1, 2):
         hv.fft_engine_mode(mode)
         try:
             got[mode] = _rows(raw_in, np.dtype(dtype).itemsize, big_endian, W, H, B, premul, inverse, 0.5, slot0,
@@ -81,6 +81,10 @@ def test_row_pass_engines(cuda, dtype, big_endian, W, H, use_premul, inverse):
             assert rel_l2(got[mode][(slot0 + b) % nslots], ref[b]) <= 1e-5, (mode, b)
         assert np.all(got[mode][1] == 0)  # untouched slot
     assert rel_l2(got[0], got[1]) <= 2e-6
+    # engine 0 feeds 1024-point rows of 8-/16-bit pixels (8 | H) through the persistent TMA kernel,
+    # engine 2 through the register-loading one: the same arithmetic
+    assert np.array_equal(got[0], got[2])
+    assert hv.lib().hv_fft_status() == hv.HV_OK
 
 
 @pytest.mark.gpu
