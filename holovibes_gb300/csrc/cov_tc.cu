@@ -10,11 +10,11 @@
 // three BF16 MMAs with FP32 accumulation per K step recover ~16-bit-mantissa accuracy.
 //
 // Kernel: one CTA per SM walks a contiguous range of 64-pixel chunks (K slices of Y):
-//   warp 9     loader: one 2-D tensor copy (TMA) per pair of chunks (T x 128 complex samples, rows
+//   warp 17    loader: one 2-D tensor copy (TMA) per pair of chunks (T x 128 complex samples, rows
 //              of 1 KB) into a ring of R raw stages (zero fill past the frame)
-//   warps 0-7  converters: raw samples -> Yh / Yl tiles of an A stage (128-byte-swizzled K-major,
+//   warps 0-15 converters: raw samples -> Yh / Yl tiles of an A stage (128-byte-swizzled K-major,
 //              rows >= 2T stay zero), each warp releasing its part of the raw and A stages
-//   warp 8     MMA issuer (M = 128 rows of Y, N = 2T rounded to 16, K = 16) into three TMEM
+//   warp 16    MMA issuer (M = 128 rows of Y, N = 2T rounded to 16, K = 16) into three TMEM
 //              accumulators (Yh Yh^T, Yh Yl^T, Yl Yh^T: independent chains, summed by the
 //              epilogue), tcgen05.commit frees the A stage; after the last chunk a commit to
 //              `done` releases the epilogue (warps 0-3 read the accumulator lanes 32w..32w+31)
@@ -30,9 +30,9 @@ namespace hv {
 
 namespace {
 
-constexpr int TC_CONVERTERS = 256;              // warps 0-7
-constexpr int TC_MMA_WARP = TC_CONVERTERS / 32;  // warp 8 issues the MMAs
-constexpr int TC_LOAD_WARP = TC_MMA_WARP + 1;    // warp 9 issues the tensor copies
+constexpr int TC_CONVERTERS = 512;              // warps 0-15
+constexpr int TC_MMA_WARP = TC_CONVERTERS / 32;  // warp 16 issues the MMAs
+constexpr int TC_LOAD_WARP = TC_MMA_WARP + 1;    // warp 17 issues the tensor copies
 constexpr int TC_THREADS = TC_CONVERTERS + 64;
 constexpr int TC_A_STAGES = 2;
 constexpr int TC_A_STAGES_PACKED = 4;
