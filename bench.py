@@ -271,11 +271,13 @@ def steps_for(hv, fd, s, dev_batch, stream):
     view = buf(HW * 4)
     tc_ws = L.hv_time_view_tc_workspace(K, T)
     if K >= 8 and tc_ws and HW % 2 == 0:
-        # the pipe's automatic engine for K >= 8 bins: tcgen05 (the call also re-splits the weights)
+        # the pipe's automatic engine for K >= 8 bins: tcgen05; the weights are split once (as the
+        # pipe does per settings refresh) and only the contraction kernel is timed
         vw = buf(tc_ws)
-        out.append(("time_view_tc", lambda: L.hv_time_view_tc(ring.data_ptr(), T, W, H, wts.data_ptr(), K,
-                                                              s.image_type, 1.0, s.fft_shift, view.data_ptr(), None,
-                                                              vw.data_ptr(), stream), T * HW * 8 + HW * 4))
+        hv.check(L.hv_time_view_tc_prepare(wts.data_ptr(), K, T, vw.data_ptr(), stream), "view_tc prepare")
+        out.append(("time_view_tc", lambda: L.hv_time_view_tc_run(ring.data_ptr(), T, W, H, K, s.image_type, 1.0,
+                                                                  s.fft_shift, view.data_ptr(), None, vw.data_ptr(),
+                                                                  stream), T * HW * 8 + HW * 4))
     else:
         out.append(("time_view", lambda: L.hv_time_view(ring.data_ptr(), T, W, H, wts.data_ptr(), K, s.image_type,
                                                         1.0, s.fft_shift, view.data_ptr(), None, stream),

@@ -247,6 +247,23 @@ hv_status hv_time_view_tc(const void* ring_c64, int T, int width, int height, co
                    partials_f64, work, S(stream));
 }
 
+hv_status hv_time_view_tc_prepare(const void* weights_c64, int K, int T, void* work, void* stream)
+{
+    if (!weights_c64 || !work || T <= 0)
+        return HV_INVALID_VALUE;
+    return view_tc_prepare(static_cast<const float2*>(weights_c64), K, T, work, S(stream));
+}
+
+hv_status hv_time_view_tc_run(const void* ring_c64, int T, int width, int height, int K, int img_type, float scale,
+                              int shift, float* out_f32, double* partials_f64, void* work, void* stream)
+{
+    if (!ring_c64 || !out_f32 || !work || img_type < 0 || img_type > HV_IMG_ARGUMENT || T <= 0 || width <= 0 ||
+        height <= 0)
+        return HV_INVALID_VALUE;
+    return view_tc(static_cast<const float2*>(ring_c64), T, width, height, K, img_type, scale, shift, out_f32,
+                   partials_f64, work, S(stream));
+}
+
 hv_status hv_time_view_tc_status(const void* work)
 {
     if (!work)

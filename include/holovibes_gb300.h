@@ -320,6 +320,13 @@ hv_status hv_time_view_tc(const void* ring_c64, int T, int width, int height, co
                           int img_type, float scale, int shift, float* out_f32, double* partials_f64, void* work,
                           void* stream);
 size_t hv_time_view_tc_workspace(int K, int T);
+/* The two halves of hv_time_view_tc, for weights that stay fixed over many windows (the pipe's
+ * use: once per settings refresh, like hv_stft_weights): _prepare splits the K x T weights into
+ * the BF16 operand image in `work`; _run then contracts a ring with the prepared image (same
+ * arguments and checks as hv_time_view_tc, without the weights). */
+hv_status hv_time_view_tc_prepare(const void* weights_c64, int K, int T, void* work, void* stream);
+hv_status hv_time_view_tc_run(const void* ring_c64, int T, int width, int height, int K, int img_type, float scale,
+                              int shift, float* out_f32, double* partials_f64, void* work, void* stream);
 /* Engine of the pipe's time view (process-wide, read when a pipe is built): 0 = automatic (tensor
  * cores for 8 <= K <= 64 selected bins, FP32 SIMT otherwise), 1 = SIMT, 2 = tensor cores wherever
  * hv_time_view_tc supports the shape. */

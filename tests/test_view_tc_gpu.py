@@ -116,3 +116,23 @@ def test_view_tc_rejects(cuda):
     st = hv.lib().hv_time_view_tc(ptr(dev(_ring(T, 7, 7, 1))), T, 7, 7, ptr(w), 8, 0, 1.0, 0, ptr(out), None,
                                   ptr(work), None)
     assert st == hv.HV_ERR_UNSUPPORTED
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("T,pmin,pmax,img", [(32, 3, 13, hv.IMG_MODULUS), (256, 100, 132, hv.IMG_ARGUMENT)])
+def test_prepare_then_run_matches_one_call(cuda, T, pmin, pmax, img):
+    """hv_time_view_tc_prepare once + hv_time_view_tc_run per window gives exactly what
+    hv_time_view_tc gives (the run reuses the prepared operand image, here for two rings)."""
+    H, W = 24, 40
+    K = pmax - pmin + 1
+    w = empty(K * T * 8)
+    call("hv_stft_weights", ptr(w), T, pmin, pmax, None)
+    work = empty(hv.lib().hv_time_view_tc_workspace(K, T))
+    call("hv_time_view_tc_prepare", ptr(w), K, T, ptr(work), None)
+    for seed in (1, 2):
+        ring_d = dev(_ring(T, H, W, seed))
+        one, _ = _run_tc(ring_d, T, W, H, w, K, img)
+        out = empty(H * W * 4)
+        call("hv_time_view_tc_run", ptr(ring_d), T, W, H, K, img, 1.0, 0, ptr(out), None, ptr(work), None)
+        assert np.array_equal(host(out, np.float32, (H, W)), one)
+    assert hv.lib().hv_time_view_tc_status(ptr(work)) == hv.HV_OK
