@@ -243,6 +243,11 @@ def steps_for(hv, fd, s, dev_batch, stream):
     HW = W * H
     buf = lambda n: torch.empty(max(int(n), 16), dtype=torch.uint8, device="cuda")
     lens, work, ring = buf(HW * 8), buf(B * HW * 8), buf(T * HW * 8)
+    # the FFT timings below fill only B of the T ring frames: start from finite sample values so
+    # that no kernel reads uninitialised memory
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    ring.view(torch.float32).normal_(0.0, 1000.0, generator=gen)
+    work.view(torch.float32).normal_(0.0, 1000.0, generator=gen)
     if s.space_transformation == hv.SPACE_FRESNELTR:
         L.hv_fresnel_lens(lens.data_ptr(), W, H, s.lambda_, s.z_distance, s.pixel_size, s.lens_mode, stream)
     else:
@@ -258,9 +263,13 @@ def steps_for(hv, fd, s, dev_batch, stream):
     elif s.space_transformation == hv.SPACE_ANGULARSP:
         out.append(("fft_rows(convert)", lambda: L.hv_fft_rows(raw, fd.depth, 0, work.data_ptr(), W, H, B, None, 0,
                                                                1.0, 0, B, stream), B * HW * (fd.depth + 8)))
-        out.append(("fft_cols(fwd*G,inv)", lambda: L.hv_fft_cols(work.data_ptr(), work.data_ptr(), W, H, B,
+        # out of place (the pipe runs it in place): repeated in-place launches would scale the
+        # unnormalised forward * G * inverse by H W per launch into Inf / NaN, and the views'
+        # atan2 is slower on non-finite and all-zero samples than on image data
+        work2 = buf(B * HW * 8)
+        out.append(("fft_cols(fwd*G,inv)", lambda: L.hv_fft_cols(work.data_ptr(), work2.data_ptr(), W, H, B,
                                                                  lens.data_ptr(), 2, 1.0, 0, B, stream), B * HW * 16))
-        out.append(("fft_rows(inv->ring)", lambda: L.hv_fft_rows(work.data_ptr(), 8, 0, ring.data_ptr(), W, H, B,
+        out.append(("fft_rows(inv->ring)", lambda: L.hv_fft_rows(work2.data_ptr(), 8, 0, ring.data_ptr(), W, H, B,
                                                                  None, 1, 1.0 / HW, 0, T, stream), B * HW * 16))
     pmin = s.p_start
     pmax = min(s.p_start + s.p_width, T) if s.p_width else s.p_start
@@ -296,6 +305,7 @@ NCU_TRAFFIC = {
     ("cfg0", "fft_cols(fwd*G,inv)"): 35683840 + 0,
     ("cfg1", "fft_cols(->ring)"): 268523520 + 214097664,
     ("cfg2", "time_view_tc"): 1208223232 + 5527808,
+    ("cfg2", "fft_cols(fwd*G,inv)"): 307309312 + 245959936,
 }
 
 
