@@ -16,7 +16,10 @@
 //   column pass: forward column FFT (+ transfer function G, inverse column FFT for AS)
 //   row pass   : inverse row FFT * 1/(H*W) (AS only)
 // and the last pass writes straight into the time-ring slots, so the reference's separate
-// mask, divide and ring-copy passes disappear.
+// mask, divide and ring-copy passes disappear. Passes of 512, 768 and 1024 points use the warp
+// engine (fft_warp.cuh: 32 samples per thread, one transpose; the 1024-point passes persistent and
+// fed by TMA where they apply), every other length the shared-memory Stockham tile engine
+// (fft_smem.cuh).
 #include <math.h>
 
 #include <atomic>
