@@ -26,6 +26,26 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
+def test_every_declared_function_has_a_python_signature():
+    """The ctypes binding sets restype / argtypes for every function of the header (an untyped
+    call would pass 64-bit pointers and sizes as C ints); the argument count matches the
+    declaration's."""
+    L = hv.lib()
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    untyped, wrong_count = [], []
+    for name in declared_functions():
+        fn = getattr(L, name)
+        if fn.argtypes is None:
+            untyped.append(name)
+            continue
+        m = re.search(r"\b" + name + r"\s*\(([^)]*)\)", text)
+        params = [a for a in m.group(1).split(",") if a.strip() and a.strip() != "void"]
+        if len(params) != len(fn.argtypes):
+            wrong_count.append((name, len(params), len(fn.argtypes)))
+    assert not untyped, untyped
+    assert not wrong_count, wrong_count
+
+
 def test_version_and_defaults():
     assert "sm_103a" in hv.version()
     s = hv.Settings.defaults()
