@@ -302,7 +302,7 @@ def steps_for(hv, fd, s, dev_batch, stream):
 # captures of the same launch summarised in profiles/ (k_fft_cols_w32_tma_1024x1024.md,
 # launches_cfg2_768x768_u16_as_stft_T256_K33.md, launches_cfg0_512x512_u16_as_stft_T16.md)
 NCU_TRAFFIC = {
-    ("cfg0", "fft_cols(fwd*G,inv)"): 35683840 + 0,
+    ("cfg0", "fft_cols(fwd*G,inv)"): 35712256 + 1280,
     ("cfg1", "fft_cols(->ring)"): 268523520 + 214097664,
     ("cfg2", "time_view_tc"): 1208223232 + 5527808,
     ("cfg2", "fft_cols(fwd*G,inv)"): 307309312 + 245959936,
