@@ -10,14 +10,24 @@ ring + time transform + view + render + uint16). Prints ONE JSON line (rank 0):
   e2e        the same through the public API from pinned host memory: every step copies its
              raw batch host->device and reads its uint16 hologram device->host
   latency_ms p50 / p99 frame-to-hologram latency of the e2e steps (push start -> output on host)
-  roofline   dominant kernel: algorithmic bytes / CUDA-event duration vs MEASURED_PEAKS.json
-  cpu_baseline the FP64 numpy oracle (the reference has no CPU path) on a bounded sample
+  roofline   the slowest hot kernel timed alone with CUDA events on its stream: algorithmic bytes
+             (and tensor-core flops where it contracts) per launch over its duration, against
+             MEASURED_PEAKS.json; `bound` is the roof it is closer to
+  cpu_baseline the FP64 numpy oracle (and its FP32 twin) on a bounded sample of the workload; the
+             same leg reports `parity`: the GPU Pipe's output on the sampled window against it
+  serving    (default run) the served engine against plain pipes on 512x512 STFT-32 streams
+  clocks     NVML SM clock and clock-event reasons sampled every 10 ms over the whole run
+`--impl reference` times the CPU restatement of the path (the reference has no CPU
+implementation; its own GPU build is timed beside it in `reference_gpu_build`).
 The path does not shard (one stream per GPU): N GPUs run N independent replicas ("replicas only").
 """
 
 from __future__ import annotations
 
 import argparse
+import ctypes
+import hashlib
+import importlib.util
 import json
 import os
 import subprocess
@@ -32,6 +42,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 DEFAULT_WORKLOAD = "cfg1"
+SPACE_NAMES = {0: "NONE", 1: "FRESNELTR", 2: "ANGULARSP"}
+TIME_NAMES = {0: "NONE", 1: "STFT", 2: "PCA", 3: "SSA_STFT"}
+IMG_NAMES = {0: "MODULUS", 1: "SQUARED_MODULUS", 2: "ARGUMENT"}
 
 
 def parse():
@@ -42,6 +55,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving comparison of the default run")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--server-mode", default="stream", choices=["bucket", "stream", "eager"],
                     help="serving workloads: one CUDA graph per stream on its own CUDA stream (default), one "
@@ -70,58 +84,123 @@ def replica_throughput(ms_local: float, frames_per_rank: int, world: int, device
     return ms, frames_per_rank * world / (ms * 1e-3)
 
 
+def load_synthetic():
+    """holovibes_gb300/synthetic.py loaded on its own (plain numpy): the generator and the workload
+    table, without importing the package, so the CPU arm never maps the product library."""
+    name = "_hv_synthetic_standalone"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, ROOT / "holovibes_gb300" / "synthetic.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def load_oracle():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import holovibes_oracle as O
+
+    return O
+
+
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
+    """SM clock, maximum SM clock and clock-event reasons of one GPU, read every 10 ms through NVML
+    (read-only queries of the driver's management library) from start to stop; nvidia-smi at
+    100 ms when NVML cannot be loaded."""
 
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits (nvmlClocksEventReason*)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+    IDLE = 0x1
 
-    def __init__(self, index: int):
-        self.index = index
-        self.proc = None
-        self.lines = []
+    def __init__(self, index: int, uuid: str | None = None, period_s: float = 0.01):
+        self.index, self.uuid, self.period = index, uuid, period_s
+        self.samples = []  # (sm_mhz, reasons bitmask)
+        self.max_mhz = None
+        self.source = None
+        self._stop = threading.Event()
+        self._thread = None
+        self._proc = None
 
-    def __enter__(self):
+    def _nvml(self):
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = ctypes.c_void_p()
+        rc = 1
+        if self.uuid:
+            rc = nv.nvmlDeviceGetHandleByUUID(self.uuid.encode(), ctypes.byref(h))
+        if rc != 0:
+            rc = nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h))
+        if rc != 0:
+            raise OSError("no NVML handle")
+        reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        return nv, h, reasons_fn
+
+    def start(self):
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except FileNotFoundError:
-            self.proc = None
+            nv, h, reasons_fn = self._nvml()
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:  # NVML_CLOCK_SM
+                self.max_mhz = float(mx.value)
+            self.source = "nvml"
+
+            def run():
+                clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+                while not self._stop.is_set():
+                    if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and \
+                            reasons_fn(h, ctypes.byref(rs)) == 0:
+                        self.samples.append((float(clk.value), int(rs.value)))
+                    self._stop.wait(self.period)
+                nv.nvmlShutdown()
+
+            self._thread = threading.Thread(target=run, daemon=True)
+            self._thread.start()
+        except (OSError, AttributeError):
+            self._start_smi()
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+    def _start_smi(self):
+        query = "clocks.sm,clocks.max.sm,clocks_event_reasons.active"
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={query}",
+                                           "--format=csv,noheader,nounits", "-lms", "100"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            return
+        self.source = "nvidia-smi"
 
-    def __exit__(self, *exc):
-        if self.proc is not None:
-            self.proc.terminate()
+        def read():
+            for line in self._proc.stdout:
+                parts = [p.strip() for p in line.split(",")]
+                try:
+                    self.max_mhz = float(parts[1])
+                    self.samples.append((float(parts[0]), int(parts[2], 16)))
+                except (ValueError, IndexError):
+                    continue
+
+        self._thread = threading.Thread(target=read, daemon=True)
+        self._thread.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()
             try:
-                self.proc.wait(timeout=5)
+                self._proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
-                self.proc.kill()
+                self._proc.kill()
+        if self._thread is not None:
+            self._thread.join(timeout=5)
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                mx = float(parts[2])
-            except ValueError:
-                continue
-            for n, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        busy = [(c, r) for c, r in self.samples if not r & self.IDLE]
+        use = busy or self.samples
+        reasons = sorted({n for _, r in use for bit, n in self.REASONS.items() if r & bit})
+        return {"sm_mhz": float(np.median([c for c, _ in use])) if use else None, "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.samples), "samples_not_idle": len(busy),
+                "source": self.source}
 
 
 def measured_peaks():
@@ -133,6 +212,36 @@ def measured_peaks():
 
 
 # ------------------------------------------------------------------------------------ workloads
+def workload_config(name: str, world: int = 1) -> tuple[dict, dict]:
+    """(the workload's table entry, the `config` object both arms print)."""
+    c = load_synthetic().CONFIGS[name]
+    st = c["settings"]
+    HW = c["width"] * c["height"]
+    T, S, B = st["time_transformation_size"], st["time_stride"], st["batch_size"]
+    cfg = {"workload": f"{name}: {c['desc']}", "width": c["width"], "height": c["height"], "depth_bytes": c["depth"],
+           "batch": B, "time_stride": S, "time_transformation_size": T, "parallelism": f"replicas x{world}",
+           "l2": "inputs larger than L2: time ring %d MB + 4 cycled input batches of %d MB" % (
+               HW * 8 * T >> 20, B * HW * c["depth"] >> 20),
+           "B_alg_bytes_per_frame": HW * (c["depth"] + 8 + 8.0 * T / S + 2.0 / S)}
+    return c, cfg
+
+
+def oracle_settings_for(c: dict, O, precision: str = "fp64"):
+    """The oracle's settings for a workload-table entry (the library's defaults elsewhere)."""
+    st = c["settings"]
+    return O.OracleSettings(
+        width=c["width"], height=c["height"], depth=c["depth"],
+        space_transformation=SPACE_NAMES[st["space_transformation"]],
+        time_transformation=TIME_NAMES[st["time_transformation"]],
+        time_transformation_size=st["time_transformation_size"], time_stride=st["time_stride"],
+        batch_size=st["batch_size"], lam=st["lambda_"], z=st["z_distance"], pixel_size=st["pixel_size"],
+        image_type=IMG_NAMES[st["image_type"]], p_start=st["p_start"], p_width=st["p_width"],
+        fft_shift=bool(st["fft_shift"]), renorm=bool(st["renorm"]), accumulation=st["accumulation"],
+        contrast_enabled=bool(st["contrast_enabled"]), contrast_auto_refresh=bool(st["contrast_auto_refresh"]),
+        contrast_lower=st["contrast_lower"], contrast_upper=st["contrast_upper"],
+        unwrap_2d=bool(st.get("unwrap_2d", 0)), precision=precision)
+
+
 def make_workload(name: str):
     import holovibes_gb300 as hv
     from holovibes_gb300.synthetic import CONFIGS, generator, settings_for
@@ -151,68 +260,142 @@ def unique_batches(gen, B: int, nbatches: int, frames_cap: int):
     return frames[idx].reshape(nbatches, B, *frames.shape[1:])
 
 
-def algorithmic_bytes_per_frame(fd, s):
-    """B_alg = HW * (b + 8 + 8*T/S + 2/S): raw read, ring write, T/S ring reads, uint16 output."""
-    HW = fd.width * fd.height
-    T, S = s.time_transformation_size, s.time_stride
-    return HW * (fd.depth + 8 + 8.0 * T / S + 2.0 / S)
+def window_frames(gen, st: dict) -> list:
+    """The raw batches up to and including the first rendered window (T / B batches)."""
+    B, T, S = st["batch_size"], st["time_transformation_size"], st["time_stride"]
+    n = max(1, (T + B - 1) // B) * (S // B)
+    return [gen.frames(i * B, B) for i in range(n)]
 
 
-# ------------------------------------------------------------------------------------ CPU oracle
-def cpu_oracle_run(c, fd, s, gen, budget_s: float, max_batches: int | None = None):
-    """Times the FP64 numpy oracle (OraclePipe) on whole batches of the same workload until the
-    budget is spent; returns (frames/s, frames, seconds, batches)."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import holovibes_oracle as O
-
-    names = ({0: "NONE", 1: "FRESNELTR", 2: "ANGULARSP"}, {0: "NONE", 1: "STFT", 2: "PCA"},
-             {0: "MODULUS", 1: "SQUARED_MODULUS", 2: "ARGUMENT"})
-    os_ = O.OracleSettings(
-        width=fd.width, height=fd.height, depth=fd.depth, space_transformation=names[0][s.space_transformation],
-        time_transformation=names[1][s.time_transformation], time_transformation_size=s.time_transformation_size,
-        time_stride=s.time_stride, batch_size=s.batch_size, lam=s.lambda_, z=s.z_distance, pixel_size=s.pixel_size,
-        image_type=names[2][s.image_type], p_start=s.p_start, p_width=s.p_width, fft_shift=bool(s.fft_shift),
-        renorm=bool(s.renorm), renorm_constant=s.renorm_constant, accumulation=s.accumulation,
-        contrast_enabled=bool(s.contrast_enabled), contrast_lower=s.contrast_lower, contrast_upper=s.contrast_upper,
-        unwrap_2d=bool(s.unwrap_2d))
-    pipe = O.OraclePipe(os_)
-    B = s.batch_size
-    batch = gen.frames(0, B)
-    # fill the ring untimed so every timed batch renders like the steady state
-    fill = max(0, s.time_transformation_size // max(1, B) - 1) * (s.time_stride // B)
-    for _ in range(fill):
-        pipe.process_batch(batch)
+# ------------------------------------------------------------------------------------ CPU legs
+def cpu_oracle_run(c, batches, budget_s: float, precision: str = "fp64", max_batches: int | None = None):
+    """Times the numpy oracle (OraclePipe, FP64 or its FP32 twin) on whole batches of the workload:
+    the ring is filled untimed, then the window's last batch is pushed until the budget is spent.
+    Returns (frames/s, frames, seconds, batches, the first timed output)."""
+    O = load_oracle()
+    pipe = O.OraclePipe(oracle_settings_for(c, O, precision))
+    B = c["settings"]["batch_size"]
+    for b in batches[:-1]:
+        pipe.process_batch(b)
     n = 0
+    first = None
     t0 = time.perf_counter()
     while True:
-        pipe.process_batch(batch)
+        out = pipe.process_batch(batches[-1])
+        if first is None:
+            first = out
         n += 1
         el = time.perf_counter() - t0
         if el >= budget_s or (max_batches and n >= max_batches):
             break
-    return n * B / el, n * B, el, n
+    return n * B / el, n * B, el, n, first
+
+
+def parity_against(hv, O, fd, s, batches, ref_out) -> dict:
+    """A fresh Pipe on the same window as the oracle's first timed output: rel-L2 of the float
+    frame fed to the contrast stage (argument views: wrapped differences, branch-cut pixels
+    counted apart), uint16 mismatches against the oracle's contrast stage on the GPU's own float
+    frame, and for PCA the relative error of the kept eigenvalues."""
+    pipe = hv.Pipe(fd, s)
+    for b in batches[:-1]:
+        pipe.enqueue(b)
+    pipe.enqueue(batches[-1])
+    got_u16 = pipe.pull()
+    got_f = pipe.float_frame()
+    lo, hi = pipe.contrast_range()
+    ring = pipe.ring()[0] if s.time_transformation == hv.TIME_PCA else None
+    pipe.close()
+    ref = ref_out.float_frame
+    res = {"output": "first rendered window of the sample"}
+    if s.image_type == hv.IMG_ARGUMENT and not s.unwrap_2d:
+        wd = (got_f - ref + np.pi) % (2 * np.pi) - np.pi
+        cut = np.abs(wd) > 1e-3
+        res["rel_l2"] = float(np.linalg.norm(wd[~cut]) / np.linalg.norm(ref[~cut]))
+        res["branch_cut_fraction"] = float(np.mean(cut))
+    else:
+        res["rel_l2"] = float(np.linalg.norm(got_f - ref) / np.linalg.norm(ref))
+    res["u16_mismatch"] = int(np.count_nonzero(got_u16 != O.float_to_ushort(O.apply_contrast(got_f, lo, hi))))
+    if ring is not None:
+        import torch
+
+        T = s.time_transformation_size
+        L = hv.lib()
+        npix = fd.width * fd.height
+        rd = torch.from_numpy(ring.view(np.float32)).cuda()
+        cov = torch.empty(T * T * 2, dtype=torch.float64, device="cuda")
+        cw = torch.empty(max(16, L.hv_pca_cov_workspace(T, npix)), dtype=torch.uint8, device="cuda")
+        hv.check(L.hv_pca_covariance(rd.data_ptr(), T, npix, cov.data_ptr(), cw.data_ptr(), None), "covariance")
+        ev = torch.empty(T, dtype=torch.float64, device="cuda")
+        vec = torch.empty(T * T * 2, dtype=torch.float64, device="cuda")
+        ew = torch.empty(max(16, L.hv_pca_eigh_workspace(T)), dtype=torch.uint8, device="cuda")
+        hv.check(L.hv_pca_eigh(cov.data_ptr(), T, ev.data_ptr(), vec.data_ptr(), 0, 0, None, ew.data_ptr(), None),
+                 "eigh")
+        got_w = ev.cpu().numpy()
+        ref_w, _ = O.pca_eigh(O.pca_covariance(ring.astype(np.complex128)))
+        pmin, pmax = O.p_range(s.p_start, s.p_width, T)
+        k = slice(pmin, pmax + 1)
+        res["eig_rel_err_kept"] = float(np.max(np.abs(got_w[k] - ref_w[k]) / np.abs(ref_w[k])))
+    return res
 
 
 # ------------------------------------------------------------------------------------ reference arm
+def reference_gpu_build(c, batches, steps: int, warmup: int) -> dict:
+    """The reference's own GPU build (unmodified cuFFT / cuBLAS / cuSOLVER translation units, one
+    Pipe cycle per batch with its stream synchronisations) on device-resident batches."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    try:
+        import ref_pipe
+        import torch
+
+        if not ref_pipe.available():
+            return {"unavailable": "reference sources not staged (oracle/ref_build.py stages them from the "
+                                   "reference tree)"}
+        O = load_oracle()
+        rp = ref_pipe.RefPipe.from_oracle_settings(oracle_settings_for(c, O), keep_float_frame=False)
+        dev = [torch.from_numpy(np.ascontiguousarray(b).reshape(-1).view(np.uint8)).cuda() for b in batches]
+        ptrs = [d.data_ptr() for d in dev]
+        B, T = c["settings"]["batch_size"], c["settings"]["time_transformation_size"]
+        rp.run_device_batches(ptrs, max(1, T // B) + warmup)
+        ms = rp.run_device_batches(ptrs, steps)
+        rp.close()
+        return {"value": steps * B / (ms * 1e-3), "unit": "frames/s", "ms_per_step": ms / steps, "steps": steps,
+                "inputs": "device-resident raw batches (the BatchInputQueue's device slots)",
+                "what": "the reference's hot-path translation units compiled unmodified for sm_103a, one Pipe "
+                        "cycle per batch in Pipe::refresh order with its host synchronisations"}
+    except Exception as e:  # reported, the CPU line stands
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
-    c, fd, s, gen = make_workload(args.workload)
+    if args.workload in SERVE_WORKLOADS:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference runs one pipeline per process and has "
+                                                              "no serving engine; serving is compared against "
+                                                              "plain pipes by the default arm"}), flush=True)
+        return 0
+    c, cfg = workload_config(args.workload, world)
+    cfg["parallelism"] = f"replicas x{world}"
+    gen = load_synthetic().generator(args.workload, seed=1234)
+    st = c["settings"]
     cores = os.cpu_count() or 1
-    budget = max(5.0, min(120.0, 2.0 * args.steps))  # bounded: the run ends within a few minutes
-    fps, frames, el, nb = cpu_oracle_run(c, fd, s, gen, budget_s=min(budget, 60.0), max_batches=args.steps)
+    batches = window_frames(gen, st)
+    budget = max(5.0, min(60.0, 2.0 * args.steps))  # bounded: the run ends within a few minutes
+    fps, frames, el, nb, _ = cpu_oracle_run(c, batches, budget_s=budget, max_batches=args.steps)
     line = {
         "metric": "input frames/s", "value": fps, "unit": "frames/s", "n_gpus": args.gpus, "steps": nb,
         "warmup": args.warmup, "ms_per_step": 1000.0 * el / nb, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded interferograms)", "impl": "reference",
-        "config": {"workload": f"{args.workload}: {c['desc']}", "width": fd.width, "height": fd.height,
-                   "batch": s.batch_size, "time_transformation_size": s.time_transformation_size},
+        "config": cfg,
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
-                         "sample": f"{nb} batches of {s.batch_size} frames through the FP64 numpy oracle "
-                                   f"(scipy.fft with {cores} workers; FFTW unavailable)"},
+                         "sample": f"{nb} batches of {st['batch_size']} frames through the FP64 numpy oracle "
+                                   f"(scipy.fft with {cores} workers; FFTW unavailable); the reference has no CPU "
+                                   f"implementation of this path"},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_cpu_baseline:
+        line["reference_gpu_build"] = reference_gpu_build(c, batches, steps=max(args.steps, 20), warmup=args.warmup)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -235,7 +418,9 @@ def time_kernel(fn, stream, n=20):
 
 def steps_for(hv, fd, s, dev_batch, stream):
     """Single-kernel launches of the workload's hot path on `stream`, each with its algorithmic
-    bytes per launch (minimal DRAM traffic of that kernel: inputs read once, outputs written once)."""
+    bytes per launch (minimal DRAM traffic: inputs read once, outputs written once) and, for the
+    tensor-core contractions, its tensor flops per launch (split-BF16: 3 BF16 products per FP32
+    product)."""
     import torch
 
     L = hv.lib()
@@ -257,20 +442,21 @@ def steps_for(hv, fd, s, dev_batch, stream):
     if s.space_transformation == hv.SPACE_FRESNELTR:
         out.append(("fft_rows(convert*lens)", lambda: L.hv_fft_rows(raw, fd.depth, 0, work.data_ptr(), W, H, B,
                                                                     lens.data_ptr(), 0, 1.0, 0, B, stream),
-                    B * HW * (fd.depth + 8)))
+                    B * HW * (fd.depth + 8), 0))
         out.append(("fft_cols(->ring)", lambda: L.hv_fft_cols(work.data_ptr(), ring.data_ptr(), W, H, B, None, 0, 1.0,
-                                                              0, T, stream), B * HW * 16))
+                                                              0, T, stream), B * HW * 16, 0))
     elif s.space_transformation == hv.SPACE_ANGULARSP:
         out.append(("fft_rows(convert)", lambda: L.hv_fft_rows(raw, fd.depth, 0, work.data_ptr(), W, H, B, None, 0,
-                                                               1.0, 0, B, stream), B * HW * (fd.depth + 8)))
+                                                               1.0, 0, B, stream), B * HW * (fd.depth + 8), 0))
         # out of place (the pipe runs it in place): repeated in-place launches would scale the
         # unnormalised forward * G * inverse by H W per launch into Inf / NaN, and the views'
         # atan2 is slower on non-finite and all-zero samples than on image data
         work2 = buf(B * HW * 8)
         out.append(("fft_cols(fwd*G,inv)", lambda: L.hv_fft_cols(work.data_ptr(), work2.data_ptr(), W, H, B,
-                                                                 lens.data_ptr(), 2, 1.0, 0, B, stream), B * HW * 16))
+                                                                 lens.data_ptr(), 2, 1.0, 0, B, stream), B * HW * 16,
+                    0))
         out.append(("fft_rows(inv->ring)", lambda: L.hv_fft_rows(work2.data_ptr(), 8, 0, ring.data_ptr(), W, H, B,
-                                                                 None, 1, 1.0 / HW, 0, T, stream), B * HW * 16))
+                                                                 None, 1, 1.0 / HW, 0, T, stream), B * HW * 16, 0))
     pmin = s.p_start
     pmax = min(s.p_start + s.p_width, T) if s.p_width else s.p_start
     pmax = min(pmax, T - 1)
@@ -286,47 +472,84 @@ def steps_for(hv, fd, s, dev_batch, stream):
         hv.check(L.hv_time_view_tc_prepare(wts.data_ptr(), K, T, vw.data_ptr(), stream), "view_tc prepare")
         out.append(("time_view_tc", lambda: L.hv_time_view_tc_run(ring.data_ptr(), T, W, H, K, s.image_type, 1.0,
                                                                   s.fft_shift, view.data_ptr(), None, vw.data_ptr(),
-                                                                  stream), T * HW * 8 + HW * 4))
+                                                                  stream), T * HW * 8 + HW * 4, 3 * 8 * HW * T * K))
     else:
         out.append(("time_view", lambda: L.hv_time_view(ring.data_ptr(), T, W, H, wts.data_ptr(), K, s.image_type,
                                                         1.0, s.fft_shift, view.data_ptr(), None, stream),
-                    T * HW * 8 + HW * 4))
+                    T * HW * 8 + HW * 4, 0))
     if s.time_transformation == hv.TIME_PCA:
         cov, cw = buf(T * T * 16), buf(L.hv_pca_cov_workspace(T, HW))
         out.append(("pca_covariance", lambda: L.hv_pca_covariance(ring.data_ptr(), T, HW, cov.data_ptr(),
-                                                                  cw.data_ptr(), stream), T * HW * 8))
+                                                                  cw.data_ptr(), stream), T * HW * 8,
+                    3 * 8 * HW * T * T))
     return out
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant kernel, from the ncu
-# captures of the same launch summarised in profiles/ (k_fft_cols_w32_tma_1024x1024.md,
-# launches_cfg2_768x768_u16_as_stft_T256_K33.md, launches_cfg0_512x512_u16_as_stft_T16.md)
-NCU_TRAFFIC = {
-    ("cfg0", "fft_cols(fwd*G,inv)"): 35712256 + 1280,
-    ("cfg1", "fft_cols(->ring)"): 268523520 + 214097664,
-    ("cfg2", "time_view_tc"): 1208223232 + 5527808,
-    ("cfg2", "fft_cols(fwd*G,inv)"): 307309312 + 245959936,
-}
+def ncu_traffic(workload: str, kernel: str):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu capture summary
+    (profiles/ncu_traffic.json), used only when the capture was taken on the same kernel sources
+    as this build (its digest matches); otherwise None."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None, None
+    d = json.loads(p.read_text())
+    e = d.get("captures", {}).get(f"{workload}/{kernel}")
+    if not e or e.get("kernel_sources_sha256") != kernel_sources_digest():
+        return None, e.get("kernel_sources_sha256") if e else None
+    return e["dram_bytes"], e.get("command")
 
 
-def roofline(hv, fd, s, dev_batch, peak_gbs, peak_src, workload=""):
-    """Dominant kernel measured alone with CUDA events on its launching stream."""
+def kernel_sources_digest() -> str:
+    h = hashlib.sha256()
+    for f in sorted((ROOT / "holovibes_gb300" / "csrc").glob("*")):
+        if f.suffix in (".cu", ".cuh", ".cpp", ".h"):
+            h.update(f.name.encode())
+            h.update(f.read_bytes())
+    return h.hexdigest()
+
+
+def roofline(hv, fd, s, dev_batch, peaks, workload=""):
+    """Every hot kernel measured alone with CUDA events on its launching stream; the slowest is
+    reported against the roof it is closer to (HBM bytes, or tensor flops for the contractions)."""
     import torch
 
+    peak_gbs, peak_tf, peak_src = peaks
     stream = torch.cuda.Stream()
     kernels = steps_for(hv, fd, s, dev_batch, stream.cuda_stream)
     rows = []
     with torch.cuda.stream(stream):
-        for name, fn, alg_bytes in kernels:
+        for name, fn, alg_bytes, flops in kernels:
             ms = time_kernel(lambda: hv.check(fn(), name), stream)
-            rows.append((name, ms, alg_bytes))
-    name, ms, alg = max(rows, key=lambda r: r[1])
-    achieved = alg / (ms * 1e-3) / 1e9
-    traffic = NCU_TRAFFIC.get((workload, name))
-    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-            "frac": achieved / peak_gbs, "traffic": traffic, "peak_source": peak_src,
-            "per_launch_bytes": alg, "ms_per_launch": ms,
-            "all": {n: {"ms": round(m, 5), "GB/s": round(b / (m * 1e-3) / 1e9, 1)} for n, m, b in rows}}
+            rows.append((name, ms, alg_bytes, flops))
+    name, ms, alg, flops = max(rows, key=lambda r: r[1])
+    gbs = alg / (ms * 1e-3) / 1e9
+    tfs = flops / (ms * 1e-3) / 1e12
+    hbm_frac, tc_frac = gbs / peak_gbs, tfs / peak_tf
+    traffic, cmd = ncu_traffic(workload, name)
+    out = {"kernel": name, "peak_source": peak_src, "per_launch_bytes": alg, "per_launch_tensor_flops": flops,
+           "ms_per_launch": ms, "traffic": traffic,
+           "traffic_source": cmd if traffic else "no ncu capture of these kernel sources (profiles/ncu_traffic.json)",
+           "all": {n: {"ms": round(m, 5), "GB/s": round(b / (m * 1e-3) / 1e9, 1),
+                       **({"TFLOP/s": round(f / (m * 1e-3) / 1e12, 1)} if f else {})} for n, m, b, f in rows}}
+    if tc_frac > hbm_frac:
+        out.update(bound="tensor", achieved=tfs, peak=peak_tf, unit="TFLOP/s", frac=tc_frac, hbm_frac=hbm_frac)
+    else:
+        out.update(bound="hbm", achieved=gbs, peak=peak_gbs, unit="GB/s", frac=hbm_frac,
+                   **({"tensor_frac": tc_frac} if flops else {}))
+    return out
+
+
+def dtype_of(hv, s) -> str:
+    parts = ["f32 (convert, FFT passes, views, render)"]
+    if s.time_transformation == hv.TIME_PCA:
+        # the bench keeps the library's default eigensolver precision (FP32 sweeps up to T = 512)
+        eig = "f64 Jacobi sweeps" if s.time_transformation_size > 512 else \
+            "f32 Jacobi sweeps + f64 Rayleigh quotients / normalisation"
+        parts.append("bf16x3 on tcgen05 with f32 accumulation, f64 reduce (covariance)")
+        parts.append(f"{eig} (eigensolve)")
+    elif s.time_transformation in (hv.TIME_STFT, hv.TIME_SSA_STFT):
+        parts.append("f64-built weights; bf16x3 tcgen05 contraction for >= 8 bins, else f32 (STFT bins)")
+    return ", ".join(parts)
 
 
 def run_ours(args):
@@ -343,7 +566,10 @@ def run_ours(args):
     import holovibes_gb300 as hv
 
     hv.lib()
+    clk = ClockSampler(local, uuid=f"GPU-{torch.cuda.get_device_properties(torch.cuda.current_device()).uuid}")
+    clk.start()
     c, fd, s, gen = make_workload(args.workload)
+    _, cfg = workload_config(args.workload, world)
     B = s.batch_size
     HW = fd.width * fd.height
     nb_unique = 4
@@ -366,13 +592,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     launches0 = pipe.kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for i in range(args.steps):
-            step(i)
-        pipe.join()  # the rendering stream joins the pipe stream before the closing event
-        e1.record(stream)
-        torch.cuda.synchronize()
+    e0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    pipe.join()  # the rendering stream joins the pipe stream before the closing event
+    e1.record(stream)
+    torch.cuda.synchronize()
     launches = pipe.kernel_launches() - launches0
     ms, value = replica_throughput(e0.elapsed_time(e1), args.steps * B, world)
 
@@ -401,44 +626,55 @@ def run_ours(args):
     pipe.sync()
     t_e2e_ms, e2e_value = replica_throughput((time.perf_counter() - t0) * 1e3, e2e_steps * B, world)
     lat_ms = np.array(lat) * 1e3 if lat else np.array([float("nan")])
-
-    peak_gbs, _, peak_src = measured_peaks()
-    rl = roofline(hv, fd, s, dev_batches[0], peak_gbs, peak_src, args.workload) if rank == 0 else None
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        fps, frames, el, nb = cpu_oracle_run(c, fd, s, gen, budget_s=args.cpu_budget_s)
-        cpu = {"value": fps, "unit": "frames/s", "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": f"{nb} batches of {B} frames ({frames} frames, {el:.1f} s) through the FP64 numpy "
-                         f"oracle, scipy.fft workers={os.cpu_count()} (FFTW unavailable)"}
     pipe.close()
+
+    peaks = measured_peaks()
+    rl = roofline(hv, fd, s, dev_batches[0], peaks, args.workload) if rank == 0 else None
+    serving = None
+    if rank == 0 and world == 1 and not args.no_serving and args.workload == DEFAULT_WORKLOAD:
+        try:
+            serving = serving_comparison(args, "serve512", steps=max(50, min(args.steps, 200)))
+        except Exception as e:  # reported in the line; the headline measurement stands
+            serving = {"error": f"{type(e).__name__}: {e}"}
+    clk.stop()
+    cpu = parity = None
+    if rank == 0 and not args.no_cpu_baseline:
+        O = load_oracle()
+        win = window_frames(gen, c["settings"])
+        fps, frames, el, nb, first = cpu_oracle_run(c, win, budget_s=args.cpu_budget_s)
+        fps32, frames32, el32, nb32, _ = cpu_oracle_run(c, win, budget_s=args.cpu_budget_s / 2, precision="fp32")
+        cores = os.cpu_count() or 1
+        cpu = {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+               "sample": f"{nb} batches of {B} frames ({frames} frames, {el:.1f} s) through the FP64 numpy oracle "
+                         f"after an untimed ring fill, scipy.fft workers={cores} (FFTW unavailable)",
+               "fp32": {"value": fps32, "unit": "frames/s", "cores": cores,
+                        "sample": f"{nb32} batches ({frames32} frames, {el32:.1f} s), same equations in "
+                                  f"complex64 / float32"}}
+        # the GPU Pipe's output on the sampled window against the oracle's (the checker's use)
+        parity = parity_against(hv, O, fd, s, win, first)
     if rank == 0:
-        balg = algorithmic_bytes_per_frame(fd, s)
+        balg = cfg["B_alg_bytes_per_frame"]
         line = {
             "metric": "input frames/s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (FFT, views), bf16x3/f32 (PCA covariance), f64 (eigensolve)",
+            "vs_baseline": None, "dtype": dtype_of(hv, s),
             "data": "synthetic (seeded interferograms, generator in holovibes_gb300/synthetic.py)",
-            "config": {"workload": f"{args.workload}: {c['desc']}", "width": fd.width, "height": fd.height,
-                       "depth_bytes": fd.depth, "batch": B, "time_stride": s.time_stride,
-                       "time_transformation_size": s.time_transformation_size,
-                       "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2: time ring %d MB + %d cycled input batches of %d MB" % (
-                           HW * 8 * s.time_transformation_size >> 20, nb_unique, B * frame_bytes >> 20),
-                       "B_alg_bytes_per_frame": balg},
+            "config": cfg,
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": B * frame_bytes,
                     "d2h_bytes_per_step": HW * 2},
             "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99))},
-            "pipeline_hbm_frac": value / world * balg / (peak_gbs * 1e9),
+            "pipeline_hbm_frac": value / world * balg / (peaks[0] * 1e9),
             "gpu_launches": int(launches),
             "roofline": rl,
             "cpu_baseline": cpu,
+            "parity": parity,
+            "serving": serving,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
-
 
 
 # ------------------------------------------------------------------------------------ serving
@@ -528,7 +764,7 @@ def _plain_process(idx: int, workload: str, steps: int, warmup: int, barrier, qu
         queue.put((idx, -1, 0.0, 0.0, repr(e)))
 
 
-def run_plain_processes(args, nstreams: int, steps: int) -> dict:
+def run_plain_processes(args, nstreams: int, steps: int, workload: str) -> dict:
     """Aggregate input frames/s of one plain pipe per process over all streams (wall clock from
     the first timed push to the last hologram of any process)."""
     import multiprocessing as mp
@@ -536,7 +772,7 @@ def run_plain_processes(args, nstreams: int, steps: int) -> dict:
     ctx = mp.get_context("spawn")
     barrier = ctx.Barrier(nstreams)
     queue = ctx.Queue()
-    procs = [ctx.Process(target=_plain_process, args=(i, args.workload, steps, args.warmup, barrier, queue))
+    procs = [ctx.Process(target=_plain_process, args=(i, workload, steps, args.warmup, barrier, queue))
              for i in range(nstreams)]
     for p in procs:
         p.start()
@@ -553,18 +789,16 @@ def run_plain_processes(args, nstreams: int, steps: int) -> dict:
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}}
 
 
-def run_serving(args):
-    """Served (hv_server: engine thread, shape buckets, CUDA graphs) vs plain (one hv_pipe per
-    stream) on the same streams, from pinned host memory with holograms read back: one client
-    thread pushes one batch per stream per step and reads back the holograms of the previous step."""
+def serving_comparison(args, workload: str, steps: int) -> dict:
+    """Served (hv_server: engine thread, shape buckets, CUDA graphs) against plain in-process pipes
+    (one hv_pipe per stream, each on its own CUDA stream) and one plain pipe per process, on the
+    same streams, from pinned host memory with holograms read back: one client thread pushes one
+    batch per stream per step and reads back the holograms of the previous step."""
     import torch
 
     import holovibes_gb300 as hv
 
-    torch.cuda.set_device(0)
-    hv.lib()
-    streams = serve_streams(args.workload)
-    steps = max(20, min(args.steps, 400))
+    streams = serve_streams(workload)
     pinned = [torch.from_numpy(b.copy()).pin_memory() for (_, _, b) in streams]
     outs = [torch.empty(fd.width * fd.height * 2, dtype=torch.uint8).pin_memory() for (fd, _, _) in streams]
     frames_per_step = sum(s.batch_size for (_, s, _) in streams)
@@ -583,89 +817,103 @@ def run_serving(args):
                         lat.append(time.perf_counter() - pushed[i].pop(0))
         return t0
 
+    def pct(lat):
+        a = np.array(lat) * 1e3
+        return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99))}
+
     results = {}
-    with ClockSampler(0) as clk:
-        # ---- plain: one Pipe per stream, driven by the client thread
-        pipes = [hv.Pipe(fd, s) for (fd, s, _) in streams]
-        push = lambda i, ptr, n: pipes[i].enqueue_ptr(ptr, n, hv.MEM_HOST)
-        count = lambda i: pipes[i].output_count()
-        pull = lambda i, ptr: pipes[i].pull_into(ptr, hv.MEM_HOST)
-        warm = max(s.time_transformation_size // s.batch_size for (_, s, _) in streams) + args.warmup
-        drive(push, count, pull, warm, [])
-        for p in pipes:
-            p.sync()
-        lat = []
-        t0 = drive(push, count, pull, steps, lat)
-        for i, p in enumerate(pipes):
-            p.sync()
-            while p.output_count():
-                p.pull_into(outs[i].data_ptr(), hv.MEM_HOST)
-        el = time.perf_counter() - t0
-        launches = sum(p.kernel_launches() for p in pipes)
-        for p in pipes:
-            p.close()
-        results["plain"] = {"frames_per_s": steps * frames_per_step / el,
-                            "latency_ms": {"p50": float(np.percentile(np.array(lat) * 1e3, 50)),
-                                           "p99": float(np.percentile(np.array(lat) * 1e3, 99))}}
-        # ---- served
-        flags = {"bucket": 0, "stream": hv.SERVER_STREAM_GRAPHS, "eager": hv.SERVER_NO_GRAPHS}[args.server_mode]
-        srv = hv.Server(flags=flags)
-        sts = [srv.open_stream(fd, s) for (fd, s, _) in streams]
-        push = lambda i, ptr, n: sts[i].enqueue_ptr(ptr, n, hv.MEM_HOST)
-        count = lambda i: sts[i].output_count()
-        pull = lambda i, ptr: sts[i].pull_into(ptr, hv.MEM_HOST)
-        drive(push, count, pull, warm, [])
-        srv.sync()
-        for i, st in enumerate(sts):
-            while st.output_count():
-                st.pull_into(outs[i].data_ptr(), hv.MEM_HOST)
-        srv.reset_stats()
-        g0 = srv.stats()
-        k0 = hv.kernel_launches()
-        lat = []
-        t0 = drive(push, count, pull, steps, lat)
-        srv.sync()
-        for i, st in enumerate(sts):
-            while st.output_count():
-                st.pull_into(outs[i].data_ptr(), hv.MEM_HOST)
-        el = time.perf_counter() - t0
-        g1 = srv.stats()
-        eager_kernels = hv.kernel_launches() - k0
-        srv.close()
-        results["served"] = {"frames_per_s": steps * frames_per_step / el,
-                             "latency_ms": {"p50": float(np.percentile(np.array(lat) * 1e3, 50)),
-                                            "p99": float(np.percentile(np.array(lat) * 1e3, 99))},
-                             "device_latency_ms": {"p50": g1["latency_p50_us"] / 1e3,
-                                                   "p99": g1["latency_p99_us"] / 1e3},
-                             "graph_launches": g1["graph_launches"] - g0["graph_launches"],
-                             "graph_kernels": g1["graph_kernels"] - g0["graph_kernels"],
-                             "eager_cycles": g1["eager_cycles"] - g0["eager_cycles"],
-                             "eager_kernels": eager_kernels,
-                             "buckets": g1["buckets"]}
-    # one plain pipe per process (the reference's deployment: one instance per stream); outside
-    # the clock sampler's window so the processes' start-up is not sampled
-    results["plain_per_process"] = run_plain_processes(args, len(streams), steps)
-    window_ms = min(1e3 * s.time_transformation_size / (results["served"]["frames_per_s"] / len(streams))
-                    for (_, s, _) in streams)
+    # ---- plain: one Pipe per stream, driven by the client thread
+    pipes = [hv.Pipe(fd, s) for (fd, s, _) in streams]
+    push = lambda i, ptr, n: pipes[i].enqueue_ptr(ptr, n, hv.MEM_HOST)
+    count = lambda i: pipes[i].output_count()
+    pull = lambda i, ptr: pipes[i].pull_into(ptr, hv.MEM_HOST)
+    warm = max(s.time_transformation_size // s.batch_size for (_, s, _) in streams) + args.warmup
+    drive(push, count, pull, warm, [])
+    for p in pipes:
+        p.sync()
+    lat = []
+    t0 = drive(push, count, pull, steps, lat)
+    for i, p in enumerate(pipes):
+        p.sync()
+        while p.output_count():
+            p.pull_into(outs[i].data_ptr(), hv.MEM_HOST)
+    el = time.perf_counter() - t0
+    plain_launches = sum(p.kernel_launches() for p in pipes)
+    for p in pipes:
+        p.close()
+    results["plain"] = {"frames_per_s": steps * frames_per_step / el, "latency_ms": pct(lat),
+                        "kernel_launches_total": plain_launches}
+    # ---- served
+    flags = {"bucket": 0, "stream": hv.SERVER_STREAM_GRAPHS, "eager": hv.SERVER_NO_GRAPHS}[args.server_mode]
+    srv = hv.Server(flags=flags)
+    sts = [srv.open_stream(fd, s) for (fd, s, _) in streams]
+    push = lambda i, ptr, n: sts[i].enqueue_ptr(ptr, n, hv.MEM_HOST)
+    count = lambda i: sts[i].output_count()
+    pull = lambda i, ptr: sts[i].pull_into(ptr, hv.MEM_HOST)
+    drive(push, count, pull, warm, [])
+    srv.sync()
+    for i, st in enumerate(sts):
+        while st.output_count():
+            st.pull_into(outs[i].data_ptr(), hv.MEM_HOST)
+    srv.reset_stats()
+    g0 = srv.stats()
+    k0 = hv.kernel_launches()
+    lat = []
+    t0 = drive(push, count, pull, steps, lat)
+    srv.sync()
+    for i, st in enumerate(sts):
+        while st.output_count():
+            st.pull_into(outs[i].data_ptr(), hv.MEM_HOST)
+    el = time.perf_counter() - t0
+    g1 = srv.stats()
+    eager_kernels = hv.kernel_launches() - k0
+    srv.close()
+    results["served"] = {"frames_per_s": steps * frames_per_step / el, "latency_ms": pct(lat),
+                         "device_latency_ms": {"p50": g1["latency_p50_us"] / 1e3, "p99": g1["latency_p99_us"] / 1e3},
+                         "graph_launches": g1["graph_launches"] - g0["graph_launches"],
+                         "graph_kernels": g1["graph_kernels"] - g0["graph_kernels"],
+                         "eager_cycles": g1["eager_cycles"] - g0["eager_cycles"],
+                         "eager_kernels": eager_kernels,
+                         "buckets": g1["buckets"], "server_mode": args.server_mode}
+    # one plain pipe per process (one Holovibes instance and one compute pipeline per stream)
+    results["plain_per_process"] = run_plain_processes(args, len(streams), steps, workload)
     v = results["served"]["frames_per_s"]
-    h2d = sum(b.shape[1] for (_, _, b) in streams)
-    d2h = sum(fd.width * fd.height * 2 // s.time_stride * s.batch_size for (fd, s, _) in streams)
+    window_ms = min(1e3 * s.time_transformation_size / (v / len(streams)) for (_, s, _) in streams)
+    results.update(
+        workload=f"{workload}: {SERVE_WORKLOADS[workload]}", streams=len(streams), frames_per_step=frames_per_step,
+        steps=steps, served_over_plain=v / results["plain"]["frames_per_s"],
+        served_over_plain_per_process=v / results["plain_per_process"]["frames_per_s"],
+        shortest_window_ms_at_served_rate=window_ms,
+        p99_under_one_window=results["served"]["latency_ms"]["p99"] < window_ms,
+        h2d_bytes_per_step=sum(b.shape[1] for (_, _, b) in streams),
+        d2h_bytes_per_step=sum(fd.width * fd.height * 2 // s.time_stride * s.batch_size for (fd, s, _) in streams))
+    return results
+
+
+def run_serving(args):
+    import torch
+
+    import holovibes_gb300 as hv
+
+    torch.cuda.set_device(0)
+    hv.lib()
+    clk = ClockSampler(0, uuid=f"GPU-{torch.cuda.get_device_properties(0).uuid}").start()
+    steps = max(20, min(args.steps, 400))
+    res = serving_comparison(args, args.workload, steps)
+    clk.stop()
+    v = res["served"]["frames_per_s"]
     line = {
         "metric": "input frames/s", "value": v, "unit": "frames/s", "n_gpus": 1, "steps": steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * frames_per_step / v, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * res["frames_per_step"] / v, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FFT, views), bf16x3/f32 (PCA covariance)",
         "data": "synthetic (seeded interferograms, one seed per stream)",
-        "config": {"workload": f"{args.workload}: {SERVE_WORKLOADS[args.workload]}", "streams": len(streams),
-                   "server_mode": args.server_mode,
-                   "frames_per_step": frames_per_step, "parallelism": "one GPU, streams overlapped",
+        "config": {"workload": res["workload"], "streams": res["streams"], "server_mode": args.server_mode,
+                   "frames_per_step": res["frames_per_step"], "parallelism": "one GPU, streams overlapped",
                    "l2": "time rings of all streams exceed L2"},
-        "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "serving": {"served": results["served"], "plain": results["plain"],
-                    "served_over_plain": v / results["plain"]["frames_per_s"],
-                    "plain_per_process": results["plain_per_process"],
-                    "served_over_plain_per_process": v / results["plain_per_process"]["frames_per_s"],
-                    "shortest_window_ms_at_served_rate": window_ms},
-        "gpu_launches": int(results["served"]["graph_kernels"] + results["served"]["eager_kernels"]),
+        "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": res["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": res["d2h_bytes_per_step"]},
+        "serving": res,
+        "gpu_launches": int(res["served"]["graph_kernels"] + res["served"]["eager_kernels"]),
         "roofline": None, "cpu_baseline": None, "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)

@@ -104,6 +104,15 @@ def byteswap16(raw: np.ndarray) -> np.ndarray:
 # ----------------------------------------------------------------------------------------
 
 
+def fma32(a, b, c) -> np.ndarray:
+    """fmaf(a, b, c) on float32 arrays: the exact a*b + c rounded once to float32 (the product of
+    two float32 values is exact in the extended format, and the sum is rounded once more there
+    before the final rounding, which can differ from a single rounding only on exact ties)."""
+    ld = np.longdouble
+    r = np.asarray(a, F32).astype(ld) * np.asarray(b, F32).astype(ld) + np.asarray(c, F32).astype(ld)
+    return np.asarray(r.astype(F32))
+
+
 def _crop_square(square: np.ndarray, W: int, H: int) -> np.ndarray:
     """Centre crop of the max(W,H) square lens (fresnel_transform.cu:37-62)."""
     S = square.shape[0]
@@ -138,7 +147,8 @@ def fresnel_lens(W: int, H: int, lam: float, z: float, pixel_size_um: float, mod
         dx = F32(ps32 * F32(1.0e-6))
         x = (idx.astype(F32) - F32(S >> 1)) * dx
         xx = (x * x).astype(F32)
-        cs = (c * (xx[None, :] + xx[:, None]).astype(F32)).astype(F32)
+        # x * x + y * y as one fused multiply-add (the reference's compiled form)
+        cs = (c * fma32(x[None, :], x[None, :], xx[:, None])).astype(F32)
         lens = np.cos(cs.astype(np.float64)) + 1j * np.sin(cs.astype(np.float64))
     else:
         raise ValueError(mode)
@@ -164,8 +174,10 @@ def angular_spectrum_lens(W: int, H: int, lam: float, z: float, pixel_size_um: f
     then quadrant-swapped into FFT layout (fourier_transform.cc:134).
 
     mode "ref32" follows the float32 expression of masks.cu:43-55: u_step = 1.0f/(Nx*x_step),
-    u = (x-(Nx>>1))*u_step, tmp = 1.0f - lam*lam*(u*u+v*v) in float32, and the phase
-    2.0f*M_PI*z/lam*sqrtf(tmp) evaluated in double then rounded to float32.
+    u = (x-(Nx>>1))*u_step, tmp = 1.0f - lam*lam*(u*u+v*v) in float32 with the two fused
+    multiply-adds the reference's compiler forms (fmaf(u, u, v*v), then fmaf(-lam^2, s, 1); the
+    reference's own build matches this bit for bit), and the phase 2.0f*M_PI*z/lam*sqrtf(tmp)
+    evaluated in double (M_PI is a double) then rounded to float32.
     """
     xs = np.arange(W)
     ys = np.arange(H)
@@ -186,11 +198,10 @@ def angular_spectrum_lens(W: int, H: int, lam: float, z: float, pixel_size_um: f
         v_step = F32(F32(1.0) / F32(F32(H) * step))
         u = (xs - (W >> 1)).astype(F32) * u_step
         v = (ys - (H >> 1)).astype(F32) * v_step
-        uu = (u * u).astype(F32)
         vv = (v * v).astype(F32)
-        s = (uu[None, :] + vv[:, None]).astype(F32)
+        s = fma32(u[None, :], u[None, :], vv[:, None])
         ll = F32(lam32 * lam32)
-        tmp = (F32(1.0) - (ll * s).astype(F32)).astype(F32)
+        tmp = fma32(-ll, s, F32(1.0))
         tmp = np.maximum(tmp, F32(0.0))
         sq = np.sqrt(tmp).astype(F32).astype(np.float64)
         ph = ((2.0 * math.pi * float(z32)) / float(lam32)) * sq
@@ -334,7 +345,7 @@ def stft_bins(storage: np.ndarray, pmin: int, pmax: int) -> np.ndarray:
     T = storage.shape[0]
     t = np.arange(T)
     ks = np.arange(pmin, pmax + 1)
-    W = np.exp(-2j * np.pi * np.outer(ks, t) / T)  # [K, T]
+    W = np.exp(-2j * np.pi * np.outer(ks, t) / T).astype(np.result_type(storage.dtype, np.complex64))  # [K, T]
     flat = storage.reshape(T, -1)
     return (W @ flat).reshape((len(ks),) + storage.shape[1:])
 
@@ -363,7 +374,7 @@ def pca_project(storage: np.ndarray, V: np.ndarray, pmin: int, pmax: int) -> np.
     """p_acc[:, j] = H @ V[:, j] (matrix_multiply_complex, matrix_operations.cc:77-103), for j in [pmin, pmax]."""
     T = storage.shape[0]
     Hm = storage.reshape(T, -1).T
-    P = Hm @ V[:, pmin:pmax + 1]  # [HW, K]
+    P = Hm @ V[:, pmin:pmax + 1].astype(np.result_type(storage.dtype, np.complex64))  # [HW, K]
     return P.T.reshape((pmax - pmin + 1,) + storage.shape[1:])
 
 
@@ -751,6 +762,9 @@ class OracleSettings:
     filter2d_contrast_invert: bool = False
     filter2d_contrast_min: float = 1.0
     filter2d_contrast_max: float = 65535.0
+    # "fp64" (the oracle), or "fp32": the same equations in complex64 / float32 (the FP32 CPU
+    # baseline; FFTs in single precision, covariance and eigensolve in complex64)
+    precision: str = "fp64"
 
 
 @dataclass
@@ -852,13 +866,14 @@ class OraclePipe:
     def __init__(self, s: OracleSettings):
         self.s = s
         H, W = s.height, s.width
-        self.ring = Ring(s.time_transformation_size, (H, W))
+        self.cdtype = np.complex64 if s.precision == "fp32" else np.complex128
+        self.ring = Ring(s.time_transformation_size, (H, W), dtype=self.cdtype)
         self.batch_index = 0
         self.lens = None
         if s.space_transformation == "FRESNELTR":
-            self.lens = fresnel_lens(W, H, s.lam, s.z, s.pixel_size, s.lens_mode)
+            self.lens = fresnel_lens(W, H, s.lam, s.z, s.pixel_size, s.lens_mode).astype(self.cdtype)
         elif s.space_transformation == "ANGULARSP":
-            self.lens = angular_spectrum_lens(W, H, s.lam, s.z, s.pixel_size, s.lens_mode)
+            self.lens = angular_spectrum_lens(W, H, s.lam, s.z, s.pixel_size, s.lens_mode).astype(self.cdtype)
         self.f2d_mask = None
         if s.filter2d_enabled:
             m = filter2d_mask(W, H, s.filter2d_n1, s.filter2d_n2, s.filter2d_smooth_low, s.filter2d_smooth_high)
@@ -884,7 +899,7 @@ class OraclePipe:
         if self.batch_index != s.time_stride:
             return None
         self.batch_index = 0
-        frames = convert_frames(raw)
+        frames = convert_frames(raw).astype(self.cdtype, copy=False)
         self.frame0 = frames[0]
         frames = spatial_transform(frames, s.space_transformation, self.lens, self.f2d_mask)
         self.ring.enqueue_multiple(frames)

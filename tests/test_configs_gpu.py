@@ -1,0 +1,152 @@
+"""The benchmark workloads at their full sizes, end to end through the Pipe C ABI, against the FP64
+oracle (OraclePipe) on the same seeded interferograms.
+
+    cfg0  512 x 512 u16, angular spectrum + STFT, B = S = T = 16, K = 1, modulus, fftshift
+    cfg1  1024 x 1024 u8, Fresnel + PCA, B = S = T = 32, squared modulus of the 4 dominant components
+    cfg2  768 x 768 u16, angular spectrum + STFT, B = S = 64, T = 256, K = 33, A = 8, argument
+          (and argument + 2-D unwrap)
+    cfg3  512 x 512 u16, PCA T = 512, B = S = 64, 16 temporal modes (eigenvalues ~ k^-2)
+
+Bars: every output's float frame (the frame fed to the contrast stage) within rel-L2 <= 1e-4 of
+the oracle (argument without unwrap: wrapped angle differences above 1e-3 rad on < 0.5% of the
+pixels, the atan2 branch cut); uint16 bit-exact against the oracle's contrast stage run on the
+GPU's own float frame; the ring storage in slot order within rel-L2 <= 1e-4. The per-output errors
+are printed (pytest -s) so that each run reports them.
+
+cfg1 selects the 4 dominant of 32 components: the squared-modulus mean over the kept components is
+invariant to rotations inside the kept eigenspace, and the eigenvalue below the selection is 2.25x
+smaller than the smallest kept one on these frames, so the view is well conditioned.
+
+cfg3 also reports the covariance of the Pipe's own ring from the split-BF16 tensor-core engine and
+the FP32 SIMT engine against FP64, and every eigenvalue of the Pipe's eigensolver against FP64
+(LAPACK on the oracle's FP64 covariance of the same ring)."""
+
+import numpy as np
+import pytest
+
+import holovibes_oracle as O
+from gpu_util import call, dev, empty, host, oracle_settings, ptr, rel_l2, wrapped_diff
+
+import holovibes_gb300 as hv
+from holovibes_gb300.synthetic import CONFIGS, generator, settings_for
+
+
+def _run(name, nbatches, seed=1234, **over):
+    """Pushes `nbatches` batches of the workload through the Pipe and the oracle; checks every
+    output; returns (pipe, oracle, hv settings, list of per-output errors). The pipe is open."""
+    c = CONFIGS[name]
+    fd = hv.FrameDescriptor(c["width"], c["height"], c["depth"])
+    s = settings_for(name, **over).validate(fd)
+    B = s.batch_size
+    gen = generator(name, seed=seed)
+    oracle = O.OraclePipe(oracle_settings(fd, s))
+    pipe = hv.Pipe(fd, s)
+    errs = []
+    for b in range(nbatches):
+        raw = gen.frames(b * B, B)
+        ref = oracle.process_batch(raw)
+        pipe.enqueue(raw)
+        if ref is None:
+            assert pipe.output_count() == 0, (name, b)
+            continue
+        assert pipe.output_count() == 1, (name, b)
+        got_u16 = pipe.pull()
+        got_f = pipe.float_frame()
+        if s.image_type == hv.IMG_ARGUMENT and not s.unwrap_2d:
+            wd = wrapped_diff(got_f, ref.float_frame)
+            cut = np.abs(wd) > 1e-3
+            frac = float(np.mean(cut))
+            err = float(np.linalg.norm(wd[~cut]) / np.linalg.norm(ref.float_frame[~cut]))
+            assert frac < 5e-3, (name, b, frac)
+            assert err <= 1e-4, (name, b, err)
+            errs.append({"batch": b, "branch_cut_fraction": frac, "rel_l2_off_cut": err})
+        else:
+            err = rel_l2(got_f, ref.float_frame)
+            errs.append({"batch": b, "rel_l2": err})
+            assert err <= 1e-4, (name, b, err)
+        if ref.autocontrast_applied:
+            expected = O.autocontrast(got_f, s.contrast_lower, s.contrast_upper)
+        else:
+            expected = pipe.contrast_range()
+        crange = pipe.contrast_range()
+        assert np.float32(crange[0]) == np.float32(expected[0]), name
+        assert np.float32(crange[1]) == np.float32(expected[1]), name
+        ref_u16 = O.float_to_ushort(O.apply_contrast(got_f, crange[0], crange[1], bool(s.contrast_invert)))
+        mism = int(np.count_nonzero(got_u16 != ref_u16))
+        errs[-1]["u16_mismatch"] = mism
+        assert mism == 0, (name, b, mism)
+    assert errs, name
+    ring, start, size = pipe.ring()
+    assert (start, size) == (oracle.ring.start, oracle.ring.size), name
+    ring_err = rel_l2(ring, oracle.ring.data)
+    assert ring_err <= 1e-4, (name, ring_err)
+    print(f"\n{name} {over or ''}: ring rel-L2 {ring_err:.2e}; outputs {errs}")
+    return pipe, oracle, s, errs
+
+
+@pytest.mark.gpu
+def test_cfg0_full_size(cuda):
+    pipe, *_ = _run("cfg0", 3)
+    pipe.close()
+
+
+@pytest.mark.gpu
+def test_cfg1_full_size(cuda):
+    pipe, oracle, s, _ = _run("cfg1", 2)
+    pipe.close()
+    # the selection edge: the largest dropped eigenvalue against the smallest kept one
+    w, _ = O.pca_eigh(O.pca_covariance(oracle.ring.data))
+    T = s.time_transformation_size
+    assert w[s.p_start - 1] < 0.8 * w[s.p_start], (w[s.p_start - 1], w[s.p_start])
+    assert s.p_start + s.p_width == T - 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("unwrap", [0, 1])
+def test_cfg2_full_size(cuda, unwrap):
+    pipe, *_ = _run("cfg2", 6, unwrap_2d=unwrap)
+    pipe.close()
+
+
+@pytest.mark.gpu
+def test_cfg3_full_size_and_eigenvalues(cuda):
+    pipe, oracle, s, _ = _run("cfg3", 8)
+    ring, _, _ = pipe.ring()
+    pipe.close()
+    T = s.time_transformation_size
+    npix = ring.shape[1] * ring.shape[2]
+    cov_ref = O.pca_covariance(ring.astype(np.complex128))  # FP64 covariance of the Pipe's own ring
+    rd = dev(ring)
+    report = {}
+    covs = {}
+    for mode, label, tol in ((2, "bf16x3 tensor cores", 2e-5), (1, "fp32 SIMT", 1e-6)):
+        cov = empty(T * T * 16)
+        work = empty(hv.lib().hv_pca_cov_workspace(T, npix))
+        hv.lib().hv_pca_covariance_mode(mode)
+        try:
+            call("hv_pca_covariance", ptr(rd), T, npix, ptr(cov), ptr(work), None)
+            cuda.cuda.synchronize()
+            assert hv.lib().hv_pca_covariance_status(ptr(work)) == hv.HV_OK
+        finally:
+            hv.lib().hv_pca_covariance_mode(0)
+        got = host(cov, np.complex128, (T, T))
+        covs[mode] = got
+        report[label] = rel_l2(got, cov_ref)
+        assert report[label] <= tol, (label, report[label])
+    # the Pipe's eigensolver (default precision) on the tensor-core covariance, against LAPACK on
+    # the FP64 covariance of the oracle's ring
+    evals = empty(T * 8)
+    evecs = empty(T * T * 16)
+    ew = empty(hv.lib().hv_pca_eigh_workspace(T))
+    call("hv_pca_eigh", ptr(dev(covs[2])), T, ptr(evals), ptr(evecs), 0, 0, None, ptr(ew), None)
+    got_w = host(evals, np.float64, (T,))
+    ref_w, _ = O.pca_eigh(O.pca_covariance(oracle.ring.data))
+    wmax = float(np.abs(ref_w).max())
+    rel = np.abs(got_w - ref_w) / np.maximum(np.abs(ref_w), 1e-300)
+    top = ref_w >= 1e-3 * wmax
+    report["eigenvalue abs err / max"] = float(np.abs(got_w - ref_w).max() / wmax)
+    report["eigenvalue rel err (>= 1e-3 max)"] = float(rel[top].max())
+    report["eigenvalues >= 1e-3 max"] = int(top.sum())
+    print(f"\ncfg3 covariance and eigenvalues vs FP64: {report}")
+    assert report["eigenvalue abs err / max"] <= 5e-5
+    assert report["eigenvalue rel err (>= 1e-3 max)"] <= 1e-2
