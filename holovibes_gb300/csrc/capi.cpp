@@ -311,8 +311,10 @@ hv_status hv_pca_eigh(void* cov_c128, int T, double* eigenvalues, void* eigenvec
         return HV_INVALID_VALUE;
     if (weights_c64 && (pmin < 0 || pmax < pmin || pmax >= T))
         return HV_INVALID_VALUE;
+    // the eigenvectors of ranks pmin..pmax (when that range is valid) are refined in FP64
+    const bool range = pmin >= 0 && pmax >= pmin && pmax < T;
     return pca_eigh(static_cast<double2*>(cov_c128), T, eigenvalues, static_cast<double2*>(eigenvectors_c128), pmin,
-                    pmax, static_cast<float2*>(weights_c64), work, S(stream));
+                    pmax, static_cast<float2*>(weights_c64), work, S(stream), range ? pmin : 0, range ? pmax : -1);
 }
 
 size_t hv_pca_eigh_workspace(int T) { return pca_eigh_workspace(T); }

@@ -6,8 +6,9 @@
 // Formulation: Y is the 2T x HW real matrix with rows 2t = Re(ring[t]) and 2t+1 = Im(ring[t]);
 // G = Y Y^T (2T x 2T) gives C_re[i][j] = G[2i][2j] + G[2i+1][2j+1] and
 // C_im[i][j] = G[2i][2j+1] - G[2i+1][2j]. Each FP32 sample is split y = yh + yl with yh, yl in
-// BF16, and G ~= Yh Yh^T + Yh Yl^T + Yl Yh^T (the Yl Yl^T term is below FP32 resolution), so
-// three BF16 MMAs with FP32 accumulation per K step recover ~16-bit-mantissa accuracy.
+// BF16, and G ~= Yh Yh^T + Yh Yl^T + Yl Yh^T (+ Yl Yl^T where it is free: the packed form for
+// 2T <= 64), so three (four) BF16 MMAs with FP32 accumulation per K step recover ~16-bit-mantissa
+// accuracy.
 //
 // Kernel: one CTA per SM walks a contiguous range of 64-pixel chunks (K slices of Y):
 //   warp 17    loader: one 2-D tensor copy (TMA) per pair of chunks (T x 128 complex samples, rows
@@ -225,7 +226,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc(const __grid_constant_
         const int r = warp * 32 + lane;
         if (packed)
         {
-            // partial layout [128][64]: row i < 64 holds Yh Yh^T + Yh Yl^T, row 64 + i holds Yl Yh^T
+            // partial layout [128][64]: row i < 64 holds Yh Yh^T + Yh Yl^T, row 64 + i holds
+            // Yl Yh^T + Yl Yl^T (the packed MMA computes all four blocks, so the fourth product
+            // costs nothing here: with it, samples whose hi + lo split is exact, such as integer
+            // camera values below 2^16, give exact products before the FP32 accumulation)
             float* dstp = part + static_cast<size_t>(blockIdx.x) * TC_ROWS * 64 + static_cast<size_t>(r) * 64;
             for (int c0 = 0; c0 < 64; c0 += 16)
             {
@@ -236,8 +240,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc(const __grid_constant_
 #pragma unroll
                 for (int i = 0; i < 16; ++i)
                 {
-                    if (r < 64)
-                        v[i] += w1[i];
+                    v[i] += w1[i];
                     dstp[c0 + i] = nmine ? v[i] : 0.f;
                 }
             }

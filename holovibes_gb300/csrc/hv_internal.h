@@ -85,8 +85,10 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
 hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st);
 size_t pca_eigh_workspace(int T);
 void set_eig_precision(int p);
+// Eigenvectors of ranks refine_lo..refine_hi (at most 64 of them) are refined in FP64 after FP32
+// sweeps; an empty range (refine_hi < refine_lo) keeps the FP32 vectors.
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
-                   cudaStream_t st);
+                   cudaStream_t st, int refine_lo, int refine_hi);
 
 // view_tc.cu
 bool view_tc_supported(int K);

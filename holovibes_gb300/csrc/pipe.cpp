@@ -442,8 +442,12 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
         // not gated by the block: served PCA / SSA_STFT cycles are launched eagerly (render cycles only)
         if ((r = pca_covariance(p->ring, p->T, p->HW, p->cov, p->cov_work, st)) != HV_OK)
             return r;
+        // refined in FP64: the viewed components (PCA) or the kept range of SSA_STFT (all columns
+        // kept: the projector is the identity, nothing to refine)
+        const int rlo = pca ? p->pmin : p->qmin;
+        const int rhi = pca ? p->pmax : (p->qn < p->T ? p->qmin + p->qn - 1 : -1);
         if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, pca ? p->weights : nullptr,
-                          p->eig_work, st)) != HV_OK)
+                          p->eig_work, st, rlo, rhi)) != HV_OK)
             return r;
         if (!pca && (r = ssa_weights(p->evecs, p->T, p->qmin, p->qn, p->pmin, p->K, p->weights, st)) != HV_OK)
             return r;

@@ -18,6 +18,7 @@
 #include <math.h>
 
 #include <mutex>
+#include <string>
 
 #include "hv_common.cuh"
 #include "hv_internal.h"
@@ -224,7 +225,10 @@ hv_status unwrap_2d(const float* in, float* out, int W, int H, void* work, cudaS
 // forbids cudaMalloc once streaming has started. hv_unwrap_2d_noalloc serves them: its scratch
 // (four complex frames and the min/max keys, the same layout hv_unwrap_2d takes from `work`) is
 // this file-scope device array, sized for frames of at most HV_UNWRAP_NOALLOC_MAX_PIXELS pixels.
-// Every GPU that loads the library keeps the array (8 MiB) until the process exits.
+// Every GPU that loads the library keeps the array (8 MiB) until the process exits. With CUDA's
+// lazy module loading the driver creates the array (and this module's other device data) when
+// one of the module's kernels first runs on a device, so the first call on each device is the
+// one that may allocate inside the driver: make it before streaming starts.
 
 constexpr size_t kUnwrapNoallocMaxPixels = HV_UNWRAP_NOALLOC_MAX_PIXELS;
 static __device__ __align__(256) float2 g_unwrap_scratch[4 * kUnwrapNoallocMaxPixels + 32];
@@ -237,16 +241,26 @@ void* g_scratch_ptr[kMaxDevices] = {};
 
 hv_status unwrap_2d_noalloc(const float* in, float* out, int W, int H, cudaStream_t st)
 {
-    const size_t n = static_cast<size_t>(W) * H;
-    if (W <= 0 || H <= 0 || n > kUnwrapNoallocMaxPixels)
+    if (W <= 0 || H <= 0)
     {
-        set_last_error_msg("hv_unwrap_2d_noalloc: frame larger than the 262144-pixel static scratch");
+        set_last_error_msg("hv_unwrap_2d_noalloc: width and height must be positive");
+        return HV_INVALID_VALUE;
+    }
+    const size_t n = static_cast<size_t>(W) * H;
+    if (n > kUnwrapNoallocMaxPixels)
+    {
+        set_last_error_msg(("hv_unwrap_2d_noalloc: the frame's " + std::to_string(n) +
+                            " pixels exceed the 262144-pixel static scratch").c_str());
         return HV_INVALID_VALUE;
     }
     int dev = 0;
     HV_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices)
+    {
+        set_last_error_msg(("hv_unwrap_2d_noalloc: device index " + std::to_string(dev) +
+                            " beyond the 64 devices this entry point serves").c_str());
         return HV_INVALID_VALUE;
+    }
     void* ptr = nullptr;
     {
         // set-up on the first call on each device (with that device current): the host-side name

@@ -666,6 +666,18 @@ struct JacScratch
     short2 blk[(JS_MAX_T / 2) * (JS_MAX_T / 2 + 1) / 2];
 };
 
+// Power of two that brings the largest diagonal entry of a Hermitian positive semi-definite matrix
+// (its largest entry in magnitude) near 1: the FP32 sweeps square entries (|a_pq|^2, a_pp a_qq),
+// which overflow for covariances of large frames (1024 x 1024 pixels of 8-bit data scaled by 257
+// give entries near 1e22). Scaling by a power of two changes no eigenvector and no relative
+// rounding. 1 for a zero or non-finite maximum.
+__device__ __forceinline__ double jac_scale(double max_diag)
+{
+    if (!(max_diag > 0.0) || !isfinite(max_diag))
+        return 1.0;
+    return ldexp(1.0, -ilogb(max_diag));
+}
+
 // Rotation annihilating a_pq of the 2 x 2 Hermitian block [[app, apq], [conj(apq), aqq]] when |apq|
 // exceeds the relative threshold thr * sqrt(|app aqq|) and `floor` (and is not 0); returns false (identity)
 // otherwise. The FP32 form uses reciprocal square roots and one division (the sweeps only need an
@@ -878,12 +890,26 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
     Cx<R>* A = js;
     Cx<R>* V = js + T * LD;
     __shared__ JacScratch<R> sc;
+    __shared__ double s_scale;
     const int tid = threadIdx.x;
+    if (tid < 32)
+    {
+        double m = 0.0;
+        for (int i = tid; i < T; i += 32)
+            m = fmax(m, fabs(Ain[static_cast<size_t>(i) * T + i].x));
+        for (int o = 16; o > 0; o >>= 1)
+            m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (tid == 0)
+            s_scale = jac_scale(m);
+    }
+    __syncthreads();
+    // the sweeps run on 2^-e A (exact scaling): the squares of the entries stay finite in FP32
+    const double scale = s_scale;
     for (int e = tid; e < T * T; e += JS_THREADS)
     {
         const int i = e / T, j = e % T;
         const double2 a = Ain[e];
-        A[i * LD + j] = {static_cast<R>(a.x), static_cast<R>(i == j ? 0.0 : a.y)};
+        A[i * LD + j] = {static_cast<R>(a.x * scale), static_cast<R>(i == j ? 0.0 : a.y * scale)};
         V[i * LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
     }
     __syncthreads();
@@ -895,7 +921,7 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
         Vout[e] = make_double2(static_cast<double>(V[i * LD + j].x), static_cast<double>(V[i * LD + j].y));
     }
     for (int i = tid; i < T; i += JS_THREADS)
-        evals[i] = static_cast<double>(A[i * LD + i].x);
+        evals[i] = static_cast<double>(A[i * LD + i].x) / scale;
 }
 
 // Grid-wide kernels (64 < T <= JC_MAX_T) synchronise through a bounded sense-reversal barrier: a
@@ -1073,13 +1099,30 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
     const size_t gsz = static_cast<size_t>(gridDim.x) * BJ_THREADS;
     const size_t TT = static_cast<size_t>(Tp) * Tp;
     const int nblk = Tp / BJ_B, npb = nblk / 2;
+    // the sweeps run on 2^-e A (exact scaling, every CTA derives the same factor): FP32 squares of
+    // the entries stay finite
+    __shared__ double s_scale;
+    if (tid < 32)
+    {
+        double m = 0.0;
+        for (int i = tid; i < T; i += 32)
+            m = fmax(m, fabs(Ain[static_cast<size_t>(i) * T + i].x));
+        for (int o = 16; o > 0; o >>= 1)
+            m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (tid == 0)
+            s_scale = jac_scale(m);
+    }
+    __syncthreads();
+    const double scale = s_scale;
     // the squared Frobenius norm is summed on the way (FP64, one atomic per CTA into fro2)
     __shared__ double s_fro[BJ_THREADS / 32];
     double fro = 0.0;
     for (size_t e = gtid; e < TT; e += gsz)
     {
         const int i = static_cast<int>(e / Tp), j = static_cast<int>(e % Tp);
-        const double2 a = (i < T && j < T) ? Ain[static_cast<size_t>(i) * T + j] : make_double2(0.0, 0.0);
+        double2 a = (i < T && j < T) ? Ain[static_cast<size_t>(i) * T + j] : make_double2(0.0, 0.0);
+        a.x *= scale;
+        a.y *= scale;
         fro += a.x * a.x + (i == j ? 0.0 : a.y * a.y);
         A0[e] = {static_cast<R>(a.x), static_cast<R>(i == j ? 0.0 : a.y)};
         V0[e] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
@@ -1240,7 +1283,7 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
         Vout[e] = make_double2(static_cast<double>(v.x), static_cast<double>(v.y));
     }
     for (size_t i = gtid; i < static_cast<size_t>(T); i += gsz)
-        evals[i] = static_cast<double>(ldcg(A + i * Tp + i).x);
+        evals[i] = static_cast<double>(ldcg(A + i * Tp + i).x) / scale;
 }
 
 
@@ -1328,15 +1371,172 @@ __global__ void k_eig_sort(const double* evals_in, const double2* V, int T, doub
     }
 }
 
+// ------------------------------------------------------------------ FP64 eigenvector refinement
+// The FP32 sweeps leave each eigenvector with an error of the FP32 round-off of the matrix over
+// the eigenvalue gap: when the gap is small against the largest eigenvalue (a dominant mean
+// component, or close pairs of temporal modes), the kept components mix with their neighbours by
+// up to 1e-3. The kept eigenvectors (ranks r0 .. r0 + K - 1, after the sort) are corrected in FP64
+// against the FP64 covariance C with the first-order residual correction
+//     lambda_j = v_j^H C v_j / v_j^H v_j,  r_j = C v_j - lambda_j v_j,
+//     v_j <- v_j + sum_{i != j} v_i (v_i^H r_j) / (lambda_j - lambda_i),
+// then normalised: an error of angle theta towards another eigenvector becomes O(theta^3) (and
+// O(theta^2) against the FP32 error of the basis). Pairs closer than 1e-12 of the largest
+// eigenvalue are numerically degenerate and left as they are. Kernels: y_j = C v_j (one warp per
+// row), D = V^H Y and G = V^H V_kept (one warp per entry), the update (one thread per row), the
+// normalisation (one CTA per kept vector).
+constexpr int ER_MAX_K = 64;  // kept eigenvectors refined at most (wider ranges keep the FP32 vectors)
+
+__device__ __forceinline__ double2 cfma_conj(double2 a, double2 b, double2 acc)
+{
+    // acc + conj(a) b
+    acc.x += a.x * b.x + a.y * b.y;
+    acc.y += a.x * b.y - a.y * b.x;
+    return acc;
+}
+
+__device__ __forceinline__ double2 warp_sum2(double2 v)
+{
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+// Y[j][t] = sum_s C[t][s] v_{r0+j}[s]; grid (ceil(T / 8), K), 256 threads
+__global__ void k_eigref_matvec(const double2* __restrict__ C, const double2* __restrict__ evecs, int T, int r0,
+                                double2* __restrict__ Y)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * 8 + warp, j = blockIdx.y;
+    if (t >= T)
+        return;
+    const double2* v = evecs + static_cast<size_t>(r0 + j) * T;
+    const double2* c = C + static_cast<size_t>(t) * T;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int s2 = lane; s2 < T; s2 += 32)
+    {
+        const double2 a = c[s2], x = v[s2];
+        acc.x += a.x * x.x - a.y * x.y;
+        acc.y += a.x * x.y + a.y * x.x;
+    }
+    acc = warp_sum2(acc);
+    if (lane == 0)
+        Y[static_cast<size_t>(j) * T + t] = acc;
+}
+
+// D[j][i] = v_i^H Y[j], G[j][i] = v_i^H v_{r0+j}; grid (ceil(T / 8), K), 256 threads
+__global__ void k_eigref_project(const double2* __restrict__ evecs, const double2* __restrict__ Y, int T, int r0,
+                                 double2* __restrict__ D, double2* __restrict__ G)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 8 + warp, j = blockIdx.y;
+    if (i >= T)
+        return;
+    const double2* vi = evecs + static_cast<size_t>(i) * T;
+    const double2* vj = evecs + static_cast<size_t>(r0 + j) * T;
+    const double2* y = Y + static_cast<size_t>(j) * T;
+    double2 d = make_double2(0.0, 0.0), g = make_double2(0.0, 0.0);
+    for (int t = lane; t < T; t += 32)
+    {
+        const double2 a = vi[t];
+        d = cfma_conj(a, y[t], d);
+        g = cfma_conj(a, vj[t], g);
+    }
+    d = warp_sum2(d);
+    g = warp_sum2(g);
+    if (lane == 0)
+    {
+        D[static_cast<size_t>(j) * T + i] = d;
+        G[static_cast<size_t>(j) * T + i] = g;
+    }
+}
+
+// Rayleigh quotient of kept vector k (0-based in the kept range)
+__device__ __forceinline__ double eigref_lambda(const double2* D, const double2* G, int T, int r0, int k)
+{
+    const size_t e = static_cast<size_t>(k) * T + r0 + k;
+    return D[e].x / G[e].x;
+}
+
+// Vn[j][t] = v_j[t] + sum_{i != j} v_i[t] (D[j][i] - lambda_j G[j][i]) / (lambda_j - lambda_i);
+// grid (ceil(T / 128), K), 128 threads (thread = row t: the loads of v_i[t] are coalesced)
+__global__ void k_eigref_update(const double2* __restrict__ evecs, const double* __restrict__ evals,
+                                const double2* __restrict__ D, const double2* __restrict__ G, int T, int r0, int K,
+                                double2* __restrict__ Vn)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (t >= T)
+        return;
+    // pairs closer than 1e-12 of the largest eigenvalue (the last in ascending order) stay mixed
+    const double degenerate = 1e-12 * fabs(evals[T - 1]);
+    const int rj = r0 + j;
+    const double lj = eigref_lambda(D, G, T, r0, j);
+    const double2* Dj = D + static_cast<size_t>(j) * T;
+    const double2* Gj = G + static_cast<size_t>(j) * T;
+    double2 acc = evecs[static_cast<size_t>(rj) * T + t];
+    for (int i = 0; i < T; ++i)
+    {
+        if (i == rj)
+            continue;
+        const double li = (i >= r0 && i < r0 + K) ? eigref_lambda(D, G, T, r0, i - r0) : evals[i];
+        const double gap = lj - li;
+        if (!(fabs(gap) > degenerate))
+            continue;
+        const double2 d = Dj[i], g = Gj[i];
+        const double cx = (d.x - lj * g.x) / gap, cy = (d.y - lj * g.y) / gap;
+        const double2 v = evecs[static_cast<size_t>(i) * T + t];
+        acc.x += v.x * cx - v.y * cy;
+        acc.y += v.x * cy + v.y * cx;
+    }
+    Vn[static_cast<size_t>(j) * T + t] = acc;
+}
+
+// Normalise the corrected vectors into evecs (column r0 + j), their eigenvalues (the Rayleigh
+// quotients of the vectors before the correction, second order in their error) and, for ranks
+// pmin..pmax, the complex64 PCA weights. One CTA (128 threads) per kept vector.
+__global__ void k_eigref_finish(double2* __restrict__ evecs, double* __restrict__ evals, const double2* __restrict__ Vn,
+                                const double2* __restrict__ D, const double2* __restrict__ G, int T, int r0, int pmin,
+                                int pmax, float2* __restrict__ weights)
+{
+    __shared__ double red[4];
+    const int j = blockIdx.x, tid = threadIdx.x, rj = r0 + j;
+    const double2* v = Vn + static_cast<size_t>(j) * T;
+    double n2 = 0.0;
+    for (int t = tid; t < T; t += blockDim.x)
+        n2 += v[t].x * v[t].x + v[t].y * v[t].y;
+    for (int o = 16; o > 0; o >>= 1)
+        n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+    if ((tid & 31) == 0)
+        red[tid >> 5] = n2;
+    __syncthreads();
+    const double inv = 1.0 / sqrt(red[0] + red[1] + red[2] + red[3]);
+    for (int t = tid; t < T; t += blockDim.x)
+    {
+        const double2 x = make_double2(v[t].x * inv, v[t].y * inv);
+        evecs[static_cast<size_t>(rj) * T + t] = x;
+        if (weights && rj >= pmin && rj <= pmax)
+            weights[static_cast<size_t>(rj - pmin) * T + t] = make_float2(static_cast<float>(x.x), static_cast<float>(x.y));
+    }
+    if (tid == 0)
+        evals[rj] = eigref_lambda(D, G, T, r0, j);
+}
+
 static std::atomic<int> g_eig_precision{HV_EIG_FP32};
 
 void set_eig_precision(int p) { g_eig_precision = p; }
+
+// bytes of the refinement buffers (Y, D, G, Vn: ER_MAX_K x T complex128 each) at the start of the
+// workspace tail
+static size_t eigref_bytes(int T) { return 4 * static_cast<size_t>(ER_MAX_K) * T * sizeof(double2) + 512; }
 
 size_t pca_eigh_workspace(int T)
 {
     const int Tp = (T % 2) ? T + 1 : T;
     size_t bytes = static_cast<size_t>(T) * T * sizeof(double2) + static_cast<size_t>(2 * Tp) * sizeof(double) +
-                   static_cast<size_t>(T) * sizeof(double) + static_cast<size_t>(Tp) * sizeof(int) + 256;
+                   static_cast<size_t>(T) * sizeof(double) + static_cast<size_t>(Tp) * sizeof(int) + 256 +
+                   eigref_bytes(T);
     if (T > JS_MAX_T && T <= JC_MAX_T)
     {
         // block Jacobi: FP32 A and V (two copies each) of the size rounded up to 64, the step's
@@ -1348,7 +1548,7 @@ size_t pca_eigh_workspace(int T)
 }
 
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
-                   cudaStream_t st)
+                   cudaStream_t st, int refine_lo, int refine_hi)
 {
     if (T <= 0 || !work)
         return HV_INVALID_VALUE;
@@ -1362,6 +1562,9 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     double* ev_unsorted = reinterpret_cast<double*>(base + off);
     off += static_cast<size_t>(T) * sizeof(double);
     int* pairs = reinterpret_cast<int*>(base + off);
+    // refinement buffers: after the pair list, before the block-Jacobi arrays
+    char* er_base = base + ((off + static_cast<size_t>(Tp) * sizeof(int) + 255) & ~static_cast<size_t>(255));
+    off += eigref_bytes(T);
     if (T <= JS_MAX_T && prec == HV_EIG_FP32)
     {
         const size_t smem = 2 * static_cast<size_t>(T) * (T + 1) * sizeof(float2);
@@ -1430,6 +1633,26 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     k_eig_sort<<<T, 128, 0, st>>>(ev_unsorted, V, T, evals, evecs, pmin, pmax, weights);
     HV_LAUNCH_CHECK();
     count_launch(2);
+    // FP32 sweeps: the kept eigenvectors are corrected in FP64 (FP64 sweeps need no correction)
+    const bool fp32_sweeps = T <= JS_MAX_T ? prec == HV_EIG_FP32 : (T <= JC_MAX_T && prec == HV_EIG_FP32);
+    const int K = refine_hi - refine_lo + 1;
+    if (fp32_sweeps && refine_lo >= 0 && refine_hi < T && K >= 1 && K <= ER_MAX_K)
+    {
+        double2* Y = reinterpret_cast<double2*>(er_base);
+        double2* D = Y + static_cast<size_t>(ER_MAX_K) * T;
+        double2* G = D + static_cast<size_t>(ER_MAX_K) * T;
+        double2* Vn = G + static_cast<size_t>(ER_MAX_K) * T;
+        const dim3 gw((T + 7) / 8, K), gt((T + 127) / 128, K);
+        k_eigref_matvec<<<gw, 256, 0, st>>>(cov, evecs, T, refine_lo, Y);
+        HV_LAUNCH_CHECK();
+        k_eigref_project<<<gw, 256, 0, st>>>(evecs, Y, T, refine_lo, D, G);
+        HV_LAUNCH_CHECK();
+        k_eigref_update<<<gt, 128, 0, st>>>(evecs, evals, D, G, T, refine_lo, K, Vn);
+        HV_LAUNCH_CHECK();
+        k_eigref_finish<<<K, 128, 0, st>>>(evecs, evals, Vn, D, G, T, refine_lo, pmin, pmax, weights);
+        HV_LAUNCH_CHECK();
+        count_launch(4);
+    }
     return HV_OK;
 }
 

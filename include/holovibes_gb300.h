@@ -420,8 +420,10 @@ size_t hv_unwrap_workspace(int width, int height);
  * allocating library routine. Its scratch is a static device array inside the library, sized for
  * frames of at most HV_UNWRAP_NOALLOC_MAX_PIXELS pixels; larger frames fail with HV_INVALID_VALUE.
  * Every GPU that loads the library keeps that array (8 MiB) until the process exits.
- * The first call on each device looks up the array's device address (with that device current);
- * make that first call before any stream capture. All calls share the one array: calls whose GPU
+ * The first call on each device looks up the array's device address (with that device current),
+ * and under CUDA's lazy module loading it is also when the driver creates the array on that
+ * device: make that first call before streaming starts (and before any stream capture); later
+ * calls allocate nothing. All calls share the one array: calls whose GPU
  * work overlaps (different streams, or different host threads) race and corrupt each other's
  * results, so serialise them on one stream. Results match hv_unwrap_2d. */
 #define HV_UNWRAP_NOALLOC_MAX_PIXELS 262144

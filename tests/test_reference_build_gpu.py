@@ -33,8 +33,10 @@ import ref_pipe  # noqa: E402
 
 pytestmark = pytest.mark.skipif(not ref_pipe.available(), reason="reference build sources are not staged")
 
-# float frame bars, reference build against the FP64 oracle and against the product
-BARS = {"STFT": 1e-4, "PCA": 2e-4}
+# float frame bars, reference build against the FP64 oracle and against the product; the 2-D
+# unwrap spreads branch-cut flips of the argument over the frame (the reference's own build is
+# 2.9e-4 from the FP64 oracle on the cfg2 frames)
+BARS = {"STFT": 1e-4, "PCA": 1e-4, "UNWRAP": 2e-3}
 
 
 def _f32_fma(a, b, c):
@@ -114,7 +116,7 @@ def _reference_cycle_compare(name, nbatches, **over):
     gen = generator(name, seed=1234)
     B = s.batch_size
     argument = s.image_type == hv.IMG_ARGUMENT and not s.unwrap_2d
-    bar = BARS["PCA" if s.time_transformation == hv.TIME_PCA else "STFT"]
+    bar = BARS["UNWRAP" if s.unwrap_2d else "PCA" if s.time_transformation == hv.TIME_PCA else "STFT"]
     rows = []
     for b in range(nbatches):
         raw = gen.frames(b * B, B)
