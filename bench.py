@@ -606,23 +606,39 @@ def run_ours(args):
     host_out = torch.empty(HW * 2, dtype=torch.uint8).pin_memory()
     while pipe.output_count():
         pipe.pull_into(host_out.data_ptr(), hv.MEM_HOST)
-    # acquisition-style loop with one batch in flight: push batch i (its H2D copy), then read the
-    # hologram of batch i-1 back to the host (D2H); latency = push start -> hologram on the host
+    # acquisition-style loop: the caller's thread pushes every batch from pinned memory (its H2D
+    # copy) as the camera would deliver it, and a consumer thread reads each hologram back to the
+    # host (D2H) as soon as it is ready; latency = push start -> hologram on the host. With
+    # stride == batch every batch renders one window, so there are as many holograms as batches.
     lat = []
     e2e_steps = args.steps
+    pushed = [0.0] * e2e_steps
     if world > 1:
         torch.distributed.barrier()
-    pushed = []
+    errors = []
+
+    def consume():
+        try:
+            deadline = time.perf_counter() + 60.0
+            for k in range(e2e_steps):
+                while pipe.output_count() == 0:  # not yet enqueued by the pushing thread
+                    if time.perf_counter() > deadline:
+                        raise TimeoutError("no hologram within 60 s")
+                    time.sleep(0)
+                pipe.pull_into(host_out.data_ptr(), hv.MEM_HOST, timeout_us=30_000_000)
+                lat.append(time.perf_counter() - pushed[k])
+        except Exception as e:  # reported after the join
+            errors.append(e)
+
+    consumer = threading.Thread(target=consume)
     t0 = time.perf_counter()
+    consumer.start()
     for i in range(e2e_steps):
-        pushed.append(time.perf_counter())
+        pushed[i] = time.perf_counter()
         pipe.enqueue_ptr(host_in[i % nb_unique].data_ptr(), B, hv.MEM_HOST)
-        while pipe.output_count() > 1:
-            pipe.pull_into(host_out.data_ptr(), hv.MEM_HOST)
-            lat.append(time.perf_counter() - pushed.pop(0))
-    while pipe.output_count():
-        pipe.pull_into(host_out.data_ptr(), hv.MEM_HOST)
-        lat.append(time.perf_counter() - pushed.pop(0))
+    consumer.join()
+    if errors:
+        raise errors[0]
     pipe.sync()
     t_e2e_ms, e2e_value = replica_throughput((time.perf_counter() - t0) * 1e3, e2e_steps * B, world)
     lat_ms = np.array(lat) * 1e3 if lat else np.array([float("nan")])

@@ -588,17 +588,30 @@ struct TiledPlan
     size_t chunks_per_split;
 };
 
+// Longest accumulation chain (64-pixel chunks, 4 MMA K-steps each) one TMEM accumulator takes.
+// The FP32 accumulation of a tcgen05.mma into its accumulator does not round to nearest: summing
+// 262144 pixels (4096 K-steps) into one accumulator drifted by 3.4e-4 relative to the FP64 sum on
+// 512 x 512 frames (measured), about one unit of the last place per step in one direction; with
+// chains of 64 chunks the drift was 1e-5 (a uniform scale: 9e-7 left after it). The partial tiles
+// are summed in FP64. The packed kernel (T <= 32) keeps one wave up to 128 chunks per CTA (1024 x
+// 1024 frames: 108), where its extra waves cost more time than the drift costs accuracy.
+constexpr size_t kMaxChainChunks = 64;
+constexpr size_t kMaxChainChunksPacked = 128;
+
 TiledPlan tiled_plan(int T, size_t npix)
 {
     TiledPlan p;
     p.nb = (T + TT_FRAMES - 1) / TT_FRAMES;
     p.npairs = p.nb * (p.nb + 1) / 2;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    int ns = sm_count() / p.npairs;  // one wave of persistent CTAs
+    size_t ns = static_cast<size_t>(sm_count() / p.npairs);  // one wave of persistent CTAs
     if (ns < 1)
         ns = 1;
-    if (static_cast<size_t>(ns) > nchunks)
-        ns = static_cast<int>(nchunks);
+    const size_t min_ns = (nchunks + kMaxChainChunks - 1) / kMaxChainChunks;
+    if (ns < min_ns)
+        ns = min_ns;
+    if (ns > nchunks)
+        ns = nchunks;
     p.chunks_per_split = (nchunks + ns - 1) / ns;
     p.nsplit = static_cast<int>((nchunks + p.chunks_per_split - 1) / p.chunks_per_split);
     return p;
@@ -629,7 +642,13 @@ TcPlan tc_plan(int T, size_t npix)
 {
     TcPlan p;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    int ctas = sm_count();  // one persistent CTA per SM
+    // one persistent CTA per SM, or whole waves of them when a CTA's chain would exceed the limit
+    const size_t sms = static_cast<size_t>(sm_count());
+    const size_t chain = 2 * T <= 64 ? kMaxChainChunksPacked : kMaxChainChunks;
+    size_t waves = (nchunks + sms * chain - 1) / (sms * chain);
+    if (waves < 1)
+        waves = 1;
+    int ctas = static_cast<int>(sms * waves);
     if (static_cast<size_t>(ctas) > nchunks)
         ctas = static_cast<int>(nchunks);
     if (ctas < 1)

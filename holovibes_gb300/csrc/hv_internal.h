@@ -86,9 +86,11 @@ hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, v
 size_t pca_eigh_workspace(int T);
 void set_eig_precision(int p);
 // Eigenvectors of ranks refine_lo..refine_hi (at most 64 of them) are refined in FP64 after FP32
-// sweeps; an empty range (refine_hi < refine_lo) keeps the FP32 vectors.
+// sweeps; an empty range (refine_hi < refine_lo) keeps the FP32 vectors. `warm`: `work` holds the
+// eigenvectors of the previous successful call with the same T (a window of the same stream), from
+// which the FP32 sweeps start (T <= 64).
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
-                   cudaStream_t st, int refine_lo, int refine_hi);
+                   cudaStream_t st, int refine_lo, int refine_hi, bool warm = false);
 
 // view_tc.cu
 bool view_tc_supported(int K);

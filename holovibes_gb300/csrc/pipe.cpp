@@ -59,12 +59,23 @@ void free_buffers(hv_pipe* p)
     for (void* v : p->allocs)
         cudaFree(v);
     p->allocs.clear();
-    for (cudaEvent_t* e : {&p->ring_ready[0], &p->ring_ready[1], &p->ring_free[0], &p->ring_free[1], &p->join_ev})
+    for (hv_pipe::Lane& L : p->lanes)
+    {
+        for (cudaEvent_t* e : {&L.ready, &L.free})
+            if (*e)
+            {
+                cudaEventDestroy(*e);
+                *e = nullptr;
+            }
+        L = hv_pipe::Lane{};
+    }
+    for (cudaEvent_t* e : {&p->join_ev, &p->range_ev})
         if (*e)
         {
             cudaEventDestroy(*e);
             *e = nullptr;
         }
+    p->range_ev_set = false;
     for (auto* vec : {&p->in_filled, &p->in_consumed, &p->out_ready, &p->out_freed, &p->views[0].out_ready,
                       &p->views[0].out_freed, &p->views[1].out_ready, &p->views[1].out_freed, &p->views[2].out_ready,
                       &p->views[2].out_freed})
@@ -96,6 +107,25 @@ struct Sizes
     void add(size_t b) { total += (b + 255) / 256 * 256; }
 };
 
+// Fast mode (batch == stride == window, plain pipes): how many lanes have their own render stream
+// (eigensolve workloads without state carried from window to window), and how many rings are in
+// flight.
+int fast_renders(const hv_settings& s, bool served)
+{
+    if (served || s.batch_size != s.time_stride || s.batch_size != s.time_transformation_size)
+        return 1;
+    const bool own = uses_eig(s) && s.accumulation <= 1 && !s.cuts_enabled && !uses_f2d_view(s) &&
+                     !uses_phase_increase(s) && !uses_unwrap(s);
+    return own ? hv_pipe::kMaxLanes : 1;
+}
+
+int fast_lanes(const hv_settings& s, bool served)
+{
+    if (served || s.batch_size != s.time_stride || s.batch_size != s.time_transformation_size)
+        return 0;
+    return fast_renders(s, served) > 1 ? hv_pipe::kMaxLanes : 2;
+}
+
 size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = false)
 {
     const size_t HW = static_cast<size_t>(fd.width) * fd.height;
@@ -109,8 +139,23 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
     if (uses_f2d_mask(s) && s.space_transformation == HV_SPACE_FRESNELTR)
         z.add(HW * 8 * B);  // second spatial buffer
     z.add(HW * 8 * T);                                                  // ring
-    if (!served && B == s.time_stride && B == T)
-        z.add(HW * 8 * T);  // second ring of the double-buffered fast mode
+    const int lanes = fast_lanes(s, served), renders = fast_renders(s, served);
+    for (int l = 1; l < lanes; ++l)
+        z.add(HW * 8 * T);  // further rings of the fast mode
+    for (int l = 1; l < renders; ++l)
+    {
+        // per-window buffers of a lane with its own render stream
+        z.add(static_cast<size_t>(K > 0 ? K : 1) * T * 8);
+        z.add(static_cast<size_t>(T) * T * 16 * 2 + T * 8);
+        z.add(pca_cov_workspace(T, HW));
+        z.add(pca_eigh_workspace(T));
+        z.add(HW * 4 * 2);
+        if (use_view_tc(s, K, HW))
+            z.add(view_tc_workspace(K, T));
+        z.add(static_cast<size_t>(time_view_partials(fd.width, fd.height)) * 8);
+        z.add(reduce_workspace(HW));
+        z.add(64);
+    }
     z.add(static_cast<size_t>(K > 0 ? K : 1) * T * 8);                 // weights
     if (uses_eig(s))
     {
@@ -205,13 +250,14 @@ hv_status build(hv_pipe* p)
             HV_ALLOC(p->work2, HW * p->B * sizeof(float2));
         }
     }
-    p->fast = !p->served && p->B == p->S && p->B == p->T;
+    p->nlanes = fast_lanes(s, p->served);
+    p->nrender = fast_renders(s, p->served);
+    p->fast = p->nlanes > 0;
     HV_ALLOC(p->ring, HW * p->T * sizeof(float2));
-    p->rings[0] = p->ring;
-    p->rings[1] = nullptr;
-    if (p->fast)
+    p->lanes[0].ring = p->ring;
+    for (int l = 1; l < p->nlanes; ++l)
     {
-        HV_ALLOC(p->rings[1], HW * p->T * sizeof(float2));
+        HV_ALLOC(p->lanes[l].ring, HW * p->T * sizeof(float2));
     }
     HV_ALLOC(p->weights, static_cast<size_t>(p->K) * p->T * sizeof(float2));
     if (uses_eig(s))
@@ -221,6 +267,7 @@ hv_status build(hv_pipe* p)
         HV_ALLOC(p->evals, static_cast<size_t>(p->T) * sizeof(double));
         HV_ALLOC(p->cov_work, pca_cov_workspace(p->T, HW));
         HV_ALLOC(p->eig_work, pca_eigh_workspace(p->T));
+        p->eig_warm = false;
     }
     HV_ALLOC(p->view, HW * sizeof(float));
     p->bin_w = nullptr;
@@ -258,6 +305,42 @@ hv_status build(hv_pipe* p)
         HV_ALLOC(p->acc_ring, HW * p->A * sizeof(float));
     }
     HV_ALLOC(p->range, 4 * sizeof(float));
+    // lane 0 uses the buffers above; lanes with their own render stream get their own copies
+    {
+        hv_pipe::Lane& L0 = p->lanes[0];
+        L0.weights = p->weights;
+        L0.cov = p->cov;
+        L0.evals = p->evals;
+        L0.evecs = p->evecs;
+        L0.cov_work = p->cov_work;
+        L0.eig_work = p->eig_work;
+        L0.eig_warm = false;
+        L0.view = p->view;
+        L0.post = p->post;
+        L0.partials = p->partials;
+        L0.reduce_work = p->reduce_work;
+        L0.factors = p->factors;
+        L0.view_tc_work = p->view_tc_work;
+        for (int l = 1; l < p->nrender; ++l)
+        {
+            hv_pipe::Lane& L = p->lanes[l];
+            HV_ALLOC(L.weights, static_cast<size_t>(p->K) * p->T * sizeof(float2));
+            HV_ALLOC(L.cov, static_cast<size_t>(p->T) * p->T * sizeof(double2));
+            HV_ALLOC(L.evecs, static_cast<size_t>(p->T) * p->T * sizeof(double2));
+            HV_ALLOC(L.evals, static_cast<size_t>(p->T) * sizeof(double));
+            HV_ALLOC(L.cov_work, pca_cov_workspace(p->T, HW));
+            HV_ALLOC(L.eig_work, pca_eigh_workspace(p->T));
+            HV_ALLOC(L.view, HW * sizeof(float));
+            HV_ALLOC(L.post, HW * sizeof(float));
+            HV_ALLOC(L.partials, static_cast<size_t>(p->npartials) * sizeof(double));
+            HV_ALLOC(L.reduce_work, reduce_workspace(HW));
+            HV_ALLOC(L.factors, 4 * sizeof(float));
+            if (p->view_on_tc)
+            {
+                HV_ALLOC(L.view_tc_work, view_tc_workspace(p->K, p->T));
+            }
+        }
+    }
     p->cuts = s.cuts_enabled != 0;
     size_t pct_n = HW;
     if (p->cuts)
@@ -328,16 +411,28 @@ hv_status build(hv_pipe* p)
 
     // ring starts zeroed like Queue::resize (queue.cc:131-134)
     HV_CUDA_TRY(cudaMemsetAsync(p->ring, 0, HW * p->T * sizeof(float2), p->stream));
-    if (p->fast)
+    for (int l = 0; l < p->nlanes; ++l)
     {
-        HV_CUDA_TRY(cudaMemsetAsync(p->rings[1], 0, HW * p->T * sizeof(float2), p->stream));
-        for (int i = 0; i < 2; ++i)
+        hv_pipe::Lane& L = p->lanes[l];
+        if (l > 0)
+            HV_CUDA_TRY(cudaMemsetAsync(L.ring, 0, HW * p->T * sizeof(float2), p->stream));
+        HV_CUDA_TRY(cudaEventCreateWithFlags(&L.ready, cudaEventDisableTiming));
+        HV_CUDA_TRY(cudaEventCreateWithFlags(&L.free, cudaEventDisableTiming));
+        L.st = (p->nrender > 1 && l > 0) ? p->render_extra[l - 1] : p->render_stream_owned;
+        if (l >= p->nrender)
         {
-            HV_CUDA_TRY(cudaEventCreateWithFlags(&p->ring_ready[i], cudaEventDisableTiming));
-            HV_CUDA_TRY(cudaEventCreateWithFlags(&p->ring_free[i], cudaEventDisableTiming));
+            // lanes sharing lane 0's render stream share its buffers
+            const float2* ring = L.ring;
+            const cudaEvent_t ready = L.ready, fr = L.free;
+            L = p->lanes[0];
+            L.ring = const_cast<float2*>(ring);
+            L.ready = ready;
+            L.free = fr;
         }
     }
     HV_CUDA_TRY(cudaEventCreateWithFlags(&p->join_ev, cudaEventDisableTiming));
+    HV_CUDA_TRY(cudaEventCreateWithFlags(&p->range_ev, cudaEventDisableTiming));
+    p->range_ev_set = false;
     p->render_stream = p->fast ? p->render_stream_owned : p->stream;
     p->windows = 0;
     // lens (computed once per refresh, fourier_transform.cc:93-137)
@@ -446,9 +541,11 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
         // kept: the projector is the identity, nothing to refine)
         const int rlo = pca ? p->pmin : p->qmin;
         const int rhi = pca ? p->pmax : (p->qn < p->T ? p->qmin + p->qn - 1 : -1);
+        // the sweeps start from the previous window's eigenvectors once there is one
         if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, pca ? p->weights : nullptr,
-                          p->eig_work, st, rlo, rhi)) != HV_OK)
+                          p->eig_work, st, rlo, rhi, p->eig_warm)) != HV_OK)
             return r;
+        p->eig_warm = true;
         if (!pca && (r = ssa_weights(p->evecs, p->T, p->qmin, p->qn, p->pmin, p->K, p->weights, st)) != HV_OK)
             return r;
         if (p->view_on_tc && (r = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, st)) != HV_OK)
@@ -686,9 +783,21 @@ hv_status render(hv_pipe* p)
         const bool apply = p->A == 0 || p->acc_size == p->A || p->acc_size == 1;
         if (apply)
         {
+            if (p->nrender > 1)
+            {
+                // earlier windows on the other lanes read the range being replaced: wait for them
+                for (int l = 0; l < p->nlanes; ++l)
+                    if (p->lanes[l].st != st)
+                        HV_CUDA_TRY(cudaStreamWaitEvent(st, p->lanes[l].free, 0));
+            }
             if ((r = percentile(p->post, p->W, p->H, s.contrast_lower, s.contrast_upper,
                                 s.reticle_display ? s.reticle_scale : 0.0f, p->range, p->pct_work, st)) != HV_OK)
                 return r;
+            if (p->nrender > 1)
+            {
+                HV_CUDA_TRY(cudaEventRecord(p->range_ev, st));
+                p->range_ev_set = true;
+            }
             if (p->A == 0 || p->acc_size == p->A)
                 p->autocontrast_pending = false;
         }
@@ -743,29 +852,53 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
     if (p->fast)
     {
         // batch == stride == window: every batch refills the whole ring in batch order (with B = T,
-        // Queue::enqueue_multiple always lands frame j in slot j), so two rings alternate. The
-        // spatial passes of batch k+1 run on `stream` while window k is transformed and rendered
-        // on `render_stream`; ring k % 2 is reused only after window k-2 finished with it.
-        const int r = static_cast<int>(p->windows & 1);
-        float2* ring = p->rings[r];
-        HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ring_free[r], 0));
+        // Queue::enqueue_multiple always lands frame j in slot j), so the lanes' rings alternate.
+        // The spatial passes of batch k+1 run on `stream` while window k (and, with a render stream
+        // per lane, windows k-1 and k-2) are transformed and rendered; ring k % nlanes is reused
+        // only after window k - nlanes finished with it.
+        const int r = static_cast<int>(p->windows % static_cast<uint64_t>(p->nlanes));
+        hv_pipe::Lane& L = p->lanes[r];
+        HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, L.free, 0));
         hv_status st = spatial_transform(raw, p->kind, p->W, p->H, p->T, p->s.space_transformation, p->lens,
-                                         p->spatial, ring, 0, p->T, p->stream, nullptr, p->f2d_mask, p->work2);
+                                         p->spatial, L.ring, 0, p->T, p->stream, nullptr, p->f2d_mask, p->work2);
         if (st != HV_OK)
             return st;
         p->f2d_buf = r;  // one spectrum per ring: window k's render reads it while batch k+1 runs
         if (p->f2d_view && (st = capture_f2d_spectrum(p, raw, r)) != HV_OK)
             return st;
-        HV_CUDA_TRY(cudaEventRecord(p->ring_ready[r], p->stream));
-        HV_CUDA_TRY(cudaStreamWaitEvent(p->render_stream, p->ring_ready[r], 0));
-        p->ring = ring;
+        HV_CUDA_TRY(cudaEventRecord(L.ready, p->stream));
+        HV_CUDA_TRY(cudaStreamWaitEvent(L.st, L.ready, 0));
+        // the lane's ring, render stream and (with its own stream) per-window buffers
+        p->ring = L.ring;
+        p->render_stream = L.st;
+        if (p->nrender > 1)
+        {
+            p->weights = L.weights;
+            p->cov = L.cov;
+            p->evals = L.evals;
+            p->evecs = L.evecs;
+            p->cov_work = L.cov_work;
+            p->eig_work = L.eig_work;
+            p->eig_warm = L.eig_warm;
+            p->view = L.view;
+            p->post = L.post;
+            p->partials = L.partials;
+            p->reduce_work = L.reduce_work;
+            p->factors = L.factors;
+            p->view_tc_work = L.view_tc_work;
+            // the contrast range of the last autocontrast (computed on another lane)
+            if (p->range_ev_set)
+                HV_CUDA_TRY(cudaStreamWaitEvent(L.st, p->range_ev, 0));
+        }
         p->ring_start = 0;
         p->ring_size = p->T;
         ++p->windows;
         st = render(p);
         if (st != HV_OK)
             return st;
-        HV_CUDA_TRY(cudaEventRecord(p->ring_free[r], p->render_stream));
+        if (p->nrender > 1)
+            L.eig_warm = p->eig_warm;
+        HV_CUDA_TRY(cudaEventRecord(L.free, L.st));
         return HV_OK;
     }
     // Queue::enqueue_multiple (queue.cc:332-380)
@@ -1122,7 +1255,9 @@ hv_pipe* hv_pipe_create(const hv_frame_desc* fd, const hv_settings* settings, vo
         p->own_stream = true;
     }
     if (cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&p->render_stream_owned, cudaStreamNonBlocking) != cudaSuccess)
+        cudaStreamCreateWithFlags(&p->render_stream_owned, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&p->render_extra[0], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&p->render_extra[1], cudaStreamNonBlocking) != cudaSuccess)
     {
         out = HV_ERR_CUDA;
         hv_pipe_destroy(p);
@@ -1147,11 +1282,17 @@ void hv_pipe_destroy(hv_pipe* p)
         cudaStreamSynchronize(p->copy_stream);
     if (p->render_stream_owned)
         cudaStreamSynchronize(p->render_stream_owned);
+    for (cudaStream_t e : p->render_extra)
+        if (e)
+            cudaStreamSynchronize(e);
     free_buffers(p);
     if (p->copy_stream)
         cudaStreamDestroy(p->copy_stream);
     if (p->render_stream_owned)
         cudaStreamDestroy(p->render_stream_owned);
+    for (cudaStream_t e : p->render_extra)
+        if (e)
+            cudaStreamDestroy(e);
     if (p->own_stream && p->stream)
         cudaStreamDestroy(p->stream);
     delete p;
@@ -1257,6 +1398,16 @@ hv_status hv_pipe_pull_output(hv_pipe* p, uint16_t* dst, int mem, int64_t timeou
     return HV_OK;
 }
 
+// Waits for the rendering of every window enqueued so far (all lanes' render streams).
+static hv_status sync_render(hv_pipe* p)
+{
+    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    if (p->nrender > 1)
+        for (int l = 0; l < p->nrender; ++l)
+            HV_CUDA_TRY(cudaStreamSynchronize(p->lanes[l].st));
+    return HV_OK;
+}
+
 hv_status hv_pipe_update_settings(hv_pipe* p, const hv_settings* settings)
 {
     if (!p || !settings)
@@ -1269,7 +1420,11 @@ hv_status hv_pipe_update_settings(hv_pipe* p, const hv_settings* settings)
         return HV_NO_CHANGE;
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
     HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
-    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    {
+        const hv_status rs = sync_render(p);
+        if (rs != HV_OK)
+            return rs;
+    }
     p->s = ns;
     return build(p);
 }
@@ -1295,8 +1450,7 @@ hv_status hv_pipe_sync(hv_pipe* p)
         return HV_INVALID_VALUE;
     HV_CUDA_TRY(cudaStreamSynchronize(p->copy_stream));
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
-    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
-    return HV_OK;
+    return sync_render(p);
 }
 
 hv_status hv_pipe_join(hv_pipe* p)
@@ -1305,8 +1459,14 @@ hv_status hv_pipe_join(hv_pipe* p)
         return HV_INVALID_VALUE;
     if (p->render_stream != p->stream)
     {
-        HV_CUDA_TRY(cudaEventRecord(p->join_ev, p->render_stream));
-        HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->join_ev, 0));
+        // one event, recorded and waited on per render stream in turn (a wait takes the event's
+        // state at the time of the call)
+        const int n = p->nrender > 1 ? p->nrender : 1;
+        for (int l = 0; l < n; ++l)
+        {
+            HV_CUDA_TRY(cudaEventRecord(p->join_ev, n > 1 ? p->lanes[l].st : p->render_stream));
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->join_ev, 0));
+        }
     }
     return HV_OK;
 }
@@ -1317,7 +1477,11 @@ hv_status hv_pipe_get_contrast_range(hv_pipe* p, float* min_out, float* max_out)
         return HV_INVALID_VALUE;
     float r[2];
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
-    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    {
+        const hv_status rs = sync_render(p);
+        if (rs != HV_OK)
+            return rs;
+    }
     HV_CUDA_TRY(cudaMemcpy(r, p->range, sizeof(r), cudaMemcpyDeviceToHost));
     if (min_out)
         *min_out = r[0];
@@ -1333,7 +1497,11 @@ hv_status hv_pipe_get_float_frame(hv_pipe* p, float* dst)
     if (!p->last_frame_valid)
         return HV_NO_IN_DATA;
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
-    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    {
+        const hv_status rs = sync_render(p);
+        if (rs != HV_OK)
+            return rs;
+    }
     HV_CUDA_TRY(cudaMemcpy(dst, p->post, p->HW * sizeof(float), cudaMemcpyDeviceToHost));
     return HV_OK;
 }
@@ -1408,7 +1576,11 @@ hv_status hv_pipe_get_view_float_frame(hv_pipe* p, int which, float* dst, float*
         return HV_NO_IN_DATA;
     const hv_pipe::SecondaryView& c = p->views[which];
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
-    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    {
+        const hv_status rs = sync_render(p);
+        if (rs != HV_OK)
+            return rs;
+    }
     if (dst)
         HV_CUDA_TRY(cudaMemcpy(dst, c.post, static_cast<size_t>(c.w) * c.h * sizeof(float), cudaMemcpyDeviceToHost));
     if (range_out)
@@ -1421,7 +1593,11 @@ hv_status hv_pipe_get_ring(hv_pipe* p, void* dst_host, int32_t* start, int32_t* 
     if (!p)
         return HV_INVALID_VALUE;
     HV_CUDA_TRY(cudaStreamSynchronize(p->stream));
-    HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    {
+        const hv_status rs = sync_render(p);
+        if (rs != HV_OK)
+            return rs;
+    }
     if (dst_host)
         HV_CUDA_TRY(cudaMemcpy(dst_host, p->ring, p->HW * p->T * sizeof(float2), cudaMemcpyDeviceToHost));
     if (start)

@@ -32,11 +32,38 @@ struct hv_pipe
     float2* f2d_mask = nullptr;  // filter2D mask in FFT layout (Fresnel / no propagation)
     float2* work2 = nullptr;     // second spatial buffer of the filtered Fresnel passes
     float2* ring = nullptr;
-    // fast mode (batch == stride == window): two rings, spatial on `stream`, the window's time
-    // transform and rendering on `render_stream`, so the next batch's spatial passes overlap them
+    // fast mode (batch == stride == window): window k fills the ring of lane k % nlanes on
+    // `stream` while earlier windows are transformed and rendered. With nrender == 1 the lanes
+    // share `render_stream` and the per-window buffers; with nrender == nlanes (eigensolve
+    // workloads, whose covariance -> eigensolve -> projection chain per window is longer than the
+    // spatial passes) every lane has its own render stream and per-window buffers, so the time
+    // transforms of consecutive windows overlap too.
+    static constexpr int kMaxLanes = 3;
+    struct Lane
+    {
+        float2* ring = nullptr;
+        cudaEvent_t ready = nullptr, free = nullptr;
+        cudaStream_t st = nullptr;
+        float2* weights = nullptr;
+        double2* cov = nullptr;
+        double* evals = nullptr;
+        double2* evecs = nullptr;
+        void* cov_work = nullptr;
+        void* eig_work = nullptr;
+        bool eig_warm = false;
+        float* view = nullptr;
+        float* post = nullptr;
+        double* partials = nullptr;
+        void* reduce_work = nullptr;
+        float* factors = nullptr;
+        void* view_tc_work = nullptr;
+    };
     bool fast = false;
-    float2* rings[2] = {nullptr, nullptr};
-    cudaEvent_t ring_ready[2] = {nullptr, nullptr}, ring_free[2] = {nullptr, nullptr};
+    Lane lanes[kMaxLanes];
+    int nlanes = 0, nrender = 1;
+    cudaStream_t render_extra[kMaxLanes - 1] = {nullptr, nullptr};  // render streams of lanes 1, 2
+    cudaEvent_t range_ev = nullptr;  // after the last autocontrast (lanes with their own streams)
+    bool range_ev_set = false;
     cudaEvent_t join_ev = nullptr;
     uint64_t windows = 0;
     float2* weights = nullptr;
@@ -45,6 +72,7 @@ struct hv_pipe
     double2* evecs = nullptr;
     void* cov_work = nullptr;
     void* eig_work = nullptr;
+    bool eig_warm = false;  // eig_work holds the eigenvectors of the previous window (same T)
     float* view = nullptr;
     float* unwrapped = nullptr;
     void* unwrap_work = nullptr;

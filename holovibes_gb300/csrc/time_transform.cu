@@ -880,15 +880,51 @@ __device__ bool smem_sweeps(Cx<R>* A, Cx<R>* V, int T_, int Tp_, int LD_, JacScr
     return any;
 }
 
+// C = op(X) Y for T x T shared-memory matrices (leading dimension LD), op(X) = X or X^H; every
+// thread of the block takes output elements in turn.
+template <class R, int NT>
+__device__ void smem_cgemm(const Cx<R>* X, const Cx<R>* Y, Cx<R>* C, int T, int LD, bool conj_x)
+{
+    for (int e = threadIdx.x; e < T * T; e += NT)
+    {
+        const int i = e / T, j = e % T;
+        R re = 0, im = 0;
+        for (int k = 0; k < T; ++k)
+        {
+            Cx<R> x = conj_x ? X[k * LD + i] : X[i * LD + k];
+            if (conj_x)
+                x.y = -x.y;
+            const Cx<R> y = Y[k * LD + j];
+            re += x.x * y.x - x.y * y.y;
+            im += x.x * y.y + x.y * y.x;
+        }
+        C[i * LD + j] = {re, im};
+    }
+}
+
+// Shared-memory bytes of k_jacobi_smem: A and V, plus two work matrices for a warm start.
+template <class R>
+size_t jacobi_smem_bytes(int T, bool warm)
+{
+    return (warm ? 4 : 2) * static_cast<size_t>(T) * (T + 1) * sizeof(Cx<R>);
+}
+
+// `warm` (FP32 only): Vout holds the orthonormal eigenvector basis of the previous call on this
+// workspace (a window of the same stream): the sweeps start from A' = V0^H A V0 with V = V0, which
+// is nearly diagonal when consecutive windows share their temporal modes, so one or two sweeps
+// finish it. V0 is first re-orthonormalised by one Newton-Schulz step V0 (3 I - V0^H V0) / 2, so
+// rounding does not accumulate from window to window.
 template <class R>
 __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __restrict__ Ain, double2* __restrict__ Vout,
-                                                            int T, int Tp, double* __restrict__ evals)
+                                                            int T, int Tp, double* __restrict__ evals, int warm)
 {
     extern __shared__ __align__(16) unsigned char js_raw[];
     Cx<R>* js = reinterpret_cast<Cx<R>*>(js_raw);
     const int LD = T + 1;
     Cx<R>* A = js;
     Cx<R>* V = js + T * LD;
+    Cx<R>* X = V + T * LD;  // warm start only
+    Cx<R>* N = X + T * LD;
     __shared__ JacScratch<R> sc;
     __shared__ double s_scale;
     const int tid = threadIdx.x;
@@ -910,10 +946,66 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
         const int i = e / T, j = e % T;
         const double2 a = Ain[e];
         A[i * LD + j] = {static_cast<R>(a.x * scale), static_cast<R>(i == j ? 0.0 : a.y * scale)};
-        V[i * LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
+        if (warm)
+        {
+            const double2 v = Vout[e];
+            N[i * LD + j] = {static_cast<R>(v.x), static_cast<R>(v.y)};
+        }
+        else
+            V[i * LD + j] = {static_cast<R>(i == j ? 1 : 0), static_cast<R>(0)};
     }
     __syncthreads();
-    smem_sweeps<R, JS_THREADS>(A, V, T, Tp, LD, sc, R(0), JAC_MAX_SWEEPS);
+    if (warm)
+    {
+        // V = V0 (3 I - V0^H V0) / 2 (V0 in N), then A <- V^H A V
+        smem_cgemm<R, JS_THREADS>(N, N, X, T, LD, true);
+        __syncthreads();
+        for (int e = tid; e < T * T; e += JS_THREADS)
+        {
+            const int i = e / T, j = e % T;
+            const Cx<R> x = X[i * LD + j];
+            X[i * LD + j] = {R(-0.5) * x.x + (i == j ? R(1.5) : R(0)), R(-0.5) * x.y};
+        }
+        __syncthreads();
+        smem_cgemm<R, JS_THREADS>(N, X, V, T, LD, false);
+        __syncthreads();
+        smem_cgemm<R, JS_THREADS>(A, V, X, T, LD, false);
+        __syncthreads();
+        smem_cgemm<R, JS_THREADS>(V, X, N, T, LD, true);
+        __syncthreads();
+        for (int e = tid; e < T * T; e += JS_THREADS)
+        {
+            const int i = e / T, j = e % T;
+            const Cx<R> a = N[i * LD + j], b = N[j * LD + i];
+            A[i * LD + j] = {R(0.5) * (a.x + b.x), i == j ? R(0) : R(0.5) * (a.y - b.y)};
+        }
+        __syncthreads();
+    }
+    // FP32 sweeps: rotations below the round-off level of the matrix (5e-7 of its Frobenius norm)
+    // are not applied. Below that floor the FP32 updates keep regenerating off-diagonal entries of
+    // the small eigenvalues (the round-off of the large ones exceeds the relative threshold), and
+    // the sweeps would run to their limit; the kept eigenvectors are refined in FP64 afterwards.
+    __shared__ double s_fro[JS_THREADS / 32];
+    R floor = R(0);
+    if constexpr (sizeof(R) == sizeof(float))
+    {
+        double f2 = 0.0;
+        for (int e = tid; e < T * T; e += JS_THREADS)
+        {
+            const Cx<R> a = A[(e / T) * LD + e % T];
+            f2 += static_cast<double>(a.x) * a.x + static_cast<double>(a.y) * a.y;
+        }
+        for (int o = 16; o > 0; o >>= 1)
+            f2 += __shfl_xor_sync(0xffffffffu, f2, o);
+        if ((tid & 31) == 0)
+            s_fro[tid >> 5] = f2;
+        __syncthreads();
+        double t2 = 0.0;
+        for (int w = 0; w < JS_THREADS / 32; ++w)
+            t2 += s_fro[w];
+        floor = static_cast<R>(5e-7 * sqrt(t2));
+    }
+    smem_sweeps<R, JS_THREADS>(A, V, T, Tp, LD, sc, floor, JAC_MAX_SWEEPS);
     __syncthreads();
     for (int e = tid; e < T * T; e += JS_THREADS)
     {
@@ -1461,34 +1553,44 @@ __device__ __forceinline__ double eigref_lambda(const double2* D, const double2*
 }
 
 // Vn[j][t] = v_j[t] + sum_{i != j} v_i[t] (D[j][i] - lambda_j G[j][i]) / (lambda_j - lambda_i);
-// grid (ceil(T / 128), K), 128 threads (thread = row t: the loads of v_i[t] are coalesced)
+// grid (ceil(T / 128), K), 128 threads (thread = row t: the loads of v_i[t] are coalesced). The T
+// coefficients of kept vector j are computed once per CTA into shared memory (FP64 divisions are
+// slow on this part), then every thread runs the complex multiply-adds.
 __global__ void k_eigref_update(const double2* __restrict__ evecs, const double* __restrict__ evals,
                                 const double2* __restrict__ D, const double2* __restrict__ G, int T, int r0, int K,
                                 double2* __restrict__ Vn)
 {
+    __shared__ double2 coef[JC_MAX_T];
     const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (t >= T)
-        return;
-    // pairs closer than 1e-12 of the largest eigenvalue (the last in ascending order) stay mixed
-    const double degenerate = 1e-12 * fabs(evals[T - 1]);
     const int rj = r0 + j;
     const double lj = eigref_lambda(D, G, T, r0, j);
+    // pairs closer than 1e-12 of the largest eigenvalue (the last in ascending order) stay mixed
+    const double degenerate = 1e-12 * fabs(evals[T - 1]);
     const double2* Dj = D + static_cast<size_t>(j) * T;
     const double2* Gj = G + static_cast<size_t>(j) * T;
+    for (int i = threadIdx.x; i < T; i += blockDim.x)
+    {
+        const double li = (i >= r0 && i < r0 + K) ? eigref_lambda(D, G, T, r0, i - r0) : evals[i];
+        const double gap = lj - li;
+        double2 c = make_double2(0.0, 0.0);
+        if (i != rj && fabs(gap) > degenerate)
+        {
+            const double inv = 1.0 / gap;
+            const double2 d = Dj[i], g = Gj[i];
+            c = make_double2((d.x - lj * g.x) * inv, (d.y - lj * g.y) * inv);
+        }
+        coef[i] = c;
+    }
+    __syncthreads();
+    if (t >= T)
+        return;
     double2 acc = evecs[static_cast<size_t>(rj) * T + t];
     for (int i = 0; i < T; ++i)
     {
-        if (i == rj)
-            continue;
-        const double li = (i >= r0 && i < r0 + K) ? eigref_lambda(D, G, T, r0, i - r0) : evals[i];
-        const double gap = lj - li;
-        if (!(fabs(gap) > degenerate))
-            continue;
-        const double2 d = Dj[i], g = Gj[i];
-        const double cx = (d.x - lj * g.x) / gap, cy = (d.y - lj * g.y) / gap;
+        const double2 c = coef[i];
         const double2 v = evecs[static_cast<size_t>(i) * T + t];
-        acc.x += v.x * cx - v.y * cy;
-        acc.y += v.x * cy + v.y * cx;
+        acc.x += v.x * c.x - v.y * c.y;
+        acc.y += v.x * c.y + v.y * c.x;
     }
     Vn[static_cast<size_t>(j) * T + t] = acc;
 }
@@ -1548,7 +1650,7 @@ size_t pca_eigh_workspace(int T)
 }
 
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
-                   cudaStream_t st, int refine_lo, int refine_hi)
+                   cudaStream_t st, int refine_lo, int refine_hi, bool warm)
 {
     if (T <= 0 || !work)
         return HV_INVALID_VALUE;
@@ -1567,19 +1669,19 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     off += eigref_bytes(T);
     if (T <= JS_MAX_T && prec == HV_EIG_FP32)
     {
-        const size_t smem = 2 * static_cast<size_t>(T) * (T + 1) * sizeof(float2);
+        const size_t smem = jacobi_smem_bytes<float>(T, warm);
         if (smem > 48 * 1024)
             HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(smem)));
-        k_jacobi_smem<float><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted);
+                                             static_cast<int>(jacobi_smem_bytes<float>(JS_MAX_T, true))));
+        k_jacobi_smem<float><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted, warm ? 1 : 0);
     }
     else if (T <= JS_MAX_T)
     {
-        const size_t smem = 2 * static_cast<size_t>(T) * (T + 1) * sizeof(double2);
+        const size_t smem = jacobi_smem_bytes<double>(T, false);
         if (smem > 48 * 1024)
             HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem)));
-        k_jacobi_smem<double><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted);
+        k_jacobi_smem<double><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted, 0);
     }
     else if (T <= JC_MAX_T && prec == HV_EIG_FP32)
     {
@@ -1643,15 +1745,20 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         double2* G = D + static_cast<size_t>(ER_MAX_K) * T;
         double2* Vn = G + static_cast<size_t>(ER_MAX_K) * T;
         const dim3 gw((T + 7) / 8, K), gt((T + 127) / 128, K);
-        k_eigref_matvec<<<gw, 256, 0, st>>>(cov, evecs, T, refine_lo, Y);
-        HV_LAUNCH_CHECK();
-        k_eigref_project<<<gw, 256, 0, st>>>(evecs, Y, T, refine_lo, D, G);
-        HV_LAUNCH_CHECK();
-        k_eigref_update<<<gt, 128, 0, st>>>(evecs, evals, D, G, T, refine_lo, K, Vn);
-        HV_LAUNCH_CHECK();
-        k_eigref_finish<<<K, 128, 0, st>>>(evecs, evals, Vn, D, G, T, refine_lo, pmin, pmax, weights);
-        HV_LAUNCH_CHECK();
-        count_launch(4);
+        // two corrections: the first leaves O(theta^2) against the FP32 error of the other
+        // eigenvectors, the second brings that to the FP64 level
+        for (int iter = 0; iter < 2; ++iter)
+        {
+            k_eigref_matvec<<<gw, 256, 0, st>>>(cov, evecs, T, refine_lo, Y);
+            HV_LAUNCH_CHECK();
+            k_eigref_project<<<gw, 256, 0, st>>>(evecs, Y, T, refine_lo, D, G);
+            HV_LAUNCH_CHECK();
+            k_eigref_update<<<gt, 128, 0, st>>>(evecs, evals, D, G, T, refine_lo, K, Vn);
+            HV_LAUNCH_CHECK();
+            k_eigref_finish<<<K, 128, 0, st>>>(evecs, evals, Vn, D, G, T, refine_lo, pmin, pmax, weights);
+            HV_LAUNCH_CHECK();
+            count_launch(4);
+        }
     }
     return HV_OK;
 }

@@ -124,7 +124,7 @@ def test_cfg3_full_size_and_eigenvalues(cuda):
     rd = dev(ring)
     report = {}
     covs = {}
-    for mode, label, tol in ((2, "bf16x3 tensor cores", 1e-3), (1, "fp32 SIMT", 1e-6)):
+    for mode, label in ((2, "bf16x3 tensor cores"), (1, "fp32 SIMT")):
         cov = empty(T * T * 16)
         work = empty(hv.lib().hv_pca_cov_workspace(T, npix))
         hv.lib().hv_pca_covariance_mode(mode)
@@ -142,8 +142,11 @@ def test_cfg3_full_size_and_eigenvalues(cuda):
         scale = float(np.vdot(cov_ref.ravel(), got.ravel()).real / np.vdot(cov_ref.ravel(), cov_ref.ravel()).real)
         report[label + ": scale - 1"] = scale - 1.0
         report[label + ": rel-L2 after the scale"] = rel_l2(got / scale, cov_ref)
-    for mode, label, tol in ((2, "bf16x3 tensor cores", 1e-3), (1, "fp32 SIMT", 1e-6)):
+    # FP32 accumulation over 262144 pixels: a few 1e-6 for the SIMT engine, ~1e-5 (a uniform
+    # scale: below 1e-6 after it) for the tensor cores' accumulation chains
+    for label, tol in (("bf16x3 tensor cores", 3e-5), ("fp32 SIMT", 1e-5)):
         assert report[label] <= tol, (label, report)
+    assert report["bf16x3 tensor cores: rel-L2 after the scale"] <= 3e-6, report
     # the Pipe's eigensolver (default precision) on the tensor-core covariance, against LAPACK on
     # the FP64 covariance of the oracle's ring
     evals = empty(T * 8)
