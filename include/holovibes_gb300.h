@@ -393,18 +393,23 @@ void hv_pca_covariance_mode(int mode);
 /* After the covariance's stream work finished: HV_ERR_TIMEOUT when a bounded device wait in the
  * tensor-core kernel gave up (results invalid), HV_OK otherwise. Synchronous read of `work`. */
 hv_status hv_pca_covariance_status(const void* work);
-/* FP64 cyclic Jacobi eigensolve of the Hermitian T x T complex128 matrix (lower triangle
- * read): ascending eigenvalues, orthonormal eigenvectors as columns. Replaces cusolverDnCheevd
- * (matrix_operations.cc:44-65). Writes the columns pmin..pmax as PCA weights W[k][t] = V[t][pmin+k]
- * (complex64) when weights_c64 != NULL. `cov_c128` is overwritten. `work` needs hv_pca_eigh_workspace(T) bytes. */
+/* Eigensolve of the Hermitian T x T complex128 matrix (both triangles read): ascending
+ * eigenvalues, eigenvectors as columns. Replaces cusolverDnCheevd (matrix_operations.cc:44-65).
+ * Writes the columns pmin..pmax as PCA weights W[k][t] = V[t][pmin+k] (complex64) when weights_c64
+ * != NULL. With the default precision (HV_EIG_FP32, T <= 512) the Jacobi sweeps run in FP32 on a
+ * power-of-two-scaled copy, every eigenvalue is the FP64 Rayleigh quotient of its normalised
+ * vector, and the eigenvectors of ranks pmin..pmax (when 0 <= pmin <= pmax < T, at most 64 of
+ * them) are then corrected in FP64 against `cov_c128` (two first-order residual corrections): those
+ * are accurate to the FP64 level, the others to the FP32 sweeps' (~1e-6). `cov_c128` is overwritten
+ * in HV_EIG_FP64 mode. `work` needs hv_pca_eigh_workspace(T) bytes. */
 hv_status hv_pca_eigh(void* cov_c128, int T, double* eigenvalues, void* eigenvectors_c128, int pmin, int pmax,
                       void* weights_c64, void* work, void* stream);
 size_t hv_pca_eigh_workspace(int T);
 /* Jacobi sweep precision (process-wide). HV_EIG_FP32 (default): FP32 sweeps (T <= 64: one CTA,
- * shared memory; 64 < T <= 512: block-cyclic Jacobi over a cooperative grid), then each eigenvector
- * is normalised and its eigenvalue taken as the Rayleigh quotient against the FP64 covariance
- * (GB300 runs FP64 at 1/64 of the FP32 rate, so FP64 sweeps cost milliseconds per window).
- * HV_EIG_FP64, and any T above 512: the sweeps themselves in FP64. */
+ * shared memory; 64 < T <= 512: block-cyclic Jacobi over a cooperative grid) stopping at the
+ * round-off level of the matrix, FP64 Rayleigh quotients, FP64 correction of the kept eigenvectors
+ * (GB300 runs FP64 far below its FP32 rate: FP64 sweeps take 1.7 ms at T = 32 and 87 ms at T = 128,
+ * against 0.24 and 1.6 ms). HV_EIG_FP64, and any T above 512: the sweeps themselves in FP64. */
 enum { HV_EIG_FP32 = 0, HV_EIG_FP64 = 1 };
 void hv_pca_eig_precision(int precision);
 
