@@ -88,9 +88,11 @@ void set_eig_precision(int p);
 // Eigenvectors of ranks refine_lo..refine_hi (at most 64 of them) are refined in FP64 after FP32
 // sweeps; an empty range (refine_hi < refine_lo) keeps the FP32 vectors. `warm`: `work` holds the
 // eigenvectors of the previous successful call with the same T (a window of the same stream), from
-// which the FP32 sweeps start (T <= 64).
+// which the FP32 sweeps start (T <= 64). `kept_only`: the caller uses only the refined
+// eigenvectors and the order of the eigenvalues (coarser sweeps, FP32 Rayleigh quotients for the
+// others).
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
-                   cudaStream_t st, int refine_lo, int refine_hi, bool warm = false);
+                   cudaStream_t st, int refine_lo, int refine_hi, bool warm = false, bool kept_only = false);
 
 // view_tc.cu
 bool view_tc_supported(int K);

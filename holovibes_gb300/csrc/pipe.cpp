@@ -542,8 +542,9 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
         const int rlo = pca ? p->pmin : p->qmin;
         const int rhi = pca ? p->pmax : (p->qn < p->T ? p->qmin + p->qn - 1 : -1);
         // the sweeps start from the previous window's eigenvectors once there is one
+        // PCA views read only the refined weights (the cuts read every eigenvector)
         if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, pca ? p->weights : nullptr,
-                          p->eig_work, st, rlo, rhi, p->eig_warm)) != HV_OK)
+                          p->eig_work, st, rlo, rhi, p->eig_warm, pca && !p->cuts)) != HV_OK)
             return r;
         p->eig_warm = true;
         if (!pca && (r = ssa_weights(p->evecs, p->T, p->qmin, p->qn, p->pmin, p->K, p->weights, st)) != HV_OK)

@@ -916,7 +916,8 @@ size_t jacobi_smem_bytes(int T, bool warm)
 // rounding does not accumulate from window to window.
 template <class R>
 __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __restrict__ Ain, double2* __restrict__ Vout,
-                                                            int T, int Tp, double* __restrict__ evals, int warm)
+                                                            int T, int Tp, double* __restrict__ evals, int warm,
+                                                            float floor_rel)
 {
     extern __shared__ __align__(16) unsigned char js_raw[];
     Cx<R>* js = reinterpret_cast<Cx<R>*>(js_raw);
@@ -981,10 +982,10 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
         }
         __syncthreads();
     }
-    // FP32 sweeps: rotations below the round-off level of the matrix (5e-7 of its Frobenius norm)
-    // are not applied. Below that floor the FP32 updates keep regenerating off-diagonal entries of
-    // the small eigenvalues (the round-off of the large ones exceeds the relative threshold), and
-    // the sweeps would run to their limit; the kept eigenvectors are refined in FP64 afterwards.
+    // FP32 sweeps: rotations below floor_rel of the matrix's Frobenius norm are not applied (5e-7:
+    // the round-off level of the FP32 updates, below which they keep regenerating off-diagonal
+    // entries of the small eigenvalues and the sweeps would run to their limit; 2e-5 when only the
+    // kept eigenvectors are used, which are refined in FP64 afterwards).
     __shared__ double s_fro[JS_THREADS / 32];
     R floor = R(0);
     if constexpr (sizeof(R) == sizeof(float))
@@ -1003,7 +1004,7 @@ __global__ void __launch_bounds__(JS_THREADS) k_jacobi_smem(const double2* __res
         double t2 = 0.0;
         for (int w = 0; w < JS_THREADS / 32; ++w)
             t2 += s_fro[w];
-        floor = static_cast<R>(5e-7 * sqrt(t2));
+        floor = static_cast<R>(static_cast<double>(floor_rel) * sqrt(t2));
     }
     smem_sweeps<R, JS_THREADS>(A, V, T, Tp, LD, sc, floor, JAC_MAX_SWEEPS);
     __syncthreads();
@@ -1176,7 +1177,7 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
                                                              Cx<float>* V1, Cx<float>* U, int* flags,
                                                              double* fro2, GridBarrier* bar,
                                                              double2* __restrict__ Vout,
-                                                             double* __restrict__ evals)
+                                                             double* __restrict__ evals, double floor_rel)
 {
     using R = float;
     extern __shared__ __align__(16) unsigned char bj_raw[];
@@ -1237,7 +1238,7 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
     // sweeps going; at this floor the eigenvectors of separated eigenvalues keep FP32 accuracy
     // (residual ~3e-6 of the largest eigenvalue at T = 512, the level of the sweeps' own round-off)
     if (tid == 0)
-        s_floor = static_cast<R>(sqrt(*reinterpret_cast<volatile double*>(fro2)) * 5e-7);
+        s_floor = static_cast<R>(sqrt(*reinterpret_cast<volatile double*>(fro2)) * floor_rel);
     __syncthreads();
     Cx<R>*A = A0, *An = A1, *V = V0, *Vn = V1;
     const int na = npb * (npb + 1) / 2, nrow = Tp / BJ_S;
@@ -1379,13 +1380,18 @@ __global__ void __launch_bounds__(BJ_THREADS) k_jacobi_block(const double2* __re
 }
 
 
-// FP64 finish of each eigenpair from the FP64 covariance (intact in the shared-memory paths):
-// normalise the eigenvector column in FP64 and take its Rayleigh quotient v^H A v as the
-// eigenvalue, whose error is second order in the eigenvector error. One CTA per eigenpair.
+// Finish of each eigenpair from the FP64 covariance (intact in the FP32-sweep paths): normalise
+// the eigenvector column in FP64 and take its Rayleigh quotient v^H A v as the eigenvalue, whose
+// error is second order in the eigenvector error. Acc = double: FP64 quotients; Acc = float: the
+// quadratic form accumulated in FP32 (~1e-7 of the largest eigenvalue: enough to order the
+// eigenvalues whose vectors are not refined afterwards, at a small fraction of the FP64 cost on
+// this part). One CTA per eigenpair.
+template <class Acc>
 __global__ void k_eig_refine(const double2* __restrict__ A, double2* __restrict__ V, int T, double* __restrict__ evals)
 {
     __shared__ double2 v[JC_MAX_T];
     __shared__ double red[4];
+    __shared__ Acc redl[4];
     const int i = blockIdx.x, tid = threadIdx.x;
     double n2 = 0.0;
     for (int t = tid; t < T; t += blockDim.x)
@@ -1403,27 +1409,31 @@ __global__ void k_eig_refine(const double2* __restrict__ A, double2* __restrict_
     __syncthreads();
     // v^H A v of the Hermitian A: sum_t a_tt |v_t|^2 + 2 Re sum_{t<s} conj(v_t) a_ts v_s (upper
     // triangle only: half the FP64 multiply-adds of the full product)
-    double lam = 0.0;
+    Acc lam = 0;
     for (int t = tid; t < T; t += blockDim.x)
     {
-        double2 av = make_double2(0.0, 0.0);
+        Acc ax = 0, ay = 0;
         for (int s2 = t + 1; s2 < T; ++s2)
         {
             const double2 a = A[t * T + s2], x = v[s2];
-            av.x += a.x * x.x - a.y * x.y;
-            av.y += a.x * x.y + a.y * x.x;
+            const Acc arx = static_cast<Acc>(a.x), ary = static_cast<Acc>(a.y);
+            const Acc xx = static_cast<Acc>(x.x), xy = static_cast<Acc>(x.y);
+            ax += arx * xx - ary * xy;
+            ay += arx * xy + ary * xx;
         }
         const double2 x = v[t];
-        lam += (2.0 * (x.x * av.x + x.y * av.y) + A[t * T + t].x * (x.x * x.x + x.y * x.y)) * inv * inv;
+        const Acc xx = static_cast<Acc>(x.x), xy = static_cast<Acc>(x.y);
+        lam += (Acc(2) * (xx * ax + xy * ay) + static_cast<Acc>(A[t * T + t].x) * (xx * xx + xy * xy)) *
+               static_cast<Acc>(inv * inv);
         V[t * T + i] = make_double2(x.x * inv, x.y * inv);
     }
     for (int o = 16; o > 0; o >>= 1)
         lam += __shfl_down_sync(0xffffffffu, lam, o);
     if ((tid & 31) == 0)
-        red[tid >> 5] = lam;
+        redl[tid >> 5] = lam;
     __syncthreads();
     if (tid == 0)
-        evals[i] = red[0] + red[1] + red[2] + red[3];
+        evals[i] = static_cast<double>(redl[0]) + redl[1] + redl[2] + redl[3];
 }
 
 // Sort eigenpairs ascending (rank = number of smaller values, ties by index), write the
@@ -1518,12 +1528,13 @@ __global__ void k_eigref_matvec(const double2* __restrict__ C, const double2* __
         Y[static_cast<size_t>(j) * T + t] = acc;
 }
 
-// D[j][i] = v_i^H Y[j], G[j][i] = v_i^H v_{r0+j}; grid (ceil(T / 8), K), 256 threads
+// D[j][i] = v_i^H Y[j], G[j][i] = v_i^H v_{r0+j} for the basis vectors i = b0 .. T-1;
+// grid (ceil((T - b0) / 8), K), 256 threads
 __global__ void k_eigref_project(const double2* __restrict__ evecs, const double2* __restrict__ Y, int T, int r0,
-                                 double2* __restrict__ D, double2* __restrict__ G)
+                                 int b0, double2* __restrict__ D, double2* __restrict__ G)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = blockIdx.x * 8 + warp, j = blockIdx.y;
+    const int i = b0 + blockIdx.x * 8 + warp, j = blockIdx.y;
     if (i >= T)
         return;
     const double2* vi = evecs + static_cast<size_t>(i) * T;
@@ -1552,15 +1563,20 @@ __device__ __forceinline__ double eigref_lambda(const double2* D, const double2*
     return D[e].x / G[e].x;
 }
 
-// Vn[j][t] = v_j[t] + sum_{i != j} v_i[t] (D[j][i] - lambda_j G[j][i]) / (lambda_j - lambda_i);
-// grid (ceil(T / 128), K), 128 threads (thread = row t: the loads of v_i[t] are coalesced). The T
-// coefficients of kept vector j are computed once per CTA into shared memory (FP64 divisions are
-// slow on this part), then every thread runs the complex multiply-adds.
+// Vn[j][t] = v_j[t] + sum_{i != j} v_i[t] (D[j][i] - lambda_j G[j][i]) / (lambda_j - lambda_i), over
+// the basis i = b0 .. T-1. With a partial basis (b0 > 0: the Ritz vectors of the largest
+// eigenvalues) the part of the residual r = C v_j - lambda_j v_j outside the basis is added divided
+// by lambda_j (the eigenvalues outside are the smaller ones; the factor lambda_i / lambda_j it
+// neglects shrinks with each correction). grid (ceil(T / 128), K), 128 threads (thread = row t: the
+// loads of v_i[t] are coalesced). The coefficients of kept vector j are computed once per CTA into
+// shared memory (FP64 divisions are slow on this part), then every thread runs the complex
+// multiply-adds.
 __global__ void k_eigref_update(const double2* __restrict__ evecs, const double* __restrict__ evals,
-                                const double2* __restrict__ D, const double2* __restrict__ G, int T, int r0, int K,
-                                double2* __restrict__ Vn)
+                                const double2* __restrict__ D, const double2* __restrict__ G,
+                                const double2* __restrict__ Y, int T, int r0, int K, int b0, double2* __restrict__ Vn)
 {
     __shared__ double2 coef[JC_MAX_T];
+    __shared__ double2 comp[JC_MAX_T];
     const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     const int rj = r0 + j;
     const double lj = eigref_lambda(D, G, T, r0, j);
@@ -1568,29 +1584,46 @@ __global__ void k_eigref_update(const double2* __restrict__ evecs, const double*
     const double degenerate = 1e-12 * fabs(evals[T - 1]);
     const double2* Dj = D + static_cast<size_t>(j) * T;
     const double2* Gj = G + static_cast<size_t>(j) * T;
-    for (int i = threadIdx.x; i < T; i += blockDim.x)
+    for (int i = b0 + threadIdx.x; i < T; i += blockDim.x)
     {
         const double li = (i >= r0 && i < r0 + K) ? eigref_lambda(D, G, T, r0, i - r0) : evals[i];
         const double gap = lj - li;
+        const double2 d = Dj[i], g = Gj[i];
+        const double2 cr = make_double2(d.x - lj * g.x, d.y - lj * g.y);  // component of r along v_i
         double2 c = make_double2(0.0, 0.0);
         if (i != rj && fabs(gap) > degenerate)
         {
             const double inv = 1.0 / gap;
-            const double2 d = Dj[i], g = Gj[i];
-            c = make_double2((d.x - lj * g.x) * inv, (d.y - lj * g.y) * inv);
+            c = make_double2(cr.x * inv, cr.y * inv);
         }
         coef[i] = c;
+        comp[i] = cr;
     }
     __syncthreads();
     if (t >= T)
         return;
     double2 acc = evecs[static_cast<size_t>(rj) * T + t];
-    for (int i = 0; i < T; ++i)
+    double2 proj = make_double2(0.0, 0.0);
+    for (int i = b0; i < T; ++i)
     {
         const double2 c = coef[i];
         const double2 v = evecs[static_cast<size_t>(i) * T + t];
         acc.x += v.x * c.x - v.y * c.y;
         acc.y += v.x * c.y + v.y * c.x;
+        if (b0 > 0)
+        {
+            const double2 cr = comp[i];
+            proj.x += v.x * cr.x - v.y * cr.y;
+            proj.y += v.x * cr.y + v.y * cr.x;
+        }
+    }
+    if (b0 > 0)
+    {
+        const double2 y = Y[static_cast<size_t>(j) * T + t];
+        const double2 vj = evecs[static_cast<size_t>(rj) * T + t];
+        const double inv = 1.0 / lj;
+        acc.x += (y.x - lj * vj.x - proj.x) * inv;
+        acc.y += (y.y - lj * vj.y - proj.y) * inv;
     }
     Vn[static_cast<size_t>(j) * T + t] = acc;
 }
@@ -1625,6 +1658,241 @@ __global__ void k_eigref_finish(double2* __restrict__ evecs, double* __restrict_
         evals[rj] = eigref_lambda(D, G, T, r0, j);
 }
 
+// ------------------------------------------------------------------ top eigenpairs by subspace iteration
+// When only the largest eigenpairs are used (PCA views of the dominant components, ranks T - 16 ..
+// T - 1 at most) and T > 64, the block Jacobi's full diagonalisation (~1 ms per sweep at T = 512,
+// 5 or more sweeps) is replaced by a block subspace iteration on TS_P = 32 vectors in FP32: Y = C V
+// (all CTAs), V = orth(Y) (classical Gram-Schmidt applied twice, one CTA), repeated; then
+// Rayleigh-Ritz (H = V^H C V, Jacobi on the 32 x 32 H in one CTA) gives the Ritz pairs, and the kept
+// vectors are corrected in FP64 against the FP64 covariance with the Ritz vectors as the basis.
+// The error towards an eigenvector outside the subspace falls by lambda_33 / lambda_m per
+// iteration (m: the smallest kept rank from the top). The Ritz vectors of the previous window
+// are the warm start.
+constexpr int TS_P = 32;          // subspace size
+constexpr int TS_MAX_KEEP = 16;   // top ranks served (the other 16 vectors are the guard)
+constexpr int TS_LD = TS_P + 1;   // shared-memory row pitch (float2) of the orthonormalisation
+constexpr int TS_ORTH_THREADS = 512;
+constexpr int TS_ITERS_COLD = 8, TS_ITERS_WARM = 3;
+
+static size_t ts_bytes(int T)
+{
+    return static_cast<size_t>(T) * T * sizeof(float2) + 3 * static_cast<size_t>(T) * TS_P * sizeof(float2) + 512;
+}
+
+// C32 = 2^-e C (largest diagonal entry near 1); every CTA derives the factor from the diagonal, CTA
+// 0 also stores it
+__global__ void k_ts_convert(const double2* __restrict__ C, int T, float2* __restrict__ C32, double* __restrict__ scale)
+{
+    __shared__ double s_scale;
+    if (threadIdx.x < 32)
+    {
+        double m = 0.0;
+        for (int i = threadIdx.x; i < T; i += 32)
+            m = fmax(m, fabs(C[static_cast<size_t>(i) * T + i].x));
+        for (int o = 16; o > 0; o >>= 1)
+            m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0)
+        {
+            s_scale = jac_scale(m);
+            if (blockIdx.x == 0)
+                *scale = s_scale;
+        }
+    }
+    __syncthreads();
+    const double sc = s_scale;
+    const size_t n = static_cast<size_t>(T) * T;
+    for (size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
+         e += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        const double2 a = C[e];
+        C32[e] = make_float2(static_cast<float>(a.x * sc), static_cast<float>(a.y * sc));
+    }
+}
+
+// cold start: Y[t][k] = C32[t][k T / TS_P] (columns of C span its dominant eigenvectors)
+__global__ void k_ts_init(const float2* __restrict__ C32, int T, float2* __restrict__ Y)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= T * TS_P)
+        return;
+    const int t = e / TS_P, k = e % TS_P;
+    Y[e] = C32[static_cast<size_t>(t) * T + (k * T) / TS_P];
+}
+
+// Y[t][k] = sum_s C32[t][s] V[s][k]: thread (t, k), a warp covers the TS_P columns of one row
+__global__ void k_ts_matmul(const float2* __restrict__ C32, const float2* __restrict__ V, int T, float2* __restrict__ Y)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= T * TS_P)
+        return;
+    const int t = e / TS_P, k = e % TS_P;
+    const float2* c = C32 + static_cast<size_t>(t) * T;
+    float re = 0.f, im = 0.f;
+    for (int s2 = 0; s2 < T; ++s2)
+    {
+        const float2 a = c[s2], v = V[static_cast<size_t>(s2) * TS_P + k];
+        re = fmaf(a.x, v.x, fmaf(-a.y, v.y, re));
+        im = fmaf(a.x, v.y, fmaf(a.y, v.x, im));
+    }
+    Y[e] = make_float2(re, im);
+}
+
+// V = orth(Y), T x TS_P row-major, classical Gram-Schmidt applied twice per column, one CTA
+__global__ void __launch_bounds__(TS_ORTH_THREADS) k_ts_orth(const float2* __restrict__ Y, int T, float2* __restrict__ V)
+{
+    extern __shared__ float2 ts_s[];  // T x TS_LD
+    __shared__ float2 c[TS_P];
+    __shared__ float red[TS_ORTH_THREADS / 32];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    constexpr int NW = TS_ORTH_THREADS / 32;
+    for (int e = tid; e < T * TS_P; e += TS_ORTH_THREADS)
+        ts_s[(e / TS_P) * TS_LD + e % TS_P] = Y[e];
+    __syncthreads();
+    for (int k = 0; k < TS_P; ++k)
+    {
+        for (int pass = 0; pass < 2 && k > 0; ++pass)
+        {
+            for (int i = warp; i < k; i += NW)
+            {
+                float re = 0.f, im = 0.f;
+                for (int t = lane; t < T; t += 32)
+                {
+                    const float2 a = ts_s[t * TS_LD + i], b = ts_s[t * TS_LD + k];
+                    re += a.x * b.x + a.y * b.y;
+                    im += a.x * b.y - a.y * b.x;
+                }
+                for (int o = 16; o > 0; o >>= 1)
+                {
+                    re += __shfl_xor_sync(0xffffffffu, re, o);
+                    im += __shfl_xor_sync(0xffffffffu, im, o);
+                }
+                if (lane == 0)
+                    c[i] = make_float2(re, im);
+            }
+            __syncthreads();
+            for (int t = tid; t < T; t += TS_ORTH_THREADS)
+            {
+                float2 y = ts_s[t * TS_LD + k];
+                for (int i = 0; i < k; ++i)
+                {
+                    const float2 v = ts_s[t * TS_LD + i], ci = c[i];
+                    y.x -= v.x * ci.x - v.y * ci.y;
+                    y.y -= v.x * ci.y + v.y * ci.x;
+                }
+                ts_s[t * TS_LD + k] = y;
+            }
+            __syncthreads();
+        }
+        float n2 = 0.f;
+        for (int t = tid; t < T; t += TS_ORTH_THREADS)
+        {
+            const float2 y = ts_s[t * TS_LD + k];
+            n2 += y.x * y.x + y.y * y.y;
+        }
+        for (int o = 16; o > 0; o >>= 1)
+            n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+        if (lane == 0)
+            red[warp] = n2;
+        __syncthreads();
+        float tot = 0.f;
+        for (int w = 0; w < NW; ++w)
+            tot += red[w];
+        // a column dependent on the previous ones (a covariance of rank < TS_P) is replaced by
+        // the unit vector e_k, made orthogonal at the next iteration
+        const bool dead = !(tot > 0.f) || !isfinite(tot);
+        const float inv = dead ? 0.f : rsqrtf(tot);
+        for (int t = tid; t < T; t += TS_ORTH_THREADS)
+        {
+            const float2 y = ts_s[t * TS_LD + k];
+            ts_s[t * TS_LD + k] = dead ? make_float2(t == k ? 1.f : 0.f, 0.f) : make_float2(y.x * inv, y.y * inv);
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < T * TS_P; e += TS_ORTH_THREADS)
+        V[e] = ts_s[(e / TS_P) * TS_LD + e % TS_P];
+}
+
+// Rayleigh-Ritz: H = V^H Y (Y = C32 V), H Q = Q diag(theta) by FP32 Jacobi, Ritz vectors U = V Q in
+// ascending order: evecs columns T - TS_P .. T - 1 (FP64) and the warm start `Vw`, the Ritz values
+// (scaled back) into evals[T - TS_P ..], evals below set to 0. One CTA.
+__global__ void __launch_bounds__(JS_THREADS) k_ts_rr(const float2* __restrict__ V, const float2* __restrict__ Y, int T,
+                                                     const double* __restrict__ scale, double2* __restrict__ evecs,
+                                                     double* __restrict__ evals, float2* __restrict__ Vw)
+{
+    __shared__ Cx<float> Hs[TS_P * TS_LD], Qs[TS_P * TS_LD];
+    __shared__ JacScratch<float> sc;
+    __shared__ int order[TS_P];
+    __shared__ float s_fro[JS_THREADS / 32];
+    const int tid = threadIdx.x;
+    for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
+    {
+        const int i = e / TS_P, k = e % TS_P;
+        float re = 0.f, im = 0.f;
+        for (int t = 0; t < T; ++t)
+        {
+            const float2 a = V[static_cast<size_t>(t) * TS_P + i], b = Y[static_cast<size_t>(t) * TS_P + k];
+            re += a.x * b.x + a.y * b.y;
+            im += a.x * b.y - a.y * b.x;
+        }
+        Hs[i * TS_LD + k] = {re, im};
+        Qs[i * TS_LD + k] = {i == k ? 1.f : 0.f, 0.f};
+    }
+    __syncthreads();
+    // Hermitian part, real diagonal; round-off floor as in the other FP32 sweeps
+    float f2 = 0.f;
+    for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
+    {
+        const int i = e / TS_P, k = e % TS_P;
+        if (i <= k)
+        {
+            const Cx<float> a = Hs[i * TS_LD + k], b = Hs[k * TS_LD + i];
+            const Cx<float> h = {0.5f * (a.x + b.x), i == k ? 0.f : 0.5f * (a.y - b.y)};
+            Hs[i * TS_LD + k] = h;
+            Hs[k * TS_LD + i] = {h.x, -h.y};
+            f2 += (i == k ? 1.f : 2.f) * (h.x * h.x + h.y * h.y);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        f2 += __shfl_xor_sync(0xffffffffu, f2, o);
+    if ((tid & 31) == 0)
+        s_fro[tid >> 5] = f2;
+    __syncthreads();
+    float tot = 0.f;
+    for (int w = 0; w < JS_THREADS / 32; ++w)
+        tot += s_fro[w];
+    smem_sweeps<float, JS_THREADS>(Hs, Qs, TS_P, TS_P, TS_LD, sc, 5e-7f * sqrtf(tot), JAC_MAX_SWEEPS);
+    __syncthreads();
+    if (tid < TS_P)
+    {
+        const float th = Hs[tid * TS_LD + tid].x;
+        int rank = 0;
+        for (int j = 0; j < TS_P; ++j)
+        {
+            const float tj = Hs[j * TS_LD + j].x;
+            rank += (tj < th) || (tj == th && j < tid);
+        }
+        order[rank] = tid;
+        evals[T - TS_P + rank] = static_cast<double>(th) / *scale;
+    }
+    for (int i = tid; i < T - TS_P; i += JS_THREADS)
+        evals[i] = 0.0;
+    __syncthreads();
+    for (int e = tid; e < T * TS_P; e += JS_THREADS)
+    {
+        const int t = e / TS_P, r = e % TS_P, q = order[r];
+        float re = 0.f, im = 0.f;
+        for (int k = 0; k < TS_P; ++k)
+        {
+            const float2 v = V[static_cast<size_t>(t) * TS_P + k];
+            const Cx<float> qq = Qs[k * TS_LD + q];
+            re += v.x * qq.x - v.y * qq.y;
+            im += v.x * qq.y + v.y * qq.x;
+        }
+        Vw[e] = make_float2(re, im);
+        evecs[static_cast<size_t>(T - TS_P + r) * T + t] = make_double2(re, im);
+    }
+}
+
 static std::atomic<int> g_eig_precision{HV_EIG_FP32};
 
 void set_eig_precision(int p) { g_eig_precision = p; }
@@ -1638,7 +1906,7 @@ size_t pca_eigh_workspace(int T)
     const int Tp = (T % 2) ? T + 1 : T;
     size_t bytes = static_cast<size_t>(T) * T * sizeof(double2) + static_cast<size_t>(2 * Tp) * sizeof(double) +
                    static_cast<size_t>(T) * sizeof(double) + static_cast<size_t>(Tp) * sizeof(int) + 256 +
-                   eigref_bytes(T);
+                   eigref_bytes(T) + (T > JS_MAX_T ? ts_bytes(T) : 0);
     if (T > JS_MAX_T && T <= JC_MAX_T)
     {
         // block Jacobi: FP32 A and V (two copies each) of the size rounded up to 64, the step's
@@ -1650,10 +1918,18 @@ size_t pca_eigh_workspace(int T)
 }
 
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
-                   cudaStream_t st, int refine_lo, int refine_hi, bool warm)
+                   cudaStream_t st, int refine_lo, int refine_hi, bool warm, bool kept_only)
 {
     if (T <= 0 || !work)
         return HV_INVALID_VALUE;
+    // kept_only: the caller uses the refined eigenvectors (ranks refine_lo..refine_hi) and the
+    // order of the eigenvalues only, so the FP32 sweeps stop at a coarser floor and the other
+    // eigenvalues are FP32 Rayleigh quotients (cfg3, T = 512: 15 sweeps and 13.8 ms -> 5 sweeps, the
+    // view unchanged at 3.5e-7 from FP64)
+    const int Kr = refine_hi - refine_lo + 1;
+    const bool loose = kept_only && refine_lo >= 0 && refine_hi < T && Kr >= 1 && Kr <= ER_MAX_K;
+    const float floor_rel = loose ? 2e-5f : 5e-7f;
+
     const int prec = g_eig_precision.load();  // one read: a concurrent switch cannot split the dispatch
     const int Tp = (T % 2) ? T + 1 : T;
     char* base = static_cast<char*>(work);
@@ -1664,16 +1940,82 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     double* ev_unsorted = reinterpret_cast<double*>(base + off);
     off += static_cast<size_t>(T) * sizeof(double);
     int* pairs = reinterpret_cast<int*>(base + off);
-    // refinement buffers: after the pair list, before the block-Jacobi arrays
+    // refinement buffers: after the pair list, before the subspace and block-Jacobi arrays
     char* er_base = base + ((off + static_cast<size_t>(Tp) * sizeof(int) + 255) & ~static_cast<size_t>(255));
     off += eigref_bytes(T);
+    char* ts_base = base + ((off + static_cast<size_t>(Tp) * sizeof(int) + 255) & ~static_cast<size_t>(255));
+    if (T > JS_MAX_T)
+        off += ts_bytes(T);
+    // FP64 correction of the kept eigenvectors (ranks refine_lo .. refine_hi) against the FP64
+    // covariance, with the eigenvectors of ranks b0 .. T-1 as the basis; `iters` corrections (the
+    // first leaves O(theta^2) against the FP32 error of the basis, the next bring that to the FP64
+    // level)
+    auto refine_kept = [&](int b0, int iters) -> hv_status {
+        double2* Y = reinterpret_cast<double2*>(er_base);
+        double2* D = Y + static_cast<size_t>(ER_MAX_K) * T;
+        double2* G = D + static_cast<size_t>(ER_MAX_K) * T;
+        double2* Vn = G + static_cast<size_t>(ER_MAX_K) * T;
+        const dim3 gw((T + 7) / 8, Kr), gp((T - b0 + 7) / 8, Kr), gt((T + 127) / 128, Kr);
+        for (int iter = 0; iter < iters; ++iter)
+        {
+            k_eigref_matvec<<<gw, 256, 0, st>>>(cov, evecs, T, refine_lo, Y);
+            HV_LAUNCH_CHECK();
+            k_eigref_project<<<gp, 256, 0, st>>>(evecs, Y, T, refine_lo, b0, D, G);
+            HV_LAUNCH_CHECK();
+            k_eigref_update<<<gt, 128, 0, st>>>(evecs, evals, D, G, Y, T, refine_lo, Kr, b0, Vn);
+            HV_LAUNCH_CHECK();
+            k_eigref_finish<<<Kr, 128, 0, st>>>(evecs, evals, Vn, D, G, T, refine_lo, pmin, pmax, weights);
+            HV_LAUNCH_CHECK();
+            count_launch(4);
+        }
+        return HV_OK;
+    };
+    // the largest eigenpairs only: subspace iteration instead of the block Jacobi
+    if (loose && prec == HV_EIG_FP32 && T > JS_MAX_T && T <= JC_MAX_T && refine_lo >= T - TS_MAX_KEEP)
+    {
+        float2* C32 = reinterpret_cast<float2*>(ts_base);
+        float2* Vs = C32 + static_cast<size_t>(T) * T;
+        float2* Ys = Vs + static_cast<size_t>(T) * TS_P;
+        float2* Vw = Ys + static_cast<size_t>(T) * TS_P;
+        double* scale = reinterpret_cast<double*>(Vw + static_cast<size_t>(T) * TS_P);
+        const int gb = (T * TS_P + 255) / 256;
+        const size_t osmem = static_cast<size_t>(T) * TS_LD * sizeof(float2);
+        static const cudaError_t attr = cudaFuncSetAttribute(
+            k_ts_orth, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(JC_MAX_T * TS_LD * sizeof(float2)));
+        HV_CUDA_TRY(attr);
+        k_ts_convert<<<std::min(512, (T * T + 1023) / 1024), 256, 0, st>>>(cov, T, C32, scale);
+        HV_LAUNCH_CHECK();
+        if (warm)
+            k_ts_orth<<<1, TS_ORTH_THREADS, osmem, st>>>(Vw, T, Vs);
+        else
+        {
+            k_ts_init<<<gb, 256, 0, st>>>(C32, T, Ys);
+            HV_LAUNCH_CHECK();
+            k_ts_orth<<<1, TS_ORTH_THREADS, osmem, st>>>(Ys, T, Vs);
+        }
+        HV_LAUNCH_CHECK();
+        const int iters = warm ? TS_ITERS_WARM : TS_ITERS_COLD;
+        for (int it = 0; it < iters; ++it)
+        {
+            k_ts_matmul<<<gb, 256, 0, st>>>(C32, Vs, T, Ys);
+            HV_LAUNCH_CHECK();
+            k_ts_orth<<<1, TS_ORTH_THREADS, osmem, st>>>(Ys, T, Vs);
+            HV_LAUNCH_CHECK();
+        }
+        k_ts_matmul<<<gb, 256, 0, st>>>(C32, Vs, T, Ys);
+        HV_LAUNCH_CHECK();
+        k_ts_rr<<<1, JS_THREADS, 0, st>>>(Vs, Ys, T, scale, evecs, evals, Vw);
+        HV_LAUNCH_CHECK();
+        count_launch(4 + 2 * iters + (warm ? 0 : 1));
+        return refine_kept(T - TS_P, 3);
+    }
     if (T <= JS_MAX_T && prec == HV_EIG_FP32)
     {
         const size_t smem = jacobi_smem_bytes<float>(T, warm);
         if (smem > 48 * 1024)
             HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(jacobi_smem_bytes<float>(JS_MAX_T, true))));
-        k_jacobi_smem<float><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted, warm ? 1 : 0);
+        k_jacobi_smem<float><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted, warm ? 1 : 0, floor_rel);
     }
     else if (T <= JS_MAX_T)
     {
@@ -1681,7 +2023,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         if (smem > 48 * 1024)
             HV_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem)));
-        k_jacobi_smem<double><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted, 0);
+        k_jacobi_smem<double><<<1, JS_THREADS, smem, st>>>(cov, V, T, Tp, ev_unsorted, 0, 0.0f);
     }
     else if (T <= JC_MAX_T && prec == HV_EIG_FP32)
     {
@@ -1718,7 +2060,8 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         nb = nb > cap ? cap : nb;
         int Ti = T, Tbi = Tb;
         const double2* cin = cov;
-        void* args[] = {&cin, &Ti, &Tbi, &A0, &A1, &V0, &V1, &U, &flags, &fro2, &bar, &V, &ev_unsorted};
+        double fr = floor_rel;
+        void* args[] = {&cin, &Ti, &Tbi, &A0, &A1, &V0, &V1, &U, &flags, &fro2, &bar, &V, &ev_unsorted, &fr};
         HV_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_jacobi_block), nb, BJ_THREADS, args, BJ_SMEM,
                                                 st));
         count_launch();
@@ -1726,7 +2069,10 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     if (T <= JS_MAX_T || (T <= JC_MAX_T && prec == HV_EIG_FP32))
     {
         HV_LAUNCH_CHECK();
-        k_eig_refine<<<T, 128, 0, st>>>(cov, V, T, ev_unsorted);
+        if (loose)
+            k_eig_refine<float><<<T, 128, 0, st>>>(cov, V, T, ev_unsorted);
+        else
+            k_eig_refine<double><<<T, 128, 0, st>>>(cov, V, T, ev_unsorted);
         count_launch();
     }
     else
@@ -1737,28 +2083,11 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
     count_launch(2);
     // FP32 sweeps: the kept eigenvectors are corrected in FP64 (FP64 sweeps need no correction)
     const bool fp32_sweeps = T <= JS_MAX_T ? prec == HV_EIG_FP32 : (T <= JC_MAX_T && prec == HV_EIG_FP32);
-    const int K = refine_hi - refine_lo + 1;
-    if (fp32_sweeps && refine_lo >= 0 && refine_hi < T && K >= 1 && K <= ER_MAX_K)
+    if (fp32_sweeps && refine_lo >= 0 && refine_hi < T && Kr >= 1 && Kr <= ER_MAX_K)
     {
-        double2* Y = reinterpret_cast<double2*>(er_base);
-        double2* D = Y + static_cast<size_t>(ER_MAX_K) * T;
-        double2* G = D + static_cast<size_t>(ER_MAX_K) * T;
-        double2* Vn = G + static_cast<size_t>(ER_MAX_K) * T;
-        const dim3 gw((T + 7) / 8, K), gt((T + 127) / 128, K);
-        // two corrections: the first leaves O(theta^2) against the FP32 error of the other
-        // eigenvectors, the second brings that to the FP64 level
-        for (int iter = 0; iter < 2; ++iter)
-        {
-            k_eigref_matvec<<<gw, 256, 0, st>>>(cov, evecs, T, refine_lo, Y);
-            HV_LAUNCH_CHECK();
-            k_eigref_project<<<gw, 256, 0, st>>>(evecs, Y, T, refine_lo, D, G);
-            HV_LAUNCH_CHECK();
-            k_eigref_update<<<gt, 128, 0, st>>>(evecs, evals, D, G, T, refine_lo, K, Vn);
-            HV_LAUNCH_CHECK();
-            k_eigref_finish<<<K, 128, 0, st>>>(evecs, evals, Vn, D, G, T, refine_lo, pmin, pmax, weights);
-            HV_LAUNCH_CHECK();
-            count_launch(4);
-        }
+        hv_status rr = refine_kept(0, loose ? 3 : 2);
+        if (rr != HV_OK)
+            return rr;
     }
     return HV_OK;
 }

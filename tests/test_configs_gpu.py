@@ -115,7 +115,8 @@ def test_cfg2_full_size(cuda, unwrap):
 
 @pytest.mark.gpu
 def test_cfg3_full_size_and_eigenvalues(cuda):
-    pipe, oracle, s, _ = _run("cfg3", 8)
+    # two windows: the second one's eigensolve starts from the first one's Ritz vectors
+    pipe, oracle, s, _ = _run("cfg3", 9)
     ring, _, _ = pipe.ring()
     pipe.close()
     T = s.time_transformation_size

@@ -74,11 +74,13 @@ def test_covariance_and_eigh(cuda, T, H, W):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("T,img", [(32, 0), (64, 1), (16, 0)])
+@pytest.mark.parametrize("T,img", [(32, 0), (64, 1), (16, 0), (128, 0), (256, 1)])
 def test_pipe_pca_windows_warm_start(cuda, T, img):
-    """Consecutive PCA windows of one Pipe: from the second window on, the FP32 sweeps start from
-    the previous window's eigenvectors. Every window's float frame within rel-L2 1e-4 of the oracle
-    (modulus views depend on each kept eigenvector, not only on the kept subspace)."""
+    """Consecutive PCA windows of one Pipe: from the second window on, the eigensolve starts from
+    the previous window's eigenvectors (T <= 64: the FP32 Jacobi sweeps; T > 64 with the dominant
+    components kept: the subspace iteration from the previous Ritz vectors). Every window's float
+    frame within rel-L2 1e-4 of the oracle (modulus views depend on each kept eigenvector, not only
+    on the kept subspace)."""
     from gpu_util import oracle_settings
 
     from holovibes_gb300.synthetic import Interferogram
