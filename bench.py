@@ -402,19 +402,38 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------------ our arm
-def time_kernel(fn, stream, n=20):
+def time_kernel(fn, stream, n=20, reps=3):
+    """Device time of one call of `fn` (ms) and how it was taken. The n calls are captured in a CUDA
+    graph and replayed, so that the host's enqueue rate (a ctypes call and its launches take tens of
+    microseconds on the host cores) does not set the figure for kernels of 50-100 us; calls that
+    cannot be captured are timed as n eager launches."""
     import torch
 
     for _ in range(3):
         fn()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            for _ in range(n):
+                fn()
+        g.replay()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            g.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / (n * reps), "graph"
+    except Exception:
+        torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(n):
         fn()
     e1.record(stream)
     torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / n  # ms
+    return e0.elapsed_time(e1) / n, "eager"
 
 
 def steps_for(hv, fd, s, dev_batch, stream):
@@ -480,9 +499,32 @@ def steps_for(hv, fd, s, dev_batch, stream):
                     T * HW * 8 + HW * 4, 0))
     if s.time_transformation == hv.TIME_PCA:
         cov, cw = buf(T * T * 16), buf(L.hv_pca_cov_workspace(T, HW))
-        out.append(("pca_covariance", lambda: L.hv_pca_covariance(ring.data_ptr(), T, HW, cov.data_ptr(),
-                                                                  cw.data_ptr(), stream), T * HW * 8,
-                    3 * 8 * HW * T * T))
+        pb = L.hv_pca_planes_bytes(T, HW)
+        S = s.time_stride
+        if pb and S < T:
+            # the pipe's path for T > 64: each window's S new frames are split into BF16 planes, and
+            # the covariance rows and columns of the 64-frame slot blocks they land in (one window:
+            # slots 0 .. S-1) are recomputed from the planes: every frame of the ring is read once,
+            # the tiles touching those blocks are multiplied
+            planes = buf(pb)
+            hv.check(L.hv_pca_split_planes(ring.data_ptr(), T, HW, 0, T, planes.data_ptr(), stream), "split")
+            nb = (T + 63) // 64
+            blocks = 0
+            for sl in range(S):
+                blocks |= 1 << (sl // 64)
+            tiles = sum(1 for bm in range(nb) for bn in range(bm, nb) if (blocks >> bm) & 1 or (blocks >> bn) & 1)
+            out.append(("ring_split", lambda: L.hv_pca_split_planes(ring.data_ptr(), T, HW, 0, S, planes.data_ptr(),
+                                                                    stream), S * HW * 16, 0))
+            out.append(("pca_covariance", lambda: L.hv_pca_covariance_planes(planes.data_ptr(), T, HW, blocks,
+                                                                             cov.data_ptr(), cw.data_ptr(), stream),
+                        T * HW * 8, tiles * 3 * 2 * 128 * 128 * HW))
+        else:
+            # tensor flops: the 128 x 128 tiles of the 2T x 2T real Gram matrix on or above its
+            # diagonal, three BF16 products each (T <= 32: one packed 128 x 128 product)
+            nb = (T + 63) // 64
+            flops = 2 * 128 * 128 * HW if 2 * T <= 64 else nb * (nb + 1) // 2 * 3 * 2 * 128 * 128 * HW
+            out.append(("pca_covariance", lambda: L.hv_pca_covariance(ring.data_ptr(), T, HW, cov.data_ptr(),
+                                                                      cw.data_ptr(), stream), T * HW * 8, flops))
     return out
 
 
@@ -518,9 +560,10 @@ def roofline(hv, fd, s, dev_batch, peaks, workload=""):
     stream = torch.cuda.Stream()
     kernels = steps_for(hv, fd, s, dev_batch, stream.cuda_stream)
     rows = []
+    timing = {}
     with torch.cuda.stream(stream):
         for name, fn, alg_bytes, flops in kernels:
-            ms = time_kernel(lambda: hv.check(fn(), name), stream)
+            ms, timing[name] = time_kernel(lambda: hv.check(fn(), name), stream)
             rows.append((name, ms, alg_bytes, flops))
     name, ms, alg, flops = max(rows, key=lambda r: r[1])
     gbs = alg / (ms * 1e-3) / 1e9
@@ -531,7 +574,8 @@ def roofline(hv, fd, s, dev_batch, peaks, workload=""):
            "ms_per_launch": ms, "traffic": traffic,
            "traffic_source": cmd if traffic else "no ncu capture of these kernel sources (profiles/ncu_traffic.json)",
            "all": {n: {"ms": round(m, 5), "GB/s": round(b / (m * 1e-3) / 1e9, 1),
-                       **({"TFLOP/s": round(f / (m * 1e-3) / 1e12, 1)} if f else {})} for n, m, b, f in rows}}
+                       **({"TFLOP/s": round(f / (m * 1e-3) / 1e12, 1)} if f else {}), "timing": timing[n]}
+                   for n, m, b, f in rows}}
     if tc_frac > hbm_frac:
         out.update(bound="tensor", achieved=tfs, peak=peak_tf, unit="TFLOP/s", frac=tc_frac, hbm_frac=hbm_frac)
     else:
@@ -543,9 +587,16 @@ def roofline(hv, fd, s, dev_batch, peaks, workload=""):
 def dtype_of(hv, s) -> str:
     parts = ["f32 (convert, FFT passes, views, render)"]
     if s.time_transformation == hv.TIME_PCA:
-        # the bench keeps the library's default eigensolver precision (FP32 sweeps up to T = 512)
-        eig = "f64 Jacobi sweeps" if s.time_transformation_size > 512 else \
-            "f32 Jacobi sweeps + f64 Rayleigh quotients / normalisation"
+        # the library's default eigensolver precision: FP32 iterations, the viewed (kept) eigenvectors
+        # corrected in FP64 against the FP64 covariance; FP64 sweeps above T = 512
+        T = s.time_transformation_size
+        top = s.p_start >= T - 16
+        if T > 512:
+            eig = "f64 Jacobi sweeps"
+        elif T > 64 and top:
+            eig = "f32 block subspace iteration (32 vectors) + Rayleigh-Ritz, f64 correction of the kept eigenvectors"
+        else:
+            eig = "f32 Jacobi sweeps, f64 correction of the kept eigenvectors"
         parts.append("bf16x3 on tcgen05 with f32 accumulation, f64 reduce (covariance)")
         parts.append(f"{eig} (eigensolve)")
     elif s.time_transformation in (hv.TIME_STFT, hv.TIME_SSA_STFT):

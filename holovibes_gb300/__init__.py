@@ -197,7 +197,7 @@ def lib() -> C.CDLL:
 
 
 def _declare(L: C.CDLL) -> None:
-    vp, sz, i32, f32, i64, u64 = C.c_void_p, C.c_size_t, C.c_int, C.c_float, C.c_int64, C.c_uint64
+    vp, sz, i32, f32, i64, u64, u32 = C.c_void_p, C.c_size_t, C.c_int, C.c_float, C.c_int64, C.c_uint64, C.c_uint
     st = C.c_int
     sig = {
         "hv_version": (C.c_char_p, []),
@@ -258,6 +258,10 @@ def _declare(L: C.CDLL) -> None:
         "hv_pca_covariance": (st, [vp, i32, sz, vp, vp, vp]),
         "hv_pca_cov_workspace": (sz, [i32, sz]),
         "hv_pca_covariance_mode": (None, [i32]),
+        "hv_pca_cov_incremental": (None, [i32]),
+        "hv_pca_planes_bytes": (sz, [i32, sz]),
+        "hv_pca_split_planes": (st, [vp, i32, sz, i32, i32, vp, vp]),
+        "hv_pca_covariance_planes": (st, [vp, i32, sz, u32, vp, vp, vp]),
         "hv_pca_covariance_status": (st, [vp]),
         "hv_pca_eigh": (st, [vp, i32, vp, vp, i32, i32, vp, vp, vp]),
         "hv_pca_eigh_workspace": (sz, [i32]),

@@ -21,6 +21,8 @@
 //              `done` releases the epilogue (warps 0-3 read the accumulator lanes 32w..32w+31)
 // Every wait is bounded in time and reports through the error flag. Per-CTA partial G tiles are
 // summed in FP64 by k_cov_tc_reduce.
+#include <algorithm>
+#include <cstring>
 #include <cuda_bf16.h>
 
 #include "hv_common.cuh"
@@ -348,21 +350,22 @@ constexpr int TT_THREADS = TT_CONVERTERS + 64;
 constexpr uint32_t TT_RAW_HALF = TT_FRAMES * TC_KC * 8;  // one [64 frames][64 px] complex chunk: 32 KB
 constexpr int TT_MAX_RAW = 3;
 
-__device__ __forceinline__ void tile_pair(int tp, int nb, int& bm, int& bn)
-{
-    int m = 0, rem = tp;
-    while (rem >= nb - m)
-    {
-        rem -= nb - m;
-        ++m;
-    }
-    bm = m;
-    bn = m + rem;
-}
+constexpr int TT_MAX_BLOCKS = COV_TC_MAX_T / TT_FRAMES;  // 64-frame blocks of a ring (16)
+constexpr int TT_MAX_PAIRS = TT_MAX_BLOCKS * (TT_MAX_BLOCKS + 1) / 2;
 
-// part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * npairs + tp)
+// The tiles (bm <= bn) one launch computes, and the index of tile (bm, bn) in that list (-1: not
+// computed): every tile of G, or the tiles touching the 64-frame blocks whose ring slots were
+// rewritten since the covariance was last computed.
+struct TileList
+{
+    int n;
+    unsigned char bm[TT_MAX_PAIRS], bn[TT_MAX_PAIRS];
+    signed char index[TT_MAX_BLOCKS][TT_MAX_BLOCKS];
+};
+
+// part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * tiles.n + tp)
 __global__ void __launch_bounds__(TT_THREADS, 1) k_cov_tc_tiled(const __grid_constant__ CUtensorMap ring_map,
-                                                                size_t npix, int nb, int npairs,
+                                                                size_t npix, const __grid_constant__ TileList tiles_in,
                                                                 size_t chunks_per_split, int raw_stages,
                                                                 float* __restrict__ part, int* __restrict__ err)
 {
@@ -376,10 +379,9 @@ __global__ void __launch_bounds__(TT_THREADS, 1) k_cov_tc_tiled(const __grid_con
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int R = raw_stages;
-    const int tp = static_cast<int>(blockIdx.x % static_cast<unsigned>(npairs));
-    const int ks = static_cast<int>(blockIdx.x / static_cast<unsigned>(npairs));
-    int bm, bn;
-    tile_pair(tp, nb, bm, bn);
+    const int tp = static_cast<int>(blockIdx.x % static_cast<unsigned>(tiles_in.n));
+    const int ks = static_cast<int>(blockIdx.x / static_cast<unsigned>(tiles_in.n));
+    const int bm = tiles_in.bm[tp], bn = tiles_in.bn[tp];
     const bool diag = bm == bn;
     const uint32_t raw_bytes = 2 * TT_RAW_HALF;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
@@ -556,30 +558,266 @@ __global__ void __launch_bounds__(TT_THREADS, 1) k_cov_tc_tiled(const __grid_con
 }
 
 // cov[i][j] from the tiled partials: row 2i of G is row 2 (i % 64) of tile row i / 64; the upper
-// triangle (i <= j) is read from tile (i / 64, j / 64) and mirrored. Sums in FP64 over the splits.
-__global__ void k_cov_tc_tiled_reduce(const float* __restrict__ part, int T, int nb, int npairs, int nsplit,
-                                      double2* __restrict__ cov)
+// triangle (i <= j) is read from tile (i / 64, j / 64) and mirrored. Sums in FP64 over the splits:
+// a CTA holds TR_ENTRIES consecutive entries, group q of its threads sums the splits q, q + TR_GROUPS,
+// ..., and the group sums are added in group order. Entries of tiles outside the list are left as
+// they are.
+constexpr int TR_ENTRIES = 64, TR_GROUPS = 4;
+__global__ void __launch_bounds__(TR_ENTRIES * TR_GROUPS) k_cov_tc_tiled_reduce(const float* __restrict__ part, int T,
+                                                                               const __grid_constant__ TileList tiles,
+                                                                               int nsplit, double2* __restrict__ cov)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= T * T)
-        return;
-    const int ei = e / T, ej = e % T;
-    const bool mirror = ei > ej;
-    const int i = mirror ? ej : ei, j = mirror ? ei : ej;
-    const int bm = i / TT_FRAMES, bn = j / TT_FRAMES;
-    const int tp = bm * nb - bm * (bm - 1) / 2 + (bn - bm);  // rows 0 .. bm-1 hold nb, nb-1, ... tiles
-    const int ri = 2 * (i % TT_FRAMES), cj = 2 * (j % TT_FRAMES);
-    double g00 = 0, g11 = 0, g01 = 0, g10 = 0;
-    for (int k = 0; k < nsplit; ++k)
+    __shared__ double red[TR_GROUPS - 1][4][TR_ENTRIES];
+    const int q = threadIdx.x / TR_ENTRIES, el = threadIdx.x % TR_ENTRIES;
+    const int e = blockIdx.x * TR_ENTRIES + el;
+    int tp = -1, ri = 0, cj = 0;
+    bool mirror = false, diag = false;
+    if (e < T * T)
     {
-        const float* G = part + (static_cast<size_t>(k) * npairs + tp) * TC_ROWS * TC_ROWS;
-        g00 += G[ri * TC_ROWS + cj];
-        g11 += G[(ri + 1) * TC_ROWS + cj + 1];
-        g01 += G[ri * TC_ROWS + cj + 1];
-        g10 += G[(ri + 1) * TC_ROWS + cj];
+        const int ei = e / T, ej = e % T;
+        mirror = ei > ej;
+        diag = ei == ej;
+        const int i = mirror ? ej : ei, j = mirror ? ei : ej;
+        tp = tiles.index[i / TT_FRAMES][j / TT_FRAMES];
+        ri = 2 * (i % TT_FRAMES);
+        cj = 2 * (j % TT_FRAMES);
     }
-    const double im = i == j ? 0.0 : (g01 - g10);
+    double g00 = 0, g11 = 0, g01 = 0, g10 = 0;
+    if (tp >= 0)
+    {
+        const int npairs = tiles.n;
+        for (int k = q; k < nsplit; k += TR_GROUPS)
+        {
+            const float* G = part + (static_cast<size_t>(k) * npairs + tp) * TC_ROWS * TC_ROWS;
+            g00 += G[ri * TC_ROWS + cj];
+            g11 += G[(ri + 1) * TC_ROWS + cj + 1];
+            g01 += G[ri * TC_ROWS + cj + 1];
+            g10 += G[(ri + 1) * TC_ROWS + cj];
+        }
+    }
+    if (q > 0)
+    {
+        red[q - 1][0][el] = g00;
+        red[q - 1][1][el] = g11;
+        red[q - 1][2][el] = g01;
+        red[q - 1][3][el] = g10;
+    }
+    __syncthreads();
+    if (q > 0 || tp < 0)
+        return;
+    for (int w = 0; w < TR_GROUPS - 1; ++w)
+    {
+        g00 += red[w][0][el];
+        g11 += red[w][1][el];
+        g01 += red[w][2][el];
+        g10 += red[w][3][el];
+    }
+    const double im = diag ? 0.0 : (g01 - g10);
     cov[e] = make_double2(g00 + g11, mirror ? -im : im);
+}
+
+// ------------------------------------------------------------------ tiled, from pre-split planes
+// The split-BF16 operands of the ring kept beside it: planes[p][2 s + c][px] (p = 0: hi = bf16_rn(x),
+// p = 1: lo = bf16_rn(x - hi); c = 0: real, c = 1: imaginary part of pixel px of ring slot s), written
+// once per frame when it enters the ring. The tiled covariance then streams the four operand tiles
+// of a chunk (Ah, Al, Bh, Bl: 128 rows x 64 pixels each) by 3-D tensor copies straight into the
+// swizzled K-major layout the MMAs read: no converter warps, and a chunk is split once instead of
+// once per tile it takes part in. Same tiles, splits, MMA order and partial layout as
+// k_cov_tc_tiled: the results are bit-identical.
+
+// Thread: 8 consecutive pixels of one frame of slots slot0 .. slot0 + n - 1 (mod T).
+__global__ void k_ring_split(const float2* __restrict__ ring, int T, size_t npix, int slot0, int n,
+                             uint16_t* __restrict__ planes)
+{
+    const size_t groups = npix / 8;
+    const size_t total = static_cast<size_t>(n) * groups;
+    const size_t plane = 2 * static_cast<size_t>(T) * npix;
+    for (size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
+         e += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        const int f = static_cast<int>(e / groups);
+        const size_t g = e % groups;
+        const size_t slot = static_cast<size_t>((slot0 + f) % T);
+        const float4* src = reinterpret_cast<const float4*>(ring + slot * npix + 8 * g);
+        const float4 a = src[0], b = src[1], c = src[2], d = src[3];
+        uint4 rh, rl, ih, il;
+        tc::split2(a.x, a.z, rh.x, rl.x);
+        tc::split2(b.x, b.z, rh.y, rl.y);
+        tc::split2(c.x, c.z, rh.z, rl.z);
+        tc::split2(d.x, d.z, rh.w, rl.w);
+        tc::split2(a.y, a.w, ih.x, il.x);
+        tc::split2(b.y, b.w, ih.y, il.y);
+        tc::split2(c.y, c.w, ih.z, il.z);
+        tc::split2(d.y, d.w, ih.w, il.w);
+        uint16_t* re = planes + 2 * slot * npix + 8 * g;
+        *reinterpret_cast<uint4*>(re) = rh;
+        *reinterpret_cast<uint4*>(re + npix) = ih;
+        *reinterpret_cast<uint4*>(re + plane) = rl;
+        *reinterpret_cast<uint4*>(re + plane + npix) = il;
+    }
+}
+
+constexpr int TP_STAGES = 3;
+constexpr int TP_EPI_WARPS = 4;               // warps 0-3 read the accumulators
+constexpr int TP_MMA_WARP = TP_EPI_WARPS;     // warp 4 issues the MMAs
+constexpr int TP_LOAD_WARP = TP_EPI_WARPS + 1;  // warp 5 issues the tensor copies
+constexpr int TP_THREADS = (TP_EPI_WARPS + 2) * 32;
+constexpr uint32_t TP_STAGE_BYTES = 4 * TILE_BYTES;  // Ah, Al, Bh, Bl
+
+// part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * tiles.n + tp), as k_cov_tc_tiled
+__global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_planes(const __grid_constant__ CUtensorMap planes_map,
+                                                                 size_t npix, const __grid_constant__ TileList tiles_in,
+                                                                 size_t chunks_per_split, float* __restrict__ part,
+                                                                 int* __restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* stages = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
+    __shared__ __align__(8) uint64_t full[TP_STAGES], empty[TP_STAGES];
+    __shared__ __align__(8) uint64_t done, drain;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_abort, s_issued;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tp = static_cast<int>(blockIdx.x % static_cast<unsigned>(tiles_in.n));
+    const int ks = static_cast<int>(blockIdx.x / static_cast<unsigned>(tiles_in.n));
+    const int bm = tiles_in.bm[tp], bn = tiles_in.bn[tp];
+    const bool diag = bm == bn;
+    const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
+    const size_t c_begin = static_cast<size_t>(ks) * chunks_per_split;
+    size_t c_end = c_begin + chunks_per_split;
+    if (c_end > nchunks)
+        c_end = nchunks;
+    const int nmine = static_cast<int>(c_end > c_begin ? c_end - c_begin : 0);
+    volatile int* abort = &s_abort;
+    constexpr uint32_t N = TC_ROWS;
+
+    if (tid == 0)
+    {
+        for (int i = 0; i < TP_STAGES; ++i)
+        {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(&done, 1);
+        mbar_init(&drain, 1);
+        s_abort = 0;
+        s_issued = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == TP_MMA_WARP)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(512u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == TP_LOAD_WARP)
+    {
+        if (lane == 0)
+        {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(&planes_map) : "memory");
+            int m = 0;
+            for (; m < nmine; ++m)
+            {
+                const int st = m % TP_STAGES;
+                if (m >= TP_STAGES)
+                    mbar_wait(&empty[st], static_cast<uint32_t>(((m / TP_STAGES) - 1) & 1), abort);
+                if (*abort)
+                    break;
+                const int x = static_cast<int>(TC_KC * (c_begin + m));
+                uint8_t* dst = stages + st * TP_STAGE_BYTES;
+                tc::mbar_arrive_expect_tx(&full[st], diag ? 2 * TILE_BYTES : 4 * TILE_BYTES);
+                tc::tma_load_3d(dst, &planes_map, x, bm * TC_ROWS, 0, &full[st]);
+                tc::tma_load_3d(dst + TILE_BYTES, &planes_map, x, bm * TC_ROWS, 1, &full[st]);
+                if (!diag)
+                {
+                    tc::tma_load_3d(dst + 2 * TILE_BYTES, &planes_map, x, bn * TC_ROWS, 0, &full[st]);
+                    tc::tma_load_3d(dst + 3 * TILE_BYTES, &planes_map, x, bn * TC_ROWS, 1, &full[st]);
+                }
+            }
+            s_issued = m;
+        }
+        __syncwarp();
+    }
+    else if (warp == TP_MMA_WARP)
+    {
+        if (lane == 0)
+        {
+            const uint32_t idesc = instr_desc(TC_ROWS, TC_ROWS);
+            for (int it = 0; it < nmine; ++it)
+            {
+                const int st = it % TP_STAGES;
+                mbar_wait(&full[st], static_cast<uint32_t>((it / TP_STAGES) & 1), abort);
+                if (*abort)
+                    break;
+                tc_fence_after();
+                const uint32_t ah = smem_u32(stages + st * TP_STAGE_BYTES), al = ah + TILE_BYTES;
+                const uint32_t bh = diag ? ah : ah + 2 * TILE_BYTES, bl = diag ? al : ah + 3 * TILE_BYTES;
+#pragma unroll
+                for (int s2 = 0; s2 < TC_KC / 16; ++s2)
+                {
+                    const uint64_t dah = smem_desc(ah + s2 * 32), dal = smem_desc(al + s2 * 32);
+                    const uint64_t dbh = smem_desc(bh + s2 * 32), dbl = smem_desc(bl + s2 * 32);
+                    const uint32_t acc = (it > 0 || s2 > 0) ? 1u : 0u;
+                    mma_bf16(tmem, dah, dbh, idesc, acc);          // Ah Bh^T
+                    mma_bf16(tmem + N, dah, dbl, idesc, acc);      // Ah Bl^T
+                    mma_bf16(tmem + 2 * N, dal, dbh, idesc, acc);  // Al Bh^T
+                }
+                mma_commit(&empty[st]);
+            }
+            mma_commit(&done);
+        }
+        __syncwarp();
+    }
+    else
+    {
+        // epilogue: warp w reads rows 32w .. 32w + 31 of the tile
+        mbar_wait(&done, 0, abort);
+        tc_fence_after();
+        const int r = warp * 32 + lane;
+        float* dst = part + static_cast<size_t>(blockIdx.x) * TC_ROWS * TC_ROWS + static_cast<size_t>(r) * TC_ROWS;
+        for (int c0 = 0; c0 < TC_ROWS; c0 += 16)
+        {
+            float v[16], w1[16], w2[16];
+            const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
+            tmem_ld16(taddr, v);
+            tmem_ld16(taddr + N, w1);
+            tmem_ld16(taddr + 2 * N, w2);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                dst[c0 + i] = nmine ? v[i] + w1[i] + w2[i] : 0.f;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (s_abort)
+    {
+        // a wait gave up: the copies and MMAs already issued finish before shared and tensor memory
+        // are released (bounded waits)
+        if (warp == TP_LOAD_WARP && lane == 0)
+        {
+            const int issued = s_issued;
+            for (int m = issued - TP_STAGES > 0 ? issued - TP_STAGES : 0; m < issued; ++m)
+                mbar_wait(&full[m % TP_STAGES], static_cast<uint32_t>((m / TP_STAGES) & 1));
+            atomicExch(err, 1);
+        }
+        if (warp == TP_MMA_WARP && lane == 0)
+        {
+            mma_commit(&drain);
+            mbar_wait(&drain, 0);
+        }
+        __syncthreads();
+    }
+    if (warp == TP_MMA_WARP)
+    {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+    }
 }
 
 struct TiledPlan
@@ -680,6 +918,121 @@ size_t cov_tc_workspace(int T, size_t npix)
     return static_cast<size_t>(p.ctas) * per * sizeof(float) + 256;
 }
 
+// The tiles touching the 64-frame blocks set in `blocks` (bit b: frames 64 b .. 64 b + 63), or all
+// of them. The split of the pixels is the full computation's (the same chunks per split whatever
+// the tile count), so a recomputed entry is bit-identical to the full computation's.
+static hv_status cov_tc_tiled_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err,
+                                     uint32_t blocks, cudaStream_t st)
+{
+    const TiledPlan q = tiled_plan(T, npix);
+    TileList tl{};
+    std::memset(tl.index, -1, sizeof(tl.index));
+    for (int bm = 0; bm < q.nb; ++bm)
+        for (int bn = bm; bn < q.nb; ++bn)
+            if (((blocks >> bm) & 1u) || ((blocks >> bn) & 1u))
+            {
+                tl.bm[tl.n] = static_cast<unsigned char>(bm);
+                tl.bn[tl.n] = static_cast<unsigned char>(bn);
+                tl.index[bm][bn] = static_cast<signed char>(tl.n);
+                ++tl.n;
+            }
+    if (tl.n == 0)
+        return HV_OK;
+    CUtensorMap tmap;
+    if (!tc::encode_tmap_2d_f32(&tmap, ring, 2 * npix, static_cast<uint64_t>(T), npix * 8, 2 * TC_KC,
+                                static_cast<uint32_t>(TT_FRAMES)))
+    {
+        set_last_error_msg("tensor-core covariance: cuTensorMapEncodeTiled failed");
+        return HV_ERR_CUDA;
+    }
+    const int raw = 2;
+    const size_t smem = 4 * static_cast<size_t>(TILE_BYTES) + raw * 2 * static_cast<size_t>(TT_RAW_HALF) + 1024;
+    HV_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+    float* tpart = static_cast<float*>(work);
+    k_cov_tc_tiled<<<q.nsplit * tl.n, TT_THREADS, smem, st>>>(tmap, npix, tl, q.chunks_per_split, raw, tpart, err);
+    HV_LAUNCH_CHECK();
+    k_cov_tc_tiled_reduce<<<(T * T + TR_ENTRIES - 1) / TR_ENTRIES, TR_ENTRIES * TR_GROUPS, 0, st>>>(tpart, T, tl,
+                                                                                                  q.nsplit, cov);
+    HV_LAUNCH_CHECK();
+    count_launch(2);
+    return HV_OK;
+}
+
+hv_status cov_tc_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, uint32_t blocks,
+                        cudaStream_t st)
+{
+    if (!cov_tc_supported(T) || 2 * T <= TC_ROWS || npix == 0 || npix % 8 != 0 ||
+        (reinterpret_cast<uintptr_t>(ring) & 15) != 0 || npix > (1ull << 29))
+        return HV_ERR_UNSUPPORTED;
+    return cov_tc_tiled_blocks(ring, T, npix, cov, work, err, blocks, st);
+}
+
+size_t cov_planes_bytes(int T, size_t npix) { return 8 * static_cast<size_t>(T) * npix; }
+
+bool cov_planes_supported(int T, size_t npix)
+{
+    return cov_tc_supported(T) && 2 * T > TC_ROWS && npix > 0 && npix % 8 == 0 && npix <= (1ull << 29);
+}
+
+hv_status cov_split_planes(const float2* ring, int T, size_t npix, int slot0, int n, uint16_t* planes, cudaStream_t st)
+{
+    if (!cov_planes_supported(T, npix) || (reinterpret_cast<uintptr_t>(ring) & 15) != 0 ||
+        (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
+        return HV_ERR_UNSUPPORTED;
+    if (n <= 0)
+        return HV_OK;
+    if (slot0 < 0 || slot0 >= T || n > T)
+        return HV_INVALID_VALUE;
+    const size_t total = static_cast<size_t>(n) * (npix / 8);
+    const size_t cap = static_cast<size_t>(sm_count()) * 8;
+    const int grid = static_cast<int>(std::min((total + 255) / 256, cap));
+    k_ring_split<<<grid, 256, 0, st>>>(ring, T, npix, slot0, n, planes);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+hv_status cov_tc_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, int* err,
+                        uint32_t blocks, cudaStream_t st)
+{
+    if (!cov_planes_supported(T, npix) || (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
+        return HV_ERR_UNSUPPORTED;
+    const TiledPlan q = tiled_plan(T, npix);
+    TileList tl{};
+    std::memset(tl.index, -1, sizeof(tl.index));
+    for (int bm = 0; bm < q.nb; ++bm)
+        for (int bn = bm; bn < q.nb; ++bn)
+            if (((blocks >> bm) & 1u) || ((blocks >> bn) & 1u))
+            {
+                tl.bm[tl.n] = static_cast<unsigned char>(bm);
+                tl.bn[tl.n] = static_cast<unsigned char>(bn);
+                tl.index[bm][bn] = static_cast<signed char>(tl.n);
+                ++tl.n;
+            }
+    if (tl.n == 0)
+        return HV_OK;
+    CUtensorMap tmap;
+    if (!tc::encode_tmap_3d_bf16_sw128(&tmap, planes, npix, 2 * static_cast<uint64_t>(T), 2, npix * 2,
+                                       4 * static_cast<uint64_t>(T) * npix, TC_KC, TC_ROWS))
+    {
+        set_last_error_msg("tensor-core covariance: cuTensorMapEncodeTiled failed for the split planes");
+        return HV_ERR_CUDA;
+    }
+    const size_t smem = static_cast<size_t>(TP_STAGES) * TP_STAGE_BYTES + 1024;
+    static const cudaError_t attr = cudaFuncSetAttribute(k_cov_tc_planes, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         static_cast<int>(smem));
+    HV_CUDA_TRY(attr);
+    float* tpart = static_cast<float*>(work);
+    k_cov_tc_planes<<<q.nsplit * tl.n, TP_THREADS, smem, st>>>(tmap, npix, tl, q.chunks_per_split, tpart, err);
+    HV_LAUNCH_CHECK();
+    k_cov_tc_tiled_reduce<<<(T * T + TR_ENTRIES - 1) / TR_ENTRIES, TR_ENTRIES * TR_GROUPS, 0, st>>>(tpart, T, tl,
+                                                                                                  q.nsplit, cov);
+    HV_LAUNCH_CHECK();
+    count_launch(2);
+    return HV_OK;
+}
+
 hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, cudaStream_t st)
 {
     if (!cov_tc_supported(T) || npix == 0)
@@ -695,28 +1048,7 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
         return HV_ERR_UNSUPPORTED;
     }
     if (2 * T > TC_ROWS)
-    {
-        const TiledPlan q = tiled_plan(T, npix);
-        CUtensorMap tmap;
-        if (!tc::encode_tmap_2d_f32(&tmap, ring, 2 * npix, static_cast<uint64_t>(T), npix * 8, 2 * TC_KC,
-                                    static_cast<uint32_t>(TT_FRAMES)))
-        {
-            set_last_error_msg("tensor-core covariance: cuTensorMapEncodeTiled failed");
-            return HV_ERR_CUDA;
-        }
-        const int raw = 2;
-        const size_t smem = 4 * static_cast<size_t>(TILE_BYTES) + raw * 2 * static_cast<size_t>(TT_RAW_HALF) + 1024;
-        HV_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem)));
-        float* tpart = static_cast<float*>(work);
-        k_cov_tc_tiled<<<q.nsplit * q.npairs, TT_THREADS, smem, st>>>(tmap, npix, q.nb, q.npairs, q.chunks_per_split,
-                                                                      raw, tpart, err);
-        HV_LAUNCH_CHECK();
-        k_cov_tc_tiled_reduce<<<(T * T + 255) / 256, 256, 0, st>>>(tpart, T, q.nb, q.npairs, q.nsplit, cov);
-        HV_LAUNCH_CHECK();
-        count_launch(2);
-        return HV_OK;
-    }
+        return cov_tc_tiled_blocks(ring, T, npix, cov, work, err, ~0u, st);
     const TcPlan p = tc_plan(T, npix);
     // raw stages: T x 64 complex samples (T x 512 B) each, as many as fit beside the two A stages
     const size_t raw_bytes = static_cast<size_t>(T) * TC_KC * 16;  // pairs of 64-pixel chunks

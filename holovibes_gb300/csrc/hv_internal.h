@@ -77,12 +77,35 @@ hv_status phase_increase(const float2* ring, int T, size_t HW, const float2* w, 
 hv_status rescale_float(const float* in, size_t HW, const float2* mm, float post_scale, float* out, cudaStream_t st);
 size_t pca_cov_workspace(int T, size_t npix);
 void set_cov_mode(int mode);
+int cov_mode();
+void set_cov_incremental(bool on);
+bool cov_incremental();
 hv_status pca_cov_status(const void* work);
 // cov_tc.cu
 bool cov_tc_supported(int T);
 size_t cov_tc_workspace(int T, size_t npix);
 hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, cudaStream_t st);
+hv_status cov_tc_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, uint32_t blocks,
+                        cudaStream_t st);
+// Split-BF16 planes of the ring (T > 64): bytes, whether (T, npix) has them, the split of ring slots
+// slot0 .. slot0 + n - 1 (mod T) into them, and the tiled covariance (blocks as cov_tc_blocks, ~0u:
+// all) from them, bit-identical to cov_tc on the ring.
+size_t cov_planes_bytes(int T, size_t npix);
+bool cov_planes_supported(int T, size_t npix);
+hv_status cov_split_planes(const float2* ring, int T, size_t npix, int slot0, int n, uint16_t* planes, cudaStream_t st);
+hv_status cov_tc_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, int* err,
+                        uint32_t blocks, cudaStream_t st);
 hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st);
+// The covariance from the split planes (engine modes 0 and 2; HV_ERR_UNSUPPORTED for the SIMT mode
+// and shapes without planes).
+hv_status pca_covariance_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
+                                cudaStream_t st);
+// Recomputes only the rows and columns of `cov` (the previous covariance of the same ring) of the
+// 64-frame blocks set in `blocks` (bit b: ring slots 64 b .. 64 b + 63), bit-identical to a full
+// recomputation; HV_ERR_UNSUPPORTED when the engine in use has no such update (T <= 64, the FP32
+// SIMT engine): the caller then recomputes all of it.
+hv_status pca_covariance_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
+                                cudaStream_t st);
 size_t pca_eigh_workspace(int T);
 void set_eig_precision(int p);
 // Eigenvectors of ranks refine_lo..refine_hi (at most 64 of them) are refined in FP64 after FP32
@@ -90,9 +113,11 @@ void set_eig_precision(int p);
 // eigenvectors of the previous successful call with the same T (a window of the same stream), from
 // which the FP32 sweeps start (T <= 64). `kept_only`: the caller uses only the refined
 // eigenvectors and the order of the eigenvalues (coarser sweeps, FP32 Rayleigh quotients for the
-// others).
+// others). `cov_kept` (optional): false when the eigensolve overwrote `cov` (the FP64 sweeps in
+// global memory).
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
-                   cudaStream_t st, int refine_lo, int refine_hi, bool warm = false, bool kept_only = false);
+                   cudaStream_t st, int refine_lo, int refine_hi, bool warm = false, bool kept_only = false,
+                   bool* cov_kept = nullptr);
 
 // view_tc.cu
 bool view_tc_supported(int K);

@@ -126,6 +126,14 @@ int fast_lanes(const hv_settings& s, bool served)
     return fast_renders(s, served) > 1 ? hv_pipe::kMaxLanes : 2;
 }
 
+// The split-BF16 planes beside the ring (tiled covariance, T > 64): plain pipes whose ring slots the
+// host tracks (not served, not the fast lanes)
+bool uses_planes(const hv_frame_desc& fd, const hv_settings& s, bool served)
+{
+    const size_t HW = static_cast<size_t>(fd.width) * fd.height;
+    return uses_eig(s) && !served && fast_lanes(s, served) == 0 && cov_planes_supported(s.time_transformation_size, HW);
+}
+
 size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = false)
 {
     const size_t HW = static_cast<size_t>(fd.width) * fd.height;
@@ -163,6 +171,8 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
         z.add(pca_cov_workspace(T, HW));
         z.add(pca_eigh_workspace(T));
     }
+    if (uses_planes(fd, s, served))
+        z.add(cov_planes_bytes(T, HW));
     z.add(HW * 4 * 2);  // view + post
     if (is_moment(s.image_type))
         z.add(static_cast<size_t>(K > 0 ? K : 1) * sizeof(float));
@@ -267,7 +277,20 @@ hv_status build(hv_pipe* p)
         HV_ALLOC(p->evals, static_cast<size_t>(p->T) * sizeof(double));
         HV_ALLOC(p->cov_work, pca_cov_workspace(p->T, HW));
         HV_ALLOC(p->eig_work, pca_eigh_workspace(p->T));
+        // no warm start is read before an eigensolve wrote one; zeros if it ever is
+        HV_CUDA_TRY(cudaMemsetAsync(p->eig_work, 0, pca_eigh_workspace(p->T), p->stream));
         p->eig_warm = false;
+        p->cov_valid = false;
+        p->cov_dirty = ~0u;
+    }
+    p->planes = nullptr;
+    p->planes_ok = false;
+    if (uses_planes(p->fd, s, p->served))
+    {
+        // zero like the ring
+        HV_ALLOC(p->planes, cov_planes_bytes(p->T, HW));
+        HV_CUDA_TRY(cudaMemsetAsync(p->planes, 0, cov_planes_bytes(p->T, HW), p->stream));
+        p->planes_ok = true;
     }
     HV_ALLOC(p->view, HW * sizeof(float));
     p->bin_w = nullptr;
@@ -330,6 +353,7 @@ hv_status build(hv_pipe* p)
             HV_ALLOC(L.evals, static_cast<size_t>(p->T) * sizeof(double));
             HV_ALLOC(L.cov_work, pca_cov_workspace(p->T, HW));
             HV_ALLOC(L.eig_work, pca_eigh_workspace(p->T));
+            HV_CUDA_TRY(cudaMemsetAsync(L.eig_work, 0, pca_eigh_workspace(p->T), p->stream));
             HV_ALLOC(L.view, HW * sizeof(float));
             HV_ALLOC(L.post, HW * sizeof(float));
             HV_ALLOC(L.partials, static_cast<size_t>(p->npartials) * sizeof(double));
@@ -534,19 +558,50 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
     const bool pinc = uses_phase_increase(s);
     if (uses_eig(s))
     {
-        // not gated by the block: served PCA / SSA_STFT cycles are launched eagerly (render cycles only)
-        if ((r = pca_covariance(p->ring, p->T, p->HW, p->cov, p->cov_work, st)) != HV_OK)
+        // not gated by the block: served PCA / SSA_STFT cycles are launched eagerly (render cycles only).
+        // A sliding window (stride < T) rewrites S of the T ring slots between renders: only the
+        // covariance rows and columns of those slots change, and those are recomputed (the other
+        // entries are the previous window's, computed from the same samples: bit-identical to a
+        // full recomputation).
+        const int nblk = (p->T + 63) / 64;
+        const uint32_t all = nblk >= 32 ? ~0u : ((1u << nblk) - 1u);
+        const uint32_t dirty = p->cov_dirty & all;
+        bool done = false;
+        const bool inc = !ctl && p->nrender <= 1 && p->cov_valid && p->cov_mode == cov_mode() && dirty != all &&
+                         cov_incremental();
+        if (!ctl && p->planes_ok)
+        {
+            r = inc && !dirty ? HV_OK
+                              : pca_covariance_planes(p->planes, p->T, p->HW, p->cov, p->cov_work, inc ? dirty : ~0u, st);
+            if (r == HV_OK)
+                done = true;
+            else if (r != HV_ERR_UNSUPPORTED)
+                return r;
+        }
+        if (!done && inc)
+        {
+            r = dirty ? pca_covariance_blocks(p->ring, p->T, p->HW, p->cov, p->cov_work, dirty, st) : HV_OK;
+            if (r == HV_OK)
+                done = true;
+            else if (r != HV_ERR_UNSUPPORTED)
+                return r;
+        }
+        if (!done && (r = pca_covariance(p->ring, p->T, p->HW, p->cov, p->cov_work, st)) != HV_OK)
             return r;
+        p->cov_dirty = 0;
+        p->cov_mode = cov_mode();
         // refined in FP64: the viewed components (PCA) or the kept range of SSA_STFT (all columns
         // kept: the projector is the identity, nothing to refine)
         const int rlo = pca ? p->pmin : p->qmin;
         const int rhi = pca ? p->pmax : (p->qn < p->T ? p->qmin + p->qn - 1 : -1);
         // the sweeps start from the previous window's eigenvectors once there is one
         // PCA views read only the refined weights (the cuts read every eigenvector)
+        bool kept = false;
         if ((r = pca_eigh(p->cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, pca ? p->weights : nullptr,
-                          p->eig_work, st, rlo, rhi, p->eig_warm, pca && !p->cuts)) != HV_OK)
+                          p->eig_work, st, rlo, rhi, p->eig_warm, pca && !p->cuts, &kept)) != HV_OK)
             return r;
         p->eig_warm = true;
+        p->cov_valid = kept && !ctl;
         if (!pca && (r = ssa_weights(p->evecs, p->T, p->qmin, p->qn, p->pmin, p->K, p->weights, st)) != HV_OK)
             return r;
         if (p->view_on_tc && (r = view_tc_prepare(p->weights, p->K, p->T, p->view_tc_work, st)) != HV_OK)
@@ -864,6 +919,7 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
                                          p->spatial, L.ring, 0, p->T, p->stream, nullptr, p->f2d_mask, p->work2);
         if (st != HV_OK)
             return st;
+        p->cov_dirty = ~0u;  // every slot rewritten
         p->f2d_buf = r;  // one spectrum per ring: window k's render reads it while batch k+1 runs
         if (p->f2d_view && (st = capture_f2d_spectrum(p, raw, r)) != HV_OK)
             return st;
@@ -917,6 +973,11 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
     hv_status r = spatial_transform(raw, p->kind, p->W, p->H, nb, p->s.space_transformation, p->lens, p->spatial,
                                     p->ring, begin, T, p->stream, nullptr, p->f2d_mask, p->work2);
     if (r != HV_OK)
+        return r;
+    // the 64-frame slot blocks whose covariance rows change, and their split planes
+    for (int f = 0; f < nb; f += 1)
+        p->cov_dirty |= 1u << (((begin + f) % T) / 64 & 31);
+    if (p->planes_ok && (r = cov_split_planes(p->ring, T, p->HW, begin, nb, p->planes, p->stream)) != HV_OK)
         return r;
     p->ring_size += nb;
     if (p->ring_size > T)
@@ -1161,6 +1222,9 @@ hv_status served_record(hv_pipe* p, const CycleCtl* ctl, const ServedCycle& c, b
         if ((r = spatial_transform(p->in_ring, p->kind, p->W, p->H, p->B, s.space_transformation, p->lens, p->spatial,
                                    p->ring, 0, p->T, st, ctl, p->f2d_mask, p->work2)) != HV_OK)
             return r;
+        // ring slots chosen on the device: no record of which covariance rows changed
+        p->cov_valid = false;
+        p->planes_ok = false;
     }
     if (!gated && !c.render)
         return HV_OK;

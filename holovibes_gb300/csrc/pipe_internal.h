@@ -73,6 +73,14 @@ struct hv_pipe
     void* cov_work = nullptr;
     void* eig_work = nullptr;
     bool eig_warm = false;  // eig_work holds the eigenvectors of the previous window (same T)
+    // `cov` holds the covariance of the ring as it was at the last render, computed with engine
+    // mode `cov_mode`; the 64-frame slot blocks rewritten since then are set in `cov_dirty`
+    bool cov_valid = false;
+    int cov_mode = -1;
+    uint32_t cov_dirty = ~0u;
+    // split-BF16 planes of the ring for the tiled covariance; planes_ok: they mirror every slot
+    uint16_t* planes = nullptr;
+    bool planes_ok = false;
     float* view = nullptr;
     float* unwrapped = nullptr;
     void* unwrap_work = nullptr;

@@ -128,6 +128,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst_smem, const void* tmap, in
         : "memory");
 }
 
+__device__ __forceinline__ void tma_load_3d(void* dst_smem, const void* tmap, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst_smem)),
+        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate)
 {
@@ -216,6 +225,33 @@ inline bool encode_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, const vo
     const cuuint32_t estr[2] = {1, 1};
     return fn(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Host: tensor map of `planes` row-major BF16 matrices (`rows` x `cols`, row pitch `pitch_bytes`,
+// matrix pitch `plane_bytes`, both multiples of 16) for boxes of box_rows x box_cols of one matrix,
+// landing in shared memory in the 128-byte-swizzled K-major layout above (box_cols = 64: one
+// 128-byte line per row); zero fill out of range.
+inline bool encode_tmap_3d_bf16_sw128(CUtensorMap* map, const void* base, uint64_t cols, uint64_t rows,
+                                      uint64_t planes, uint64_t pitch_bytes, uint64_t plane_bytes, uint32_t box_cols,
+                                      uint32_t box_rows)
+{
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    if (!fn)
+        return false;
+    const cuuint64_t dims[3] = {cols, rows, planes};
+    const cuuint64_t strides[2] = {pitch_bytes, plane_bytes};
+    const cuuint32_t box[3] = {box_cols, box_rows, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 

@@ -412,6 +412,11 @@ size_t pca_cov_workspace(int T, size_t npix)
 }
 
 void set_cov_mode(int mode) { g_cov_mode = mode; }
+int cov_mode() { return g_cov_mode.load(); }
+
+static std::atomic<bool> g_cov_incremental{true};
+void set_cov_incremental(bool on) { g_cov_incremental = on; }
+bool cov_incremental() { return g_cov_incremental.load(); }
 
 hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st)
 {
@@ -444,6 +449,33 @@ hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, v
     HV_LAUNCH_CHECK();
     count_launch(2);
     return HV_OK;
+}
+
+hv_status pca_covariance_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
+                                cudaStream_t st)
+{
+    if (T <= 0 || npix == 0)
+        return HV_INVALID_VALUE;
+    const int mode = g_cov_mode.load();
+    if (mode == 1)
+        return HV_ERR_UNSUPPORTED;
+    int* err = static_cast<int*>(work);
+    char* ws = static_cast<char*>(work) + COV_FLAGS;
+    HV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+    return cov_tc_blocks(ring, T, npix, cov, ws, err, blocks, st);
+}
+
+hv_status pca_covariance_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
+                                cudaStream_t st)
+{
+    if (T <= 0 || npix == 0 || !planes || !cov || !work)
+        return HV_INVALID_VALUE;
+    if (g_cov_mode.load() == 1)
+        return HV_ERR_UNSUPPORTED;
+    int* err = static_cast<int*>(work);
+    char* ws = static_cast<char*>(work) + COV_FLAGS;
+    HV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+    return cov_tc_planes(planes, T, npix, cov, ws, err, blocks, st);
 }
 
 hv_status pca_cov_status(const void* work)
@@ -1528,20 +1560,23 @@ __global__ void k_eigref_matvec(const double2* __restrict__ C, const double2* __
         Y[static_cast<size_t>(j) * T + t] = acc;
 }
 
-// D[j][i] = v_i^H Y[j], G[j][i] = v_i^H v_{r0+j} for the basis vectors i = b0 .. T-1;
-// grid (ceil((T - b0) / 8), K), 256 threads
-__global__ void k_eigref_project(const double2* __restrict__ evecs, const double2* __restrict__ Y, int T, int r0,
-                                 int b0, double2* __restrict__ D, double2* __restrict__ G)
+// D[j][i] = v_i^H Y[j], G[j][i] = v_i^H v_{r0+j} for the basis vectors i = b0 .. T-1; grid (T - b0, K),
+// 64 threads (FP64 throughput is a few operations per clock per SM on this part: one basis vector
+// per CTA spreads the products over the SMs); the two warps' sums are added in warp order
+constexpr int ER_PROJ_THREADS = 64;
+__global__ void __launch_bounds__(ER_PROJ_THREADS) k_eigref_project(const double2* __restrict__ evecs,
+                                                                   const double2* __restrict__ Y, int T, int r0,
+                                                                   int b0, double2* __restrict__ D,
+                                                                   double2* __restrict__ G)
 {
+    __shared__ double2 sd[ER_PROJ_THREADS / 32], sg[ER_PROJ_THREADS / 32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = b0 + blockIdx.x * 8 + warp, j = blockIdx.y;
-    if (i >= T)
-        return;
+    const int i = b0 + blockIdx.x, j = blockIdx.y;
     const double2* vi = evecs + static_cast<size_t>(i) * T;
     const double2* vj = evecs + static_cast<size_t>(r0 + j) * T;
     const double2* y = Y + static_cast<size_t>(j) * T;
     double2 d = make_double2(0.0, 0.0), g = make_double2(0.0, 0.0);
-    for (int t = lane; t < T; t += 32)
+    for (int t = threadIdx.x; t < T; t += ER_PROJ_THREADS)
     {
         const double2 a = vi[t];
         d = cfma_conj(a, y[t], d);
@@ -1551,6 +1586,19 @@ __global__ void k_eigref_project(const double2* __restrict__ evecs, const double
     g = warp_sum2(g);
     if (lane == 0)
     {
+        sd[warp] = d;
+        sg[warp] = g;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        for (int w = 1; w < ER_PROJ_THREADS / 32; ++w)
+        {
+            d.x += sd[w].x;
+            d.y += sd[w].y;
+            g.x += sg[w].x;
+            g.y += sg[w].y;
+        }
         D[static_cast<size_t>(j) * T + i] = d;
         G[static_cast<size_t>(j) * T + i] = g;
     }
@@ -1567,17 +1615,23 @@ __device__ __forceinline__ double eigref_lambda(const double2* D, const double2*
 // the basis i = b0 .. T-1. With a partial basis (b0 > 0: the Ritz vectors of the largest
 // eigenvalues) the part of the residual r = C v_j - lambda_j v_j outside the basis is added divided
 // by lambda_j (the eigenvalues outside are the smaller ones; the factor lambda_i / lambda_j it
-// neglects shrinks with each correction). grid (ceil(T / 128), K), 128 threads (thread = row t: the
-// loads of v_i[t] are coalesced). The coefficients of kept vector j are computed once per CTA into
-// shared memory (FP64 divisions are slow on this part), then every thread runs the complex
-// multiply-adds.
-__global__ void k_eigref_update(const double2* __restrict__ evecs, const double* __restrict__ evals,
-                                const double2* __restrict__ D, const double2* __restrict__ G,
-                                const double2* __restrict__ Y, int T, int r0, int K, int b0, double2* __restrict__ Vn)
+// neglects shrinks with each correction). grid (ceil(T / 32), K), ER_UPD_WARPS warps: lane = row t
+// of the CTA's 32 rows (coalesced loads of v_i[t]), warp w sums the basis vectors i = b0 + w,
+// b0 + w + ER_UPD_WARPS, ..., and the warps' sums are added in warp order. The coefficients of kept
+// vector j are computed once per CTA into shared memory (FP64 divisions are slow on this part).
+constexpr int ER_UPD_WARPS = 4;
+__global__ void __launch_bounds__(32 * ER_UPD_WARPS) k_eigref_update(const double2* __restrict__ evecs,
+                                                                    const double* __restrict__ evals,
+                                                                    const double2* __restrict__ D,
+                                                                    const double2* __restrict__ G,
+                                                                    const double2* __restrict__ Y, int T, int r0,
+                                                                    int K, int b0, double2* __restrict__ Vn)
 {
     __shared__ double2 coef[JC_MAX_T];
     __shared__ double2 comp[JC_MAX_T];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    __shared__ double2 pacc[ER_UPD_WARPS][32], pproj[ER_UPD_WARPS][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * 32 + lane, j = blockIdx.y;
     const int rj = r0 + j;
     const double lj = eigref_lambda(D, G, T, r0, j);
     // pairs closer than 1e-12 of the largest eigenvalue (the last in ascending order) stay mixed
@@ -1600,27 +1654,39 @@ __global__ void k_eigref_update(const double2* __restrict__ evecs, const double*
         comp[i] = cr;
     }
     __syncthreads();
-    if (t >= T)
-        return;
-    double2 acc = evecs[static_cast<size_t>(rj) * T + t];
-    double2 proj = make_double2(0.0, 0.0);
-    for (int i = b0; i < T; ++i)
-    {
-        const double2 c = coef[i];
-        const double2 v = evecs[static_cast<size_t>(i) * T + t];
-        acc.x += v.x * c.x - v.y * c.y;
-        acc.y += v.x * c.y + v.y * c.x;
-        if (b0 > 0)
+    double2 acc = make_double2(0.0, 0.0), proj = make_double2(0.0, 0.0);
+    if (t < T)
+        for (int i = b0 + warp; i < T; i += ER_UPD_WARPS)
         {
-            const double2 cr = comp[i];
-            proj.x += v.x * cr.x - v.y * cr.y;
-            proj.y += v.x * cr.y + v.y * cr.x;
+            const double2 c = coef[i];
+            const double2 v = evecs[static_cast<size_t>(i) * T + t];
+            acc.x += v.x * c.x - v.y * c.y;
+            acc.y += v.x * c.y + v.y * c.x;
+            if (b0 > 0)
+            {
+                const double2 cr = comp[i];
+                proj.x += v.x * cr.x - v.y * cr.y;
+                proj.y += v.x * cr.y + v.y * cr.x;
+            }
         }
+    pacc[warp][lane] = acc;
+    pproj[warp][lane] = proj;
+    __syncthreads();
+    if (warp != 0 || t >= T)
+        return;
+    const double2 vj = evecs[static_cast<size_t>(rj) * T + t];
+    acc = vj;
+    proj = make_double2(0.0, 0.0);
+    for (int w = 0; w < ER_UPD_WARPS; ++w)
+    {
+        acc.x += pacc[w][lane].x;
+        acc.y += pacc[w][lane].y;
+        proj.x += pproj[w][lane].x;
+        proj.y += pproj[w][lane].y;
     }
     if (b0 > 0)
     {
         const double2 y = Y[static_cast<size_t>(j) * T + t];
-        const double2 vj = evecs[static_cast<size_t>(rj) * T + t];
         const double inv = 1.0 / lj;
         acc.x += (y.x - lj * vj.x - proj.x) * inv;
         acc.y += (y.y - lj * vj.y - proj.y) * inv;
@@ -1662,17 +1728,23 @@ __global__ void k_eigref_finish(double2* __restrict__ evecs, double* __restrict_
 // When only the largest eigenpairs are used (PCA views of the dominant components, ranks T - 16 ..
 // T - 1 at most) and T > 64, the block Jacobi's full diagonalisation (~1 ms per sweep at T = 512,
 // 5 or more sweeps) is replaced by a block subspace iteration on TS_P = 32 vectors in FP32: Y = C V
-// (all CTAs), V = orth(Y) (classical Gram-Schmidt applied twice, one CTA), repeated; then
-// Rayleigh-Ritz (H = V^H C V, Jacobi on the 32 x 32 H in one CTA) gives the Ritz pairs, and the kept
-// vectors are corrected in FP64 against the FP64 covariance with the Ritz vectors as the basis.
-// The error towards an eigenvector outside the subspace falls by lambda_33 / lambda_m per
-// iteration (m: the smallest kept rank from the top). The Ritz vectors of the previous window
-// are the warm start.
+// (all CTAs), V = orth(Y) (classical Gram-Schmidt with a second pass where needed, one CTA),
+// repeated; then Rayleigh-Ritz (H = V^H C V, Jacobi on the 32 x 32 H in one CTA) gives the Ritz
+// pairs, and the kept vectors are corrected in FP64 against the FP64 covariance with the Ritz
+// vectors as the basis. The error towards an eigenvector outside the subspace falls by
+// lambda_33 / lambda_m per iteration (m: the smallest kept rank from the top). The Ritz vectors of
+// the previous window are the warm start (TS_ITERS_WARM iterations; TS_ITERS_COLD from the columns
+// of C).
 constexpr int TS_P = 32;          // subspace size
 constexpr int TS_MAX_KEEP = 16;   // top ranks served (the other 16 vectors are the guard)
-constexpr int TS_LD = TS_P + 1;   // shared-memory row pitch (float2) of the orthonormalisation
-constexpr int TS_ORTH_THREADS = 512;
-constexpr int TS_ITERS_COLD = 8, TS_ITERS_WARM = 3;
+constexpr int TS_LD = TS_P + 1;   // shared-memory row pitch (float2) of the Rayleigh-Ritz matrices
+constexpr int TS_ORTH_THREADS = 256;
+constexpr int TS_ORTH_RPT = 2;    // rows per thread of the orthonormalisation (T <= 512)
+constexpr int TS_MM_ROWS = 1;     // rows of C V per CTA
+constexpr int TS_MM_SPLIT = 16;   // warps per row (warp q sums the terms s = q mod 16)
+constexpr int TS_ITERS_COLD = 8, TS_ITERS_WARM = 2;
+static_assert(TS_P == 32, "one lane per subspace vector");
+static_assert(TS_ORTH_THREADS * TS_ORTH_RPT >= JC_MAX_T, "the orthonormalisation holds every row in registers");
 
 static size_t ts_bytes(int T)
 {
@@ -1719,123 +1791,273 @@ __global__ void k_ts_init(const float2* __restrict__ C32, int T, float2* __restr
     Y[e] = C32[static_cast<size_t>(t) * T + (k * T) / TS_P];
 }
 
-// Y[t][k] = sum_s C32[t][s] V[s][k]: thread (t, k), a warp covers the TS_P columns of one row
-__global__ void k_ts_matmul(const float2* __restrict__ C32, const float2* __restrict__ V, int T, float2* __restrict__ Y)
+// Y[t][k] = sum_s C32[t][s] V[s][k]. Warp (row t, part q) of a CTA sums the terms s = q,
+// q + TS_MM_SPLIT, ... for the TS_P columns (lane k) in two interleaved chains; the parts are added
+// in part order.
+__global__ void __launch_bounds__(TS_MM_ROWS * TS_MM_SPLIT * 32)
+    k_ts_matmul(const float2* __restrict__ C32, const float2* __restrict__ V, int T, float2* __restrict__ Y)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= T * TS_P)
-        return;
-    const int t = e / TS_P, k = e % TS_P;
-    const float2* c = C32 + static_cast<size_t>(t) * T;
-    float re = 0.f, im = 0.f;
-    for (int s2 = 0; s2 < T; ++s2)
+    __shared__ float2 part[TS_MM_ROWS * TS_MM_SPLIT][TS_P];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * TS_MM_ROWS + warp / TS_MM_SPLIT, q = warp % TS_MM_SPLIT;
+    float re0 = 0.f, im0 = 0.f, re1 = 0.f, im1 = 0.f;
+    if (t < T)
     {
-        const float2 a = c[s2], v = V[static_cast<size_t>(s2) * TS_P + k];
-        re = fmaf(a.x, v.x, fmaf(-a.y, v.y, re));
-        im = fmaf(a.x, v.y, fmaf(a.y, v.x, im));
+        const float2* c = C32 + static_cast<size_t>(t) * T;
+        int s2 = q;
+#pragma unroll 4
+        for (; s2 + TS_MM_SPLIT < T; s2 += 2 * TS_MM_SPLIT)
+        {
+            const float2 a0 = c[s2], v0 = V[static_cast<size_t>(s2) * TS_P + lane];
+            const float2 a1 = c[s2 + TS_MM_SPLIT], v1 = V[static_cast<size_t>(s2 + TS_MM_SPLIT) * TS_P + lane];
+            re0 = fmaf(a0.x, v0.x, fmaf(-a0.y, v0.y, re0));
+            im0 = fmaf(a0.x, v0.y, fmaf(a0.y, v0.x, im0));
+            re1 = fmaf(a1.x, v1.x, fmaf(-a1.y, v1.y, re1));
+            im1 = fmaf(a1.x, v1.y, fmaf(a1.y, v1.x, im1));
+        }
+        if (s2 < T)
+        {
+            const float2 a0 = c[s2], v0 = V[static_cast<size_t>(s2) * TS_P + lane];
+            re0 = fmaf(a0.x, v0.x, fmaf(-a0.y, v0.y, re0));
+            im0 = fmaf(a0.x, v0.y, fmaf(a0.y, v0.x, im0));
+        }
     }
-    Y[e] = make_float2(re, im);
+    part[warp][lane] = make_float2(re0 + re1, im0 + im1);
+    __syncthreads();
+    if (q == 0 && t < T)
+    {
+        float2 y = part[warp][lane];
+        for (int j = 1; j < TS_MM_SPLIT; ++j)
+        {
+            y.x += part[warp + j][lane].x;
+            y.y += part[warp + j][lane].y;
+        }
+        Y[static_cast<size_t>(t) * TS_P + lane] = y;
+    }
 }
 
-// V = orth(Y), T x TS_P row-major, classical Gram-Schmidt applied twice per column, one CTA
+// Slot j's contribution of this thread's rows to the column sums of the orthonormalisation: slot 0
+// holds |y_0|^2 (the column being processed), slot j > 0 the product y_j^H y_0.
+__device__ __forceinline__ float2 ts_slot(const float2 (&y)[TS_ORTH_RPT][TS_P], int j)
+{
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int r = 0; r < TS_ORTH_RPT; ++r)
+    {
+        const float2 a = y[r][j], b = y[r][0];
+        if (j == 0)
+            re = fmaf(b.x, b.x, fmaf(b.y, b.y, re));
+        else
+        {
+            re = fmaf(a.x, b.x, fmaf(a.y, b.y, re));
+            im = fmaf(a.x, b.y, fmaf(-a.y, b.x, im));
+        }
+    }
+    return make_float2(re, im);
+}
+
+// Sums of the 32 slots over the CTA: a reduce-scatter across each warp (lane l ends with the warp's
+// sum of slot l), then a fixed-order sum over the warps in shared memory. Every warp returns the
+// same totals (slot `lane` in its lane). `red` alternates between two buffers, so one barrier per
+// reduction suffices.
+__device__ __forceinline__ float2 ts_reduce_slots(const float2 (&y)[TS_ORTH_RPT][TS_P],
+                                                  float2 (*red)[TS_ORTH_THREADS / 32][TS_P], int& buf)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 p[TS_P / 2];
+    {
+        const bool up = lane & 16;
+#pragma unroll
+        for (int j = 0; j < TS_P / 2; ++j)
+        {
+            const float2 a = ts_slot(y, j), b = ts_slot(y, j + TS_P / 2);
+            const float2 send = up ? a : b, keep = up ? b : a;
+            p[j] = make_float2(keep.x + __shfl_xor_sync(0xffffffffu, send.x, 16),
+                               keep.y + __shfl_xor_sync(0xffffffffu, send.y, 16));
+        }
+    }
+#pragma unroll
+    for (int w = 8; w >= 1; w >>= 1)
+    {
+        const bool up = lane & w;
+#pragma unroll
+        for (int j = 0; j < w; ++j)
+        {
+            const float2 a = p[j], b = p[j + w];
+            const float2 send = up ? a : b, keep = up ? b : a;
+            p[j] = make_float2(keep.x + __shfl_xor_sync(0xffffffffu, send.x, w),
+                               keep.y + __shfl_xor_sync(0xffffffffu, send.y, w));
+        }
+    }
+    red[buf][warp][lane] = p[0];
+    __syncthreads();
+    float2 s2 = red[buf][0][lane];
+#pragma unroll
+    for (int w = 1; w < TS_ORTH_THREADS / 32; ++w)
+    {
+        s2.x += red[buf][w][lane].x;
+        s2.y += red[buf][w][lane].y;
+    }
+    buf ^= 1;
+    return s2;
+}
+
+// One Gram-Schmidt pass on register slot 0 against the processed columns (slots >= first), with
+// the totals `s2` of ts_reduce_slots: y_0 -= sum_j (y_j^H y_0) y_j. Returns |y_0|^2 before the pass
+// minus the removed squared norm.
+__device__ __forceinline__ float ts_project(float2 (&y)[TS_ORTH_RPT][TS_P], float2 s2, int first)
+{
+    const float nn = __shfl_sync(0xffffffffu, s2.x, 0);
+    float cc = 0.f;
+#pragma unroll
+    for (int j = 1; j < TS_P; ++j)
+    {
+        float cr = __shfl_sync(0xffffffffu, s2.x, j), ci = __shfl_sync(0xffffffffu, s2.y, j);
+        if (j < first)
+            cr = ci = 0.f;
+        cc = fmaf(cr, cr, fmaf(ci, ci, cc));
+#pragma unroll
+        for (int r = 0; r < TS_ORTH_RPT; ++r)
+        {
+            const float2 v = y[r][j];
+            y[r][0].x -= v.x * cr - v.y * ci;
+            y[r][0].y -= v.x * ci + v.y * cr;
+        }
+    }
+    return nn - cc;
+}
+
+// V = orth(Y), T x TS_P row-major (T <= TS_ORTH_THREADS * TS_ORTH_RPT): classical Gram-Schmidt from
+// the last column (the largest Ritz value of the warm start) to the first, with a second pass when
+// the first removed more than half of the column's squared norm ("twice is enough", Giraud et al.
+// 2005). Thread i owns rows i + TS_ORTH_THREADS r in registers; the column being processed is
+// always register slot 0 and the slots rotate by one after every column, so that registers are
+// indexed by constants only. A column left without norm (Y of rank < TS_P) becomes the unit vector
+// e_k, made orthogonal at the next iteration.
 __global__ void __launch_bounds__(TS_ORTH_THREADS) k_ts_orth(const float2* __restrict__ Y, int T, float2* __restrict__ V)
 {
-    extern __shared__ float2 ts_s[];  // T x TS_LD
-    __shared__ float2 c[TS_P];
-    __shared__ float red[TS_ORTH_THREADS / 32];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    constexpr int NW = TS_ORTH_THREADS / 32;
-    for (int e = tid; e < T * TS_P; e += TS_ORTH_THREADS)
-        ts_s[(e / TS_P) * TS_LD + e % TS_P] = Y[e];
-    __syncthreads();
+    __shared__ float2 red[2][TS_ORTH_THREADS / 32][TS_P];
+    __shared__ float red1[2][TS_ORTH_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float2 y[TS_ORTH_RPT][TS_P];  // slot j: column TS_P - 1 - j (before the first and after the last rotation)
+#pragma unroll
+    for (int r = 0; r < TS_ORTH_RPT; ++r)
+    {
+        const int t = tid + r * TS_ORTH_THREADS;
+#pragma unroll
+        for (int j = 0; j < TS_P; ++j)
+            y[r][j] = t < T ? Y[static_cast<size_t>(t) * TS_P + (TS_P - 1 - j)] : make_float2(0.f, 0.f);
+    }
+    int buf = 0, buf1 = 0;
+#pragma unroll 1
     for (int k = 0; k < TS_P; ++k)
     {
-        for (int pass = 0; pass < 2 && k > 0; ++pass)
+        const int first = TS_P - k;  // the processed columns sit in slots first .. TS_P - 1
+        const float2 s1 = ts_reduce_slots(y, red, buf);
+        const float nn = __shfl_sync(0xffffffffu, s1.x, 0);
+        float n2 = ts_project(y, s1, first);
+        // the same totals in every warp: the branch is uniform over the CTA
+        if (k > 0 && !(n2 >= 0.5f * nn))
         {
-            for (int i = warp; i < k; i += NW)
-            {
-                float re = 0.f, im = 0.f;
-                for (int t = lane; t < T; t += 32)
-                {
-                    const float2 a = ts_s[t * TS_LD + i], b = ts_s[t * TS_LD + k];
-                    re += a.x * b.x + a.y * b.y;
-                    im += a.x * b.y - a.y * b.x;
-                }
-                for (int o = 16; o > 0; o >>= 1)
-                {
-                    re += __shfl_xor_sync(0xffffffffu, re, o);
-                    im += __shfl_xor_sync(0xffffffffu, im, o);
-                }
-                if (lane == 0)
-                    c[i] = make_float2(re, im);
-            }
+            ts_project(y, ts_reduce_slots(y, red, buf), first);
+            float m = 0.f;
+#pragma unroll
+            for (int r = 0; r < TS_ORTH_RPT; ++r)
+                m = fmaf(y[r][0].x, y[r][0].x, fmaf(y[r][0].y, y[r][0].y, m));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                m += __shfl_xor_sync(0xffffffffu, m, o);
+            if (lane == 0)
+                red1[buf1][warp] = m;
             __syncthreads();
-            for (int t = tid; t < T; t += TS_ORTH_THREADS)
-            {
-                float2 y = ts_s[t * TS_LD + k];
-                for (int i = 0; i < k; ++i)
-                {
-                    const float2 v = ts_s[t * TS_LD + i], ci = c[i];
-                    y.x -= v.x * ci.x - v.y * ci.y;
-                    y.y -= v.x * ci.y + v.y * ci.x;
-                }
-                ts_s[t * TS_LD + k] = y;
-            }
-            __syncthreads();
+            n2 = red1[buf1][0];
+#pragma unroll
+            for (int w = 1; w < TS_ORTH_THREADS / 32; ++w)
+                n2 += red1[buf1][w];
+            buf1 ^= 1;
         }
-        float n2 = 0.f;
-        for (int t = tid; t < T; t += TS_ORTH_THREADS)
+        const bool dead = !(n2 > 0.f) || !isfinite(n2);
+        const float inv = dead ? 0.f : rsqrtf(n2);
+        const int col = TS_P - 1 - k;
+#pragma unroll
+        for (int r = 0; r < TS_ORTH_RPT; ++r)
         {
-            const float2 y = ts_s[t * TS_LD + k];
-            n2 += y.x * y.x + y.y * y.y;
+            const int t = tid + r * TS_ORTH_THREADS;
+            y[r][0] = dead ? make_float2(t == col ? 1.f : 0.f, 0.f) : make_float2(y[r][0].x * inv, y[r][0].y * inv);
+            const float2 done = y[r][0];
+#pragma unroll
+            for (int j = 0; j < TS_P - 1; ++j)
+                y[r][j] = y[r][j + 1];
+            y[r][TS_P - 1] = done;
         }
-        for (int o = 16; o > 0; o >>= 1)
-            n2 += __shfl_xor_sync(0xffffffffu, n2, o);
-        if (lane == 0)
-            red[warp] = n2;
-        __syncthreads();
-        float tot = 0.f;
-        for (int w = 0; w < NW; ++w)
-            tot += red[w];
-        // a column dependent on the previous ones (a covariance of rank < TS_P) is replaced by
-        // the unit vector e_k, made orthogonal at the next iteration
-        const bool dead = !(tot > 0.f) || !isfinite(tot);
-        const float inv = dead ? 0.f : rsqrtf(tot);
-        for (int t = tid; t < T; t += TS_ORTH_THREADS)
-        {
-            const float2 y = ts_s[t * TS_LD + k];
-            ts_s[t * TS_LD + k] = dead ? make_float2(t == k ? 1.f : 0.f, 0.f) : make_float2(y.x * inv, y.y * inv);
-        }
-        __syncthreads();
     }
-    for (int e = tid; e < T * TS_P; e += TS_ORTH_THREADS)
-        V[e] = ts_s[(e / TS_P) * TS_LD + e % TS_P];
+#pragma unroll
+    for (int r = 0; r < TS_ORTH_RPT; ++r)
+    {
+        const int t = tid + r * TS_ORTH_THREADS;
+        if (t < T)
+        {
+#pragma unroll
+            for (int j = 0; j < TS_P; ++j)
+                V[static_cast<size_t>(t) * TS_P + (TS_P - 1 - j)] = y[r][j];
+        }
+    }
 }
 
 // Rayleigh-Ritz: H = V^H Y (Y = C32 V), H Q = Q diag(theta) by FP32 Jacobi, Ritz vectors U = V Q in
 // ascending order: evecs columns T - TS_P .. T - 1 (FP64) and the warm start `Vw`, the Ritz values
-// (scaled back) into evals[T - TS_P ..], evals below set to 0. One CTA.
+// (scaled back) into evals[T - TS_P ..], evals below set to 0. One CTA; V and Y pass through shared
+// memory in blocks of TS_P rows (coalesced loads), the sums over t run in row order.
 __global__ void __launch_bounds__(JS_THREADS) k_ts_rr(const float2* __restrict__ V, const float2* __restrict__ Y, int T,
                                                      const double* __restrict__ scale, double2* __restrict__ evecs,
                                                      double* __restrict__ evals, float2* __restrict__ Vw)
 {
+    constexpr int NW = JS_THREADS / 32;
+    constexpr int HR = TS_P / NW;  // rows of H per warp
+    static_assert(TS_P % NW == 0 && HR % 2 == 0, "H rows split evenly over the warps, in pairs");
     __shared__ Cx<float> Hs[TS_P * TS_LD], Qs[TS_P * TS_LD];
     __shared__ JacScratch<float> sc;
     __shared__ int order[TS_P];
-    __shared__ float s_fro[JS_THREADS / 32];
-    const int tid = threadIdx.x;
-    for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
+    __shared__ float s_fro[NW];
+    __shared__ __align__(16) float2 sv[TS_P][TS_P];
+    __shared__ __align__(16) float2 sy[TS_P][TS_P + 1];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // H[i][k], i = HR warp + m, k = lane
+    float2 h[HR];
+#pragma unroll
+    for (int m = 0; m < HR; ++m)
+        h[m] = make_float2(0.f, 0.f);
+    for (int t0 = 0; t0 < T; t0 += TS_P)
     {
-        const int i = e / TS_P, k = e % TS_P;
-        float re = 0.f, im = 0.f;
-        for (int t = 0; t < T; ++t)
+        for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
         {
-            const float2 a = V[static_cast<size_t>(t) * TS_P + i], b = Y[static_cast<size_t>(t) * TS_P + k];
-            re += a.x * b.x + a.y * b.y;
-            im += a.x * b.y - a.y * b.x;
+            const int r = e / TS_P, c = e % TS_P, t = t0 + r;
+            sv[r][c] = t < T ? V[static_cast<size_t>(t) * TS_P + c] : make_float2(0.f, 0.f);
+            sy[r][c] = t < T ? Y[static_cast<size_t>(t) * TS_P + c] : make_float2(0.f, 0.f);
         }
-        Hs[i * TS_LD + k] = {re, im};
-        Qs[i * TS_LD + k] = {i == k ? 1.f : 0.f, 0.f};
+        __syncthreads();
+#pragma unroll 4
+        for (int r = 0; r < TS_P; ++r)
+        {
+            const float2 b = sy[r][lane];
+#pragma unroll
+            for (int m = 0; m < HR; m += 2)
+            {
+                const float4 a2 = *reinterpret_cast<const float4*>(&sv[r][HR * warp + m]);
+                h[m].x += a2.x * b.x + a2.y * b.y;
+                h[m].y += a2.x * b.y - a2.y * b.x;
+                h[m + 1].x += a2.z * b.x + a2.w * b.y;
+                h[m + 1].y += a2.z * b.y - a2.w * b.x;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int m = 0; m < HR; ++m)
+    {
+        const int i = HR * warp + m;
+        Hs[i * TS_LD + lane] = {h[m].x, h[m].y};
+        Qs[i * TS_LD + lane] = {i == lane ? 1.f : 0.f, 0.f};
     }
     __syncthreads();
     // Hermitian part, real diagonal; round-off floor as in the other FP32 sweeps
@@ -1846,19 +2068,19 @@ __global__ void __launch_bounds__(JS_THREADS) k_ts_rr(const float2* __restrict__
         if (i <= k)
         {
             const Cx<float> a = Hs[i * TS_LD + k], b = Hs[k * TS_LD + i];
-            const Cx<float> h = {0.5f * (a.x + b.x), i == k ? 0.f : 0.5f * (a.y - b.y)};
-            Hs[i * TS_LD + k] = h;
-            Hs[k * TS_LD + i] = {h.x, -h.y};
-            f2 += (i == k ? 1.f : 2.f) * (h.x * h.x + h.y * h.y);
+            const Cx<float> hh = {0.5f * (a.x + b.x), i == k ? 0.f : 0.5f * (a.y - b.y)};
+            Hs[i * TS_LD + k] = hh;
+            Hs[k * TS_LD + i] = {hh.x, -hh.y};
+            f2 += (i == k ? 1.f : 2.f) * (hh.x * hh.x + hh.y * hh.y);
         }
     }
     for (int o = 16; o > 0; o >>= 1)
         f2 += __shfl_xor_sync(0xffffffffu, f2, o);
-    if ((tid & 31) == 0)
-        s_fro[tid >> 5] = f2;
+    if (lane == 0)
+        s_fro[warp] = f2;
     __syncthreads();
     float tot = 0.f;
-    for (int w = 0; w < JS_THREADS / 32; ++w)
+    for (int w = 0; w < NW; ++w)
         tot += s_fro[w];
     smem_sweeps<float, JS_THREADS>(Hs, Qs, TS_P, TS_P, TS_LD, sc, 5e-7f * sqrtf(tot), JAC_MAX_SWEEPS);
     __syncthreads();
@@ -1877,19 +2099,47 @@ __global__ void __launch_bounds__(JS_THREADS) k_ts_rr(const float2* __restrict__
     for (int i = tid; i < T - TS_P; i += JS_THREADS)
         evals[i] = 0.0;
     __syncthreads();
-    for (int e = tid; e < T * TS_P; e += JS_THREADS)
+    // U = V Q in rank order: lane r holds column order[r] of Q
+    float2 q[TS_P];
     {
-        const int t = e / TS_P, r = e % TS_P, q = order[r];
-        float re = 0.f, im = 0.f;
+        const int qc = order[lane];
+#pragma unroll
         for (int k = 0; k < TS_P; ++k)
+            q[k] = make_float2(Qs[k * TS_LD + qc].x, Qs[k * TS_LD + qc].y);
+    }
+    for (int t0 = 0; t0 < T; t0 += TS_P)
+    {
+        for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
         {
-            const float2 v = V[static_cast<size_t>(t) * TS_P + k];
-            const Cx<float> qq = Qs[k * TS_LD + q];
-            re += v.x * qq.x - v.y * qq.y;
-            im += v.x * qq.y + v.y * qq.x;
+            const int r = e / TS_P, c = e % TS_P, t = t0 + r;
+            sv[r][c] = t < T ? V[static_cast<size_t>(t) * TS_P + c] : make_float2(0.f, 0.f);
         }
-        Vw[e] = make_float2(re, im);
-        evecs[static_cast<size_t>(T - TS_P + r) * T + t] = make_double2(re, im);
+        __syncthreads();
+        for (int rr = warp; rr < TS_P; rr += NW)
+        {
+            float re = 0.f, im = 0.f;
+#pragma unroll
+            for (int k = 0; k < TS_P; k += 2)
+            {
+                const float4 v2 = *reinterpret_cast<const float4*>(&sv[rr][k]);
+                re += v2.x * q[k].x - v2.y * q[k].y;
+                im += v2.x * q[k].y + v2.y * q[k].x;
+                re += v2.z * q[k + 1].x - v2.w * q[k + 1].y;
+                im += v2.z * q[k + 1].y + v2.w * q[k + 1].x;
+            }
+            sy[rr][lane] = make_float2(re, im);
+            if (t0 + rr < T)
+                Vw[static_cast<size_t>(t0 + rr) * TS_P + lane] = make_float2(re, im);
+        }
+        __syncthreads();
+        // the eigenvector columns are contiguous over t: lane = row of the block
+        if (t0 + lane < T)
+            for (int r = warp; r < TS_P; r += NW)
+            {
+                const float2 u = sy[lane][r];
+                evecs[static_cast<size_t>(T - TS_P + r) * T + t0 + lane] = make_double2(u.x, u.y);
+            }
+        __syncthreads();
     }
 }
 
@@ -1918,16 +2168,22 @@ size_t pca_eigh_workspace(int T)
 }
 
 hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin, int pmax, float2* weights, void* work,
-                   cudaStream_t st, int refine_lo, int refine_hi, bool warm, bool kept_only)
+                   cudaStream_t st, int refine_lo, int refine_hi, bool warm, bool kept_only, bool* cov_kept)
 {
+    if (cov_kept)
+        *cov_kept = true;
     if (T <= 0 || !work)
         return HV_INVALID_VALUE;
     // kept_only: the caller uses the refined eigenvectors (ranks refine_lo..refine_hi) and the
     // order of the eigenvalues only, so the FP32 sweeps stop at a coarser floor and the other
-    // eigenvalues are FP32 Rayleigh quotients (cfg3, T = 512: 15 sweeps and 13.8 ms -> 5 sweeps, the
-    // view unchanged at 3.5e-7 from FP64)
+    // eigenvalues are FP32 Rayleigh quotients (T = 512: 15 sweeps and 13.8 ms -> 5 sweeps, the view
+    // unchanged at 3.5e-7 from FP64). The floor is relative to the whole matrix, so only kept ranks
+    // among the TS_MAX_KEEP largest qualify: for smaller kept eigenvalues (ranks 175-178 of 192 at
+    // ~1.5e-3 of the largest) the rotations skipped below it left errors the FP64 corrections did
+    // not remove (view 1e-4 .. 4e-4 from FP64).
     const int Kr = refine_hi - refine_lo + 1;
-    const bool loose = kept_only && refine_lo >= 0 && refine_hi < T && Kr >= 1 && Kr <= ER_MAX_K;
+    const bool loose = kept_only && refine_lo >= 0 && refine_hi < T && Kr >= 1 && Kr <= ER_MAX_K &&
+                       refine_lo >= T - TS_MAX_KEEP;
     const float floor_rel = loose ? 2e-5f : 5e-7f;
 
     const int prec = g_eig_precision.load();  // one read: a concurrent switch cannot split the dispatch
@@ -1955,14 +2211,14 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         double2* D = Y + static_cast<size_t>(ER_MAX_K) * T;
         double2* G = D + static_cast<size_t>(ER_MAX_K) * T;
         double2* Vn = G + static_cast<size_t>(ER_MAX_K) * T;
-        const dim3 gw((T + 7) / 8, Kr), gp((T - b0 + 7) / 8, Kr), gt((T + 127) / 128, Kr);
+        const dim3 gw((T + 7) / 8, Kr), gp(T - b0, Kr), gt((T + 31) / 32, Kr);
         for (int iter = 0; iter < iters; ++iter)
         {
             k_eigref_matvec<<<gw, 256, 0, st>>>(cov, evecs, T, refine_lo, Y);
             HV_LAUNCH_CHECK();
-            k_eigref_project<<<gp, 256, 0, st>>>(evecs, Y, T, refine_lo, b0, D, G);
+            k_eigref_project<<<gp, ER_PROJ_THREADS, 0, st>>>(evecs, Y, T, refine_lo, b0, D, G);
             HV_LAUNCH_CHECK();
-            k_eigref_update<<<gt, 128, 0, st>>>(evecs, evals, D, G, Y, T, refine_lo, Kr, b0, Vn);
+            k_eigref_update<<<gt, 32 * ER_UPD_WARPS, 0, st>>>(evecs, evals, D, G, Y, T, refine_lo, Kr, b0, Vn);
             HV_LAUNCH_CHECK();
             k_eigref_finish<<<Kr, 128, 0, st>>>(evecs, evals, Vn, D, G, T, refine_lo, pmin, pmax, weights);
             HV_LAUNCH_CHECK();
@@ -1979,35 +2235,35 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         float2* Vw = Ys + static_cast<size_t>(T) * TS_P;
         double* scale = reinterpret_cast<double*>(Vw + static_cast<size_t>(T) * TS_P);
         const int gb = (T * TS_P + 255) / 256;
-        const size_t osmem = static_cast<size_t>(T) * TS_LD * sizeof(float2);
-        static const cudaError_t attr = cudaFuncSetAttribute(
-            k_ts_orth, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(JC_MAX_T * TS_LD * sizeof(float2)));
-        HV_CUDA_TRY(attr);
+        const int gm = (T + TS_MM_ROWS - 1) / TS_MM_ROWS;
+        constexpr int mm_threads = TS_MM_ROWS * TS_MM_SPLIT * 32;
         k_ts_convert<<<std::min(512, (T * T + 1023) / 1024), 256, 0, st>>>(cov, T, C32, scale);
         HV_LAUNCH_CHECK();
-        if (warm)
-            k_ts_orth<<<1, TS_ORTH_THREADS, osmem, st>>>(Vw, T, Vs);
-        else
+        // warm: the previous window's Ritz vectors are orthonormal (V Q with V orthonormal, Q unitary)
+        // and start the iteration as they are
+        if (!warm)
         {
             k_ts_init<<<gb, 256, 0, st>>>(C32, T, Ys);
             HV_LAUNCH_CHECK();
-            k_ts_orth<<<1, TS_ORTH_THREADS, osmem, st>>>(Ys, T, Vs);
+            k_ts_orth<<<1, TS_ORTH_THREADS, 0, st>>>(Ys, T, Vs);
+            HV_LAUNCH_CHECK();
         }
-        HV_LAUNCH_CHECK();
         const int iters = warm ? TS_ITERS_WARM : TS_ITERS_COLD;
         for (int it = 0; it < iters; ++it)
         {
-            k_ts_matmul<<<gb, 256, 0, st>>>(C32, Vs, T, Ys);
+            k_ts_matmul<<<gm, mm_threads, 0, st>>>(C32, it == 0 && warm ? Vw : Vs, T, Ys);
             HV_LAUNCH_CHECK();
-            k_ts_orth<<<1, TS_ORTH_THREADS, osmem, st>>>(Ys, T, Vs);
+            k_ts_orth<<<1, TS_ORTH_THREADS, 0, st>>>(Ys, T, Vs);
             HV_LAUNCH_CHECK();
         }
-        k_ts_matmul<<<gb, 256, 0, st>>>(C32, Vs, T, Ys);
+        k_ts_matmul<<<gm, mm_threads, 0, st>>>(C32, Vs, T, Ys);
         HV_LAUNCH_CHECK();
         k_ts_rr<<<1, JS_THREADS, 0, st>>>(Vs, Ys, T, scale, evecs, evals, Vw);
         HV_LAUNCH_CHECK();
-        count_launch(4 + 2 * iters + (warm ? 0 : 1));
-        return refine_kept(T - TS_P, 3);
+        count_launch(3 + 2 * iters + (warm ? 0 : 2));
+        // two corrections: on the benchmark's sliding windows (T = 512, stride 64) one warm iteration
+        // and two corrections already reach the view error of three and three (3.5e-7 .. 1.9e-6)
+        return refine_kept(T - TS_P, 2);
     }
     if (T <= JS_MAX_T && prec == HV_EIG_FP32)
     {
@@ -2076,7 +2332,11 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         count_launch();
     }
     else
-        k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);  // FP64 sweeps
+    {
+        k_jacobi<<<1, JAC_THREADS, 0, st>>>(cov, V, T, Tp, ev_unsorted, pairs, rot);  // FP64 sweeps, in place
+        if (cov_kept)
+            *cov_kept = false;
+    }
     HV_LAUNCH_CHECK();
     k_eig_sort<<<T, 128, 0, st>>>(ev_unsorted, V, T, evals, evecs, pmin, pmax, weights);
     HV_LAUNCH_CHECK();

@@ -48,6 +48,59 @@ def test_covariance_engine(cuda, mode, tol, T, npix):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("T,npix", [(65, 1000), (128, 65536), (200, 4104), (512, 16384)])
+def test_covariance_planes_bit_identical(cuda, T, npix):
+    """The tiled tensor-core covariance from the split-BF16 planes (hv_pca_split_planes, then
+    hv_pca_covariance_planes: tensor copies straight into the MMA operand layout) is bit-identical to
+    the same engine converting the ring itself; after a wrapping range of ring slots is rewritten and
+    only those slots re-split, the update of the rows and columns of their 64-frame blocks equals the
+    full recomputation bit for bit."""
+    L = hv.lib()
+    ring = _ring(T, npix, T + 7)
+    rd = dev(ring)
+    work = empty(L.hv_pca_cov_workspace(T, npix))
+    planes = empty(L.hv_pca_planes_bytes(T, npix))
+    assert L.hv_pca_planes_bytes(T, npix) == 8 * T * npix
+    cov_ring, cov_pl = empty(T * T * 16), empty(T * T * 16)
+    L.hv_pca_covariance_mode(2)
+    try:
+        call("hv_pca_covariance", ptr(rd), T, npix, ptr(cov_ring), ptr(work), None)
+        call("hv_pca_split_planes", ptr(rd), T, npix, 0, T, ptr(planes), None)
+        call("hv_pca_covariance_planes", ptr(planes), T, npix, 0xFFFFFFFF, ptr(cov_pl), ptr(work), None)
+        cuda.cuda.synchronize()
+        assert L.hv_pca_covariance_status(ptr(work)) == hv.HV_OK
+        a, b = host(cov_ring, np.complex128, (T, T)), host(cov_pl, np.complex128, (T, T))
+        assert np.array_equal(a, b), float(np.abs(a - b).max() / np.abs(a).max())
+        assert rel_l2(b, O.pca_covariance(ring.astype(np.complex128).reshape(T, npix, 1))) <= 2e-5
+        # rewrite slots T - 20 .. T + 29 (mod T)
+        slot0, n = T - 20, min(50, T)
+        slots = [(slot0 + f) % T for f in range(n)]
+        ring2 = ring.copy()
+        ring2[slots] = _ring(T, npix, T + 8)[slots]
+        rd2 = dev(ring2)
+        blocks = 0
+        for sl in slots:
+            blocks |= 1 << (sl // 64)
+        assert blocks != (1 << ((T + 63) // 64)) - 1 or T <= 128
+        call("hv_pca_split_planes", ptr(rd2), T, npix, slot0, n, ptr(planes), None)
+        call("hv_pca_covariance_planes", ptr(planes), T, npix, blocks, ptr(cov_pl), ptr(work), None)
+        call("hv_pca_covariance", ptr(rd2), T, npix, ptr(cov_ring), ptr(work), None)
+        cuda.cuda.synchronize()
+        assert L.hv_pca_covariance_status(ptr(work)) == hv.HV_OK
+    finally:
+        L.hv_pca_covariance_mode(0)
+    a, b = host(cov_ring, np.complex128, (T, T)), host(cov_pl, np.complex128, (T, T))
+    assert np.array_equal(a, b), float(np.abs(a - b).max() / np.abs(a).max())
+    # the SIMT mode has no planes path
+    L.hv_pca_covariance_mode(1)
+    try:
+        assert L.hv_pca_covariance_planes(ptr(planes), T, npix, 0xFFFFFFFF, ptr(cov_pl), ptr(work), None) == \
+            hv.HV_ERR_UNSUPPORTED
+    finally:
+        L.hv_pca_covariance_mode(0)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("T", [2, 31, 64, 96, 129, 256, 512])
 def test_jacobi_paths(cuda, T, precision):
