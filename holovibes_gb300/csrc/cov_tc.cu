@@ -33,12 +33,12 @@ namespace hv {
 
 namespace {
 
-constexpr int TC_CONVERTERS = 512;              // warps 0-15
-constexpr int TC_MMA_WARP = TC_CONVERTERS / 32;  // warp 16 issues the MMAs
-constexpr int TC_LOAD_WARP = TC_MMA_WARP + 1;    // warp 17 issues the tensor copies
+constexpr int TC_CONVERTERS = 256;              // warps 0-7
+constexpr int TC_MMA_WARP = TC_CONVERTERS / 32;  // warp 8 issues the MMAs
+constexpr int TC_LOAD_WARP = TC_MMA_WARP + 1;    // warp 9 issues the tensor copies
 constexpr int TC_THREADS = TC_CONVERTERS + 64;
 constexpr int TC_A_STAGES = 2;
-constexpr int TC_A_STAGES_PACKED = 4;
+constexpr int TC_A_STAGES_PACKED = 2;
 constexpr int TC_MAX_RAW = 8;
 constexpr int TC_KC = 64;           // pixels (K elements) per chunk
 constexpr int TC_ROWS = 128;        // M rows of the operand tile (2T <= 128, zero padded)
@@ -59,7 +59,7 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) { return tc::sw128_
 using tc::instr_desc;
 
 // part: [gridDim.x][2T][2T] FP32 partial G; err: set to 1 when a bounded wait gave up.
-__global__ void __launch_bounds__(TC_THREADS, 1) k_cov_tc(const __grid_constant__ CUtensorMap ring_map, int T,
+__global__ void __launch_bounds__(TC_THREADS, 2) k_cov_tc(const __grid_constant__ CUtensorMap ring_map, int T,
                                                           size_t npix, size_t chunks_per_cta, int N, uint32_t tmem_cols,
                                                           int raw_stages, int packed, float* __restrict__ part,
                                                           int* __restrict__ err)
@@ -336,19 +336,26 @@ int sm_count();
 // ------------------------------------------------------------------------------ tiled (T > 64)
 // G (2T x 2T) in 128 x 128 tiles (bm, bn), bm <= bn: operand A = Y rows of frames 64 bm .. 64 bm + 63,
 // B = frames 64 bn .. (the same as A on diagonal tiles; frames >= T are zero-filled by the tensor
-// copy). CTA (split ks, tile tp) walks the 64-pixel chunks of split ks: the loader brings the A
-// and B chunks ([64 frames][64 px] complex, 32 KB each) into a ring of R raw stages, the sixteen
-// converter warps split them into Ah / Al / Bh / Bl (one converted stage), the MMA warp issues
-// Ah Bh^T, Ah Bl^T, Al Bh^T (M = N = 128, K = 16) into three TMEM accumulators. The CTAs of one
-// split stream the same chunks at the same time, so each chunk comes from HBM about once and the
-// other tiles read it from L2.
+// copy), from the split-BF16 planes of the ring (below). CTA (split ks, tile tp) walks the 64-pixel
+// chunks of split ks (TT_SPLIT_CHUNKS chunks, whatever the number of tiles, so that an entry's sums
+// do not depend on which tiles a launch computes); the MMA warp issues Ah Bh^T, Ah Bl^T, Al Bh^T
+// (M = N = 128, K = 16) into three TMEM accumulators in chains of at most kMaxChainChunks chunks,
+// whose sums the epilogue warps add in FP32 registers. The CTAs of one split stream the same
+// chunks at about the same time, so each chunk comes from HBM about once and the other tiles read
+// it from L2.
 constexpr int TT_FRAMES = 64;                          // frames per operand tile (128 rows of Y)
-constexpr int TT_CONVERTERS = 512;                     // warps 0-15 convert
-constexpr int TT_MMA_WARP = TT_CONVERTERS / 32;        // warp 16 issues the MMAs
-constexpr int TT_LOAD_WARP = TT_MMA_WARP + 1;          // warp 17 issues the tensor copies
-constexpr int TT_THREADS = TT_CONVERTERS + 64;
-constexpr uint32_t TT_RAW_HALF = TT_FRAMES * TC_KC * 8;  // one [64 frames][64 px] complex chunk: 32 KB
-constexpr int TT_MAX_RAW = 3;
+
+// Longest accumulation chain (64-pixel chunks, 4 MMA K-steps each) one TMEM accumulator takes.
+// The FP32 accumulation of a tcgen05.mma into its accumulator does not round to nearest: summing
+// 262144 pixels (4096 K-steps) into one accumulator drifted by 3.4e-4 relative to the FP64 sum on
+// 512 x 512 frames (measured), about one unit of the last place per step in one direction; with
+// chains of 64 chunks the drift was 1e-5 (a uniform scale: 9e-7 left after it). Chain sums are
+// added in FP32 registers (round to nearest) within a split, the splits' partial tiles in FP64.
+// The packed kernel (T <= 32) keeps one wave up to 128 chunks per CTA (1024 x 1024 frames: 108),
+// where its extra waves cost more time than the drift costs accuracy.
+constexpr size_t kMaxChainChunks = 64;
+constexpr size_t kMaxChainChunksPacked = 128;
+constexpr size_t TT_SPLIT_CHUNKS = 4 * kMaxChainChunks;  // chunks per split of the tiled kernel
 
 constexpr int TT_MAX_BLOCKS = COV_TC_MAX_T / TT_FRAMES;  // 64-frame blocks of a ring (16)
 constexpr int TT_MAX_PAIRS = TT_MAX_BLOCKS * (TT_MAX_BLOCKS + 1) / 2;
@@ -362,200 +369,6 @@ struct TileList
     unsigned char bm[TT_MAX_PAIRS], bn[TT_MAX_PAIRS];
     signed char index[TT_MAX_BLOCKS][TT_MAX_BLOCKS];
 };
-
-// part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * tiles.n + tp)
-__global__ void __launch_bounds__(TT_THREADS, 1) k_cov_tc_tiled(const __grid_constant__ CUtensorMap ring_map,
-                                                                size_t npix, const __grid_constant__ TileList tiles_in,
-                                                                size_t chunks_per_split, int raw_stages,
-                                                                float* __restrict__ part, int* __restrict__ err)
-{
-    extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t* tiles = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);  // Ah, Al, Bh, Bl (16 KB each)
-    uint8_t* raw_base = tiles + 4 * TILE_BYTES;
-    __shared__ __align__(8) uint64_t raw_full[TT_MAX_RAW], raw_empty[TT_MAX_RAW];
-    __shared__ __align__(8) uint64_t a_full, a_empty, done, drain;
-    __shared__ uint32_t tmem_base;
-    __shared__ int s_abort;
-
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int R = raw_stages;
-    const int tp = static_cast<int>(blockIdx.x % static_cast<unsigned>(tiles_in.n));
-    const int ks = static_cast<int>(blockIdx.x / static_cast<unsigned>(tiles_in.n));
-    const int bm = tiles_in.bm[tp], bn = tiles_in.bn[tp];
-    const bool diag = bm == bn;
-    const uint32_t raw_bytes = 2 * TT_RAW_HALF;
-    const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    const size_t c_begin = static_cast<size_t>(ks) * chunks_per_split;
-    size_t c_end = c_begin + chunks_per_split;
-    if (c_end > nchunks)
-        c_end = nchunks;
-    const int nmine = static_cast<int>(c_end > c_begin ? c_end - c_begin : 0);
-    volatile int* abort = &s_abort;
-    constexpr uint32_t N = TC_ROWS;  // accumulator columns per product
-
-    if (tid == 0)
-    {
-        for (int i = 0; i < R; ++i)
-        {
-            mbar_init(&raw_full[i], 1);
-            mbar_init(&raw_empty[i], TT_CONVERTERS / 32);
-        }
-        mbar_init(&a_full, TT_CONVERTERS / 32);
-        mbar_init(&a_empty, 1);
-        mbar_init(&done, 1);
-        mbar_init(&drain, 1);
-        s_abort = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (warp == TT_MMA_WARP)
-    {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                     "r"(512u)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = tmem_base;
-
-    if (warp == TT_LOAD_WARP)
-    {
-        // ------------------------------------------------------------------ loader (TMA)
-        if (lane == 0)
-        {
-            asm volatile("prefetch.tensormap [%0];" ::"l"(&ring_map) : "memory");
-            for (int m = 0; m < nmine; ++m)
-            {
-                const int r = m % R;
-                if (m >= R)
-                    mbar_wait(&raw_empty[r], static_cast<uint32_t>(((m / R) - 1) & 1), abort);
-                if (*abort)
-                    break;
-                const int x = static_cast<int>(2 * TC_KC * (c_begin + m));
-                tc::mbar_arrive_expect_tx(&raw_full[r], diag ? TT_RAW_HALF : raw_bytes);
-                uint8_t* dst = raw_base + r * raw_bytes;
-                tc::tma_load_2d(dst, &ring_map, x, bm * TT_FRAMES, &raw_full[r]);
-                if (!diag)
-                    tc::tma_load_2d(dst + TT_RAW_HALF, &ring_map, x, bn * TT_FRAMES, &raw_full[r]);
-            }
-        }
-        __syncwarp();
-    }
-    else if (warp < TT_MMA_WARP)
-    {
-        // ------------------------------------------------------------------ converters
-        // row t of a raw chunk (frame t: 64 complex samples, 512 B): lane l reads pixels 2l, 2l+1
-        // and writes 32-bit words of rows 2t (Re) and 2t + 1 (Im), K group l / 4
-        const int g = lane >> 2;
-        const uint32_t j4 = static_cast<uint32_t>(lane & 3) * 4u;
-        for (int it = 0; it < nmine; ++it)
-        {
-            const int r = it % R;
-            mbar_wait(&raw_full[r], static_cast<uint32_t>((it / R) & 1), abort);
-            if (it >= 1)
-                mbar_wait(&a_empty, static_cast<uint32_t>((it - 1) & 1), abort);
-            if (*abort)
-                break;
-            const uint8_t* raw = raw_base + r * raw_bytes;
-            for (int op = 0; op < (diag ? 1 : 2); ++op)
-            {
-                const uint8_t* src = raw + op * TT_RAW_HALF;
-                uint8_t* th = tiles + (2 * op) * TILE_BYTES;
-                uint8_t* tl = th + TILE_BYTES;
-                for (int t = warp; t < TT_FRAMES; t += TT_CONVERTERS / 32)
-                {
-                    const float4 f = reinterpret_cast<const float4*>(src + t * (TC_KC * 8))[lane];
-                    uint32_t reh, rel, imh, iml;
-                    tc::split2(f.x, f.z, reh, rel);
-                    tc::split2(f.y, f.w, imh, iml);
-                    const uint32_t ore = tile_offset(2 * t, g) + j4, oim = tile_offset(2 * t + 1, g) + j4;
-                    *reinterpret_cast<uint32_t*>(th + ore) = reh;
-                    *reinterpret_cast<uint32_t*>(th + oim) = imh;
-                    *reinterpret_cast<uint32_t*>(tl + ore) = rel;
-                    *reinterpret_cast<uint32_t*>(tl + oim) = iml;
-                }
-            }
-            fence_async_smem();
-            __syncwarp();
-            if (lane == 0)
-            {
-                mbar_arrive(&raw_empty[r]);
-                mbar_arrive(&a_full);
-            }
-        }
-    }
-    else if (lane == 0)
-    {
-        // ------------------------------------------------------------------ MMA issuer
-        const uint32_t idesc = instr_desc(TC_ROWS, TC_ROWS);
-        const uint32_t ah = smem_u32(tiles), al = ah + TILE_BYTES;
-        const uint32_t bh = diag ? ah : ah + 2 * TILE_BYTES, bl = diag ? al : ah + 3 * TILE_BYTES;
-        for (int it = 0; it < nmine; ++it)
-        {
-            mbar_wait(&a_full, static_cast<uint32_t>(it & 1), abort);
-            if (*abort)
-                break;
-            tc_fence_after();
-#pragma unroll
-            for (int s2 = 0; s2 < TC_KC / 16; ++s2)
-            {
-                const uint64_t dah = smem_desc(ah + s2 * 32), dal = smem_desc(al + s2 * 32);
-                const uint64_t dbh = smem_desc(bh + s2 * 32), dbl = smem_desc(bl + s2 * 32);
-                const uint32_t acc = (it > 0 || s2 > 0) ? 1u : 0u;
-                mma_bf16(tmem, dah, dbh, idesc, acc);          // Ah Bh^T
-                mma_bf16(tmem + N, dah, dbl, idesc, acc);      // Ah Bl^T
-                mma_bf16(tmem + 2 * N, dal, dbh, idesc, acc);  // Al Bh^T
-            }
-            mma_commit(&a_empty);
-        }
-        mma_commit(&done);
-    }
-    // epilogue: warps 0-3 read rows 32w .. 32w + 31 of the tile
-    if (warp < 4)
-    {
-        mbar_wait(&done, 0, abort);
-        tc_fence_after();
-        const int r = warp * 32 + lane;
-        float* dst = part + static_cast<size_t>(blockIdx.x) * TC_ROWS * TC_ROWS + static_cast<size_t>(r) * TC_ROWS;
-        for (int c0 = 0; c0 < TC_ROWS; c0 += 16)
-        {
-            float v[16], w1[16], w2[16];
-            const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
-            tmem_ld16(taddr, v);
-            tmem_ld16(taddr + N, w1);
-            tmem_ld16(taddr + 2 * N, w2);
-#pragma unroll
-            for (int i = 0; i < 16; ++i)
-                dst[c0 + i] = nmine ? v[i] + w1[i] + w2[i] : 0.f;
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (s_abort)
-    {
-        // a wait gave up: the copies and MMAs already issued finish before shared and tensor memory
-        // are released (bounded waits)
-        if (warp == TT_LOAD_WARP && lane == 0)
-        {
-            for (int m = nmine - R > 0 ? nmine - R : 0; m < nmine; ++m)
-                mbar_wait(&raw_full[m % R], static_cast<uint32_t>((m / R) & 1));
-            atomicExch(err, 1);
-        }
-        if (warp == TT_MMA_WARP && lane == 0)
-        {
-            mma_commit(&drain);
-            mbar_wait(&drain, 0);
-        }
-        __syncthreads();
-    }
-    if (warp == TT_MMA_WARP)
-    {
-        tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
-    }
-}
 
 // cov[i][j] from the tiled partials: row 2i of G is row 2 (i % 64) of tile row i / 64; the upper
 // triangle (i <= j) is read from tile (i / 64, j / 64) and mirrored. Sums in FP64 over the splits:
@@ -616,14 +429,12 @@ __global__ void __launch_bounds__(TR_ENTRIES * TR_GROUPS) k_cov_tc_tiled_reduce(
     cov[e] = make_double2(g00 + g11, mirror ? -im : im);
 }
 
-// ------------------------------------------------------------------ tiled, from pre-split planes
-// The split-BF16 operands of the ring kept beside it: planes[p][2 s + c][px] (p = 0: hi = bf16_rn(x),
-// p = 1: lo = bf16_rn(x - hi); c = 0: real, c = 1: imaginary part of pixel px of ring slot s), written
-// once per frame when it enters the ring. The tiled covariance then streams the four operand tiles
-// of a chunk (Ah, Al, Bh, Bl: 128 rows x 64 pixels each) by 3-D tensor copies straight into the
-// swizzled K-major layout the MMAs read: no converter warps, and a chunk is split once instead of
-// once per tile it takes part in. Same tiles, splits, MMA order and partial layout as
-// k_cov_tc_tiled: the results are bit-identical.
+// ------------------------------------------------------------------ split-BF16 planes of the ring
+// planes[p][2 s + c][px] (p = 0: hi = bf16_rn(x), p = 1: lo = bf16_rn(x - hi); c = 0: real, c = 1:
+// imaginary part of pixel px of ring slot s), written once per frame when it enters the ring. The
+// tiled covariance streams the four operand tiles of a chunk (Ah, Al, Bh, Bl: 128 rows x 64 pixels
+// each) from them by 3-D tensor copies straight into the swizzled K-major layout the MMAs read, so
+// that a chunk is split once instead of once per tile it takes part in.
 
 // Thread: 8 consecutive pixels of one frame of slots slot0 .. slot0 + n - 1 (mod T).
 __global__ void k_ring_split(const float2* __restrict__ ring, int T, size_t npix, int slot0, int n,
@@ -664,16 +475,15 @@ constexpr int TP_LOAD_WARP = TP_EPI_WARPS + 1;  // warp 5 issues the tensor copi
 constexpr int TP_THREADS = (TP_EPI_WARPS + 2) * 32;
 constexpr uint32_t TP_STAGE_BYTES = 4 * TILE_BYTES;  // Ah, Al, Bh, Bl
 
-// part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * tiles.n + tp), as k_cov_tc_tiled
-__global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_planes(const __grid_constant__ CUtensorMap planes_map,
-                                                                 size_t npix, const __grid_constant__ TileList tiles_in,
-                                                                 size_t chunks_per_split, float* __restrict__ part,
-                                                                 int* __restrict__ err)
+// part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * tiles.n + tp)
+__global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_tiled(const __grid_constant__ CUtensorMap planes_map,
+                                                                size_t npix, const __grid_constant__ TileList tiles_in,
+                                                                float* __restrict__ part, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* stages = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
     __shared__ __align__(8) uint64_t full[TP_STAGES], empty[TP_STAGES];
-    __shared__ __align__(8) uint64_t done, drain;
+    __shared__ __align__(8) uint64_t acc_full, acc_empty, drain;
     __shared__ uint32_t tmem_base;
     __shared__ int s_abort, s_issued;
 
@@ -683,11 +493,13 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_planes(const __grid_co
     const int bm = tiles_in.bm[tp], bn = tiles_in.bn[tp];
     const bool diag = bm == bn;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    const size_t c_begin = static_cast<size_t>(ks) * chunks_per_split;
-    size_t c_end = c_begin + chunks_per_split;
+    const size_t c_begin = static_cast<size_t>(ks) * TT_SPLIT_CHUNKS;
+    size_t c_end = c_begin + TT_SPLIT_CHUNKS;
     if (c_end > nchunks)
         c_end = nchunks;
     const int nmine = static_cast<int>(c_end > c_begin ? c_end - c_begin : 0);
+    constexpr int CHAIN = static_cast<int>(kMaxChainChunks);
+    const int nchains = (nmine + CHAIN - 1) / CHAIN;
     volatile int* abort = &s_abort;
     constexpr uint32_t N = TC_ROWS;
 
@@ -698,7 +510,8 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_planes(const __grid_co
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
-        mbar_init(&done, 1);
+        mbar_init(&acc_full, 1);
+        mbar_init(&acc_empty, TP_EPI_WARPS);
         mbar_init(&drain, 1);
         s_abort = 0;
         s_issued = 0;
@@ -718,6 +531,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_planes(const __grid_co
 
     if (warp == TP_LOAD_WARP)
     {
+        // ------------------------------------------------------------------ loader (TMA)
         if (lane == 0)
         {
             asm volatile("prefetch.tensormap [%0];" ::"l"(&planes_map) : "memory");
@@ -746,11 +560,19 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_planes(const __grid_co
     }
     else if (warp == TP_MMA_WARP)
     {
+        // ------------------------------------------------------------------ MMA issuer
         if (lane == 0)
         {
             const uint32_t idesc = instr_desc(TC_ROWS, TC_ROWS);
             for (int it = 0; it < nmine; ++it)
             {
+                const int pos = it % CHAIN;
+                if (pos == 0 && it > 0)
+                {
+                    // chain it / CHAIN - 1 done: the epilogue reads the accumulators before the next starts
+                    mma_commit(&acc_full);
+                    mbar_wait(&acc_empty, static_cast<uint32_t>((it / CHAIN - 1) & 1), abort);
+                }
                 const int st = it % TP_STAGES;
                 mbar_wait(&full[st], static_cast<uint32_t>((it / TP_STAGES) & 1), abort);
                 if (*abort)
@@ -763,35 +585,54 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_planes(const __grid_co
                 {
                     const uint64_t dah = smem_desc(ah + s2 * 32), dal = smem_desc(al + s2 * 32);
                     const uint64_t dbh = smem_desc(bh + s2 * 32), dbl = smem_desc(bl + s2 * 32);
-                    const uint32_t acc = (it > 0 || s2 > 0) ? 1u : 0u;
+                    const uint32_t acc = (pos > 0 || s2 > 0) ? 1u : 0u;
                     mma_bf16(tmem, dah, dbh, idesc, acc);          // Ah Bh^T
                     mma_bf16(tmem + N, dah, dbl, idesc, acc);      // Ah Bl^T
                     mma_bf16(tmem + 2 * N, dal, dbh, idesc, acc);  // Al Bh^T
                 }
                 mma_commit(&empty[st]);
             }
-            mma_commit(&done);
+            mma_commit(&acc_full);
         }
         __syncwarp();
     }
     else
     {
-        // epilogue: warp w reads rows 32w .. 32w + 31 of the tile
-        mbar_wait(&done, 0, abort);
-        tc_fence_after();
+        // ------------------------------------------------------------------ epilogue
+        // thread r (warp w, lane l: r = 32w + l) keeps row r of the split's tile: the sum over the
+        // chains of the three products' accumulators
         const int r = warp * 32 + lane;
-        float* dst = part + static_cast<size_t>(blockIdx.x) * TC_ROWS * TC_ROWS + static_cast<size_t>(r) * TC_ROWS;
-        for (int c0 = 0; c0 < TC_ROWS; c0 += 16)
-        {
-            float v[16], w1[16], w2[16];
-            const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
-            tmem_ld16(taddr, v);
-            tmem_ld16(taddr + N, w1);
-            tmem_ld16(taddr + 2 * N, w2);
+        float sum[TC_ROWS];
 #pragma unroll
-            for (int i = 0; i < 16; ++i)
-                dst[c0 + i] = nmine ? v[i] + w1[i] + w2[i] : 0.f;
+        for (int i = 0; i < TC_ROWS; ++i)
+            sum[i] = 0.f;
+        for (int c = 0; c < nchains; ++c)
+        {
+            mbar_wait(&acc_full, static_cast<uint32_t>(c & 1), abort);
+            if (*abort)
+                break;
+            tc_fence_after();
+#pragma unroll
+            for (int c0 = 0; c0 < TC_ROWS; c0 += 16)
+            {
+                float v[16], w1[16], w2[16];
+                const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
+                tmem_ld16(taddr, v);
+                tmem_ld16(taddr + N, w1);
+                tmem_ld16(taddr + 2 * N, w2);
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    sum[c0 + i] += v[i] + w1[i] + w2[i];
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(&acc_empty);
         }
+        float* dst = part + static_cast<size_t>(blockIdx.x) * TC_ROWS * TC_ROWS + static_cast<size_t>(r) * TC_ROWS;
+#pragma unroll
+        for (int i = 0; i < TC_ROWS; i += 4)
+            *reinterpret_cast<float4*>(dst + i) = make_float4(sum[i], sum[i + 1], sum[i + 2], sum[i + 3]);
     }
     tc_fence_before();
     __syncthreads();
@@ -826,15 +667,6 @@ struct TiledPlan
     size_t chunks_per_split;
 };
 
-// Longest accumulation chain (64-pixel chunks, 4 MMA K-steps each) one TMEM accumulator takes.
-// The FP32 accumulation of a tcgen05.mma into its accumulator does not round to nearest: summing
-// 262144 pixels (4096 K-steps) into one accumulator drifted by 3.4e-4 relative to the FP64 sum on
-// 512 x 512 frames (measured), about one unit of the last place per step in one direction; with
-// chains of 64 chunks the drift was 1e-5 (a uniform scale: 9e-7 left after it). The partial tiles
-// are summed in FP64. The packed kernel (T <= 32) keeps one wave up to 128 chunks per CTA (1024 x
-// 1024 frames: 108), where its extra waves cost more time than the drift costs accuracy.
-constexpr size_t kMaxChainChunks = 64;
-constexpr size_t kMaxChainChunksPacked = 128;
 
 TiledPlan tiled_plan(int T, size_t npix)
 {
@@ -842,16 +674,8 @@ TiledPlan tiled_plan(int T, size_t npix)
     p.nb = (T + TT_FRAMES - 1) / TT_FRAMES;
     p.npairs = p.nb * (p.nb + 1) / 2;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    size_t ns = static_cast<size_t>(sm_count() / p.npairs);  // one wave of persistent CTAs
-    if (ns < 1)
-        ns = 1;
-    const size_t min_ns = (nchunks + kMaxChainChunks - 1) / kMaxChainChunks;
-    if (ns < min_ns)
-        ns = min_ns;
-    if (ns > nchunks)
-        ns = nchunks;
-    p.chunks_per_split = (nchunks + ns - 1) / ns;
-    p.nsplit = static_cast<int>((nchunks + p.chunks_per_split - 1) / p.chunks_per_split);
+    p.chunks_per_split = TT_SPLIT_CHUNKS;
+    p.nsplit = static_cast<int>((nchunks + TT_SPLIT_CHUNKS - 1) / TT_SPLIT_CHUNKS);
     return p;
 }
 
@@ -880,8 +704,10 @@ TcPlan tc_plan(int T, size_t npix)
 {
     TcPlan p;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    // one persistent CTA per SM, or whole waves of them when a CTA's chain would exceed the limit
-    const size_t sms = static_cast<size_t>(sm_count());
+    // two persistent CTAs per SM (96 KB of shared memory each: two handoff pipelines per SM, 85.9
+    // -> 76.3 us at T = 32 on 1024 x 1024 frames against one CTA with 200 KB), or whole waves of
+    // them when a CTA's chain would exceed the limit
+    const size_t sms = 2 * static_cast<size_t>(sm_count());
     const size_t chain = 2 * T <= 64 ? kMaxChainChunksPacked : kMaxChainChunks;
     size_t waves = (nchunks + sms * chain - 1) / (sms * chain);
     if (waves < 1)
@@ -906,69 +732,26 @@ TcPlan tc_plan(int T, size_t npix)
 
 bool cov_tc_supported(int T) { return T >= 1 && T <= COV_TC_MAX_T; }
 
+// partial tiles of the tiled kernel (every tile), rounded to 256 bytes: the planes of a ring passed
+// to cov_tc follow them in the workspace
+static size_t tiled_part_bytes(int T, size_t npix)
+{
+    const TiledPlan q = tiled_plan(T, npix);
+    return (static_cast<size_t>(q.nsplit) * q.npairs * TC_ROWS * TC_ROWS * sizeof(float) + 255) & ~static_cast<size_t>(255);
+}
+
 size_t cov_tc_workspace(int T, size_t npix)
 {
     if (2 * T > TC_ROWS)
-    {
-        const TiledPlan q = tiled_plan(T, npix);
-        return static_cast<size_t>(q.nsplit) * q.npairs * TC_ROWS * TC_ROWS * sizeof(float) + 256;
-    }
+        return tiled_part_bytes(T, npix) + cov_planes_bytes(T, npix) + 256;
     const TcPlan p = tc_plan(T, npix);
     const size_t per = p.packed ? static_cast<size_t>(TC_ROWS) * 64 : static_cast<size_t>(4) * T * T;
     return static_cast<size_t>(p.ctas) * per * sizeof(float) + 256;
 }
 
-// The tiles touching the 64-frame blocks set in `blocks` (bit b: frames 64 b .. 64 b + 63), or all
-// of them. The split of the pixels is the full computation's (the same chunks per split whatever
-// the tile count), so a recomputed entry is bit-identical to the full computation's.
-static hv_status cov_tc_tiled_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err,
-                                     uint32_t blocks, cudaStream_t st)
-{
-    const TiledPlan q = tiled_plan(T, npix);
-    TileList tl{};
-    std::memset(tl.index, -1, sizeof(tl.index));
-    for (int bm = 0; bm < q.nb; ++bm)
-        for (int bn = bm; bn < q.nb; ++bn)
-            if (((blocks >> bm) & 1u) || ((blocks >> bn) & 1u))
-            {
-                tl.bm[tl.n] = static_cast<unsigned char>(bm);
-                tl.bn[tl.n] = static_cast<unsigned char>(bn);
-                tl.index[bm][bn] = static_cast<signed char>(tl.n);
-                ++tl.n;
-            }
-    if (tl.n == 0)
-        return HV_OK;
-    CUtensorMap tmap;
-    if (!tc::encode_tmap_2d_f32(&tmap, ring, 2 * npix, static_cast<uint64_t>(T), npix * 8, 2 * TC_KC,
-                                static_cast<uint32_t>(TT_FRAMES)))
-    {
-        set_last_error_msg("tensor-core covariance: cuTensorMapEncodeTiled failed");
-        return HV_ERR_CUDA;
-    }
-    const int raw = 2;
-    const size_t smem = 4 * static_cast<size_t>(TILE_BYTES) + raw * 2 * static_cast<size_t>(TT_RAW_HALF) + 1024;
-    HV_CUDA_TRY(cudaFuncSetAttribute(k_cov_tc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-    float* tpart = static_cast<float*>(work);
-    k_cov_tc_tiled<<<q.nsplit * tl.n, TT_THREADS, smem, st>>>(tmap, npix, tl, q.chunks_per_split, raw, tpart, err);
-    HV_LAUNCH_CHECK();
-    k_cov_tc_tiled_reduce<<<(T * T + TR_ENTRIES - 1) / TR_ENTRIES, TR_ENTRIES * TR_GROUPS, 0, st>>>(tpart, T, tl,
-                                                                                                  q.nsplit, cov);
-    HV_LAUNCH_CHECK();
-    count_launch(2);
-    return HV_OK;
-}
-
-hv_status cov_tc_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, uint32_t blocks,
-                        cudaStream_t st)
-{
-    if (!cov_tc_supported(T) || 2 * T <= TC_ROWS || npix == 0 || npix % 8 != 0 ||
-        (reinterpret_cast<uintptr_t>(ring) & 15) != 0 || npix > (1ull << 29))
-        return HV_ERR_UNSUPPORTED;
-    return cov_tc_tiled_blocks(ring, T, npix, cov, work, err, blocks, st);
-}
-
 size_t cov_planes_bytes(int T, size_t npix) { return 8 * static_cast<size_t>(T) * npix; }
+
+size_t cov_tc_partial_bytes(int T, size_t npix) { return 2 * T > TC_ROWS ? tiled_part_bytes(T, npix) + 256 : 0; }
 
 bool cov_planes_supported(int T, size_t npix)
 {
@@ -1020,11 +803,11 @@ hv_status cov_tc_planes(const uint16_t* planes, int T, size_t npix, double2* cov
         return HV_ERR_CUDA;
     }
     const size_t smem = static_cast<size_t>(TP_STAGES) * TP_STAGE_BYTES + 1024;
-    static const cudaError_t attr = cudaFuncSetAttribute(k_cov_tc_planes, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    static const cudaError_t attr = cudaFuncSetAttribute(k_cov_tc_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                          static_cast<int>(smem));
     HV_CUDA_TRY(attr);
     float* tpart = static_cast<float*>(work);
-    k_cov_tc_planes<<<q.nsplit * tl.n, TP_THREADS, smem, st>>>(tmap, npix, tl, q.chunks_per_split, tpart, err);
+    k_cov_tc_tiled<<<q.nsplit * tl.n, TP_THREADS, smem, st>>>(tmap, npix, tl, tpart, err);
     HV_LAUNCH_CHECK();
     k_cov_tc_tiled_reduce<<<(T * T + TR_ENTRIES - 1) / TR_ENTRIES, TR_ENTRIES * TR_GROUPS, 0, st>>>(tpart, T, tl,
                                                                                                   q.nsplit, cov);
@@ -1048,13 +831,20 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
         return HV_ERR_UNSUPPORTED;
     }
     if (2 * T > TC_ROWS)
-        return cov_tc_tiled_blocks(ring, T, npix, cov, work, err, ~0u, st);
+    {
+        // the ring's split planes in the workspace after the partial tiles
+        uint16_t* planes = reinterpret_cast<uint16_t*>(static_cast<char*>(work) + tiled_part_bytes(T, npix));
+        hv_status r = cov_split_planes(ring, T, npix, 0, T, planes, st);
+        if (r != HV_OK)
+            return r;
+        return cov_tc_planes(planes, T, npix, cov, work, err, ~0u, st);
+    }
     const TcPlan p = tc_plan(T, npix);
-    // raw stages: T x 64 complex samples (T x 512 B) each, as many as fit beside the two A stages
+    // raw stages: T x 64 complex samples (T x 512 B) each, as many as fit beside the A stages in 96 KB
     const size_t raw_bytes = static_cast<size_t>(T) * TC_KC * 16;  // pairs of 64-pixel chunks
     const size_t a_bytes = p.packed ? static_cast<size_t>(TC_A_STAGES_PACKED) * TILE_BYTES
                                     : static_cast<size_t>(TC_A_STAGES) * 2 * TILE_BYTES;
-    int raw = static_cast<int>((200 * 1024 - a_bytes) / raw_bytes);
+    int raw = static_cast<int>((96 * 1024 - a_bytes) / raw_bytes);
     raw = raw > TC_MAX_RAW ? TC_MAX_RAW : (raw < 2 ? 2 : raw);
     const size_t smem = a_bytes + raw * raw_bytes + 1024;
     CUtensorMap map;

@@ -76,6 +76,8 @@ hv_status phase_increase(const float2* ring, int T, size_t HW, const float2* w, 
                          int use_hist, float* out, float2* mm, cudaStream_t st);
 hv_status rescale_float(const float* in, size_t HW, const float2* mm, float post_scale, float* out, cudaStream_t st);
 size_t pca_cov_workspace(int T, size_t npix);
+// the workspace of pca_covariance_planes (the caller keeps the planes) and of the SIMT engine
+size_t pca_cov_workspace_planes(int T, size_t npix);
 void set_cov_mode(int mode);
 int cov_mode();
 void set_cov_incremental(bool on);
@@ -85,11 +87,14 @@ hv_status pca_cov_status(const void* work);
 bool cov_tc_supported(int T);
 size_t cov_tc_workspace(int T, size_t npix);
 hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, cudaStream_t st);
-hv_status cov_tc_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, int* err, uint32_t blocks,
-                        cudaStream_t st);
+// partial tiles of the tiled tensor-core covariance (T > 64): the workspace when the caller passes
+// its own split planes
+size_t cov_tc_partial_bytes(int T, size_t npix);
 // Split-BF16 planes of the ring (T > 64): bytes, whether (T, npix) has them, the split of ring slots
-// slot0 .. slot0 + n - 1 (mod T) into them, and the tiled covariance (blocks as cov_tc_blocks, ~0u:
-// all) from them, bit-identical to cov_tc on the ring.
+// slot0 .. slot0 + n - 1 (mod T) into them, and the tiled covariance from them: `blocks` = ~0u for
+// all of it, else only the rows and columns of the 64-frame slot blocks set (bit b: slots 64 b ..
+// 64 b + 63), bit-identical to a full computation; cov_tc on a ring (T > 64) splits it into planes
+// in its workspace first.
 size_t cov_planes_bytes(int T, size_t npix);
 bool cov_planes_supported(int T, size_t npix);
 hv_status cov_split_planes(const float2* ring, int T, size_t npix, int slot0, int n, uint16_t* planes, cudaStream_t st);
@@ -99,12 +104,6 @@ hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, v
 // The covariance from the split planes (engine modes 0 and 2; HV_ERR_UNSUPPORTED for the SIMT mode
 // and shapes without planes).
 hv_status pca_covariance_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
-                                cudaStream_t st);
-// Recomputes only the rows and columns of `cov` (the previous covariance of the same ring) of the
-// 64-frame blocks set in `blocks` (bit b: ring slots 64 b .. 64 b + 63), bit-identical to a full
-// recomputation; HV_ERR_UNSUPPORTED when the engine in use has no such update (T <= 64, the FP32
-// SIMT engine): the caller then recomputes all of it.
-hv_status pca_covariance_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
                                 cudaStream_t st);
 size_t pca_eigh_workspace(int T);
 void set_eig_precision(int p);

@@ -168,7 +168,7 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
     if (uses_eig(s))
     {
         z.add(static_cast<size_t>(T) * T * 16 * 2 + T * 8);
-        z.add(pca_cov_workspace(T, HW));
+        z.add(uses_planes(fd, s, served) ? pca_cov_workspace_planes(T, HW) : pca_cov_workspace(T, HW));
         z.add(pca_eigh_workspace(T));
     }
     if (uses_planes(fd, s, served))
@@ -275,7 +275,8 @@ hv_status build(hv_pipe* p)
         HV_ALLOC(p->cov, static_cast<size_t>(p->T) * p->T * sizeof(double2));
         HV_ALLOC(p->evecs, static_cast<size_t>(p->T) * p->T * sizeof(double2));
         HV_ALLOC(p->evals, static_cast<size_t>(p->T) * sizeof(double));
-        HV_ALLOC(p->cov_work, pca_cov_workspace(p->T, HW));
+        HV_ALLOC(p->cov_work, uses_planes(p->fd, s, p->served) ? pca_cov_workspace_planes(p->T, HW)
+                                                                : pca_cov_workspace(p->T, HW));
         HV_ALLOC(p->eig_work, pca_eigh_workspace(p->T));
         // no warm start is read before an eigensolve wrote one; zeros if it ever is
         HV_CUDA_TRY(cudaMemsetAsync(p->eig_work, 0, pca_eigh_workspace(p->T), p->stream));
@@ -573,14 +574,6 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
         {
             r = inc && !dirty ? HV_OK
                               : pca_covariance_planes(p->planes, p->T, p->HW, p->cov, p->cov_work, inc ? dirty : ~0u, st);
-            if (r == HV_OK)
-                done = true;
-            else if (r != HV_ERR_UNSUPPORTED)
-                return r;
-        }
-        if (!done && inc)
-        {
-            r = dirty ? pca_covariance_blocks(p->ring, p->T, p->HW, p->cov, p->cov_work, dirty, st) : HV_OK;
             if (r == HV_OK)
                 done = true;
             else if (r != HV_ERR_UNSUPPORTED)

@@ -411,6 +411,14 @@ size_t pca_cov_workspace(int T, size_t npix)
     return COV_FLAGS + (simt > tc ? simt : tc);
 }
 
+size_t pca_cov_workspace_planes(int T, size_t npix)
+{
+    const CovPlan p = cov_plan(T, npix);
+    size_t simt = static_cast<size_t>(p.chunks) * p.ntiles * COV_TILE * COV_TILE * sizeof(float2);
+    size_t tc = cov_tc_supported(T) ? (2 * T > 128 ? cov_tc_partial_bytes(T, npix) : cov_tc_workspace(T, npix)) : 0;
+    return COV_FLAGS + (simt > tc ? simt : tc);
+}
+
 void set_cov_mode(int mode) { g_cov_mode = mode; }
 int cov_mode() { return g_cov_mode.load(); }
 
@@ -449,20 +457,6 @@ hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, v
     HV_LAUNCH_CHECK();
     count_launch(2);
     return HV_OK;
-}
-
-hv_status pca_covariance_blocks(const float2* ring, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
-                                cudaStream_t st)
-{
-    if (T <= 0 || npix == 0)
-        return HV_INVALID_VALUE;
-    const int mode = g_cov_mode.load();
-    if (mode == 1)
-        return HV_ERR_UNSUPPORTED;
-    int* err = static_cast<int*>(work);
-    char* ws = static_cast<char*>(work) + COV_FLAGS;
-    HV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
-    return cov_tc_blocks(ring, T, npix, cov, ws, err, blocks, st);
 }
 
 hv_status pca_covariance_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
@@ -1742,13 +1736,15 @@ constexpr int TS_ORTH_THREADS = 256;
 constexpr int TS_ORTH_RPT = 2;    // rows per thread of the orthonormalisation (T <= 512)
 constexpr int TS_MM_ROWS = 1;     // rows of C V per CTA
 constexpr int TS_MM_SPLIT = 16;   // warps per row (warp q sums the terms s = q mod 16)
-constexpr int TS_ITERS_COLD = 8, TS_ITERS_WARM = 2;
+constexpr int TS_ITERS_COLD = 8, TS_ITERS_WARM = 1;
 static_assert(TS_P == 32, "one lane per subspace vector");
 static_assert(TS_ORTH_THREADS * TS_ORTH_RPT >= JC_MAX_T, "the orthonormalisation holds every row in registers");
 
+// C32 (T x T), V, Y, Vw (T x TS_P each), then H and Q (TS_P x TS_P each) and the scale factor
 static size_t ts_bytes(int T)
 {
-    return static_cast<size_t>(T) * T * sizeof(float2) + 3 * static_cast<size_t>(T) * TS_P * sizeof(float2) + 512;
+    return static_cast<size_t>(T) * T * sizeof(float2) + 3 * static_cast<size_t>(T) * TS_P * sizeof(float2) +
+           2 * static_cast<size_t>(TS_P) * TS_P * sizeof(float2) + 512;
 }
 
 // C32 = 2^-e C (largest diagonal entry near 1); every CTA derives the factor from the diagonal, CTA
@@ -2004,75 +2000,71 @@ __global__ void __launch_bounds__(TS_ORTH_THREADS) k_ts_orth(const float2* __res
     }
 }
 
-// Rayleigh-Ritz: H = V^H Y (Y = C32 V), H Q = Q diag(theta) by FP32 Jacobi, Ritz vectors U = V Q in
-// ascending order: evecs columns T - TS_P .. T - 1 (FP64) and the warm start `Vw`, the Ritz values
-// (scaled back) into evals[T - TS_P ..], evals below set to 0. One CTA; V and Y pass through shared
-// memory in blocks of TS_P rows (coalesced loads), the sums over t run in row order.
-__global__ void __launch_bounds__(JS_THREADS) k_ts_rr(const float2* __restrict__ V, const float2* __restrict__ Y, int T,
-                                                     const double* __restrict__ scale, double2* __restrict__ evecs,
-                                                     double* __restrict__ evals, float2* __restrict__ Vw)
+// Rayleigh-Ritz in three launches. k_ts_gram: H = V^H Y (Y = C32 V), one CTA per row i of H, warp w
+// summing the rows t = w mod 8 in two chains, the warps added in warp order.
+constexpr int TS_GRAM_WARPS = 8;
+__global__ void __launch_bounds__(TS_GRAM_WARPS * 32) k_ts_gram(const float2* __restrict__ V,
+                                                               const float2* __restrict__ Y, int T,
+                                                               float2* __restrict__ H)
+{
+    __shared__ float2 part[TS_GRAM_WARPS][TS_P];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, i = blockIdx.x;
+    float r0 = 0.f, i0 = 0.f, r1 = 0.f, i1 = 0.f;
+    int t = warp;
+#pragma unroll 4
+    for (; t + TS_GRAM_WARPS < T; t += 2 * TS_GRAM_WARPS)
+    {
+        const float2 a0 = V[static_cast<size_t>(t) * TS_P + i], b0 = Y[static_cast<size_t>(t) * TS_P + lane];
+        const float2 a1 = V[static_cast<size_t>(t + TS_GRAM_WARPS) * TS_P + i];
+        const float2 b1 = Y[static_cast<size_t>(t + TS_GRAM_WARPS) * TS_P + lane];
+        r0 = fmaf(a0.x, b0.x, fmaf(a0.y, b0.y, r0));
+        i0 = fmaf(a0.x, b0.y, fmaf(-a0.y, b0.x, i0));
+        r1 = fmaf(a1.x, b1.x, fmaf(a1.y, b1.y, r1));
+        i1 = fmaf(a1.x, b1.y, fmaf(-a1.y, b1.x, i1));
+    }
+    if (t < T)
+    {
+        const float2 a0 = V[static_cast<size_t>(t) * TS_P + i], b0 = Y[static_cast<size_t>(t) * TS_P + lane];
+        r0 = fmaf(a0.x, b0.x, fmaf(a0.y, b0.y, r0));
+        i0 = fmaf(a0.x, b0.y, fmaf(-a0.y, b0.x, i0));
+    }
+    part[warp][lane] = make_float2(r0 + r1, i0 + i1);
+    __syncthreads();
+    if (warp == 0)
+    {
+        float2 h = part[0][lane];
+        for (int w = 1; w < TS_GRAM_WARPS; ++w)
+        {
+            h.x += part[w][lane].x;
+            h.y += part[w][lane].y;
+        }
+        H[i * TS_P + lane] = h;
+    }
+}
+
+// k_ts_rr: H Q = Q diag(theta) by FP32 Jacobi on the Hermitian part of H (one CTA); the Ritz values
+// (scaled back) into evals[T - TS_P ..] in ascending order, evals below set to 0, and Qo = the columns
+// of Q in that order.
+__global__ void __launch_bounds__(JS_THREADS) k_ts_rr(const float2* __restrict__ H, int T,
+                                                     const double* __restrict__ scale, double* __restrict__ evals,
+                                                     float2* __restrict__ Qo)
 {
     constexpr int NW = JS_THREADS / 32;
-    constexpr int HR = TS_P / NW;  // rows of H per warp
-    static_assert(TS_P % NW == 0 && HR % 2 == 0, "H rows split evenly over the warps, in pairs");
     __shared__ Cx<float> Hs[TS_P * TS_LD], Qs[TS_P * TS_LD];
     __shared__ JacScratch<float> sc;
     __shared__ int order[TS_P];
     __shared__ float s_fro[NW];
-    __shared__ __align__(16) float2 sv[TS_P][TS_P];
-    __shared__ __align__(16) float2 sy[TS_P][TS_P + 1];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // H[i][k], i = HR warp + m, k = lane
-    float2 h[HR];
-#pragma unroll
-    for (int m = 0; m < HR; ++m)
-        h[m] = make_float2(0.f, 0.f);
-    for (int t0 = 0; t0 < T; t0 += TS_P)
-    {
-        for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
-        {
-            const int r = e / TS_P, c = e % TS_P, t = t0 + r;
-            sv[r][c] = t < T ? V[static_cast<size_t>(t) * TS_P + c] : make_float2(0.f, 0.f);
-            sy[r][c] = t < T ? Y[static_cast<size_t>(t) * TS_P + c] : make_float2(0.f, 0.f);
-        }
-        __syncthreads();
-#pragma unroll 4
-        for (int r = 0; r < TS_P; ++r)
-        {
-            const float2 b = sy[r][lane];
-#pragma unroll
-            for (int m = 0; m < HR; m += 2)
-            {
-                const float4 a2 = *reinterpret_cast<const float4*>(&sv[r][HR * warp + m]);
-                h[m].x += a2.x * b.x + a2.y * b.y;
-                h[m].y += a2.x * b.y - a2.y * b.x;
-                h[m + 1].x += a2.z * b.x + a2.w * b.y;
-                h[m + 1].y += a2.z * b.y - a2.w * b.x;
-            }
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int m = 0; m < HR; ++m)
-    {
-        const int i = HR * warp + m;
-        Hs[i * TS_LD + lane] = {h[m].x, h[m].y};
-        Qs[i * TS_LD + lane] = {i == lane ? 1.f : 0.f, 0.f};
-    }
-    __syncthreads();
     // Hermitian part, real diagonal; round-off floor as in the other FP32 sweeps
     float f2 = 0.f;
     for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
     {
         const int i = e / TS_P, k = e % TS_P;
-        if (i <= k)
-        {
-            const Cx<float> a = Hs[i * TS_LD + k], b = Hs[k * TS_LD + i];
-            const Cx<float> hh = {0.5f * (a.x + b.x), i == k ? 0.f : 0.5f * (a.y - b.y)};
-            Hs[i * TS_LD + k] = hh;
-            Hs[k * TS_LD + i] = {hh.x, -hh.y};
-            f2 += (i == k ? 1.f : 2.f) * (hh.x * hh.x + hh.y * hh.y);
-        }
+        const float2 a = H[i * TS_P + k], b = H[k * TS_P + i];
+        const Cx<float> hh = {0.5f * (a.x + b.x), i == k ? 0.f : 0.5f * (a.y - b.y)};
+        Hs[i * TS_LD + k] = hh;
+        Qs[i * TS_LD + k] = {i == k ? 1.f : 0.f, 0.f};
+        f2 += hh.x * hh.x + hh.y * hh.y;
     }
     for (int o = 16; o > 0; o >>= 1)
         f2 += __shfl_xor_sync(0xffffffffu, f2, o);
@@ -2099,48 +2091,52 @@ __global__ void __launch_bounds__(JS_THREADS) k_ts_rr(const float2* __restrict__
     for (int i = tid; i < T - TS_P; i += JS_THREADS)
         evals[i] = 0.0;
     __syncthreads();
-    // U = V Q in rank order: lane r holds column order[r] of Q
-    float2 q[TS_P];
+    for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
     {
-        const int qc = order[lane];
+        const int k = e / TS_P, r = e % TS_P;
+        const Cx<float> q = Qs[k * TS_LD + order[r]];
+        Qo[e] = make_float2(q.x, q.y);
+    }
+}
+
+// k_ts_ritz: the Ritz vectors U = V Qo, TS_P rows of U per CTA (warp w: rows w, w + 8, ..., lane =
+// column r): into the warm start Vw (row-major) and evecs columns T - TS_P + r (FP64, through a
+// shared-memory transpose so that each eigenvector's rows are written contiguously)
+__global__ void __launch_bounds__(256) k_ts_ritz(const float2* __restrict__ V, const float2* __restrict__ Qo, int T,
+                                                 double2* __restrict__ evecs, float2* __restrict__ Vw)
+{
+    __shared__ float2 q[TS_P][TS_P];
+    __shared__ float2 u[TS_P][TS_P + 1];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int t0 = blockIdx.x * TS_P;
+    for (int e = tid; e < TS_P * TS_P; e += 256)
+        q[e / TS_P][e % TS_P] = Qo[e];
+    __syncthreads();
+    for (int rr = warp; rr < TS_P; rr += 8)
+    {
+        const int t = t0 + rr;
+        if (t >= T)
+            break;
+        const float2 v = V[static_cast<size_t>(t) * TS_P + lane];
+        float re = 0.f, im = 0.f;
 #pragma unroll
         for (int k = 0; k < TS_P; ++k)
-            q[k] = make_float2(Qs[k * TS_LD + qc].x, Qs[k * TS_LD + qc].y);
-    }
-    for (int t0 = 0; t0 < T; t0 += TS_P)
-    {
-        for (int e = tid; e < TS_P * TS_P; e += JS_THREADS)
         {
-            const int r = e / TS_P, c = e % TS_P, t = t0 + r;
-            sv[r][c] = t < T ? V[static_cast<size_t>(t) * TS_P + c] : make_float2(0.f, 0.f);
+            const float vx = __shfl_sync(0xffffffffu, v.x, k), vy = __shfl_sync(0xffffffffu, v.y, k);
+            const float2 qq = q[k][lane];
+            re += vx * qq.x - vy * qq.y;
+            im += vx * qq.y + vy * qq.x;
         }
-        __syncthreads();
-        for (int rr = warp; rr < TS_P; rr += NW)
-        {
-            float re = 0.f, im = 0.f;
-#pragma unroll
-            for (int k = 0; k < TS_P; k += 2)
-            {
-                const float4 v2 = *reinterpret_cast<const float4*>(&sv[rr][k]);
-                re += v2.x * q[k].x - v2.y * q[k].y;
-                im += v2.x * q[k].y + v2.y * q[k].x;
-                re += v2.z * q[k + 1].x - v2.w * q[k + 1].y;
-                im += v2.z * q[k + 1].y + v2.w * q[k + 1].x;
-            }
-            sy[rr][lane] = make_float2(re, im);
-            if (t0 + rr < T)
-                Vw[static_cast<size_t>(t0 + rr) * TS_P + lane] = make_float2(re, im);
-        }
-        __syncthreads();
-        // the eigenvector columns are contiguous over t: lane = row of the block
-        if (t0 + lane < T)
-            for (int r = warp; r < TS_P; r += NW)
-            {
-                const float2 u = sy[lane][r];
-                evecs[static_cast<size_t>(T - TS_P + r) * T + t0 + lane] = make_double2(u.x, u.y);
-            }
-        __syncthreads();
+        u[rr][lane] = make_float2(re, im);
+        Vw[static_cast<size_t>(t) * TS_P + lane] = make_float2(re, im);
     }
+    __syncthreads();
+    if (t0 + lane < T)
+        for (int r = warp; r < TS_P; r += 8)
+        {
+            const float2 x = u[lane][r];
+            evecs[static_cast<size_t>(T - TS_P + r) * T + t0 + lane] = make_double2(x.x, x.y);
+        }
 }
 
 static std::atomic<int> g_eig_precision{HV_EIG_FP32};
@@ -2233,7 +2229,9 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         float2* Vs = C32 + static_cast<size_t>(T) * T;
         float2* Ys = Vs + static_cast<size_t>(T) * TS_P;
         float2* Vw = Ys + static_cast<size_t>(T) * TS_P;
-        double* scale = reinterpret_cast<double*>(Vw + static_cast<size_t>(T) * TS_P);
+        float2* Hm = Vw + static_cast<size_t>(T) * TS_P;
+        float2* Qo = Hm + TS_P * TS_P;
+        double* scale = reinterpret_cast<double*>(Qo + TS_P * TS_P);
         const int gb = (T * TS_P + 255) / 256;
         const int gm = (T + TS_MM_ROWS - 1) / TS_MM_ROWS;
         constexpr int mm_threads = TS_MM_ROWS * TS_MM_SPLIT * 32;
@@ -2258,11 +2256,15 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         }
         k_ts_matmul<<<gm, mm_threads, 0, st>>>(C32, Vs, T, Ys);
         HV_LAUNCH_CHECK();
-        k_ts_rr<<<1, JS_THREADS, 0, st>>>(Vs, Ys, T, scale, evecs, evals, Vw);
+        k_ts_gram<<<TS_P, TS_GRAM_WARPS * 32, 0, st>>>(Vs, Ys, T, Hm);
         HV_LAUNCH_CHECK();
-        count_launch(3 + 2 * iters + (warm ? 0 : 2));
-        // two corrections: on the benchmark's sliding windows (T = 512, stride 64) one warm iteration
-        // and two corrections already reach the view error of three and three (3.5e-7 .. 1.9e-6)
+        k_ts_rr<<<1, JS_THREADS, 0, st>>>(Hm, T, scale, evals, Qo);
+        HV_LAUNCH_CHECK();
+        k_ts_ritz<<<(T + TS_P - 1) / TS_P, 256, 0, st>>>(Vs, Qo, T, evecs, Vw);
+        HV_LAUNCH_CHECK();
+        count_launch(5 + 2 * iters + (warm ? 0 : 2));
+        // two corrections: on 512 x 512 frames with T = 512 and stride 64, one warm iteration and two
+        // corrections reach the view error of three and three (3.5e-7 .. 1.9e-6 from FP64)
         return refine_kept(T - TS_P, 2);
     }
     if (T <= JS_MAX_T && prec == HV_EIG_FP32)

@@ -383,7 +383,8 @@ hv_status hv_stft_weights(void* weights_c64, int T, int pmin, int pmax, void* st
 
 /* PCA: covariance C = H^H H of the ring (H = HW x T column-major view), FP32 accumulation,
  * written as complex128 T x T (both triangles). Replaces cov_matrix (matrix_operations.cc:9-26).
- * `work` must hold hv_pca_cov_workspace(T, W*H) bytes. */
+ * `work` must hold hv_pca_cov_workspace(T, W*H) bytes (for the tensor-core engine at 64 < T: the
+ * split-BF16 planes of the ring, 8 T npix bytes, and the partial tiles). */
 hv_status hv_pca_covariance(const void* ring_c64, int T, size_t npix, void* cov_c128, void* work, void* stream);
 size_t hv_pca_cov_workspace(int T, size_t npix);
 /* Covariance engine: 0 = automatic (tcgen05 split-BF16 tensor cores for T <= 1024 and frames of a
@@ -403,7 +404,9 @@ hv_status hv_pca_covariance_status(const void* work);
  * imaginary part of pixel px of ring slot s. hv_pca_planes_bytes: their size (8 T npix bytes; 0 when
  * the shape has none). hv_pca_split_planes: planes of ring slots slot0 .. slot0 + n - 1 (mod T), as
  * a Pipe writes them when frames enter its ring. hv_pca_covariance_planes: the covariance from the
- * planes, bit-identical to hv_pca_covariance's tensor-core engine on the ring; `blocks` = ~0u for
+ * planes (the engine hv_pca_covariance runs on planes it splits into `work`; `work` here needs only
+ * the partial tiles, hv_pca_cov_workspace(T, npix) - hv_pca_planes_bytes(T, npix) bytes at least),
+ * bit-identical to hv_pca_covariance's tensor-core engine on the ring; `blocks` = ~0u for
  * all of it, else only the rows and columns of the 64-frame slot blocks set (bit b: slots 64 b ..
  * 64 b + 63), the other entries of `cov_c128` left as they are. HV_ERR_UNSUPPORTED for the SIMT
  * engine mode and shapes without planes. */

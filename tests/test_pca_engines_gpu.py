@@ -50,11 +50,11 @@ def test_covariance_engine(cuda, mode, tol, T, npix):
 @pytest.mark.gpu
 @pytest.mark.parametrize("T,npix", [(65, 1000), (128, 65536), (200, 4104), (512, 16384)])
 def test_covariance_planes_bit_identical(cuda, T, npix):
-    """The tiled tensor-core covariance from the split-BF16 planes (hv_pca_split_planes, then
-    hv_pca_covariance_planes: tensor copies straight into the MMA operand layout) is bit-identical to
-    the same engine converting the ring itself; after a wrapping range of ring slots is rewritten and
-    only those slots re-split, the update of the rows and columns of their 64-frame blocks equals the
-    full recomputation bit for bit."""
+    """The tiled tensor-core covariance from split-BF16 planes the caller keeps (hv_pca_split_planes,
+    then hv_pca_covariance_planes: tensor copies straight into the MMA operand layout) is
+    bit-identical to hv_pca_covariance on the ring (which splits it into its workspace); after a
+    wrapping range of ring slots is rewritten and only those slots re-split, the update of the rows
+    and columns of their 64-frame blocks equals the full recomputation bit for bit."""
     L = hv.lib()
     ring = _ring(T, npix, T + 7)
     rd = dev(ring)
