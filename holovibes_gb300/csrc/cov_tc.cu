@@ -337,8 +337,7 @@ int sm_count();
 // G (2T x 2T) in 128 x 128 tiles (bm, bn), bm <= bn: operand A = Y rows of frames 64 bm .. 64 bm + 63,
 // B = frames 64 bn .. (the same as A on diagonal tiles; frames >= T are zero-filled by the tensor
 // copy), from the split-BF16 planes of the ring (below). CTA (split ks, tile tp) walks the 64-pixel
-// chunks of split ks (TT_SPLIT_CHUNKS chunks, whatever the number of tiles, so that an entry's sums
-// do not depend on which tiles a launch computes); the MMA warp issues Ah Bh^T, Ah Bl^T, Al Bh^T
+// chunks of split ks (tiled_plan); the MMA warp issues Ah Bh^T, Ah Bl^T, Al Bh^T
 // (M = N = 128, K = 16) into three TMEM accumulators in chains of at most kMaxChainChunks chunks,
 // whose sums the epilogue warps add in FP32 registers. The CTAs of one split stream the same
 // chunks at about the same time, so each chunk comes from HBM about once and the other tiles read
@@ -355,8 +354,6 @@ constexpr int TT_FRAMES = 64;                          // frames per operand til
 // where its extra waves cost more time than the drift costs accuracy.
 constexpr size_t kMaxChainChunks = 64;
 constexpr size_t kMaxChainChunksPacked = 128;
-constexpr size_t TT_SPLIT_CHUNKS = 4 * kMaxChainChunks;  // chunks per split of the tiled kernel
-
 constexpr int TT_MAX_BLOCKS = COV_TC_MAX_T / TT_FRAMES;  // 64-frame blocks of a ring (16)
 constexpr int TT_MAX_PAIRS = TT_MAX_BLOCKS * (TT_MAX_BLOCKS + 1) / 2;
 
@@ -478,7 +475,8 @@ constexpr uint32_t TP_STAGE_BYTES = 4 * TILE_BYTES;  // Ah, Al, Bh, Bl
 // part: [gridDim.x][128][128] FP32 partial tiles (CTA index = ks * tiles.n + tp)
 __global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_tiled(const __grid_constant__ CUtensorMap planes_map,
                                                                 size_t npix, const __grid_constant__ TileList tiles_in,
-                                                                float* __restrict__ part, int* __restrict__ err)
+                                                                size_t chunks_per_split, float* __restrict__ part,
+                                                                int* __restrict__ err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* stages = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
@@ -493,8 +491,8 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_cov_tc_tiled(const __grid_con
     const int bm = tiles_in.bm[tp], bn = tiles_in.bn[tp];
     const bool diag = bm == bn;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    const size_t c_begin = static_cast<size_t>(ks) * TT_SPLIT_CHUNKS;
-    size_t c_end = c_begin + TT_SPLIT_CHUNKS;
+    const size_t c_begin = static_cast<size_t>(ks) * chunks_per_split;
+    size_t c_end = c_begin + chunks_per_split;
     if (c_end > nchunks)
         c_end = nchunks;
     const int nmine = static_cast<int>(c_end > c_begin ? c_end - c_begin : 0);
@@ -668,14 +666,24 @@ struct TiledPlan
 };
 
 
+// The pixel splits depend on (T, npix) only, never on which tiles a launch computes, so that a
+// recomputed entry equals the full computation's bit for bit. Their count fills one wave for the
+// tiles of one 64-frame block (nb tiles: the update after one stride of <= 64 frames), with at
+// least kMaxChainChunks chunks per split.
 TiledPlan tiled_plan(int T, size_t npix)
 {
     TiledPlan p;
     p.nb = (T + TT_FRAMES - 1) / TT_FRAMES;
     p.npairs = p.nb * (p.nb + 1) / 2;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
-    p.chunks_per_split = TT_SPLIT_CHUNKS;
-    p.nsplit = static_cast<int>((nchunks + TT_SPLIT_CHUNKS - 1) / TT_SPLIT_CHUNKS);
+    size_t ns = static_cast<size_t>(sm_count() / p.nb);
+    const size_t max_ns = (nchunks + kMaxChainChunks - 1) / kMaxChainChunks;
+    if (ns > max_ns)
+        ns = max_ns;
+    if (ns < 1)
+        ns = 1;
+    p.chunks_per_split = (nchunks + ns - 1) / ns;
+    p.nsplit = static_cast<int>((nchunks + p.chunks_per_split - 1) / p.chunks_per_split);
     return p;
 }
 
@@ -807,7 +815,7 @@ hv_status cov_tc_planes(const uint16_t* planes, int T, size_t npix, double2* cov
                                                          static_cast<int>(smem));
     HV_CUDA_TRY(attr);
     float* tpart = static_cast<float*>(work);
-    k_cov_tc_tiled<<<q.nsplit * tl.n, TP_THREADS, smem, st>>>(tmap, npix, tl, tpart, err);
+    k_cov_tc_tiled<<<q.nsplit * tl.n, TP_THREADS, smem, st>>>(tmap, npix, tl, q.chunks_per_split, tpart, err);
     HV_LAUNCH_CHECK();
     k_cov_tc_tiled_reduce<<<(T * T + TR_ENTRIES - 1) / TR_ENTRIES, TR_ENTRIES * TR_GROUPS, 0, st>>>(tpart, T, tl,
                                                                                                   q.nsplit, cov);

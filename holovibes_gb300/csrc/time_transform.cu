@@ -141,6 +141,117 @@ __global__ void __launch_bounds__(TV_THREADS) k_time_view(const float2* __restri
     }
 }
 
+// Two adjacent pixels per thread (16-byte ring loads: 512 contiguous bytes per warp and frame;
+// HW even). 128 threads cover 256 pixels and write the two 128-pixel renormalisation partials of
+// their CTA, the same partials as k_time_view.
+template <int KC>
+__global__ void __launch_bounds__(TV_THREADS) k_time_view2(const float2* __restrict__ ring, int T, int W, int H,
+                                                            const float2* __restrict__ weights, int K, int img_type,
+                                                            float scale, int shift, float* __restrict__ out,
+                                                            double* __restrict__ partials, int npartials,
+                                                            const CycleCtl* ctl, const float* __restrict__ bin_w)
+{
+    if (!ctl_render(ctl))
+        return;
+    extern __shared__ __align__(16) float2 wsm[];  // [T][KC]
+    __shared__ double red[TV_THREADS / 32];
+    const size_t HW = static_cast<size_t>(W) * H;
+    const size_t pix0 = 2 * (blockIdx.x * static_cast<size_t>(TV_THREADS) + threadIdx.x);
+    const bool valid = pix0 < HW;
+    float view0 = 0.f, view1 = 0.f;
+    for (int k0 = 0; k0 < K; k0 += KC)
+    {
+        __syncthreads();
+        for (int e = threadIdx.x; e < T * KC; e += TV_THREADS)
+        {
+            const int t = e / KC, kk = e - t * KC;
+            const int k = k0 + kk;
+            wsm[e] = (k < K) ? weights[static_cast<size_t>(k) * T + t] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        float2 a0[KC], a1[KC];
+#pragma unroll
+        for (int kk = 0; kk < KC; ++kk)
+            a0[kk] = a1[kk] = make_float2(0.f, 0.f);
+        if (valid)
+        {
+            const float4* src = reinterpret_cast<const float4*>(ring + pix0);
+            const size_t step = HW / 2;
+#pragma unroll 8
+            for (int t = 0; t < T; ++t)
+            {
+                const float4 x = __ldg(src + static_cast<size_t>(t) * step);
+                const float2* wt = wsm + t * KC;
+#pragma unroll
+                for (int kk = 0; kk < KC; ++kk)
+                {
+                    const float2 w = wt[kk];
+                    a0[kk].x = fmaf(x.x, w.x, fmaf(-x.y, w.y, a0[kk].x));
+                    a0[kk].y = fmaf(x.x, w.y, fmaf(x.y, w.x, a0[kk].y));
+                    a1[kk].x = fmaf(x.z, w.x, fmaf(-x.w, w.y, a1[kk].x));
+                    a1[kk].y = fmaf(x.z, w.y, fmaf(x.w, w.x, a1[kk].y));
+                }
+            }
+            const int kn = (K - k0) < KC ? (K - k0) : KC;
+#pragma unroll
+            for (int kk = 0; kk < KC; ++kk)
+                if (kk < kn)
+                {
+                    if (bin_w)
+                    {
+                        const float bw = __ldg(bin_w + k0 + kk);
+                        view0 += (a0[kk].x * a0[kk].x + a0[kk].y * a0[kk].y) * bw;
+                        view1 += (a1[kk].x * a1[kk].x + a1[kk].y * a1[kk].y) * bw;
+                    }
+                    else
+                    {
+                        view0 += view_value(a0[kk], img_type);
+                        view1 += view_value(a1[kk], img_type);
+                    }
+                }
+        }
+    }
+    float v0 = 0.f, v1 = 0.f;
+    if (valid)
+    {
+        v0 = bin_w ? view0 : view0 / static_cast<float>(K);
+        v1 = bin_w ? view1 : view1 / static_cast<float>(K);
+        if (scale != 1.0f)
+        {
+            v0 = v0 * scale;
+            v1 = v1 * scale;
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+        {
+            const size_t pix = pix0 + q;
+            const int x = static_cast<int>(pix % W);
+            const int y = static_cast<int>(pix / W);
+            size_t dst = pix;
+            if (shift)
+                dst = static_cast<size_t>((y + H / 2) % H) * W + (x + W / 2) % W;
+            out[dst] = q ? v1 : v0;
+        }
+    }
+    if (partials)
+    {
+        double d = valid ? static_cast<double>(v0) + static_cast<double>(v1) : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            d += __shfl_down_sync(0xffffffffu, d, o);
+        if ((threadIdx.x & 31) == 0)
+            red[threadIdx.x >> 5] = d;
+        __syncthreads();
+        // warps 0-1: pixels 0..127 of the CTA, warps 2-3: 128..255
+        if (threadIdx.x < 2)
+        {
+            const int pi = 2 * blockIdx.x + threadIdx.x;
+            if (pi < npartials)
+                partials[pi] = red[2 * threadIdx.x] + red[2 * threadIdx.x + 1];
+        }
+    }
+}
+
 int time_view_partials(int W, int H)
 {
     const size_t HW = static_cast<size_t>(W) * H;
@@ -161,7 +272,21 @@ static hv_status launch_time_view(const float2* ring, int T, int W, int H, const
     if (smem > 48 * 1024)
         HV_CUDA_TRY(cudaFuncSetAttribute(k_time_view<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem)));
-    const int grid = time_view_partials(W, H);
+    const int np = time_view_partials(W, H);
+    const size_t HW = static_cast<size_t>(W) * H;
+    if (KC <= 4 && HW % 2 == 0)
+    {
+        if (smem > 48 * 1024)
+            HV_CUDA_TRY(cudaFuncSetAttribute(k_time_view2<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem)));
+        const int grid2 = static_cast<int>((HW + 2 * TV_THREADS - 1) / (2 * TV_THREADS));
+        k_time_view2<KC><<<grid2, TV_THREADS, smem, st>>>(ring, T, W, H, weights, K, img_type, scale, shift, out,
+                                                          partials, np, ctl, bin_w);
+        HV_LAUNCH_CHECK();
+        count_launch();
+        return HV_OK;
+    }
+    const int grid = np;
     k_time_view<KC><<<grid, TV_THREADS, smem, st>>>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials,
                                                     ctl, bin_w);
     HV_LAUNCH_CHECK();
