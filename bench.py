@@ -499,25 +499,32 @@ def steps_for(hv, fd, s, dev_batch, stream):
                     T * HW * 8 + HW * 4, 0))
     if s.time_transformation == hv.TIME_PCA:
         cov, cw = buf(T * T * 16), buf(L.hv_pca_cov_workspace(T, HW))
-        pb = L.hv_pca_planes_bytes(T, HW)
+        real = 1 if s.space_transformation == hv.SPACE_NONE and not s.filter2d_enabled else 0
+        pb = L.hv_pca_planes_bytes(T, HW, real)
         S = s.time_stride
         if pb and S < T:
-            # the pipe's path for T > 64: each window's S new frames are split into BF16 planes, and
-            # the covariance rows and columns of the 64-frame slot blocks they land in (one window:
-            # slots 0 .. S-1) are recomputed from the planes: every frame of the ring is read once,
-            # the tiles touching those blocks are multiplied
+            # the pipe's path for T > 64: each window's S new frames are split into BF16 planes (real
+            # parts only for a real ring), and the covariance rows and columns of the slot blocks they
+            # land in (64 frames, 128 for real planes; one window: slots 0 .. S-1) are recomputed from
+            # the planes: every frame of the ring is read once, the tiles touching those blocks are
+            # multiplied
+            if real:
+                # the pipe's ring without a spatial transform: imaginary parts 0
+                ring.view(torch.float32).view(-1, 2)[:, 1].zero_()
             planes = buf(pb)
-            hv.check(L.hv_pca_split_planes(ring.data_ptr(), T, HW, 0, T, planes.data_ptr(), stream), "split")
-            nb = (T + 63) // 64
+            hv.check(L.hv_pca_split_planes(ring.data_ptr(), T, HW, 0, T, real, planes.data_ptr(), stream), "split")
+            fb = 128 if real else 64
+            nb = (T + fb - 1) // fb
             blocks = 0
             for sl in range(S):
-                blocks |= 1 << (sl // 64)
+                blocks |= 1 << (sl // fb)
             tiles = sum(1 for bm in range(nb) for bn in range(bm, nb) if (blocks >> bm) & 1 or (blocks >> bn) & 1)
-            out.append(("ring_split", lambda: L.hv_pca_split_planes(ring.data_ptr(), T, HW, 0, S, planes.data_ptr(),
-                                                                    stream), S * HW * 16, 0))
-            out.append(("pca_covariance", lambda: L.hv_pca_covariance_planes(planes.data_ptr(), T, HW, blocks,
+            out.append(("ring_split", lambda: L.hv_pca_split_planes(ring.data_ptr(), T, HW, 0, S, real,
+                                                                    planes.data_ptr(), stream),
+                        S * HW * (12 if real else 16), 0))
+            out.append(("pca_covariance", lambda: L.hv_pca_covariance_planes(planes.data_ptr(), T, HW, real, blocks,
                                                                              cov.data_ptr(), cw.data_ptr(), stream),
-                        T * HW * 8, tiles * 3 * 2 * 128 * 128 * HW))
+                        T * HW * (4 if real else 8), tiles * 3 * 2 * 128 * 128 * HW))
         else:
             # tensor flops: the 128 x 128 tiles of the 2T x 2T real Gram matrix on or above its
             # diagonal, three BF16 products each (T <= 32: one packed 128 x 128 product)

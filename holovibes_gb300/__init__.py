@@ -259,9 +259,9 @@ def _declare(L: C.CDLL) -> None:
         "hv_pca_cov_workspace": (sz, [i32, sz]),
         "hv_pca_covariance_mode": (None, [i32]),
         "hv_pca_cov_incremental": (None, [i32]),
-        "hv_pca_planes_bytes": (sz, [i32, sz]),
-        "hv_pca_split_planes": (st, [vp, i32, sz, i32, i32, vp, vp]),
-        "hv_pca_covariance_planes": (st, [vp, i32, sz, u32, vp, vp, vp]),
+        "hv_pca_planes_bytes": (sz, [i32, sz, i32]),
+        "hv_pca_split_planes": (st, [vp, i32, sz, i32, i32, i32, vp, vp]),
+        "hv_pca_covariance_planes": (st, [vp, i32, sz, i32, u32, vp, vp, vp]),
         "hv_pca_covariance_status": (st, [vp]),
         "hv_pca_eigh": (st, [vp, i32, vp, vp, i32, i32, vp, vp, vp]),
         "hv_pca_eigh_workspace": (sz, [i32]),

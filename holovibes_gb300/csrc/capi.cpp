@@ -299,23 +299,27 @@ void hv_pca_covariance_mode(int mode) { set_cov_mode(mode); }
 
 void hv_pca_cov_incremental(int enable) { set_cov_incremental(enable != 0); }
 
-size_t hv_pca_planes_bytes(int T, size_t npix) { return cov_planes_supported(T, npix) ? cov_planes_bytes(T, npix) : 0; }
+size_t hv_pca_planes_bytes(int T, size_t npix, int real)
+{
+    return cov_planes_supported(T, npix) ? cov_planes_bytes(T, npix, real ? 1 : 0) : 0;
+}
 
-hv_status hv_pca_split_planes(const void* ring_c64, int T, size_t npix, int slot0, int n, void* planes, void* stream)
+hv_status hv_pca_split_planes(const void* ring_c64, int T, size_t npix, int slot0, int n, int real, void* planes,
+                              void* stream)
 {
     if (!ring_c64 || !planes)
         return HV_INVALID_VALUE;
     return cov_split_planes(static_cast<const float2*>(ring_c64), T, npix, slot0, n, static_cast<uint16_t*>(planes),
-                            S(stream));
+                            real ? 1 : 0, S(stream));
 }
 
-hv_status hv_pca_covariance_planes(const void* planes, int T, size_t npix, unsigned int blocks, void* cov_c128,
-                                   void* work, void* stream)
+hv_status hv_pca_covariance_planes(const void* planes, int T, size_t npix, int real, unsigned int blocks,
+                                   void* cov_c128, void* work, void* stream)
 {
     if (!planes || !cov_c128 || !work)
         return HV_INVALID_VALUE;
     return pca_covariance_planes(static_cast<const uint16_t*>(planes), T, npix, static_cast<double2*>(cov_c128), work,
-                                 blocks, S(stream));
+                                 blocks, real ? 1 : 0, S(stream));
 }
 
 hv_status hv_pca_covariance_status(const void* work)

@@ -375,7 +375,8 @@ struct TileList
 constexpr int TR_ENTRIES = 64, TR_GROUPS = 4;
 __global__ void __launch_bounds__(TR_ENTRIES * TR_GROUPS) k_cov_tc_tiled_reduce(const float* __restrict__ part, int T,
                                                                                const __grid_constant__ TileList tiles,
-                                                                               int nsplit, double2* __restrict__ cov)
+                                                                               int nsplit, int real,
+                                                                               double2* __restrict__ cov)
 {
     __shared__ double red[TR_GROUPS - 1][4][TR_ENTRIES];
     const int q = threadIdx.x / TR_ENTRIES, el = threadIdx.x % TR_ENTRIES;
@@ -388,9 +389,11 @@ __global__ void __launch_bounds__(TR_ENTRIES * TR_GROUPS) k_cov_tc_tiled_reduce(
         mirror = ei > ej;
         diag = ei == ej;
         const int i = mirror ? ej : ei, j = mirror ? ei : ej;
-        tp = tiles.index[i / TT_FRAMES][j / TT_FRAMES];
-        ri = 2 * (i % TT_FRAMES);
-        cj = 2 * (j % TT_FRAMES);
+        // complex planes: 64 frames (128 rows: Re, Im) per block; real planes: 128 frames
+        const int fb = real ? TC_ROWS : TT_FRAMES;
+        tp = tiles.index[i / fb][j / fb];
+        ri = real ? i % fb : 2 * (i % fb);
+        cj = real ? j % fb : 2 * (j % fb);
     }
     double g00 = 0, g11 = 0, g01 = 0, g10 = 0;
     if (tp >= 0)
@@ -400,9 +403,12 @@ __global__ void __launch_bounds__(TR_ENTRIES * TR_GROUPS) k_cov_tc_tiled_reduce(
         {
             const float* G = part + (static_cast<size_t>(k) * npairs + tp) * TC_ROWS * TC_ROWS;
             g00 += G[ri * TC_ROWS + cj];
-            g11 += G[(ri + 1) * TC_ROWS + cj + 1];
-            g01 += G[ri * TC_ROWS + cj + 1];
-            g10 += G[(ri + 1) * TC_ROWS + cj];
+            if (!real)
+            {
+                g11 += G[(ri + 1) * TC_ROWS + cj + 1];
+                g01 += G[ri * TC_ROWS + cj + 1];
+                g10 += G[(ri + 1) * TC_ROWS + cj];
+            }
         }
     }
     if (q > 0)
@@ -431,15 +437,17 @@ __global__ void __launch_bounds__(TR_ENTRIES * TR_GROUPS) k_cov_tc_tiled_reduce(
 // imaginary part of pixel px of ring slot s), written once per frame when it enters the ring. The
 // tiled covariance streams the four operand tiles of a chunk (Ah, Al, Bh, Bl: 128 rows x 64 pixels
 // each) from them by 3-D tensor copies straight into the swizzled K-major layout the MMAs read, so
-// that a chunk is split once instead of once per tile it takes part in.
+// that a chunk is split once instead of once per tile it takes part in. A real ring (no spatial
+// transform: imaginary parts exactly 0) keeps the real rows only (planes[p][s][px]): half the bytes,
+// and C = Re Re^T from tiles of 128 frames, a quarter of the products.
 
 // Thread: 8 consecutive pixels of one frame of slots slot0 .. slot0 + n - 1 (mod T).
-__global__ void k_ring_split(const float2* __restrict__ ring, int T, size_t npix, int slot0, int n,
+__global__ void k_ring_split(const float2* __restrict__ ring, int T, size_t npix, int slot0, int n, int real,
                              uint16_t* __restrict__ planes)
 {
     const size_t groups = npix / 8;
     const size_t total = static_cast<size_t>(n) * groups;
-    const size_t plane = 2 * static_cast<size_t>(T) * npix;
+    const size_t plane = (real ? 1 : 2) * static_cast<size_t>(T) * npix;
     for (size_t e = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
          e += static_cast<size_t>(gridDim.x) * blockDim.x)
     {
@@ -457,11 +465,14 @@ __global__ void k_ring_split(const float2* __restrict__ ring, int T, size_t npix
         tc::split2(b.y, b.w, ih.y, il.y);
         tc::split2(c.y, c.w, ih.z, il.z);
         tc::split2(d.y, d.w, ih.w, il.w);
-        uint16_t* re = planes + 2 * slot * npix + 8 * g;
+        uint16_t* re = planes + (real ? 1 : 2) * slot * npix + 8 * g;
         *reinterpret_cast<uint4*>(re) = rh;
-        *reinterpret_cast<uint4*>(re + npix) = ih;
         *reinterpret_cast<uint4*>(re + plane) = rl;
-        *reinterpret_cast<uint4*>(re + plane + npix) = il;
+        if (!real)
+        {
+            *reinterpret_cast<uint4*>(re + npix) = ih;
+            *reinterpret_cast<uint4*>(re + plane + npix) = il;
+        }
     }
 }
 
@@ -668,12 +679,12 @@ struct TiledPlan
 
 // The pixel splits depend on (T, npix) only, never on which tiles a launch computes, so that a
 // recomputed entry equals the full computation's bit for bit. Their count fills one wave for the
-// tiles of one 64-frame block (nb tiles: the update after one stride of <= 64 frames), with at
-// least kMaxChainChunks chunks per split.
-TiledPlan tiled_plan(int T, size_t npix)
+// tiles of one block (nb tiles: the update after one stride of <= 64 frames), with at least
+// kMaxChainChunks chunks per split. Blocks: 64 frames (complex planes), 128 frames (real planes).
+TiledPlan tiled_plan(int T, size_t npix, int real = 0)
 {
     TiledPlan p;
-    p.nb = (T + TT_FRAMES - 1) / TT_FRAMES;
+    p.nb = real ? (T + TC_ROWS - 1) / TC_ROWS : (T + TT_FRAMES - 1) / TT_FRAMES;
     p.npairs = p.nb * (p.nb + 1) / 2;
     const size_t nchunks = (npix + TC_KC - 1) / TC_KC;
     size_t ns = static_cast<size_t>(sm_count() / p.nb);
@@ -751,13 +762,13 @@ static size_t tiled_part_bytes(int T, size_t npix)
 size_t cov_tc_workspace(int T, size_t npix)
 {
     if (2 * T > TC_ROWS)
-        return tiled_part_bytes(T, npix) + cov_planes_bytes(T, npix) + 256;
+        return tiled_part_bytes(T, npix) + cov_planes_bytes(T, npix, 0) + 256;
     const TcPlan p = tc_plan(T, npix);
     const size_t per = p.packed ? static_cast<size_t>(TC_ROWS) * 64 : static_cast<size_t>(4) * T * T;
     return static_cast<size_t>(p.ctas) * per * sizeof(float) + 256;
 }
 
-size_t cov_planes_bytes(int T, size_t npix) { return 8 * static_cast<size_t>(T) * npix; }
+size_t cov_planes_bytes(int T, size_t npix, int real) { return (real ? 4 : 8) * static_cast<size_t>(T) * npix; }
 
 size_t cov_tc_partial_bytes(int T, size_t npix) { return 2 * T > TC_ROWS ? tiled_part_bytes(T, npix) + 256 : 0; }
 
@@ -766,7 +777,8 @@ bool cov_planes_supported(int T, size_t npix)
     return cov_tc_supported(T) && 2 * T > TC_ROWS && npix > 0 && npix % 8 == 0 && npix <= (1ull << 29);
 }
 
-hv_status cov_split_planes(const float2* ring, int T, size_t npix, int slot0, int n, uint16_t* planes, cudaStream_t st)
+hv_status cov_split_planes(const float2* ring, int T, size_t npix, int slot0, int n, uint16_t* planes, int real,
+                           cudaStream_t st)
 {
     if (!cov_planes_supported(T, npix) || (reinterpret_cast<uintptr_t>(ring) & 15) != 0 ||
         (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
@@ -778,18 +790,18 @@ hv_status cov_split_planes(const float2* ring, int T, size_t npix, int slot0, in
     const size_t total = static_cast<size_t>(n) * (npix / 8);
     const size_t cap = static_cast<size_t>(sm_count()) * 8;
     const int grid = static_cast<int>(std::min((total + 255) / 256, cap));
-    k_ring_split<<<grid, 256, 0, st>>>(ring, T, npix, slot0, n, planes);
+    k_ring_split<<<grid, 256, 0, st>>>(ring, T, npix, slot0, n, real ? 1 : 0, planes);
     HV_LAUNCH_CHECK();
     count_launch();
     return HV_OK;
 }
 
 hv_status cov_tc_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, int* err,
-                        uint32_t blocks, cudaStream_t st)
+                        uint32_t blocks, int real, cudaStream_t st)
 {
     if (!cov_planes_supported(T, npix) || (reinterpret_cast<uintptr_t>(planes) & 15) != 0)
         return HV_ERR_UNSUPPORTED;
-    const TiledPlan q = tiled_plan(T, npix);
+    const TiledPlan q = tiled_plan(T, npix, real);
     TileList tl{};
     std::memset(tl.index, -1, sizeof(tl.index));
     for (int bm = 0; bm < q.nb; ++bm)
@@ -804,8 +816,8 @@ hv_status cov_tc_planes(const uint16_t* planes, int T, size_t npix, double2* cov
     if (tl.n == 0)
         return HV_OK;
     CUtensorMap tmap;
-    if (!tc::encode_tmap_3d_bf16_sw128(&tmap, planes, npix, 2 * static_cast<uint64_t>(T), 2, npix * 2,
-                                       4 * static_cast<uint64_t>(T) * npix, TC_KC, TC_ROWS))
+    const uint64_t rows = (real ? 1 : 2) * static_cast<uint64_t>(T);
+    if (!tc::encode_tmap_3d_bf16_sw128(&tmap, planes, npix, rows, 2, npix * 2, rows * npix * 2, TC_KC, TC_ROWS))
     {
         set_last_error_msg("tensor-core covariance: cuTensorMapEncodeTiled failed for the split planes");
         return HV_ERR_CUDA;
@@ -818,7 +830,8 @@ hv_status cov_tc_planes(const uint16_t* planes, int T, size_t npix, double2* cov
     k_cov_tc_tiled<<<q.nsplit * tl.n, TP_THREADS, smem, st>>>(tmap, npix, tl, q.chunks_per_split, tpart, err);
     HV_LAUNCH_CHECK();
     k_cov_tc_tiled_reduce<<<(T * T + TR_ENTRIES - 1) / TR_ENTRIES, TR_ENTRIES * TR_GROUPS, 0, st>>>(tpart, T, tl,
-                                                                                                  q.nsplit, cov);
+                                                                                                  q.nsplit, real ? 1 : 0,
+                                                                                                  cov);
     HV_LAUNCH_CHECK();
     count_launch(2);
     return HV_OK;
@@ -842,10 +855,10 @@ hv_status cov_tc(const float2* ring, int T, size_t npix, double2* cov, void* wor
     {
         // the ring's split planes in the workspace after the partial tiles
         uint16_t* planes = reinterpret_cast<uint16_t*>(static_cast<char*>(work) + tiled_part_bytes(T, npix));
-        hv_status r = cov_split_planes(ring, T, npix, 0, T, planes, st);
+        hv_status r = cov_split_planes(ring, T, npix, 0, T, planes, 0, st);
         if (r != HV_OK)
             return r;
-        return cov_tc_planes(planes, T, npix, cov, work, err, ~0u, st);
+        return cov_tc_planes(planes, T, npix, cov, work, err, ~0u, 0, st);
     }
     const TcPlan p = tc_plan(T, npix);
     // raw stages: T x 64 complex samples (T x 512 B) each, as many as fit beside the A stages in 96 KB

@@ -95,16 +95,18 @@ size_t cov_tc_partial_bytes(int T, size_t npix);
 // all of it, else only the rows and columns of the 64-frame slot blocks set (bit b: slots 64 b ..
 // 64 b + 63), bit-identical to a full computation; cov_tc on a ring (T > 64) splits it into planes
 // in its workspace first.
-size_t cov_planes_bytes(int T, size_t npix);
+// `real`: the ring's imaginary parts are 0 (no spatial transform): real rows only, 128-frame blocks.
+size_t cov_planes_bytes(int T, size_t npix, int real);
 bool cov_planes_supported(int T, size_t npix);
-hv_status cov_split_planes(const float2* ring, int T, size_t npix, int slot0, int n, uint16_t* planes, cudaStream_t st);
+hv_status cov_split_planes(const float2* ring, int T, size_t npix, int slot0, int n, uint16_t* planes, int real,
+                           cudaStream_t st);
 hv_status cov_tc_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, int* err,
-                        uint32_t blocks, cudaStream_t st);
+                        uint32_t blocks, int real, cudaStream_t st);
 hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, void* work, cudaStream_t st);
 // The covariance from the split planes (engine modes 0 and 2; HV_ERR_UNSUPPORTED for the SIMT mode
 // and shapes without planes).
 hv_status pca_covariance_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
-                                cudaStream_t st);
+                                int real, cudaStream_t st);
 size_t pca_eigh_workspace(int T);
 void set_eig_precision(int p);
 // Eigenvectors of ranks refine_lo..refine_hi (at most 64 of them) are refined in FP64 after FP32

@@ -128,6 +128,12 @@ int fast_lanes(const hv_settings& s, bool served)
 
 // The split-BF16 planes beside the ring (tiled covariance, T > 64): plain pipes whose ring slots the
 // host tracks (not served, not the fast lanes)
+// the ring holds the converted frames (imaginary parts 0): real planes
+int planes_real(const hv_settings& s)
+{
+    return s.space_transformation == HV_SPACE_NONE && !s.filter2d_enabled ? 1 : 0;
+}
+
 bool uses_planes(const hv_frame_desc& fd, const hv_settings& s, bool served)
 {
     const size_t HW = static_cast<size_t>(fd.width) * fd.height;
@@ -172,7 +178,7 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
         z.add(pca_eigh_workspace(T));
     }
     if (uses_planes(fd, s, served))
-        z.add(cov_planes_bytes(T, HW));
+        z.add(cov_planes_bytes(T, HW, planes_real(s)));
     z.add(HW * 4 * 2);  // view + post
     if (is_moment(s.image_type))
         z.add(static_cast<size_t>(K > 0 ? K : 1) * sizeof(float));
@@ -289,8 +295,9 @@ hv_status build(hv_pipe* p)
     if (uses_planes(p->fd, s, p->served))
     {
         // zero like the ring
-        HV_ALLOC(p->planes, cov_planes_bytes(p->T, HW));
-        HV_CUDA_TRY(cudaMemsetAsync(p->planes, 0, cov_planes_bytes(p->T, HW), p->stream));
+        p->planes_real = planes_real(s);
+        HV_ALLOC(p->planes, cov_planes_bytes(p->T, HW, p->planes_real));
+        HV_CUDA_TRY(cudaMemsetAsync(p->planes, 0, cov_planes_bytes(p->T, HW, p->planes_real), p->stream));
         p->planes_ok = true;
     }
     HV_ALLOC(p->view, HW * sizeof(float));
@@ -572,8 +579,19 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
                          cov_incremental();
         if (!ctl && p->planes_ok)
         {
+            // real planes: 128-frame blocks (pairs of the 64-frame blocks)
+            uint32_t blocks = inc ? dirty : ~0u;
+            if (p->planes_real && inc)
+            {
+                uint32_t b2 = 0;
+                for (int b = 0; b < 16; ++b)
+                    if ((dirty >> (2 * b)) & 3u)
+                        b2 |= 1u << b;
+                blocks = b2;
+            }
             r = inc && !dirty ? HV_OK
-                              : pca_covariance_planes(p->planes, p->T, p->HW, p->cov, p->cov_work, inc ? dirty : ~0u, st);
+                              : pca_covariance_planes(p->planes, p->T, p->HW, p->cov, p->cov_work, blocks,
+                                                      p->planes_real, st);
             if (r == HV_OK)
                 done = true;
             else if (r != HV_ERR_UNSUPPORTED)
@@ -970,7 +988,8 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
     // the 64-frame slot blocks whose covariance rows change, and their split planes
     for (int f = 0; f < nb; f += 1)
         p->cov_dirty |= 1u << (((begin + f) % T) / 64 & 31);
-    if (p->planes_ok && (r = cov_split_planes(p->ring, T, p->HW, begin, nb, p->planes, p->stream)) != HV_OK)
+    if (p->planes_ok &&
+        (r = cov_split_planes(p->ring, T, p->HW, begin, nb, p->planes, p->planes_real, p->stream)) != HV_OK)
         return r;
     p->ring_size += nb;
     if (p->ring_size > T)

@@ -81,6 +81,7 @@ struct hv_pipe
     // split-BF16 planes of the ring for the tiled covariance; planes_ok: they mirror every slot
     uint16_t* planes = nullptr;
     bool planes_ok = false;
+    int planes_real = 0;  // the ring's imaginary parts are 0: real rows only
     float* view = nullptr;
     float* unwrapped = nullptr;
     void* unwrap_work = nullptr;

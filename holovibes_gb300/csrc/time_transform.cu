@@ -585,7 +585,7 @@ hv_status pca_covariance(const float2* ring, int T, size_t npix, double2* cov, v
 }
 
 hv_status pca_covariance_planes(const uint16_t* planes, int T, size_t npix, double2* cov, void* work, uint32_t blocks,
-                                cudaStream_t st)
+                                int real, cudaStream_t st)
 {
     if (T <= 0 || npix == 0 || !planes || !cov || !work)
         return HV_INVALID_VALUE;
@@ -594,7 +594,7 @@ hv_status pca_covariance_planes(const uint16_t* planes, int T, size_t npix, doub
     int* err = static_cast<int*>(work);
     char* ws = static_cast<char*>(work) + COV_FLAGS;
     HV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
-    return cov_tc_planes(planes, T, npix, cov, ws, err, blocks, st);
+    return cov_tc_planes(planes, T, npix, cov, ws, err, blocks, real, st);
 }
 
 hv_status pca_cov_status(const void* work)

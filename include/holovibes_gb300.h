@@ -401,19 +401,22 @@ void hv_pca_cov_incremental(int enable);
 hv_status hv_pca_covariance_status(const void* work);
 /* Split-BF16 planes of a ring for the tiled tensor-core covariance (64 < T <= 1024, npix a multiple
  * of 8): planes[p][2 s + c][px], p = 0: hi = bf16_rn(x), p = 1: lo = bf16_rn(x - hi), c = 0 / 1: real /
- * imaginary part of pixel px of ring slot s. hv_pca_planes_bytes: their size (8 T npix bytes; 0 when
- * the shape has none). hv_pca_split_planes: planes of ring slots slot0 .. slot0 + n - 1 (mod T), as
- * a Pipe writes them when frames enter its ring. hv_pca_covariance_planes: the covariance from the
- * planes (the engine hv_pca_covariance runs on planes it splits into `work`; `work` here needs only
- * the partial tiles, hv_pca_cov_workspace(T, npix) - hv_pca_planes_bytes(T, npix) bytes at least),
- * bit-identical to hv_pca_covariance's tensor-core engine on the ring; `blocks` = ~0u for
- * all of it, else only the rows and columns of the 64-frame slot blocks set (bit b: slots 64 b ..
- * 64 b + 63), the other entries of `cov_c128` left as they are. HV_ERR_UNSUPPORTED for the SIMT
- * engine mode and shapes without planes. */
-size_t hv_pca_planes_bytes(int T, size_t npix);
-hv_status hv_pca_split_planes(const void* ring_c64, int T, size_t npix, int slot0, int n, void* planes, void* stream);
-hv_status hv_pca_covariance_planes(const void* planes, int T, size_t npix, unsigned int blocks, void* cov_c128,
-                                   void* work, void* stream);
+ * imaginary part of pixel px of ring slot s; with `real` != 0 (a ring whose imaginary parts are 0,
+ * such as the converted frames without a spatial transform) planes[p][s][px] of the real parts only.
+ * hv_pca_planes_bytes: their size (8 T npix bytes, 4 T npix for `real`; 0 when the shape has none).
+ * hv_pca_split_planes: planes of ring slots slot0 .. slot0 + n - 1 (mod T), as a Pipe writes them when
+ * frames enter its ring. hv_pca_covariance_planes: the covariance from the planes (the engine
+ * hv_pca_covariance runs on planes it splits into `work`; `work` here needs only the partial tiles,
+ * hv_pca_cov_workspace(T, npix) - hv_pca_planes_bytes(T, npix, 0) bytes at least), bit-identical to
+ * hv_pca_covariance's tensor-core engine on the ring for complex planes; `blocks` = ~0u for all of
+ * it, else only the rows and columns of the slot blocks set (bit b: slots 64 b .. 64 b + 63 for
+ * complex planes, 128 b .. 128 b + 127 for real ones), the other entries of `cov_c128` left as they
+ * are. HV_ERR_UNSUPPORTED for the SIMT engine mode and shapes without planes. */
+size_t hv_pca_planes_bytes(int T, size_t npix, int real);
+hv_status hv_pca_split_planes(const void* ring_c64, int T, size_t npix, int slot0, int n, int real, void* planes,
+                              void* stream);
+hv_status hv_pca_covariance_planes(const void* planes, int T, size_t npix, int real, unsigned int blocks,
+                                   void* cov_c128, void* work, void* stream);
 /* Eigensolve of the Hermitian T x T complex128 matrix (both triangles read): ascending
  * eigenvalues, eigenvectors as columns. Replaces cusolverDnCheevd (matrix_operations.cc:44-65).
  * Writes the columns pmin..pmax as PCA weights W[k][t] = V[t][pmin+k] (complex64) when weights_c64

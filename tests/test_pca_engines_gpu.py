@@ -48,53 +48,71 @@ def test_covariance_engine(cuda, mode, tol, T, npix):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("real", [0, 1])
 @pytest.mark.parametrize("T,npix", [(65, 1000), (128, 65536), (200, 4104), (512, 16384)])
-def test_covariance_planes_bit_identical(cuda, T, npix):
+def test_covariance_planes_bit_identical(cuda, T, npix, real):
     """The tiled tensor-core covariance from split-BF16 planes the caller keeps (hv_pca_split_planes,
-    then hv_pca_covariance_planes: tensor copies straight into the MMA operand layout) is
-    bit-identical to hv_pca_covariance on the ring (which splits it into its workspace); after a
-    wrapping range of ring slots is rewritten and only those slots re-split, the update of the rows
-    and columns of their 64-frame blocks equals the full recomputation bit for bit."""
+    then hv_pca_covariance_planes: tensor copies straight into the MMA operand layout). Complex
+    planes: bit-identical to hv_pca_covariance on the ring (which splits it into its workspace). Real
+    planes (a ring with zero imaginary parts, as without a spatial transform): within rel-L2 2e-5 of
+    FP64 and exactly real. Either way, after a wrapping range of ring slots is rewritten and only
+    those slots re-split, the update of the rows and columns of their slot blocks (64 frames complex,
+    128 real) equals the full recomputation from the planes bit for bit."""
     L = hv.lib()
     ring = _ring(T, npix, T + 7)
+    if real:
+        ring = ring.real.astype(np.complex64)
     rd = dev(ring)
     work = empty(L.hv_pca_cov_workspace(T, npix))
-    planes = empty(L.hv_pca_planes_bytes(T, npix))
-    assert L.hv_pca_planes_bytes(T, npix) == 8 * T * npix
+    planes = empty(L.hv_pca_planes_bytes(T, npix, real))
+    assert L.hv_pca_planes_bytes(T, npix, real) == (4 if real else 8) * T * npix
     cov_ring, cov_pl = empty(T * T * 16), empty(T * T * 16)
     L.hv_pca_covariance_mode(2)
     try:
         call("hv_pca_covariance", ptr(rd), T, npix, ptr(cov_ring), ptr(work), None)
-        call("hv_pca_split_planes", ptr(rd), T, npix, 0, T, ptr(planes), None)
-        call("hv_pca_covariance_planes", ptr(planes), T, npix, 0xFFFFFFFF, ptr(cov_pl), ptr(work), None)
+        call("hv_pca_split_planes", ptr(rd), T, npix, 0, T, real, ptr(planes), None)
+        call("hv_pca_covariance_planes", ptr(planes), T, npix, real, 0xFFFFFFFF, ptr(cov_pl), ptr(work), None)
         cuda.cuda.synchronize()
         assert L.hv_pca_covariance_status(ptr(work)) == hv.HV_OK
         a, b = host(cov_ring, np.complex128, (T, T)), host(cov_pl, np.complex128, (T, T))
-        assert np.array_equal(a, b), float(np.abs(a - b).max() / np.abs(a).max())
+        if real:
+            assert not np.any(b.imag)
+            assert rel_l2(b, a) <= 2e-5
+        else:
+            assert np.array_equal(a, b), float(np.abs(a - b).max() / np.abs(a).max())
         assert rel_l2(b, O.pca_covariance(ring.astype(np.complex128).reshape(T, npix, 1))) <= 2e-5
         # rewrite slots T - 20 .. T + 29 (mod T)
         slot0, n = T - 20, min(50, T)
         slots = [(slot0 + f) % T for f in range(n)]
         ring2 = ring.copy()
-        ring2[slots] = _ring(T, npix, T + 8)[slots]
+        new = _ring(T, npix, T + 8)
+        ring2[slots] = (new.real.astype(np.complex64) if real else new)[slots]
         rd2 = dev(ring2)
+        fb = 128 if real else 64
         blocks = 0
         for sl in slots:
-            blocks |= 1 << (sl // 64)
-        assert blocks != (1 << ((T + 63) // 64)) - 1 or T <= 128
-        call("hv_pca_split_planes", ptr(rd2), T, npix, slot0, n, ptr(planes), None)
-        call("hv_pca_covariance_planes", ptr(planes), T, npix, blocks, ptr(cov_pl), ptr(work), None)
-        call("hv_pca_covariance", ptr(rd2), T, npix, ptr(cov_ring), ptr(work), None)
+            blocks |= 1 << (sl // fb)
+        call("hv_pca_split_planes", ptr(rd2), T, npix, slot0, n, real, ptr(planes), None)
+        call("hv_pca_covariance_planes", ptr(planes), T, npix, real, blocks, ptr(cov_pl), ptr(work), None)
+        # the full recomputation from freshly split planes
+        planes2 = empty(L.hv_pca_planes_bytes(T, npix, real))
+        cov_full = empty(T * T * 16)
+        call("hv_pca_split_planes", ptr(rd2), T, npix, 0, T, real, ptr(planes2), None)
+        call("hv_pca_covariance_planes", ptr(planes2), T, npix, real, 0xFFFFFFFF, ptr(cov_full), ptr(work), None)
+        if not real:
+            call("hv_pca_covariance", ptr(rd2), T, npix, ptr(cov_ring), ptr(work), None)
         cuda.cuda.synchronize()
         assert L.hv_pca_covariance_status(ptr(work)) == hv.HV_OK
     finally:
         L.hv_pca_covariance_mode(0)
-    a, b = host(cov_ring, np.complex128, (T, T)), host(cov_pl, np.complex128, (T, T))
+    a, b = host(cov_full, np.complex128, (T, T)), host(cov_pl, np.complex128, (T, T))
     assert np.array_equal(a, b), float(np.abs(a - b).max() / np.abs(a).max())
+    if not real:
+        assert np.array_equal(host(cov_ring, np.complex128, (T, T)), b)
     # the SIMT mode has no planes path
     L.hv_pca_covariance_mode(1)
     try:
-        assert L.hv_pca_covariance_planes(ptr(planes), T, npix, 0xFFFFFFFF, ptr(cov_pl), ptr(work), None) == \
+        assert L.hv_pca_covariance_planes(ptr(planes), T, npix, real, 0xFFFFFFFF, ptr(cov_pl), ptr(work), None) == \
             hv.HV_ERR_UNSUPPORTED
     finally:
         L.hv_pca_covariance_mode(0)
