@@ -981,14 +981,18 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
         nb = T;
     }
     const int begin = (p->ring_start + p->ring_size) % T;
+    // real planes (no spatial transform) come out of the conversion pass itself
+    const bool fused_split =
+        p->planes_ok && p->planes_real && p->HW % 8 == 0 && (reinterpret_cast<uintptr_t>(raw) & 15) == 0;
     hv_status r = spatial_transform(raw, p->kind, p->W, p->H, nb, p->s.space_transformation, p->lens, p->spatial,
-                                    p->ring, begin, T, p->stream, nullptr, p->f2d_mask, p->work2);
+                                    p->ring, begin, T, p->stream, nullptr, p->f2d_mask, p->work2,
+                                    fused_split ? p->planes : nullptr);
     if (r != HV_OK)
         return r;
     // the 64-frame slot blocks whose covariance rows change, and their split planes
     for (int f = 0; f < nb; f += 1)
         p->cov_dirty |= 1u << (((begin + f) % T) / 64 & 31);
-    if (p->planes_ok &&
+    if (p->planes_ok && !fused_split &&
         (r = cov_split_planes(p->ring, T, p->HW, begin, nb, p->planes, p->planes_real, p->stream)) != HV_OK)
         return r;
     p->ring_size += nb;

@@ -1074,6 +1074,76 @@ __global__ void __launch_bounds__(W32_THREADS, 2) k_fft_cols_w768(ColPass p)
         o[(static_cast<size_t>(g) + 32 * k2) * Ws] = cscale(cconj(x[k2]), sc);
 }
 
+// Raw -> complex into ring slots (space transformation NONE), 8 pixels of one frame per thread
+// (frames of a multiple of 8 pixels, 16-byte aligned rows of the raw batch); with `planes`, the
+// real rows of the ring's split-BF16 planes of those slots as well (planes[p][slot][px]: the
+// covariance operands of a ring with zero imaginary parts), so the frame is read once.
+__global__ void k_convert8(const void* in, int kind, size_t frame_px, int batch, float2* ring, FrameMap map,
+                           const CycleCtl* ctl, uint16_t* planes)
+{
+    if (!ctl_active(ctl))
+        return;
+    if (ctl)
+        in = static_cast<const uint8_t*>(in) + ctl->raw_offset;
+    const size_t groups = frame_px / 8;
+    const size_t total = groups * batch;
+    const size_t plane = static_cast<size_t>(map.nslots) * frame_px;
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        const int b = static_cast<int>(e / groups);
+        const size_t px = (e - static_cast<size_t>(b) * groups) * 8;
+        const size_t src = static_cast<size_t>(b) * frame_px + px;
+        float v[8];
+        if (kind == IN_U8)
+        {
+            const uint2 w = *reinterpret_cast<const uint2*>(static_cast<const uint8_t*>(in) + src);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+            {
+                v[i] = static_cast<float>((w.x >> (8 * i)) & 0xffu) * 257.0f;
+                v[4 + i] = static_cast<float>((w.y >> (8 * i)) & 0xffu) * 257.0f;
+            }
+        }
+        else if (kind == IN_U16 || kind == IN_U16_BE)
+        {
+            const uint4 w = *reinterpret_cast<const uint4*>(static_cast<const uint16_t*>(in) + src);
+            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+            {
+                uint32_t x = ww[i];
+                if (kind == IN_U16_BE)
+                    x = ((x & 0x00ff00ffu) << 8) | ((x >> 8) & 0x00ff00ffu);
+                v[2 * i] = static_cast<float>(x & 0xffffu);
+                v[2 * i + 1] = static_cast<float>(x >> 16);
+            }
+        }
+        else
+        {
+            const float4* f = reinterpret_cast<const float4*>(static_cast<const float*>(in) + src);
+            const float4 a = f[0], c = f[1];
+            v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = c.x, v[5] = c.y, v[6] = c.z, v[7] = c.w;
+        }
+        const size_t off = map.offset(b);
+        float4* o = reinterpret_cast<float4*>(ring + off + px);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            __stcs(o + i, make_float4(v[2 * i], 0.f, v[2 * i + 1], 0.f));
+        if (planes)
+        {
+            uint4 hi, lo;
+            tc::split2(v[0], v[1], hi.x, lo.x);
+            tc::split2(v[2], v[3], hi.y, lo.y);
+            tc::split2(v[4], v[5], hi.z, lo.z);
+            tc::split2(v[6], v[7], hi.w, lo.w);
+            const size_t slot_px = off / map.frame_stride * frame_px + px;
+            *reinterpret_cast<uint4*>(planes + slot_px) = hi;
+            *reinterpret_cast<uint4*>(planes + plane + slot_px) = lo;
+        }
+    }
+}
+
 // Raw -> complex into ring slots (space transformation NONE).
 __global__ void k_convert(const void* in, int kind, size_t frame_px, int batch, float2* ring, FrameMap map,
                           const CycleCtl* ctl)
@@ -1590,7 +1660,7 @@ void set_spatial_sub_batch_mb(int mb) { g_spatial_sub_mb = mb < 0 ? 0 : mb; }
 
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
                             float2* work, float2* ring, int slot0, int nslots, cudaStream_t st, const CycleCtl* ctl,
-                            const float2* f2d_mask, float2* work2)
+                            const float2* f2d_mask, float2* work2, uint16_t* real_planes)
 {
     // With a cycle control block, `raw` is the input ring base (the batch sits at ctl->raw_offset)
     // and the ring slot of frame 0 is slot0 + ctl->ring_begin; every pass is gated by ctl->active.
@@ -1607,8 +1677,25 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
         return HV_INVALID_VALUE;
     if (space == HV_SPACE_NONE && !f2d)
     {
-        const size_t total = HW * batch;
         const int block = 256;
+        // 8-pixel groups: 8-byte (8-bit), 16-byte (16-bit) and 32-byte (float) aligned loads when the
+        // batch starts on 16 bytes and frames hold a multiple of 8 pixels
+        if (HW % 8 == 0 && kind != IN_C64 && (reinterpret_cast<uintptr_t>(raw) & 15) == 0 &&
+            (reinterpret_cast<uintptr_t>(ring) & 15) == 0)
+        {
+            const size_t total = HW / 8 * batch;
+            const int grid = static_cast<int>((total + block - 1) / block < 152 * 8 ? (total + block - 1) / block : 152 * 8);
+            k_convert8<<<grid, block, 0, st>>>(raw, kind, HW, batch, ring, ring_map, ctl, real_planes);
+            HV_LAUNCH_CHECK();
+            count_launch();
+            return HV_OK;
+        }
+        if (real_planes)
+        {
+            set_last_error_msg("converting into the split planes needs frames of a multiple of 8 pixels");
+            return HV_ERR_UNSUPPORTED;
+        }
+        const size_t total = HW * batch;
         const int grid = static_cast<int>((total + block - 1) / block < 152 * 16 ? (total + block - 1) / block : 152 * 16);
         k_convert<<<grid, block, 0, st>>>(raw, kind, HW, batch, ring, ring_map, ctl);
         HV_LAUNCH_CHECK();
