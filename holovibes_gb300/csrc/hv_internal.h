@@ -43,11 +43,13 @@ int raw_kind(int raw_bytes, int big_endian);
 hv_status make_fresnel_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st);
 hv_status make_spectral_lens(float2* lens, int W, int H, float lam, float z, float ps, int mode, cudaStream_t st);
 // real_planes (no spatial transform, frames of a multiple of 8 pixels): the real split-BF16 planes
-// of the ring slots written are produced in the same pass (cov_tc.cu layout, real rows)
+// of the ring slots written are produced in the same pass (cov_tc.cu layout, real rows).
+// reserve_sms: the persistent (TMA-fed) FFT passes leave that many SMs to kernels of other streams
+// (a Pipe's render lanes).
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
                             float2* work, float2* ring, int slot0, int nslots, cudaStream_t st,
                             const CycleCtl* ctl = nullptr, const float2* f2d_mask = nullptr,
-                            float2* work2 = nullptr, uint16_t* real_planes = nullptr);
+                            float2* work2 = nullptr, uint16_t* real_planes = nullptr, int reserve_sms = 0);
 // filter2D band-pass mask in FFT layout: written as complex (multiply = 0) or multiplied into dst.
 hv_status filter2d_mask(float2* dst, int W, int H, int n1, int n2, int smooth_low, int smooth_high, int multiply,
                         cudaStream_t st);

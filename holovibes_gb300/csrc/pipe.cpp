@@ -126,6 +126,9 @@ int fast_lanes(const hv_settings& s, bool served)
     return fast_renders(s, served) > 1 ? hv_pipe::kMaxLanes : 2;
 }
 
+// SMs the persistent spatial passes leave to the render lanes' kernels
+constexpr int kLaneReserveSms = 8;
+
 // The split-BF16 planes beside the ring (tiled covariance, T > 64): plain pipes whose ring slots the
 // host tracks (not served, not the fast lanes)
 // the ring holds the converted frames (imaginary parts 0): real planes
@@ -926,8 +929,12 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
         const int r = static_cast<int>(p->windows % static_cast<uint64_t>(p->nlanes));
         hv_pipe::Lane& L = p->lanes[r];
         HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, L.free, 0));
+        // with render lanes of their own, the persistent spatial passes leave SMs to the lanes'
+        // covariance / eigensolve / view kernels (1024 x 1024 8-bit Fresnel + PCA, T = 32: 88.8k -> 99.5k
+        // frames/s with 8 of 152)
         hv_status st = spatial_transform(raw, p->kind, p->W, p->H, p->T, p->s.space_transformation, p->lens,
-                                         p->spatial, L.ring, 0, p->T, p->stream, nullptr, p->f2d_mask, p->work2);
+                                         p->spatial, L.ring, 0, p->T, p->stream, nullptr, p->f2d_mask, p->work2,
+                                         nullptr, p->nrender > 1 ? kLaneReserveSms : 0);
         if (st != HV_OK)
             return st;
         p->cov_dirty = ~0u;  // every slot rewritten

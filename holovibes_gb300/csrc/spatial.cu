@@ -135,6 +135,7 @@ struct RowPass
     int stream_out;        // 1: output written with an evict-first hint (ring slots)
     const CycleCtl* ctl = nullptr;  // served cycle: gate (active) and, with raw_from_ctl, the input offset
     int raw_from_ctl = 0;           // 1: `in` is the input ring base, the batch is at ctl->raw_offset
+    int reserve_sms = 0;            // persistent passes leave this many SMs to kernels of other streams
 };
 
 // Copies the plan's twiddle tables next to the tile in shared memory (read conflict-free:
@@ -285,6 +286,7 @@ struct ColPass
     int tw_count;
     int stream_out;         // 1: output written with an evict-first hint (ring slots)
     const CycleCtl* ctl = nullptr;  // served cycle: gate (active)
+    int reserve_sms = 0;            // persistent passes leave this many SMs to kernels of other streams
 };
 
 template <int N, int F>
@@ -1314,7 +1316,8 @@ bool launch_rows_w32_tma(const RowPass& p, int nframes, cudaStream_t st, hv_stat
         return false;
     *status = HV_OK;
     const int ntiles = (p.rows / RT_ROWS) * nframes;
-    const int per = (ntiles + 2 * sms - 1) / (2 * sms);  // two CTAs per SM
+    const int use = sms - p.reserve_sms > 0 ? sms - p.reserve_sms : 1;
+    const int per = (ntiles + 2 * use - 1) / (2 * use);  // two CTAs per SM
     const int grid = (ntiles + per - 1) / per;
     RowPass q = p;
     if ((q.tw = twiddles_w32<WT_N>()) == nullptr)
@@ -1404,7 +1407,8 @@ bool launch_cols_w32_tma(const ColPass& p, int nframes, cudaStream_t st, hv_stat
     q.tw_count = fftw::Warp<WT_N>::TW_COUNT;
     const int tiles_x = p.width / WT_COLS;
     const int ntiles = tiles_x * nframes;
-    const int grid = ntiles < sms ? ntiles : sms;
+    const int use = sms - p.reserve_sms > 0 ? sms - p.reserve_sms : 1;
+    const int grid = ntiles < use ? ntiles : use;
     k_fft_cols_w32_tma<<<grid, W32_THREADS, WT_SMEM, st>>>(map, q, tiles_x, ntiles);
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess)
@@ -1660,7 +1664,7 @@ void set_spatial_sub_batch_mb(int mb) { g_spatial_sub_mb = mb < 0 ? 0 : mb; }
 
 hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, int space, const float2* lens,
                             float2* work, float2* ring, int slot0, int nslots, cudaStream_t st, const CycleCtl* ctl,
-                            const float2* f2d_mask, float2* work2, uint16_t* real_planes)
+                            const float2* f2d_mask, float2* work2, uint16_t* real_planes, int reserve_sms)
 {
     // With a cycle control block, `raw` is the input ring base (the batch sits at ctl->raw_offset)
     // and the ring slot of frame 0 is slot0 + ctl->ring_begin; every pass is gated by ctl->active.
@@ -1769,11 +1773,13 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
             RowPass r{raw_b, kind, HW, work, work_b, lens, H, 0, 1.0f};
             r.ctl = ctl;
             r.raw_from_ctl = ctl ? 1 : 0;
+            r.reserve_sms = reserve_sms;
             if ((s = fft_rows(r, W, nb, st)) != HV_OK)
                 return s;
             ColPass c{work, HW, ring, ring_b, nullptr, W, 0, 1.0f};
             c.stream_out = 1;
             c.ctl = ctl;
+            c.reserve_sms = reserve_sms;
             if ((s = fft_cols(c, H, nb, st)) != HV_OK)
                 return s;
         }
@@ -1783,6 +1789,7 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
             RowPass r{raw_b, kind, HW, work, work_b, nullptr, H, 0, 1.0f};
             r.ctl = ctl;
             r.raw_from_ctl = ctl ? 1 : 0;
+            r.reserve_sms = reserve_sms;
             if ((s = fft_rows(r, W, nb, st)) != HV_OK)
                 return s;
             ColPass c{work, HW, work, work_b, lens, W, 2, 1.0f};
