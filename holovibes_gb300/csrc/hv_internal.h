@@ -50,6 +50,11 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
                             float2* work, float2* ring, int slot0, int nslots, cudaStream_t st,
                             const CycleCtl* ctl = nullptr, const float2* f2d_mask = nullptr,
                             float2* work2 = nullptr, uint16_t* real_planes = nullptr, int reserve_sms = 0);
+// Raw 8/16-bit frames (no spatial transform) -> the real split-BF16 planes of ring slots slot0 ..
+// (mod T) only; and the ring slots back from those planes (exact for integer pixels below 2^16).
+hv_status convert_to_planes(const void* raw, int kind, size_t HW, int batch, int slot0, int T, uint16_t* planes,
+                            cudaStream_t st);
+hv_status ring_from_planes(const uint16_t* planes, int T, size_t HW, int slot0, int n, float2* ring, cudaStream_t st);
 // filter2D band-pass mask in FFT layout: written as complex (multiply = 0) or multiplied into dst.
 hv_status filter2d_mask(float2* dst, int W, int H, int n1, int n2, int smooth_low, int smooth_high, int multiply,
                         cudaStream_t st);

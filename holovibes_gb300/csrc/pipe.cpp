@@ -69,12 +69,15 @@ void free_buffers(hv_pipe* p)
             }
         L = hv_pipe::Lane{};
     }
-    for (cudaEvent_t* e : {&p->join_ev, &p->range_ev})
+    for (cudaEvent_t* e : {&p->join_ev, &p->range_ev, &p->pp_cov_ev[0], &p->pp_cov_ev[1], &p->pp_eig_ev[0],
+                           &p->pp_eig_ev[1], &p->pp_view_ev[0], &p->pp_view_ev[1], &p->pp_main_ev, &p->pp_ring_ev[0],
+                           &p->pp_ring_ev[1], &p->pp_ring_ev[2], &p->pp_ring_ev[3]})
         if (*e)
         {
             cudaEventDestroy(*e);
             *e = nullptr;
         }
+    p->pp = false;
     p->range_ev_set = false;
     for (auto* vec : {&p->in_filled, &p->in_consumed, &p->out_ready, &p->out_freed, &p->views[0].out_ready,
                       &p->views[0].out_freed, &p->views[1].out_ready, &p->views[1].out_freed, &p->views[2].out_ready,
@@ -137,6 +140,20 @@ int planes_real(const hv_settings& s)
     return s.space_transformation == HV_SPACE_NONE && !s.filter2d_enabled ? 1 : 0;
 }
 
+bool uses_planes(const hv_frame_desc& fd, const hv_settings& s, bool served);
+
+// PCA on the converted integer frames (no spatial transform) with sliding windows: the windows are
+// pipelined over three streams (process_batch, render_view). The ring is rebuilt from the real
+// split planes (exact for integer pixels), so only the conversion into the planes reads the input
+// batch; a window's eigensolve then overlaps the next batch's conversion and covariance update and
+// the previous window's view.
+bool uses_pca_pipeline(const hv_frame_desc& fd, const hv_settings& s, bool served)
+{
+    const int T = s.time_transformation_size, B = s.batch_size;
+    return uses_pca(s) && uses_planes(fd, s, served) && planes_real(s) && fd.depth <= 2 && !s.cuts_enabled &&
+           !uses_phase_increase(s) && T >= 2 * B;
+}
+
 bool uses_planes(const hv_frame_desc& fd, const hv_settings& s, bool served)
 {
     const size_t HW = static_cast<size_t>(fd.width) * fd.height;
@@ -182,6 +199,8 @@ size_t footprint(const hv_frame_desc& fd, const hv_settings& s, bool served = fa
     }
     if (uses_planes(fd, s, served))
         z.add(cov_planes_bytes(T, HW, planes_real(s)));
+    if (uses_pca_pipeline(fd, s, served))  // the second covariance and weights buffers
+        z.add(static_cast<size_t>(T) * T * 16 + static_cast<size_t>(K > 0 ? K : 1) * T * 8);
     z.add(HW * 4 * 2);  // view + post
     if (is_moment(s.image_type))
         z.add(static_cast<size_t>(K > 0 ? K : 1) * sizeof(float));
@@ -470,6 +489,23 @@ hv_status build(hv_pipe* p)
     p->range_ev_set = false;
     p->render_stream = p->fast ? p->render_stream_owned : p->stream;
     p->windows = 0;
+    // PCA windows over three streams (the tensor-core view's prepared weights are not double-buffered)
+    p->pp = uses_pca_pipeline(p->fd, s, p->served) && p->planes_ok && !p->view_on_tc && !p->fast;
+    p->pp_w = p->pp_b = 0;
+    if (p->pp)
+    {
+        p->render_stream = p->render_stream_owned;
+        p->pp_cov[0] = p->cov;
+        if ((st = dalloc(p, p->pp_cov[1], static_cast<size_t>(p->T) * p->T * sizeof(double2))) != HV_OK)
+            return st;
+        p->pp_weights[0] = p->weights;
+        if ((st = dalloc(p, p->pp_weights[1], static_cast<size_t>(p->K) * p->T * sizeof(float2))) != HV_OK)
+            return st;
+        for (cudaEvent_t* e : {&p->pp_cov_ev[0], &p->pp_cov_ev[1], &p->pp_eig_ev[0], &p->pp_eig_ev[1],
+                               &p->pp_view_ev[0], &p->pp_view_ev[1], &p->pp_main_ev, &p->pp_ring_ev[0],
+                               &p->pp_ring_ev[1], &p->pp_ring_ev[2], &p->pp_ring_ev[3]})
+            HV_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
     // lens (computed once per refresh, fourier_transform.cc:93-137)
     if (s.space_transformation == HV_SPACE_FRESNELTR)
         st = make_fresnel_lens(p->lens, p->W, p->H, s.lambda, s.z_distance, s.pixel_size, s.lens_mode, p->stream);
@@ -560,6 +596,70 @@ hv_status build(hv_pipe* p)
 // sets *frame to the float frame that the fused renorm / shift / accumulation pass reads and
 // *shift_after when that pass applies the fftshift (the view kernels apply it themselves
 // otherwise). `ctl` gates the kernels of a served cycle (null for the plain pipe).
+hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const float** frame, int* shift_after);
+
+// The covariance and eigensolve of a PCA window of the three-stream pipeline (p->pp): the update
+// of covariance buffer w % 2 on the pipe stream (from the other buffer, the previous window's),
+// the eigensolve into weights buffer w % 2 on the eigensolve stream, then the view on the render
+// stream `st` (render_view's view part, with p->weights bound to the window's buffer).
+hv_status render_view_pp(hv_pipe* p, cudaStream_t st, uint32_t dirty, uint32_t all, const float** frame,
+                         int* shift_after)
+{
+    const int w = p->pp_w++, i = w & 1;
+    double2* cov = p->pp_cov[i];
+    cudaStream_t es = p->render_extra[0];
+    hv_status r;
+    if (w >= 2)  // window w - 2's eigensolve read this buffer
+        HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->pp_eig_ev[i], 0));
+    const bool inc = w >= 1 && p->cov_valid && p->cov_mode == cov_mode() && dirty != all && cov_incremental();
+    if (inc)
+        HV_CUDA_TRY(cudaMemcpyAsync(cov, p->pp_cov[i ^ 1], static_cast<size_t>(p->T) * p->T * sizeof(double2),
+                                    cudaMemcpyDeviceToDevice, p->stream));
+    if (!inc || dirty)
+    {
+        uint32_t blocks = inc ? dirty : ~0u;
+        if (inc)
+        {
+            uint32_t b2 = 0;  // real planes: 128-frame blocks
+            for (int b = 0; b < 16; ++b)
+                if ((dirty >> (2 * b)) & 3u)
+                    b2 |= 1u << b;
+            blocks = b2;
+        }
+        r = pca_covariance_planes(p->planes, p->T, p->HW, cov, p->cov_work, blocks, 1, p->stream);
+        if (r == HV_ERR_UNSUPPORTED)  // the SIMT engine mode: from the ring, which the render stream writes
+        {
+            HV_CUDA_TRY(cudaEventRecord(p->pp_main_ev, st));
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->pp_main_ev, 0));
+            r = pca_covariance(p->ring, p->T, p->HW, cov, p->cov_work, p->stream);
+        }
+        if (r != HV_OK)
+            return r;
+    }
+    p->cov_dirty = 0;
+    p->cov_mode = cov_mode();
+    HV_CUDA_TRY(cudaEventRecord(p->pp_cov_ev[i], p->stream));
+    HV_CUDA_TRY(cudaStreamWaitEvent(es, p->pp_cov_ev[i], 0));
+    if (w >= 2)  // window w - 2's view read this weights buffer
+        HV_CUDA_TRY(cudaStreamWaitEvent(es, p->pp_view_ev[i], 0));
+    bool kept = false;
+    if ((r = pca_eigh(cov, p->T, p->evals, p->evecs, p->pmin, p->pmax, p->pp_weights[i], p->eig_work, es, p->pmin,
+                      p->pmax, p->eig_warm, true, &kept)) != HV_OK)
+        return r;
+    p->eig_warm = true;
+    p->cov_valid = kept;
+    HV_CUDA_TRY(cudaEventRecord(p->pp_eig_ev[i], es));
+    HV_CUDA_TRY(cudaStreamWaitEvent(st, p->pp_eig_ev[i], 0));
+    p->weights = p->pp_weights[i];
+    p->pp_nested = true;
+    r = render_view(p, st, nullptr, frame, shift_after);
+    p->pp_nested = false;
+    if (r != HV_OK)
+        return r;
+    HV_CUDA_TRY(cudaEventRecord(p->pp_view_ev[i], st));
+    return HV_OK;
+}
+
 hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const float** frame, int* shift_after)
 {
     const hv_settings& s = p->s;
@@ -567,7 +667,7 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
     const bool pca = uses_pca(s);
     const bool unwrap = uses_unwrap(s);
     const bool pinc = uses_phase_increase(s);
-    if (uses_eig(s))
+    if (uses_eig(s) && !p->pp_nested)
     {
         // not gated by the block: served PCA / SSA_STFT cycles are launched eagerly (render cycles only).
         // A sliding window (stride < T) rewrites S of the T ring slots between renders: only the
@@ -577,6 +677,8 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
         const int nblk = (p->T + 63) / 64;
         const uint32_t all = nblk >= 32 ? ~0u : ((1u << nblk) - 1u);
         const uint32_t dirty = p->cov_dirty & all;
+        if (p->pp && !ctl)
+            return render_view_pp(p, st, dirty, all, frame, shift_after);
         bool done = false;
         const bool inc = !ctl && p->nrender <= 1 && p->cov_valid && p->cov_mode == cov_mode() && dirty != all &&
                          cov_incremental();
@@ -988,18 +1090,52 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
         nb = T;
     }
     const int begin = (p->ring_start + p->ring_size) % T;
+    hv_status r = HV_OK;
+    if (p->pp)
+    {
+        // the batch is read once, into its slots' planes (pipe stream: the covariance update reads
+        // them next); the render stream writes the ring slots from the planes after the previous
+        // window's view. Planes of batch b overwrite slots whose ring copy was made T / B >= 2
+        // batches ago: wait for the copy of batch b - 2.
+        const int b = p->pp_b++;
+        if (b >= 2)
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->pp_ring_ev[(b - 2) & 3], 0));
+        r = convert_to_planes(raw, p->kind, p->HW, nb, begin, T, p->planes, p->stream);
+        if (r == HV_OK)
+        {
+            HV_CUDA_TRY(cudaEventRecord(p->pp_main_ev, p->stream));
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->render_stream, p->pp_main_ev, 0));
+            if ((r = ring_from_planes(p->planes, T, p->HW, begin, nb, p->ring, p->render_stream)) != HV_OK)
+                return r;
+        }
+        else if (r == HV_ERR_UNSUPPORTED)
+        {
+            // a batch off 16-byte alignment: converted into the ring on the pipe stream once the
+            // render stream is idle, then split
+            HV_CUDA_TRY(cudaEventRecord(p->pp_main_ev, p->render_stream));
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->pp_main_ev, 0));
+            if ((r = spatial_transform(raw, p->kind, p->W, p->H, nb, p->s.space_transformation, p->lens, p->spatial,
+                                       p->ring, begin, T, p->stream, nullptr, p->f2d_mask, p->work2)) != HV_OK ||
+                (r = cov_split_planes(p->ring, T, p->HW, begin, nb, p->planes, 1, p->stream)) != HV_OK)
+                return r;
+            HV_CUDA_TRY(cudaEventRecord(p->pp_main_ev, p->stream));
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->render_stream, p->pp_main_ev, 0));
+        }
+        else
+            return r;
+        HV_CUDA_TRY(cudaEventRecord(p->pp_ring_ev[b & 3], p->render_stream));
+    }
     // real planes (no spatial transform) come out of the conversion pass itself
-    const bool fused_split =
-        p->planes_ok && p->planes_real && p->HW % 8 == 0 && (reinterpret_cast<uintptr_t>(raw) & 15) == 0;
-    hv_status r = spatial_transform(raw, p->kind, p->W, p->H, nb, p->s.space_transformation, p->lens, p->spatial,
-                                    p->ring, begin, T, p->stream, nullptr, p->f2d_mask, p->work2,
-                                    fused_split ? p->planes : nullptr);
-    if (r != HV_OK)
+    const bool fused_split = !p->pp && p->planes_ok && p->planes_real && p->HW % 8 == 0 &&
+                             (reinterpret_cast<uintptr_t>(raw) & 15) == 0;
+    if (!p->pp && (r = spatial_transform(raw, p->kind, p->W, p->H, nb, p->s.space_transformation, p->lens,
+                                         p->spatial, p->ring, begin, T, p->stream, nullptr, p->f2d_mask, p->work2,
+                                         fused_split ? p->planes : nullptr)) != HV_OK)
         return r;
     // the 64-frame slot blocks whose covariance rows change, and their split planes
     for (int f = 0; f < nb; f += 1)
         p->cov_dirty |= 1u << (((begin + f) % T) / 64 & 31);
-    if (p->planes_ok && !fused_split &&
+    if (p->planes_ok && !fused_split && !p->pp &&
         (r = cov_split_planes(p->ring, T, p->HW, begin, nb, p->planes, p->planes_real, p->stream)) != HV_OK)
         return r;
     p->ring_size += nb;
@@ -1490,6 +1626,8 @@ hv_status hv_pipe_pull_output(hv_pipe* p, uint16_t* dst, int mem, int64_t timeou
 static hv_status sync_render(hv_pipe* p)
 {
     HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
+    if (p->pp)
+        HV_CUDA_TRY(cudaStreamSynchronize(p->render_extra[0]));
     if (p->nrender > 1)
         for (int l = 0; l < p->nrender; ++l)
             HV_CUDA_TRY(cudaStreamSynchronize(p->lanes[l].st));

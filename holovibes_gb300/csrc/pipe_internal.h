@@ -82,6 +82,17 @@ struct hv_pipe
     uint16_t* planes = nullptr;
     bool planes_ok = false;
     int planes_real = 0;  // the ring's imaginary parts are 0: real rows only
+    // PCA windows pipelined over three streams (pipe.cpp, `pp`): the pipe stream converts each
+    // batch into the split planes and updates the covariance, the eigensolve stream solves it,
+    // the render stream writes the ring from the planes and renders; covariance and weights
+    // alternate between two buffers by window parity
+    bool pp = false, pp_nested = false;
+    int pp_w = 0, pp_b = 0;
+    double2* pp_cov[2] = {nullptr, nullptr};
+    float2* pp_weights[2] = {nullptr, nullptr};
+    cudaEvent_t pp_cov_ev[2] = {nullptr, nullptr}, pp_eig_ev[2] = {nullptr, nullptr};
+    cudaEvent_t pp_view_ev[2] = {nullptr, nullptr}, pp_main_ev = nullptr;
+    cudaEvent_t pp_ring_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float* view = nullptr;
     float* unwrapped = nullptr;
     void* unwrap_work = nullptr;

@@ -1128,10 +1128,13 @@ __global__ void k_convert8(const void* in, int kind, size_t frame_px, int batch,
             v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = c.x, v[5] = c.y, v[6] = c.z, v[7] = c.w;
         }
         const size_t off = map.offset(b);
-        float4* o = reinterpret_cast<float4*>(ring + off + px);
+        if (ring)
+        {
+            float4* o = reinterpret_cast<float4*>(ring + off + px);
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-            __stcs(o + i, make_float4(v[2 * i], 0.f, v[2 * i + 1], 0.f));
+            for (int i = 0; i < 4; ++i)
+                __stcs(o + i, make_float4(v[2 * i], 0.f, v[2 * i + 1], 0.f));
+        }
         if (planes)
         {
             uint4 hi, lo;
@@ -1142,6 +1145,35 @@ __global__ void k_convert8(const void* in, int kind, size_t frame_px, int batch,
             const size_t slot_px = off / map.frame_stride * frame_px + px;
             *reinterpret_cast<uint4*>(planes + slot_px) = hi;
             *reinterpret_cast<uint4*>(planes + plane + slot_px) = lo;
+        }
+    }
+}
+
+// Ring slots slot0 .. slot0 + n - 1 (mod T) from their real split planes: x = hi + lo, exact for
+// integer pixels below 2^16 (hi keeps the top 8 significant bits, lo the rest), imaginary part 0.
+__global__ void k_ring_from_planes(const uint16_t* __restrict__ planes, int T, size_t frame_px, int slot0, int n,
+                                   float2* __restrict__ ring)
+{
+    const size_t groups = frame_px / 8;
+    const size_t total = groups * n;
+    const size_t plane = static_cast<size_t>(T) * frame_px;
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        const int f = static_cast<int>(e / groups);
+        const size_t px = (e - static_cast<size_t>(f) * groups) * 8;
+        const size_t at = static_cast<size_t>((slot0 + f) % T) * frame_px + px;
+        const uint4 hi = *reinterpret_cast<const uint4*>(planes + at);
+        const uint4 lo = *reinterpret_cast<const uint4*>(planes + plane + at);
+        const uint32_t h[4] = {hi.x, hi.y, hi.z, hi.w}, l[4] = {lo.x, lo.y, lo.z, lo.w};
+        float4* o = reinterpret_cast<float4*>(ring + at);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+        {
+            // bf16 = the top half of an FP32 word
+            const float a = __uint_as_float(h[i] << 16) + __uint_as_float(l[i] << 16);
+            const float b = __uint_as_float(h[i] & 0xffff0000u) + __uint_as_float(l[i] & 0xffff0000u);
+            __stcs(o + i, make_float4(a, 0.f, b, 0.f));
         }
     }
 }
@@ -1811,6 +1843,34 @@ hv_status spatial_transform(const void* raw, int kind, int W, int H, int batch, 
     return HV_OK;
     set_last_error_msg("unknown space transformation");
     return HV_INVALID_VALUE;
+}
+
+hv_status convert_to_planes(const void* raw, int kind, size_t HW, int batch, int slot0, int T, uint16_t* planes,
+                            cudaStream_t st)
+{
+    if (HW % 8 != 0 || kind == IN_C64 || (reinterpret_cast<uintptr_t>(raw) & 15) != 0 || batch <= 0)
+        return HV_ERR_UNSUPPORTED;
+    const FrameMap map{HW, slot0, T};
+    const size_t total = HW / 8 * batch;
+    const int block = 256;
+    const int grid = static_cast<int>((total + block - 1) / block < 152 * 8 ? (total + block - 1) / block : 152 * 8);
+    k_convert8<<<grid, block, 0, st>>>(raw, kind, HW, batch, nullptr, map, nullptr, planes);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+hv_status ring_from_planes(const uint16_t* planes, int T, size_t HW, int slot0, int n, float2* ring, cudaStream_t st)
+{
+    if (HW % 8 != 0 || n <= 0)
+        return n <= 0 ? HV_OK : HV_ERR_UNSUPPORTED;
+    const size_t total = HW / 8 * n;
+    const int block = 256;
+    const int grid = static_cast<int>((total + block - 1) / block < 152 * 8 ? (total + block - 1) / block : 152 * 8);
+    k_ring_from_planes<<<grid, block, 0, st>>>(planes, T, HW, slot0, n, ring);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
 }
 
 hv_status fft_rows_pass(const void* in, int kind, float2* out, int W, int H, int batch, const float2* premul,

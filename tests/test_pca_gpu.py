@@ -109,28 +109,31 @@ def test_pipe_pca_windows_warm_start(cuda, T, img):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("T,B,p_start,modes", [(128, 24, 124, 8), (192, 40, 175, 24), (256, 64, 252, 8)])
-def test_pipe_incremental_covariance_bit_identical(cuda, T, B, p_start, modes):
+@pytest.mark.parametrize("T,B,p_start,modes,space,depth", [(128, 24, 124, 8, 1, 2), (192, 40, 175, 24, 1, 2),
+                                                             (256, 64, 252, 8, 1, 2), (128, 32, 124, 8, 0, 2),
+                                                             (192, 64, 188, 8, 0, 1)])
+def test_pipe_incremental_covariance_bit_identical(cuda, T, B, p_start, modes, space, depth):
     """Sliding windows (stride B < T): between two renders only the ring slots of one stride are
     rewritten, and the Pipe recomputes only the covariance rows and columns of the 64-frame slot
     blocks holding them (batches not aligned to the blocks and wrapping around the ring here; the
     subspace iteration for the dominant components, the block Jacobi for ranks 175-178 of T = 192 with
     24 seeded modes: two pairs of close eigenvalues with gaps of 25% and 18% to the ranks outside, and
     the squared-modulus view, invariant to rotations inside the kept subspace, so that the oracle
-    comparison is well conditioned). Every output
-    (float frame and uint16) is bit-identical to the same Pipe recomputing the whole covariance at
+    comparison is well conditioned; without a spatial transform the windows run on the three-stream
+    pipeline with real planes). Every output (float frame and uint16) is bit-identical to the same Pipe recomputing the whole covariance at
     every window, and within rel-L2 1e-4 of the oracle."""
     from gpu_util import oracle_settings
 
     from holovibes_gb300.synthetic import Interferogram
 
     W = H = 64
-    fd = hv.FrameDescriptor(W, H, 2)
-    s = hv.Settings.defaults().update(space_transformation=1, time_transformation=2, time_transformation_size=T,
+    fd = hv.FrameDescriptor(W, H, depth)
+    s = hv.Settings.defaults().update(space_transformation=space, time_transformation=2, time_transformation_size=T,
                                       time_stride=B, batch_size=B, z_distance=0.3, pixel_size=20.0, image_type=1,
                                       p_start=p_start, p_width=3, renorm=1, contrast_enabled=1).validate(fd)
     nb = -(-T // B) + 8
-    raw = Interferogram(width=W, height=H, seed=T + B, modes=modes).frames(0, nb * B)
+    raw = Interferogram(width=W, height=H, seed=T + B, modes=modes, dtype=np.uint8 if depth == 1 else np.uint16,
+                        max_value=255 if depth == 1 else 4095).frames(0, nb * B)
     outs = {}
     for inc in (1, 0):
         hv.lib().hv_pca_cov_incremental(inc)
@@ -158,3 +161,52 @@ def test_pipe_incremental_covariance_bit_identical(cuda, T, B, p_start, modes):
             errs.append(rel_l2(outs[1][len(errs)][0], ref.float_frame))
     assert len(errs) == len(outs[1])
     assert max(errs) <= 1e-4, errs
+
+
+@pytest.mark.gpu
+def test_pipe_pca_pipeline_unaligned_device_batches(cuda):
+    """PCA windows on the three-stream pipeline fed with device batches off 16-byte alignment (the
+    conversion then writes the ring on the pipe stream and splits it): every output equals the same
+    windows fed from aligned host batches, and is within rel-L2 1e-4 of the oracle."""
+    import torch
+    from gpu_util import oracle_settings
+
+    from holovibes_gb300.synthetic import Interferogram
+
+    T, B, W, H = 128, 32, 64, 64
+    fd = hv.FrameDescriptor(W, H, 2)
+    s = hv.Settings.defaults().update(space_transformation=0, time_transformation=2, time_transformation_size=T,
+                                      time_stride=B, batch_size=B, image_type=1, p_start=T - 4, p_width=3, renorm=1,
+                                      contrast_enabled=1).validate(fd)
+    nb = T // B + 6
+    raw = Interferogram(width=W, height=H, seed=7, modes=8).frames(0, nb * B)
+    outs = []
+    for unaligned in (0, 1):
+        pipe = hv.Pipe(fd, s)
+        frames = []
+        buf = torch.empty(raw[:B].nbytes + 16, dtype=torch.uint8, device="cuda")
+        for b in range(nb):
+            batch = np.ascontiguousarray(raw[b * B:(b + 1) * B])
+            if unaligned:
+                src = torch.from_numpy(batch.view(np.uint8).reshape(-1).copy()).cuda()
+                buf[2:2 + src.numel()].copy_(src)
+                torch.cuda.synchronize()
+                pipe.enqueue_ptr(buf.data_ptr() + 2, B, hv.MEM_DEVICE)
+                pipe.sync()
+            else:
+                pipe.enqueue(batch)
+            if pipe.output_count():
+                pipe.pull()
+                frames.append(pipe.float_frame().copy())
+        pipe.close()
+        outs.append(frames)
+    assert len(outs[0]) == len(outs[1]) == nb - T // B + 1
+    for a, b2 in zip(*outs):
+        assert np.array_equal(a, b2)
+    oracle = O.OraclePipe(oracle_settings(fd, s))
+    k = 0
+    for b in range(nb):
+        ref = oracle.process_batch(raw[b * B:(b + 1) * B])
+        if ref is not None:
+            assert rel_l2(outs[0][k], ref.float_frame) <= 1e-4
+            k += 1
