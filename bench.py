@@ -525,6 +525,13 @@ def steps_for(hv, fd, s, dev_batch, stream):
             out.append(("pca_covariance", lambda: L.hv_pca_covariance_planes(planes.data_ptr(), T, HW, real, blocks,
                                                                              cov.data_ptr(), cw.data_ptr(), stream),
                         T * HW * (4 if real else 8), tiles * 3 * 2 * 128 * 128 * HW))
+            if real and T >= 2 * B and fd.depth <= 2:
+                # the pipe's view of a real ring pipelined over streams: the planes, except the B
+                # slots the next batch overwrites, which come from the ring
+                out = [r for r in out if r[0] != "time_view"]
+                out.append(("time_view_planes", lambda: L.hv_time_view_planes(
+                    planes.data_ptr(), ring.data_ptr(), S % T, B, T, W, H, wts.data_ptr(), K, s.image_type, 1.0,
+                    s.fft_shift, view.data_ptr(), None, stream), (T - B) * HW * 4 + B * HW * 8 + HW * 4, 0))
         else:
             # tensor flops: the 128 x 128 tiles of the 2T x 2T real Gram matrix on or above its
             # diagonal, three BF16 products each (T <= 32: one packed 128 x 128 product)

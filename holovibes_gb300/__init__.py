@@ -240,6 +240,7 @@ def _declare(L: C.CDLL) -> None:
         "hv_fft_cols": (st, [vp, vp, i32, i32, i32, vp, i32, f32, i32, i32, vp]),
         "hv_time_view": (st, [vp, i32, i32, i32, vp, i32, i32, f32, i32, vp, vp, vp]),
         "hv_time_view_partials": (i32, [i32, i32]),
+        "hv_time_view_planes": (st, [vp, vp, i32, i32, i32, i32, i32, vp, i32, i32, f32, i32, vp, vp, vp]),
         "hv_time_view_tc": (st, [vp, i32, i32, i32, vp, i32, i32, f32, i32, vp, vp, vp, vp]),
         "hv_time_view_tc_prepare": (st, [vp, i32, i32, vp, vp]),
         "hv_time_view_tc_run": (st, [vp, i32, i32, i32, i32, i32, f32, i32, vp, vp, vp, vp]),

@@ -154,6 +154,18 @@ hv_status hv_time_view(const void* ring_c64, int T, int width, int height, const
                      img_type, scale, shift, out_f32, partials_f64, S(stream));
 }
 
+hv_status hv_time_view_planes(const void* planes_u16, const void* ring_c64, int ring_slot0, int ring_n, int T,
+                              int width, int height, const void* weights_c64, int K, int img_type, float scale,
+                              int shift, float* out_f32, double* partials_f64, void* stream)
+{
+    if (!planes_u16 || (ring_n > 0 && !ring_c64) || !weights_c64 || !out_f32 || img_type < 0 ||
+        img_type > HV_IMG_ARGUMENT)
+        return HV_INVALID_VALUE;
+    return time_view_planes(static_cast<const uint16_t*>(planes_u16), static_cast<const float2*>(ring_c64),
+                            ring_slot0, ring_n, T, width, height, static_cast<const float2*>(weights_c64), K, img_type,
+                            scale, shift, out_f32, partials_f64, S(stream));
+}
+
 int hv_time_view_partials(int width, int height) { return time_view_partials(width, height); }
 
 void hv_time_view_mode(int mode) { set_view_mode(mode); }

@@ -72,6 +72,12 @@ int time_view_partials(int W, int H);
 hv_status time_view(const float2* ring, int T, int W, int H, const float2* weights, int K, int img_type, float scale,
                     int shift, float* out, double* partials, cudaStream_t st, const CycleCtl* ctl = nullptr,
                     const float* bin_w = nullptr);
+// time_view on a real ring held as split-BF16 planes ([2][T][HW] bf16, hi then lo; HW % 8 == 0),
+// the slots [ring_slot0, ring_slot0 + ring_n) mod T read from the complex ring instead.
+hv_status time_view_planes(const uint16_t* planes, const float2* ring, int ring_slot0, int ring_n, int T, int W, int H,
+                           const float2* weights, int K, int img_type, float scale, int shift, float* out,
+                           double* partials, cudaStream_t st, const CycleCtl* ctl = nullptr,
+                           const float* bin_w = nullptr);
 hv_status moment_bin_weights(float* bin_w, int T, int pmin, int pmax, int order, float camera_fps, cudaStream_t st);
 inline bool is_moment(int img_type) { return img_type >= HV_IMG_MOMENTS_0 && img_type <= HV_IMG_MOMENTS_2; }
 hv_status stft_weights(float2* weights, int T, int pmin, int pmax, cudaStream_t st);

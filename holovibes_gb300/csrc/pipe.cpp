@@ -607,7 +607,7 @@ hv_status render_view_pp(hv_pipe* p, cudaStream_t st, uint32_t dirty, uint32_t a
 {
     const int w = p->pp_w++, i = w & 1;
     double2* cov = p->pp_cov[i];
-    cudaStream_t es = p->render_extra[0];
+    cudaStream_t es = p->eig_stream;
     hv_status r;
     if (w >= 2)  // window w - 2's eigensolve read this buffer
         HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->pp_eig_ev[i], 0));
@@ -658,6 +658,23 @@ hv_status render_view_pp(hv_pipe* p, cudaStream_t st, uint32_t dirty, uint32_t a
         return r;
     HV_CUDA_TRY(cudaEventRecord(p->pp_view_ev[i], st));
     return HV_OK;
+}
+
+// The FP32 SIMT time view of the ring into p->view. The pipelined PCA windows (p->pp: a real
+// ring) read the real split planes instead, half the bytes; the slots that the next batch's
+// planes overwrite while this view may still run (the next batch waits only for the views
+// enqueued before the previous batch) are read from the ring, which holds every slot.
+hv_status ring_view(hv_pipe* p, cudaStream_t st, float scale, int shift, double* partials, const CycleCtl* ctl,
+                    bool bins = true)
+{
+    const hv_settings& s = p->s;
+    const float* bin_w = bins ? p->bin_w : nullptr;
+    if (p->pp)
+        return time_view_planes(p->planes, p->ring, (p->ring_start + p->ring_size) % p->T, std::min(p->B, p->T),
+                                p->T, p->W, p->H, p->weights, p->K, s.image_type, scale, shift, p->view, partials, st,
+                                ctl, bin_w);
+    return time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale, shift, p->view, partials, st,
+                     ctl, bin_w);
 }
 
 hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const float** frame, int* shift_after)
@@ -766,9 +783,8 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
         const int shift_in_view = s.fft_shift ? 1 : 0;
         if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, scale, shift_in_view, p->view,
                                          renorm ? p->partials : nullptr, p->view_tc_work, st, ctl, p->bin_w)
-                               : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, scale,
-                                           shift_in_view, p->view, renorm ? p->partials : nullptr, st, ctl,
-                                           p->bin_w)) != HV_OK)
+                               : ring_view(p, st, scale, shift_in_view, renorm ? p->partials : nullptr, ctl)) !=
+            HV_OK)
             return r;
         if (renorm && (r = renorm_factors(p->view, p->HW, s.renorm_constant, p->partials, p->npartials, p->factors,
                                           p->reduce_work, st, ctl)) != HV_OK)
@@ -778,8 +794,7 @@ hv_status render_view(hv_pipe* p, cudaStream_t st, const CycleCtl* ctl, const fl
     // not gated by the block: served unwrap cycles are launched eagerly (render cycles only)
     if ((r = p->view_on_tc ? view_tc(p->ring, p->T, p->W, p->H, p->K, s.image_type, 1.0f, 0, p->view, nullptr,
                                      p->view_tc_work, st, ctl)
-                           : time_view(p->ring, p->T, p->W, p->H, p->weights, p->K, s.image_type, 1.0f, 0, p->view,
-                                       nullptr, st, ctl)) != HV_OK)
+                           : ring_view(p, st, 1.0f, 0, nullptr, ctl, false)) != HV_OK)
         return r;
     if ((r = unwrap_2d(p->view, p->unwrapped, p->W, p->H, p->unwrap_work, st)) != HV_OK)
         return r;
@@ -1095,11 +1110,13 @@ hv_status process_batch(hv_pipe* p, const uint8_t* raw)
     {
         // the batch is read once, into its slots' planes (pipe stream: the covariance update reads
         // them next); the render stream writes the ring slots from the planes after the previous
-        // window's view. Planes of batch b overwrite slots whose ring copy was made T / B >= 2
-        // batches ago: wait for the copy of batch b - 2.
+        // window's view. The views read the planes: batch b waits for the ring copy of batch b - 1,
+        // which the render stream runs after every view enqueued before batch b - 1. A view
+        // enqueued since (it may run while batch b is converted) reads the slots of batch b from
+        // the ring (ring_view).
         const int b = p->pp_b++;
-        if (b >= 2)
-            HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->pp_ring_ev[(b - 2) & 3], 0));
+        if (b >= 1)
+            HV_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->pp_ring_ev[(b - 1) & 3], 0));
         r = convert_to_planes(raw, p->kind, p->HW, nb, begin, T, p->planes, p->stream);
         if (r == HV_OK)
         {
@@ -1478,10 +1495,15 @@ hv_pipe* hv_pipe_create(const hv_frame_desc* fd, const hv_settings* settings, vo
         }
         p->own_stream = true;
     }
+    // the eigensolve chain of a pipelined PCA window is latency bound and on the critical path: its
+    // small grids go first when SMs free up
+    int least_prio = 0, greatest_prio = 0;
     if (cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&p->render_stream_owned, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&p->render_extra[0], cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&p->render_extra[1], cudaStreamNonBlocking) != cudaSuccess)
+        cudaStreamCreateWithFlags(&p->render_extra[1], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaDeviceGetStreamPriorityRange(&least_prio, &greatest_prio) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&p->eig_stream, cudaStreamNonBlocking, greatest_prio) != cudaSuccess)
     {
         out = HV_ERR_CUDA;
         hv_pipe_destroy(p);
@@ -1509,6 +1531,8 @@ void hv_pipe_destroy(hv_pipe* p)
     for (cudaStream_t e : p->render_extra)
         if (e)
             cudaStreamSynchronize(e);
+    if (p->eig_stream)
+        cudaStreamSynchronize(p->eig_stream);
     free_buffers(p);
     if (p->copy_stream)
         cudaStreamDestroy(p->copy_stream);
@@ -1517,6 +1541,8 @@ void hv_pipe_destroy(hv_pipe* p)
     for (cudaStream_t e : p->render_extra)
         if (e)
             cudaStreamDestroy(e);
+    if (p->eig_stream)
+        cudaStreamDestroy(p->eig_stream);
     if (p->own_stream && p->stream)
         cudaStreamDestroy(p->stream);
     delete p;
@@ -1627,7 +1653,7 @@ static hv_status sync_render(hv_pipe* p)
 {
     HV_CUDA_TRY(cudaStreamSynchronize(p->render_stream));
     if (p->pp)
-        HV_CUDA_TRY(cudaStreamSynchronize(p->render_extra[0]));
+        HV_CUDA_TRY(cudaStreamSynchronize(p->eig_stream));
     if (p->nrender > 1)
         for (int l = 0; l < p->nrender; ++l)
             HV_CUDA_TRY(cudaStreamSynchronize(p->lanes[l].st));

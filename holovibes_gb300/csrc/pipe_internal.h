@@ -62,6 +62,7 @@ struct hv_pipe
     Lane lanes[kMaxLanes];
     int nlanes = 0, nrender = 1;
     cudaStream_t render_extra[kMaxLanes - 1] = {nullptr, nullptr};  // render streams of lanes 1, 2
+    cudaStream_t eig_stream = nullptr;  // the pipelined PCA windows' eigensolves (greatest priority)
     cudaEvent_t range_ev = nullptr;  // after the last autocontrast (lanes with their own streams)
     bool range_ev_set = false;
     cudaEvent_t join_ev = nullptr;

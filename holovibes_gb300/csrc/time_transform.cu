@@ -252,6 +252,199 @@ __global__ void __launch_bounds__(TV_THREADS) k_time_view2(const float2* __restr
     }
 }
 
+// sum_t x_t W[k][t] over slots [t0, t1) of a real ring, two adjacent pixels, from the split-BF16
+// planes (hi = bf16(x), lo = bf16(x - hi): a 4-byte load from each plane) or from the complex ring
+// (real parts of one 16-byte load). Either source takes the same FMAs in the same order as
+// k_time_view / k_time_view2 on the ring (the zero imaginary parts leave those sums unchanged).
+// The planes hold half the bytes per sample: twice the frames per unrolled step keep as many bytes
+// in flight as the ring view.
+template <int KC>
+__device__ __forceinline__ void tvp_accumulate(float2 (&a)[2][KC], uint32_t h, uint32_t l, const float2* wt)
+{
+    // bf16 = the top half of an FP32 word; hi + lo is exact for integer pixels below 2^16
+    const float x0 = __uint_as_float(h << 16) + __uint_as_float(l << 16);
+    const float x1 = __uint_as_float(h & 0xffff0000u) + __uint_as_float(l & 0xffff0000u);
+#pragma unroll
+    for (int kk = 0; kk < KC; ++kk)
+    {
+        const float2 w = wt[kk];
+        a[0][kk].x = fmaf(x0, w.x, a[0][kk].x);
+        a[0][kk].y = fmaf(x0, w.y, a[0][kk].y);
+        a[1][kk].x = fmaf(x1, w.x, a[1][kk].x);
+        a[1][kk].y = fmaf(x1, w.y, a[1][kk].y);
+    }
+}
+
+template <int KC>
+__device__ __forceinline__ void tvp_planes(float2 (&a)[2][KC], const uint32_t* __restrict__ hi,
+                                           const uint32_t* __restrict__ lo, size_t step, int t0, int t1,
+                                           const float2* wsm)
+{
+    constexpr int D = 16;  // frames whose loads are issued before the first is used
+    int t = t0;
+    for (; t + D <= t1; t += D)
+    {
+        uint32_t h[D], l[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+        {
+            h[i] = __ldcs(hi + static_cast<size_t>(t + i) * step);
+            l[i] = __ldcs(lo + static_cast<size_t>(t + i) * step);
+        }
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+            tvp_accumulate<KC>(a, h[i], l[i], wsm + (t + i) * KC);
+    }
+    for (; t < t1; ++t)
+        tvp_accumulate<KC>(a, __ldcs(hi + static_cast<size_t>(t) * step), __ldcs(lo + static_cast<size_t>(t) * step),
+                           wsm + t * KC);
+}
+
+template <int KC>
+__device__ __forceinline__ void tvp_ring(float2 (&a)[2][KC], const float4* __restrict__ ring, size_t step, int t0,
+                                         int t1, const float2* wsm)
+{
+#pragma unroll 8
+    for (int t = t0; t < t1; ++t)
+    {
+        const float4 r = __ldg(ring + static_cast<size_t>(t) * step);
+        const float2* wt = wsm + t * KC;
+#pragma unroll
+        for (int kk = 0; kk < KC; ++kk)
+        {
+            const float2 w = wt[kk];
+            a[0][kk].x = fmaf(r.x, w.x, a[0][kk].x);
+            a[0][kk].y = fmaf(r.x, w.y, a[0][kk].y);
+            a[1][kk].x = fmaf(r.z, w.x, a[1][kk].x);
+            a[1][kk].y = fmaf(r.z, w.y, a[1][kk].y);
+        }
+    }
+}
+
+// The view of a real ring (zero imaginary parts) read from its split-BF16 planes ([2][T][HW] bf16,
+// hi then lo): 4 bytes per sample instead of the 8 of the complex ring. The ring slots
+// [r0, r0 + rn) mod T are read from the complex ring instead (the slots that the next batch's
+// planes overwrite while this view may still run). Two adjacent pixels per thread, 128 threads
+// cover 256 pixels and write their two 128-pixel renormalisation partials (those of k_time_view).
+// The view values equal k_time_view's on the same ring.
+template <int KC>
+__global__ void __launch_bounds__(TV_THREADS, 7) k_time_view_planes(const uint16_t* __restrict__ planes,
+                                                                 const float2* __restrict__ ring, int r0, int rn, int T,
+                                                                 int W, int H, const float2* __restrict__ weights,
+                                                                 int K, int img_type, float scale, int shift,
+                                                                 float* __restrict__ out, double* __restrict__ partials,
+                                                                 int npartials, const CycleCtl* ctl,
+                                                                 const float* __restrict__ bin_w)
+{
+    if (!ctl_render(ctl))
+        return;
+    extern __shared__ __align__(16) float2 wsm[];  // [T][KC]
+    __shared__ double red[TV_THREADS / 32];
+    const size_t HW = static_cast<size_t>(W) * H;
+    const size_t pix0 = 2 * (blockIdx.x * static_cast<size_t>(TV_THREADS) + threadIdx.x);
+    const bool valid = pix0 < HW;  // HW even: both pixels or none
+    // slot order [0, T) cut into at most three runs, each from one source
+    int cut[4], src[3], nrun;
+    if (rn <= 0)
+    {
+        cut[0] = 0, cut[1] = T, src[0] = 0, nrun = 1;
+    }
+    else if (r0 + rn <= T)
+    {
+        cut[0] = 0, cut[1] = r0, cut[2] = r0 + rn, cut[3] = T;
+        src[0] = 0, src[1] = 1, src[2] = 0, nrun = 3;
+    }
+    else
+    {
+        cut[0] = 0, cut[1] = r0 + rn - T, cut[2] = r0, cut[3] = T;
+        src[0] = 1, src[1] = 0, src[2] = 1, nrun = 3;
+    }
+    float view0 = 0.f, view1 = 0.f;
+    for (int k0 = 0; k0 < K; k0 += KC)
+    {
+        __syncthreads();
+        for (int e = threadIdx.x; e < T * KC; e += TV_THREADS)
+        {
+            const int t = e / KC, kk = e - t * KC;
+            const int k = k0 + kk;
+            wsm[e] = (k < K) ? weights[static_cast<size_t>(k) * T + t] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        float2 a[2][KC];
+#pragma unroll
+        for (int kk = 0; kk < KC; ++kk)
+            a[0][kk] = a[1][kk] = make_float2(0.f, 0.f);
+        if (valid)
+        {
+            for (int r = 0; r < nrun; ++r)
+            {
+                if (src[r])
+                    tvp_ring<KC>(a, reinterpret_cast<const float4*>(ring + pix0), HW / 2, cut[r], cut[r + 1], wsm);
+                else
+                    tvp_planes<KC>(a, reinterpret_cast<const uint32_t*>(planes + pix0),
+                                   reinterpret_cast<const uint32_t*>(planes + static_cast<size_t>(T) * HW + pix0),
+                                   HW / 2, cut[r], cut[r + 1], wsm);
+            }
+            const int kn = (K - k0) < KC ? (K - k0) : KC;
+#pragma unroll
+            for (int kk = 0; kk < KC; ++kk)
+                if (kk < kn)
+                {
+                    if (bin_w)
+                    {
+                        const float bw = __ldg(bin_w + k0 + kk);
+                        view0 += (a[0][kk].x * a[0][kk].x + a[0][kk].y * a[0][kk].y) * bw;
+                        view1 += (a[1][kk].x * a[1][kk].x + a[1][kk].y * a[1][kk].y) * bw;
+                    }
+                    else
+                    {
+                        view0 += view_value(a[0][kk], img_type);
+                        view1 += view_value(a[1][kk], img_type);
+                    }
+                }
+        }
+    }
+    float v0 = 0.f, v1 = 0.f;
+    if (valid)
+    {
+        v0 = bin_w ? view0 : view0 / static_cast<float>(K);
+        v1 = bin_w ? view1 : view1 / static_cast<float>(K);
+        if (scale != 1.0f)
+        {
+            v0 = v0 * scale;
+            v1 = v1 * scale;
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+        {
+            const size_t pix = pix0 + q;
+            const int x = static_cast<int>(pix % W);
+            const int y = static_cast<int>(pix / W);
+            size_t dst = pix;
+            if (shift)
+                dst = static_cast<size_t>((y + H / 2) % H) * W + (x + W / 2) % W;
+            out[dst] = q ? v1 : v0;
+        }
+    }
+    if (partials)
+    {
+        double d = valid ? static_cast<double>(v0) + static_cast<double>(v1) : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            d += __shfl_down_sync(0xffffffffu, d, o);
+        if ((threadIdx.x & 31) == 0)
+            red[threadIdx.x >> 5] = d;
+        __syncthreads();
+        // warps 0-1: pixels 0..127 of the CTA, warps 2-3: 128..255
+        if (threadIdx.x < 2)
+        {
+            const int pi = 2 * blockIdx.x + threadIdx.x;
+            if (pi < npartials)
+                partials[pi] = red[2 * threadIdx.x] + red[2 * threadIdx.x + 1];
+        }
+    }
+}
+
 int time_view_partials(int W, int H)
 {
     const size_t HW = static_cast<size_t>(W) * H;
@@ -323,6 +516,63 @@ hv_status time_view(const float2* ring, int T, int W, int H, const float2* weigh
     if (need <= 11)
         return launch_time_view<11>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
     return launch_time_view<16>(ring, T, W, H, weights, K, img_type, scale, shift, out, partials, st, ctl, bin_w);
+}
+
+template <int KC>
+static hv_status launch_time_view_planes(const uint16_t* planes, const float2* ring, int r0, int rn, int T, int W,
+                                         int H, const float2* weights, int K, int img_type, float scale, int shift,
+                                         float* out, double* partials, cudaStream_t st, const CycleCtl* ctl,
+                                         const float* bin_w)
+{
+    const size_t smem = static_cast<size_t>(T) * KC * sizeof(float2);
+    if (smem > 200 * 1024)
+    {
+        set_last_error_msg("time window too large for the time-view kernel");
+        return HV_ERR_UNSUPPORTED;
+    }
+    if (smem > 48 * 1024)
+        HV_CUDA_TRY(cudaFuncSetAttribute(k_time_view_planes<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem)));
+    const size_t HW = static_cast<size_t>(W) * H;
+    const int grid = static_cast<int>((HW + 2 * TV_THREADS - 1) / (2 * TV_THREADS));
+    k_time_view_planes<KC><<<grid, TV_THREADS, smem, st>>>(planes, ring, r0, rn, T, W, H, weights, K, img_type, scale,
+                                                           shift, out, partials, time_view_partials(W, H), ctl,
+                                                           bin_w);
+    HV_LAUNCH_CHECK();
+    count_launch();
+    return HV_OK;
+}
+
+hv_status time_view_planes(const uint16_t* planes, const float2* ring, int ring_slot0, int ring_n, int T, int W, int H,
+                           const float2* weights, int K, int img_type, float scale, int shift, float* out,
+                           double* partials, cudaStream_t st, const CycleCtl* ctl, const float* bin_w)
+{
+    if (T <= 0 || K <= 0 || W <= 0 || H <= 0 || ring_n < 0 || ring_n > T || ring_slot0 < 0 || ring_slot0 >= T)
+    {
+        set_last_error_msg("time_view_planes: bad sizes");
+        return HV_INVALID_VALUE;
+    }
+    if (shift && ((W & 1) || (H & 1)))
+    {
+        set_last_error_msg("fftshift needs even width and height");
+        return HV_INVALID_VALUE;
+    }
+    const size_t HW = static_cast<size_t>(W) * H;
+    if (HW % 8 != 0 || (reinterpret_cast<uintptr_t>(planes) & 15) != 0 ||
+        (ring_n > 0 && (reinterpret_cast<uintptr_t>(ring) & 15) != 0))
+    {
+        set_last_error_msg("time_view_planes: W x H must be a multiple of 8 and the planes and ring 16-byte aligned");
+        return HV_ERR_UNSUPPORTED;
+    }
+    // chunks of up to 4 bins (2 KC complex accumulators per thread)
+    if (K == 1)
+        return launch_time_view_planes<1>(planes, ring, ring_slot0, ring_n, T, W, H, weights, K, img_type, scale, shift,
+                                          out, partials, st, ctl, bin_w);
+    if (K == 2)
+        return launch_time_view_planes<2>(planes, ring, ring_slot0, ring_n, T, W, H, weights, K, img_type, scale, shift,
+                                          out, partials, st, ctl, bin_w);
+    return launch_time_view_planes<4>(planes, ring, ring_slot0, ring_n, T, W, H, weights, K, img_type, scale, shift,
+                                      out, partials, st, ctl, bin_w);
 }
 
 // ------------------------------------------------------------------------------ weights

@@ -310,6 +310,16 @@ hv_status hv_fft_cols(const void* in_c64, void* out_c64, int width, int height, 
 hv_status hv_time_view(const void* ring_c64, int T, int width, int height, const void* weights_c64, int K,
                        int img_type, float scale, int shift, float* out_f32, double* partials_f64, void* stream);
 int hv_time_view_partials(int width, int height);
+/* hv_time_view of a real ring (zero imaginary parts: frames converted without a spatial
+ * transform) from its split-BF16 planes (hv_pca_split_planes with real = 1: 4 bytes per sample
+ * against the ring's 8). The slots [ring_slot0, ring_slot0 + ring_n) mod T are read from the
+ * complex ring instead (ring_n = 0: the planes only, ring_c64 may be NULL): the pipe's slots that
+ * the next batch overwrites in the planes while the view may still run. The view values equal
+ * hv_time_view's on the ring for integer pixels below 2^16 (hi + lo is exact there); the partials
+ * are the same 128-pixel sums. width x height a multiple of 8. */
+hv_status hv_time_view_planes(const void* planes_u16, const void* ring_c64, int ring_slot0, int ring_n, int T,
+                              int width, int height, const void* weights_c64, int K, int img_type, float scale,
+                              int shift, float* out_f32, double* partials_f64, void* stream);
 /* hv_time_view on the tensor cores (tcgen05, split-BF16 with FP32 accumulation): the K-bin
  * contraction runs as a 128-pixel x 2K x 2T GEMM per pixel tile. K <= 64, width * height even
  * and at most 2^29, ring and work 16-byte aligned (HV_ERR_UNSUPPORTED otherwise: the ring is

@@ -75,3 +75,51 @@ def test_storage_order_quirk(cuda):
     for g, r in zip(outs, ref):
         assert np.abs(wrapped_diff(g, r)).max() < 1e-4
     assert np.abs(wrapped_diff(outs[0], outs[1])).max() > 0.1
+
+
+def _bf16_rn(x):
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32)
+    return ((u + (((u >> 16) & 1) + 0x7FFF)) >> 16).astype(np.uint16)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("T,K,slot0,n", [(256, 4, 64, 32), (256, 4, 240, 32), (512, 4, 0, 64), (128, 1, 0, 0),
+                                         (64, 2, 63, 1), (96, 6, 40, 96), (16, 4, 8, 8)])
+@pytest.mark.parametrize("img,shift", [(hv.IMG_SQUARED_MODULUS, 0), (hv.IMG_MODULUS, 1), (hv.IMG_ARGUMENT, 0)])
+def test_view_from_real_planes(cuda, T, K, slot0, n, img, shift):
+    """hv_time_view_planes on the real split planes of an integer ring (frames converted without a
+    spatial transform), with the slots [slot0, slot0 + n) mod T read from the ring: the same view
+    values as hv_time_view on the ring (bit for bit) and the same 128-pixel partial sums. Random
+    complex weights (eigenvector-like); W x H a multiple of 8 but not of 128 (a partial last
+    renormalisation group). K > 4 runs in chunks of 4 bins there and in one chunk on the ring:
+    within 1e-6."""
+    H, W = 24, 44
+    rng = np.random.default_rng(T + K + slot0)
+    ring = np.zeros((T, H, W), np.complex64)
+    ring.real = rng.integers(0, 65536, size=(T, H, W)).astype(np.float32)
+    w = ((rng.standard_normal((K, T)) + 1j * rng.standard_normal((K, T))) / np.sqrt(T)).astype(np.complex64)
+    rd, wd = dev(ring), dev(w)
+    # the split on the host: hi = bf16(x), lo = bf16(x - hi), round to nearest even; [2][T][HW]
+    x = ring.real.reshape(T, H * W)
+    hi = _bf16_rn(x)
+    lo = _bf16_rn(x - (hi.astype(np.uint32) << 16).view(np.float32))
+    host_planes = np.stack([hi, lo])
+    planes = dev(host_planes)
+    if 2 * T > 128:  # the device split (the pipe's) writes the same planes
+        dp = empty(hv.lib().hv_pca_planes_bytes(T, H * W, 1))
+        call("hv_pca_split_planes", ptr(rd), T, H * W, 0, T, 1, ptr(dp), None)
+        assert np.array_equal(host(dp, np.uint16, host_planes.shape), host_planes)
+    npart = hv.lib().hv_time_view_partials(W, H)
+    outs, parts = [], []
+    for fn, args in (("hv_time_view", (ptr(rd), T)), ("hv_time_view_planes", (ptr(planes), ptr(rd), slot0, n, T))):
+        out, part = empty(H * W * 4), empty(npart * 8)
+        call(fn, *args, W, H, ptr(wd), K, img, 131071.0, shift, ptr(out), ptr(part), None)
+        outs.append(host(out, np.float32, (H, W)))
+        parts.append(host(part, np.float64, (npart,)))
+    assert np.isfinite(outs[0]).all()
+    if K <= 4:  # both two-pixel kernels, one chunk of bins: bit for bit
+        assert np.array_equal(outs[0], outs[1])
+        np.testing.assert_allclose(parts[1], parts[0], rtol=1e-12, atol=0)
+    else:  # chunks of 4 against one of 6: the compiler may contract the bin sums differently
+        np.testing.assert_allclose(outs[1], outs[0], rtol=1e-6, atol=0)
+        np.testing.assert_allclose(parts[1], parts[0], rtol=1e-6, atol=0)
