@@ -267,6 +267,7 @@ def _declare(L: C.CDLL) -> None:
         "hv_pca_eigh": (st, [vp, i32, vp, vp, i32, i32, vp, vp, vp]),
         "hv_pca_eigh_workspace": (sz, [i32]),
         "hv_pca_eig_precision": (None, [i32]),
+        "hv_pca_eig_cholqr": (None, [i32]),
         "hv_unwrap_2d": (st, [vp, vp, i32, i32, vp, vp]),
         "hv_unwrap_workspace": (sz, [i32, i32]),
         "hv_unwrap_2d_noalloc": (st, [vp, vp, i32, i32, vp]),

@@ -358,6 +358,8 @@ size_t hv_pca_eigh_workspace(int T) { return pca_eigh_workspace(T); }
 
 void hv_pca_eig_precision(int precision) { set_eig_precision(precision == HV_EIG_FP64 ? HV_EIG_FP64 : HV_EIG_FP32); }
 
+void hv_pca_eig_cholqr(int enable) { set_eig_cholqr(enable); }
+
 hv_status hv_unwrap_2d(const float* in, float* out, int width, int height, void* work, void* stream)
 {
     if (!in || !out || !work)

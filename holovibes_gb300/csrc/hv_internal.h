@@ -124,6 +124,9 @@ hv_status pca_covariance_planes(const uint16_t* planes, int T, size_t npix, doub
                                 int real, cudaStream_t st);
 size_t pca_eigh_workspace(int T);
 void set_eig_precision(int p);
+// 1 (default): the warm subspace iteration orthonormalises by Cholesky-QR (Gram-Schmidt when its
+// factorisation fails); 0: Gram-Schmidt always.
+void set_eig_cholqr(int on);
 // Eigenvectors of ranks refine_lo..refine_hi (at most 64 of them) are refined in FP64 after FP32
 // sweeps; an empty range (refine_hi < refine_lo) keeps the FP32 vectors. `warm`: `work` holds the
 // eigenvectors of the previous successful call with the same T (a window of the same stream), from

@@ -2305,8 +2305,11 @@ __device__ __forceinline__ float ts_project(float2 (&y)[TS_ORTH_RPT][TS_P], floa
 // always register slot 0 and the slots rotate by one after every column, so that registers are
 // indexed by constants only. A column left without norm (Y of rank < TS_P) becomes the unit vector
 // e_k, made orthogonal at the next iteration.
-__global__ void __launch_bounds__(TS_ORTH_THREADS) k_ts_orth(const float2* __restrict__ Y, int T, float2* __restrict__ V)
+__global__ void __launch_bounds__(TS_ORTH_THREADS) k_ts_orth(const float2* __restrict__ Y, int T, float2* __restrict__ V,
+                                                              const int* __restrict__ only_if = nullptr)
 {
+    if (only_if && *only_if == 0)  // the Cholesky-QR of the warm iteration succeeded
+        return;
     __shared__ float2 red[2][TS_ORTH_THREADS / 32][TS_P];
     __shared__ float red1[2][TS_ORTH_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -2373,6 +2376,86 @@ __global__ void __launch_bounds__(TS_ORTH_THREADS) k_ts_orth(const float2* __res
                 V[static_cast<size_t>(t) * TS_P + (TS_P - 1 - j)] = y[r][j];
         }
     }
+}
+
+// The warm iteration's V = orth(Y) as a Cholesky-QR: with G = Y^H Y (k_ts_gram) and D = diag(G)^-1/2,
+// G' = D G D = L L^H and V = Y D L^-H (V^H V = L^-1 G' L^-H = I); k_ts_ritz applies M = D L^-H.
+// The Cholesky runs from the last column down (the largest Ritz value of the warm start, as in
+// k_ts_orth), so V's last column is Y's last column normalised and column j spans the columns
+// j .. TS_P - 1 of Y. The warm start's C V has near-orthogonal columns (the previous window's Ritz
+// vectors times a covariance that changed by one stride), so G' is near the identity and the FP32
+// factorisation is well conditioned. A pivot below 1e-6 (Y of rank < TS_P, or columns too close to
+// dependent) sets *fail and k_ts_orth recomputes V by Gram-Schmidt. One warp.
+__global__ void __launch_bounds__(32) k_ts_cholqr(const float2* __restrict__ G, float2* __restrict__ M,
+                                                  int* __restrict__ fail)
+{
+    __shared__ float2 L[TS_P][TS_P + 1];  // index a = TS_P - 1 - (column of Y); lower triangle = L
+    __shared__ float2 X[TS_P][TS_P + 1];  // L^-1
+    __shared__ float d[TS_P];
+    const int lane = threadIdx.x;
+    {
+        const float g = G[(TS_P - 1 - lane) * TS_P + (TS_P - 1 - lane)].x;
+        d[lane] = (g > 0.f && isfinite(g)) ? rsqrtf(g) : 0.f;
+    }
+    __syncwarp();
+    for (int a = 0; a < TS_P; ++a)
+    {
+        const float2 v = G[(TS_P - 1 - a) * TS_P + (TS_P - 1 - lane)];
+        const float sc = d[a] * d[lane];
+        L[a][lane] = make_float2(v.x * sc, v.y * sc);
+    }
+    __syncwarp();
+    bool ok = true;
+    for (int j = 0; j < TS_P; ++j)
+    {
+        // every lane forms the same pivot from the same (broadcast) values
+        float p = L[j][j].x;
+        for (int k = 0; k < j; ++k)
+        {
+            const float2 l = L[j][k];
+            p -= l.x * l.x + l.y * l.y;
+        }
+        ok = ok && p > 1e-6f && isfinite(p);
+        const float ljj = sqrtf(fmaxf(p, 1e-6f));
+        __syncwarp();
+        if (lane > j)
+        {
+            float2 a = L[lane][j];
+            for (int k = 0; k < j; ++k)
+            {
+                const float2 li = L[lane][k], lj = L[j][k];  // a -= li conj(lj)
+                a.x -= li.x * lj.x + li.y * lj.y;
+                a.y -= li.y * lj.x - li.x * lj.y;
+            }
+            L[lane][j] = make_float2(a.x / ljj, a.y / ljj);
+        }
+        if (lane == 0)
+            L[j][j] = make_float2(ljj, 0.f);
+        __syncwarp();
+    }
+    // X = L^-1 by forward substitution, lane = column
+    for (int i = 0; i < TS_P; ++i)
+    {
+        float2 a = make_float2(i == lane ? 1.f : 0.f, 0.f);
+        for (int k = 0; k < i; ++k)
+        {
+            const float2 l = L[i][k], x = X[k][lane];
+            a.x -= l.x * x.x - l.y * x.y;
+            a.y -= l.x * x.y + l.y * x.x;
+        }
+        const float inv = 1.f / L[i][i].x;
+        X[i][lane] = make_float2(a.x * inv, a.y * inv);
+    }
+    __syncwarp();
+    // M[k][r] (Y column k into V column r) = d_k conj(X[b][a]) with a = TS_P-1-k, b = TS_P-1-r, a <= b
+    for (int k = 0; k < TS_P; ++k)
+    {
+        const int a = TS_P - 1 - k, b = TS_P - 1 - lane;
+        const float2 x = X[b][a];
+        M[k * TS_P + lane] = a <= b ? make_float2(d[a] * x.x, -d[a] * x.y) : make_float2(0.f, 0.f);
+    }
+    if (lane == 0)
+        *fail = ok ? 0 : 1;
 }
 
 // Rayleigh-Ritz in three launches. k_ts_gram: H = V^H Y (Y = C32 V), one CTA per row i of H, warp w
@@ -2475,8 +2558,9 @@ __global__ void __launch_bounds__(JS_THREADS) k_ts_rr(const float2* __restrict__
 }
 
 // k_ts_ritz: the Ritz vectors U = V Qo, TS_P rows of U per CTA (warp w: rows w, w + 8, ..., lane =
-// column r): into the warm start Vw (row-major) and evecs columns T - TS_P + r (FP64, through a
-// shared-memory transpose so that each eigenvector's rows are written contiguously)
+// column r): into the warm start Vw (row-major) and, when evecs is not null, evecs columns
+// T - TS_P + r (FP64, through a shared-memory transpose so that each eigenvector's rows are written
+// contiguously). Also the Cholesky-QR's V = Y M (evecs null).
 __global__ void __launch_bounds__(256) k_ts_ritz(const float2* __restrict__ V, const float2* __restrict__ Qo, int T,
                                                  double2* __restrict__ evecs, float2* __restrict__ Vw)
 {
@@ -2506,7 +2590,7 @@ __global__ void __launch_bounds__(256) k_ts_ritz(const float2* __restrict__ V, c
         Vw[static_cast<size_t>(t) * TS_P + lane] = make_float2(re, im);
     }
     __syncthreads();
-    if (t0 + lane < T)
+    if (evecs && t0 + lane < T)
         for (int r = warp; r < TS_P; r += 8)
         {
             const float2 x = u[lane][r];
@@ -2515,6 +2599,10 @@ __global__ void __launch_bounds__(256) k_ts_ritz(const float2* __restrict__ V, c
 }
 
 static std::atomic<int> g_eig_precision{HV_EIG_FP32};
+static std::atomic<int> g_cholqr{1};
+
+void set_eig_cholqr(int on) { g_cholqr = on ? 1 : 0; }
+static bool cholqr_enabled() { return g_cholqr.load() != 0; }
 
 void set_eig_precision(int p) { g_eig_precision = p; }
 
@@ -2622,12 +2710,30 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
             HV_LAUNCH_CHECK();
         }
         const int iters = warm ? TS_ITERS_WARM : TS_ITERS_COLD;
+        int* chol_fail = reinterpret_cast<int*>(scale + 1);
+        int extra = 0;
         for (int it = 0; it < iters; ++it)
         {
             k_ts_matmul<<<gm, mm_threads, 0, st>>>(C32, it == 0 && warm ? Vw : Vs, T, Ys);
             HV_LAUNCH_CHECK();
-            k_ts_orth<<<1, TS_ORTH_THREADS, 0, st>>>(Ys, T, Vs);
-            HV_LAUNCH_CHECK();
+            if (warm && cholqr_enabled())
+            {
+                // Cholesky-QR (Gram, 32 x 32 factorisation, V = Y M), Gram-Schmidt only if it failed
+                k_ts_gram<<<TS_P, TS_GRAM_WARPS * 32, 0, st>>>(Ys, Ys, T, Hm);
+                HV_LAUNCH_CHECK();
+                k_ts_cholqr<<<1, 32, 0, st>>>(Hm, Qo, chol_fail);
+                HV_LAUNCH_CHECK();
+                k_ts_ritz<<<(T + TS_P - 1) / TS_P, 256, 0, st>>>(Ys, Qo, T, nullptr, Vs);
+                HV_LAUNCH_CHECK();
+                k_ts_orth<<<1, TS_ORTH_THREADS, 0, st>>>(Ys, T, Vs, chol_fail);
+                HV_LAUNCH_CHECK();
+                extra += 3;
+            }
+            else
+            {
+                k_ts_orth<<<1, TS_ORTH_THREADS, 0, st>>>(Ys, T, Vs);
+                HV_LAUNCH_CHECK();
+            }
         }
         k_ts_matmul<<<gm, mm_threads, 0, st>>>(C32, Vs, T, Ys);
         HV_LAUNCH_CHECK();
@@ -2637,7 +2743,7 @@ hv_status pca_eigh(double2* cov, int T, double* evals, double2* evecs, int pmin,
         HV_LAUNCH_CHECK();
         k_ts_ritz<<<(T + TS_P - 1) / TS_P, 256, 0, st>>>(Vs, Qo, T, evecs, Vw);
         HV_LAUNCH_CHECK();
-        count_launch(5 + 2 * iters + (warm ? 0 : 2));
+        count_launch(5 + 2 * iters + extra + (warm ? 0 : 2));
         // two corrections: on 512 x 512 frames with T = 512 and stride 64, one warm iteration and two
         // corrections reach the view error of three and three (3.5e-7 .. 1.9e-6 from FP64)
         return refine_kept(T - TS_P, 2);

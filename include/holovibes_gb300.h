@@ -446,6 +446,11 @@ size_t hv_pca_eigh_workspace(int T);
  * against 0.24 and 1.6 ms). HV_EIG_FP64, and any T above 512: the sweeps themselves in FP64. */
 enum { HV_EIG_FP32 = 0, HV_EIG_FP64 = 1 };
 void hv_pca_eig_precision(int precision);
+/* Orthonormalisation of the warm subspace iteration (T > 64, dominant components): 1 (default) a
+ * Cholesky-QR of the iterate (its Gram matrix, a 32 x 32 factorisation, one product), with the
+ * Gram-Schmidt kernel run instead when the factorisation meets a pivot below 1e-6; 0 Gram-Schmidt
+ * always. Both span the same subspace; the Ritz pairs agree to FP32 round-off. */
+void hv_pca_eig_cholqr(int enable);
 
 /* 2-D phase unwrap of a float phase image, then rescale to [0, 65535]. Replaces unwrap_2d +
  * rescale_float_unwrap2d (tools_unwrap.cu:269-369, tools_conversion.cu:315-335). `work` must hold

@@ -74,13 +74,14 @@ def test_covariance_and_eigh(cuda, T, H, W):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("T,img", [(32, 0), (64, 1), (16, 0), (128, 0), (256, 1)])
-def test_pipe_pca_windows_warm_start(cuda, T, img):
+@pytest.mark.parametrize("T,img,cholqr", [(32, 0, 1), (64, 1, 1), (16, 0, 1), (128, 0, 1), (256, 1, 1), (128, 0, 0),
+                                         (256, 1, 0)])
+def test_pipe_pca_windows_warm_start(cuda, T, img, cholqr):
     """Consecutive PCA windows of one Pipe: from the second window on, the eigensolve starts from
     the previous window's eigenvectors (T <= 64: the FP32 Jacobi sweeps; T > 64 with the dominant
-    components kept: the subspace iteration from the previous Ritz vectors). Every window's float
-    frame within rel-L2 1e-4 of the oracle (modulus views depend on each kept eigenvector, not only
-    on the kept subspace)."""
+    components kept: the subspace iteration from the previous Ritz vectors, orthonormalised by
+    Cholesky-QR, or by Gram-Schmidt with cholqr = 0). Every window's float frame within rel-L2 1e-4
+    of the oracle (modulus views depend on each kept eigenvector, not only on the kept subspace)."""
     from gpu_util import oracle_settings
 
     from holovibes_gb300.synthetic import Interferogram
@@ -93,17 +94,21 @@ def test_pipe_pca_windows_warm_start(cuda, T, img):
                                       contrast_enabled=0).validate(fd)
     raw = Interferogram(width=W, height=H, seed=T + img, modes=8).frames(0, 6 * T // 2)
     oracle = O.OraclePipe(oracle_settings(fd, s))
-    pipe = hv.Pipe(fd, s)
-    errs = []
-    for b in range(6):
-        batch = raw[b * (T // 2):(b + 1) * (T // 2)]
-        ref = oracle.process_batch(batch)
-        pipe.enqueue(batch)
-        if ref is None:
-            continue
-        pipe.pull()
-        errs.append(rel_l2(pipe.float_frame(), ref.float_frame))
-    pipe.close()
+    hv.lib().hv_pca_eig_cholqr(cholqr)
+    try:
+        pipe = hv.Pipe(fd, s)
+        errs = []
+        for b in range(6):
+            batch = raw[b * (T // 2):(b + 1) * (T // 2)]
+            ref = oracle.process_batch(batch)
+            pipe.enqueue(batch)
+            if ref is None:
+                continue
+            pipe.pull()
+            errs.append(rel_l2(pipe.float_frame(), ref.float_frame))
+        pipe.close()
+    finally:
+        hv.lib().hv_pca_eig_cholqr(1)
     assert len(errs) == 5
     assert max(errs) <= 1e-4, errs
 
