@@ -1853,7 +1853,10 @@ hv_status convert_to_planes(const void* raw, int kind, size_t HW, int batch, int
     const FrameMap map{HW, slot0, T};
     const size_t total = HW / 8 * batch;
     const int block = 256;
-    const int grid = static_cast<int>((total + block - 1) / block < 152 * 8 ? (total + block - 1) / block : 152 * 8);
+    // three quarters of the SMs' thread slots: the pipelined windows' eigensolve kernels (another
+    // stream) find room beside this pass
+    const int cap = device_sms() * 6;
+    const int grid = static_cast<int>((total + block - 1) / block < static_cast<size_t>(cap) ? (total + block - 1) / block : cap);
     k_convert8<<<grid, block, 0, st>>>(raw, kind, HW, batch, nullptr, map, nullptr, planes);
     HV_LAUNCH_CHECK();
     count_launch();
@@ -1866,7 +1869,8 @@ hv_status ring_from_planes(const uint16_t* planes, int T, size_t HW, int slot0, 
         return n <= 0 ? HV_OK : HV_ERR_UNSUPPORTED;
     const size_t total = HW / 8 * n;
     const int block = 256;
-    const int grid = static_cast<int>((total + block - 1) / block < 152 * 8 ? (total + block - 1) / block : 152 * 8);
+    const int cap = device_sms() * 6;  // as convert_to_planes: room for the eigensolve stream's kernels
+    const int grid = static_cast<int>((total + block - 1) / block < static_cast<size_t>(cap) ? (total + block - 1) / block : cap);
     k_ring_from_planes<<<grid, block, 0, st>>>(planes, T, HW, slot0, n, ring);
     HV_LAUNCH_CHECK();
     count_launch();

@@ -280,7 +280,7 @@ __device__ __forceinline__ void tvp_planes(float2 (&a)[2][KC], const uint32_t* _
                                            const uint32_t* __restrict__ lo, size_t step, int t0, int t1,
                                            const float2* wsm)
 {
-    constexpr int D = 16;  // frames whose loads are issued before the first is used
+    constexpr int D = 12;  // frames whose loads are issued before the first is used
     int t = t0;
     for (; t + D <= t1; t += D)
     {
@@ -326,9 +326,10 @@ __device__ __forceinline__ void tvp_ring(float2 (&a)[2][KC], const float4* __res
 // [r0, r0 + rn) mod T are read from the complex ring instead (the slots that the next batch's
 // planes overwrite while this view may still run). Two adjacent pixels per thread, 128 threads
 // cover 256 pixels and write their two 128-pixel renormalisation partials (those of k_time_view).
-// The view values equal k_time_view's on the same ring.
+// The view values equal k_time_view's on the same ring. 64 registers: the grid leaves a CTA slot
+// free on most SMs for the pipelined windows' eigensolve kernels (another stream).
 template <int KC>
-__global__ void __launch_bounds__(TV_THREADS, 7) k_time_view_planes(const uint16_t* __restrict__ planes,
+__global__ void __launch_bounds__(TV_THREADS, 8) k_time_view_planes(const uint16_t* __restrict__ planes,
                                                                  const float2* __restrict__ ring, int r0, int rn, int T,
                                                                  int W, int H, const float2* __restrict__ weights,
                                                                  int K, int img_type, float scale, int shift,
